@@ -1,0 +1,203 @@
+/*
+ * phx.h -- C ABI of the GB300-native tet-FEM Newton path.
+ *
+ * The library replaces PhySim's CPU hot path for nonlinear tetrahedral FEM:
+ * per-tet energy / gradient / Hessian, global assembly, and the Newton solver
+ * with its linear solve and backtracking line search.  Everything runs on one
+ * GPU (sm_103a); these entry points take plain host pointers and sizes.
+ *
+ * Conventions
+ *  - Every call returns an int status: PHX_OK (0) or a negative PHX_E* code.
+ *    No C++ exception crosses this boundary.  phx_last_error() gives a message.
+ *  - Host buffers are caller owned; device state is library owned.
+ *  - All calls are synchronous and thread-compatible: one context per host
+ *    thread; a context and its instances must not be used from two threads at once.
+ *  - DoF layout: DoF d of node v is 3*v + d (KinematicsTree offsets,
+ *    source/PhySim/Kinematics/KinematicsTree.cpp:25-40).
+ */
+#ifndef PHX_H
+#define PHX_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define PHX_OK 0
+#define PHX_EINVAL (-1)   /* invalid argument or malformed mesh */
+#define PHX_ENOMEM (-2)   /* device arena exhausted / admission refused */
+#define PHX_ETIMEOUT (-3) /* a bounded device wait gave up */
+#define PHX_ECUDA (-4)    /* CUDA runtime error */
+#define PHX_EBUSY (-5)    /* object in use (e.g. instance already admitted) */
+#define PHX_ENOTFOUND (-6)
+
+/* OSResult (include/PhySim/BasicTypes.h:69-77), same numbering */
+#define PHX_OS_ONGOING 0
+#define PHX_OS_SUCCESS 1
+#define PHX_OS_MINSTEP 2
+#define PHX_OS_MINIMPR 3
+#define PHX_OS_FAILURE 4
+#define PHX_OS_MAXITER 5
+#define PHX_OS_NONDESC 6
+
+/* LSResult (include/PhySim/BasicTypes.h:61-67) */
+#define PHX_LS_SUCCESS 0
+#define PHX_LS_FAILURE 1
+
+/* material models (MaterialModel_3Din3D_CoNH / _StVK, MaterialModels.h:166-299) */
+#define PHX_MODEL_CONH 0
+#define PHX_MODEL_STVK 1
+
+/* arithmetic of the Hessian, element-Hessian kernel and PCG */
+#define PHX_PREC_FP64 0         /* plain path: FP64 everywhere */
+#define PHX_PREC_FP32_REFINE 1  /* served path: FP32 Hessian + PCG, FP64 residual refinement */
+
+typedef struct phx_context_s* phx_context;
+typedef struct phx_instance_s* phx_instance;
+
+/* One FEM volume (Simulable_FEM + its boundary conditions).  Replaces the
+ * model set-up path Simulable::Setup (source/PhySim/Physics/Simulables/Simulable.cpp:73-106)
+ * with Tet4 shape functions and the Tet1 quadrature. */
+typedef struct phx_mesh {
+  int32_t num_nodes;
+  int32_t num_tets;
+  const double* X0;       /* [3*num_nodes] rest positions (Tag::Position_0) */
+  const int32_t* tets;    /* [4*num_tets] node ids, positive rest volume required */
+  const double* lame;     /* [2*num_tets] (LAME1 = lambda, LAME2 = mu) per tet */
+  const double* rho;      /* [num_tets] density per tet (lumped mass) */
+  const uint8_t* model;   /* [num_tets] PHX_MODEL_*; NULL = all CoNH */
+  const uint8_t* fixed;   /* [3*num_nodes] hard-fixed DoFs (BC_FixDoF hard mode); NULL = none */
+  const double* force;    /* [3*num_nodes] EnergyElement_Force f (energy x.f); NULL = none */
+  double gravity[3];      /* BC_Gravity value */
+} phx_mesh;
+
+/* Mirrors OptimSolverOptions (include/PhySim/Solvers/OptimSolver.h:47-70)
+ * field for field, plus the GPU-path settings at the end. */
+typedef struct phx_options {
+  int32_t qp_solver;          /* 0 Steepest, 1 Newton (QPSolverType) */
+  double tol_max_error;       /* absolute ||g|| */
+  double tol_min_step;
+  int32_t min_step_max_count;
+  double tol_min_impr;
+  int32_t min_impr_max_count;
+  int32_t num_max_iters;
+  int32_t try_steepest;
+  double max_step_size;
+  int32_t ls_solver;          /* 1 EigenCG semantics (the only linear solver on the device) */
+  int32_t ls_num_max_iters;   /* PCG iterations per linear solve */
+  double ls_tol_max_error;    /* PCG relative residual ||r|| < tol ||b|| */
+  int32_t ls_num_reg_trials;
+  int32_t lsearch_type;       /* 1 Simple */
+  double lsearch_alpha;
+  int32_t lsearch_num_try;
+  /* GPU path */
+  int32_t precision;          /* PHX_PREC_* */
+  int32_t precond;            /* 0 diagonal (Eigen DiagonalPreconditioner), 1 3x3 block Jacobi */
+  double inner_tol;           /* FP32 inner PCG relative tolerance per refinement sweep */
+  int32_t max_refine_sweeps;  /* FP64 refinement sweeps per linear solve (FP32 path) */
+  int32_t warm_guess;         /* 1: PCG starts from the previous accepted step (EigenCG solveWithGuess) */
+  int32_t pcg_chunk;          /* PCG iterations per device round (launch granularity) */
+} phx_options;
+
+typedef struct phx_report {
+  int32_t result;           /* PHX_OS_* */
+  int32_t iterations;       /* Newton iterations (SolveFull itCount) */
+  int32_t bisections;       /* line-search bisections summed */
+  int32_t reg_trials;       /* regularised linear solves */
+  int64_t pcg_iterations;   /* PCG iterations summed */
+  int32_t refine_sweeps;    /* FP64 residual refinement sweeps summed */
+  int32_t status;           /* PHX_OK or a device-side error code */
+  double obj;               /* final energy */
+  double opt;               /* final ||g|| */
+  double opt0;              /* ||g|| at the first step (after the loads are applied) */
+  double seconds;           /* wall time of the call */
+} phx_report;
+
+/* ---- library ----------------------------------------------------------- */
+int phx_version(void);
+const char* phx_last_error(void);
+void phx_default_options(phx_options* opts);
+
+/* ---- context: one device, one stream, one device-memory arena ----------
+ * arena_bytes = 0 picks a default (a quarter of free device memory). */
+int phx_context_create(int32_t device, int64_t arena_bytes, phx_context* out);
+int phx_context_destroy(phx_context ctx);
+int phx_context_memory(phx_context ctx, int64_t* used_bytes, int64_t* capacity_bytes);
+
+/* ---- instances: Simulable_FEM set-up (replaces Simulable::Setup + the first
+ * triplet assembly that fixes the Hessian pattern, source/PhySim/BasicTypes.cpp:118-145).
+ * Validates the mesh (PHX_EINVAL on bad ids or non-positive rest volume),
+ * builds the 3x3 block pattern and the scatter map, uploads everything. */
+int phx_instance_create(phx_context ctx, const phx_mesh* mesh, phx_instance* out);
+int phx_instance_destroy(phx_instance inst);
+int phx_instance_sizes(phx_instance inst, int64_t* num_dofs, int64_t* hessian_nnz,
+                       int64_t* lower_blocks, int64_t* full_blocks);
+/* Model state (ISimulable::Get/SetDOFVector, Tag::Position_X / Tag::Velocity, Simulable.h:55-94) */
+int phx_instance_set_positions(phx_instance inst, const double* x);
+int phx_instance_get_positions(phx_instance inst, double* x);
+int phx_instance_set_velocities(phx_instance inst, const double* v);
+int phx_instance_get_velocities(phx_instance inst, double* v);
+/* Replace the nodal loads (EnergyElement_Force f, BC_Gravity g) of a live instance; warm re-solves. */
+int phx_instance_update_load(phx_instance inst, const double* force, const double* gravity);
+
+/* ---- model evaluation (ISimulable::GetEnergy / GetGradient / GetHessian) --- */
+/* Energy and gradient at x[3n] (x == NULL: current positions).  fix != 0 applies
+ * FixVectorDoFs (Simulable.cpp:735-744). */
+int phx_energy_gradient(phx_instance inst, const double* x, double* energy, double* gradient, int32_t fix);
+/* Hessian values on the Eigen lower pattern (diagonal 3x3 node blocks in full),
+ * column-major like MatrixSd; fix != 0 applies FixMatrixDoFs (Simulable.cpp:746-760). */
+int phx_hessian(phx_instance inst, const double* x, int32_t precision, double* values, int32_t fix);
+int phx_hessian_pattern(phx_instance inst, int32_t* colptr /* 3n+1 */, int32_t* rowidx /* nnz */);
+/* Lower-block slot of the 10 local node pairs (0,0),(1,0),(1,1),(2,0),(2,1),(2,2),(3,0),...,(3,3)
+ * of every tet, blocks counted column-major over the pattern (DerivativeAssembler.cpp:205-300). */
+int phx_scatter_map(phx_instance inst, int32_t* map /* 10*num_tets */);
+/* Per-element values (IEnergyElement::GetLocal*, EnergyElement_FEM.cpp:125-222):
+ * E[m], g[12m], H[144m] row-major 12x12; any output may be NULL. */
+int phx_element_local(phx_instance inst, const double* x, int32_t precision, double* E, double* g, double* H);
+
+/* ---- solver (IOptimSolver::SolveFull / SolveStep, OptimSolver.cpp:148-311,
+ * on OptimProblem_BasicStatic / OptimProblem_BasicDynamic) -------------- */
+/* Static equilibrium from x_inout (NULL: from the instance's current positions). */
+int phx_solve_static(phx_instance inst, const phx_options* opts, double* x_inout, phx_report* rep);
+/* One SolveStep (a single Newton iteration with its line search). */
+int phx_solve_step(phx_instance inst, const phx_options* opts, double* x_inout, phx_report* rep);
+/* One implicit-Euler step: minimises the incremental potential (OptimProblem_BasicDynamic). */
+int phx_dynamic_step(phx_instance inst, const phx_options* opts, double dt, double* x_inout,
+                     double* v_inout, phx_report* rep);
+/* Many independent static solves in one device batch (persistent kernels over a
+ * packed instance index).  x_inout[i] may be NULL; reps has count entries. */
+int phx_batch_solve(phx_context ctx, int32_t count, phx_instance* insts, const phx_options* opts,
+                    double* const* x_inout, phx_report* reps);
+/* Batched implicit-Euler steps (one per instance). */
+int phx_batch_dynamic_step(phx_context ctx, int32_t count, phx_instance* insts, const phx_options* opts,
+                           double dt, phx_report* reps);
+
+/* ---- serving: continuous batching over the same device engine ----------
+ * Requests are admitted at Newton-iteration boundaries while the device is
+ * busy with others, bounded by free slots and the memory budget. */
+typedef struct phx_server_s* phx_server;
+int phx_server_create(phx_context ctx, int32_t max_slots, int64_t budget_bytes, const phx_options* opts,
+                      phx_server* out);
+int phx_server_destroy(phx_server srv);
+/* Queue a static solve of inst (from its current positions); tag is returned by poll. */
+int phx_server_submit(phx_server srv, phx_instance inst, int64_t tag);
+/* Advance the device by one round; admits queued requests first. */
+int phx_server_progress(phx_server srv, int32_t* active, int32_t* queued);
+/* Pop up to cap finished requests: tags, reports. Returns the number popped (>= 0) or an error. */
+int phx_server_poll(phx_server srv, int64_t* tags, phx_report* reps, int32_t cap);
+
+/* ---- measurement hooks ------------------------------------------------- */
+/* Kernel timing with CUDA events on the library's stream; kind names:
+ * "elem_eg", "gather", "elem_hess", "assemble", "jacobi", "spmv", "pcg_update", ... */
+int phx_profile_enable(phx_context ctx, int32_t on);
+int phx_profile_read(phx_context ctx, const char* kind, int64_t* launches, double* total_ms);
+int phx_profile_reset(phx_context ctx);
+/* Launch count of the library's own kernels since creation (or the last reset). */
+int64_t phx_kernel_launches(phx_context ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PHX_H */

@@ -1,0 +1,212 @@
+"""ctypes binding of the CPU oracle (test infrastructure only).
+
+The oracle restates PhySim's CPU tet-FEM Newton path (see phx_oracle.cpp for
+the reference file:line each part follows).  Only tests/, the smoke check and
+the benchmark's CPU-baseline leg import this package; the product path never
+does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+_ref = None
+
+OS_NAMES = {0: "ONGOING", 1: "SUCCESS", 2: "MINSTEP", 3: "MINIMPR", 4: "FAILURE", 5: "MAXITER", 6: "NONDESC"}
+
+
+class OrcMesh(C.Structure):
+    _fields_ = [("n", C.c_int32), ("m", C.c_int32), ("X0", C.c_void_p), ("T", C.c_void_p),
+                ("lame", C.c_void_p), ("rho", C.c_void_p), ("model", C.c_void_p),
+                ("fixed", C.c_void_p), ("force", C.c_void_p), ("gravity", C.c_double * 3)]
+
+
+class OrcOptions(C.Structure):
+    _fields_ = [("qp_solver", C.c_int32), ("tol_max_error", C.c_double), ("tol_min_step", C.c_double),
+                ("min_step_max_count", C.c_int32), ("tol_min_impr", C.c_double),
+                ("min_impr_max_count", C.c_int32), ("num_max_iters", C.c_int32),
+                ("try_steepest", C.c_int32), ("max_step_size", C.c_double), ("ls_solver", C.c_int32),
+                ("ls_num_max_iters", C.c_int32), ("ls_tol_max_error", C.c_double),
+                ("ls_num_reg_trials", C.c_int32), ("lsearch_type", C.c_int32),
+                ("lsearch_alpha", C.c_double), ("lsearch_num_try", C.c_int32),
+                ("cg_block_jacobi", C.c_int32), ("threads", C.c_int32)]
+
+
+class OrcReport(C.Structure):
+    _fields_ = [("result", C.c_int32), ("iterations", C.c_int32), ("bisections", C.c_int32),
+                ("reg_trials", C.c_int32), ("lin_iterations", C.c_int64), ("obj", C.c_double),
+                ("opt", C.c_double), ("opt0", C.c_double), ("seconds", C.c_double),
+                ("t_cal_ene", C.c_double), ("t_cal_gra", C.c_double), ("t_cal_hes", C.c_double),
+                ("t_ass_gra", C.c_double), ("t_ass_hes", C.c_double), ("t_opt_sol", C.c_double),
+                ("t_opt_lis", C.c_double)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["result_name"] = OS_NAMES.get(self.result, str(self.result))
+        return d
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        L = C.CDLL(path)
+        vp = C.c_void_p
+        L.orc_create.argtypes = [C.POINTER(OrcMesh), C.POINTER(vp)]
+        L.orc_destroy.argtypes = [vp]
+        L.orc_default_options.argtypes = [C.POINTER(OrcOptions)]
+        L.orc_element_local.argtypes = [vp, vp, vp, vp, vp]
+        L.orc_material.argtypes = [C.c_int, C.c_double, C.c_double, vp, vp, vp, vp]
+        L.orc_energy.argtypes = [vp, vp, C.POINTER(C.c_double)]
+        L.orc_gradient.argtypes = [vp, vp, vp, C.c_int]
+        L.orc_hessian_nnz.argtypes = [vp]
+        L.orc_hessian_nnz.restype = C.c_int64
+        L.orc_hessian_pattern.argtypes = [vp, vp, vp]
+        L.orc_hessian.argtypes = [vp, vp, vp, C.c_int]
+        L.orc_scatter_map.argtypes = [vp, vp]
+        L.orc_solve_static.argtypes = [vp, C.POINTER(OrcOptions), vp, C.POINTER(OrcReport)]
+        L.orc_solve_dynamic.argtypes = [vp, C.POINTER(OrcOptions), C.c_double, vp, vp, C.POINTER(OrcReport)]
+        L.orc_linear_solve.argtypes = [vp, C.POINTER(OrcOptions), vp, vp, vp, C.POINTER(C.c_int32),
+                                       C.POINTER(C.c_int64)]
+        L.orc_last_log.argtypes = [vp, vp, vp, vp, vp, C.c_int32]
+        _lib = L
+    return _lib
+
+
+def ref_lib():
+    """The reference's own .mcg material code, when it could be built here (else None)."""
+    global _ref
+    if _ref is None:
+        path = _build.build_ref()
+        if path is None:
+            return None
+        R = C.CDLL(path)
+        for f in (R.ref_conh, R.ref_stvk):
+            f.argtypes = [C.c_double, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        _ref = R
+    return _ref
+
+
+def _p(a):
+    return a.ctypes.data if a is not None else None
+
+
+def default_options(**kw) -> OrcOptions:
+    o = OrcOptions()
+    lib().orc_default_options(C.byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise AttributeError(k)
+        setattr(o, k, v)
+    return o
+
+
+def material(model: int, lam: float, mu: float, Fv: np.ndarray):
+    Fv = np.ascontiguousarray(Fv, dtype=np.float64)
+    psi = np.zeros(1); P = np.zeros(9); D = np.zeros(81)
+    lib().orc_material(int(model), float(lam), float(mu), _p(Fv), _p(psi), _p(P), _p(D))
+    return psi[0], P, D.reshape(9, 9)
+
+
+class Oracle:
+    """One mesh instance in the CPU restatement."""
+
+    def __init__(self, mesh):
+        self.mesh = mesh
+        self._keep = [np.ascontiguousarray(mesh.X0, dtype=np.float64).ravel(),
+                      np.ascontiguousarray(mesh.T, dtype=np.int32).ravel(),
+                      np.ascontiguousarray(mesh.lame, dtype=np.float64).ravel(),
+                      np.ascontiguousarray(mesh.rho, dtype=np.float64).ravel(),
+                      np.ascontiguousarray(mesh.model, dtype=np.uint8).ravel(),
+                      np.ascontiguousarray(mesh.fixed, dtype=np.uint8).ravel(),
+                      np.ascontiguousarray(mesh.force, dtype=np.float64).ravel()]
+        d = OrcMesh()
+        d.n = mesh.n; d.m = mesh.m
+        d.X0, d.T, d.lame, d.rho, d.model, d.fixed, d.force = [a.ctypes.data for a in self._keep]
+        for c in range(3):
+            d.gravity[c] = float(mesh.gravity[c])
+        self._desc = d
+        h = C.c_void_p()
+        if lib().orc_create(C.byref(d), C.byref(h)) != 0:
+            raise ValueError("oracle rejected the mesh")
+        self.h = h
+        self.N = 3 * mesh.n
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_destroy(self.h)
+            self.h = None
+
+    def rest(self):
+        return np.ascontiguousarray(self.mesh.X0, dtype=np.float64).ravel().copy()
+
+    def element_local(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        m = self.mesh.m
+        E = np.zeros(m); g = np.zeros((m, 12)); H = np.zeros((m, 12, 12))
+        lib().orc_element_local(self.h, _p(x), _p(E), _p(g), _p(H))
+        return E, g, H
+
+    def energy(self, x) -> float:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        e = C.c_double()
+        lib().orc_energy(self.h, _p(x), C.byref(e))
+        return e.value
+
+    def gradient(self, x, fix=True):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        g = np.zeros(self.N)
+        lib().orc_gradient(self.h, _p(x), _p(g), int(fix))
+        return g
+
+    def pattern(self):
+        nnz = lib().orc_hessian_nnz(self.h)
+        cp = np.zeros(self.N + 1, dtype=np.int32); ri = np.zeros(nnz, dtype=np.int32)
+        lib().orc_hessian_pattern(self.h, _p(cp), _p(ri))
+        return cp, ri
+
+    def hessian(self, x, fix=True):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        v = np.zeros(lib().orc_hessian_nnz(self.h))
+        lib().orc_hessian(self.h, _p(x), _p(v), int(fix))
+        return v
+
+    def scatter_map(self):
+        mp = np.zeros((self.mesh.m, 10), dtype=np.int32)
+        lib().orc_scatter_map(self.h, _p(mp))
+        return mp
+
+    def solve_static(self, x=None, **opts):
+        x = self.rest() if x is None else np.ascontiguousarray(x, dtype=np.float64).copy()
+        o = default_options(**opts)
+        r = OrcReport()
+        lib().orc_solve_static(self.h, C.byref(o), _p(x), C.byref(r))
+        return x, r.as_dict()
+
+    def solve_dynamic(self, x, v, dt, **opts):
+        x = np.ascontiguousarray(x, dtype=np.float64).copy()
+        v = np.ascontiguousarray(v, dtype=np.float64).copy()
+        o = default_options(**opts)
+        r = OrcReport()
+        lib().orc_solve_dynamic(self.h, C.byref(o), float(dt), _p(x), _p(v), C.byref(r))
+        return x, v, r.as_dict()
+
+    def linear_solve(self, x, b, dx0=None, **opts):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        dx = np.zeros(self.N) if dx0 is None else np.ascontiguousarray(dx0, dtype=np.float64).copy()
+        o = default_options(**opts)
+        res = C.c_int32(); it = C.c_int64()
+        lib().orc_linear_solve(self.h, C.byref(o), _p(x), _p(b), _p(dx), C.byref(res), C.byref(it))
+        return dx, res.value, it.value
+
+    def last_log(self):
+        n = lib().orc_last_log(self.h, None, None, None, None, 0)
+        obj = np.zeros(n); opt = np.zeros(n); bis = np.zeros(n, dtype=np.int32); step = np.zeros(n)
+        lib().orc_last_log(self.h, _p(obj), _p(opt), _p(bis), _p(step), n)
+        return {"obj": obj, "opt": opt, "bis": bis, "step": step}

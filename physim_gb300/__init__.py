@@ -1,0 +1,361 @@
+"""physim_gb300 -- GB300-native tet-FEM Newton path behind PhySim's solver interface.
+
+The compute path is libphx.so (hand-written sm_103a CUDA + a C ABI, see
+include/phx.h).  This module is a thin ctypes binding over that ABI; it has
+no compute of its own and no fallback: if libphx.so cannot be loaded, every
+entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import mesh  # noqa: F401  (re-exported)
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libphx.so")
+
+PREC_FP64 = 0
+PREC_FP32_REFINE = 1
+OS_NAMES = {0: "ONGOING", 1: "SUCCESS", 2: "MINSTEP", 3: "MINIMPR", 4: "FAILURE", 5: "MAXITER", 6: "NONDESC"}
+
+PHX_OK, PHX_EINVAL, PHX_ENOMEM, PHX_ETIMEOUT, PHX_ECUDA, PHX_EBUSY, PHX_ENOTFOUND = 0, -1, -2, -3, -4, -5, -6
+
+# every entry point include/phx.h declares
+EXPORTS = [
+    "phx_version", "phx_last_error", "phx_default_options", "phx_context_create", "phx_context_destroy",
+    "phx_context_memory", "phx_instance_create", "phx_instance_destroy", "phx_instance_sizes",
+    "phx_instance_set_positions", "phx_instance_get_positions", "phx_instance_set_velocities",
+    "phx_instance_get_velocities", "phx_instance_update_load", "phx_energy_gradient", "phx_hessian",
+    "phx_hessian_pattern", "phx_scatter_map", "phx_element_local", "phx_solve_static", "phx_solve_step",
+    "phx_dynamic_step", "phx_batch_solve", "phx_batch_dynamic_step", "phx_server_create", "phx_server_destroy",
+    "phx_server_submit", "phx_server_progress", "phx_server_poll", "phx_profile_enable", "phx_profile_read",
+    "phx_profile_reset", "phx_kernel_launches",
+]
+
+
+class PhxError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"phx error {code}: {msg}")
+        self.code = code
+
+
+class Mesh_(C.Structure):
+    _fields_ = [("num_nodes", C.c_int32), ("num_tets", C.c_int32), ("X0", C.c_void_p), ("tets", C.c_void_p),
+                ("lame", C.c_void_p), ("rho", C.c_void_p), ("model", C.c_void_p), ("fixed", C.c_void_p),
+                ("force", C.c_void_p), ("gravity", C.c_double * 3)]
+
+
+class Options(C.Structure):
+    """phx_options: OptimSolverOptions (include/PhySim/Solvers/OptimSolver.h:47-70) + GPU settings."""
+    _fields_ = [("qp_solver", C.c_int32), ("tol_max_error", C.c_double), ("tol_min_step", C.c_double),
+                ("min_step_max_count", C.c_int32), ("tol_min_impr", C.c_double),
+                ("min_impr_max_count", C.c_int32), ("num_max_iters", C.c_int32), ("try_steepest", C.c_int32),
+                ("max_step_size", C.c_double), ("ls_solver", C.c_int32), ("ls_num_max_iters", C.c_int32),
+                ("ls_tol_max_error", C.c_double), ("ls_num_reg_trials", C.c_int32), ("lsearch_type", C.c_int32),
+                ("lsearch_alpha", C.c_double), ("lsearch_num_try", C.c_int32), ("precision", C.c_int32),
+                ("precond", C.c_int32), ("inner_tol", C.c_double), ("max_refine_sweeps", C.c_int32),
+                ("warm_guess", C.c_int32), ("pcg_chunk", C.c_int32)]
+
+
+class Report(C.Structure):
+    _fields_ = [("result", C.c_int32), ("iterations", C.c_int32), ("bisections", C.c_int32),
+                ("reg_trials", C.c_int32), ("pcg_iterations", C.c_int64), ("refine_sweeps", C.c_int32),
+                ("status", C.c_int32), ("obj", C.c_double), ("opt", C.c_double), ("opt0", C.c_double),
+                ("seconds", C.c_double)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["result_name"] = OS_NAMES.get(self.result, str(self.result))
+        return d
+
+
+_lib = None
+
+
+def lib():
+    """Loads libphx.so; raises if the CUDA path is not built (there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build the CUDA path first (physim_gb300.build.build())")
+    L = C.CDLL(LIB_PATH)
+    vp, i32, i64, dbl = C.c_void_p, C.c_int32, C.c_int64, C.c_double
+    sig = {
+        "phx_version": ([], C.c_int),
+        "phx_last_error": ([], C.c_char_p),
+        "phx_default_options": ([C.POINTER(Options)], None),
+        "phx_context_create": ([i32, i64, C.POINTER(vp)], C.c_int),
+        "phx_context_destroy": ([vp], C.c_int),
+        "phx_context_memory": ([vp, C.POINTER(i64), C.POINTER(i64)], C.c_int),
+        "phx_instance_create": ([vp, C.POINTER(Mesh_), C.POINTER(vp)], C.c_int),
+        "phx_instance_destroy": ([vp], C.c_int),
+        "phx_instance_sizes": ([vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)], C.c_int),
+        "phx_instance_set_positions": ([vp, vp], C.c_int),
+        "phx_instance_get_positions": ([vp, vp], C.c_int),
+        "phx_instance_set_velocities": ([vp, vp], C.c_int),
+        "phx_instance_get_velocities": ([vp, vp], C.c_int),
+        "phx_instance_update_load": ([vp, vp, vp], C.c_int),
+        "phx_energy_gradient": ([vp, vp, C.POINTER(dbl), vp, i32], C.c_int),
+        "phx_hessian": ([vp, vp, i32, vp, i32], C.c_int),
+        "phx_hessian_pattern": ([vp, vp, vp], C.c_int),
+        "phx_scatter_map": ([vp, vp], C.c_int),
+        "phx_element_local": ([vp, vp, i32, vp, vp, vp], C.c_int),
+        "phx_solve_static": ([vp, C.POINTER(Options), vp, C.POINTER(Report)], C.c_int),
+        "phx_solve_step": ([vp, C.POINTER(Options), vp, C.POINTER(Report)], C.c_int),
+        "phx_dynamic_step": ([vp, C.POINTER(Options), dbl, vp, vp, C.POINTER(Report)], C.c_int),
+        "phx_batch_solve": ([vp, i32, vp, C.POINTER(Options), vp, vp], C.c_int),
+        "phx_batch_dynamic_step": ([vp, i32, vp, C.POINTER(Options), dbl, vp], C.c_int),
+        "phx_server_create": ([vp, i32, i64, C.POINTER(Options), C.POINTER(vp)], C.c_int),
+        "phx_server_destroy": ([vp], C.c_int),
+        "phx_server_submit": ([vp, vp, i64], C.c_int),
+        "phx_server_progress": ([vp, C.POINTER(i32), C.POINTER(i32)], C.c_int),
+        "phx_server_poll": ([vp, vp, vp, i32], C.c_int),
+        "phx_profile_enable": ([vp, i32], C.c_int),
+        "phx_profile_read": ([vp, C.c_char_p, C.POINTER(i64), C.POINTER(dbl)], C.c_int),
+        "phx_profile_reset": ([vp], C.c_int),
+        "phx_kernel_launches": ([vp], i64),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _check(rc: int):
+    if rc != PHX_OK:
+        raise PhxError(rc, lib().phx_last_error().decode(errors="replace"))
+
+
+def _p(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data
+
+
+def options(**kw) -> Options:
+    o = Options()
+    lib().phx_default_options(C.byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise AttributeError(f"unknown option {k}")
+        setattr(o, k, v)
+    return o
+
+
+class Context:
+    """One GPU, one stream, one device-memory arena."""
+
+    def __init__(self, device: int = 0, arena_bytes: int = 0):
+        h = C.c_void_p()
+        _check(lib().phx_context_create(int(device), int(arena_bytes), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().phx_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def memory(self):
+        u = C.c_int64(); c = C.c_int64()
+        _check(lib().phx_context_memory(self.h, C.byref(u), C.byref(c)))
+        return u.value, c.value
+
+    def kernel_launches(self) -> int:
+        return int(lib().phx_kernel_launches(self.h))
+
+    def profile(self, on: bool = True):
+        _check(lib().phx_profile_enable(self.h, int(on)))
+
+    def profile_reset(self):
+        _check(lib().phx_profile_reset(self.h))
+
+    def profile_read(self, kind: str):
+        n = C.c_int64(); ms = C.c_double()
+        _check(lib().phx_profile_read(self.h, kind.encode(), C.byref(n), C.byref(ms)))
+        return n.value, ms.value
+
+    def batch_solve(self, insts: Sequence["Instance"], opts: Options, xs: Optional[List[np.ndarray]] = None):
+        n = len(insts)
+        arr = (C.c_void_p * n)(*[i.h.value for i in insts])
+        reps = (Report * n)()
+        if xs is not None:
+            xs = [np.ascontiguousarray(x, dtype=np.float64) for x in xs]
+            xp = (C.c_void_p * n)(*[x.ctypes.data for x in xs])
+        else:
+            xp = None
+        _check(lib().phx_batch_solve(self.h, n, arr, C.byref(opts), xp, reps))
+        return [r.as_dict() for r in reps], xs
+
+    def batch_dynamic_step(self, insts: Sequence["Instance"], opts: Options, dt: float):
+        n = len(insts)
+        arr = (C.c_void_p * n)(*[i.h.value for i in insts])
+        reps = (Report * n)()
+        _check(lib().phx_batch_dynamic_step(self.h, n, arr, C.byref(opts), float(dt), reps))
+        return [r.as_dict() for r in reps]
+
+
+class Instance:
+    """One FEM volume on the device (Simulable_FEM + boundary conditions)."""
+
+    def __init__(self, ctx: Context, m):
+        self.ctx = ctx
+        self.mesh = m
+        keep = [np.ascontiguousarray(m.X0, dtype=np.float64).ravel(),
+                np.ascontiguousarray(m.T, dtype=np.int32).ravel(),
+                np.ascontiguousarray(m.lame, dtype=np.float64).ravel(),
+                np.ascontiguousarray(m.rho, dtype=np.float64).ravel(),
+                np.ascontiguousarray(m.model, dtype=np.uint8).ravel(),
+                np.ascontiguousarray(m.fixed, dtype=np.uint8).ravel(),
+                np.ascontiguousarray(m.force, dtype=np.float64).ravel()]
+        d = Mesh_()
+        d.num_nodes = m.n
+        d.num_tets = m.m
+        d.X0, d.tets, d.lame, d.rho, d.model, d.fixed, d.force = [a.ctypes.data for a in keep]
+        for c in range(3):
+            d.gravity[c] = float(m.gravity[c])
+        h = C.c_void_p()
+        _check(lib().phx_instance_create(ctx.h, C.byref(d), C.byref(h)))
+        self.h = h
+        self.N = 3 * m.n
+
+    def close(self):
+        if getattr(self, "h", None) and self.ctx.h:
+            lib().phx_instance_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sizes(self):
+        a, b, c, d = (C.c_int64() for _ in range(4))
+        _check(lib().phx_instance_sizes(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
+        return {"ndof": a.value, "nnz": b.value, "lower_blocks": c.value, "full_blocks": d.value}
+
+    def set_positions(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        _check(lib().phx_instance_set_positions(self.h, _p(x)))
+
+    def positions(self):
+        x = np.zeros(self.N)
+        _check(lib().phx_instance_get_positions(self.h, _p(x)))
+        return x
+
+    def set_velocities(self, v):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        _check(lib().phx_instance_set_velocities(self.h, _p(v)))
+
+    def velocities(self):
+        v = np.zeros(self.N)
+        _check(lib().phx_instance_get_velocities(self.h, _p(v)))
+        return v
+
+    def update_load(self, force=None, gravity=None):
+        f = None if force is None else np.ascontiguousarray(force, dtype=np.float64)
+        g = None if gravity is None else np.ascontiguousarray(gravity, dtype=np.float64)
+        _check(lib().phx_instance_update_load(self.h, _p(f), _p(g)))
+
+    def energy_gradient(self, x=None, fix=True):
+        xx = None if x is None else np.ascontiguousarray(x, dtype=np.float64)
+        e = C.c_double()
+        g = np.zeros(self.N)
+        _check(lib().phx_energy_gradient(self.h, _p(xx), C.byref(e), _p(g), int(fix)))
+        return e.value, g
+
+    def hessian(self, x=None, precision=PREC_FP64, fix=True):
+        xx = None if x is None else np.ascontiguousarray(x, dtype=np.float64)
+        v = np.zeros(self.sizes()["nnz"])
+        _check(lib().phx_hessian(self.h, _p(xx), int(precision), _p(v), int(fix)))
+        return v
+
+    def pattern(self):
+        s = self.sizes()
+        cp = np.zeros(self.N + 1, dtype=np.int32)
+        ri = np.zeros(s["nnz"], dtype=np.int32)
+        _check(lib().phx_hessian_pattern(self.h, _p(cp), _p(ri)))
+        return cp, ri
+
+    def scatter_map(self):
+        mp = np.zeros((self.mesh.m, 10), dtype=np.int32)
+        _check(lib().phx_scatter_map(self.h, _p(mp)))
+        return mp
+
+    def element_local(self, x=None, precision=PREC_FP64):
+        xx = None if x is None else np.ascontiguousarray(x, dtype=np.float64)
+        m = self.mesh.m
+        E = np.zeros(m); g = np.zeros((m, 12)); H = np.zeros((m, 12, 12))
+        _check(lib().phx_element_local(self.h, _p(xx), int(precision), _p(E), _p(g), _p(H)))
+        return E, g, H
+
+    def solve_static(self, opts: Options, x=None):
+        xx = None if x is None else np.ascontiguousarray(x, dtype=np.float64).copy()
+        r = Report()
+        _check(lib().phx_solve_static(self.h, C.byref(opts), _p(xx), C.byref(r)))
+        return (self.positions() if xx is None else xx), r.as_dict()
+
+    def solve_step(self, opts: Options, x=None):
+        xx = None if x is None else np.ascontiguousarray(x, dtype=np.float64).copy()
+        r = Report()
+        _check(lib().phx_solve_step(self.h, C.byref(opts), _p(xx), C.byref(r)))
+        return (self.positions() if xx is None else xx), r.as_dict()
+
+    def dynamic_step(self, opts: Options, dt: float, x=None, v=None):
+        xx = None if x is None else np.ascontiguousarray(x, dtype=np.float64).copy()
+        vv = None if v is None else np.ascontiguousarray(v, dtype=np.float64).copy()
+        r = Report()
+        _check(lib().phx_dynamic_step(self.h, C.byref(opts), float(dt), _p(xx), _p(vv), C.byref(r)))
+        if xx is None:
+            xx = self.positions()
+        if vv is None:
+            vv = self.velocities()
+        return xx, vv, r.as_dict()
+
+
+class Server:
+    """Continuous batching over the device engine (phx_server_*)."""
+
+    def __init__(self, ctx: Context, max_slots: int, budget_bytes: int, opts: Options):
+        h = C.c_void_p()
+        _check(lib().phx_server_create(ctx.h, int(max_slots), int(budget_bytes), C.byref(opts), C.byref(h)))
+        self.h = h
+        self.ctx = ctx
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().phx_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, inst: Instance, tag: int):
+        _check(lib().phx_server_submit(self.h, inst.h, int(tag)))
+
+    def progress(self):
+        a = C.c_int32(); q = C.c_int32()
+        _check(lib().phx_server_progress(self.h, C.byref(a), C.byref(q)))
+        return a.value, q.value
+
+    def poll(self, cap: int = 1024):
+        tags = np.zeros(cap, dtype=np.int64)
+        reps = (Report * cap)()
+        n = lib().phx_server_poll(self.h, _p(tags), reps, cap)
+        if n < 0:
+            _check(n)
+        return [(int(tags[i]), reps[i].as_dict()) for i in range(n)]

@@ -1,0 +1,1049 @@
+// engine.cu -- host side of the device engine and the C ABI declared in include/phx.h.
+//
+// A context owns one device, one stream and one device-memory arena.  An
+// instance is one FEM volume: its pattern and scatter map are built on the
+// host once (pattern.cpp) and uploaded; all solver state then lives on the
+// device.  A solve (or a batch of solves, or a serving loop) runs "rounds" of
+// persistent kernels over the packed tile index of the active instances; the
+// per-instance state machine (newton_control.h) advances between kernels on
+// the device, and the host only reads the active count after each round.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "../../include/phx.h"
+#include "kernels.h"
+#include "newton_control.h"
+#include "pattern.h"
+
+using namespace phx;
+
+namespace {
+
+thread_local std::string g_err;
+
+int set_err(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CU(call)                                                                              \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess)                                                                    \
+      return set_err(PHX_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_));          \
+  } while (0)
+
+using clk = std::chrono::steady_clock;
+
+// wall-clock limit of one blocking solve call (the device never waits; this bounds the host loop)
+constexpr double kSolveTimeLimit = 600.0;
+
+// ---------------------------------------------------------------------------
+// device arena: one allocation, first-fit free list with coalescing, 256 B alignment
+// ---------------------------------------------------------------------------
+struct Arena {
+  char* base = nullptr;
+  size_t cap = 0, used = 0;
+  std::map<size_t, size_t> free_;
+  std::map<size_t, size_t> live_;
+
+  cudaError_t init(size_t bytes) {
+    cap = (bytes + 255) & ~(size_t)255;
+    cudaError_t e = cudaMalloc(&base, cap);
+    if (e != cudaSuccess) { base = nullptr; cap = 0; return e; }
+    free_[0] = cap;
+    return cudaSuccess;
+  }
+  void release() {
+    if (base) cudaFree(base);
+    base = nullptr;
+    free_.clear();
+    live_.clear();
+    cap = used = 0;
+  }
+  void* alloc(size_t bytes) {
+    bytes = std::max<size_t>(256, (bytes + 255) & ~(size_t)255);
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second >= bytes) {
+        size_t off = it->first, sz = it->second;
+        free_.erase(it);
+        if (sz > bytes) free_[off + bytes] = sz - bytes;
+        live_[off] = bytes;
+        used += bytes;
+        return base + off;
+      }
+    }
+    return nullptr;
+  }
+  void free(void* p) {
+    if (!p) return;
+    size_t off = (char*)p - base;
+    auto it = live_.find(off);
+    if (it == live_.end()) return;
+    size_t sz = it->second;
+    live_.erase(it);
+    used -= sz;
+    auto nx = free_.lower_bound(off);
+    if (nx != free_.end() && off + sz == nx->first) {
+      sz += nx->second;
+      nx = free_.erase(nx);
+    }
+    if (nx != free_.begin()) {
+      auto pv = std::prev(nx);
+      if (pv->first + pv->second == off) {
+        pv->second += sz;
+        return;
+      }
+    }
+    free_[off] = sz;
+  }
+};
+
+}  // namespace
+
+struct phx_context_s {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  Arena arena;
+  int64_t launches = 0;
+  // profiling
+  bool profiling = false;
+  struct Ev { int kind; cudaEvent_t a, b; };
+  std::vector<Ev> evs;
+  std::vector<cudaEvent_t> pool;
+  double prof_ms[K_COUNT] = {0};
+  int64_t prof_n[K_COUNT] = {0};
+  // batch buffers
+  int cap = 0;
+  InstDev* d_inst = nullptr;
+  int32_t* d_pre = nullptr;   // 3 * (cap + 1) + 1 (num)
+  int32_t* d_flags = nullptr; // 8 + cap
+  int32_t* h_flags = nullptr; // pinned mirror
+  std::vector<int32_t> h_pre;
+  const void* batch_owner = nullptr;  // who set the batch buffers last
+};
+
+struct phx_instance_s {
+  phx_context ctx = nullptr;
+  HostPattern hp;
+  InstDev dev{};
+  std::vector<void*> blocks;
+  NState* d_st = nullptr;
+  DevOpts* d_opts = nullptr;
+  bool have32 = false, have64 = false;
+  int64_t bytes = 0;
+  bool in_server = false;
+  double gravity[3] = {0, 0, 0};
+  std::vector<double> force;
+};
+
+namespace {
+
+template <typename T>
+int arena_alloc(phx_instance inst, T** out, size_t count, bool zero = false) {
+  size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+  void* p = inst->ctx->arena.alloc(bytes);
+  if (!p) return set_err(PHX_ENOMEM, "device arena exhausted (" + std::to_string(bytes) + " bytes requested)");
+  inst->blocks.push_back(p);
+  inst->bytes += (int64_t)((bytes + 255) & ~(size_t)255);
+  if (zero) {
+    cudaError_t e = cudaMemsetAsync(p, 0, bytes, inst->ctx->stream);
+    if (e != cudaSuccess) return set_err(PHX_ECUDA, cudaGetErrorString(e));
+  }
+  *out = (T*)p;
+  return PHX_OK;
+}
+
+template <typename T>
+int upload(phx_instance inst, T** out, const std::vector<T>& v) {
+  int rc = arena_alloc(inst, out, v.size());
+  if (rc) return rc;
+  if (!v.empty()) CU(cudaMemcpyAsync(*out, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, inst->ctx->stream));
+  return PHX_OK;
+}
+
+#define TRY(x)            \
+  do {                    \
+    int rc_ = (x);        \
+    if (rc_) return rc_;  \
+  } while (0)
+
+int ensure_precision(phx_instance inst, bool fp64) {
+  InstDev& D = inst->dev;
+  const size_t n4 = 4 * (size_t)D.n, m = D.m;
+  if (fp64 && !inst->have64) {
+    TRY(arena_alloc(inst, &D.Hloc64, 90 * m));
+    TRY(arena_alloc(inst, &D.H64, 9 * (size_t)D.nslots, true));
+    TRY(arena_alloc(inst, &D.rd, n4, true));
+    TRY(arena_alloc(inst, &D.zd, n4, true));
+    TRY(arena_alloc(inst, &D.pda, n4, true));
+    TRY(arena_alloc(inst, &D.pdb, n4, true));
+    TRY(arena_alloc(inst, &D.qd, n4, true));
+    TRY(arena_alloc(inst, &D.ed, n4, true));
+    TRY(arena_alloc(inst, &D.minvd, 9 * (size_t)D.n, true));
+    inst->have64 = true;
+  }
+  if (!fp64 && !inst->have32) {
+    TRY(arena_alloc(inst, &D.Hloc32, 90 * m));
+    TRY(arena_alloc(inst, &D.H32, 9 * (size_t)D.nslots, true));
+    TRY(arena_alloc(inst, &D.r32, n4, true));
+    TRY(arena_alloc(inst, &D.z32, n4, true));
+    TRY(arena_alloc(inst, &D.p32a, n4, true));
+    TRY(arena_alloc(inst, &D.p32b, n4, true));
+    TRY(arena_alloc(inst, &D.q32, n4, true));
+    TRY(arena_alloc(inst, &D.e32, n4, true));
+    TRY(arena_alloc(inst, &D.minv32, 9 * (size_t)D.n, true));
+    inst->have32 = true;
+  }
+  return PHX_OK;
+}
+
+int tiles(int count) { return (count + kTile - 1) / kTile; }
+
+// ---------------------------------------------------------------------------
+// batches
+// ---------------------------------------------------------------------------
+int ensure_batch_cap(phx_context ctx, int num) {
+  if (num <= ctx->cap) return PHX_OK;
+  int cap = std::max(num, std::max(16, ctx->cap * 2));
+  if (ctx->d_inst) cudaFree(ctx->d_inst);
+  if (ctx->d_pre) cudaFree(ctx->d_pre);
+  if (ctx->d_flags) cudaFree(ctx->d_flags);
+  if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
+  ctx->d_inst = nullptr; ctx->d_pre = nullptr; ctx->d_flags = nullptr; ctx->h_flags = nullptr;
+  CU(cudaMalloc(&ctx->d_inst, sizeof(InstDev) * cap));
+  CU(cudaMalloc(&ctx->d_pre, sizeof(int32_t) * (3 * (cap + 1) + 1)));
+  CU(cudaMalloc(&ctx->d_flags, sizeof(int32_t) * (8 + cap)));
+  CU(cudaMallocHost(&ctx->h_flags, sizeof(int32_t) * (8 + cap)));
+  ctx->cap = cap;
+  return PHX_OK;
+}
+
+struct Grids { int tet = 0, node = 0, lob = 0; };
+
+// Uploads the descriptors and tile prefix arrays of a set of instances.
+int set_batch(phx_context ctx, const std::vector<phx_instance>& list, BatchDev& B, Grids& G) {
+  int num = (int)list.size();
+  ctx->batch_owner = nullptr;
+  TRY(ensure_batch_cap(ctx, std::max(num, 1)));
+  std::vector<InstDev> d(num);
+  std::vector<int32_t>& pre = ctx->h_pre;
+  pre.assign(3 * (ctx->cap + 1) + 1, 0);
+  int32_t* pt = pre.data();
+  int32_t* pn = pt + (ctx->cap + 1);
+  int32_t* pl = pn + (ctx->cap + 1);
+  for (int i = 0; i < num; ++i) {
+    d[i] = list[i]->dev;
+    pt[i + 1] = pt[i] + tiles(list[i]->dev.m);
+    pn[i + 1] = pn[i] + tiles(list[i]->dev.n);
+    pl[i + 1] = pl[i] + tiles(list[i]->dev.nlo);
+  }
+  pre[3 * (ctx->cap + 1)] = num;
+  if (num) CU(cudaMemcpyAsync(ctx->d_inst, d.data(), sizeof(InstDev) * num, cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaMemcpyAsync(ctx->d_pre, pre.data(), sizeof(int32_t) * pre.size(), cudaMemcpyHostToDevice, ctx->stream));
+  B.num = ctx->d_pre + 3 * (ctx->cap + 1);
+  B.pre_tet = ctx->d_pre;
+  B.pre_node = ctx->d_pre + (ctx->cap + 1);
+  B.pre_lob = ctx->d_pre + 2 * (ctx->cap + 1);
+  B.inst = ctx->d_inst;
+  B.flags = ctx->d_flags;
+  const int sms = std::max(1, ctx->num_sms);
+  G.tet = std::min(pt[num], sms * 8);
+  G.node = std::min(pn[num], sms * 16);
+  G.lob = std::min(pl[num], sms * 6);
+  return PHX_OK;
+}
+
+void do_launch(phx_context ctx, KernelId id, int grid, const BatchDev& B, bool fp64) {
+  if (grid <= 0) return;
+  if (ctx->profiling) {
+    cudaEvent_t a, b;
+    if (ctx->pool.size() >= 2) {
+      a = ctx->pool.back(); ctx->pool.pop_back();
+      b = ctx->pool.back(); ctx->pool.pop_back();
+    } else {
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+    }
+    cudaEventRecord(a, ctx->stream);
+    launch(id, grid, ctx->stream, B, fp64);
+    cudaEventRecord(b, ctx->stream);
+    ctx->evs.push_back({(int)id, a, b});
+  } else {
+    launch(id, grid, ctx->stream, B, fp64);
+  }
+  ctx->launches++;
+}
+
+// One round of the device engine (see the phase sequence in newton_control.h).
+void run_round(phx_context ctx, const BatchDev& B, const Grids& G, bool fp64, int pcg_chunk) {
+  auto L = [&](KernelId id, int grid) { do_launch(ctx, id, grid, B, fp64); };
+  L(K_CONTROL, 1); L(K_VECOP, G.node); L(K_CONTROL, 1);
+  L(K_ELEM_EG, G.tet); L(K_GATHER, G.node);
+  L(K_CONTROL, 1); L(K_VECOP, G.node); L(K_CONTROL, 1);
+  L(K_ELEM_HESS, G.tet); L(K_ASSEMBLE, G.lob); L(K_JACOBI, G.node);
+  L(K_LINSETUP, G.node); L(K_RESID, G.node);
+  for (int k = 0; k < pcg_chunk; ++k) { L(K_PCG_A, G.node); L(K_PCG_B, G.node); }
+  L(K_ACCUM, G.node); L(K_RESID, G.node);
+  L(K_CONTROL, 1); L(K_VECOP, G.node); L(K_CONTROL, 1);
+  L(K_ELEM_EG, G.tet); L(K_GATHER, G.node);
+}
+
+int read_flags(phx_context ctx, int num) {
+  CU(cudaMemcpyAsync(ctx->h_flags, ctx->d_flags, sizeof(int32_t) * (8 + num), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return PHX_OK;
+}
+
+DevOpts make_opts(const phx_options* o, bool dynamic, double dt) {
+  DevOpts d{};
+  d.qp_solver = o->qp_solver;
+  d.min_step_max_count = o->min_step_max_count;
+  d.min_impr_max_count = o->min_impr_max_count;
+  d.num_max_iters = o->num_max_iters;
+  d.try_steepest = o->try_steepest;
+  d.ls_num_max_iters = o->ls_num_max_iters;
+  d.ls_num_reg_trials = o->ls_num_reg_trials;
+  d.lsearch_num_try = o->lsearch_num_try;
+  d.precision = o->precision;
+  d.precond = o->precond;
+  d.max_refine_sweeps = o->precision == PHX_PREC_FP64 ? 1 : std::max(1, o->max_refine_sweeps);
+  d.warm_guess = o->warm_guess;
+  d.dynamic = dynamic ? 1 : 0;
+  d.tol_max_error = o->tol_max_error;
+  d.tol_min_step = o->tol_min_step;
+  d.tol_min_impr = o->tol_min_impr;
+  d.max_step_size = o->max_step_size;
+  d.ls_tol_max_error = o->ls_tol_max_error;
+  d.lsearch_alpha = o->lsearch_alpha;
+  d.inner_tol = o->inner_tol;
+  d.dt = dt;
+  return d;
+}
+
+int validate_opts(const phx_options* o) {
+  if (!o) return set_err(PHX_EINVAL, "options: NULL");
+  if (o->precision != PHX_PREC_FP64 && o->precision != PHX_PREC_FP32_REFINE)
+    return set_err(PHX_EINVAL, "options: unknown precision");
+  if (o->qp_solver != 0 && o->qp_solver != 1) return set_err(PHX_EINVAL, "options: qp_solver must be 0 (Steepest) or 1 (Newton)");
+  if (o->lsearch_type != 1) return set_err(PHX_EINVAL, "options: only the Simple line search runs on the device");
+  if (o->ls_num_reg_trials < 1 || o->ls_num_max_iters < 0 || o->num_max_iters < 1)
+    return set_err(PHX_EINVAL, "options: non-positive iteration limit");
+  if (!(o->lsearch_alpha > 0 && o->lsearch_alpha < 1)) return set_err(PHX_EINVAL, "options: lsearch_alpha out of (0,1)");
+  if (o->pcg_chunk < 1 || o->pcg_chunk > 4096) return set_err(PHX_EINVAL, "options: pcg_chunk out of [1,4096]");
+  return PHX_OK;
+}
+
+int upload_x(phx_instance inst, const double* x3, double* dst) {
+  const int n = inst->dev.n;
+  std::vector<double> buf(4 * (size_t)n, 0.0);
+  for (int v = 0; v < n; ++v)
+    for (int c = 0; c < 3; ++c) buf[4 * (size_t)v + c] = x3[3 * (size_t)v + c];
+  CU(cudaMemcpyAsync(dst, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice, inst->ctx->stream));
+  CU(cudaStreamSynchronize(inst->ctx->stream));
+  return PHX_OK;
+}
+
+int download_x(phx_instance inst, const double* src, double* x3) {
+  const int n = inst->dev.n;
+  std::vector<double> buf(4 * (size_t)n);
+  CU(cudaMemcpyAsync(buf.data(), src, buf.size() * sizeof(double), cudaMemcpyDeviceToHost, inst->ctx->stream));
+  CU(cudaStreamSynchronize(inst->ctx->stream));
+  for (int v = 0; v < n; ++v)
+    for (int c = 0; c < 3; ++c) x3[3 * (size_t)v + c] = buf[4 * (size_t)v + c];
+  return PHX_OK;
+}
+
+int reset_state(phx_instance inst, int phase, int nofix, double shift) {
+  NState s{};
+  s.phase = phase;
+  s.nofix = nofix;
+  s.shift = shift;
+  s.opt0 = -1.0;
+  CU(cudaMemcpyAsync(inst->d_st, &s, sizeof(NState), cudaMemcpyHostToDevice, inst->ctx->stream));
+  return PHX_OK;
+}
+
+int read_state(phx_instance inst, NState* s) {
+  CU(cudaMemcpyAsync(s, inst->d_st, sizeof(NState), cudaMemcpyDeviceToHost, inst->ctx->stream));
+  CU(cudaStreamSynchronize(inst->ctx->stream));
+  return PHX_OK;
+}
+
+void fill_report(const NState& s, bool step, double seconds, phx_report* r) {
+  if (!r) return;
+  r->result = step ? s.step_result : s.result;
+  r->iterations = s.it;
+  r->bisections = s.total_bis;
+  r->reg_trials = s.total_reg;
+  r->pcg_iterations = s.pcg_total;
+  r->refine_sweeps = s.total_sweeps;
+  r->status = s.error ? PHX_ETIMEOUT : PHX_OK;
+  r->obj = s.obj;
+  r->opt = s.opt;
+  r->opt0 = s.opt0;
+  r->seconds = seconds;
+}
+
+// Runs a set of instances (states already reset to PH_START) until all are done.
+int run_to_completion(phx_context ctx, const std::vector<phx_instance>& list, bool fp64, int pcg_chunk) {
+  BatchDev B{};
+  Grids G;
+  TRY(set_batch(ctx, list, B, G));
+  const int num = (int)list.size();
+  const auto t0 = clk::now();
+  for (int64_t r = 0;; ++r) {
+    run_round(ctx, B, G, fp64, pcg_chunk);
+    CU(cudaGetLastError());
+    TRY(read_flags(ctx, num));
+    if (ctx->h_flags[0] == 0) return PHX_OK;
+    if (std::chrono::duration<double>(clk::now() - t0).count() > kSolveTimeLimit)
+      return set_err(PHX_ETIMEOUT, "solver did not finish within " + std::to_string(kSolveTimeLimit) + " s");
+  }
+}
+
+int start_solve(phx_instance inst, const phx_options* o, bool dynamic, double dt, int max_iters_override) {
+  TRY(validate_opts(o));
+  const bool fp64 = o->precision == PHX_PREC_FP64;
+  TRY(ensure_precision(inst, fp64));
+  DevOpts d = make_opts(o, dynamic, dt);
+  if (max_iters_override > 0) d.num_max_iters = max_iters_override;
+  CU(cudaMemcpyAsync(inst->d_opts, &d, sizeof(DevOpts), cudaMemcpyHostToDevice, inst->ctx->stream));
+  TRY(reset_state(inst, PH_START, 0, 0.0));
+  return PHX_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int phx_version(void) { return 10000; }
+
+const char* phx_last_error(void) { return g_err.c_str(); }
+
+void phx_default_options(phx_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->qp_solver = 1;
+  o->tol_max_error = 1e-6;
+  o->tol_min_step = 1e-5;
+  o->min_step_max_count = 3;
+  o->tol_min_impr = 1e-9;
+  o->min_impr_max_count = 3;
+  o->num_max_iters = 100;
+  o->try_steepest = 1;
+  o->max_step_size = 1000;
+  o->ls_solver = 1;
+  o->ls_num_max_iters = 1000;
+  o->ls_tol_max_error = 1e-9;
+  o->ls_num_reg_trials = 10;
+  o->lsearch_type = 1;
+  o->lsearch_alpha = 0.5;
+  o->lsearch_num_try = 32;
+  o->precision = PHX_PREC_FP64;
+  o->precond = 1;
+  o->inner_tol = 1e-3;
+  o->max_refine_sweeps = 12;
+  o->warm_guess = 1;
+  o->pcg_chunk = 32;
+}
+
+int phx_context_create(int32_t device, int64_t arena_bytes, phx_context* out) {
+  if (!out) return set_err(PHX_EINVAL, "out is NULL");
+  *out = nullptr;
+  int count = 0;
+  CU(cudaGetDeviceCount(&count));
+  if (device < 0 || device >= count) return set_err(PHX_EINVAL, "no such CUDA device");
+  CU(cudaSetDevice(device));
+  auto* ctx = new phx_context_s();
+  ctx->device = device;
+  cudaError_t e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = setup_kernel_attributes();
+  size_t fr = 0, tot = 0;
+  if (e == cudaSuccess) e = cudaMemGetInfo(&fr, &tot);
+  if (e == cudaSuccess) {
+    size_t want = arena_bytes > 0 ? (size_t)arena_bytes : fr / 4;
+    e = ctx->arena.init(want);
+  }
+  if (e != cudaSuccess) {
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return set_err(PHX_ECUDA, std::string("context: ") + cudaGetErrorString(e));
+  }
+  *out = ctx;
+  return PHX_OK;
+}
+
+int phx_context_destroy(phx_context ctx) {
+  if (!ctx) return PHX_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& ev : ctx->evs) { cudaEventDestroy(ev.a); cudaEventDestroy(ev.b); }
+  for (auto& ev : ctx->pool) cudaEventDestroy(ev);
+  if (ctx->d_inst) cudaFree(ctx->d_inst);
+  if (ctx->d_pre) cudaFree(ctx->d_pre);
+  if (ctx->d_flags) cudaFree(ctx->d_flags);
+  if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
+  ctx->arena.release();
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return PHX_OK;
+}
+
+int phx_context_memory(phx_context ctx, int64_t* used, int64_t* cap) {
+  if (!ctx) return set_err(PHX_EINVAL, "ctx is NULL");
+  if (used) *used = (int64_t)ctx->arena.used;
+  if (cap) *cap = (int64_t)ctx->arena.cap;
+  return PHX_OK;
+}
+
+int phx_instance_destroy(phx_instance inst) {
+  if (!inst) return PHX_OK;
+  if (inst->in_server) return set_err(PHX_EBUSY, "instance is admitted to a server");
+  cudaStreamSynchronize(inst->ctx->stream);
+  for (void* p : inst->blocks) inst->ctx->arena.free(p);
+  delete inst;
+  return PHX_OK;
+}
+
+int phx_instance_create(phx_context ctx, const phx_mesh* mesh, phx_instance* out) {
+  if (!ctx || !mesh || !out) return set_err(PHX_EINVAL, "NULL argument");
+  *out = nullptr;
+  MeshIn in;
+  in.n = mesh->num_nodes;
+  in.m = mesh->num_tets;
+  in.X0 = mesh->X0;
+  in.T = mesh->tets;
+  in.lame = mesh->lame;
+  in.rho = mesh->rho;
+  in.model = mesh->model;
+  in.fixed = mesh->fixed;
+  in.force = mesh->force;
+  for (int c = 0; c < 3; ++c) in.gravity[c] = mesh->gravity[c];
+  auto* inst = new phx_instance_s();
+  inst->ctx = ctx;
+  std::string err;
+  if (!build_pattern(in, inst->hp, err)) {
+    delete inst;
+    return set_err(PHX_EINVAL, err);
+  }
+  for (int c = 0; c < 3; ++c) inst->gravity[c] = mesh->gravity[c];
+  if (mesh->force) inst->force.assign(mesh->force, mesh->force + 3 * (size_t)in.n);
+  CU(cudaSetDevice(ctx->device));
+  HostPattern& hp = inst->hp;
+  InstDev& D = inst->dev;
+  D.n = hp.n; D.m = hp.m; D.nlo = hp.nlo; D.nchunks = hp.nchunks; D.nslots = hp.nslots;
+  auto fail = [&](int rc) { phx_instance_destroy(inst); return rc; };
+  int rc = PHX_OK;
+  const size_t n4 = 4 * (size_t)hp.n;
+#define UP(field, vec)                                          \
+  do {                                                          \
+    std::remove_const_t<std::remove_pointer_t<decltype(D.field)>>* p_;  \
+    rc = upload(inst, &p_, vec);                                \
+    if (rc) return fail(rc);                                    \
+    D.field = p_;                                               \
+  } while (0)
+  UP(tets, hp.tets);
+  UP(rest64, hp.rest64);
+  UP(rest32, hp.rest32);
+  UP(model, hp.model);
+  UP(chunk_off, hp.chunk_off);
+  UP(slot_col, hp.slot_col);
+  UP(diag_slot, hp.diag_slot);
+  UP(lo_rc, hp.lo_rc);
+  UP(lo_slot, hp.lo_slot);
+  UP(up_slot, hp.up_slot);
+  UP(seg_ptr, hp.seg_ptr);
+  UP(seg_c, hp.seg_c);
+  UP(nseg_ptr, hp.nseg_ptr);
+  UP(nseg_c, hp.nseg_c);
+  UP(fixmask, hp.fixmask);
+  UP(mass, hp.mass);
+  UP(hlin, hp.hlin);
+#undef UP
+  double** vecs[] = {&D.x, &D.xs, &D.dx, &D.g, &D.gn, &D.dxprev, &D.x0, &D.v0, &D.v, &D.r64, &D.bvec};
+  for (double** pv : vecs)
+    if ((rc = arena_alloc(inst, pv, n4, true))) return fail(rc);
+  if ((rc = arena_alloc(inst, &D.Eloc, (size_t)hp.m))) return fail(rc);
+  if ((rc = arena_alloc(inst, &D.Gloc, 12 * (size_t)hp.m))) return fail(rc);
+  size_t maxt = std::max({tiles(hp.m), tiles(hp.n), tiles(hp.nlo)});
+  if ((rc = arena_alloc(inst, &D.partials, maxt * kPartials))) return fail(rc);
+  if ((rc = arena_alloc(inst, &D.counter, 1, true))) return fail(rc);
+  if ((rc = arena_alloc(inst, &inst->d_st, 1, true))) return fail(rc);
+  if ((rc = arena_alloc(inst, &inst->d_opts, 1, true))) return fail(rc);
+  D.st = inst->d_st;
+  D.opts = inst->d_opts;
+  // rest positions
+  if ((rc = upload_x(inst, mesh->X0, D.x))) return fail(rc);
+  // keep only what later calls need on the host
+  hp.rest64.clear(); hp.rest64.shrink_to_fit();
+  hp.rest32.clear(); hp.rest32.shrink_to_fit();
+  hp.seg_c.clear(); hp.seg_c.shrink_to_fit();
+  hp.nseg_c.clear(); hp.nseg_c.shrink_to_fit();
+  hp.slot_col.clear(); hp.slot_col.shrink_to_fit();
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return fail(set_err(PHX_ECUDA, cudaGetErrorString(e)));
+  *out = inst;
+  return PHX_OK;
+}
+
+int phx_instance_sizes(phx_instance inst, int64_t* ndof, int64_t* nnz, int64_t* nlo, int64_t* nfull) {
+  if (!inst) return set_err(PHX_EINVAL, "inst is NULL");
+  if (ndof) *ndof = 3 * (int64_t)inst->dev.n;
+  if (nnz) *nnz = 9 * (int64_t)inst->dev.nlo;
+  if (nlo) *nlo = inst->dev.nlo;
+  if (nfull) *nfull = 2 * (int64_t)inst->dev.nlo - inst->dev.n;
+  return PHX_OK;
+}
+
+int phx_instance_set_positions(phx_instance inst, const double* x) {
+  if (!inst || !x) return set_err(PHX_EINVAL, "NULL argument");
+  return upload_x(inst, x, inst->dev.x);
+}
+int phx_instance_get_positions(phx_instance inst, double* x) {
+  if (!inst || !x) return set_err(PHX_EINVAL, "NULL argument");
+  return download_x(inst, inst->dev.x, x);
+}
+int phx_instance_set_velocities(phx_instance inst, const double* v) {
+  if (!inst || !v) return set_err(PHX_EINVAL, "NULL argument");
+  return upload_x(inst, v, inst->dev.v);
+}
+int phx_instance_get_velocities(phx_instance inst, double* v) {
+  if (!inst || !v) return set_err(PHX_EINVAL, "NULL argument");
+  return download_x(inst, inst->dev.v, v);
+}
+
+int phx_instance_update_load(phx_instance inst, const double* force, const double* gravity) {
+  if (!inst) return set_err(PHX_EINVAL, "inst is NULL");
+  if (inst->in_server) return set_err(PHX_EBUSY, "instance is admitted to a server");
+  HostPattern& hp = inst->hp;
+  if (force) inst->force.assign(force, force + 3 * (size_t)hp.n);
+  if (gravity) for (int c = 0; c < 3; ++c) inst->gravity[c] = gravity[c];
+  MeshIn in;
+  in.n = hp.n;
+  in.force = inst->force.empty() ? nullptr : inst->force.data();
+  for (int c = 0; c < 3; ++c) in.gravity[c] = inst->gravity[c];
+  rebuild_load(in, hp);
+  CU(cudaMemcpyAsync(inst->dev.hlin, hp.hlin.data(), hp.hlin.size() * sizeof(double), cudaMemcpyHostToDevice,
+                     inst->ctx->stream));
+  CU(cudaStreamSynchronize(inst->ctx->stream));
+  return PHX_OK;
+}
+
+int phx_hessian_pattern(phx_instance inst, int32_t* colptr, int32_t* rowidx) {
+  if (!inst || !colptr || !rowidx) return set_err(PHX_EINVAL, "NULL argument");
+  const HostPattern& hp = inst->hp;
+  int64_t q = 0;
+  for (int C = 0; C < hp.n; ++C)
+    for (int b = 0; b < 3; ++b) {
+      colptr[3 * C + b] = (int32_t)q;
+      for (int k = hp.lo_colptr[C]; k < hp.lo_colptr[C + 1]; ++k) {
+        int R = hp.lo_rc[2 * (size_t)k];
+        for (int a = 0; a < 3; ++a) rowidx[q++] = 3 * R + a;
+      }
+    }
+  colptr[3 * hp.n] = (int32_t)q;
+  return PHX_OK;
+}
+
+int phx_scatter_map(phx_instance inst, int32_t* map) {
+  if (!inst || !map) return set_err(PHX_EINVAL, "NULL argument");
+  std::copy(inst->hp.scatter.begin(), inst->hp.scatter.end(), map);
+  return PHX_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Runs only the given kernels for one instance whose state is set to `phase`.
+int run_kernels(phx_instance inst, const std::vector<KernelId>& ids, bool fp64) {
+  phx_context ctx = inst->ctx;
+  BatchDev B{};
+  Grids G;
+  TRY(set_batch(ctx, {inst}, B, G));
+  for (KernelId id : ids) {
+    int grid = 1;
+    switch (id) {
+      case K_ELEM_EG: case K_ELEM_HESS: grid = G.tet; break;
+      case K_ASSEMBLE: grid = G.lob; break;
+      case K_CONTROL: grid = 1; break;
+      default: grid = G.node; break;
+    }
+    do_launch(ctx, id, grid, B, fp64);
+  }
+  CU(cudaGetLastError());
+  CU(cudaStreamSynchronize(ctx->stream));
+  return PHX_OK;
+}
+
+int eval_eg(phx_instance inst, const double* x, int nofix, NState* s) {
+  if (x) TRY(upload_x(inst, x, inst->dev.x));
+  DevOpts d{};
+  d.precision = 0;
+  CU(cudaMemcpyAsync(inst->d_opts, &d, sizeof(DevOpts), cudaMemcpyHostToDevice, inst->ctx->stream));
+  TRY(reset_state(inst, PH_EVAL, nofix, 0.0));
+  TRY(run_kernels(inst, {K_ELEM_EG, K_GATHER}, true));
+  return read_state(inst, s);
+}
+
+int eval_hess(phx_instance inst, const double* x, bool fp64, int nofix) {
+  if (x) TRY(upload_x(inst, x, inst->dev.x));
+  TRY(ensure_precision(inst, fp64));
+  DevOpts d{};
+  d.precision = fp64 ? 0 : 1;
+  d.precond = 1;
+  CU(cudaMemcpyAsync(inst->d_opts, &d, sizeof(DevOpts), cudaMemcpyHostToDevice, inst->ctx->stream));
+  TRY(reset_state(inst, PH_HESS, nofix, 0.0));
+  return run_kernels(inst, {K_ELEM_HESS, K_ASSEMBLE}, fp64);
+}
+
+}  // namespace
+
+extern "C" {
+
+int phx_energy_gradient(phx_instance inst, const double* x, double* energy, double* gradient, int32_t fix) {
+  if (!inst) return set_err(PHX_EINVAL, "inst is NULL");
+  NState s;
+  TRY(eval_eg(inst, x, fix ? 0 : 1, &s));
+  if (energy) *energy = s.E_eval;
+  if (gradient) TRY(download_x(inst, inst->dev.gn, gradient));
+  return PHX_OK;
+}
+
+int phx_hessian(phx_instance inst, const double* x, int32_t precision, double* values, int32_t fix) {
+  if (!inst || !values) return set_err(PHX_EINVAL, "NULL argument");
+  if (precision != PHX_PREC_FP64 && precision != PHX_PREC_FP32_REFINE) return set_err(PHX_EINVAL, "precision");
+  const bool fp64 = precision == PHX_PREC_FP64;
+  TRY(eval_hess(inst, x, fp64, fix ? 0 : 1));
+  const HostPattern& hp = inst->hp;
+  const size_t nv = 9 * (size_t)hp.nslots;
+  std::vector<double> H(nv);
+  if (fp64) {
+    CU(cudaMemcpy(H.data(), inst->dev.H64, nv * sizeof(double), cudaMemcpyDeviceToHost));
+  } else {
+    std::vector<float> Hf(nv);
+    CU(cudaMemcpy(Hf.data(), inst->dev.H32, nv * sizeof(float), cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < nv; ++k) H[k] = Hf[k];
+  }
+  // CSC position of lower block k entry (a, b): column 3C+b starts at 9*lo_colptr[C] + 3*b*len(C)
+  for (int C = 0; C < hp.n; ++C) {
+    const int k0 = hp.lo_colptr[C], len = hp.lo_colptr[C + 1] - k0;
+    for (int k = k0; k < k0 + len; ++k)
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+          size_t pos = 9 * (size_t)k0 + 3 * (size_t)b * len + 3 * (size_t)(k - k0) + a;
+          values[pos] = H[sell_addr(hp.lo_slot[k], a * 3 + b)];
+        }
+  }
+  return PHX_OK;
+}
+
+int phx_element_local(phx_instance inst, const double* x, int32_t precision, double* E, double* g, double* Hout) {
+  if (!inst) return set_err(PHX_EINVAL, "inst is NULL");
+  if (precision != PHX_PREC_FP64 && precision != PHX_PREC_FP32_REFINE) return set_err(PHX_EINVAL, "precision");
+  const int m = inst->dev.m;
+  NState s;
+  TRY(eval_eg(inst, x, 0, &s));
+  if (E) CU(cudaMemcpy(E, inst->dev.Eloc, m * sizeof(double), cudaMemcpyDeviceToHost));
+  if (g) CU(cudaMemcpy(g, inst->dev.Gloc, 12 * (size_t)m * sizeof(double), cudaMemcpyDeviceToHost));
+  if (Hout) {
+    const bool fp64 = precision == PHX_PREC_FP64;
+    TRY(eval_hess(inst, nullptr, fp64, 0));
+    std::vector<double> Hl(90 * (size_t)m);
+    if (fp64) {
+      CU(cudaMemcpy(Hl.data(), inst->dev.Hloc64, Hl.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    } else {
+      std::vector<float> Hf(Hl.size());
+      CU(cudaMemcpy(Hf.data(), inst->dev.Hloc32, Hf.size() * sizeof(float), cudaMemcpyDeviceToHost));
+      for (size_t k = 0; k < Hf.size(); ++k) Hl[k] = Hf[k];
+    }
+    const int32_t* T = inst->hp.tets.data();
+    for (int e = 0; e < m; ++e) {
+      double* He = Hout + 144 * (size_t)e;
+      for (int p = 0; p < 10; ++p) {
+        int li = kPairI[p], lj = kPairJ[p];
+        bool keep = T[4 * (size_t)e + li] >= T[4 * (size_t)e + lj];  // block stored as (li, lj)
+        const double* blk = &Hl[90 * (size_t)e + 9 * p];
+        for (int a = 0; a < 3; ++a)
+          for (int b = 0; b < 3; ++b) {
+            double v = blk[a * 3 + b];
+            int r = keep ? 3 * li + a : 3 * lj + a;
+            int c = keep ? 3 * lj + b : 3 * li + b;
+            He[r * 12 + c] = v;
+            He[c * 12 + r] = v;
+          }
+      }
+    }
+  }
+  return PHX_OK;
+}
+
+int phx_solve_static(phx_instance inst, const phx_options* o, double* x, phx_report* rep) {
+  if (!inst) return set_err(PHX_EINVAL, "inst is NULL");
+  if (inst->in_server) return set_err(PHX_EBUSY, "instance is admitted to a server");
+  auto t0 = clk::now();
+  if (x) TRY(upload_x(inst, x, inst->dev.x));
+  TRY(start_solve(inst, o, false, 0.0, 0));
+  TRY(run_to_completion(inst->ctx, {inst}, o->precision == PHX_PREC_FP64, o->pcg_chunk));
+  NState s;
+  TRY(read_state(inst, &s));
+  if (x) TRY(download_x(inst, inst->dev.x, x));
+  fill_report(s, false, std::chrono::duration<double>(clk::now() - t0).count(), rep);
+  return PHX_OK;
+}
+
+int phx_solve_step(phx_instance inst, const phx_options* o, double* x, phx_report* rep) {
+  if (!inst) return set_err(PHX_EINVAL, "inst is NULL");
+  if (inst->in_server) return set_err(PHX_EBUSY, "instance is admitted to a server");
+  auto t0 = clk::now();
+  if (x) TRY(upload_x(inst, x, inst->dev.x));
+  TRY(start_solve(inst, o, false, 0.0, 1));
+  TRY(run_to_completion(inst->ctx, {inst}, o->precision == PHX_PREC_FP64, o->pcg_chunk));
+  NState s;
+  TRY(read_state(inst, &s));
+  if (x) TRY(download_x(inst, inst->dev.x, x));
+  fill_report(s, true, std::chrono::duration<double>(clk::now() - t0).count(), rep);
+  return PHX_OK;
+}
+
+int phx_dynamic_step(phx_instance inst, const phx_options* o, double dt, double* x, double* v, phx_report* rep) {
+  if (!inst) return set_err(PHX_EINVAL, "inst is NULL");
+  if (!(dt > 0)) return set_err(PHX_EINVAL, "dt must be positive");
+  if (inst->in_server) return set_err(PHX_EBUSY, "instance is admitted to a server");
+  auto t0 = clk::now();
+  if (x) TRY(upload_x(inst, x, inst->dev.x));
+  if (v) TRY(upload_x(inst, v, inst->dev.v));
+  TRY(start_solve(inst, o, true, dt, 0));
+  TRY(run_to_completion(inst->ctx, {inst}, o->precision == PHX_PREC_FP64, o->pcg_chunk));
+  NState s;
+  TRY(read_state(inst, &s));
+  if (x) TRY(download_x(inst, inst->dev.x, x));
+  if (v) TRY(download_x(inst, inst->dev.v, v));
+  fill_report(s, false, std::chrono::duration<double>(clk::now() - t0).count(), rep);
+  return PHX_OK;
+}
+
+int phx_batch_solve(phx_context ctx, int32_t count, phx_instance* insts, const phx_options* o, double* const* x,
+                    phx_report* reps) {
+  if (!ctx || count < 0 || (count > 0 && !insts)) return set_err(PHX_EINVAL, "bad arguments");
+  auto t0 = clk::now();
+  std::vector<phx_instance> list(insts, insts + count);
+  for (int i = 0; i < count; ++i) {
+    if (!list[i] || list[i]->ctx != ctx) return set_err(PHX_EINVAL, "instance from another context");
+    if (list[i]->in_server) return set_err(PHX_EBUSY, "instance is admitted to a server");
+    for (int j = 0; j < i; ++j)
+      if (list[j] == list[i]) return set_err(PHX_EINVAL, "instance listed twice");
+    if (x && x[i]) TRY(upload_x(list[i], x[i], list[i]->dev.x));
+    TRY(start_solve(list[i], o, false, 0.0, 0));
+  }
+  if (count == 0) return PHX_OK;
+  TRY(run_to_completion(ctx, list, o->precision == PHX_PREC_FP64, o->pcg_chunk));
+  double secs = std::chrono::duration<double>(clk::now() - t0).count();
+  for (int i = 0; i < count; ++i) {
+    NState s;
+    TRY(read_state(list[i], &s));
+    if (x && x[i]) TRY(download_x(list[i], list[i]->dev.x, x[i]));
+    if (reps) fill_report(s, false, secs, &reps[i]);
+  }
+  return PHX_OK;
+}
+
+int phx_batch_dynamic_step(phx_context ctx, int32_t count, phx_instance* insts, const phx_options* o, double dt,
+                           phx_report* reps) {
+  if (!ctx || count < 0 || (count > 0 && !insts)) return set_err(PHX_EINVAL, "bad arguments");
+  if (!(dt > 0)) return set_err(PHX_EINVAL, "dt must be positive");
+  auto t0 = clk::now();
+  std::vector<phx_instance> list(insts, insts + count);
+  for (int i = 0; i < count; ++i) {
+    if (!list[i] || list[i]->ctx != ctx) return set_err(PHX_EINVAL, "instance from another context");
+    if (list[i]->in_server) return set_err(PHX_EBUSY, "instance is admitted to a server");
+    for (int j = 0; j < i; ++j)
+      if (list[j] == list[i]) return set_err(PHX_EINVAL, "instance listed twice");
+    TRY(start_solve(list[i], o, true, dt, 0));
+  }
+  if (count == 0) return PHX_OK;
+  TRY(run_to_completion(ctx, list, o->precision == PHX_PREC_FP64, o->pcg_chunk));
+  double secs = std::chrono::duration<double>(clk::now() - t0).count();
+  for (int i = 0; i < count; ++i) {
+    NState s;
+    TRY(read_state(list[i], &s));
+    if (reps) fill_report(s, false, secs, &reps[i]);
+  }
+  return PHX_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// serving: continuous batching
+// ===========================================================================
+struct phx_server_s {
+  phx_context ctx = nullptr;
+  int max_slots = 0;
+  int64_t budget = 0, in_use = 0;
+  phx_options opts{};
+  bool fp64 = true;
+  struct Req { phx_instance inst; int64_t tag; clk::time_point t_submit; };
+  std::deque<Req> queue;
+  std::vector<Req> active;
+  struct Done { int64_t tag; phx_report rep; };
+  std::deque<Done> done;
+  bool dirty = true;
+  BatchDev B{};
+  Grids G;
+};
+
+extern "C" {
+
+int phx_server_create(phx_context ctx, int32_t max_slots, int64_t budget, const phx_options* o, phx_server* out) {
+  if (!ctx || !out || max_slots < 1) return set_err(PHX_EINVAL, "bad arguments");
+  TRY(validate_opts(o));
+  auto* s = new phx_server_s();
+  s->ctx = ctx;
+  s->max_slots = max_slots;
+  s->budget = budget > 0 ? budget : (int64_t)ctx->arena.cap;
+  s->opts = *o;
+  s->fp64 = o->precision == PHX_PREC_FP64;
+  *out = s;
+  return PHX_OK;
+}
+
+int phx_server_destroy(phx_server s) {
+  if (!s) return PHX_OK;
+  cudaStreamSynchronize(s->ctx->stream);
+  for (auto& r : s->active) r.inst->in_server = false;
+  for (auto& r : s->queue) r.inst->in_server = false;
+  delete s;
+  return PHX_OK;
+}
+
+int phx_server_submit(phx_server s, phx_instance inst, int64_t tag) {
+  if (!s || !inst || inst->ctx != s->ctx) return set_err(PHX_EINVAL, "bad arguments");
+  if (inst->in_server) return set_err(PHX_EBUSY, "instance already queued or active");
+  if (inst->bytes > s->budget) return set_err(PHX_ENOMEM, "instance larger than the server budget");
+  inst->in_server = true;
+  s->queue.push_back({inst, tag, clk::now()});
+  return PHX_OK;
+}
+
+int phx_server_progress(phx_server s, int32_t* active, int32_t* queued) {
+  if (!s) return set_err(PHX_EINVAL, "server is NULL");
+  // retire finished requests (phases from the last round of this server)
+  if (!s->active.empty() && !s->dirty && s->ctx->batch_owner == s) {
+    std::vector<phx_server_s::Req> keep;
+    for (size_t i = 0; i < s->active.size(); ++i) {
+      if (s->ctx->h_flags[8 + i] == PH_DONE) {
+        auto& r = s->active[i];
+        NState st;
+        TRY(read_state(r.inst, &st));
+        phx_report rep{};
+        fill_report(st, false, std::chrono::duration<double>(clk::now() - r.t_submit).count(), &rep);
+        s->done.push_back({r.tag, rep});
+        r.inst->in_server = false;
+        s->in_use -= r.inst->bytes;
+        s->dirty = true;
+      } else {
+        keep.push_back(s->active[i]);
+      }
+    }
+    s->active.swap(keep);
+  }
+  // admit queued requests at this Newton-round boundary (slots + memory budget)
+  while (!s->queue.empty() && (int)s->active.size() < s->max_slots) {
+    auto& r = s->queue.front();
+    if (s->in_use + r.inst->bytes > s->budget) break;
+    TRY(start_solve(r.inst, &s->opts, false, 0.0, 0));
+    s->in_use += r.inst->bytes;
+    s->active.push_back(r);
+    s->queue.pop_front();
+    s->dirty = true;
+  }
+  if (!s->active.empty()) {
+    if (s->dirty || s->ctx->batch_owner != s) {
+      std::vector<phx_instance> list;
+      for (auto& r : s->active) list.push_back(r.inst);
+      TRY(set_batch(s->ctx, list, s->B, s->G));
+      s->ctx->batch_owner = s;
+      s->dirty = false;
+    }
+    run_round(s->ctx, s->B, s->G, s->fp64, s->opts.pcg_chunk);
+    CU(cudaGetLastError());
+    TRY(read_flags(s->ctx, (int)s->active.size()));
+  }
+  if (active) *active = (int32_t)s->active.size();
+  if (queued) *queued = (int32_t)s->queue.size();
+  return PHX_OK;
+}
+
+int phx_server_poll(phx_server s, int64_t* tags, phx_report* reps, int32_t cap) {
+  if (!s) return set_err(PHX_EINVAL, "server is NULL");
+  int n = 0;
+  while (n < cap && !s->done.empty()) {
+    if (tags) tags[n] = s->done.front().tag;
+    if (reps) reps[n] = s->done.front().rep;
+    s->done.pop_front();
+    ++n;
+  }
+  return n;
+}
+
+// ---- profiling -------------------------------------------------------------
+int phx_profile_enable(phx_context ctx, int32_t on) {
+  if (!ctx) return set_err(PHX_EINVAL, "ctx is NULL");
+  ctx->profiling = on != 0;
+  return PHX_OK;
+}
+
+static int collect_events(phx_context ctx) {
+  CU(cudaStreamSynchronize(ctx->stream));
+  for (auto& ev : ctx->evs) {
+    float ms = 0;
+    CU(cudaEventElapsedTime(&ms, ev.a, ev.b));
+    ctx->prof_ms[ev.kind] += ms;
+    ctx->prof_n[ev.kind]++;
+    ctx->pool.push_back(ev.a);
+    ctx->pool.push_back(ev.b);
+  }
+  ctx->evs.clear();
+  return PHX_OK;
+}
+
+int phx_profile_read(phx_context ctx, const char* kind, int64_t* launches, double* total_ms) {
+  if (!ctx || !kind) return set_err(PHX_EINVAL, "bad arguments");
+  TRY(collect_events(ctx));
+  for (int k = 0; k < K_COUNT; ++k)
+    if (std::strcmp(kernel_name((KernelId)k), kind) == 0) {
+      if (launches) *launches = ctx->prof_n[k];
+      if (total_ms) *total_ms = ctx->prof_ms[k];
+      return PHX_OK;
+    }
+  return set_err(PHX_ENOTFOUND, std::string("unknown kernel kind ") + kind);
+}
+
+int phx_profile_reset(phx_context ctx) {
+  if (!ctx) return set_err(PHX_EINVAL, "ctx is NULL");
+  TRY(collect_events(ctx));
+  for (int k = 0; k < K_COUNT; ++k) { ctx->prof_ms[k] = 0; ctx->prof_n[k] = 0; }
+  ctx->launches = 0;
+  return PHX_OK;
+}
+
+int64_t phx_kernel_launches(phx_context ctx) { return ctx ? ctx->launches : -1; }
+
+}  // extern "C"

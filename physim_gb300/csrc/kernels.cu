@@ -1,0 +1,979 @@
+// kernels.cu -- sm_103a kernels of the tet-FEM Newton path.
+//
+// Every kernel is persistent over a packed tile index of the active batch:
+// tiles of 128 tets, 128 nodes (4 SELL chunks of 32 rows) or 128 lower blocks,
+// numbered instance by instance through prefix arrays, so uneven meshes share
+// one launch.  A kernel touches only the instances whose Newton state is in
+// the phase it serves; the others' tiles are skipped.  Per-instance reductions
+// are deterministic: each tile writes its partial sums, and the CTA that
+// finishes an instance's last tile (counted with one atomic) sums the partials
+// in tile order and advances that instance's state.  Nothing waits on another
+// CTA, so no kernel here can hang.
+//
+// Reference behaviour each kernel restates:
+//   k_elem_eg     EnergyElement_FEM::ComputeAndStore_{Energy,Gradient}_Internal
+//                 (source/PhySim/Physics/Elements/EnergyElement_FEM.cpp:125-191),
+//                 inverted element -> energy HUGE_VAL (:126-131)
+//   k_gather      Simulable::AddGradient / AddEnergy order (Simulable.cpp:321-521),
+//                 lumped-mass gravity (MassElement_Lumped.cpp:56-76), nodal forces
+//                 (EnergyElement_Force.cpp:43-56), FixVectorDoFs (Simulable.cpp:735-744),
+//                 implicit-Euler inertia (OptimProblem_BasicDynamic.cpp:58-101)
+//   k_elem_hess   EnergyElement_FEM::ComputeAndStore_Hessian_Internal (:193-222)
+//   k_assemble    DerivativeAssembler::AssembleHessian + AMatrixSd static blocks
+//                 (DerivativeAssembler.cpp:268-300, BasicTypes.cpp:45-62) and
+//                 FixMatrixDoFs (Simulable.cpp:746-760); + M/dt^2 for dynamics
+//   k_jacobi ... k_accum   LinearSolver_EigenCG::SolveInternal (LinearSolver_EigenCG.cpp:51-125)
+//                 with a 3x3 block-Jacobi (or Eigen's diagonal) preconditioner and,
+//                 on the FP32 path, FP64 residual refinement sweeps.
+#include <cfloat>
+#include <cstdint>
+
+#include "kernels.h"
+#include "newton_control.h"
+
+namespace phx {
+
+// ---------------------------------------------------------------------------
+// small helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int find_tile(const int32_t* pre, int num, int t) {
+  int lo = 0, hi = num;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (__ldg(pre + mid) <= t) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ int tiles_of(int count) { return (count + kTile - 1) / kTile; }
+
+template <int K>
+__device__ __forceinline__ void block_sum(double (&v)[K], double* sm) {
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], off);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < K; ++k) sm[warp * K + k] = v[k];
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      v[k] = lane < nw ? sm[lane * K + k] : 0.0;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], off);
+    }
+  }
+}
+
+// Records this tile's partial sums; in the CTA that completes the instance's
+// last tile, returns true and leaves the instance totals in thread 0's tot[].
+template <int K>
+__device__ bool tile_done(const InstDev& I, int lt, int ntiles, double (&v)[K], double (&tot)[K],
+                          double* sm, int* flag) {
+  block_sum<K>(v, sm);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) I.partials[(size_t)lt * K + k] = v[k];
+    __threadfence();
+    unsigned prev = atomicAdd(I.counter, 1u);
+    *flag = (prev == (unsigned)(ntiles - 1));
+  }
+  __syncthreads();
+  if (!*flag) return false;
+  __threadfence();
+  double acc[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) acc[k] = 0.0;
+  for (int t = threadIdx.x; t < ntiles; t += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[k] += __ldcg(I.partials + (size_t)t * K + k);
+  block_sum<K>(acc, sm);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) tot[k] = acc[k];
+    *I.counter = 0u;
+  }
+  return true;
+}
+
+__device__ __forceinline__ void ld4(const double* p, int64_t v, double (&o)[3]) {
+  const double2* q = reinterpret_cast<const double2*>(p) + 2 * v;
+  double2 a = q[0], b = q[1];
+  o[0] = a.x; o[1] = a.y; o[2] = b.x;
+}
+__device__ __forceinline__ void st4(double* p, int64_t v, const double (&o)[3]) {
+  double2* q = reinterpret_cast<double2*>(p) + 2 * v;
+  q[0] = make_double2(o[0], o[1]);
+  q[1] = make_double2(o[2], 0.0);
+}
+__device__ __forceinline__ void ld4(const float* p, int64_t v, float (&o)[3]) {
+  float4 a = reinterpret_cast<const float4*>(p)[v];
+  o[0] = a.x; o[1] = a.y; o[2] = a.z;
+}
+__device__ __forceinline__ void st4(float* p, int64_t v, const float (&o)[3]) {
+  reinterpret_cast<float4*>(p)[v] = make_float4(o[0], o[1], o[2], 0.f);
+}
+
+template <typename T> struct PcgBufs;
+template <> struct PcgBufs<float> {
+  __device__ static float* H(const InstDev& I) { return I.H32; }
+  __device__ static float* Hloc(const InstDev& I) { return I.Hloc32; }
+  __device__ static float* r(const InstDev& I) { return I.r32; }
+  __device__ static float* z(const InstDev& I) { return I.z32; }
+  __device__ static float* pa(const InstDev& I) { return I.p32a; }
+  __device__ static float* pb(const InstDev& I) { return I.p32b; }
+  __device__ static float* q(const InstDev& I) { return I.q32; }
+  __device__ static float* e(const InstDev& I) { return I.e32; }
+  __device__ static float* minv(const InstDev& I) { return I.minv32; }
+  __device__ static const float* rest(const InstDev& I) { return I.rest32; }
+};
+template <> struct PcgBufs<double> {
+  __device__ static double* H(const InstDev& I) { return I.H64; }
+  __device__ static double* Hloc(const InstDev& I) { return I.Hloc64; }
+  __device__ static double* r(const InstDev& I) { return I.rd; }
+  __device__ static double* z(const InstDev& I) { return I.zd; }
+  __device__ static double* pa(const InstDev& I) { return I.pda; }
+  __device__ static double* pb(const InstDev& I) { return I.pdb; }
+  __device__ static double* q(const InstDev& I) { return I.qd; }
+  __device__ static double* e(const InstDev& I) { return I.ed; }
+  __device__ static double* minv(const InstDev& I) { return I.minvd; }
+  __device__ static const double* rest(const InstDev& I) { return I.rest64; }
+};
+
+template <typename T> __device__ __forceinline__ T dlog(T x);
+template <> __device__ __forceinline__ float dlog<float>(float x) { return logf(x); }
+template <> __device__ __forceinline__ double dlog<double>(double x) { return log(x); }
+
+template <typename T>
+__device__ __forceinline__ T det3(const T* F) {
+  return F[0] * (F[4] * F[8] - F[7] * F[5]) - F[3] * (F[1] * F[8] - F[7] * F[2]) +
+         F[6] * (F[1] * F[5] - F[4] * F[2]);
+}
+
+// cofactor matrix, column-major: C(i,j) = C[i + 3j]
+template <typename T>
+__device__ __forceinline__ void cof3(const T* F, T* C) {
+  C[0] = F[4] * F[8] - F[7] * F[5];
+  C[1] = F[6] * F[5] - F[3] * F[8];
+  C[2] = F[3] * F[7] - F[6] * F[4];
+  C[3] = F[7] * F[2] - F[1] * F[8];
+  C[4] = F[0] * F[8] - F[6] * F[2];
+  C[5] = F[6] * F[1] - F[0] * F[7];
+  C[6] = F[1] * F[5] - F[4] * F[2];
+  C[7] = F[3] * F[2] - F[0] * F[5];
+  C[8] = F[0] * F[4] - F[3] * F[1];
+}
+
+// Loads a tet: node ids, rest data, and Ds = [x1-x0, x2-x0, x3-x0] in FP64.
+__device__ __forceinline__ void load_ds(const InstDev& I, int e, int (&nd)[4], double (&Ds)[9]) {
+  int4 t = reinterpret_cast<const int4*>(I.tets)[e];
+  nd[0] = t.x; nd[1] = t.y; nd[2] = t.z; nd[3] = t.w;
+  double x0[3], xa[3];
+  ld4(I.x, nd[0], x0);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    ld4(I.x, nd[c + 1], xa);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) Ds[r + 3 * c] = xa[r] - x0[r];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// vector ops of the state machine
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kTile) k_vecop(BatchDev B) {
+  __shared__ double sm[32 * 1];
+  __shared__ int flag;
+  const int num = *B.num;
+  const int total = B.pre_node[num];
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int i = find_tile(B.pre_node, num, t), lt = t - B.pre_node[i];
+    const InstDev& I = B.inst[i];
+    NState* st = I.st;
+    if (st->phase != PH_VEC) continue;
+    const int ops = st->vecop;
+    const double a = st->alpha_trial, dt = I.opts->dt;
+    const int v = lt * kTile + threadIdx.x;
+    if (v < I.n) {
+      double x[3], xs[3], dx[3], tmp[3], tmp2[3];
+      ld4(I.x, v, x);
+      if (ops & VO_PRED) {
+        double vv[3];
+        ld4(I.v, v, vv);
+        st4(I.x0, v, x);
+        st4(I.v0, v, vv);
+        for (int c = 0; c < 3; ++c) x[c] = x[c] + dt * vv[c];
+        st4(I.x, v, x);
+      }
+      if (ops & VO_RESTORE) {
+        ld4(I.xs, v, x);
+        st4(I.x, v, x);
+      }
+      if (ops & (VO_ACCEPT | VO_GCOPY)) {
+        ld4(I.gn, v, tmp);
+        st4(I.g, v, tmp);
+      }
+      if (ops & VO_ACCEPT) {
+        ld4(I.dx, v, dx);
+        for (int c = 0; c < 3; ++c) tmp2[c] = a * dx[c];
+        st4(I.dxprev, v, tmp2);
+      }
+      if (ops & VO_SAVE) st4(I.xs, v, x);
+      if (ops & VO_ZERODX) {
+        for (int c = 0; c < 3; ++c) tmp[c] = 0.0;
+        st4(I.dx, v, tmp);
+      }
+      if (ops & VO_STEEP) {
+        ld4(I.g, v, tmp);
+        for (int c = 0; c < 3; ++c) tmp[c] = -tmp[c];
+        st4(I.dx, v, tmp);
+      }
+      if (ops & VO_TRIAL) {
+        ld4(I.xs, v, xs);
+        ld4(I.dx, v, dx);
+        for (int c = 0; c < 3; ++c) x[c] = xs[c] + a * dx[c];
+        st4(I.x, v, x);
+      }
+      if (ops & VO_VEL) {
+        double x0[3];
+        ld4(I.x0, v, x0);
+        for (int c = 0; c < 3; ++c) tmp[c] = (x[c] - x0[c]) / dt;
+        st4(I.v, v, tmp);
+      }
+    }
+    double p[1] = {0.0}, tot[1];
+    if (tile_done<1>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
+      st->phase = st->next_phase;
+      st->vecop = 0;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// element energy + gradient (FP64)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void material_eg(int model, double lam, double mu, const double* F, double* psi,
+                                            double* P) {
+  if (model == 1) {
+    // Saint-Venant Kirchhoff: E = (F^T F - I)/2, S = lam tr(E) I + 2 mu E, P = F S
+    double E[9];
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+        E[i + 3 * j] = 0.5 * (F[0 + 3 * i] * F[0 + 3 * j] + F[1 + 3 * i] * F[1 + 3 * j] + F[2 + 3 * i] * F[2 + 3 * j]);
+    E[0] -= 0.5; E[4] -= 0.5; E[8] -= 0.5;
+    double trE = E[0] + E[4] + E[8];
+    double ee = 0;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) ee += E[k] * E[k];
+    *psi = 0.5 * lam * trE * trE + mu * ee;
+    double S[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) S[k] = 2.0 * mu * E[k];
+    S[0] += lam * trE; S[4] += lam * trE; S[8] += lam * trE;
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int i = 0; i < 3; ++i) P[i + 3 * j] = F[i] * S[3 * j] + F[i + 3] * S[1 + 3 * j] + F[i + 6] * S[2 + 3 * j];
+  } else {
+    // compressible Neo-Hookean: psi = mu/2 (I1 - 3 - log J^2) + lam/8 (log J^2)^2
+    double J = det3(F);
+    double logJ2 = log(J * J);
+    double I1 = 0;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) I1 += F[k] * F[k];
+    *psi = mu * (I1 - 3.0 - logJ2) / 2.0 + lam * logJ2 * logJ2 / 8.0;
+    double C[9];
+    cof3(F, C);
+    double c = (0.5 * lam * logJ2 - mu) / J;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) P[k] = mu * F[k] + c * C[k];
+  }
+}
+
+__global__ void __launch_bounds__(kTile) k_elem_eg(BatchDev B) {
+  __shared__ double sm[32];
+  __shared__ int flag;
+  const int num = *B.num;
+  const int total = B.pre_tet[num];
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int i = find_tile(B.pre_tet, num, t), lt = t - B.pre_tet[i];
+    const InstDev& I = B.inst[i];
+    NState* st = I.st;
+    if (st->phase != PH_EVAL) continue;
+    const int e = lt * kTile + threadIdx.x;
+    double Ee = 0.0;
+    if (e < I.m) {
+      int nd[4];
+      double Ds[9];
+      load_ds(I, e, nd, Ds);
+      double R[12];
+      const double2* r2 = reinterpret_cast<const double2*>(I.rest64 + 12 * (size_t)e);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) { double2 q = r2[k]; R[2 * k] = q.x; R[2 * k + 1] = q.y; }
+      double F[9];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+          F[r + 3 * c] = Ds[r] * R[0 + 3 * c] + Ds[r + 3] * R[1 + 3 * c] + Ds[r + 6] * R[2 + 3 * c];
+      const double w = R[9], lam = R[10], mu = R[11];
+      double psi, P[9];
+      material_eg(I.model[e], lam, mu, F, &psi, P);
+      Ee = (det3(Ds) / 6.0 < 0.0) ? __longlong_as_double(0x7ff0000000000000LL) : psi * w;
+      // g_a = w * P * B_a, B_a = row (a-1) of Dm^-1, B_0 = -(B_1 + B_2 + B_3)
+      double g[12];
+#pragma unroll
+      for (int a = 1; a < 4; ++a)
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+          g[3 * a + r] = (P[r] * R[(a - 1)] + P[r + 3] * R[(a - 1) + 3] + P[r + 6] * R[(a - 1) + 6]) * w;
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        double b0 = -(R[0] + R[1] + R[2]), b1 = -(R[3] + R[4] + R[5]), b2 = -(R[6] + R[7] + R[8]);
+        g[r] = (P[r] * b0 + P[r + 3] * b1 + P[r + 6] * b2) * w;
+      }
+      double2* go = reinterpret_cast<double2*>(I.Gloc + 12 * (size_t)e);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) go[k] = make_double2(g[2 * k], g[2 * k + 1]);
+      I.Eloc[e] = Ee;
+    }
+    double p[1] = {Ee}, tot[1];
+    if (tile_done<1>(I, lt, tiles_of(I.m), p, tot, sm, &flag) && threadIdx.x == 0) st->E_el = tot[0];
+  }
+}
+
+// node gather of element gradients + linear loads (+ inertia), energy and ||g||^2
+__global__ void __launch_bounds__(kTile) k_gather(BatchDev B) {
+  __shared__ double sm[32 * 2];
+  __shared__ int flag;
+  const int num = *B.num;
+  const int total = B.pre_node[num];
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int i = find_tile(B.pre_node, num, t), lt = t - B.pre_node[i];
+    const InstDev& I = B.inst[i];
+    NState* st = I.st;
+    if (st->phase != PH_EVAL) continue;
+    const int v = lt * kTile + threadIdx.x;
+    double p[2] = {0.0, 0.0};
+    if (v < I.n) {
+      double g[3] = {0.0, 0.0, 0.0};
+      const int c0 = I.nseg_ptr[v], c1 = I.nseg_ptr[v + 1];
+      for (int c = c0; c < c1; ++c) {
+        const double* src = I.Gloc + 3 * (size_t)I.nseg_c[c];
+        g[0] += src[0]; g[1] += src[1]; g[2] += src[2];
+      }
+      double h[3], x[3];
+      ld4(I.hlin, v, h);
+      ld4(I.x, v, x);
+      double elin = x[0] * h[0] + x[1] * h[1] + x[2] * h[2];
+      for (int c = 0; c < 3; ++c) g[c] += h[c];
+      if (I.opts->dynamic) {
+        const double dt = I.opts->dt, m = I.mass[v];
+        double x0[3], v0[3], acc = 0.0;
+        ld4(I.x0, v, x0);
+        ld4(I.v0, v, v0);
+        for (int c = 0; c < 3; ++c) {
+          double a = (x[c] - x0[c]) / (dt * dt) - v0[c] / dt;
+          g[c] += m * a;
+          acc += a * (m * a);
+        }
+        elin += (dt * dt / 2.0) * acc;
+      }
+      if (!st->nofix) {
+        const int fm = I.fixmask[v];
+        for (int c = 0; c < 3; ++c)
+          if (fm & (1 << c)) g[c] = 0.0;
+      }
+      st4(I.gn, v, g);
+      p[0] = elin;
+      p[1] = g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
+    }
+    double tot[2];
+    if (tile_done<2>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
+      st->E_eval = st->E_el + tot[0];
+      st->gg_eval = tot[1];
+      st->phase = PH_EVAL_DONE;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// element Hessian: the 10 node blocks of H_e = w DFDx^T dP/dF DFDx in closed form.
+// With B_a the shape-function gradients and u_a a per-node 3-vector,
+//   H_np = w [ s_np I + lam u_n u_p^T + beta u_p u_n^T + t_np M ]
+//   CoNH: u_a = F^-T B_a, s = mu B_n.B_p, beta = mu - lam/2 log J^2, t = 0
+//   StVK: u_a = F B_a,    s = B_n^T S B_p, beta = mu, t = mu B_n.B_p, M = F F^T
+// Each block is written oriented as the global lower block (row node = larger id).
+// ---------------------------------------------------------------------------
+__constant__ int c_pi[10] = {0, 1, 1, 2, 2, 2, 3, 3, 3, 3};
+__constant__ int c_pj[10] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
+
+template <typename Real>
+__device__ __forceinline__ void elem_blocks(const InstDev& I, int e, Real* out /* 90, stride 1 */) {
+  int nd[4];
+  double Ds64[9];
+  load_ds(I, e, nd, Ds64);
+  const Real* rest = PcgBufs<Real>::rest(I) + 12 * (size_t)e;
+  Real R[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) R[k] = rest[k];
+  Real Ds[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) Ds[k] = (Real)Ds64[k];
+  Real F[9];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) F[r + 3 * c] = Ds[r] * R[0 + 3 * c] + Ds[r + 3] * R[1 + 3 * c] + Ds[r + 6] * R[2 + 3 * c];
+  const Real w = R[9], lam = R[10], mu = R[11];
+  Real Bv[4][3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    Bv[1][c] = R[0 + 3 * c];
+    Bv[2][c] = R[1 + 3 * c];
+    Bv[3][c] = R[2 + 3 * c];
+    Bv[0][c] = -(Bv[1][c] + Bv[2][c] + Bv[3][c]);
+  }
+  Real u[4][3], beta, M[9], S[9];
+  const bool stvk = I.model[e] == 1;
+  if (stvk) {
+    Real E[9];
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+        E[i + 3 * j] = (Real)0.5 * (F[3 * i] * F[3 * j] + F[1 + 3 * i] * F[1 + 3 * j] + F[2 + 3 * i] * F[2 + 3 * j]);
+    E[0] -= (Real)0.5; E[4] -= (Real)0.5; E[8] -= (Real)0.5;
+    Real trE = E[0] + E[4] + E[8];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) S[k] = (Real)2 * mu * E[k];
+    S[0] += lam * trE; S[4] += lam * trE; S[8] += lam * trE;
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int i = 0; i < 3; ++i) M[i + 3 * j] = F[i] * F[j] + F[i + 3] * F[j + 3] + F[i + 6] * F[j + 6];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int m2 = 0; m2 < 3; ++m2) u[a][m2] = F[m2] * Bv[a][0] + F[m2 + 3] * Bv[a][1] + F[m2 + 6] * Bv[a][2];
+    beta = mu;
+  } else {
+    Real C[9];
+    cof3(F, C);
+    Real J = det3(F);
+    Real logJ2 = dlog<Real>(J * J);
+    Real invJ = (Real)1 / J;
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int m2 = 0; m2 < 3; ++m2)
+        u[a][m2] = (C[m2] * Bv[a][0] + C[m2 + 3] * Bv[a][1] + C[m2 + 6] * Bv[a][2]) * invJ;
+    beta = mu - (Real)0.5 * lam * logJ2;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) { M[k] = 0; S[k] = 0; }
+  }
+#pragma unroll
+  for (int p = 0; p < 10; ++p) {
+    const int li = c_pi[p], lj = c_pj[p];
+    const int n = (nd[li] >= nd[lj]) ? li : lj;
+    const int q = (nd[li] >= nd[lj]) ? lj : li;
+    const Real bb = Bv[n][0] * Bv[q][0] + Bv[n][1] * Bv[q][1] + Bv[n][2] * Bv[q][2];
+    Real s, tt;
+    if (stvk) {
+      Real SBq[3];
+#pragma unroll
+      for (int r = 0; r < 3; ++r) SBq[r] = S[r] * Bv[q][0] + S[r + 3] * Bv[q][1] + S[r + 6] * Bv[q][2];
+      s = Bv[n][0] * SBq[0] + Bv[n][1] * SBq[1] + Bv[n][2] * SBq[2];
+      tt = mu * bb;
+    } else {
+      s = mu * bb;
+      tt = 0;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        Real val = lam * u[n][a] * u[q][b] + beta * u[q][a] * u[n][b] + tt * M[a + 3 * b];
+        if (a == b) val += s;
+        out[p * 9 + a * 3 + b] = val * w;
+      }
+  }
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(kTile) k_elem_hess(BatchDev B) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  Real* sh = reinterpret_cast<Real*>(smraw);  // [kTile][90]
+  const int num = *B.num;
+  const int total = B.pre_tet[num];
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int i = find_tile(B.pre_tet, num, t), lt = t - B.pre_tet[i];
+    const InstDev& I = B.inst[i];
+    if (I.st->phase != PH_HESS) continue;
+    const int e0 = lt * kTile;
+    const int cnt = min(kTile, I.m - e0);
+    if ((int)threadIdx.x < cnt) elem_blocks<Real>(I, e0 + threadIdx.x, sh + threadIdx.x * 90);
+    __syncthreads();
+    Real* dst = PcgBufs<Real>::Hloc(I) + (size_t)e0 * 90;
+    for (int k = threadIdx.x; k < cnt * 90; k += blockDim.x) dst[k] = sh[k];
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// assembly: one 9-lane group per lower block sums its contributions in element
+// order (the segment list), applies inertia and FixMatrixDoFs, and writes the
+// block and its transpose into the SELL matrix; ||A||_F^2 of the stored lower
+// entries is reduced for the regularisation threshold (LinearSolver.cpp:57-66).
+// ---------------------------------------------------------------------------
+template <typename Real>
+__global__ void __launch_bounds__(288) k_assemble(BatchDev B) {
+  __shared__ double sm[32];
+  __shared__ int flag;
+  const int num = *B.num;
+  const int total = B.pre_lob[num];
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int i = find_tile(B.pre_lob, num, t), lt = t - B.pre_lob[i];
+    const InstDev& I = B.inst[i];
+    NState* st = I.st;
+    if (st->phase != PH_HESS) continue;
+    const Real* Hloc = PcgBufs<Real>::Hloc(I);
+    Real* H = PcgBufs<Real>::H(I);
+    const bool dyn = I.opts->dynamic != 0, nofix = st->nofix != 0;
+    const double dt = I.opts->dt;
+    const int ent = threadIdx.x % 9, a = ent / 3, b = ent % 3;
+    double nrm = 0.0;
+    for (int pass = 0; pass < 4; ++pass) {
+      const int k = lt * kTile + pass * 32 + threadIdx.x / 9;
+      if (k >= I.nlo) continue;
+      Real s = 0;
+      const int c0 = I.seg_ptr[k], c1 = I.seg_ptr[k + 1];
+      for (int c = c0; c < c1; ++c) s += Hloc[(size_t)I.seg_c[c] * 9 + ent];
+      const int R = I.lo_rc[2 * k], C = I.lo_rc[2 * k + 1];
+      if (dyn && R == C && a == b) s += (Real)(I.mass[R] / (dt * dt));
+      if (!nofix) {
+        const bool fr = (I.fixmask[R] >> a) & 1, fc = (I.fixmask[C] >> b) & 1;
+        if (fr || fc) s = (R == C && a == b) ? (Real)1 : (Real)0;
+      }
+      H[sell_addr(I.lo_slot[k], ent)] = s;
+      if (R != C) H[sell_addr(I.up_slot[k], b * 3 + a)] = s;
+      nrm += (double)s * (double)s;
+    }
+    double p[1] = {nrm}, tot[1];
+    if (tile_done<1>(I, lt, tiles_of(I.nlo), p, tot, sm, &flag) && threadIdx.x == 0) {
+      st->normA2 = tot[0];
+      st->regT = 1e-6 * sqrt(tot[0]);
+    }
+  }
+}
+
+// preconditioner: inverse of each node's 3x3 diagonal block (+ shift), or of its diagonal
+template <typename Real>
+__global__ void __launch_bounds__(kTile) k_jacobi(BatchDev B) {
+  __shared__ double sm[32];
+  __shared__ int flag;
+  const int num = *B.num;
+  const int total = B.pre_node[num];
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int i = find_tile(B.pre_node, num, t), lt = t - B.pre_node[i];
+    const InstDev& I = B.inst[i];
+    NState* st = I.st;
+    if (st->phase != PH_HESS && st->phase != PH_JACOBI) continue;
+    const int v = lt * kTile + threadIdx.x;
+    if (v < I.n) {
+      const Real* H = PcgBufs<Real>::H(I);
+      Real* Mi = PcgBufs<Real>::minv(I);
+      const int64_t s = I.diag_slot[v];
+      double D[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) D[k] = (double)H[sell_addr(s, k)];  // row-major a*3+b
+      D[0] += st->shift; D[4] += st->shift; D[8] += st->shift;
+      double inv[9];
+      if (I.opts->precond == 1) {
+        double C[9];
+        cof3(D, C);  // symmetric: cofactor == adjugate^T == adjugate
+        double d = D[0] * C[0] + D[3] * C[3] + D[6] * C[6];
+        if (d != 0.0 && isfinite(d)) {
+#pragma unroll
+          for (int k = 0; k < 9; ++k) inv[k] = C[k] / d;
+        } else {
+#pragma unroll
+          for (int k = 0; k < 9; ++k) inv[k] = (k % 4 == 0) ? 1.0 : 0.0;
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) inv[k] = 0.0;
+        inv[0] = D[0] != 0.0 ? 1.0 / D[0] : 1.0;
+        inv[4] = D[4] != 0.0 ? 1.0 / D[4] : 1.0;
+        inv[8] = D[8] != 0.0 ? 1.0 / D[8] : 1.0;
+      }
+#pragma unroll
+      for (int k = 0; k < 9; ++k) Mi[(size_t)k * I.n + v] = (Real)inv[k];
+    }
+    double p[1] = {0.0}, tot[1];
+    if (tile_done<1>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) st->phase = PH_LINSETUP;
+  }
+}
+
+// b = -g, dx = guess (previous accepted step, EigenCG solveWithGuess) or 0
+__global__ void __launch_bounds__(kTile) k_linsetup(BatchDev B) {
+  __shared__ double sm[32];
+  __shared__ int flag;
+  const int num = *B.num;
+  const int total = B.pre_node[num];
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int i = find_tile(B.pre_node, num, t), lt = t - B.pre_node[i];
+    const InstDev& I = B.inst[i];
+    NState* st = I.st;
+    if (st->phase != PH_LINSETUP) continue;
+    const int v = lt * kTile + threadIdx.x;
+    double p[1] = {0.0};
+    if (v < I.n) {
+      double g[3], d[3] = {0.0, 0.0, 0.0};
+      ld4(I.g, v, g);
+      for (int c = 0; c < 3; ++c) g[c] = -g[c];
+      st4(I.bvec, v, g);
+      if (I.opts->warm_guess) ld4(I.dxprev, v, d);
+      st4(I.dx, v, d);
+      p[0] = g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
+    }
+    double tot[1];
+    if (tile_done<1>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
+      const double tol = I.opts->ls_tol_max_error;
+      st->bb = tot[0];
+      st->thr_final = fmax(tol * tol * tot[0], DBL_MIN);
+      st->sweeps = 0;
+      st->lin_status = LIN_RUNNING;
+      if (tot[0] == 0.0) {  // zero right-hand side: x = 0
+        st->lin_status = LIN_CONVERGED;
+        st->b_dot_dx = 0.0;
+        st->dx_norm = 0.0;
+        st->vecop = VO_ZERODX;
+        st->next_phase = PH_LIN_DONE;
+        st->phase = PH_VEC;
+      } else {
+        st->phase = PH_RESID;
+      }
+    }
+  }
+}
+
+// SELL-32 row sweep: acc = sum_k H(row, col_k) * X(col_k), X given per column by a functor.
+template <typename Real, typename Acc, typename GetX>
+__device__ __forceinline__ void sell_row(const InstDev& I, const Real* H, int v, GetX getx, Acc (&acc)[3]) {
+  const int c = v >> 5, lane = v & 31;
+  const int s0 = I.chunk_off[c];
+  const int len = (I.chunk_off[c + 1] - s0) >> 5;
+  acc[0] = acc[1] = acc[2] = (Acc)0;
+  for (int k = 0; k < len; ++k) {
+    const int64_t s = (int64_t)s0 + k * 32 + lane;
+    const int col = __ldg(I.slot_col + s);
+    const Real* hp = H + (s >> 5) * 288 + (s & 31);
+    Acc h[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) h[q] = (Acc)hp[q * 32];
+    Acc xc[3];
+    getx(col, xc);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) acc[a] += h[3 * a] * xc[0] + h[3 * a + 1] * xc[1] + h[3 * a + 2] * xc[2];
+  }
+}
+
+// r64 = b - (H + shift I) dx in FP64 (FP32 values promoted); starts an inner PCG on r
+template <typename Real>
+__global__ void __launch_bounds__(kTile) k_resid(BatchDev B) {
+  __shared__ double sm[32 * 5];
+  __shared__ int flag;
+  const int num = *B.num;
+  const int total = B.pre_node[num];
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int i = find_tile(B.pre_node, num, t), lt = t - B.pre_node[i];
+    const InstDev& I = B.inst[i];
+    NState* st = I.st;
+    if (st->phase != PH_RESID) continue;
+    const int v = lt * kTile + threadIdx.x;
+    double p[5] = {0, 0, 0, 0, 0};
+    if (v < I.n) {
+      const Real* H = PcgBufs<Real>::H(I);
+      double acc[3];
+      const double* dxv = I.dx;
+      sell_row<Real, double>(I, H, v, [&](int col, double (&xc)[3]) { ld4(dxv, col, xc); }, acc);
+      double xv[3], b[3];
+      ld4(I.dx, v, xv);
+      ld4(I.bvec, v, b);
+      const double sh = st->shift;
+      double r[3];
+      for (int a = 0; a < 3; ++a) r[a] = b[a] - (acc[a] + sh * xv[a]);
+      st4(I.r64, v, r);
+      p[0] = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+      p[1] = b[0] * xv[0] + b[1] * xv[1] + b[2] * xv[2];
+      p[2] = xv[0] * xv[0] + xv[1] * xv[1] + xv[2] * xv[2];
+      // inner PCG start: e = 0, r = (Real) r64, z = Minv r, p_prev = 0
+      Real rr_[3] = {(Real)r[0], (Real)r[1], (Real)r[2]}, zero[3] = {0, 0, 0}, z[3];
+      const Real* Mi = PcgBufs<Real>::minv(I);
+      for (int a = 0; a < 3; ++a)
+        z[a] = Mi[(size_t)(3 * a) * I.n + v] * rr_[0] + Mi[(size_t)(3 * a + 1) * I.n + v] * rr_[1] +
+               Mi[(size_t)(3 * a + 2) * I.n + v] * rr_[2];
+      st4(PcgBufs<Real>::r(I), v, rr_);
+      st4(PcgBufs<Real>::z(I), v, z);
+      st4(PcgBufs<Real>::e(I), v, zero);
+      st4(PcgBufs<Real>::pa(I), v, zero);
+      p[3] = (double)(rr_[0] * z[0] + rr_[1] * z[1] + rr_[2] * z[2]);
+      p[4] = (double)(rr_[0] * rr_[0] + rr_[1] * rr_[1] + rr_[2] * rr_[2]);
+    }
+    double tot[5];
+    if (tile_done<5>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
+      st->rr64 = tot[0];
+      st->b_dot_dx = tot[1];
+      st->dx_norm = sqrt(tot[2]);
+      const bool conv = tot[0] < st->thr_final;
+      if (conv || st->sweeps >= I.opts->max_refine_sweeps) {
+        if (conv) st->lin_status = LIN_CONVERGED;
+        else if (st->lin_status == LIN_RUNNING) st->lin_status = LIN_MAXITER;
+        st->phase = PH_LIN_DONE;
+      } else {
+        const double it = I.opts->inner_tol;
+        st->thr_inner = (I.opts->precision == 0) ? st->thr_final : fmax(it * it * tot[0], st->thr_final);
+        st->rz = tot[3];
+        st->rr = tot[4];
+        st->pcg_iter = 0;
+        st->pcg_parity = 0;
+        st->beta = 0.0;
+        st->lin_status = LIN_RUNNING;
+        st->phase = PH_PCG;
+      }
+    }
+  }
+}
+
+// PCG step 1: p = z + beta p_prev (formed on the fly for every column, written
+// for the own row into the other buffer), q = (H + shift I) p, pq = p.q
+template <typename Real>
+__global__ void __launch_bounds__(kTile) k_pcg_a(BatchDev B) {
+  __shared__ double sm[32];
+  __shared__ int flag;
+  const int num = *B.num;
+  const int total = B.pre_node[num];
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int i = find_tile(B.pre_node, num, t), lt = t - B.pre_node[i];
+    const InstDev& I = B.inst[i];
+    NState* st = I.st;
+    if (st->phase != PH_PCG) continue;
+    const int v = lt * kTile + threadIdx.x;
+    double p[1] = {0.0};
+    if (v < I.n) {
+      const int par = st->pcg_parity;
+      const Real* pold = par ? PcgBufs<Real>::pb(I) : PcgBufs<Real>::pa(I);
+      Real* pnew = par ? PcgBufs<Real>::pa(I) : PcgBufs<Real>::pb(I);
+      const Real* z = PcgBufs<Real>::z(I);
+      const Real beta = (Real)st->beta, sh = (Real)st->shift;
+      Real acc[3];
+      sell_row<Real, Real>(I, PcgBufs<Real>::H(I), v,
+                           [&](int col, Real (&xc)[3]) {
+                             Real zc[3], pc[3];
+                             ld4(z, col, zc);
+                             ld4(pold, col, pc);
+                             for (int a = 0; a < 3; ++a) xc[a] = zc[a] + beta * pc[a];
+                           },
+                           acc);
+      Real zv[3], pv[3];
+      ld4(z, v, zv);
+      ld4(pold, v, pv);
+      for (int a = 0; a < 3; ++a) {
+        pv[a] = zv[a] + beta * pv[a];
+        acc[a] += sh * pv[a];
+      }
+      st4(pnew, v, pv);
+      st4(PcgBufs<Real>::q(I), v, acc);
+      p[0] = (double)pv[0] * acc[0] + (double)pv[1] * acc[1] + (double)pv[2] * acc[2];
+    }
+    double tot[1];
+    if (tile_done<1>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
+      st->pq = tot[0];
+      if (!(tot[0] > 0.0)) {  // not positive definite along p (or non-finite)
+        st->lin_status = LIN_BREAKDOWN;
+        st->phase = PH_LIN_DONE;
+      } else {
+        st->alpha = st->rz / tot[0];
+      }
+    }
+  }
+}
+
+// PCG step 2: e += alpha p, r -= alpha q, z = Minv r; convergence ||r||^2 < thr (Eigen's rule)
+template <typename Real>
+__global__ void __launch_bounds__(kTile) k_pcg_b(BatchDev B) {
+  __shared__ double sm[32 * 2];
+  __shared__ int flag;
+  const int num = *B.num;
+  const int total = B.pre_node[num];
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int i = find_tile(B.pre_node, num, t), lt = t - B.pre_node[i];
+    const InstDev& I = B.inst[i];
+    NState* st = I.st;
+    if (st->phase != PH_PCG) continue;
+    const int v = lt * kTile + threadIdx.x;
+    double p[2] = {0.0, 0.0};
+    if (v < I.n) {
+      const Real alpha = (Real)st->alpha;
+      const Real* pc = st->pcg_parity ? PcgBufs<Real>::pa(I) : PcgBufs<Real>::pb(I);
+      Real pv[3], qv[3], ev[3], rv[3], z[3];
+      ld4(pc, v, pv);
+      ld4(PcgBufs<Real>::q(I), v, qv);
+      ld4(PcgBufs<Real>::e(I), v, ev);
+      ld4(PcgBufs<Real>::r(I), v, rv);
+      for (int a = 0; a < 3; ++a) {
+        ev[a] += alpha * pv[a];
+        rv[a] -= alpha * qv[a];
+      }
+      const Real* Mi = PcgBufs<Real>::minv(I);
+      for (int a = 0; a < 3; ++a)
+        z[a] = Mi[(size_t)(3 * a) * I.n + v] * rv[0] + Mi[(size_t)(3 * a + 1) * I.n + v] * rv[1] +
+               Mi[(size_t)(3 * a + 2) * I.n + v] * rv[2];
+      st4(PcgBufs<Real>::e(I), v, ev);
+      st4(PcgBufs<Real>::r(I), v, rv);
+      st4(PcgBufs<Real>::z(I), v, z);
+      p[0] = (double)rv[0] * rv[0] + (double)rv[1] * rv[1] + (double)rv[2] * rv[2];
+      p[1] = (double)rv[0] * z[0] + (double)rv[1] * z[1] + (double)rv[2] * z[2];
+    }
+    double tot[2];
+    if (tile_done<2>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
+      st->pcg_iter++;
+      st->pcg_total++;
+      st->rr = tot[0];
+      if (tot[0] < st->thr_inner) {
+        st->lin_status = LIN_CONVERGED;
+        st->phase = PH_ACCUM;
+      } else if (st->pcg_iter >= I.opts->ls_num_max_iters) {
+        st->lin_status = LIN_MAXITER;
+        st->phase = PH_ACCUM;
+      } else {
+        st->beta = tot[1] / st->rz;
+        st->rz = tot[1];
+        st->pcg_parity ^= 1;
+      }
+    }
+  }
+}
+
+// dx += e (FP64), then back to the FP64 residual
+template <typename Real>
+__global__ void __launch_bounds__(kTile) k_accum(BatchDev B) {
+  __shared__ double sm[32];
+  __shared__ int flag;
+  const int num = *B.num;
+  const int total = B.pre_node[num];
+  for (int t = blockIdx.x; t < total; t += gridDim.x) {
+    const int i = find_tile(B.pre_node, num, t), lt = t - B.pre_node[i];
+    const InstDev& I = B.inst[i];
+    NState* st = I.st;
+    if (st->phase != PH_ACCUM) continue;
+    const int v = lt * kTile + threadIdx.x;
+    if (v < I.n) {
+      Real ev[3];
+      double d[3];
+      ld4(PcgBufs<Real>::e(I), v, ev);
+      ld4(I.dx, v, d);
+      for (int a = 0; a < 3; ++a) d[a] += (double)ev[a];
+      st4(I.dx, v, d);
+    }
+    double p[1] = {0.0}, tot[1];
+    if (tile_done<1>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
+      st->sweeps++;
+      st->total_sweeps++;
+      st->phase = PH_RESID;
+    }
+  }
+}
+
+// the state machine: one thread per instance; writes the active count and phases
+__global__ void __launch_bounds__(256) k_control(BatchDev B) {
+  __shared__ double sm[32];
+  const int num = *B.num;
+  double active = 0.0;
+  for (int i = threadIdx.x; i < num; i += blockDim.x) {
+    NState s = *B.inst[i].st;
+    const DevOpts o = *B.inst[i].opts;
+    ctl_advance(s, o);
+    *B.inst[i].st = s;
+    B.flags[8 + i] = s.phase;
+    active += (s.phase != PH_DONE) ? 1.0 : 0.0;
+  }
+  double v[1] = {active};
+  block_sum<1>(v, sm);
+  if (threadIdx.x == 0) B.flags[0] = (int)v[0];
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+template <typename Real>
+size_t hess_smem() { return (size_t)kTile * 90 * sizeof(Real); }
+
+cudaError_t setup_kernel_attributes() {
+  cudaError_t e = cudaFuncSetAttribute(k_elem_hess<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)hess_smem<double>());
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_elem_hess<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)hess_smem<float>());
+}
+
+void launch(KernelId id, int grid, cudaStream_t s, const BatchDev& B, bool fp64) {
+  if (grid <= 0) return;
+  switch (id) {
+    case K_CONTROL: k_control<<<1, 256, 0, s>>>(B); break;
+    case K_VECOP: k_vecop<<<grid, kTile, 0, s>>>(B); break;
+    case K_ELEM_EG: k_elem_eg<<<grid, kTile, 0, s>>>(B); break;
+    case K_GATHER: k_gather<<<grid, kTile, 0, s>>>(B); break;
+    case K_ELEM_HESS:
+      if (fp64) k_elem_hess<double><<<grid, kTile, hess_smem<double>(), s>>>(B);
+      else k_elem_hess<float><<<grid, kTile, hess_smem<float>(), s>>>(B);
+      break;
+    case K_ASSEMBLE:
+      if (fp64) k_assemble<double><<<grid, 288, 0, s>>>(B); else k_assemble<float><<<grid, 288, 0, s>>>(B);
+      break;
+    case K_JACOBI:
+      if (fp64) k_jacobi<double><<<grid, kTile, 0, s>>>(B); else k_jacobi<float><<<grid, kTile, 0, s>>>(B);
+      break;
+    case K_LINSETUP: k_linsetup<<<grid, kTile, 0, s>>>(B); break;
+    case K_RESID:
+      if (fp64) k_resid<double><<<grid, kTile, 0, s>>>(B); else k_resid<float><<<grid, kTile, 0, s>>>(B);
+      break;
+    case K_PCG_A:
+      if (fp64) k_pcg_a<double><<<grid, kTile, 0, s>>>(B); else k_pcg_a<float><<<grid, kTile, 0, s>>>(B);
+      break;
+    case K_PCG_B:
+      if (fp64) k_pcg_b<double><<<grid, kTile, 0, s>>>(B); else k_pcg_b<float><<<grid, kTile, 0, s>>>(B);
+      break;
+    case K_ACCUM:
+      if (fp64) k_accum<double><<<grid, kTile, 0, s>>>(B); else k_accum<float><<<grid, kTile, 0, s>>>(B);
+      break;
+    default: break;
+  }
+}
+
+const char* kernel_name(KernelId id) {
+  switch (id) {
+    case K_CONTROL: return "control";
+    case K_VECOP: return "vecop";
+    case K_ELEM_EG: return "elem_eg";
+    case K_GATHER: return "gather";
+    case K_ELEM_HESS: return "elem_hess";
+    case K_ASSEMBLE: return "assemble";
+    case K_JACOBI: return "jacobi";
+    case K_LINSETUP: return "linsetup";
+    case K_RESID: return "resid";
+    case K_PCG_A: return "spmv";
+    case K_PCG_B: return "pcg_update";
+    case K_ACCUM: return "accum";
+    default: return "?";
+  }
+}
+
+}  // namespace phx

@@ -1,0 +1,206 @@
+// newton_control.h -- the per-instance Newton / line-search state machine.
+//
+// One device thread owns one instance's NState and advances it between the
+// node- and element-parallel kernels.  The transitions restate, step for step:
+//   OptimSolver::SolveFull          source/PhySim/Solvers/OptimSolver.cpp:163-311
+//   OptimSolver_USQP_LS::SolveStepInternal  source/PhySim/Solvers/OptimSolver_USQP_LS.cpp:18-68
+//   OptimSolver::ComputeStep        OptimSolver.cpp:313-352 (step clamp to maxStepSize)
+//   OptimSolver::LineSearch_Simple  OptimSolver.cpp:688-736
+//   OptimSolver::UpdateStepResult   OptimSolver.cpp:402-466
+//   regularisation retry loop       source/PhySim/Solvers/LinearSolver_EigenCG.cpp:67-122,
+//                                   LinearSolver.cpp:57-66 (regT = 1e-6 ||A||_F, cumulative
+//                                   shift regT * 10^(i-1) at trial i)
+// The header is plain C++ so the same code is exercised on the host by the tests.
+#pragma once
+
+#include <math.h>
+
+#include "phx_types.h"
+
+namespace phx {
+
+enum OSResult : int32_t { OS_ONGOING = 0, OS_SUCCESS = 1, OS_MINSTEP = 2, OS_MINIMPR = 3,
+                          OS_FAILURE = 4, OS_MAXITER = 5, OS_NONDESC = 6 };
+
+// SolveFull's decisions after one SolveStep; returns the next phase.
+PHX_HD inline int32_t ctl_post_step(NState& s, const DevOpts& o) {
+  bool brk = false;
+  if (s.result == OS_NONDESC) {
+    if (!o.try_steepest) brk = true;
+    else if (s.steepest) brk = true;
+    else s.steepest = 1;
+  }
+  if (!brk && s.result == OS_MINIMPR) {
+    if (s.min_impr_count == o.min_impr_max_count) brk = true;
+    else if (o.try_steepest) s.steepest = !s.steepest;
+  }
+  if (!brk && s.result == OS_MINSTEP) {
+    if (s.min_step_count == o.min_step_max_count) brk = true;
+    else if (o.try_steepest) s.steepest = !s.steepest;
+  }
+  if (!brk && s.result == OS_SUCCESS) {
+    if (s.opt <= o.tol_max_error) brk = true;
+    else s.result = OS_ONGOING;
+  }
+  if (!brk && s.result == OS_ONGOING) s.steepest = 0;
+  if (!brk && s.it + 1 > o.num_max_iters) {
+    s.result = OS_MAXITER;
+    brk = true;
+  }
+  if (brk) {
+    if (o.dynamic) s.vecop |= VO_VEL;
+    return PH_DONE;
+  }
+  return PH_ITER;
+}
+
+// Moves to the next device phase, through a vector op when one is pending.
+PHX_HD inline void ctl_goto(NState& s, int32_t next) {
+  if (s.vecop) {
+    s.next_phase = next;
+    s.phase = PH_VEC;
+  } else {
+    s.phase = next;
+  }
+}
+
+// Start of SolveStepInternal (energy, gradient and ||g|| at x are known).
+PHX_HD inline void ctl_iter_begin(NState& s, const DevOpts& o) {
+  s.it++;
+  if (s.opt0 < 0) s.opt0 = s.opt;
+  s.num_bis = 0;
+  if (s.opt < o.tol_max_error) {
+    s.result = OS_SUCCESS;
+    s.step_result = OS_SUCCESS;
+    ctl_goto(s, ctl_post_step(s, o));
+    return;
+  }
+  int qp = s.steepest ? 0 : o.qp_solver;
+  if (qp == 0) {
+    // Steepest: dx = -g, so ||dx|| = ||g||
+    s.dx_norm = s.opt;
+    s.scale = (s.dx_norm > o.max_step_size) ? o.max_step_size / s.dx_norm : 1.0;
+    s.factor = 1.0;
+    s.alpha_trial = s.scale * s.factor;
+    s.purpose = 1;
+    s.vecop = VO_STEEP | VO_TRIAL;
+    ctl_goto(s, PH_EVAL);
+  } else {
+    s.reg_trial = 0;
+    s.shift = 0.0;
+    s.phase = PH_HESS;
+  }
+}
+
+// After a linear solve: regularise and retry, or clamp the step and start the line search.
+PHX_HD inline void ctl_lin_done(NState& s, const DevOpts& o) {
+  bool bad = (s.lin_status == LIN_BREAKDOWN) || !(s.b_dot_dx >= 0.0) || !isfinite(s.dx_norm);
+  if (bad && s.reg_trial + 1 < o.ls_num_reg_trials) {
+    s.reg_trial++;
+    s.total_reg++;
+    s.shift += s.regT * pow(10.0, (double)(s.reg_trial - 1));
+    s.phase = PH_JACOBI;
+    return;
+  }
+  s.scale = (s.dx_norm > o.max_step_size) ? o.max_step_size / s.dx_norm : 1.0;
+  s.factor = 1.0;
+  s.num_bis = 0;
+  s.alpha_trial = s.scale * s.factor;
+  s.purpose = 1;
+  s.vecop = VO_TRIAL;
+  ctl_goto(s, PH_EVAL);
+}
+
+// Line-search trial evaluated: accept, bisect, or give up (LineSearch_Simple + UpdateStepResult).
+PHX_HD inline void ctl_ls_check(NState& s, const DevOpts& o) {
+  double objNew = s.E_eval;
+  if (objNew < s.obj) {
+    double impr = s.obj - objNew;
+    double step = s.alpha_trial * s.dx_norm;
+    double optNew = sqrt(s.gg_eval);
+    if (impr < o.tol_min_impr) {
+      s.min_impr_count++;
+      s.result = OS_MINIMPR;
+    } else if (step < o.tol_min_step) {
+      s.min_step_count++;
+      s.result = OS_MINSTEP;
+    } else if (optNew <= o.tol_max_error) {
+      s.result = OS_SUCCESS;
+      s.min_impr_count = 0;
+      s.min_step_count = 0;
+    } else {
+      s.result = OS_ONGOING;
+      s.min_impr_count = 0;
+      s.min_step_count = 0;
+    }
+    s.step_result = s.result;
+    s.obj = objNew;
+    s.opt = optNew;
+    s.total_bis += s.num_bis;
+    s.vecop = VO_ACCEPT | VO_SAVE;
+    ctl_goto(s, ctl_post_step(s, o));
+    return;
+  }
+  double stepCur = s.alpha_trial * s.dx_norm;
+  s.factor *= o.lsearch_alpha;
+  if (stepCur > o.tol_min_step && s.num_bis <= o.lsearch_num_try) {
+    s.num_bis++;
+    s.alpha_trial = s.scale * s.factor;
+    s.vecop = VO_TRIAL;
+    ctl_goto(s, PH_EVAL);
+    return;
+  }
+  // line search failed: state restored, step rejected
+  s.result = OS_NONDESC;
+  s.step_result = OS_NONDESC;
+  s.total_bis += s.num_bis;
+  s.vecop = VO_RESTORE;
+  ctl_goto(s, ctl_post_step(s, o));
+}
+
+// Advances one instance until it needs device work or is done.
+PHX_HD inline void ctl_advance(NState& s, const DevOpts& o) {
+  for (int guard = 0; guard < 8; ++guard) {
+    switch (s.phase) {
+      case PH_START:
+        s.it = 0;
+        s.result = OS_SUCCESS;
+        s.step_result = OS_ONGOING;
+        s.steepest = 0;
+        s.min_impr_count = 0;
+        s.min_step_count = 0;
+        s.total_bis = 0;
+        s.total_reg = 0;
+        s.total_sweeps = 0;
+        s.pcg_total = 0;
+        s.opt0 = -1.0;
+        s.purpose = 0;
+        s.vecop = o.dynamic ? VO_PRED : 0;
+        ctl_goto(s, PH_EVAL);
+        return;
+      case PH_EVAL_DONE:
+        if (s.purpose == 0) {
+          s.obj = s.E_eval;
+          s.opt = sqrt(s.gg_eval);
+          s.vecop = VO_GCOPY | VO_SAVE;
+          s.next_phase = PH_ITER;
+          s.phase = PH_VEC;
+          return;
+        }
+        ctl_ls_check(s, o);
+        if (s.phase == PH_ITER) continue;
+        return;
+      case PH_ITER:
+        ctl_iter_begin(s, o);
+        if (s.phase == PH_ITER) continue;
+        return;
+      case PH_LIN_DONE:
+        ctl_lin_done(s, o);
+        return;
+      default:
+        return;  // a device phase, a pending vector op, or done
+    }
+  }
+}
+
+}  // namespace phx

@@ -1,0 +1,268 @@
+// pattern.cpp -- Hessian block pattern, scatter map and SELL layout, built on the host.
+//
+// The stored pattern is the one AMatrixSd builds on its first (triplet) assembly
+// (source/PhySim/BasicTypes.cpp:64-78, 118-145; DerivativeAssembler.cpp:205-300):
+// every tet contributes, for each local node pair (i, j <= i), a 3x3 block at
+// (max(node_i, node_j), min(node_i, node_j)); node diagonal blocks are stored in
+// full, duplicates are summed and structural zeros kept.  Expanded per DoF that
+// is Eigen's lower CSC; per node it is a block-lower pattern with one block per
+// node and one per mesh edge.  Block k is numbered column-major (C, then R),
+// which is the order Eigen stores them in.
+//
+// For the device, the symmetric matrix is stored in full (V + 2E blocks) in
+// SELL-32 order so a warp reads 32 rows' entries with one coalesced access, and
+// the scatter map is inverted into per-block contribution lists ("segments")
+// in element order, so the device sums each entry in exactly the order the
+// reference's serial assembly does, without atomics.
+#include "pattern.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace phx {
+
+const int kPairI[10] = {0, 1, 1, 2, 2, 2, 3, 3, 3, 3};
+const int kPairJ[10] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
+
+namespace {
+
+inline double det3(const double* F) {
+  return F[0] * (F[4] * F[8] - F[7] * F[5]) - F[3] * (F[1] * F[8] - F[7] * F[2]) +
+         F[6] * (F[1] * F[5] - F[4] * F[2]);
+}
+
+// inverse of a column-major 3x3 (adjugate / det)
+inline void inv3(const double* A, double d, double* Ai) {
+  auto a = [&](int i, int j) { return A[i + 3 * j]; };
+  double C[9];
+  C[0] = a(1, 1) * a(2, 2) - a(1, 2) * a(2, 1);
+  C[1] = a(0, 2) * a(2, 1) - a(0, 1) * a(2, 2);
+  C[2] = a(0, 1) * a(1, 2) - a(0, 2) * a(1, 1);
+  C[3] = a(1, 2) * a(2, 0) - a(1, 0) * a(2, 2);
+  C[4] = a(0, 0) * a(2, 2) - a(0, 2) * a(2, 0);
+  C[5] = a(0, 2) * a(1, 0) - a(0, 0) * a(1, 2);
+  C[6] = a(1, 0) * a(2, 1) - a(1, 1) * a(2, 0);
+  C[7] = a(0, 1) * a(2, 0) - a(0, 0) * a(2, 1);
+  C[8] = a(0, 0) * a(1, 1) - a(0, 1) * a(1, 0);
+  // C is the cofactor matrix stored column-major as C(i,j) = C[i + 3j] with the index
+  // pattern above giving cofactor(i, j); inverse(i, j) = cofactor(j, i) / det.
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) Ai[i + 3 * j] = C[j + 3 * i] / d;
+}
+
+}  // namespace
+
+void rebuild_load(const MeshIn& in, HostPattern& hp) {
+  hp.hlin.assign(4 * (size_t)hp.n, 0.0);
+  for (int v = 0; v < hp.n; ++v)
+    for (int c = 0; c < 3; ++c) {
+      double f = in.force ? in.force[3 * (size_t)v + c] : 0.0;
+      hp.hlin[4 * (size_t)v + c] = f - hp.mass[v] * in.gravity[c];
+    }
+}
+
+bool build_pattern(const MeshIn& in, HostPattern& hp, std::string& err) {
+  const int n = in.n, m = in.m;
+  if (n <= 0 || m <= 0 || !in.X0 || !in.T || !in.lame || !in.rho) {
+    err = "mesh: empty or missing arrays";
+    return false;
+  }
+  if ((int64_t)m * 10 > 2000000000LL) {
+    err = "mesh: too many tets for 32-bit scatter indices";
+    return false;
+  }
+  hp.n = n;
+  hp.m = m;
+  hp.tets.assign(in.T, in.T + 4 * (size_t)m);
+  hp.model.assign(m, 0);
+  if (in.model)
+    for (int e = 0; e < m; ++e) {
+      if (in.model[e] > 1) { err = "mesh: unknown material model"; return false; }
+      hp.model[e] = in.model[e];
+    }
+  std::vector<char> used(n, 0);
+  hp.rest64.resize(12 * (size_t)m);
+  hp.rest32.resize(12 * (size_t)m);
+  hp.mass.assign(n, 0.0);
+  for (int e = 0; e < m; ++e) {
+    const int32_t* t = &hp.tets[4 * (size_t)e];
+    for (int a = 0; a < 4; ++a) {
+      if (t[a] < 0 || t[a] >= n) { err = "mesh: node id out of range in tet " + std::to_string(e); return false; }
+      for (int b = 0; b < a; ++b)
+        if (t[a] == t[b]) { err = "mesh: repeated node in tet " + std::to_string(e); return false; }
+      used[t[a]] = 1;
+    }
+    double Dm[9];
+    for (int c = 0; c < 3; ++c)
+      for (int r = 0; r < 3; ++r) Dm[r + 3 * c] = in.X0[3 * (size_t)t[c + 1] + r] - in.X0[3 * (size_t)t[0] + r];
+    double d = det3(Dm);
+    if (!(d > 0.0) || !std::isfinite(d)) {
+      err = "mesh: non-positive rest volume in tet " + std::to_string(e);
+      return false;
+    }
+    double lam = in.lame[2 * (size_t)e], mu = in.lame[2 * (size_t)e + 1], rho = in.rho[e];
+    if (!std::isfinite(lam) || !std::isfinite(mu) || !std::isfinite(rho)) {
+      err = "mesh: non-finite material parameter in tet " + std::to_string(e);
+      return false;
+    }
+    double* R = &hp.rest64[12 * (size_t)e];
+    inv3(Dm, d, R);
+    R[9] = d / 6.0;  // quadrature weight (1/6) * det J (EnergyElement_FEM.cpp:87-91)
+    R[10] = lam;
+    R[11] = mu;
+    for (int k = 0; k < 12; ++k) hp.rest32[12 * (size_t)e + k] = (float)R[k];
+    // MassElement_Lumped::ComputeAndStore_Mass: rho * V / 4 per node
+    double me = rho * (d / 6.0) / 4.0;
+    for (int a = 0; a < 4; ++a) hp.mass[t[a]] += me;
+  }
+  for (int v = 0; v < n; ++v)
+    if (!used[v]) { err = "mesh: node " + std::to_string(v) + " belongs to no tet"; return false; }
+
+  // ---- lower blocks, column-major (C, R) -------------------------------
+  std::vector<int32_t> cnt(n + 1, 0);
+  for (int e = 0; e < m; ++e)
+    for (int p = 0; p < 10; ++p) {
+      int ni = hp.tets[4 * (size_t)e + kPairI[p]], nj = hp.tets[4 * (size_t)e + kPairJ[p]];
+      cnt[std::min(ni, nj) + 1]++;
+    }
+  for (int v = 0; v < n; ++v) cnt[v + 1] += cnt[v];
+  std::vector<int32_t> rows(cnt[n]);
+  {
+    std::vector<int32_t> pos(cnt.begin(), cnt.end() - 1);
+    for (int e = 0; e < m; ++e)
+      for (int p = 0; p < 10; ++p) {
+        int ni = hp.tets[4 * (size_t)e + kPairI[p]], nj = hp.tets[4 * (size_t)e + kPairJ[p]];
+        rows[pos[std::min(ni, nj)]++] = std::max(ni, nj);
+      }
+  }
+  hp.lo_colptr.assign(n + 1, 0);
+  std::vector<int32_t> lo_R;
+  lo_R.reserve(cnt[n] / 3);
+  for (int C = 0; C < n; ++C) {
+    auto b = rows.begin() + cnt[C], en = rows.begin() + cnt[C + 1];
+    std::sort(b, en);
+    auto u = std::unique(b, en);
+    for (auto it = b; it != u; ++it) lo_R.push_back(*it);
+    hp.lo_colptr[C + 1] = (int32_t)lo_R.size();
+  }
+  hp.nlo = (int32_t)lo_R.size();
+  hp.lo_rc.resize(2 * (size_t)hp.nlo);
+  for (int C = 0; C < n; ++C)
+    for (int k = hp.lo_colptr[C]; k < hp.lo_colptr[C + 1]; ++k) {
+      hp.lo_rc[2 * (size_t)k] = lo_R[k];
+      hp.lo_rc[2 * (size_t)k + 1] = C;
+    }
+  // every node has its diagonal block first in its column
+  for (int C = 0; C < n; ++C)
+    if (hp.lo_colptr[C + 1] == hp.lo_colptr[C] || lo_R[hp.lo_colptr[C]] != C) {
+      err = "pattern: missing diagonal block";
+      return false;
+    }
+
+  // ---- scatter map and its inverse (segments) --------------------------
+  hp.scatter.resize(10 * (size_t)m);
+  for (int e = 0; e < m; ++e)
+    for (int p = 0; p < 10; ++p) {
+      int ni = hp.tets[4 * (size_t)e + kPairI[p]], nj = hp.tets[4 * (size_t)e + kPairJ[p]];
+      int R = std::max(ni, nj), C = std::min(ni, nj);
+      auto b = lo_R.begin() + hp.lo_colptr[C], en = lo_R.begin() + hp.lo_colptr[C + 1];
+      hp.scatter[10 * (size_t)e + p] = (int32_t)(std::lower_bound(b, en, R) - lo_R.begin());
+    }
+  hp.seg_ptr.assign(hp.nlo + 1, 0);
+  for (size_t c = 0; c < hp.scatter.size(); ++c) hp.seg_ptr[hp.scatter[c] + 1]++;
+  for (int k = 0; k < hp.nlo; ++k) hp.seg_ptr[k + 1] += hp.seg_ptr[k];
+  hp.seg_c.resize(hp.scatter.size());
+  {
+    std::vector<int32_t> pos(hp.seg_ptr.begin(), hp.seg_ptr.end() - 1);
+    for (size_t c = 0; c < hp.scatter.size(); ++c) hp.seg_c[pos[hp.scatter[c]]++] = (int32_t)c;
+  }
+  hp.nseg_ptr.assign(n + 1, 0);
+  for (size_t c = 0; c < 4 * (size_t)m; ++c) hp.nseg_ptr[hp.tets[c] + 1]++;
+  for (int v = 0; v < n; ++v) hp.nseg_ptr[v + 1] += hp.nseg_ptr[v];
+  hp.nseg_c.resize(4 * (size_t)m);
+  {
+    std::vector<int32_t> pos(hp.nseg_ptr.begin(), hp.nseg_ptr.end() - 1);
+    for (size_t c = 0; c < 4 * (size_t)m; ++c) hp.nseg_c[pos[hp.tets[c]]++] = (int32_t)c;
+  }
+
+  // ---- full rows and SELL-32 slots ---------------------------------------
+  // row v: [C < v from lower blocks (v, C)] [v] [R > v from column v]
+  std::vector<int32_t> rowL_cnt(n + 1, 0);
+  for (int k = 0; k < hp.nlo; ++k) {
+    int R = hp.lo_rc[2 * (size_t)k], C = hp.lo_rc[2 * (size_t)k + 1];
+    if (R != C) rowL_cnt[R + 1]++;
+  }
+  std::vector<int32_t> rowL_ptr(n + 1, 0);
+  for (int v = 0; v < n; ++v) rowL_ptr[v + 1] = rowL_ptr[v] + rowL_cnt[v + 1];
+  std::vector<int32_t> rowL_col(rowL_ptr[n]);
+  hp.lo_slot.assign(hp.nlo, -1);
+  hp.up_slot.assign(hp.nlo, -1);
+  std::vector<int32_t> rowL_k(rowL_ptr[n]);
+  {
+    std::vector<int32_t> pos(rowL_ptr.begin(), rowL_ptr.end() - 1);
+    for (int k = 0; k < hp.nlo; ++k) {  // k ascends with C, so each row list comes out sorted
+      int R = hp.lo_rc[2 * (size_t)k], C = hp.lo_rc[2 * (size_t)k + 1];
+      if (R != C) {
+        rowL_col[pos[R]] = C;
+        rowL_k[pos[R]] = k;
+        pos[R]++;
+      }
+    }
+  }
+  hp.nchunks = (n + kChunk - 1) / kChunk;
+  hp.chunk_off.assign(hp.nchunks + 1, 0);
+  std::vector<int32_t> rowlen(n);
+  for (int v = 0; v < n; ++v)
+    rowlen[v] = (rowL_ptr[v + 1] - rowL_ptr[v]) + (hp.lo_colptr[v + 1] - hp.lo_colptr[v]);
+  for (int c = 0; c < hp.nchunks; ++c) {
+    int len = 0;
+    for (int v = c * kChunk; v < std::min(n, (c + 1) * kChunk); ++v) len = std::max(len, rowlen[v]);
+    hp.chunk_off[c + 1] = hp.chunk_off[c] + len * kChunk;
+  }
+  hp.nslots = hp.chunk_off[hp.nchunks];
+  hp.slot_col.assign(hp.nslots, 0);
+  hp.diag_slot.assign(n, -1);
+  for (int c = 0; c < hp.nchunks; ++c) {
+    int len = (hp.chunk_off[c + 1] - hp.chunk_off[c]) / kChunk;
+    for (int lane = 0; lane < kChunk; ++lane) {
+      int v = c * kChunk + lane;
+      for (int k = 0; k < len; ++k) {
+        int64_t s = hp.chunk_off[c] + (int64_t)k * kChunk + lane;
+        hp.slot_col[s] = v < n ? v : 0;  // padding points at the row itself, value 0
+      }
+      if (v >= n) continue;
+      int k = 0;
+      for (int q = rowL_ptr[v]; q < rowL_ptr[v + 1]; ++q, ++k) {
+        int64_t s = hp.chunk_off[c] + (int64_t)k * kChunk + lane;
+        hp.slot_col[s] = rowL_col[q];
+        hp.lo_slot[rowL_k[q]] = (int32_t)s;
+      }
+      for (int kk = hp.lo_colptr[v]; kk < hp.lo_colptr[v + 1]; ++kk, ++k) {
+        int64_t s = hp.chunk_off[c] + (int64_t)k * kChunk + lane;
+        int R = hp.lo_rc[2 * (size_t)kk];
+        hp.slot_col[s] = R;
+        if (R == v) {
+          hp.diag_slot[v] = (int32_t)s;
+          hp.lo_slot[kk] = (int32_t)s;
+        } else {
+          hp.up_slot[kk] = (int32_t)s;
+        }
+      }
+    }
+  }
+  if (hp.nslots >= (int64_t)2000000000) {
+    err = "pattern: too many blocks for 32-bit slot ids";
+    return false;
+  }
+  // ---- boundary conditions ------------------------------------------------
+  hp.fixmask.assign(n, 0);
+  if (in.fixed)
+    for (int v = 0; v < n; ++v)
+      for (int c = 0; c < 3; ++c)
+        if (in.fixed[3 * (size_t)v + c]) hp.fixmask[v] |= (uint8_t)(1u << c);
+  rebuild_load(in, hp);
+  return true;
+}
+
+}  // namespace phx

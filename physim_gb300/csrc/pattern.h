@@ -1,0 +1,60 @@
+// pattern.h -- host-side construction of the Hessian block pattern and the scatter map.
+#pragma once
+
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "phx_types.h"
+
+namespace phx {
+
+struct MeshIn {
+  int32_t n = 0, m = 0;
+  const double* X0 = nullptr;
+  const int32_t* T = nullptr;
+  const double* lame = nullptr;
+  const double* rho = nullptr;
+  const uint8_t* model = nullptr;
+  const uint8_t* fixed = nullptr;
+  const double* force = nullptr;
+  double gravity[3] = {0, 0, 0};
+};
+
+// Everything the device needs, built once per mesh on the host.
+struct HostPattern {
+  int32_t n = 0, m = 0, nlo = 0, nchunks = 0;
+  int64_t nslots = 0;
+  std::vector<int32_t> tets;          // [4m]
+  std::vector<double> rest64;         // [12m]
+  std::vector<float> rest32;          // [12m]
+  std::vector<uint8_t> model;         // [m]
+  std::vector<int32_t> lo_rc;         // [2 nlo] (R, C), column-major block order (C, then R)
+  std::vector<int32_t> lo_colptr;     // [n+1] lower blocks of block column C: [lo_colptr[C], lo_colptr[C+1])
+  std::vector<int32_t> scatter;       // [10m] lower block of each (tet, local pair)
+  std::vector<int32_t> seg_ptr;       // [nlo+1]
+  std::vector<int32_t> seg_c;         // [10m]
+  std::vector<int32_t> nseg_ptr;      // [n+1]
+  std::vector<int32_t> nseg_c;        // [4m]
+  std::vector<int32_t> chunk_off;     // [nchunks+1]
+  std::vector<int32_t> slot_col;      // [nslots]
+  std::vector<int32_t> diag_slot;     // [n]
+  std::vector<int32_t> lo_slot;       // [nlo]
+  std::vector<int32_t> up_slot;       // [nlo]
+  std::vector<uint8_t> fixmask;       // [n]
+  std::vector<double> mass;           // [n]
+  std::vector<double> hlin;           // [4n]  f - m g
+};
+
+// Validates the mesh and builds the pattern; returns false with a message on bad input.
+bool build_pattern(const MeshIn& in, HostPattern& out, std::string& err);
+
+// Recomputes hlin = f - m g after a load update.
+void rebuild_load(const MeshIn& in, HostPattern& hp);
+
+// Local node pairs (i, j <= i) in the reference's propagate order (DerivativeAssembler.cpp:205-245).
+extern const int kPairI[10];
+extern const int kPairJ[10];
+
+}  // namespace phx

@@ -1,0 +1,146 @@
+// phx_types.h -- device-resident data layout of one instance and of a batch.
+//
+// Layout in HBM, per instance (all buffers 256-byte aligned, from the context arena):
+//   tets        int4 [m]            node ids
+//   rest64      double[m][12]       Dm^-1 (col-major 9), w = rest volume, lambda, mu
+//   rest32      float [m][12]       same in FP32 (FP32 Hessian kernel)
+//   model       uint8 [m]
+//   node vectors double4 [n]        x, xs (saved state), dx, g, gn, dxprev, x0, v0, v, hlin
+//   SELL-32 3x3 block matrix        chunks of 32 rows, each padded to its longest row;
+//                                   slot s, entry e lives at vals[(s>>5)*288 + e*32 + (s&31)]
+//   lower-block tables              lo_slot / up_slot / seg_ptr / seg_c (scatter map)
+//   node tables                     nseg_ptr / nseg_c (gradient gather), fixmask, mass
+//   PCG vectors (Real = float|double, 4-wide per node): r, z, p[2], q, e; Minv [9][n]
+#pragma once
+
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define PHX_HD __host__ __device__
+#include <vector_types.h>
+#else
+#define PHX_HD
+#endif
+
+namespace phx {
+
+constexpr int kTile = 128;       // tets / nodes / lower blocks per tile
+constexpr int kChunk = 32;       // SELL chunk height (one warp)
+constexpr int kPartials = 5;     // doubles reduced per tile (at most)
+
+// Phases of the per-instance Newton state machine (see control in kernels.cu).
+enum Phase : int32_t {
+  PH_DONE = 0,
+  PH_START = 1,       // control: begin SolveFull
+  PH_VEC = 2,         // node-parallel vector op pending (vecop flags), then next_phase
+  PH_EVAL = 3,        // device: energy + gradient at x
+  PH_EVAL_DONE = 4,   // control
+  PH_ITER = 5,        // control: start of SolveStepInternal
+  PH_HESS = 6,        // device: element Hessian + assembly + Jacobi
+  PH_JACOBI = 7,      // device: Jacobi only (new regularisation shift)
+  PH_LINSETUP = 8,    // device: b = -g, dx = guess
+  PH_RESID = 9,       // device: r = b - (H + s I) dx in FP64, inner rhs
+  PH_PCG = 10,        // device: PCG iterations
+  PH_ACCUM = 11,      // device: dx += e, norms
+  PH_LIN_DONE = 12,   // control: regularisation checks, clamp, line search start
+};
+
+enum VecOp : int32_t {
+  VO_RESTORE = 1,     // x = xs
+  VO_ACCEPT = 2,      // g = gn ; dxprev = alpha * dx
+  VO_SAVE = 4,        // xs = x
+  VO_STEEP = 8,       // dx = -g
+  VO_TRIAL = 16,      // x = xs + alpha * dx
+  VO_VEL = 32,        // v = (x - x0) / dt
+  VO_PRED = 64,       // x0 = x ; v0 = v ; x = x0 + dt * v0
+  VO_GCOPY = 128,     // g = gn
+  VO_ZERODX = 256,    // dx = 0
+};
+
+enum LinStatus : int32_t { LIN_RUNNING = 0, LIN_CONVERGED = 1, LIN_MAXITER = 2, LIN_BREAKDOWN = 3 };
+
+enum DevError : int32_t { DEV_OK = 0, DEV_NONFINITE = 1, DEV_BADSTATE = 2 };
+
+// Solver options as the device sees them (host phx_options, resolved).
+struct DevOpts {
+  int32_t qp_solver, min_step_max_count, min_impr_max_count, num_max_iters, try_steepest;
+  int32_t ls_num_max_iters, ls_num_reg_trials, lsearch_num_try, precision, precond;
+  int32_t max_refine_sweeps, warm_guess, dynamic, pad0;
+  double tol_max_error, tol_min_step, tol_min_impr, max_step_size, ls_tol_max_error;
+  double lsearch_alpha, inner_tol, dt;
+};
+
+// Scalar state of one instance's solve (one thread of the control kernel owns it).
+struct NState {
+  int32_t phase, next_phase, vecop, purpose;   // purpose: 0 init eval, 1 line-search eval
+  int32_t result, it, steepest, min_impr_count;
+  int32_t min_step_count, num_bis, total_bis, reg_trial;
+  int32_t total_reg, sweeps, total_sweeps, lin_status;
+  int32_t pcg_iter, pcg_parity, error, first_step;
+  int32_t step_result, nofix, pad2, pad3;
+  int64_t pcg_total;
+  double obj, opt, opt0, obj_new;
+  double alpha_trial, factor, scale, dx_norm;
+  double b_dot_dx, E_el, E_eval, gg_eval;
+  double normA2, shift, regT, bb;
+  double rr64, rz, rr, pq;
+  double alpha, beta, thr_inner, thr_final;
+};
+
+// Device descriptor of one instance (pointers into the arena).
+struct InstDev {
+  int32_t n, m, nlo, nchunks;
+  int64_t nslots;
+  // mesh + rest data
+  const int32_t* tets;        // [m][4]
+  const double* rest64;       // [m][12]
+  const float* rest32;        // [m][12]
+  const uint8_t* model;       // [m]
+  // pattern / scatter map
+  const int32_t* chunk_off;   // [nchunks+1] slot offsets (multiples of 32)
+  const int32_t* slot_col;    // [nslots]
+  const int32_t* diag_slot;   // [n]
+  const int32_t* lo_rc;       // [nlo][2] (R, C)
+  const int32_t* lo_slot;     // [nlo]
+  const int32_t* up_slot;     // [nlo], -1 on the diagonal
+  const int32_t* seg_ptr;     // [nlo+1]
+  const int32_t* seg_c;       // [10m] e*10 + p, grouped by lower block, element order
+  const int32_t* nseg_ptr;    // [n+1]
+  const int32_t* nseg_c;      // [4m] e*4 + a, grouped by node, element order
+  const uint8_t* fixmask;     // [n] bit d = DoF d fixed
+  const double* mass;         // [n] lumped mass per node
+  double* hlin;               // [n][4] f - m g : linear-load term of energy and gradient
+  // FP64 node vectors [n][4]
+  double* x; double* xs; double* dx; double* g; double* gn; double* dxprev;
+  double* x0; double* v0; double* v; double* r64; double* bvec;
+  // element scratch
+  double* Eloc;               // [m]
+  double* Gloc;               // [m][12]
+  float* Hloc32;              // [m][90]
+  double* Hloc64;             // [m][90]
+  // matrix values (SELL)
+  float* H32;                 // [nslots*9]
+  double* H64;
+  // PCG vectors, Real = float / double, 4-wide per node
+  float* r32; float* z32; float* p32a; float* p32b; float* q32; float* e32; float* minv32;
+  double* rd; double* zd; double* pda; double* pdb; double* qd; double* ed; double* minvd;
+  // reductions
+  double* partials;           // [max tiles][kPartials]
+  uint32_t* counter;          // [1]
+  NState* st;
+  const DevOpts* opts;
+};
+
+// Tile prefix arrays of the active batch (device memory).
+struct BatchDev {
+  const int32_t* num;         // [1] active instances
+  const int32_t* pre_tet;     // [num+1]
+  const int32_t* pre_node;
+  const int32_t* pre_lob;
+  InstDev* inst;              // [num]
+  int32_t* flags;             // [8] device flags: [0] active count, [1] pcg running count, [2] error
+};
+
+PHX_HD inline int64_t sell_addr(int64_t s, int e) { return (s >> 5) * 288 + (int64_t)e * 32 + (s & 31); }
+
+}  // namespace phx

@@ -1,0 +1,81 @@
+"""The product's Newton / line-search state machine, driven on the host, against the oracle's SolveFull."""
+import numpy as np
+import pytest
+
+import oracle
+from physim_gb300 import mesh as M
+import ctl_harness as H
+from conftest import rel
+
+
+def _case(model=0, dims=(2, 2, 6)):
+    if model == 0:
+        return M.cantilever(*dims)
+    return M.make_box(*dims, (0.02 * dims[0], 0.02 * dims[1], 0.02 * dims[2]), 2e5, 0.35, 1000.0, 1,
+                      (0.0, -9.81, 0.0), clamp_face=4, load_face=5, traction=(300.0, -500.0, 200.0))
+
+
+@pytest.mark.parametrize("model", [0, 1])
+def test_static_newton_matches_oracle(ctl_shim, model):
+    m = _case(model)
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    g0 = np.linalg.norm(orc.gradient(x0))
+    # below ~1e-9 the strict E_new < E_old test sits in double-precision noise for the StVK case
+    tol = (1e-9 if model == 0 else 1e-6) * g0
+    xo, ro = orc.solve_static(x0, ls_solver=1, cg_block_jacobi=1, tol_max_error=tol, tol_min_impr=0.0,
+                              tol_min_step=0.0)
+    opts = H.make_opts(tol_max_error=tol, tol_min_impr=0.0, tol_min_step=0.0)
+    x, _, s = H.run(ctl_shim, orc, x0, opts)
+    assert ro["result_name"] == "SUCCESS" and s.result == 1
+    assert s.it == ro["iterations"]
+    assert s.total_bis == ro["bisections"]
+    assert rel(x - x0, xo - x0) < 1e-9
+    assert abs(s.obj - ro["obj"]) <= 1e-10 * abs(ro["obj"])
+    log = orc.last_log()
+    assert s.opt0 == pytest.approx(g0, rel=1e-12)
+
+
+def test_default_tolerances_stop_like_the_reference(ctl_shim):
+    # reference defaults (absolute tolMaxError 1e-6, tolMinImpr 1e-9, tolMinStep 1e-5): MINIMPR/MINSTEP paths
+    m = _case(0, (2, 2, 4))
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    xo, ro = orc.solve_static(x0, ls_solver=1, cg_block_jacobi=1)
+    x, _, s = H.run(ctl_shim, orc, x0, H.make_opts())
+    assert s.result == ro["result"] and s.it == ro["iterations"]
+    assert rel(x - x0, xo - x0) < 1e-7
+
+
+def test_steepest_only(ctl_shim):
+    m = _case(0, (1, 1, 3))
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    xo, ro = orc.solve_static(x0, qp_solver=0, num_max_iters=15)
+    x, _, s = H.run(ctl_shim, orc, x0, H.make_opts(qp_solver=0, num_max_iters=15))
+    assert s.result == ro["result"] and s.it == ro["iterations"] and s.total_bis == ro["bisections"]
+    assert rel(x - x0, xo - x0) < 1e-10
+
+
+def test_implicit_euler_step_matches_oracle(ctl_shim):
+    m = M.make_box(2, 2, 3, (0.02, 0.02, 0.03), 1e5, 0.3, 1000.0, 0, (0.0, -9.81, 0.0), clamp_face=2)
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    v0 = np.zeros(orc.N)
+    v0[1::3] = 0.2
+    v0[m.fixed.astype(bool)] = 0
+    dt = 1e-3
+    kw = dict(tol_max_error=1e-11, tol_min_impr=0.0, tol_min_step=0.0)
+    xo, vo, ro = orc.solve_dynamic(x0, v0, dt, ls_solver=1, cg_block_jacobi=1, **kw)
+    x, v, s = H.run(ctl_shim, orc, x0, H.make_opts(dynamic=1, dt=dt, **kw), dynamic=True, v0=v0)
+    assert s.result == ro["result"] == 1 and s.it == ro["iterations"]
+    assert rel(x - x0, xo - x0) < 1e-9
+    assert rel(v, vo) < 1e-9
+
+
+def test_max_iterations_cap(ctl_shim):
+    m = _case(0, (2, 2, 6))
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    x, _, s = H.run(ctl_shim, orc, x0, H.make_opts(num_max_iters=2, tol_max_error=1e-14))
+    assert s.result == 5 and s.it == 2  # MAXITER after two SolveSteps

@@ -1,0 +1,194 @@
+"""Device-resident Newton solves against the oracle.
+
+Parity bar: converged displacements within 1e-6 relative of the oracle's
+LDLT Newton solve, FP64 energies at the same positions within 1e-9 relative.
+Iterate-level parity is checked against the oracle's CG mode, whose linear
+solver has the same semantics as the device PCG.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import physim_gb300 as px
+from physim_gb300 import mesh as M
+from conftest import rel
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_solution(m, rel_tol):
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    g0 = np.linalg.norm(orc.gradient(x0))
+    x, rep = orc.solve_static(x0, tol_max_error=rel_tol * g0, tol_min_impr=0.0, tol_min_step=0.0)
+    return orc, x0, g0, x, rep
+
+
+def disp_err(x, xr, x0):
+    return rel(x - x0, xr - x0)
+
+
+@pytest.fixture(scope="module")
+def c1_oracle():
+    return oracle_solution(M.cantilever(), 1e-10)
+
+
+def test_cantilever_fp64_plain(gpu_ctx, c1_oracle):
+    orc, x0, g0, xr, rep = c1_oracle
+    inst = px.Instance(gpu_ctx, orc.mesh)
+    o = px.options(tol_max_error=1e-8 * g0, tol_min_impr=0.0, tol_min_step=0.0)
+    x, r = inst.solve_static(o, x0)
+    assert r["result_name"] == "SUCCESS", r
+    assert r["opt"] <= 1e-8 * g0 and abs(r["opt0"] - g0) <= 1e-12 * g0
+    assert disp_err(x, xr, x0) < 1e-6
+    # energy at the same positions
+    Eg, _ = inst.energy_gradient(x)
+    assert abs(Eg - orc.energy(x)) <= 1e-9 * abs(orc.energy(x))
+    assert abs(r["obj"] - orc.energy(x)) <= 1e-9 * abs(orc.energy(x))
+
+
+def test_cantilever_fp32_refine(gpu_ctx, c1_oracle):
+    orc, x0, g0, xr, rep = c1_oracle
+    inst = px.Instance(gpu_ctx, orc.mesh)
+    o = px.options(precision=px.PREC_FP32_REFINE, tol_max_error=1e-8 * g0, tol_min_impr=0.0, tol_min_step=0.0)
+    x, r = inst.solve_static(o, x0)
+    assert r["result_name"] == "SUCCESS", r
+    assert r["refine_sweeps"] > 0
+    assert disp_err(x, xr, x0) < 1e-6
+
+
+def test_iterates_match_oracle_cg_mode(gpu_ctx):
+    m = M.cantilever(3, 3, 10)
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    g0 = np.linalg.norm(orc.gradient(x0))
+    kw = dict(tol_max_error=1e-9 * g0, tol_min_impr=0.0, tol_min_step=0.0)
+    xo, ro = orc.solve_static(x0, ls_solver=1, cg_block_jacobi=1, **kw)
+    log = orc.last_log()
+    inst = px.Instance(gpu_ctx, m)
+    x, r = inst.solve_static(px.options(**kw), x0)
+    assert r["iterations"] == ro["iterations"] and r["bisections"] == ro["bisections"]
+    assert abs(r["pcg_iterations"] - ro["lin_iterations"]) <= 2 * ro["iterations"]
+    assert disp_err(x, xo, x0) < 1e-9
+    # one SolveStep from rest lands on the oracle's first iterate
+    inst2 = px.Instance(gpu_ctx, m)
+    x1, r1 = inst2.solve_step(px.options(**kw), x0)
+    assert abs(r1["obj"] - log["obj"][0]) <= 1e-10 * abs(log["obj"][0])
+
+
+def test_stvk_traction_box(gpu_ctx):
+    m = M.make_box(3, 3, 6, (0.03, 0.03, 0.06), 2e5, 0.35, 1000.0, M.MODEL_STVK, (0.0, 0.0, 0.0),
+                   clamp_face=4, load_face=5, traction=(400.0, -300.0, 800.0))
+    orc, x0, g0, xr, rep = oracle_solution(m, 1e-9)
+    inst = px.Instance(gpu_ctx, m)
+    for prec in (px.PREC_FP64, px.PREC_FP32_REFINE):
+        x, r = inst.solve_static(px.options(precision=prec, tol_max_error=1e-7 * g0, tol_min_impr=0.0,
+                                            tol_min_step=0.0), x0)
+        assert r["result_name"] == "SUCCESS"
+        assert disp_err(x, xr, x0) < 1e-6
+
+
+def test_reference_default_options(gpu_ctx):
+    # reference defaults end in SUCCESS / MINIMPR like the oracle does
+    m = M.cantilever(2, 2, 6)
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    xo, ro = orc.solve_static(x0, ls_solver=1, cg_block_jacobi=1)
+    inst = px.Instance(gpu_ctx, m)
+    x, r = inst.solve_static(px.options(), x0)
+    assert r["result"] == ro["result"] and r["iterations"] == ro["iterations"]
+    assert disp_err(x, xo, x0) < 1e-6
+
+
+def test_implicit_euler_steps(gpu_ctx):
+    m = M.make_box(3, 3, 3, (0.03, 0.03, 0.03), 1e5, 0.45, 1000.0, 0, (0.0, -9.81, 0.0), clamp_face=2)
+    orc = oracle.Oracle(m)
+    x = orc.rest()
+    v = np.zeros(orc.N)
+    v[1::3] = 0.5 * np.sin(np.pi * m.X0[:, 0] / 0.03)
+    v[m.fixed.astype(bool)] = 0
+    inst = px.Instance(gpu_ctx, m)
+    xg, vg = x.copy(), v.copy()
+    kw = dict(tol_max_error=1e-10, tol_min_impr=0.0, tol_min_step=0.0)
+    for step in range(5):
+        x, v, ro = orc.solve_dynamic(x, v, 1e-3, **kw)
+        for prec in (px.PREC_FP64,):
+            xg, vg, r = inst.dynamic_step(px.options(precision=prec, **kw), 1e-3, xg, vg)
+        assert r["result_name"] == "SUCCESS"
+        assert rel(xg - orc.rest(), x - orc.rest()) < 1e-7
+        assert rel(vg, v) < 1e-6
+
+
+def test_batch_equals_alone_bitwise(gpu_ctx):
+    meshes = [M.batch_instance(3, i) for i in range(6)]
+    o = px.options(precision=px.PREC_FP32_REFINE, tol_max_error=1e-7, tol_min_impr=0.0, tol_min_step=0.0)
+    alone = []
+    for m in meshes:
+        inst = px.Instance(gpu_ctx, m)
+        x, r = inst.solve_static(o, m.X0.ravel())
+        alone.append((x, r))
+    insts = [px.Instance(gpu_ctx, m) for m in meshes]
+    reps, xs = gpu_ctx.batch_solve(insts, o, [m.X0.ravel() for m in meshes])
+    for (xa, ra), xb, rb in zip(alone, xs, reps):
+        assert np.array_equal(xa, xb)
+        assert ra["iterations"] == rb["iterations"] and ra["pcg_iterations"] == rb["pcg_iterations"]
+        assert ra["obj"] == rb["obj"]
+
+
+def test_batch_against_oracle(gpu_ctx):
+    meshes = [M.batch_instance(3, i) for i in range(10, 14)]
+    insts = [px.Instance(gpu_ctx, m) for m in meshes]
+    tols = []
+    for m in meshes:
+        orc = oracle.Oracle(m)
+        tols.append(np.linalg.norm(orc.gradient(orc.rest())))
+    o = px.options(precision=px.PREC_FP32_REFINE, tol_max_error=1e-6 * min(tols), tol_min_impr=0.0,
+                   tol_min_step=0.0)
+    reps, xs = gpu_ctx.batch_solve(insts, o, [m.X0.ravel() for m in meshes])
+    for m, x, r in zip(meshes, xs, reps):
+        orc, x0, g0, xr, _ = oracle_solution(m, 1e-10)
+        assert r["result_name"] == "SUCCESS"
+        assert disp_err(x, xr, x0) < 1e-6
+
+
+def test_server_results_same_alone_and_in_the_mix(gpu_ctx):
+    meshes = [M.serving_request(11, i) for i in range(8)]
+    meshes = [m for m in meshes if m.m < 40000][:5]
+    o = px.options(precision=px.PREC_FP32_REFINE, tol_max_error=1e-7, tol_min_impr=0.0, tol_min_step=0.0)
+    alone = {}
+    for i, m in enumerate(meshes):
+        inst = px.Instance(gpu_ctx, m)
+        x, r = inst.solve_static(o, m.X0.ravel())
+        alone[i] = x
+    srv = px.Server(gpu_ctx, max_slots=3, budget_bytes=8 << 30, opts=o)
+    insts = [px.Instance(gpu_ctx, m) for m in meshes]
+    done = {}
+    submitted = 0
+    rounds = 0
+    while len(done) < len(insts):
+        if submitted < len(insts) and rounds % 3 == 0:  # staggered arrivals while others run
+            srv.submit(insts[submitted], submitted)
+            submitted += 1
+        srv.progress()
+        for tag, rep in srv.poll():
+            assert rep["result_name"] == "SUCCESS"
+            done[tag] = insts[tag].positions()
+        rounds += 1
+        assert rounds < 100000
+    for i in alone:
+        assert np.array_equal(alone[i], done[i])
+    srv.close()
+
+
+def test_warm_resolve_after_load_update(gpu_ctx):
+    m = M.serving_request(11, 2)
+    inst = px.Instance(gpu_ctx, m)
+    o = px.options(precision=px.PREC_FP32_REFINE, tol_max_error=1e-8, tol_min_impr=0.0, tol_min_step=0.0)
+    x1, r1 = inst.solve_static(o, m.X0.ravel())
+    m2 = M.perturb_load(m, 11, 2)
+    inst.update_load(m2.force, m2.gravity)
+    x2, r2 = inst.solve_static(o)  # from the previous equilibrium
+    orc, x0, g0, xr, _ = oracle_solution(m2, 1e-10)
+    assert r2["result_name"] == "SUCCESS"
+    assert r2["iterations"] <= r1["iterations"]
+    assert disp_err(x2, xr, x0) < 1e-6

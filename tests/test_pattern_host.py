@@ -1,0 +1,161 @@
+"""The product's host pattern builder (physim_gb300/csrc/pattern.cpp) against the oracle.
+
+Bit-exact requirements: the lower block pattern (Eigen's stored CSC, expanded
+per DoF), and the scatter map of every tet's 10 local node pairs onto it.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle
+from physim_gb300 import mesh as M
+
+
+def build(shim, m):
+    arrs = [np.ascontiguousarray(m.X0, dtype=np.float64).ravel(), np.ascontiguousarray(m.T, dtype=np.int32).ravel(),
+            np.ascontiguousarray(m.lame, dtype=np.float64).ravel(), np.ascontiguousarray(m.rho, dtype=np.float64),
+            np.ascontiguousarray(m.model, dtype=np.uint8), np.ascontiguousarray(m.fixed, dtype=np.uint8),
+            np.ascontiguousarray(m.force, dtype=np.float64), np.ascontiguousarray(m.gravity, dtype=np.float64)]
+    shim.pat_build.argtypes = [C.c_int, C.c_int] + [C.c_void_p] * 8
+    shim.pat_error.restype = C.c_char_p
+    rc = shim.pat_build(m.n, m.m, *[a.ctypes.data for a in arrs])
+    if rc != 0:
+        return None, shim.pat_error().decode()
+    sz = np.zeros(5, dtype=np.int64)
+    shim.pat_sizes(sz.ctypes.data_as(C.c_void_p))
+    n, mm, nlo, nch, nslots = (int(v) for v in sz)
+    out = {"n": n, "m": mm, "nlo": nlo, "nchunks": nch, "nslots": nslots}
+
+    def get(name, count, dtype):
+        a = np.zeros(count, dtype=dtype)
+        getattr(shim, "pat_" + name)(a.ctypes.data_as(C.c_void_p))
+        return a
+
+    out["lo_rc"] = get("lo_rc", 2 * nlo, np.int32).reshape(-1, 2)
+    out["lo_colptr"] = get("lo_colptr", n + 1, np.int32)
+    out["scatter"] = get("scatter", 10 * mm, np.int32).reshape(-1, 10)
+    out["seg_ptr"] = get("seg_ptr", nlo + 1, np.int32)
+    out["seg_c"] = get("seg_c", 10 * mm, np.int32)
+    out["nseg_ptr"] = get("nseg_ptr", n + 1, np.int32)
+    out["nseg_c"] = get("nseg_c", 4 * mm, np.int32)
+    out["chunk_off"] = get("chunk_off", nch + 1, np.int32)
+    out["slot_col"] = get("slot_col", nslots, np.int32)
+    out["diag_slot"] = get("diag_slot", n, np.int32)
+    out["lo_slot"] = get("lo_slot", nlo, np.int32)
+    out["up_slot"] = get("up_slot", nlo, np.int32)
+    out["rest64"] = get("rest64", 12 * mm, np.float64).reshape(-1, 12)
+    out["mass"] = get("mass", n, np.float64)
+    out["hlin"] = get("hlin", 4 * n, np.float64).reshape(-1, 4)
+    out["fixmask"] = get("fixmask", n, np.uint8)
+    return out, None
+
+
+def csc_from_blocks(P):
+    """Per-DoF lower CSC implied by the block pattern (column-major blocks)."""
+    n = P["n"]
+    colptr = [0]
+    rows = []
+    for Cn in range(n):
+        ks = range(P["lo_colptr"][Cn], P["lo_colptr"][Cn + 1])
+        for b in range(3):
+            for k in ks:
+                R = P["lo_rc"][k, 0]
+                rows.extend([3 * R, 3 * R + 1, 3 * R + 2])
+            colptr.append(len(rows))
+    return np.array(colptr, dtype=np.int32), np.array(rows, dtype=np.int32)
+
+
+MESHES = [
+    lambda: M.cantilever(3, 2, 5),
+    lambda: M.batch_instance(3, 4),
+    lambda: M.make_box(1, 1, 1, (1.0, 1.0, 1.0), 1e5, 0.3),
+]
+
+
+@pytest.mark.parametrize("make", MESHES)
+def test_pattern_and_scatter_bit_exact(pattern_shim, make):
+    m = make()
+    P, err = build(pattern_shim, m)
+    assert err is None, err
+    o = oracle.Oracle(m)
+    cp, ri = o.pattern()
+    mcp, mri = csc_from_blocks(P)
+    assert np.array_equal(cp, mcp) and np.array_equal(ri, mri)
+    assert np.array_equal(P["scatter"], o.scatter_map())
+    assert P["nlo"] == m.n + len(M.unique_edges(m.T))
+
+
+@pytest.mark.parametrize("make", MESHES)
+def test_segments_and_sell_layout(pattern_shim, make):
+    m = make()
+    P, _ = build(pattern_shim, m)
+    n, nlo = P["n"], P["nlo"]
+    # segments: every (tet, pair) exactly once, grouped by target block, element order inside
+    assert P["seg_ptr"][-1] == 10 * m.m
+    flat = P["scatter"].ravel()
+    for k in range(0, nlo, max(1, nlo // 200)):
+        seg = P["seg_c"][P["seg_ptr"][k]:P["seg_ptr"][k + 1]]
+        assert np.all(flat[seg] == k) and np.all(np.diff(seg) > 0)
+    assert np.array_equal(np.sort(P["seg_c"]), np.arange(10 * m.m))
+    # node segments
+    assert np.array_equal(np.sort(P["nseg_c"]), np.arange(4 * m.m))
+    for v in range(0, n, max(1, n // 100)):
+        seg = P["nseg_c"][P["nseg_ptr"][v]:P["nseg_ptr"][v + 1]]
+        assert np.all(m.T.ravel()[seg] == v) and np.all(np.diff(seg) > 0)
+    # SELL: every full block (R,C) and (C,R) lands in a distinct slot of the right row/column
+    def slot_row(s):
+        chunk = np.searchsorted(P["chunk_off"], s, side="right") - 1
+        return chunk * 32 + (s - P["chunk_off"][chunk]) % 32
+    used = np.zeros(P["nslots"], dtype=np.int32)
+    for k in range(nlo):
+        R, Cn = P["lo_rc"][k]
+        s = P["lo_slot"][k]
+        assert slot_row(s) == R and P["slot_col"][s] == Cn
+        used[s] += 1
+        if R != Cn:
+            u = P["up_slot"][k]
+            assert slot_row(u) == Cn and P["slot_col"][u] == R
+            used[u] += 1
+        else:
+            assert P["up_slot"][k] == -1 and P["diag_slot"][R] == s
+    assert used.max() == 1 and used.sum() == 2 * nlo - n
+    # rows sorted by column within the SELL order
+    for v in range(0, n, max(1, n // 50)):
+        c = v // 32
+        L = (P["chunk_off"][c + 1] - P["chunk_off"][c]) // 32
+        cols = [P["slot_col"][P["chunk_off"][c] + k * 32 + v % 32] for k in range(L)]
+        real = [col for k, col in enumerate(cols) if used[P["chunk_off"][c] + k * 32 + v % 32]]
+        assert real == sorted(real)
+
+
+def test_rest_data_and_loads(pattern_shim):
+    m = M.batch_instance(3, 9)
+    P, _ = build(pattern_shim, m)
+    vol = M.signed_volumes(m.X0, m.T)
+    assert np.allclose(P["rest64"][:, 9], vol, rtol=1e-14)
+    for e in range(0, m.m, 97):
+        Dm = np.stack([m.X0[m.T[e, c + 1]] - m.X0[m.T[e, 0]] for c in range(3)], axis=1)
+        assert np.allclose(P["rest64"][e, :9].reshape(3, 3).T @ Dm, np.eye(3), atol=1e-10)
+    mass = np.zeros(m.n)
+    for e in range(m.m):
+        mass[m.T[e]] += m.rho[e] * vol[e] / 4
+    assert np.allclose(P["mass"], mass, rtol=1e-13)
+    h = m.force.reshape(-1, 3) - mass[:, None] * m.gravity[None, :]
+    assert np.allclose(P["hlin"][:, :3], h, rtol=1e-14, atol=0)
+    assert np.array_equal(P["fixmask"], m.fixed.reshape(-1, 3) @ np.array([1, 2, 4]))
+
+
+def test_rejects_malformed_meshes(pattern_shim):
+    base = M.cantilever(2, 1, 2)
+    bad = base.copy(); bad.T[3, 1] = base.n + 5
+    assert build(pattern_shim, bad)[1].startswith("mesh: node id out of range")
+    bad = base.copy(); bad.T[2, [1, 2]] = bad.T[2, [2, 1]]
+    assert "non-positive rest volume" in build(pattern_shim, bad)[1]
+    bad = base.copy(); bad.T[0, 1] = bad.T[0, 0]
+    assert "repeated node" in build(pattern_shim, bad)[1]
+    bad = base.copy(); bad.X0 = np.vstack([bad.X0, [[9.0, 9.0, 9.0]]])
+    bad.fixed = np.zeros(3 * (base.n + 1), dtype=np.uint8); bad.force = np.zeros(3 * (base.n + 1))
+    assert "belongs to no tet" in build(pattern_shim, bad)[1]
+    bad = base.copy(); bad.lame[4, 0] = np.nan
+    assert "non-finite" in build(pattern_shim, bad)[1]
