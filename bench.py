@@ -1,0 +1,444 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 tet-FEM Newton path.
+
+Default workload (the one the headline metric's target is stated on): the
+batched uneven stream -- 512 independent 6-tet box meshes, nx, ny in [3, 12],
+nz in [6, 48], hex edge 1 cm, Neo-Hookean or StVK 50/50, E log-uniform in
+[1e4, 1e6] Pa, nu in [0.2, 0.45], one face clamped and the opposite face under
+a traction of 1e2..1e3 Pa (seeded synthetic inputs).  One "step" solves every
+instance of the batch to static equilibrium at ||g|| <= 1e-6 ||g0||.
+
+  value     batched FP32+refinement solves/s, positions reset on the device,
+            everything resident in HBM (device-timed with CUDA events)
+  e2e       the same solves through the public C ABI from host meshes:
+            instance creation (pattern + upload), solve, download, destroy
+  plain_gpu the plain FP64 device-resident drop-in, one instance per solve
+            call like the reference's per-object solver, on a bounded sample
+  cpu_baseline / --impl reference
+            the CPU restatement of the reference's Newton path (LDLT Newton,
+            the reference's default linear solver), all host threads, on a
+            bounded sample of the same instances
+
+Other workloads: --workload cantilever (8x8x32, FP64 plain vs the CPU
+reference), large (48x48x192 single instance), serve (Poisson stream),
+dynamics (implicit Euler, 32^3 blocks).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+
+
+# ---------------------------------------------------------------------------
+# helpers
+# ---------------------------------------------------------------------------
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    return PEAKS_FALLBACK, "fallback"
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        torch.cuda.set_device(local)
+    return world, rank, local, dist
+
+
+def dist_max(dist, value):
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_sum(dist, value):
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def dist_barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def percentile(a, q):
+    a = sorted(a)
+    if not a:
+        return None
+    k = (len(a) - 1) * q / 100.0
+    f, c = math.floor(k), math.ceil(k)
+    return a[f] if f == c else a[f] + (a[c] - a[f]) * (k - f)
+
+
+# ---------------------------------------------------------------------------
+# CPU reference arm: the oracle restatement of the reference's Newton path
+# ---------------------------------------------------------------------------
+def cpu_reference(meshes, budget_s, tol_rel, threads):
+    import oracle
+    t0 = time.perf_counter()
+    done = 0
+    sols = {}
+    for i, m in enumerate(meshes):
+        orc = oracle.Oracle(m)
+        x0 = orc.rest()
+        g0 = float(np.linalg.norm(orc.gradient(x0)))
+        x, rep = orc.solve_static(x0, tol_max_error=tol_rel * g0, tol_min_impr=0.0, tol_min_step=0.0,
+                                  threads=threads)
+        sols[i] = (x, rep)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return done, dt, sols
+
+
+# ---------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------
+def batch_meshes(count, seed):
+    from physim_gb300 import mesh as M
+    return [M.batch_instance(seed, i) for i in range(count)]
+
+
+def run_batch(args, world, rank, dist):
+    import physim_gb300 as px
+    from physim_gb300 import build
+    build.build()
+    count = args.count
+    meshes = batch_meshes(count, seed=3 + 1000 * rank)
+    tets = sum(m.m for m in meshes)
+    ctx = px.Context(0, arena_bytes=int(args.arena_gb * (1 << 30)))
+    insts = [px.Instance(ctx, m) for m in meshes]
+    served = px.options(precision=px.PREC_FP32_REFINE, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0,
+                        tol_min_step=0.0, pcg_chunk=args.pcg_chunk, inner_tol=args.inner_tol)
+    plain = px.options(precision=px.PREC_FP64, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0,
+                       tol_min_step=0.0, pcg_chunk=args.pcg_chunk)
+
+    def step():
+        for it in insts:
+            it.reset()
+        return ctx.batch_solve(insts, served)[0]
+
+    for _ in range(args.warmup):
+        reps = step()
+    bad = [r for r in reps if r["result_name"] != "SUCCESS"]
+    # timed region: device events on the library stream, clocks sampled meanwhile
+    ctx.profile(True)
+    ctx.profile_reset()
+    clocks = ClockSampler(0)
+    clocks.start()
+    dist_barrier(dist)
+    launches0 = ctx.kernel_launches()
+    ctx.mark(0)
+    for _ in range(args.steps):
+        reps = step()
+    ctx.mark(1)
+    ms = ctx.elapsed_ms(0, 1)
+    launches = ctx.kernel_launches() - launches0
+    clk = clocks.stop()
+    kinds = ["control", "vecop", "elem_eg", "gather", "elem_hess", "assemble", "jacobi", "linsetup", "resid",
+             "spmv", "pcg_update", "accum"]
+    prof = {}
+    for k in kinds:
+        n, t = ctx.profile_read(k)
+        prof[k] = {"launches": n, "ms": t, "bytes": ctx.profile_bytes(k)}
+    ctx.profile(False)
+    ms = dist_max(dist, ms)
+    total = dist_sum(dist, float(count * args.steps))
+    value = total / (ms / 1e3)
+    rel_res = [r["opt"] / r["opt0"] for r in reps if r["opt0"] > 0]
+    newton = [r["iterations"] for r in reps]
+    pcg = [r["pcg_iterations"] for r in reps]
+
+    # dominant kernel roofline
+    peaks, peaks_kind = load_peaks()
+    dom = max(prof, key=lambda k: prof[k]["ms"])
+    dk = prof[dom]
+    achieved = dk["bytes"] / (dk["ms"] / 1e3) / 1e9 if dk["ms"] > 0 else 0.0
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tfile):
+        with open(tfile) as f:
+            tj = json.load(f)
+        if dom in tj and dk["launches"]:
+            traffic = tj[dom]["dram_over_algorithmic"] * dk["bytes"] / dk["launches"]
+    roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"],
+                "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
+                "traffic": traffic, "algorithmic_bytes_per_launch": dk["bytes"] / max(1, dk["launches"]),
+                "avg_launch_us": 1e3 * dk["ms"] / max(1, dk["launches"]), "peak_kind": peaks_kind}
+    spmv = prof["spmv"]
+    spmv_gbs = spmv["bytes"] / (spmv["ms"] / 1e3) / 1e9 if spmv["ms"] > 0 else None
+    eh = prof["elem_hess"]
+
+    # e2e through the public API from host meshes: create, solve, download, destroy
+    e2e_ms = []
+    h2d = 0
+    d2h = 0
+    sub = meshes if args.e2e_full else meshes[: max(1, count // 4)]
+    for _ in range(1):
+        t0 = time.perf_counter()
+        tmp = [px.Instance(ctx, m) for m in sub]
+        xs = [m.X0.ravel().copy() for m in sub]
+        r2, xo = ctx.batch_solve(tmp, served, xs)
+        for it in tmp:
+            it.close()
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        h2d = sum(m.X0.nbytes + m.T.nbytes + m.lame.nbytes + m.rho.nbytes + m.model.nbytes + m.fixed.nbytes +
+                  m.force.nbytes for m in sub) + sum(x.nbytes for x in xs)
+        d2h = sum(x.nbytes for x in xo)
+    e2e_value = len(sub) / (statistics.median(e2e_ms) / 1e3)
+
+    # plain FP64 drop-in on a bounded sample (one solve call per instance)
+    order = np.argsort([m.m for m in meshes])
+    pick = order[np.linspace(0, len(order) - 1, min(args.plain_sample, len(order))).astype(int)]
+    t0 = time.perf_counter()
+    plain_reps = []
+    for i in pick:
+        insts[i].reset()
+        _, r = insts[i].solve_static(plain)
+        plain_reps.append(r)
+    plain_s = time.perf_counter() - t0
+    # the same sample through the served path, batched, for a like-for-like ratio
+    for i in pick:
+        insts[i].reset()
+    ctx.mark(2)
+    served_sample = ctx.batch_solve([insts[i] for i in pick], served)[0]
+    ctx.mark(3)
+    served_sample_ms = ctx.elapsed_ms(2, 3)
+    plain_value = len(pick) / plain_s
+
+    out = {
+        "metric": "static solves/s @1e-6 rel residual: served batched FP32+refine (value) vs plain FP64 GPU drop-in",
+        "value": round(value, 3), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (Hessian, PCG) + fp64 (gradient, residual, energy)",
+        "data": "synthetic (seeded)",
+        "config": {"workload": f"batched uneven boxes: {count} instances, 6-tet hexes, {tets} tets "
+                               f"(configs[2])", "instances": count, "tets": tets, "tol_rel": args.tol_rel,
+                   "l2": "inputs larger than L2 (per-step working set well above 129 MB)",
+                   "inner_tol": args.inner_tol, "pcg_chunk": args.pcg_chunk},
+        "e2e": {"value": round(e2e_value, 3), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "sample": f"{len(sub)} instances created from host meshes, "
+                "solved, downloaded and destroyed per step"},
+        "roofline": roofline,
+        "plain_gpu": {"value": round(plain_value, 3), "unit": "solves/s",
+                      "sample": f"{len(pick)} instances across the size range, one FP64 solve call each",
+                      "served_same_sample": round(len(pick) / (served_sample_ms / 1e3), 3),
+                      "ratio_served_over_plain": round((len(pick) / (served_sample_ms / 1e3)) / plain_value, 2),
+                      "results": sorted(set(r["result_name"] for r in plain_reps))},
+        "elements_per_s": round(sum(r["hessian_evals"] * m.m for r, m in zip(reps, meshes)) * args.steps /
+                                (eh["ms"] / 1e3), 1) if eh["ms"] > 0 else None,
+        "elem_hess": {"launches": eh["launches"], "ms": round(eh["ms"], 3)},
+        "spmv_gbs": None if spmv_gbs is None else round(spmv_gbs, 1),
+        "kernels_ms": {k: round(v["ms"], 3) for k, v in prof.items()},
+        "accuracy": {"rel_residual_max": max(rel_res) if rel_res else None,
+                     "non_success": len(bad), "newton_median": statistics.median(newton),
+                     "pcg_iters_median": statistics.median(pcg)},
+        "clocks": clk, "gpu_launches": int(launches),
+    }
+    # CPU baseline on a bounded sample (rank 0 only)
+    if rank == 0 and not args.no_cpu:
+        cpu_pick = list(order[np.linspace(0, len(order) - 1, 24).astype(int)])
+        done, secs, sols = cpu_reference([meshes[i] for i in cpu_pick], args.cpu_seconds, args.tol_rel,
+                                         os.cpu_count())
+        out["cpu_baseline"] = {"value": round(done / secs, 4), "unit": "solves/s", "cores": os.cpu_count(),
+                               "kind": "port", "sample": f"{done} instances across the size range, LDLT Newton "
+                                                         f"(reference default linear solver), {secs:.1f} s"}
+        # accuracy of the served results against the FP64 oracle on those instances
+        errs = []
+        for j, i in enumerate(cpu_pick[:done]):
+            x0 = meshes[i].X0.ravel()
+            xg = insts[i].positions()
+            xr = sols[j][0]
+            errs.append(float(np.linalg.norm(xg - xr) / max(np.linalg.norm(xr - x0), 1e-300)))
+        out["accuracy"]["rel_displacement_err_max"] = max(errs) if errs else None
+    ctx.close()
+    return out
+
+
+def run_reference(args, world, rank):
+    """--impl reference: the CPU restatement of the reference path, all host threads."""
+    if rank != 0:
+        return None
+    meshes = batch_meshes(args.count, seed=3)
+    order = np.argsort([m.m for m in meshes])
+    vals = []
+    samples = []
+    for _ in range(args.warmup):
+        cpu_reference([meshes[order[len(order) // 2]]], 1e9, args.tol_rel, os.cpu_count())
+    for s in range(args.steps):
+        pick = list(order[np.linspace(0, len(order) - 1, 16).astype(int)])
+        pick = pick[s % 4::4] + pick[:0]
+        done, secs, _ = cpu_reference([meshes[i] for i in pick], args.cpu_seconds / max(1, args.steps), args.tol_rel,
+                                      os.cpu_count())
+        vals.append(done / secs)
+        samples.append(done)
+    v = statistics.median(vals)
+    return {"impl": "reference", "metric": "static solves/s @1e-6 rel residual: served batched FP32+refine (value) "
+                                           "vs plain FP64 GPU drop-in",
+            "value": round(v, 4), "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded)",
+            "config": {"workload": f"batched uneven boxes: {args.count} instances (configs[2])",
+                       "tol_rel": args.tol_rel},
+            "cpu_baseline": {"value": round(v, 4), "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"{sum(samples)} instances across the size range, LDLT Newton"},
+            "e2e": {"value": round(v, 4), "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def run_cantilever(args, world, rank, dist):
+    import oracle
+    import physim_gb300 as px
+    from physim_gb300 import build, mesh as M
+    build.build()
+    m = M.cantilever()
+    ctx = px.Context(0, arena_bytes=4 << 30)
+    inst = px.Instance(ctx, m)
+    x0 = m.X0.ravel().copy()
+    o = px.options(precision=px.PREC_FP64, tol_rel=1e-8, tol_max_error=0.0, tol_min_impr=0.0, tol_min_step=0.0,
+                   pcg_chunk=args.pcg_chunk)
+    for _ in range(args.warmup):
+        inst.reset(); inst.solve_static(o)
+    ctx.profile(True); ctx.profile_reset()
+    clocks = ClockSampler(0); clocks.start()
+    ctx.mark(0)
+    for _ in range(args.steps):
+        inst.reset()
+        x, r = inst.solve_static(o)
+    ctx.mark(1)
+    ms = ctx.elapsed_ms(0, 1)
+    clk = clocks.stop()
+    out = {"metric": "cantilever static solves/s (FP64 plain GPU Newton, ||g||/||g0|| < 1e-8)",
+           "value": round(args.steps / (ms / 1e3), 3), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
+           "config": {"workload": "cantilever 8x8x32 hexes x 6 tets (configs[0])"}, "report": r, "clocks": clk}
+    if rank == 0 and not args.no_cpu:
+        orc = oracle.Oracle(m)
+        g0 = float(np.linalg.norm(orc.gradient(x0)))
+        t0 = time.perf_counter()
+        xr, rr = orc.solve_static(x0, tol_max_error=1e-8 * g0, tol_min_impr=0.0, tol_min_step=0.0,
+                                  threads=os.cpu_count())
+        secs = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round(1 / secs, 4), "unit": "solves/s", "cores": os.cpu_count(),
+                               "kind": "port", "sample": "one LDLT Newton solve", "report": rr}
+        out["rel_displacement_err"] = float(np.linalg.norm(x - xr) / np.linalg.norm(xr - x0))
+        out["speedup_vs_cpu"] = round(secs / (ms / 1e3 / args.steps), 1)
+    ctx.close()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "cantilever"])
+    ap.add_argument("--count", type=int, default=512)
+    ap.add_argument("--tol-rel", type=float, default=1e-6)
+    ap.add_argument("--inner-tol", type=float, default=1e-3)
+    ap.add_argument("--pcg-chunk", type=int, default=32)
+    ap.add_argument("--plain-sample", type=int, default=24)
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--arena-gb", type=float, default=48.0)
+    ap.add_argument("--e2e-full", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world, rank, local, dist = dist_setup()
+    if args.impl == "reference":
+        out = run_reference(args, world, rank)
+        if out is not None:
+            print(json.dumps(out), flush=True)
+        return
+    if args.workload == "cantilever":
+        out = run_cantilever(args, world, rank, dist)
+    else:
+        out = run_batch(args, world, rank, dist)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

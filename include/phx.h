@@ -99,6 +99,7 @@ typedef struct phx_options {
   int32_t max_refine_sweeps;  /* FP64 refinement sweeps per linear solve (FP32 path) */
   int32_t warm_guess;         /* 1: PCG starts from the previous accepted step (EigenCG solveWithGuess) */
   int32_t pcg_chunk;          /* PCG iterations per device round (launch granularity) */
+  double tol_rel;             /* if > 0: stop at ||g|| <= max(tol_max_error, tol_rel * ||g0||), g0 after loading */
 } phx_options;
 
 typedef struct phx_report {
@@ -113,6 +114,8 @@ typedef struct phx_report {
   double opt;               /* final ||g|| */
   double opt0;              /* ||g|| at the first step (after the loads are applied) */
   double seconds;           /* wall time of the call */
+  int32_t hessian_evals;    /* element Hessian + assembly passes */
+  int32_t reserved;
 } phx_report;
 
 /* ---- library ----------------------------------------------------------- */
@@ -134,6 +137,8 @@ int phx_instance_create(phx_context ctx, const phx_mesh* mesh, phx_instance* out
 int phx_instance_destroy(phx_instance inst);
 int phx_instance_sizes(phx_instance inst, int64_t* num_dofs, int64_t* hessian_nnz,
                        int64_t* lower_blocks, int64_t* full_blocks);
+/* Positions back to rest (Tag::Position_0), velocities and the warm-start step to zero, on the device. */
+int phx_instance_reset(phx_instance inst);
 /* Model state (ISimulable::Get/SetDOFVector, Tag::Position_X / Tag::Velocity, Simulable.h:55-94) */
 int phx_instance_set_positions(phx_instance inst, const double* x);
 int phx_instance_get_positions(phx_instance inst, double* x);
@@ -194,6 +199,12 @@ int phx_server_poll(phx_server srv, int64_t* tags, phx_report* reps, int32_t cap
 int phx_profile_enable(phx_context ctx, int32_t on);
 int phx_profile_read(phx_context ctx, const char* kind, int64_t* launches, double* total_ms);
 int phx_profile_reset(phx_context ctx);
+/* Algorithmic bytes the launches of one kernel kind moved since the last reset (profiling on):
+ * matrix blocks, indices and vectors each launch must read or write once, per active instance. */
+int phx_profile_bytes(phx_context ctx, const char* kind, double* bytes);
+/* CUDA events on the library's stream: record slot (0..15); elapsed ms between two recorded slots. */
+int phx_timer_mark(phx_context ctx, int32_t slot);
+int phx_timer_elapsed(phx_context ctx, int32_t slot_a, int32_t slot_b, double* ms);
 /* Launch count of the library's own kernels since creation (or the last reset). */
 int64_t phx_kernel_launches(phx_context ctx);
 

@@ -28,12 +28,12 @@ PHX_OK, PHX_EINVAL, PHX_ENOMEM, PHX_ETIMEOUT, PHX_ECUDA, PHX_EBUSY, PHX_ENOTFOUN
 EXPORTS = [
     "phx_version", "phx_last_error", "phx_default_options", "phx_context_create", "phx_context_destroy",
     "phx_context_memory", "phx_instance_create", "phx_instance_destroy", "phx_instance_sizes",
-    "phx_instance_set_positions", "phx_instance_get_positions", "phx_instance_set_velocities",
+    "phx_instance_reset", "phx_instance_set_positions", "phx_instance_get_positions", "phx_instance_set_velocities",
     "phx_instance_get_velocities", "phx_instance_update_load", "phx_energy_gradient", "phx_hessian",
     "phx_hessian_pattern", "phx_scatter_map", "phx_element_local", "phx_solve_static", "phx_solve_step",
     "phx_dynamic_step", "phx_batch_solve", "phx_batch_dynamic_step", "phx_server_create", "phx_server_destroy",
     "phx_server_submit", "phx_server_progress", "phx_server_poll", "phx_profile_enable", "phx_profile_read",
-    "phx_profile_reset", "phx_kernel_launches",
+    "phx_profile_reset", "phx_profile_bytes", "phx_kernel_launches", "phx_timer_mark", "phx_timer_elapsed",
 ]
 
 
@@ -58,14 +58,14 @@ class Options(C.Structure):
                 ("ls_tol_max_error", C.c_double), ("ls_num_reg_trials", C.c_int32), ("lsearch_type", C.c_int32),
                 ("lsearch_alpha", C.c_double), ("lsearch_num_try", C.c_int32), ("precision", C.c_int32),
                 ("precond", C.c_int32), ("inner_tol", C.c_double), ("max_refine_sweeps", C.c_int32),
-                ("warm_guess", C.c_int32), ("pcg_chunk", C.c_int32)]
+                ("warm_guess", C.c_int32), ("pcg_chunk", C.c_int32), ("tol_rel", C.c_double)]
 
 
 class Report(C.Structure):
     _fields_ = [("result", C.c_int32), ("iterations", C.c_int32), ("bisections", C.c_int32),
                 ("reg_trials", C.c_int32), ("pcg_iterations", C.c_int64), ("refine_sweeps", C.c_int32),
                 ("status", C.c_int32), ("obj", C.c_double), ("opt", C.c_double), ("opt0", C.c_double),
-                ("seconds", C.c_double)]
+                ("seconds", C.c_double), ("hessian_evals", C.c_int32), ("reserved", C.c_int32)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}
@@ -95,6 +95,7 @@ def lib():
         "phx_instance_create": ([vp, C.POINTER(Mesh_), C.POINTER(vp)], C.c_int),
         "phx_instance_destroy": ([vp], C.c_int),
         "phx_instance_sizes": ([vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)], C.c_int),
+        "phx_instance_reset": ([vp], C.c_int),
         "phx_instance_set_positions": ([vp, vp], C.c_int),
         "phx_instance_get_positions": ([vp, vp], C.c_int),
         "phx_instance_set_velocities": ([vp, vp], C.c_int),
@@ -117,8 +118,11 @@ def lib():
         "phx_server_poll": ([vp, vp, vp, i32], C.c_int),
         "phx_profile_enable": ([vp, i32], C.c_int),
         "phx_profile_read": ([vp, C.c_char_p, C.POINTER(i64), C.POINTER(dbl)], C.c_int),
+        "phx_profile_bytes": ([vp, C.c_char_p, C.POINTER(dbl)], C.c_int),
         "phx_profile_reset": ([vp], C.c_int),
         "phx_kernel_launches": ([vp], i64),
+        "phx_timer_mark": ([vp, i32], C.c_int),
+        "phx_timer_elapsed": ([vp, i32, i32, C.POINTER(dbl)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -171,6 +175,15 @@ class Context:
         _check(lib().phx_context_memory(self.h, C.byref(u), C.byref(c)))
         return u.value, c.value
 
+    def mark(self, slot: int):
+        """Records CUDA event `slot` on the library's stream."""
+        _check(lib().phx_timer_mark(self.h, int(slot)))
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        ms = C.c_double()
+        _check(lib().phx_timer_elapsed(self.h, int(a), int(b), C.byref(ms)))
+        return ms.value
+
     def kernel_launches(self) -> int:
         return int(lib().phx_kernel_launches(self.h))
 
@@ -179,6 +192,11 @@ class Context:
 
     def profile_reset(self):
         _check(lib().phx_profile_reset(self.h))
+
+    def profile_bytes(self, kind: str) -> float:
+        b = C.c_double()
+        _check(lib().phx_profile_bytes(self.h, kind.encode(), C.byref(b)))
+        return b.value
 
     def profile_read(self, kind: str):
         n = C.c_int64(); ms = C.c_double()
@@ -190,7 +208,7 @@ class Context:
         arr = (C.c_void_p * n)(*[i.h.value for i in insts])
         reps = (Report * n)()
         if xs is not None:
-            xs = [np.ascontiguousarray(x, dtype=np.float64) for x in xs]
+            xs = [np.array(x, dtype=np.float64, copy=True).ravel() for x in xs]
             xp = (C.c_void_p * n)(*[x.ctypes.data for x in xs])
         else:
             xp = None
@@ -244,6 +262,10 @@ class Instance:
         a, b, c, d = (C.c_int64() for _ in range(4))
         _check(lib().phx_instance_sizes(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
         return {"ndof": a.value, "nnz": b.value, "lower_blocks": c.value, "full_blocks": d.value}
+
+    def reset(self):
+        """Positions back to rest, velocities and the warm-start step to zero (device-side copies)."""
+        _check(lib().phx_instance_reset(self.h))
 
     def set_positions(self, x):
         x = np.ascontiguousarray(x, dtype=np.float64)

@@ -132,6 +132,8 @@ struct phx_context_s {
   int32_t* h_flags = nullptr; // pinned mirror
   std::vector<int32_t> h_pre;
   const void* batch_owner = nullptr;  // who set the batch buffers last
+  double* d_algo = nullptr;           // [K_COUNT] algorithmic bytes per kernel kind (profiling)
+  cudaEvent_t marks[16] = {};
 };
 
 struct phx_instance_s {
@@ -258,6 +260,7 @@ int set_batch(phx_context ctx, const std::vector<phx_instance>& list, BatchDev& 
   B.pre_lob = ctx->d_pre + 2 * (ctx->cap + 1);
   B.inst = ctx->d_inst;
   B.flags = ctx->d_flags;
+  B.algo_total = ctx->profiling ? ctx->d_algo : nullptr;
   const int sms = std::max(1, ctx->num_sms);
   G.tet = std::min(pt[num], sms * 8);
   G.node = std::min(pn[num], sms * 16);
@@ -329,6 +332,7 @@ DevOpts make_opts(const phx_options* o, bool dynamic, double dt) {
   d.lsearch_alpha = o->lsearch_alpha;
   d.inner_tol = o->inner_tol;
   d.dt = dt;
+  d.tol_rel = o->tol_rel;
   return d;
 }
 
@@ -342,6 +346,7 @@ int validate_opts(const phx_options* o) {
     return set_err(PHX_EINVAL, "options: non-positive iteration limit");
   if (!(o->lsearch_alpha > 0 && o->lsearch_alpha < 1)) return set_err(PHX_EINVAL, "options: lsearch_alpha out of (0,1)");
   if (o->pcg_chunk < 1 || o->pcg_chunk > 4096) return set_err(PHX_EINVAL, "options: pcg_chunk out of [1,4096]");
+  if (!(o->tol_rel >= 0.0)) return set_err(PHX_EINVAL, "options: tol_rel must be >= 0");
   return PHX_OK;
 }
 
@@ -394,6 +399,8 @@ void fill_report(const NState& s, bool step, double seconds, phx_report* r) {
   r->opt = s.opt;
   r->opt0 = s.opt0;
   r->seconds = seconds;
+  r->hessian_evals = s.hess_count;
+  r->reserved = 0;
 }
 
 // Runs a set of instances (states already reset to PH_START) until all are done.
@@ -413,12 +420,30 @@ int run_to_completion(phx_context ctx, const std::vector<phx_instance>& list, bo
   }
 }
 
+// Algorithmic bytes one launch of each kernel moves for this instance: every input it
+// must read and every output it must write, once (padding, re-reads and caches excluded).
+void set_algo_bytes(InstDev& D, bool fp64) {
+  const double s = fp64 ? 8.0 : 4.0, n = D.n, m = D.m, nlo = D.nlo, nfull = 2.0 * D.nlo - D.n, N = 3.0 * D.n;
+  for (int k = 0; k < 12; ++k) D.algo[k] = 0.0;
+  D.algo[K_ELEM_EG] = 16 * m + 96 * m + m + 8 * N + 96 * m + 8 * m;
+  D.algo[K_GATHER] = 96 * m + 16 * m + 4 * (n + 1) + n + 3 * 8 * N;
+  D.algo[K_ELEM_HESS] = 16 * m + 12 * s * m + m + 8 * N + 90 * s * m;
+  D.algo[K_ASSEMBLE] = 90 * s * m + 40 * m + 4 * (nlo + 1) + 16 * nlo + n + 9 * s * nfull;
+  D.algo[K_JACOBI] = 18 * s * n;
+  D.algo[K_LINSETUP] = 4 * 8 * N;
+  D.algo[K_RESID] = nfull * (9 * s + 4) + 3 * 8 * N + 9 * s * n + 4 * s * N;
+  D.algo[K_PCG_A] = nfull * (9 * s + 4) + 4 * s * N;
+  D.algo[K_PCG_B] = 7 * s * N + 9 * s * n;
+  D.algo[K_ACCUM] = s * N + 2 * 8 * N;
+}
+
 int start_solve(phx_instance inst, const phx_options* o, bool dynamic, double dt, int max_iters_override) {
   TRY(validate_opts(o));
   const bool fp64 = o->precision == PHX_PREC_FP64;
   TRY(ensure_precision(inst, fp64));
   DevOpts d = make_opts(o, dynamic, dt);
   if (max_iters_override > 0) d.num_max_iters = max_iters_override;
+  set_algo_bytes(inst->dev, fp64);
   CU(cudaMemcpyAsync(inst->d_opts, &d, sizeof(DevOpts), cudaMemcpyHostToDevice, inst->ctx->stream));
   TRY(reset_state(inst, PH_START, 0, 0.0));
   return PHX_OK;
@@ -460,6 +485,7 @@ void phx_default_options(phx_options* o) {
   o->max_refine_sweeps = 12;
   o->warm_guess = 1;
   o->pcg_chunk = 32;
+  o->tol_rel = 0.0;
 }
 
 int phx_context_create(int32_t device, int64_t arena_bytes, phx_context* out) {
@@ -499,6 +525,9 @@ int phx_context_destroy(phx_context ctx) {
   if (ctx->d_pre) cudaFree(ctx->d_pre);
   if (ctx->d_flags) cudaFree(ctx->d_flags);
   if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
+  if (ctx->d_algo) cudaFree(ctx->d_algo);
+  for (auto& ev : ctx->marks)
+    if (ev) cudaEventDestroy(ev);
   ctx->arena.release();
   cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -549,6 +578,7 @@ int phx_instance_create(phx_context ctx, const phx_mesh* mesh, phx_instance* out
   InstDev& D = inst->dev;
   D.n = hp.n; D.m = hp.m; D.nlo = hp.nlo; D.nchunks = hp.nchunks; D.nslots = hp.nslots;
   auto fail = [&](int rc) { phx_instance_destroy(inst); return rc; };
+  cudaError_t e0 = cudaSuccess;
   int rc = PHX_OK;
   const size_t n4 = 4 * (size_t)hp.n;
 #define UP(field, vec)                                          \
@@ -576,6 +606,11 @@ int phx_instance_create(phx_context ctx, const phx_mesh* mesh, phx_instance* out
   UP(mass, hp.mass);
   UP(hlin, hp.hlin);
 #undef UP
+  {
+    double* xr = nullptr;
+    if ((rc = arena_alloc(inst, &xr, n4, true))) return fail(rc);
+    D.xrest = xr;
+  }
   double** vecs[] = {&D.x, &D.xs, &D.dx, &D.g, &D.gn, &D.dxprev, &D.x0, &D.v0, &D.v, &D.r64, &D.bvec};
   for (double** pv : vecs)
     if ((rc = arena_alloc(inst, pv, n4, true))) return fail(rc);
@@ -590,6 +625,8 @@ int phx_instance_create(phx_context ctx, const phx_mesh* mesh, phx_instance* out
   D.opts = inst->d_opts;
   // rest positions
   if ((rc = upload_x(inst, mesh->X0, D.x))) return fail(rc);
+  e0 = cudaMemcpyAsync((void*)D.xrest, D.x, n4 * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream);
+  if (e0 != cudaSuccess) return fail(set_err(PHX_ECUDA, cudaGetErrorString(e0)));
   // keep only what later calls need on the host
   hp.rest64.clear(); hp.rest64.shrink_to_fit();
   hp.rest32.clear(); hp.rest32.shrink_to_fit();
@@ -608,6 +645,17 @@ int phx_instance_sizes(phx_instance inst, int64_t* ndof, int64_t* nnz, int64_t* 
   if (nnz) *nnz = 9 * (int64_t)inst->dev.nlo;
   if (nlo) *nlo = inst->dev.nlo;
   if (nfull) *nfull = 2 * (int64_t)inst->dev.nlo - inst->dev.n;
+  return PHX_OK;
+}
+
+int phx_instance_reset(phx_instance inst) {
+  if (!inst) return set_err(PHX_EINVAL, "inst is NULL");
+  if (inst->in_server) return set_err(PHX_EBUSY, "instance is admitted to a server");
+  const size_t bytes = 4 * (size_t)inst->dev.n * sizeof(double);
+  cudaStream_t st = inst->ctx->stream;
+  CU(cudaMemcpyAsync(inst->dev.x, inst->dev.xrest, bytes, cudaMemcpyDeviceToDevice, st));
+  CU(cudaMemsetAsync(inst->dev.v, 0, bytes, st));
+  CU(cudaMemsetAsync(inst->dev.dxprev, 0, bytes, st));
   return PHX_OK;
 }
 
@@ -1006,8 +1054,28 @@ int phx_server_poll(phx_server s, int64_t* tags, phx_report* reps, int32_t cap) 
 // ---- profiling -------------------------------------------------------------
 int phx_profile_enable(phx_context ctx, int32_t on) {
   if (!ctx) return set_err(PHX_EINVAL, "ctx is NULL");
+  if (on && !ctx->d_algo) {
+    CU(cudaMalloc(&ctx->d_algo, sizeof(double) * K_COUNT));
+    CU(cudaMemsetAsync(ctx->d_algo, 0, sizeof(double) * K_COUNT, ctx->stream));
+  }
   ctx->profiling = on != 0;
+  ctx->batch_owner = nullptr;  // batches pick the new setting up on their next round
   return PHX_OK;
+}
+
+int phx_profile_bytes(phx_context ctx, const char* kind, double* bytes) {
+  if (!ctx || !kind || !bytes) return set_err(PHX_EINVAL, "bad arguments");
+  *bytes = 0.0;
+  if (!ctx->d_algo) return PHX_OK;
+  double h[K_COUNT];
+  CU(cudaMemcpyAsync(h, ctx->d_algo, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  for (int k = 0; k < K_COUNT; ++k)
+    if (std::strcmp(kernel_name((KernelId)k), kind) == 0) {
+      *bytes = h[k];
+      return PHX_OK;
+    }
+  return set_err(PHX_ENOTFOUND, std::string("unknown kernel kind ") + kind);
 }
 
 static int collect_events(phx_context ctx) {
@@ -1040,10 +1108,28 @@ int phx_profile_reset(phx_context ctx) {
   if (!ctx) return set_err(PHX_EINVAL, "ctx is NULL");
   TRY(collect_events(ctx));
   for (int k = 0; k < K_COUNT; ++k) { ctx->prof_ms[k] = 0; ctx->prof_n[k] = 0; }
+  if (ctx->d_algo) CU(cudaMemsetAsync(ctx->d_algo, 0, sizeof(double) * K_COUNT, ctx->stream));
   ctx->launches = 0;
   return PHX_OK;
 }
 
 int64_t phx_kernel_launches(phx_context ctx) { return ctx ? ctx->launches : -1; }
+
+int phx_timer_mark(phx_context ctx, int32_t slot) {
+  if (!ctx || slot < 0 || slot >= 16) return set_err(PHX_EINVAL, "bad timer slot");
+  if (!ctx->marks[slot]) CU(cudaEventCreate(&ctx->marks[slot]));
+  CU(cudaEventRecord(ctx->marks[slot], ctx->stream));
+  return PHX_OK;
+}
+
+int phx_timer_elapsed(phx_context ctx, int32_t a, int32_t b, double* ms) {
+  if (!ctx || !ms || a < 0 || a >= 16 || b < 0 || b >= 16 || !ctx->marks[a] || !ctx->marks[b])
+    return set_err(PHX_EINVAL, "bad timer slots");
+  CU(cudaEventSynchronize(ctx->marks[b]));
+  float f = 0;
+  CU(cudaEventElapsedTime(&f, ctx->marks[a], ctx->marks[b]));
+  *ms = f;
+  return PHX_OK;
+}
 
 }  // extern "C"

@@ -69,6 +69,10 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double* sm) {
   }
 }
 
+__device__ __forceinline__ void count_bytes(const BatchDev& B, const InstDev& I, KernelId k) {
+  if (B.algo_total) B.algo_total[k] += I.algo[k];  // single thread of the finalising CTA
+}
+
 // Records this tile's partial sums; in the CTA that completes the instance's
 // last tile, returns true and leaves the instance totals in thread 0's tot[].
 template <int K>
@@ -247,6 +251,7 @@ __global__ void __launch_bounds__(kTile) k_vecop(BatchDev B) {
     }
     double p[1] = {0.0}, tot[1];
     if (tile_done<1>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
+      count_bytes(B, I, K_VECOP);
       st->phase = st->next_phase;
       st->vecop = 0;
     }
@@ -344,7 +349,10 @@ __global__ void __launch_bounds__(kTile) k_elem_eg(BatchDev B) {
       I.Eloc[e] = Ee;
     }
     double p[1] = {Ee}, tot[1];
-    if (tile_done<1>(I, lt, tiles_of(I.m), p, tot, sm, &flag) && threadIdx.x == 0) st->E_el = tot[0];
+    if (tile_done<1>(I, lt, tiles_of(I.m), p, tot, sm, &flag) && threadIdx.x == 0) {
+      count_bytes(B, I, K_ELEM_EG);
+      st->E_el = tot[0];
+    }
   }
 }
 
@@ -396,6 +404,7 @@ __global__ void __launch_bounds__(kTile) k_gather(BatchDev B) {
     }
     double tot[2];
     if (tile_done<2>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
+      count_bytes(B, I, K_GATHER);
       st->E_eval = st->E_el + tot[0];
       st->gg_eval = tot[1];
       st->phase = PH_EVAL_DONE;
@@ -567,6 +576,8 @@ __global__ void __launch_bounds__(288) k_assemble(BatchDev B) {
     }
     double p[1] = {nrm}, tot[1];
     if (tile_done<1>(I, lt, tiles_of(I.nlo), p, tot, sm, &flag) && threadIdx.x == 0) {
+      count_bytes(B, I, K_ELEM_HESS);  // the element kernel ran on this instance in the same round
+      count_bytes(B, I, K_ASSEMBLE);
       st->normA2 = tot[0];
       st->regT = 1e-6 * sqrt(tot[0]);
     }
@@ -617,7 +628,10 @@ __global__ void __launch_bounds__(kTile) k_jacobi(BatchDev B) {
       for (int k = 0; k < 9; ++k) Mi[(size_t)k * I.n + v] = (Real)inv[k];
     }
     double p[1] = {0.0}, tot[1];
-    if (tile_done<1>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) st->phase = PH_LINSETUP;
+    if (tile_done<1>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
+      count_bytes(B, I, K_JACOBI);
+      st->phase = PH_LINSETUP;
+    }
   }
 }
 
@@ -645,6 +659,7 @@ __global__ void __launch_bounds__(kTile) k_linsetup(BatchDev B) {
     }
     double tot[1];
     if (tile_done<1>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
+      count_bytes(B, I, K_LINSETUP);
       const double tol = I.opts->ls_tol_max_error;
       st->bb = tot[0];
       st->thr_final = fmax(tol * tol * tot[0], DBL_MIN);
@@ -729,6 +744,7 @@ __global__ void __launch_bounds__(kTile) k_resid(BatchDev B) {
     }
     double tot[5];
     if (tile_done<5>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
+      count_bytes(B, I, K_RESID);
       st->rr64 = tot[0];
       st->b_dot_dx = tot[1];
       st->dx_norm = sqrt(tot[2]);
@@ -795,6 +811,7 @@ __global__ void __launch_bounds__(kTile) k_pcg_a(BatchDev B) {
     }
     double tot[1];
     if (tile_done<1>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
+      count_bytes(B, I, K_PCG_A);
       st->pq = tot[0];
       if (!(tot[0] > 0.0)) {  // not positive definite along p (or non-finite)
         st->lin_status = LIN_BREAKDOWN;
@@ -844,6 +861,7 @@ __global__ void __launch_bounds__(kTile) k_pcg_b(BatchDev B) {
     }
     double tot[2];
     if (tile_done<2>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
+      count_bytes(B, I, K_PCG_B);
       st->pcg_iter++;
       st->pcg_total++;
       st->rr = tot[0];
@@ -885,6 +903,7 @@ __global__ void __launch_bounds__(kTile) k_accum(BatchDev B) {
     }
     double p[1] = {0.0}, tot[1];
     if (tile_done<1>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
+      count_bytes(B, I, K_ACCUM);
       st->sweeps++;
       st->total_sweeps++;
       st->phase = PH_RESID;

@@ -22,6 +22,7 @@ enum KernelId : int {
   K_ACCUM,
   K_COUNT
 };
+static_assert(K_COUNT <= 12, "InstDev::algo holds 12 kernel kinds");
 
 cudaError_t setup_kernel_attributes();
 void launch(KernelId id, int grid, cudaStream_t s, const BatchDev& B, bool fp64);

@@ -39,7 +39,7 @@ PHX_HD inline int32_t ctl_post_step(NState& s, const DevOpts& o) {
     else if (o.try_steepest) s.steepest = !s.steepest;
   }
   if (!brk && s.result == OS_SUCCESS) {
-    if (s.opt <= o.tol_max_error) brk = true;
+    if (s.opt <= s.tol_eff) brk = true;
     else s.result = OS_ONGOING;
   }
   if (!brk && s.result == OS_ONGOING) s.steepest = 0;
@@ -67,9 +67,12 @@ PHX_HD inline void ctl_goto(NState& s, int32_t next) {
 // Start of SolveStepInternal (energy, gradient and ||g|| at x are known).
 PHX_HD inline void ctl_iter_begin(NState& s, const DevOpts& o) {
   s.it++;
-  if (s.opt0 < 0) s.opt0 = s.opt;
+  if (s.opt0 < 0) {
+    s.opt0 = s.opt;
+    s.tol_eff = (o.tol_rel > 0.0 && o.tol_rel * s.opt0 > o.tol_max_error) ? o.tol_rel * s.opt0 : o.tol_max_error;
+  }
   s.num_bis = 0;
-  if (s.opt < o.tol_max_error) {
+  if (s.opt < s.tol_eff) {
     s.result = OS_SUCCESS;
     s.step_result = OS_SUCCESS;
     ctl_goto(s, ctl_post_step(s, o));
@@ -88,6 +91,7 @@ PHX_HD inline void ctl_iter_begin(NState& s, const DevOpts& o) {
   } else {
     s.reg_trial = 0;
     s.shift = 0.0;
+    s.hess_count++;
     s.phase = PH_HESS;
   }
 }
@@ -124,7 +128,7 @@ PHX_HD inline void ctl_ls_check(NState& s, const DevOpts& o) {
     } else if (step < o.tol_min_step) {
       s.min_step_count++;
       s.result = OS_MINSTEP;
-    } else if (optNew <= o.tol_max_error) {
+    } else if (optNew <= s.tol_eff) {
       s.result = OS_SUCCESS;
       s.min_impr_count = 0;
       s.min_step_count = 0;
@@ -173,7 +177,9 @@ PHX_HD inline void ctl_advance(NState& s, const DevOpts& o) {
         s.total_reg = 0;
         s.total_sweeps = 0;
         s.pcg_total = 0;
+        s.hess_count = 0;
         s.opt0 = -1.0;
+        s.tol_eff = o.tol_max_error;
         s.purpose = 0;
         s.vecop = o.dynamic ? VO_PRED : 0;
         ctl_goto(s, PH_EVAL);

@@ -67,7 +67,7 @@ struct DevOpts {
   int32_t ls_num_max_iters, ls_num_reg_trials, lsearch_num_try, precision, precond;
   int32_t max_refine_sweeps, warm_guess, dynamic, pad0;
   double tol_max_error, tol_min_step, tol_min_impr, max_step_size, ls_tol_max_error;
-  double lsearch_alpha, inner_tol, dt;
+  double lsearch_alpha, inner_tol, dt, tol_rel;
 };
 
 // Scalar state of one instance's solve (one thread of the control kernel owns it).
@@ -77,7 +77,7 @@ struct NState {
   int32_t min_step_count, num_bis, total_bis, reg_trial;
   int32_t total_reg, sweeps, total_sweeps, lin_status;
   int32_t pcg_iter, pcg_parity, error, first_step;
-  int32_t step_result, nofix, pad2, pad3;
+  int32_t step_result, nofix, hess_count, pad3;
   int64_t pcg_total;
   double obj, opt, opt0, obj_new;
   double alpha_trial, factor, scale, dx_norm;
@@ -85,6 +85,7 @@ struct NState {
   double normA2, shift, regT, bb;
   double rr64, rz, rr, pq;
   double alpha, beta, thr_inner, thr_final;
+  double tol_eff;                              // max(tol_max_error, tol_rel * opt0)
 };
 
 // Device descriptor of one instance (pointers into the arena).
@@ -111,6 +112,7 @@ struct InstDev {
   const double* mass;         // [n] lumped mass per node
   double* hlin;               // [n][4] f - m g : linear-load term of energy and gradient
   // FP64 node vectors [n][4]
+  const double* xrest;
   double* x; double* xs; double* dx; double* g; double* gn; double* dxprev;
   double* x0; double* v0; double* v; double* r64; double* bvec;
   // element scratch
@@ -129,6 +131,7 @@ struct InstDev {
   uint32_t* counter;          // [1]
   NState* st;
   const DevOpts* opts;
+  double algo[12];            // algorithmic bytes of one launch of each kernel kind on this instance
 };
 
 // Tile prefix arrays of the active batch (device memory).
@@ -138,7 +141,8 @@ struct BatchDev {
   const int32_t* pre_node;
   const int32_t* pre_lob;
   InstDev* inst;              // [num]
-  int32_t* flags;             // [8] device flags: [0] active count, [1] pcg running count, [2] error
+  int32_t* flags;             // [8 + num]: [0] active count; [8 + i] phase of instance i
+  double* algo_total;         // [12] algorithmic bytes summed per kernel kind, or null
 };
 
 PHX_HD inline int64_t sell_addr(int64_t s, int e) { return (s >> 5) * 288 + (int64_t)e * 32 + (s & 31); }

@@ -20,11 +20,11 @@ class NState(C.Structure):
     _fields_ = [(n, C.c_int32) for n in (
         "phase", "next_phase", "vecop", "purpose", "result", "it", "steepest", "min_impr_count",
         "min_step_count", "num_bis", "total_bis", "reg_trial", "total_reg", "sweeps", "total_sweeps",
-        "lin_status", "pcg_iter", "pcg_parity", "error", "first_step", "step_result", "nofix", "pad2", "pad3")] + \
+        "lin_status", "pcg_iter", "pcg_parity", "error", "first_step", "step_result", "nofix", "hess_count", "pad3")] + \
         [("pcg_total", C.c_int64)] + [(n, C.c_double) for n in (
             "obj", "opt", "opt0", "obj_new", "alpha_trial", "factor", "scale", "dx_norm", "b_dot_dx", "E_el",
             "E_eval", "gg_eval", "normA2", "shift", "regT", "bb", "rr64", "rz", "rr", "pq", "alpha", "beta",
-            "thr_inner", "thr_final")]
+            "thr_inner", "thr_final", "tol_eff")]
 
 
 class DevOpts(C.Structure):
@@ -33,7 +33,7 @@ class DevOpts(C.Structure):
         "ls_num_max_iters", "ls_num_reg_trials", "lsearch_num_try", "precision", "precond",
         "max_refine_sweeps", "warm_guess", "dynamic", "pad0")] + [(n, C.c_double) for n in (
             "tol_max_error", "tol_min_step", "tol_min_impr", "max_step_size", "ls_tol_max_error",
-            "lsearch_alpha", "inner_tol", "dt")]
+            "lsearch_alpha", "inner_tol", "dt", "tol_rel")]
 
 
 def make_opts(**kw):
@@ -41,7 +41,7 @@ def make_opts(**kw):
                 ls_num_max_iters=1000, ls_num_reg_trials=10, lsearch_num_try=32, precision=0, precond=1,
                 max_refine_sweeps=1, warm_guess=1, dynamic=0, tol_max_error=1e-6, tol_min_step=1e-5,
                 tol_min_impr=1e-9, max_step_size=1000.0, ls_tol_max_error=1e-9, lsearch_alpha=0.5,
-                inner_tol=1e-3, dt=0.0)
+                inner_tol=1e-3, dt=0.0, tol_rel=0.0)
     for k, v in kw.items():
         setattr(o, k, v)
     return o

@@ -128,7 +128,7 @@ def test_batch_equals_alone_bitwise(gpu_ctx):
         x, r = inst.solve_static(o, m.X0.ravel())
         alone.append((x, r))
     insts = [px.Instance(gpu_ctx, m) for m in meshes]
-    reps, xs = gpu_ctx.batch_solve(insts, o, [m.X0.ravel() for m in meshes])
+    reps, xs = gpu_ctx.batch_solve(insts, o, [m.X0.ravel().copy() for m in meshes])
     for (xa, ra), xb, rb in zip(alone, xs, reps):
         assert np.array_equal(xa, xb)
         assert ra["iterations"] == rb["iterations"] and ra["pcg_iterations"] == rb["pcg_iterations"]
@@ -144,7 +144,7 @@ def test_batch_against_oracle(gpu_ctx):
         tols.append(np.linalg.norm(orc.gradient(orc.rest())))
     o = px.options(precision=px.PREC_FP32_REFINE, tol_max_error=1e-6 * min(tols), tol_min_impr=0.0,
                    tol_min_step=0.0)
-    reps, xs = gpu_ctx.batch_solve(insts, o, [m.X0.ravel() for m in meshes])
+    reps, xs = gpu_ctx.batch_solve(insts, o, [m.X0.ravel().copy() for m in meshes])
     for m, x, r in zip(meshes, xs, reps):
         orc, x0, g0, xr, _ = oracle_solution(m, 1e-10)
         assert r["result_name"] == "SUCCESS"
