@@ -171,6 +171,10 @@ int phx_solve_step(phx_instance inst, const phx_options* opts, double* x_inout, 
 /* One implicit-Euler step: minimises the incremental potential (OptimProblem_BasicDynamic). */
 int phx_dynamic_step(phx_instance inst, const phx_options* opts, double dt, double* x_inout,
                      double* v_inout, phx_report* rep);
+/* Per-iteration trace of the instance's last solve (OptimSolver::LineSearch logging,
+ * OptimSolver.cpp:385-395): objective, ||g||, bisections and step length per Newton
+ * iteration, up to cap entries (at most 256 are kept).  Returns the iteration count (>= 0). */
+int phx_solve_log(phx_instance inst, double* obj, double* opt, int32_t* bisections, double* step, int32_t cap);
 /* Many independent static solves in one device batch (persistent kernels over a
  * packed instance index).  x_inout[i] may be NULL; reps has count entries. */
 int phx_batch_solve(phx_context ctx, int32_t count, phx_instance* insts, const phx_options* opts,

@@ -30,7 +30,7 @@ EXPORTS = [
     "phx_context_memory", "phx_instance_create", "phx_instance_destroy", "phx_instance_sizes",
     "phx_instance_reset", "phx_instance_set_positions", "phx_instance_get_positions", "phx_instance_set_velocities",
     "phx_instance_get_velocities", "phx_instance_update_load", "phx_energy_gradient", "phx_hessian",
-    "phx_hessian_pattern", "phx_scatter_map", "phx_element_local", "phx_solve_static", "phx_solve_step",
+    "phx_hessian_pattern", "phx_scatter_map", "phx_element_local", "phx_solve_static", "phx_solve_step", "phx_solve_log",
     "phx_dynamic_step", "phx_batch_solve", "phx_batch_dynamic_step", "phx_server_create", "phx_server_destroy",
     "phx_server_submit", "phx_server_progress", "phx_server_poll", "phx_profile_enable", "phx_profile_read",
     "phx_profile_reset", "phx_profile_bytes", "phx_kernel_launches", "phx_timer_mark", "phx_timer_elapsed",
@@ -108,6 +108,7 @@ def lib():
         "phx_element_local": ([vp, vp, i32, vp, vp, vp], C.c_int),
         "phx_solve_static": ([vp, C.POINTER(Options), vp, C.POINTER(Report)], C.c_int),
         "phx_solve_step": ([vp, C.POINTER(Options), vp, C.POINTER(Report)], C.c_int),
+        "phx_solve_log": ([vp, vp, vp, vp, vp, i32], C.c_int),
         "phx_dynamic_step": ([vp, C.POINTER(Options), dbl, vp, vp, C.POINTER(Report)], C.c_int),
         "phx_batch_solve": ([vp, i32, vp, C.POINTER(Options), vp, vp], C.c_int),
         "phx_batch_dynamic_step": ([vp, i32, vp, C.POINTER(Options), dbl, vp], C.c_int),
@@ -333,6 +334,16 @@ class Instance:
         r = Report()
         _check(lib().phx_solve_step(self.h, C.byref(opts), _p(xx), C.byref(r)))
         return (self.positions() if xx is None else xx), r.as_dict()
+
+    def solve_log(self):
+        """Per-iteration trace of the last solve: obj, opt, bisections, step."""
+        n = lib().phx_solve_log(self.h, None, None, None, None, 0)
+        if n < 0:
+            _check(n)
+        k = min(n, 256)
+        obj = np.zeros(k); opt = np.zeros(k); bis = np.zeros(k, dtype=np.int32); step = np.zeros(k)
+        lib().phx_solve_log(self.h, _p(obj), _p(opt), _p(bis), _p(step), k)
+        return {"obj": obj, "opt": opt, "bis": bis, "step": step, "iterations": n}
 
     def dynamic_step(self, opts: Options, dt: float, x=None, v=None):
         xx = None if x is None else np.ascontiguousarray(x, dtype=np.float64).copy()

@@ -47,6 +47,8 @@ using clk = std::chrono::steady_clock;
 
 // wall-clock limit of one blocking solve call (the device never waits; this bounds the host loop)
 constexpr double kSolveTimeLimit = 600.0;
+// Newton rounds per engine launch in a blocking solve (the host checks completion between launches)
+constexpr int kRoundsPerLaunch = 16;
 
 // ---------------------------------------------------------------------------
 // device arena: one allocation, first-fit free list with coalescing, 256 B alignment
@@ -134,6 +136,12 @@ struct phx_context_s {
   const void* batch_owner = nullptr;  // who set the batch buffers last
   double* d_algo = nullptr;           // [K_COUNT] algorithmic bytes per kernel kind (profiling)
   cudaEvent_t marks[16] = {};
+  // engine
+  GridBar* d_bar = nullptr;
+  int32_t* d_act = nullptr;
+  int act_cap = 0;
+  unsigned long long* d_stage = nullptr;  // [32] stage ns + executions (profiling)
+  int egrid[2] = {0, 0};
 };
 
 struct phx_instance_s {
@@ -403,6 +411,39 @@ void fill_report(const NState& s, bool step, double seconds, phx_report* r) {
   r->reserved = 0;
 }
 
+int ensure_engine(phx_context ctx) {
+  if (!ctx->d_bar) CU(cudaMalloc(&ctx->d_bar, sizeof(GridBar)));
+  if (ctx->act_cap < ctx->cap) {
+    if (ctx->d_act) cudaFree(ctx->d_act);
+    ctx->d_act = nullptr;
+    CU(cudaMalloc(&ctx->d_act, sizeof(int32_t) * (1 + ctx->cap + 3 * (ctx->cap + 1))));
+    ctx->act_cap = ctx->cap;
+  }
+  if (ctx->profiling && !ctx->d_stage) {
+    CU(cudaMalloc(&ctx->d_stage, sizeof(unsigned long long) * 32));
+    CU(cudaMemsetAsync(ctx->d_stage, 0, sizeof(unsigned long long) * 32, ctx->stream));
+  }
+  return PHX_OK;
+}
+
+// One cooperative launch of the engine: up to `rounds` Newton rounds over the batch.
+int run_engine(phx_context ctx, const BatchDev& B, int num, bool fp64, int rounds, int pcg_chunk) {
+  TRY(ensure_engine(ctx));
+  int& grid = ctx->egrid[fp64 ? 1 : 0];
+  if (grid == 0) grid = engine_grid(fp64, ctx->num_sms);
+  if (grid <= 0) return set_err(PHX_ECUDA, "engine kernel cannot be made resident");
+  CU(cudaMemsetAsync(ctx->d_bar, 0, sizeof(GridBar), ctx->stream));
+  EngineArgs A{ctx->d_bar, ctx->d_act, ctx->profiling ? ctx->d_stage : nullptr, ctx->cap, rounds, pcg_chunk};
+  CU(launch_engine(fp64, grid, ctx->stream, B, A));
+  ctx->launches++;
+  GridBar hb;
+  CU(cudaMemcpyAsync(&hb, ctx->d_bar, sizeof(GridBar), cudaMemcpyDeviceToHost, ctx->stream));
+  TRY(read_flags(ctx, num));
+  if (hb.err)
+    return set_err(PHX_ETIMEOUT, "engine grid barrier timed out (stage " + std::to_string(hb.stage) + ")");
+  return PHX_OK;
+}
+
 // Runs a set of instances (states already reset to PH_START) until all are done.
 int run_to_completion(phx_context ctx, const std::vector<phx_instance>& list, bool fp64, int pcg_chunk) {
   BatchDev B{};
@@ -411,9 +452,7 @@ int run_to_completion(phx_context ctx, const std::vector<phx_instance>& list, bo
   const int num = (int)list.size();
   const auto t0 = clk::now();
   for (int64_t r = 0;; ++r) {
-    run_round(ctx, B, G, fp64, pcg_chunk);
-    CU(cudaGetLastError());
-    TRY(read_flags(ctx, num));
+    TRY(run_engine(ctx, B, num, fp64, kRoundsPerLaunch, pcg_chunk));
     if (ctx->h_flags[0] == 0) return PHX_OK;
     if (std::chrono::duration<double>(clk::now() - t0).count() > kSolveTimeLimit)
       return set_err(PHX_ETIMEOUT, "solver did not finish within " + std::to_string(kSolveTimeLimit) + " s");
@@ -526,6 +565,9 @@ int phx_context_destroy(phx_context ctx) {
   if (ctx->d_flags) cudaFree(ctx->d_flags);
   if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
   if (ctx->d_algo) cudaFree(ctx->d_algo);
+  if (ctx->d_bar) cudaFree(ctx->d_bar);
+  if (ctx->d_act) cudaFree(ctx->d_act);
+  if (ctx->d_stage) cudaFree(ctx->d_stage);
   for (auto& ev : ctx->marks)
     if (ev) cudaEventDestroy(ev);
   ctx->arena.release();
@@ -619,6 +661,7 @@ int phx_instance_create(phx_context ctx, const phx_mesh* mesh, phx_instance* out
   size_t maxt = std::max({tiles(hp.m), tiles(hp.n), tiles(hp.nlo)});
   if ((rc = arena_alloc(inst, &D.partials, maxt * kPartials))) return fail(rc);
   if ((rc = arena_alloc(inst, &D.counter, 1, true))) return fail(rc);
+  if ((rc = arena_alloc(inst, &D.log, 4 * (size_t)kLogCap, true))) return fail(rc);
   if ((rc = arena_alloc(inst, &inst->d_st, 1, true))) return fail(rc);
   if ((rc = arena_alloc(inst, &inst->d_opts, 1, true))) return fail(rc);
   D.st = inst->d_st;
@@ -691,6 +734,22 @@ int phx_instance_update_load(phx_instance inst, const double* force, const doubl
                      inst->ctx->stream));
   CU(cudaStreamSynchronize(inst->ctx->stream));
   return PHX_OK;
+}
+
+int phx_solve_log(phx_instance inst, double* obj, double* opt, int32_t* bis, double* step, int32_t cap) {
+  if (!inst) return set_err(PHX_EINVAL, "inst is NULL");
+  NState s;
+  TRY(read_state(inst, &s));
+  std::vector<double> lg(4 * (size_t)kLogCap);
+  CU(cudaMemcpy(lg.data(), inst->dev.log, lg.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  int n = std::min(std::min(s.log_count, kLogCap), std::max(cap, 0));
+  for (int i = 0; i < n; ++i) {
+    if (obj) obj[i] = lg[4 * i];
+    if (opt) opt[i] = lg[4 * i + 1];
+    if (bis) bis[i] = (int32_t)lg[4 * i + 2];
+    if (step) step[i] = lg[4 * i + 3];
+  }
+  return s.log_count;
 }
 
 int phx_hessian_pattern(phx_instance inst, int32_t* colptr, int32_t* rowidx) {
@@ -1030,9 +1089,7 @@ int phx_server_progress(phx_server s, int32_t* active, int32_t* queued) {
       s->ctx->batch_owner = s;
       s->dirty = false;
     }
-    run_round(s->ctx, s->B, s->G, s->fp64, s->opts.pcg_chunk);
-    CU(cudaGetLastError());
-    TRY(read_flags(s->ctx, (int)s->active.size()));
+    TRY(run_engine(s->ctx, s->B, (int)s->active.size(), s->fp64, 2, s->opts.pcg_chunk));
   }
   if (active) *active = (int32_t)s->active.size();
   if (queued) *queued = (int32_t)s->queue.size();
@@ -1080,6 +1137,15 @@ int phx_profile_bytes(phx_context ctx, const char* kind, double* bytes) {
 
 static int collect_events(phx_context ctx) {
   CU(cudaStreamSynchronize(ctx->stream));
+  if (ctx->d_stage) {
+    unsigned long long h[32];
+    CU(cudaMemcpy(h, ctx->d_stage, sizeof(h), cudaMemcpyDeviceToHost));
+    for (int k = 0; k < K_COUNT; ++k) {
+      ctx->prof_ms[k] += h[k] * 1e-6;
+      ctx->prof_n[k] += (int64_t)h[16 + k];
+    }
+    CU(cudaMemset(ctx->d_stage, 0, sizeof(h)));
+  }
   for (auto& ev : ctx->evs) {
     float ms = 0;
     CU(cudaEventElapsedTime(&ms, ev.a, ev.b));

@@ -36,15 +36,6 @@ namespace phx {
 // ---------------------------------------------------------------------------
 // small helpers
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ int find_tile(const int32_t* pre, int num, int t) {
-  int lo = 0, hi = num;
-  while (hi - lo > 1) {
-    int mid = (lo + hi) >> 1;
-    if (__ldg(pre + mid) <= t) lo = mid; else hi = mid;
-  }
-  return lo;
-}
-
 __device__ __forceinline__ int tiles_of(int count) { return (count + kTile - 1) / kTile; }
 
 template <int K>
@@ -151,6 +142,9 @@ template <> struct PcgBufs<double> {
 template <typename T> __device__ __forceinline__ T dlog(T x);
 template <> __device__ __forceinline__ float dlog<float>(float x) { return logf(x); }
 template <> __device__ __forceinline__ double dlog<double>(double x) { return log(x); }
+template <typename T> __device__ __forceinline__ T dlog1p(T x);
+template <> __device__ __forceinline__ float dlog1p<float>(float x) { return log1pf(x); }
+template <> __device__ __forceinline__ double dlog1p<double>(double x) { return log1p(x); }
 
 template <typename T>
 __device__ __forceinline__ T det3(const T* F) {
@@ -172,30 +166,97 @@ __device__ __forceinline__ void cof3(const T* F, T* C) {
   C[8] = F[0] * F[4] - F[3] * F[1];
 }
 
-// Loads a tet: node ids, rest data, and Ds = [x1-x0, x2-x0, x3-x0] in FP64.
-__device__ __forceinline__ void load_ds(const InstDev& I, int e, int (&nd)[4], double (&Ds)[9]) {
+// Loads a tet's displacement differences Du = [u1-u0, u2-u0, u3-u0], u = x - X0, in FP64.
+// F - I = Du Dm^-1 then carries no cancellation against the rest shape, so small strains
+// keep their digits in the strain measures below.
+__device__ __forceinline__ void load_du(const InstDev& I, int e, int (&nd)[4], double (&Du)[9]) {
   int4 t = reinterpret_cast<const int4*>(I.tets)[e];
   nd[0] = t.x; nd[1] = t.y; nd[2] = t.z; nd[3] = t.w;
-  double x0[3], xa[3];
-  ld4(I.x, nd[0], x0);
+  double u0[3], ua[3], X[3];
+  ld4(I.x, nd[0], u0);
+  ld4(I.xrest, nd[0], X);
+  for (int r = 0; r < 3; ++r) u0[r] -= X[r];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    ld4(I.x, nd[c + 1], xa);
+    ld4(I.x, nd[c + 1], ua);
+    ld4(I.xrest, nd[c + 1], X);
 #pragma unroll
-    for (int r = 0; r < 3; ++r) Ds[r + 3 * c] = xa[r] - x0[r];
+    for (int r = 0; r < 3; ++r) Du[r + 3 * c] = (ua[r] - X[r]) - u0[r];
   }
+}
+
+// y - log(1 + y) without cancellation for small y (series up to y^9 when |y| < 1e-3)
+__device__ __forceinline__ double y_minus_log1p(double y) {
+  if (fabs(y) < 1e-3) {
+    double t = y * y, s = 0.0, p = y;
+    // y^2/2 - y^3/3 + y^4/4 - ... = sum_{k>=2} (-1)^k y^k / k
+    p = t;
+    s = p / 2.0;
+#pragma unroll
+    for (int k = 3; k <= 9; ++k) {
+      p *= -y;
+      s += p / (double)k;
+    }
+    return s;
+  }
+  return y - log1p(y);
+}
+
+// ---------------------------------------------------------------------------
+// tile maps: a list of instances (all of a batch, or the compacted active ones)
+// and the prefix of their tile counts.  Loaded through L2 (ld.cg) because the
+// engine rewrites them between rounds inside one launch.
+// ---------------------------------------------------------------------------
+struct TileMap {
+  const int32_t* pre;  // [num + 1]
+  const int32_t* ids;  // [num] list entry -> instance, or null for the identity
+  int num;
+};
+
+__device__ __forceinline__ int map_total(const TileMap& M) { return __ldcg(M.pre + M.num); }
+
+__device__ __forceinline__ void map_tile(const TileMap& M, int t, int& inst, int& lt) {
+  int lo = 0, hi = M.num;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (__ldcg(M.pre + mid) <= t) lo = mid; else hi = mid;
+  }
+  inst = M.ids ? __ldcg(M.ids + lo) : lo;
+  lt = t - __ldcg(M.pre + lo);
+}
+
+__device__ __forceinline__ TileMap full_map(const BatchDev& B, const int32_t* pre) {
+  return TileMap{pre, nullptr, *B.num};
+}
+
+// Runs the state machine of instance i up to its next device phase (called by the one
+// thread that finalises a stage for the instance) and publishes the phase.
+__device__ void advance(const BatchDev& B, int i) {
+  const InstDev& I = B.inst[i];
+  NState s = *I.st;
+  ctl_advance(s, *I.opts);
+  if (s.log_pending) {
+    if (I.log && s.log_count < kLogCap) {
+      I.log[4 * s.log_count + 0] = s.obj;
+      I.log[4 * s.log_count + 1] = s.opt;
+      I.log[4 * s.log_count + 2] = (double)s.num_bis;
+      I.log[4 * s.log_count + 3] = s.log_step;
+    }
+    s.log_count++;
+    s.log_pending = 0;
+  }
+  *I.st = s;
+  B.flags[8 + i] = s.phase;
 }
 
 // ---------------------------------------------------------------------------
 // vector ops of the state machine
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kTile) k_vecop(BatchDev B) {
-  __shared__ double sm[32 * 1];
-  __shared__ int flag;
-  const int num = *B.num;
-  const int total = B.pre_node[num];
-  for (int t = blockIdx.x; t < total; t += gridDim.x) {
-    const int i = find_tile(B.pre_node, num, t), lt = t - B.pre_node[i];
+__device__ __forceinline__ void st_vecop(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag) {
+  const int total = map_total(M);
+  for (int t = cta; t < total; t += ncta) {
+    int i, lt;
+    map_tile(M, t, i, lt);
     const InstDev& I = B.inst[i];
     NState* st = I.st;
     if (st->phase != PH_VEC) continue;
@@ -254,24 +315,45 @@ __global__ void __launch_bounds__(kTile) k_vecop(BatchDev B) {
       count_bytes(B, I, K_VECOP);
       st->phase = st->next_phase;
       st->vecop = 0;
+      advance(B, i);
     }
   }
+}
+
+__global__ void __launch_bounds__(kTile) k_vecop(BatchDev B) {
+  __shared__ double sm[32 * 5];
+  __shared__ int flag;
+  st_vecop(B, full_map(B, B.pre_node), blockIdx.x, gridDim.x, sm, flag);
 }
 
 // ---------------------------------------------------------------------------
 // element energy + gradient (FP64)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void material_eg(int model, double lam, double mu, const double* F, double* psi,
-                                            double* P) {
+// Energy density and PK1 from the displacement gradient H = F - I (column-major).
+// CoNH:  psi = mu/2 (|H|^2 - 2 q + 2 f(j)) + lam/2 log(J)^2, with J - 1 = j = tr H + q,
+//        q = I2(H) + det H and f(j) = j - log(1 + j): the same function as
+//        mu/2 (tr F^T F - 3 - log J^2) + lam/8 (log J^2)^2 written without cancellation;
+//        P = mu F + (lam/2 log J^2 - mu) F^-T.
+// StVK:  E = (H + H^T + H^T H)/2, psi = lam/2 tr(E)^2 + mu E:E, P = F (lam tr(E) I + 2 mu E).
+__device__ __forceinline__ void material_eg(int model, double lam, double mu, const double* H, double* psi,
+                                            double* P, bool* inverted) {
+  double F[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) F[k] = H[k];
+  F[0] += 1.0; F[4] += 1.0; F[8] += 1.0;
+  const double trH = H[0] + H[4] + H[8];
+  const double I2 = H[0] * H[4] - H[3] * H[1] + H[0] * H[8] - H[6] * H[2] + H[4] * H[8] - H[7] * H[5];
+  const double q = I2 + det3(H);
+  const double j = trH + q;  // J - 1
+  *inverted = j < -1.0;
   if (model == 1) {
-    // Saint-Venant Kirchhoff: E = (F^T F - I)/2, S = lam tr(E) I + 2 mu E, P = F S
     double E[9];
 #pragma unroll
-    for (int j = 0; j < 3; ++j)
+    for (int jj = 0; jj < 3; ++jj)
 #pragma unroll
       for (int i = 0; i < 3; ++i)
-        E[i + 3 * j] = 0.5 * (F[0 + 3 * i] * F[0 + 3 * j] + F[1 + 3 * i] * F[1 + 3 * j] + F[2 + 3 * i] * F[2 + 3 * j]);
-    E[0] -= 0.5; E[4] -= 0.5; E[8] -= 0.5;
+        E[i + 3 * jj] = 0.5 * (H[i + 3 * jj] + H[jj + 3 * i] + H[3 * i] * H[3 * jj] + H[1 + 3 * i] * H[1 + 3 * jj] +
+                                H[2 + 3 * i] * H[2 + 3 * jj]);
     double trE = E[0] + E[4] + E[8];
     double ee = 0;
 #pragma unroll
@@ -282,17 +364,17 @@ __device__ __forceinline__ void material_eg(int model, double lam, double mu, co
     for (int k = 0; k < 9; ++k) S[k] = 2.0 * mu * E[k];
     S[0] += lam * trE; S[4] += lam * trE; S[8] += lam * trE;
 #pragma unroll
-    for (int j = 0; j < 3; ++j)
+    for (int jj = 0; jj < 3; ++jj)
 #pragma unroll
-      for (int i = 0; i < 3; ++i) P[i + 3 * j] = F[i] * S[3 * j] + F[i + 3] * S[1 + 3 * j] + F[i + 6] * S[2 + 3 * j];
+      for (int i = 0; i < 3; ++i) P[i + 3 * jj] = F[i] * S[3 * jj] + F[i + 3] * S[1 + 3 * jj] + F[i + 6] * S[2 + 3 * jj];
   } else {
-    // compressible Neo-Hookean: psi = mu/2 (I1 - 3 - log J^2) + lam/8 (log J^2)^2
-    double J = det3(F);
-    double logJ2 = log(J * J);
-    double I1 = 0;
+    double hh = 0;
 #pragma unroll
-    for (int k = 0; k < 9; ++k) I1 += F[k] * F[k];
-    *psi = mu * (I1 - 3.0 - logJ2) / 2.0 + lam * logJ2 * logJ2 / 8.0;
+    for (int k = 0; k < 9; ++k) hh += H[k] * H[k];
+    const double J = 1.0 + j;
+    const double logJ2 = (j > -1.0) ? 2.0 * log1p(j) : log(J * J);
+    const double lJ = 0.5 * logJ2;
+    *psi = 0.5 * mu * (hh - 2.0 * q + 2.0 * ((j > -1.0) ? y_minus_log1p(j) : j - lJ)) + 0.5 * lam * lJ * lJ;
     double C[9];
     cof3(F, C);
     double c = (0.5 * lam * logJ2 - mu) / J;
@@ -301,13 +383,11 @@ __device__ __forceinline__ void material_eg(int model, double lam, double mu, co
   }
 }
 
-__global__ void __launch_bounds__(kTile) k_elem_eg(BatchDev B) {
-  __shared__ double sm[32];
-  __shared__ int flag;
-  const int num = *B.num;
-  const int total = B.pre_tet[num];
-  for (int t = blockIdx.x; t < total; t += gridDim.x) {
-    const int i = find_tile(B.pre_tet, num, t), lt = t - B.pre_tet[i];
+__device__ __forceinline__ void st_elem_eg(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag) {
+  const int total = map_total(M);
+  for (int t = cta; t < total; t += ncta) {
+    int i, lt;
+    map_tile(M, t, i, lt);
     const InstDev& I = B.inst[i];
     NState* st = I.st;
     if (st->phase != PH_EVAL) continue;
@@ -315,22 +395,23 @@ __global__ void __launch_bounds__(kTile) k_elem_eg(BatchDev B) {
     double Ee = 0.0;
     if (e < I.m) {
       int nd[4];
-      double Ds[9];
-      load_ds(I, e, nd, Ds);
+      double Du[9];
+      load_du(I, e, nd, Du);
       double R[12];
       const double2* r2 = reinterpret_cast<const double2*>(I.rest64 + 12 * (size_t)e);
 #pragma unroll
       for (int k = 0; k < 6; ++k) { double2 q = r2[k]; R[2 * k] = q.x; R[2 * k + 1] = q.y; }
-      double F[9];
+      double Hd[9];
 #pragma unroll
       for (int c = 0; c < 3; ++c)
 #pragma unroll
         for (int r = 0; r < 3; ++r)
-          F[r + 3 * c] = Ds[r] * R[0 + 3 * c] + Ds[r + 3] * R[1 + 3 * c] + Ds[r + 6] * R[2 + 3 * c];
+          Hd[r + 3 * c] = Du[r] * R[0 + 3 * c] + Du[r + 3] * R[1 + 3 * c] + Du[r + 6] * R[2 + 3 * c];
       const double w = R[9], lam = R[10], mu = R[11];
       double psi, P[9];
-      material_eg(I.model[e], lam, mu, F, &psi, P);
-      Ee = (det3(Ds) / 6.0 < 0.0) ? __longlong_as_double(0x7ff0000000000000LL) : psi * w;
+      bool inverted;
+      material_eg(I.model[e], lam, mu, Hd, &psi, P, &inverted);
+      Ee = inverted ? __longlong_as_double(0x7ff0000000000000LL) : psi * w;
       // g_a = w * P * B_a, B_a = row (a-1) of Dm^-1, B_0 = -(B_1 + B_2 + B_3)
       double g[12];
 #pragma unroll
@@ -356,14 +437,18 @@ __global__ void __launch_bounds__(kTile) k_elem_eg(BatchDev B) {
   }
 }
 
-// node gather of element gradients + linear loads (+ inertia), energy and ||g||^2
-__global__ void __launch_bounds__(kTile) k_gather(BatchDev B) {
-  __shared__ double sm[32 * 2];
+__global__ void __launch_bounds__(kTile) k_elem_eg(BatchDev B) {
+  __shared__ double sm[32 * 5];
   __shared__ int flag;
-  const int num = *B.num;
-  const int total = B.pre_node[num];
-  for (int t = blockIdx.x; t < total; t += gridDim.x) {
-    const int i = find_tile(B.pre_node, num, t), lt = t - B.pre_node[i];
+  st_elem_eg(B, full_map(B, B.pre_tet), blockIdx.x, gridDim.x, sm, flag);
+}
+
+// node gather of element gradients + linear loads (+ inertia), energy and ||g||^2
+__device__ __forceinline__ void st_gather(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag) {
+  const int total = map_total(M);
+  for (int t = cta; t < total; t += ncta) {
+    int i, lt;
+    map_tile(M, t, i, lt);
     const InstDev& I = B.inst[i];
     NState* st = I.st;
     if (st->phase != PH_EVAL) continue;
@@ -408,8 +493,15 @@ __global__ void __launch_bounds__(kTile) k_gather(BatchDev B) {
       st->E_eval = st->E_el + tot[0];
       st->gg_eval = tot[1];
       st->phase = PH_EVAL_DONE;
+      advance(B, i);
     }
   }
+}
+
+__global__ void __launch_bounds__(kTile) k_gather(BatchDev B) {
+  __shared__ double sm[32 * 5];
+  __shared__ int flag;
+  st_gather(B, full_map(B, B.pre_node), blockIdx.x, gridDim.x, sm, flag);
 }
 
 // ---------------------------------------------------------------------------
@@ -426,20 +518,24 @@ __constant__ int c_pj[10] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
 template <typename Real>
 __device__ __forceinline__ void elem_blocks(const InstDev& I, int e, Real* out /* 90, stride 1 */) {
   int nd[4];
-  double Ds64[9];
-  load_ds(I, e, nd, Ds64);
+  double Du[9];
+  load_du(I, e, nd, Du);
+  const double* r64 = I.rest64 + 12 * (size_t)e;
+  // displacement gradient in FP64, then the element arithmetic in Real
+  Real Hg[9];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+      Hg[r + 3 * c] = (Real)(Du[r] * r64[0 + 3 * c] + Du[r + 3] * r64[1 + 3 * c] + Du[r + 6] * r64[2 + 3 * c]);
   const Real* rest = PcgBufs<Real>::rest(I) + 12 * (size_t)e;
   Real R[12];
 #pragma unroll
   for (int k = 0; k < 12; ++k) R[k] = rest[k];
-  Real Ds[9];
-#pragma unroll
-  for (int k = 0; k < 9; ++k) Ds[k] = (Real)Ds64[k];
   Real F[9];
 #pragma unroll
-  for (int c = 0; c < 3; ++c)
-#pragma unroll
-    for (int r = 0; r < 3; ++r) F[r + 3 * c] = Ds[r] * R[0 + 3 * c] + Ds[r + 3] * R[1 + 3 * c] + Ds[r + 6] * R[2 + 3 * c];
+  for (int k = 0; k < 9; ++k) F[k] = Hg[k];
+  F[0] += (Real)1; F[4] += (Real)1; F[8] += (Real)1;
   const Real w = R[9], lam = R[10], mu = R[11];
   Real Bv[4][3];
 #pragma unroll
@@ -457,8 +553,8 @@ __device__ __forceinline__ void elem_blocks(const InstDev& I, int e, Real* out /
     for (int j = 0; j < 3; ++j)
 #pragma unroll
       for (int i = 0; i < 3; ++i)
-        E[i + 3 * j] = (Real)0.5 * (F[3 * i] * F[3 * j] + F[1 + 3 * i] * F[1 + 3 * j] + F[2 + 3 * i] * F[2 + 3 * j]);
-    E[0] -= (Real)0.5; E[4] -= (Real)0.5; E[8] -= (Real)0.5;
+        E[i + 3 * j] = (Real)0.5 * (Hg[i + 3 * j] + Hg[j + 3 * i] + Hg[3 * i] * Hg[3 * j] + Hg[1 + 3 * i] * Hg[1 + 3 * j] +
+                                    Hg[2 + 3 * i] * Hg[2 + 3 * j]);
     Real trE = E[0] + E[4] + E[8];
 #pragma unroll
     for (int k = 0; k < 9; ++k) S[k] = (Real)2 * mu * E[k];
@@ -475,8 +571,10 @@ __device__ __forceinline__ void elem_blocks(const InstDev& I, int e, Real* out /
   } else {
     Real C[9];
     cof3(F, C);
-    Real J = det3(F);
-    Real logJ2 = dlog<Real>(J * J);
+    const Real I2 = Hg[0] * Hg[4] - Hg[3] * Hg[1] + Hg[0] * Hg[8] - Hg[6] * Hg[2] + Hg[4] * Hg[8] - Hg[7] * Hg[5];
+    const Real jm1 = Hg[0] + Hg[4] + Hg[8] + I2 + det3(Hg);  // J - 1
+    const Real J = (Real)1 + jm1;
+    const Real logJ2 = (jm1 > (Real)-1) ? (Real)2 * dlog1p<Real>(jm1) : dlog<Real>(J * J);
     Real invJ = (Real)1 / J;
 #pragma unroll
     for (int a = 0; a < 4; ++a)
@@ -516,13 +614,12 @@ __device__ __forceinline__ void elem_blocks(const InstDev& I, int e, Real* out /
 }
 
 template <typename Real>
-__global__ void __launch_bounds__(kTile) k_elem_hess(BatchDev B) {
-  extern __shared__ __align__(16) unsigned char smraw[];
+__device__ __forceinline__ void st_elem_hess(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag, unsigned char* smraw) {
   Real* sh = reinterpret_cast<Real*>(smraw);  // [kTile][90]
-  const int num = *B.num;
-  const int total = B.pre_tet[num];
-  for (int t = blockIdx.x; t < total; t += gridDim.x) {
-    const int i = find_tile(B.pre_tet, num, t), lt = t - B.pre_tet[i];
+  const int total = map_total(M);
+  for (int t = cta; t < total; t += ncta) {
+    int i, lt;
+    map_tile(M, t, i, lt);
     const InstDev& I = B.inst[i];
     if (I.st->phase != PH_HESS) continue;
     const int e0 = lt * kTile;
@@ -535,6 +632,14 @@ __global__ void __launch_bounds__(kTile) k_elem_hess(BatchDev B) {
   }
 }
 
+template <typename Real>
+__global__ void __launch_bounds__(kTile) k_elem_hess(BatchDev B) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ double sm[32 * 5];
+  __shared__ int flag;
+  st_elem_hess<Real>(B, full_map(B, B.pre_tet), blockIdx.x, gridDim.x, sm, flag, smraw);
+}
+
 // ---------------------------------------------------------------------------
 // assembly: one 9-lane group per lower block sums its contributions in element
 // order (the segment list), applies inertia and FixMatrixDoFs, and writes the
@@ -542,13 +647,11 @@ __global__ void __launch_bounds__(kTile) k_elem_hess(BatchDev B) {
 // entries is reduced for the regularisation threshold (LinearSolver.cpp:57-66).
 // ---------------------------------------------------------------------------
 template <typename Real>
-__global__ void __launch_bounds__(288) k_assemble(BatchDev B) {
-  __shared__ double sm[32];
-  __shared__ int flag;
-  const int num = *B.num;
-  const int total = B.pre_lob[num];
-  for (int t = blockIdx.x; t < total; t += gridDim.x) {
-    const int i = find_tile(B.pre_lob, num, t), lt = t - B.pre_lob[i];
+__device__ __forceinline__ void st_assemble(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag) {
+  const int total = map_total(M);
+  for (int t = cta; t < total; t += ncta) {
+    int i, lt;
+    map_tile(M, t, i, lt);
     const InstDev& I = B.inst[i];
     NState* st = I.st;
     if (st->phase != PH_HESS) continue;
@@ -556,11 +659,10 @@ __global__ void __launch_bounds__(288) k_assemble(BatchDev B) {
     Real* H = PcgBufs<Real>::H(I);
     const bool dyn = I.opts->dynamic != 0, nofix = st->nofix != 0;
     const double dt = I.opts->dt;
-    const int ent = threadIdx.x % 9, a = ent / 3, b = ent % 3;
     double nrm = 0.0;
-    for (int pass = 0; pass < 4; ++pass) {
-      const int k = lt * kTile + pass * 32 + threadIdx.x / 9;
-      if (k >= I.nlo) continue;
+    for (int it = threadIdx.x; it < kTile * 9; it += blockDim.x) {
+      const int k = lt * kTile + it / 9, ent = it % 9, a = ent / 3, b = ent % 3;
+      if (k >= I.nlo) break;
       Real s = 0;
       const int c0 = I.seg_ptr[k], c1 = I.seg_ptr[k + 1];
       for (int c = c0; c < c1; ++c) s += Hloc[(size_t)I.seg_c[c] * 9 + ent];
@@ -584,15 +686,20 @@ __global__ void __launch_bounds__(288) k_assemble(BatchDev B) {
   }
 }
 
+template <typename Real>
+__global__ void __launch_bounds__(288) k_assemble(BatchDev B) {
+  __shared__ double sm[32 * 5];
+  __shared__ int flag;
+  st_assemble<Real>(B, full_map(B, B.pre_lob), blockIdx.x, gridDim.x, sm, flag);
+}
+
 // preconditioner: inverse of each node's 3x3 diagonal block (+ shift), or of its diagonal
 template <typename Real>
-__global__ void __launch_bounds__(kTile) k_jacobi(BatchDev B) {
-  __shared__ double sm[32];
-  __shared__ int flag;
-  const int num = *B.num;
-  const int total = B.pre_node[num];
-  for (int t = blockIdx.x; t < total; t += gridDim.x) {
-    const int i = find_tile(B.pre_node, num, t), lt = t - B.pre_node[i];
+__device__ __forceinline__ void st_jacobi(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag) {
+  const int total = map_total(M);
+  for (int t = cta; t < total; t += ncta) {
+    int i, lt;
+    map_tile(M, t, i, lt);
     const InstDev& I = B.inst[i];
     NState* st = I.st;
     if (st->phase != PH_HESS && st->phase != PH_JACOBI) continue;
@@ -631,18 +738,24 @@ __global__ void __launch_bounds__(kTile) k_jacobi(BatchDev B) {
     if (tile_done<1>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
       count_bytes(B, I, K_JACOBI);
       st->phase = PH_LINSETUP;
+      advance(B, i);
     }
   }
 }
 
-// b = -g, dx = guess (previous accepted step, EigenCG solveWithGuess) or 0
-__global__ void __launch_bounds__(kTile) k_linsetup(BatchDev B) {
-  __shared__ double sm[32];
+template <typename Real>
+__global__ void __launch_bounds__(kTile) k_jacobi(BatchDev B) {
+  __shared__ double sm[32 * 5];
   __shared__ int flag;
-  const int num = *B.num;
-  const int total = B.pre_node[num];
-  for (int t = blockIdx.x; t < total; t += gridDim.x) {
-    const int i = find_tile(B.pre_node, num, t), lt = t - B.pre_node[i];
+  st_jacobi<Real>(B, full_map(B, B.pre_node), blockIdx.x, gridDim.x, sm, flag);
+}
+
+// b = -g, dx = guess (previous accepted step, EigenCG solveWithGuess) or 0
+__device__ __forceinline__ void st_linsetup(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag) {
+  const int total = map_total(M);
+  for (int t = cta; t < total; t += ncta) {
+    int i, lt;
+    map_tile(M, t, i, lt);
     const InstDev& I = B.inst[i];
     NState* st = I.st;
     if (st->phase != PH_LINSETUP) continue;
@@ -660,7 +773,7 @@ __global__ void __launch_bounds__(kTile) k_linsetup(BatchDev B) {
     double tot[1];
     if (tile_done<1>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
       count_bytes(B, I, K_LINSETUP);
-      const double tol = I.opts->ls_tol_max_error;
+      const double tol = st->lin_tol;
       st->bb = tot[0];
       st->thr_final = fmax(tol * tol * tot[0], DBL_MIN);
       st->sweeps = 0;
@@ -675,8 +788,15 @@ __global__ void __launch_bounds__(kTile) k_linsetup(BatchDev B) {
       } else {
         st->phase = PH_RESID;
       }
+      advance(B, i);
     }
   }
+}
+
+__global__ void __launch_bounds__(kTile) k_linsetup(BatchDev B) {
+  __shared__ double sm[32 * 5];
+  __shared__ int flag;
+  st_linsetup(B, full_map(B, B.pre_node), blockIdx.x, gridDim.x, sm, flag);
 }
 
 // SELL-32 row sweep: acc = sum_k H(row, col_k) * X(col_k), X given per column by a functor.
@@ -702,13 +822,11 @@ __device__ __forceinline__ void sell_row(const InstDev& I, const Real* H, int v,
 
 // r64 = b - (H + shift I) dx in FP64 (FP32 values promoted); starts an inner PCG on r
 template <typename Real>
-__global__ void __launch_bounds__(kTile) k_resid(BatchDev B) {
-  __shared__ double sm[32 * 5];
-  __shared__ int flag;
-  const int num = *B.num;
-  const int total = B.pre_node[num];
-  for (int t = blockIdx.x; t < total; t += gridDim.x) {
-    const int i = find_tile(B.pre_node, num, t), lt = t - B.pre_node[i];
+__device__ __forceinline__ void st_resid(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag) {
+  const int total = map_total(M);
+  for (int t = cta; t < total; t += ncta) {
+    int i, lt;
+    map_tile(M, t, i, lt);
     const InstDev& I = B.inst[i];
     NState* st = I.st;
     if (st->phase != PH_RESID) continue;
@@ -764,20 +882,26 @@ __global__ void __launch_bounds__(kTile) k_resid(BatchDev B) {
         st->lin_status = LIN_RUNNING;
         st->phase = PH_PCG;
       }
+      advance(B, i);
     }
   }
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(kTile) k_resid(BatchDev B) {
+  __shared__ double sm[32 * 5];
+  __shared__ int flag;
+  st_resid<Real>(B, full_map(B, B.pre_node), blockIdx.x, gridDim.x, sm, flag);
 }
 
 // PCG step 1: p = z + beta p_prev (formed on the fly for every column, written
 // for the own row into the other buffer), q = (H + shift I) p, pq = p.q
 template <typename Real>
-__global__ void __launch_bounds__(kTile) k_pcg_a(BatchDev B) {
-  __shared__ double sm[32];
-  __shared__ int flag;
-  const int num = *B.num;
-  const int total = B.pre_node[num];
-  for (int t = blockIdx.x; t < total; t += gridDim.x) {
-    const int i = find_tile(B.pre_node, num, t), lt = t - B.pre_node[i];
+__device__ __forceinline__ void st_pcg_a(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag) {
+  const int total = map_total(M);
+  for (int t = cta; t < total; t += ncta) {
+    int i, lt;
+    map_tile(M, t, i, lt);
     const InstDev& I = B.inst[i];
     NState* st = I.st;
     if (st->phase != PH_PCG) continue;
@@ -816,6 +940,7 @@ __global__ void __launch_bounds__(kTile) k_pcg_a(BatchDev B) {
       if (!(tot[0] > 0.0)) {  // not positive definite along p (or non-finite)
         st->lin_status = LIN_BREAKDOWN;
         st->phase = PH_LIN_DONE;
+        advance(B, i);
       } else {
         st->alpha = st->rz / tot[0];
       }
@@ -823,15 +948,20 @@ __global__ void __launch_bounds__(kTile) k_pcg_a(BatchDev B) {
   }
 }
 
+template <typename Real>
+__global__ void __launch_bounds__(kTile) k_pcg_a(BatchDev B) {
+  __shared__ double sm[32 * 5];
+  __shared__ int flag;
+  st_pcg_a<Real>(B, full_map(B, B.pre_node), blockIdx.x, gridDim.x, sm, flag);
+}
+
 // PCG step 2: e += alpha p, r -= alpha q, z = Minv r; convergence ||r||^2 < thr (Eigen's rule)
 template <typename Real>
-__global__ void __launch_bounds__(kTile) k_pcg_b(BatchDev B) {
-  __shared__ double sm[32 * 2];
-  __shared__ int flag;
-  const int num = *B.num;
-  const int total = B.pre_node[num];
-  for (int t = blockIdx.x; t < total; t += gridDim.x) {
-    const int i = find_tile(B.pre_node, num, t), lt = t - B.pre_node[i];
+__device__ __forceinline__ void st_pcg_b(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag) {
+  const int total = map_total(M);
+  for (int t = cta; t < total; t += ncta) {
+    int i, lt;
+    map_tile(M, t, i, lt);
     const InstDev& I = B.inst[i];
     NState* st = I.st;
     if (st->phase != PH_PCG) continue;
@@ -876,19 +1006,25 @@ __global__ void __launch_bounds__(kTile) k_pcg_b(BatchDev B) {
         st->rz = tot[1];
         st->pcg_parity ^= 1;
       }
+      if (st->phase != PH_PCG) advance(B, i);
     }
   }
 }
 
+template <typename Real>
+__global__ void __launch_bounds__(kTile) k_pcg_b(BatchDev B) {
+  __shared__ double sm[32 * 5];
+  __shared__ int flag;
+  st_pcg_b<Real>(B, full_map(B, B.pre_node), blockIdx.x, gridDim.x, sm, flag);
+}
+
 // dx += e (FP64), then back to the FP64 residual
 template <typename Real>
-__global__ void __launch_bounds__(kTile) k_accum(BatchDev B) {
-  __shared__ double sm[32];
-  __shared__ int flag;
-  const int num = *B.num;
-  const int total = B.pre_node[num];
-  for (int t = blockIdx.x; t < total; t += gridDim.x) {
-    const int i = find_tile(B.pre_node, num, t), lt = t - B.pre_node[i];
+__device__ __forceinline__ void st_accum(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag) {
+  const int total = map_total(M);
+  for (int t = cta; t < total; t += ncta) {
+    int i, lt;
+    map_tile(M, t, i, lt);
     const InstDev& I = B.inst[i];
     NState* st = I.st;
     if (st->phase != PH_ACCUM) continue;
@@ -907,8 +1043,16 @@ __global__ void __launch_bounds__(kTile) k_accum(BatchDev B) {
       st->sweeps++;
       st->total_sweeps++;
       st->phase = PH_RESID;
+      advance(B, i);
     }
   }
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(kTile) k_accum(BatchDev B) {
+  __shared__ double sm[32 * 5];
+  __shared__ int flag;
+  st_accum<Real>(B, full_map(B, B.pre_node), blockIdx.x, gridDim.x, sm, flag);
 }
 
 // the state machine: one thread per instance; writes the active count and phases
@@ -917,16 +1061,203 @@ __global__ void __launch_bounds__(256) k_control(BatchDev B) {
   const int num = *B.num;
   double active = 0.0;
   for (int i = threadIdx.x; i < num; i += blockDim.x) {
-    NState s = *B.inst[i].st;
-    const DevOpts o = *B.inst[i].opts;
-    ctl_advance(s, o);
-    *B.inst[i].st = s;
-    B.flags[8 + i] = s.phase;
-    active += (s.phase != PH_DONE) ? 1.0 : 0.0;
+    advance(B, i);
+    active += (B.flags[8 + i] != PH_DONE) ? 1.0 : 0.0;
   }
   double v[1] = {active};
   block_sum<1>(v, sm);
   if (threadIdx.x == 0) B.flags[0] = (int)v[0];
+}
+
+
+// ---------------------------------------------------------------------------
+// the persistent engine: whole Newton rounds in one cooperative launch
+// ---------------------------------------------------------------------------
+// Grid barrier over all CTAs of a cooperative launch (co-residency is guaranteed by
+// cudaLaunchCooperativeKernel).  The wait is bounded: after kBarrierLimit clock
+// cycles a CTA records a timeout and the stage it was in, and every CTA then leaves
+// the kernel at its next barrier, so a fault in the engine ends the launch instead
+// of hanging the device.
+constexpr long long kBarrierLimit = 4000000000LL;  // about 2 s of SM clock
+
+__device__ __forceinline__ bool grid_sync(GridBar* gb, unsigned int nblocks, int tag) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* vgen = &gb->gen;
+    volatile int* verr = &gb->err;
+    const unsigned int g = *vgen;
+    __threadfence();
+    const unsigned int a = atomicAdd(&gb->arrive, 1u);
+    if (a == nblocks - 1) {
+      gb->arrive = 0u;
+      __threadfence();
+      atomicAdd(&gb->gen, 1u);
+    } else {
+      const long long t0 = clock64();
+      while (*vgen == g) {
+        if (*verr) break;
+        if (clock64() - t0 > kBarrierLimit) {
+          if (atomicCAS(&gb->err, 0, 1) == 0) gb->stage = tag;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return *(volatile int*)&gb->err == 0;
+}
+
+// block-wide exclusive scan of 4 ints; returns totals in tot (all threads)
+__device__ __forceinline__ void block_scan4(int (&v)[4], int (&tot)[4], int* sm /* [32*4] */) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  int inc[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    inc[k] = v[k];
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, inc[k], off);
+      if (lane >= off) inc[k] += y;
+    }
+  }
+  __syncthreads();
+  if (lane == 31)
+#pragma unroll
+    for (int k = 0; k < 4; ++k) sm[warp * 4 + k] = inc[k];
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      int w = lane < nw ? sm[lane * 4 + k] : 0;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, w, off);
+        if (lane >= off) w += y;
+      }
+      if (lane < nw) sm[lane * 4 + k] = w;  // inclusive warp prefix
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int before = warp > 0 ? sm[(warp - 1) * 4 + k] : 0;
+    tot[k] = sm[(nw - 1) * 4 + k];
+    v[k] = before + inc[k] - v[k];  // exclusive
+  }
+  __syncthreads();
+}
+
+// One CTA: starts new solves, publishes phases, and lists the instances not yet done
+// with the prefix of their tet, node and lower-block tile counts.
+__device__ void compact(const BatchDev& B, const EngineArgs& A) {
+  __shared__ int scan_sm[32 * 4];
+  const int num = *B.num;
+  for (int i = threadIdx.x; i < num; i += blockDim.x) {
+    const int ph = *(volatile int32_t*)&B.inst[i].st->phase;
+    if (ph == PH_START) advance(B, i);
+    else B.flags[8 + i] = ph;
+  }
+  __syncthreads();
+  int* ids = A.act + 1;
+  int* pt = ids + A.cap;
+  int* pn = pt + A.cap + 1;
+  int* pl = pn + A.cap + 1;
+  int run[4] = {0, 0, 0, 0};
+  for (int base = 0; base < num; base += blockDim.x) {
+    const int i = base + threadIdx.x;
+    const bool act = i < num && B.flags[8 + i] != PH_DONE;
+    int c[4] = {act ? 1 : 0, act ? tiles_of(B.inst[i].m) : 0, act ? tiles_of(B.inst[i].n) : 0,
+                act ? tiles_of(B.inst[i].nlo) : 0};
+    int ex[4] = {c[0], c[1], c[2], c[3]}, tot[4];
+    block_scan4(ex, tot, scan_sm);
+    if (act) {
+      const int pos = run[0] + ex[0];
+      ids[pos] = i;
+      pt[pos + 1] = run[1] + ex[1] + c[1];
+      pn[pos + 1] = run[2] + ex[2] + c[2];
+      pl[pos + 1] = run[3] + ex[3] + c[3];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) run[k] += tot[k];
+  }
+  if (threadIdx.x == 0) {
+    pt[0] = 0; pn[0] = 0; pl[0] = 0;
+    A.act[0] = run[0];
+    B.flags[0] = run[0];
+  }
+  __threadfence();
+}
+
+__device__ __forceinline__ void stage_clock(const EngineArgs& A, int kind, unsigned long long& t) {
+  if (A.stage_ns && blockIdx.x == 0 && threadIdx.x == 0) {
+    unsigned long long now;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+    A.stage_ns[kind] += now - t;
+    A.stage_ns[16 + kind] += 1;
+    t = now;
+  }
+}
+
+template <typename Real>
+__global__ void __launch_bounds__(kTile, (sizeof(Real) == 4 ? 4 : 2)) k_engine(BatchDev B, EngineArgs A) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  __shared__ double sm[32 * 5];
+  __shared__ int flag;
+  const int cta = blockIdx.x, ncta = gridDim.x;
+  int* ids = A.act + 1;
+  int* pt = ids + A.cap;
+  int* pn = pt + A.cap + 1;
+  int* pl = pn + A.cap + 1;
+  unsigned long long t = 0;
+  if (A.stage_ns && cta == 0 && threadIdx.x == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+#define PHX_SYNC(tag, kind)                             \
+  if (!grid_sync(A.bar, (unsigned)ncta, tag)) return; \
+  stage_clock(A, kind, t);
+  for (int r = 0; r < A.rounds; ++r) {
+    if (cta == 0) compact(B, A);
+    PHX_SYNC(1, K_CONTROL);
+    const int na = __ldcg(A.act);
+    if (na == 0) break;
+    const TileMap Mt{pt, ids, na}, Mn{pn, ids, na}, Ml{pl, ids, na};
+    st_vecop(B, Mn, cta, ncta, sm, flag);
+    PHX_SYNC(2, K_VECOP);
+    st_elem_eg(B, Mt, cta, ncta, sm, flag);
+    PHX_SYNC(3, K_ELEM_EG);
+    st_gather(B, Mn, cta, ncta, sm, flag);
+    PHX_SYNC(4, K_GATHER);
+    st_vecop(B, Mn, cta, ncta, sm, flag);
+    PHX_SYNC(5, K_VECOP);
+    st_elem_hess<Real>(B, Mt, cta, ncta, sm, flag, smraw);
+    PHX_SYNC(6, K_ELEM_HESS);
+    st_assemble<Real>(B, Ml, cta, ncta, sm, flag);
+    PHX_SYNC(7, K_ASSEMBLE);
+    st_jacobi<Real>(B, Mn, cta, ncta, sm, flag);
+    PHX_SYNC(8, K_JACOBI);
+    st_linsetup(B, Mn, cta, ncta, sm, flag);
+    PHX_SYNC(9, K_LINSETUP);
+    st_resid<Real>(B, Mn, cta, ncta, sm, flag);
+    PHX_SYNC(10, K_RESID);
+    for (int k = 0; k < A.pcg_chunk; ++k) {
+      st_pcg_a<Real>(B, Mn, cta, ncta, sm, flag);
+      PHX_SYNC(11, K_PCG_A);
+      st_pcg_b<Real>(B, Mn, cta, ncta, sm, flag);
+      PHX_SYNC(12, K_PCG_B);
+    }
+    st_accum<Real>(B, Mn, cta, ncta, sm, flag);
+    PHX_SYNC(13, K_ACCUM);
+    st_resid<Real>(B, Mn, cta, ncta, sm, flag);
+    PHX_SYNC(14, K_RESID);
+    st_vecop(B, Mn, cta, ncta, sm, flag);
+    PHX_SYNC(15, K_VECOP);
+    st_elem_eg(B, Mt, cta, ncta, sm, flag);
+    PHX_SYNC(16, K_ELEM_EG);
+    st_gather(B, Mn, cta, ncta, sm, flag);
+    PHX_SYNC(17, K_GATHER);
+  }
+#undef PHX_SYNC
+  if (cta == 0) compact(B, A);
 }
 
 // ---------------------------------------------------------------------------
@@ -938,9 +1269,32 @@ size_t hess_smem() { return (size_t)kTile * 90 * sizeof(Real); }
 cudaError_t setup_kernel_attributes() {
   cudaError_t e = cudaFuncSetAttribute(k_elem_hess<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)hess_smem<double>());
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_elem_hess<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)hess_smem<float>());
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_elem_hess<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hess_smem<float>());
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_engine<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hess_smem<double>());
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_engine<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hess_smem<float>());
+  return e;
+}
+
+int engine_grid(bool fp64, int num_sms) {
+  int nb = 0;
+  cudaError_t e = fp64 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_engine<double>, kTile, hess_smem<double>())
+                       : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_engine<float>, kTile, hess_smem<float>());
+  if (e != cudaSuccess || nb < 1) return 0;
+  return nb * num_sms;
+}
+
+cudaError_t launch_engine(bool fp64, int grid, cudaStream_t s, const BatchDev& B, const EngineArgs& A) {
+  BatchDev b = B;
+  EngineArgs a = A;
+  void* args[] = {(void*)&b, (void*)&a};
+  if (fp64)
+    return cudaLaunchCooperativeKernel((const void*)k_engine<double>, dim3(grid), dim3(kTile), args,
+                                       hess_smem<double>(), s);
+  return cudaLaunchCooperativeKernel((const void*)k_engine<float>, dim3(grid), dim3(kTile), args, hess_smem<float>(),
+                                     s);
 }
 
 void launch(KernelId id, int grid, cudaStream_t s, const BatchDev& B, bool fp64) {

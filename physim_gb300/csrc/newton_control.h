@@ -64,6 +64,33 @@ PHX_HD inline void ctl_goto(NState& s, int32_t next) {
   }
 }
 
+// Relative tolerance of this Newton step's linear solve.  The plain FP64 path keeps the
+// reference's fixed ls_tol_max_error (LinearSolver_EigenCG with lsTolMaxError).  The FP32
+// path solves inexactly with Eisenstat-Walker forcing terms (choice 2: gamma = 0.9,
+// alpha = 2, safeguarded, eta_max = 0.1), never tighter than needed to reach the
+// nonlinear tolerance and never tighter than ls_tol_max_error; the FP64 gradient and
+// the nonlinear test decide convergence.
+PHX_HD inline double ctl_forcing(NState& s, const DevOpts& o) {
+  if (o.precision == 0) return o.ls_tol_max_error;
+  const double eta_max = 0.1, gamma = 0.9;
+  double eta;
+  if (s.opt_prev <= 0.0 || s.eta <= 0.0) {
+    eta = eta_max;
+  } else {
+    double r = s.opt / s.opt_prev;
+    eta = gamma * r * r;
+    double safe = gamma * s.eta * s.eta;
+    if (safe > 0.1 && safe > eta) eta = safe;
+  }
+  if (eta > eta_max) eta = eta_max;
+  double need = (s.opt > 0.0) ? 0.5 * s.tol_eff / s.opt : eta_max;
+  if (eta < need) eta = need;
+  if (eta > eta_max) eta = eta_max;
+  if (eta < o.ls_tol_max_error) eta = o.ls_tol_max_error;
+  s.eta = eta;
+  return eta;
+}
+
 // Start of SolveStepInternal (energy, gradient and ||g|| at x are known).
 PHX_HD inline void ctl_iter_begin(NState& s, const DevOpts& o) {
   s.it++;
@@ -75,6 +102,8 @@ PHX_HD inline void ctl_iter_begin(NState& s, const DevOpts& o) {
   if (s.opt < s.tol_eff) {
     s.result = OS_SUCCESS;
     s.step_result = OS_SUCCESS;
+    s.log_step = 0.0;
+    s.log_pending = 1;
     ctl_goto(s, ctl_post_step(s, o));
     return;
   }
@@ -92,6 +121,8 @@ PHX_HD inline void ctl_iter_begin(NState& s, const DevOpts& o) {
     s.reg_trial = 0;
     s.shift = 0.0;
     s.hess_count++;
+    s.lin_tol = ctl_forcing(s, o);
+    s.opt_prev = s.opt;
     s.phase = PH_HESS;
   }
 }
@@ -141,6 +172,8 @@ PHX_HD inline void ctl_ls_check(NState& s, const DevOpts& o) {
     s.obj = objNew;
     s.opt = optNew;
     s.total_bis += s.num_bis;
+    s.log_step = step;
+    s.log_pending = 1;
     s.vecop = VO_ACCEPT | VO_SAVE;
     ctl_goto(s, ctl_post_step(s, o));
     return;
@@ -158,6 +191,8 @@ PHX_HD inline void ctl_ls_check(NState& s, const DevOpts& o) {
   s.result = OS_NONDESC;
   s.step_result = OS_NONDESC;
   s.total_bis += s.num_bis;
+  s.log_step = stepCur;
+  s.log_pending = 1;
   s.vecop = VO_RESTORE;
   ctl_goto(s, ctl_post_step(s, o));
 }
@@ -179,6 +214,10 @@ PHX_HD inline void ctl_advance(NState& s, const DevOpts& o) {
         s.pcg_total = 0;
         s.hess_count = 0;
         s.opt0 = -1.0;
+        s.eta = 0.0;
+        s.opt_prev = 0.0;
+        s.log_count = 0;
+        s.log_pending = 0;
         s.tol_eff = o.tol_max_error;
         s.purpose = 0;
         s.vecop = o.dynamic ? VO_PRED : 0;

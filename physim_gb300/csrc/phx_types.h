@@ -86,7 +86,13 @@ struct NState {
   double rr64, rz, rr, pq;
   double alpha, beta, thr_inner, thr_final;
   double tol_eff;                              // max(tol_max_error, tol_rel * opt0)
+  double lin_tol;                              // relative residual target of this step's linear solve
+  double eta, opt_prev;                        // forcing term state (FP32 path)
+  double log_step;                             // ||dx_final|| of the step being logged
+  int32_t log_pending, log_count;              // per-iteration log bookkeeping
 };
+
+constexpr int kLogCap = 256;                   // Newton iterations kept in the per-instance log
 
 // Device descriptor of one instance (pointers into the arena).
 struct InstDev {
@@ -131,6 +137,7 @@ struct InstDev {
   uint32_t* counter;          // [1]
   NState* st;
   const DevOpts* opts;
+  double* log;                // [kLogCap][4]: obj, opt, bisections, step per Newton iteration
   double algo[12];            // algorithmic bytes of one launch of each kernel kind on this instance
 };
 

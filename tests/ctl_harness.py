@@ -24,7 +24,8 @@ class NState(C.Structure):
         [("pcg_total", C.c_int64)] + [(n, C.c_double) for n in (
             "obj", "opt", "opt0", "obj_new", "alpha_trial", "factor", "scale", "dx_norm", "b_dot_dx", "E_el",
             "E_eval", "gg_eval", "normA2", "shift", "regT", "bb", "rr64", "rz", "rr", "pq", "alpha", "beta",
-            "thr_inner", "thr_final", "tol_eff")]
+            "thr_inner", "thr_final", "tol_eff", "lin_tol", "eta", "opt_prev", "log_step")] + \
+        [("log_pending", C.c_int32), ("log_count", C.c_int32)]
 
 
 class DevOpts(C.Structure):
@@ -181,7 +182,7 @@ def run(shim, orc, x0, opts, dynamic=False, v0=None, max_steps=200000):
             b = -g
             dx = dxprev.copy() if o.warm_guess else np.zeros(N)
             s.bb = b @ b
-            s.thr_final = max(o.ls_tol_max_error ** 2 * s.bb, 2.2250738585072014e-308)
+            s.thr_final = max(s.lin_tol ** 2 * s.bb, 2.2250738585072014e-308)
             s.sweeps = 0
             s.lin_status = LIN_RUNNING
             if s.bb == 0:

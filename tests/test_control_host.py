@@ -79,3 +79,18 @@ def test_max_iterations_cap(ctl_shim):
     x0 = orc.rest()
     x, _, s = H.run(ctl_shim, orc, x0, H.make_opts(num_max_iters=2, tol_max_error=1e-14))
     assert s.result == 5 and s.it == 2  # MAXITER after two SolveSteps
+
+
+def test_inexact_newton_forcing_converges_to_the_same_point(ctl_shim):
+    """The FP32 path's Eisenstat-Walker forcing terms change the linear tolerances, not the answer."""
+    m = _case(0, (2, 2, 6))
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    g0 = np.linalg.norm(orc.gradient(x0))
+    kw = dict(tol_max_error=1e-9 * g0, tol_min_impr=0.0, tol_min_step=0.0)
+    xo, ro = orc.solve_static(x0, **kw)
+    x, _, s = H.run(ctl_shim, orc, x0, H.make_opts(precision=1, **kw))
+    assert s.result == 1 and s.opt <= 1e-9 * g0
+    assert rel(x - x0, xo - x0) < 1e-8
+    _, _, s64 = H.run(ctl_shim, orc, x0, H.make_opts(**kw))
+    assert s.pcg_total < s64.pcg_total  # looser linear solves on the way
