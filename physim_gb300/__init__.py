@@ -58,7 +58,8 @@ class Options(C.Structure):
                 ("ls_tol_max_error", C.c_double), ("ls_num_reg_trials", C.c_int32), ("lsearch_type", C.c_int32),
                 ("lsearch_alpha", C.c_double), ("lsearch_num_try", C.c_int32), ("precision", C.c_int32),
                 ("precond", C.c_int32), ("inner_tol", C.c_double), ("max_refine_sweeps", C.c_int32),
-                ("warm_guess", C.c_int32), ("pcg_chunk", C.c_int32), ("tol_rel", C.c_double)]
+                ("warm_guess", C.c_int32), ("pcg_chunk", C.c_int32), ("tol_rel", C.c_double),
+                ("pcg_cluster", C.c_int32), ("reserved0", C.c_int32)]
 
 
 class Report(C.Structure):

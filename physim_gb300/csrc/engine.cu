@@ -142,6 +142,8 @@ struct phx_context_s {
   int act_cap = 0;
   unsigned long long* d_stage = nullptr;  // [32] stage ns + executions (profiling)
   int egrid[2] = {0, 0};
+  int32_t* d_clist = nullptr;  // instances whose PCG runs per cluster (batch order)
+  int clist_cap = 0;
 };
 
 struct phx_instance_s {
@@ -412,11 +414,11 @@ void fill_report(const NState& s, bool step, double seconds, phx_report* r) {
 }
 
 int ensure_engine(phx_context ctx) {
-  if (!ctx->d_bar) CU(cudaMalloc(&ctx->d_bar, sizeof(GridBar)));
+  if (!ctx->d_bar) CU(cudaMalloc(&ctx->d_bar, 2 * sizeof(GridBar)));
   if (ctx->act_cap < ctx->cap) {
     if (ctx->d_act) cudaFree(ctx->d_act);
     ctx->d_act = nullptr;
-    CU(cudaMalloc(&ctx->d_act, sizeof(int32_t) * (1 + ctx->cap + 3 * (ctx->cap + 1))));
+    CU(cudaMalloc(&ctx->d_act, sizeof(int32_t) * (4 + ctx->cap + 3 * (ctx->cap + 1))));
     ctx->act_cap = ctx->cap;
   }
   if (ctx->profiling && !ctx->d_stage) {
@@ -432,15 +434,61 @@ int run_engine(phx_context ctx, const BatchDev& B, int num, bool fp64, int round
   int& grid = ctx->egrid[fp64 ? 1 : 0];
   if (grid == 0) grid = engine_grid(fp64, ctx->num_sms);
   if (grid <= 0) return set_err(PHX_ECUDA, "engine kernel cannot be made resident");
-  CU(cudaMemsetAsync(ctx->d_bar, 0, sizeof(GridBar), ctx->stream));
+  CU(cudaMemsetAsync(ctx->d_bar, 0, 2 * sizeof(GridBar), ctx->stream));
+  const int32_t hdr[2] = {0, grid};  // active count (set by the kernel), CTAs running
+  CU(cudaMemcpyAsync(ctx->d_act, hdr, sizeof(hdr), cudaMemcpyHostToDevice, ctx->stream));
   EngineArgs A{ctx->d_bar, ctx->d_act, ctx->profiling ? ctx->d_stage : nullptr, ctx->cap, rounds, pcg_chunk};
   CU(launch_engine(fp64, grid, ctx->stream, B, A));
   ctx->launches++;
-  GridBar hb;
-  CU(cudaMemcpyAsync(&hb, ctx->d_bar, sizeof(GridBar), cudaMemcpyDeviceToHost, ctx->stream));
+  GridBar hb[2];
+  CU(cudaMemcpyAsync(hb, ctx->d_bar, 2 * sizeof(GridBar), cudaMemcpyDeviceToHost, ctx->stream));
   TRY(read_flags(ctx, num));
-  if (hb.err)
-    return set_err(PHX_ETIMEOUT, "engine grid barrier timed out (stage " + std::to_string(hb.stage) + ")");
+  if (hb[0].err || hb[1].err)
+    return set_err(PHX_ETIMEOUT, "engine grid barrier timed out (stage " +
+                                     std::to_string(hb[1].err ? hb[1].stage : hb[0].stage) + ")");
+  return PHX_OK;
+}
+
+// Uploads the batch positions of the instances whose PCG runs per cluster, largest first.
+int set_cluster_list(phx_context ctx, const std::vector<phx_instance>& list, int* count) {
+  std::vector<int32_t> ids;
+  for (int i = 0; i < (int)list.size(); ++i)
+    if (list[i]->dev.pcg_cluster) ids.push_back(i);
+  std::stable_sort(ids.begin(), ids.end(), [&](int a, int b) { return list[a]->dev.nslots > list[b]->dev.nslots; });
+  *count = (int)ids.size();
+  if (ids.empty()) return PHX_OK;
+  if (ctx->clist_cap < (int)ids.size()) {
+    if (ctx->d_clist) cudaFree(ctx->d_clist);
+    ctx->d_clist = nullptr;
+    CU(cudaMalloc(&ctx->d_clist, sizeof(int32_t) * ids.size()));
+    ctx->clist_cap = (int)ids.size();
+  }
+  CU(cudaMemcpyAsync(ctx->d_clist, ids.data(), sizeof(int32_t) * ids.size(), cudaMemcpyHostToDevice, ctx->stream));
+  return PHX_OK;
+}
+
+// One step of the device engine: engine rounds, then (if any) the per-cluster PCG solves.
+int run_step(phx_context ctx, const BatchDev& B, int num, bool fp64, int pcg_chunk, int ccount) {
+  TRY(run_engine(ctx, B, num, fp64, kRoundsPerLaunch, pcg_chunk));
+  if (ccount > 0 && ctx->h_flags[0] > 0) {
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (ctx->profiling) {
+      if (ctx->pool.size() >= 2) {
+        a = ctx->pool.back(); ctx->pool.pop_back();
+        b = ctx->pool.back(); ctx->pool.pop_back();
+      } else {
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+      }
+      cudaEventRecord(a, ctx->stream);
+    }
+    CU(launch_pcg_cluster(fp64, ctx->stream, B, ctx->d_clist, ccount));
+    ctx->launches++;
+    if (ctx->profiling) {
+      cudaEventRecord(b, ctx->stream);
+      ctx->evs.push_back({(int)K_PCG_CLUSTER, a, b});
+    }
+  }
   return PHX_OK;
 }
 
@@ -449,10 +497,12 @@ int run_to_completion(phx_context ctx, const std::vector<phx_instance>& list, bo
   BatchDev B{};
   Grids G;
   TRY(set_batch(ctx, list, B, G));
+  int ccount = 0;
+  TRY(set_cluster_list(ctx, list, &ccount));
   const int num = (int)list.size();
   const auto t0 = clk::now();
   for (int64_t r = 0;; ++r) {
-    TRY(run_engine(ctx, B, num, fp64, kRoundsPerLaunch, pcg_chunk));
+    TRY(run_step(ctx, B, num, fp64, pcg_chunk, ccount));
     if (ctx->h_flags[0] == 0) return PHX_OK;
     if (std::chrono::duration<double>(clk::now() - t0).count() > kSolveTimeLimit)
       return set_err(PHX_ETIMEOUT, "solver did not finish within " + std::to_string(kSolveTimeLimit) + " s");
@@ -463,7 +513,7 @@ int run_to_completion(phx_context ctx, const std::vector<phx_instance>& list, bo
 // must read and every output it must write, once (padding, re-reads and caches excluded).
 void set_algo_bytes(InstDev& D, bool fp64) {
   const double s = fp64 ? 8.0 : 4.0, n = D.n, m = D.m, nlo = D.nlo, nfull = 2.0 * D.nlo - D.n, N = 3.0 * D.n;
-  for (int k = 0; k < 12; ++k) D.algo[k] = 0.0;
+  for (int k = 0; k < 16; ++k) D.algo[k] = 0.0;
   D.algo[K_ELEM_EG] = 16 * m + 96 * m + m + 8 * N + 96 * m + 8 * m;
   D.algo[K_GATHER] = 96 * m + 16 * m + 4 * (n + 1) + n + 3 * 8 * N;
   D.algo[K_ELEM_HESS] = 16 * m + 12 * s * m + m + 8 * N + 90 * s * m;
@@ -483,6 +533,9 @@ int start_solve(phx_instance inst, const phx_options* o, bool dynamic, double dt
   DevOpts d = make_opts(o, dynamic, dt);
   if (max_iters_override > 0) d.num_max_iters = max_iters_override;
   set_algo_bytes(inst->dev, fp64);
+  // the cluster PCG serves the FP32 path: FP64 arithmetic is slow on this part and needs
+  // every SM, so FP64 solves iterate on the whole GPU
+  inst->dev.pcg_cluster = (o->pcg_cluster && !fp64 && inst->dev.n <= kClusterMaxNodes) ? 1 : 0;
   CU(cudaMemcpyAsync(inst->d_opts, &d, sizeof(DevOpts), cudaMemcpyHostToDevice, inst->ctx->stream));
   TRY(reset_state(inst, PH_START, 0, 0.0));
   return PHX_OK;
@@ -525,6 +578,8 @@ void phx_default_options(phx_options* o) {
   o->warm_guess = 1;
   o->pcg_chunk = 32;
   o->tol_rel = 0.0;
+  o->pcg_cluster = 1;
+  o->reserved0 = 0;
 }
 
 int phx_context_create(int32_t device, int64_t arena_bytes, phx_context* out) {
@@ -568,6 +623,7 @@ int phx_context_destroy(phx_context ctx) {
   if (ctx->d_bar) cudaFree(ctx->d_bar);
   if (ctx->d_act) cudaFree(ctx->d_act);
   if (ctx->d_stage) cudaFree(ctx->d_stage);
+  if (ctx->d_clist) cudaFree(ctx->d_clist);
   for (auto& ev : ctx->marks)
     if (ev) cudaEventDestroy(ev);
   ctx->arena.release();
@@ -1014,6 +1070,7 @@ struct phx_server_s {
   bool dirty = true;
   BatchDev B{};
   Grids G;
+  int ccount = 0;
 };
 
 extern "C" {
@@ -1086,10 +1143,11 @@ int phx_server_progress(phx_server s, int32_t* active, int32_t* queued) {
       std::vector<phx_instance> list;
       for (auto& r : s->active) list.push_back(r.inst);
       TRY(set_batch(s->ctx, list, s->B, s->G));
+      TRY(set_cluster_list(s->ctx, list, &s->ccount));
       s->ctx->batch_owner = s;
       s->dirty = false;
     }
-    TRY(run_engine(s->ctx, s->B, (int)s->active.size(), s->fp64, 2, s->opts.pcg_chunk));
+    TRY(run_step(s->ctx, s->B, (int)s->active.size(), s->fp64, s->opts.pcg_chunk, s->ccount));
   }
   if (active) *active = (int32_t)s->active.size();
   if (queued) *queued = (int32_t)s->queue.size();

@@ -800,23 +800,34 @@ __global__ void __launch_bounds__(kTile) k_linsetup(BatchDev B) {
 }
 
 // SELL-32 row sweep: acc = sum_k H(row, col_k) * X(col_k), X given per column by a functor.
+// Slots are taken 4 at a time: all column ids, then all gathers and block loads are issued
+// before the arithmetic, so one row costs a few memory round trips instead of one per slot
+// (what bounds the sweep when only a few small instances are still iterating).
 template <typename Real, typename Acc, typename GetX>
 __device__ __forceinline__ void sell_row(const InstDev& I, const Real* H, int v, GetX getx, Acc (&acc)[3]) {
   const int c = v >> 5, lane = v & 31;
-  const int s0 = I.chunk_off[c];
-  const int len = (I.chunk_off[c + 1] - s0) >> 5;
+  const int s0 = __ldg(I.chunk_off + c);
+  const int len = (__ldg(I.chunk_off + c + 1) - s0) >> 5;
   acc[0] = acc[1] = acc[2] = (Acc)0;
-  for (int k = 0; k < len; ++k) {
-    const int64_t s = (int64_t)s0 + k * 32 + lane;
-    const int col = __ldg(I.slot_col + s);
-    const Real* hp = H + (s >> 5) * 288 + (s & 31);
-    Acc h[9];
+  for (int k0 = 0; k0 < len; k0 += 4) {
+    int col[4];
 #pragma unroll
-    for (int q = 0; q < 9; ++q) h[q] = (Acc)hp[q * 32];
-    Acc xc[3];
-    getx(col, xc);
+    for (int u = 0; u < 4; ++u) col[u] = (k0 + u < len) ? __ldg(I.slot_col + (int64_t)s0 + (k0 + u) * 32 + lane) : v;
+    Acc xc[4][3];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) acc[a] += h[3 * a] * xc[0] + h[3 * a + 1] * xc[1] + h[3 * a + 2] * xc[2];
+    for (int u = 0; u < 4; ++u) getx(col[u], xc[u]);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (k0 + u < len) {
+        const int64_t s = (int64_t)s0 + (k0 + u) * 32 + lane;
+        const Real* hp = H + (s >> 5) * 288 + (s & 31);
+        Acc h[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) h[q] = (Acc)hp[q * 32];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) acc[a] += h[3 * a] * xc[u][0] + h[3 * a + 1] * xc[u][1] + h[3 * a + 2] * xc[u][2];
+      }
+    }
   }
 }
 
@@ -904,7 +915,7 @@ __device__ __forceinline__ void st_pcg_a(const BatchDev& B, const TileMap& M, in
     map_tile(M, t, i, lt);
     const InstDev& I = B.inst[i];
     NState* st = I.st;
-    if (st->phase != PH_PCG) continue;
+    if (st->phase != PH_PCG || I.pcg_cluster) continue;
     const int v = lt * kTile + threadIdx.x;
     double p[1] = {0.0};
     if (v < I.n) {
@@ -964,7 +975,7 @@ __device__ __forceinline__ void st_pcg_b(const BatchDev& B, const TileMap& M, in
     map_tile(M, t, i, lt);
     const InstDev& I = B.inst[i];
     NState* st = I.st;
-    if (st->phase != PH_PCG) continue;
+    if (st->phase != PH_PCG || I.pcg_cluster) continue;
     const int v = lt * kTile + threadIdx.x;
     double p[2] = {0.0, 0.0};
     if (v < I.n) {
@@ -1080,11 +1091,14 @@ __global__ void __launch_bounds__(256) k_control(BatchDev B) {
 // of hanging the device.
 constexpr long long kBarrierLimit = 4000000000LL;  // about 2 s of SM clock
 
-__device__ __forceinline__ bool grid_sync(GridBar* gb, unsigned int nblocks, int tag) {
+// nblocks = the CTAs taking part (always the lowest-numbered ones).
+// `abort` is the launch-wide error flag (the round-wide barrier's): a timeout on either
+// barrier object raises it and every waiting CTA leaves.
+__device__ __forceinline__ bool grid_sync(GridBar* gb, unsigned int nblocks, int tag, int* abort) {
   __syncthreads();
   if (threadIdx.x == 0) {
     volatile unsigned int* vgen = &gb->gen;
-    volatile int* verr = &gb->err;
+    volatile int* verr = abort;
     const unsigned int g = *vgen;
     __threadfence();
     const unsigned int a = atomicAdd(&gb->arrive, 1u);
@@ -1094,19 +1108,21 @@ __device__ __forceinline__ bool grid_sync(GridBar* gb, unsigned int nblocks, int
       atomicAdd(&gb->gen, 1u);
     } else {
       const long long t0 = clock64();
+      int polls = 0;
       while (*vgen == g) {
         if (*verr) break;
         if (clock64() - t0 > kBarrierLimit) {
           if (atomicCAS(&gb->err, 0, 1) == 0) gb->stage = tag;
+          atomicExch(abort, 1);
           break;
         }
-        __nanosleep(64);
+        if (++polls > 64) __nanosleep(32);
       }
     }
     __threadfence();
   }
   __syncthreads();
-  return *(volatile int*)&gb->err == 0;
+  return *(volatile int*)abort == 0;
 }
 
 // block-wide exclusive scan of 4 ints; returns totals in tot (all threads)
@@ -1150,7 +1166,9 @@ __device__ __forceinline__ void block_scan4(int (&v)[4], int (&tot)[4], int* sm 
 }
 
 // One CTA: starts new solves, publishes phases, and lists the instances not yet done
-// with the prefix of their tet, node and lower-block tile counts.
+// with the prefix of their tet, node and lower-block tile counts.  It also sizes the
+// round: act[1] = CTAs that take part (no more than the CTAs still running, act[1] of
+// the previous round), act[2] = CTAs that take part in the PCG block.
 __device__ void compact(const BatchDev& B, const EngineArgs& A) {
   __shared__ int scan_sm[32 * 4];
   const int num = *B.num;
@@ -1160,14 +1178,22 @@ __device__ void compact(const BatchDev& B, const EngineArgs& A) {
     else B.flags[8 + i] = ph;
   }
   __syncthreads();
-  int* ids = A.act + 1;
+  int* ids = A.act + 4;
   int* pt = ids + A.cap;
   int* pn = pt + A.cap + 1;
   int* pl = pn + A.cap + 1;
   int run[4] = {0, 0, 0, 0};
+  __shared__ int eng_pcg_tiles, cluster_waiting;
+  if (threadIdx.x == 0) {
+    eng_pcg_tiles = 0;
+    cluster_waiting = 0;
+  }
+  __syncthreads();
   for (int base = 0; base < num; base += blockDim.x) {
     const int i = base + threadIdx.x;
     const bool act = i < num && B.flags[8 + i] != PH_DONE;
+    if (act && !B.inst[i].pcg_cluster) atomicAdd(&eng_pcg_tiles, tiles_of(B.inst[i].n));
+    if (act && B.inst[i].pcg_cluster && B.flags[8 + i] == PH_PCG) atomicAdd(&cluster_waiting, 1);
     int c[4] = {act ? 1 : 0, act ? tiles_of(B.inst[i].m) : 0, act ? tiles_of(B.inst[i].n) : 0,
                 act ? tiles_of(B.inst[i].nlo) : 0};
     int ex[4] = {c[0], c[1], c[2], c[3]}, tot[4];
@@ -1186,6 +1212,12 @@ __device__ void compact(const BatchDev& B, const EngineArgs& A) {
     pt[0] = 0; pn[0] = 0; pl[0] = 0;
     A.act[0] = run[0];
     B.flags[0] = run[0];
+    const int alive = A.act[1];
+    int need = max(run[1], max(run[2], run[3]));
+    int p = min(alive, max(need, 1));
+    A.act[1] = p;
+    A.act[2] = min(p, eng_pcg_tiles);  // 0: no instance iterates its PCG in the engine
+    A.act[3] = cluster_waiting;        // instances waiting for the cluster PCG kernel
   }
   __threadfence();
 }
@@ -1205,59 +1237,293 @@ __global__ void __launch_bounds__(kTile, (sizeof(Real) == 4 ? 4 : 2)) k_engine(B
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ double sm[32 * 5];
   __shared__ int flag;
-  const int cta = blockIdx.x, ncta = gridDim.x;
-  int* ids = A.act + 1;
+  const int cta = blockIdx.x;
+  int* ids = A.act + 4;
   int* pt = ids + A.cap;
   int* pn = pt + A.cap + 1;
   int* pl = pn + A.cap + 1;
   unsigned long long t = 0;
   if (A.stage_ns && cta == 0 && threadIdx.x == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-#define PHX_SYNC(tag, kind)                             \
-  if (!grid_sync(A.bar, (unsigned)ncta, tag)) return; \
+  // CTAs still running; the host sets act[1] = gridDim.x before the launch
+  int alive = gridDim.x;
+  // two barrier objects: the PCG group synchronises on its own counter while the CTAs
+  // that skip the PCG block are already arriving at the next round-wide barrier
+#define PHX_SYNC(n, tag, kind)                                          \
+  if (!grid_sync(A.bar, (unsigned)(n), tag, &A.bar->err)) return;      \
+  stage_clock(A, kind, t);
+#define PHX_SYNC_PCG(n, tag, kind)                                      \
+  if (!grid_sync(A.bar + 1, (unsigned)(n), tag, &A.bar->err)) return;  \
   stage_clock(A, kind, t);
   for (int r = 0; r < A.rounds; ++r) {
     if (cta == 0) compact(B, A);
-    PHX_SYNC(1, K_CONTROL);
+    PHX_SYNC(alive, 1, K_CONTROL);
     const int na = __ldcg(A.act);
     if (na == 0) break;
+    // hand over to the cluster PCG kernel as soon as an instance waits for it
+    if (r > 0 && __ldcg(A.act + 3) > 0) break;
+    // this round needs only P CTAs (P never grows within a launch: the rest leave)
+    const int P = __ldcg(A.act + 1), Pp = __ldcg(A.act + 2);
+    if (cta >= P) return;
+    alive = P;
     const TileMap Mt{pt, ids, na}, Mn{pn, ids, na}, Ml{pl, ids, na};
-    st_vecop(B, Mn, cta, ncta, sm, flag);
-    PHX_SYNC(2, K_VECOP);
-    st_elem_eg(B, Mt, cta, ncta, sm, flag);
-    PHX_SYNC(3, K_ELEM_EG);
-    st_gather(B, Mn, cta, ncta, sm, flag);
-    PHX_SYNC(4, K_GATHER);
-    st_vecop(B, Mn, cta, ncta, sm, flag);
-    PHX_SYNC(5, K_VECOP);
-    st_elem_hess<Real>(B, Mt, cta, ncta, sm, flag, smraw);
-    PHX_SYNC(6, K_ELEM_HESS);
-    st_assemble<Real>(B, Ml, cta, ncta, sm, flag);
-    PHX_SYNC(7, K_ASSEMBLE);
-    st_jacobi<Real>(B, Mn, cta, ncta, sm, flag);
-    PHX_SYNC(8, K_JACOBI);
-    st_linsetup(B, Mn, cta, ncta, sm, flag);
-    PHX_SYNC(9, K_LINSETUP);
-    st_resid<Real>(B, Mn, cta, ncta, sm, flag);
-    PHX_SYNC(10, K_RESID);
-    for (int k = 0; k < A.pcg_chunk; ++k) {
-      st_pcg_a<Real>(B, Mn, cta, ncta, sm, flag);
-      PHX_SYNC(11, K_PCG_A);
-      st_pcg_b<Real>(B, Mn, cta, ncta, sm, flag);
-      PHX_SYNC(12, K_PCG_B);
+    st_vecop(B, Mn, cta, P, sm, flag);
+    PHX_SYNC(P, 2, K_VECOP);
+    st_elem_eg(B, Mt, cta, P, sm, flag);
+    PHX_SYNC(P, 3, K_ELEM_EG);
+    st_gather(B, Mn, cta, P, sm, flag);
+    PHX_SYNC(P, 4, K_GATHER);
+    st_vecop(B, Mn, cta, P, sm, flag);
+    PHX_SYNC(P, 5, K_VECOP);
+    st_elem_hess<Real>(B, Mt, cta, P, sm, flag, smraw);
+    PHX_SYNC(P, 6, K_ELEM_HESS);
+    st_assemble<Real>(B, Ml, cta, P, sm, flag);
+    PHX_SYNC(P, 7, K_ASSEMBLE);
+    st_jacobi<Real>(B, Mn, cta, P, sm, flag);
+    PHX_SYNC(P, 8, K_JACOBI);
+    st_linsetup(B, Mn, cta, P, sm, flag);
+    PHX_SYNC(P, 9, K_LINSETUP);
+    st_resid<Real>(B, Mn, cta, P, sm, flag);
+    PHX_SYNC(P, 10, K_RESID);
+    if (cta < Pp) {
+      // the PCG block only needs the CTAs that cover the node tiles
+      for (int k = 0; k < A.pcg_chunk; ++k) {
+        st_pcg_a<Real>(B, Mn, cta, Pp, sm, flag);
+        PHX_SYNC_PCG(Pp, 11, K_PCG_A);
+        st_pcg_b<Real>(B, Mn, cta, Pp, sm, flag);
+        PHX_SYNC_PCG(Pp, 12, K_PCG_B);
+      }
     }
-    st_accum<Real>(B, Mn, cta, ncta, sm, flag);
-    PHX_SYNC(13, K_ACCUM);
-    st_resid<Real>(B, Mn, cta, ncta, sm, flag);
-    PHX_SYNC(14, K_RESID);
-    st_vecop(B, Mn, cta, ncta, sm, flag);
-    PHX_SYNC(15, K_VECOP);
-    st_elem_eg(B, Mt, cta, ncta, sm, flag);
-    PHX_SYNC(16, K_ELEM_EG);
-    st_gather(B, Mn, cta, ncta, sm, flag);
-    PHX_SYNC(17, K_GATHER);
+    PHX_SYNC(P, 18, K_CONTROL);
+    st_accum<Real>(B, Mn, cta, P, sm, flag);
+    PHX_SYNC(P, 13, K_ACCUM);
+    st_resid<Real>(B, Mn, cta, P, sm, flag);
+    PHX_SYNC(P, 14, K_RESID);
+    st_vecop(B, Mn, cta, P, sm, flag);
+    PHX_SYNC(P, 15, K_VECOP);
+    st_elem_eg(B, Mt, cta, P, sm, flag);
+    PHX_SYNC(P, 16, K_ELEM_EG);
+    st_gather(B, Mn, cta, P, sm, flag);
+    PHX_SYNC(P, 17, K_GATHER);
   }
 #undef PHX_SYNC
+#undef PHX_SYNC_PCG
   if (cta == 0) compact(B, A);
+}
+
+
+// ---------------------------------------------------------------------------
+// cluster PCG: one instance per thread-block cluster
+// ---------------------------------------------------------------------------
+// For instances up to kClusterMaxNodes nodes, the PCG iterations of a linear solve run
+// inside one cluster of kCl CTAs: rows are split into contiguous chunk ranges, the two
+// global reductions of an iteration go through distributed shared memory (every CTA
+// sums the kCl partials in rank order, so all CTAs take the same decisions), and the
+// iteration boundaries are hardware cluster barriers (barrier.cluster with
+// release/acquire).  Vectors stay in global memory (L2-resident for these sizes);
+// the rows another CTA wrote are read with ld.global.cg.
+__device__ __forceinline__ unsigned cl_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ unsigned cl_id() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ unsigned cl_count() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cl_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ double cl_ld(const double* local, unsigned rank) {
+  unsigned src = (unsigned)__cvta_generic_to_shared(local), dst;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(dst) : "r"(src), "r"(rank));
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(dst) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void ld4cg(const double* p, int64_t v, double (&o)[3]) {
+  const double2* q = reinterpret_cast<const double2*>(p) + 2 * v;
+  double2 a = __ldcg(q), b = __ldcg(q + 1);
+  o[0] = a.x; o[1] = a.y; o[2] = b.x;
+}
+__device__ __forceinline__ void ld4cg(const float* p, int64_t v, float (&o)[3]) {
+  float4 a = __ldcg(reinterpret_cast<const float4*>(p) + v);
+  o[0] = a.x; o[1] = a.y; o[2] = a.z;
+}
+
+// Sums K values over the CTA (256 threads) into out[] of thread 0.
+template <int K>
+__device__ __forceinline__ void cta_sum256(double (&v)[K], double (*ws)[4]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], off);
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < K; ++k) ws[warp][k] = v[k];
+  __syncthreads();
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      double s = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += ws[w][k];
+      v[k] = s;
+    }
+}
+
+template <typename Real>
+__global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(256) k_pcg_cluster(BatchDev B, const int32_t* list,
+                                                                                  int count) {
+  __shared__ double red[2][4];    // this CTA's partials, double-buffered by iteration
+  __shared__ double ws[8][4];
+  __shared__ double tot[4];
+  const unsigned rank = cl_rank();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int j = (int)cl_id(); j < count; j += (int)cl_count()) {
+    const int i = __ldg(list + j);
+    const InstDev& I = B.inst[i];
+    NState* st = I.st;
+    if (*(volatile int32_t*)&st->phase != PH_PCG) continue;  // uniform: state written before the launch
+    const int n = I.n, nch = I.nchunks;
+    const int c0 = (int)(((int64_t)nch * rank) / kCl), c1 = (int)(((int64_t)nch * (rank + 1)) / kCl);
+    const Real* H = PcgBufs<Real>::H(I);
+    const Real* z = PcgBufs<Real>::z(I);
+    Real* q = PcgBufs<Real>::q(I);
+    Real* e = PcgBufs<Real>::e(I);
+    Real* rv = PcgBufs<Real>::r(I);
+    Real* zw = PcgBufs<Real>::z(I);
+    const Real* Mi = PcgBufs<Real>::minv(I);
+    const Real sh = (Real)st->shift;
+    const double thr = st->thr_inner;
+    const int maxit = I.opts->ls_num_max_iters;
+    double rz = st->rz, beta = st->beta;
+    int parity = st->pcg_parity, iter = st->pcg_iter, done_iters = 0, status = LIN_RUNNING, buf = 0;
+    double rr = st->rr, pq = 0.0;
+    while (true) {
+      // q = (H + shift I) p, p = z + beta p_prev formed per column; p written for own rows
+      const Real* pold = parity ? PcgBufs<Real>::pb(I) : PcgBufs<Real>::pa(I);
+      Real* pnew = parity ? PcgBufs<Real>::pa(I) : PcgBufs<Real>::pb(I);
+      const Real bt = (Real)beta;
+      double pa_[1] = {0.0};
+      for (int c = c0 + warp; c < c1; c += nwarps) {
+        const int v = c * 32 + lane;
+        if (v >= n) continue;
+        Real acc[3];
+        sell_row<Real, Real>(I, H, v,
+                             [&](int col, Real (&xc)[3]) {
+                               Real zc[3], pc[3];
+                               ld4cg(z, col, zc);
+                               ld4cg(pold, col, pc);
+                               for (int a = 0; a < 3; ++a) xc[a] = zc[a] + bt * pc[a];
+                             },
+                             acc);
+        Real zv[3], pv[3];
+        ld4cg(z, v, zv);
+        ld4cg(pold, v, pv);
+        for (int a = 0; a < 3; ++a) {
+          pv[a] = zv[a] + bt * pv[a];
+          acc[a] += sh * pv[a];
+        }
+        st4(pnew, v, pv);
+        st4(q, v, acc);
+        pa_[0] += (double)pv[0] * acc[0] + (double)pv[1] * acc[1] + (double)pv[2] * acc[2];
+      }
+      cta_sum256<1>(pa_, ws);
+      if (threadIdx.x == 0) red[buf][0] = pa_[0];
+      cl_sync();
+      if (threadIdx.x == 0) {
+        double s = 0;
+        for (unsigned r = 0; r < kCl; ++r) s += cl_ld(&red[buf][0], r);
+        tot[0] = s;
+      }
+      __syncthreads();
+      pq = tot[0];
+      if (!(pq > 0.0)) {
+        status = LIN_BREAKDOWN;
+        break;
+      }
+      const Real alpha = (Real)(rz / pq);
+      // e += alpha p, r -= alpha q, z = Minv r
+      double pb_[2] = {0.0, 0.0};
+      for (int c = c0 + warp; c < c1; c += nwarps) {
+        const int v = c * 32 + lane;
+        if (v >= n) continue;
+        Real pv[3], qv[3], ev[3], rr_[3], zz[3];
+        ld4(pnew, v, pv);
+        ld4(q, v, qv);
+        ld4(e, v, ev);
+        ld4(rv, v, rr_);
+        for (int a = 0; a < 3; ++a) {
+          ev[a] += alpha * pv[a];
+          rr_[a] -= alpha * qv[a];
+        }
+        for (int a = 0; a < 3; ++a)
+          zz[a] = Mi[(size_t)(3 * a) * n + v] * rr_[0] + Mi[(size_t)(3 * a + 1) * n + v] * rr_[1] +
+                  Mi[(size_t)(3 * a + 2) * n + v] * rr_[2];
+        st4(e, v, ev);
+        st4(rv, v, rr_);
+        st4(zw, v, zz);
+        pb_[0] += (double)rr_[0] * rr_[0] + (double)rr_[1] * rr_[1] + (double)rr_[2] * rr_[2];
+        pb_[1] += (double)rr_[0] * zz[0] + (double)rr_[1] * zz[1] + (double)rr_[2] * zz[2];
+      }
+      cta_sum256<2>(pb_, ws);
+      if (threadIdx.x == 0) {
+        red[buf][1] = pb_[0];
+        red[buf][2] = pb_[1];
+      }
+      cl_sync();
+      if (threadIdx.x == 0) {
+        double s1 = 0, s2 = 0;
+        for (unsigned r = 0; r < kCl; ++r) {
+          s1 += cl_ld(&red[buf][1], r);
+          s2 += cl_ld(&red[buf][2], r);
+        }
+        tot[1] = s1;
+        tot[2] = s2;
+      }
+      __syncthreads();
+      rr = tot[1];
+      const double rzn = tot[2];
+      ++iter;
+      ++done_iters;
+      buf ^= 1;
+      if (rr < thr) {
+        status = LIN_CONVERGED;
+        break;
+      }
+      if (iter >= maxit) {
+        status = LIN_MAXITER;
+        break;
+      }
+      beta = rzn / rz;
+      rz = rzn;
+      parity ^= 1;
+    }
+    if (rank == 0 && threadIdx.x == 0) {
+      st->pcg_iter = iter;
+      st->pcg_total += done_iters;
+      st->rr = rr;
+      st->pq = pq;
+      st->rz = rz;
+      st->beta = beta;
+      st->pcg_parity = parity;
+      st->lin_status = status;
+      st->phase = (status == LIN_BREAKDOWN) ? PH_LIN_DONE : PH_ACCUM;
+      if (B.algo_total) {
+        atomicAdd(B.algo_total + K_PCG_A, I.algo[K_PCG_A] * done_iters);
+        atomicAdd(B.algo_total + K_PCG_B, I.algo[K_PCG_B] * done_iters);
+      }
+      advance(B, i);
+    }
+    cl_sync();  // partial buffers are reused by the next instance
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1284,6 +1550,14 @@ int engine_grid(bool fp64, int num_sms) {
                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_engine<float>, kTile, hess_smem<float>());
   if (e != cudaSuccess || nb < 1) return 0;
   return nb * num_sms;
+}
+
+cudaError_t launch_pcg_cluster(bool fp64, cudaStream_t s, const BatchDev& B, const int32_t* list, int count) {
+  if (count <= 0) return cudaSuccess;
+  const int grid = count * kCl;
+  if (fp64) k_pcg_cluster<double><<<grid, 256, 0, s>>>(B, list, count);
+  else k_pcg_cluster<float><<<grid, 256, 0, s>>>(B, list, count);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_engine(bool fp64, int grid, cudaStream_t s, const BatchDev& B, const EngineArgs& A) {
@@ -1345,6 +1619,7 @@ const char* kernel_name(KernelId id) {
     case K_PCG_A: return "spmv";
     case K_PCG_B: return "pcg_update";
     case K_ACCUM: return "accum";
+    case K_PCG_CLUSTER: return "pcg_cluster";
     default: return "?";
   }
 }

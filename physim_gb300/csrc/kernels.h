@@ -20,9 +20,10 @@ enum KernelId : int {
   K_PCG_A,
   K_PCG_B,
   K_ACCUM,
+  K_PCG_CLUSTER,
   K_COUNT
 };
-static_assert(K_COUNT <= 12, "InstDev::algo holds 12 kernel kinds");
+static_assert(K_COUNT <= 16, "InstDev::algo holds 16 kernel kinds");
 
 // Grid barrier state of the engine (device memory, zeroed before a launch).
 struct GridBar {
@@ -32,8 +33,9 @@ struct GridBar {
 };
 
 struct EngineArgs {
-  GridBar* bar;
-  int32_t* act;                   // [1 + cap + 3 (cap + 1)]: count, ids, tet/node/lob tile prefixes
+  GridBar* bar;                   // [2]: round-wide barrier, PCG-block barrier
+  int32_t* act;                   // [4 + cap + 3 (cap + 1)]: count, CTAs in the round, CTAs in the
+                                  // PCG block, pad; ids; tet/node/lob tile prefixes
   unsigned long long* stage_ns;   // [32]: ns per stage kind, then executions per kind; or null
   int cap;
   int rounds;
@@ -43,6 +45,8 @@ struct EngineArgs {
 cudaError_t setup_kernel_attributes();
 int engine_grid(bool fp64, int num_sms);
 cudaError_t launch_engine(bool fp64, int grid, cudaStream_t s, const BatchDev& B, const EngineArgs& A);
+// PCG of every listed instance that is in PH_PCG, one cluster per instance
+cudaError_t launch_pcg_cluster(bool fp64, cudaStream_t s, const BatchDev& B, const int32_t* list, int count);
 void launch(KernelId id, int grid, cudaStream_t s, const BatchDev& B, bool fp64);
 const char* kernel_name(KernelId id);
 

@@ -27,6 +27,8 @@ namespace phx {
 constexpr int kTile = 128;       // tets / nodes / lower blocks per tile
 constexpr int kChunk = 32;       // SELL chunk height (one warp)
 constexpr int kPartials = 5;     // doubles reduced per tile (at most)
+constexpr int kCl = 8;           // CTAs per cluster of the cluster PCG
+constexpr int kClusterMaxNodes = 40000;  // instances up to this size solve their PCG in one cluster
 
 // Phases of the per-instance Newton state machine (see control in kernels.cu).
 enum Phase : int32_t {
@@ -98,6 +100,7 @@ constexpr int kLogCap = 256;                   // Newton iterations kept in the 
 struct InstDev {
   int32_t n, m, nlo, nchunks;
   int64_t nslots;
+  int32_t pcg_cluster, pad_i;  // 1: the instance's PCG runs in k_pcg_cluster
   // mesh + rest data
   const int32_t* tets;        // [m][4]
   const double* rest64;       // [m][12]
@@ -138,7 +141,7 @@ struct InstDev {
   NState* st;
   const DevOpts* opts;
   double* log;                // [kLogCap][4]: obj, opt, bisections, step per Newton iteration
-  double algo[12];            // algorithmic bytes of one launch of each kernel kind on this instance
+  double algo[16];            // algorithmic bytes of one launch of each kernel kind on this instance
 };
 
 // Tile prefix arrays of the active batch (device memory).
@@ -149,7 +152,7 @@ struct BatchDev {
   const int32_t* pre_lob;
   InstDev* inst;              // [num]
   int32_t* flags;             // [8 + num]: [0] active count; [8 + i] phase of instance i
-  double* algo_total;         // [12] algorithmic bytes summed per kernel kind, or null
+  double* algo_total;         // [16] algorithmic bytes summed per kernel kind, or null
 };
 
 PHX_HD inline int64_t sell_addr(int64_t s, int e) { return (s >> 5) * 288 + (int64_t)e * 32 + (s & 31); }
