@@ -215,6 +215,29 @@ int phx_timer_elapsed(phx_context ctx, int32_t slot_a, int32_t slot_b, double* m
 /* Launch count of the library's own kernels since creation (or the last reset). */
 int64_t phx_kernel_launches(phx_context ctx);
 
+/* ---- element Hessian + assembly without allocation -----------------------
+ * No counterpart in the reference.  For callers that cannot allocate device memory
+ * (an engine that owns all GPU memory in its own pool, a runtime that forbids
+ * cudaMalloc while frames run): every argument is a caller-owned device pointer and the
+ * only scratch is a fixed static device array of PHX_NOALLOC_MAX_TETS * 90 doubles
+ * (about 23.6 MB, held by every GPU that loads the library until exit).  Computes the
+ * model Hessian (no fixed DoFs applied) as the lower 3x3 node blocks of the Eigen
+ * pattern, in the same element order as phx_hessian:
+ *   tets [4m] int32, rest [12m] (column-major Dm^-1, rest volume, lambda, mu per tet),
+ *   model [m] (NULL = CoNH), x, X0 [3n] positions and rest positions,
+ *   seg_ptr [nlo+1], seg_c [10m]: for each lower block, its (tet*10 + local pair)
+ *   contributions in element order (the inverted scatter map of phx_scatter_map),
+ *   blocks [9*nlo] out, row-major per block: entry (a, b) = H(3R + a, 3C + b).
+ * Kernels are queued on `stream` (a cudaStream_t; NULL = legacy default stream) and the
+ * call returns without waiting.  The scratch's device address is looked up on the first
+ * call on each device (with that device current), so that call must precede any stream
+ * capture.  Calls that overlap on the GPU race on the shared scratch.  More than
+ * PHX_NOALLOC_MAX_TETS tets: PHX_EINVAL. */
+#define PHX_NOALLOC_MAX_TETS 32768
+int phx_hessian_blocks_noalloc(int32_t num_nodes, int32_t num_tets, int32_t num_lower_blocks, const int32_t* tets,
+                               const double* rest, const uint8_t* model, const double* x, const double* X0,
+                               const int32_t* seg_ptr, const int32_t* seg_c, double* blocks, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

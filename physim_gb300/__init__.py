@@ -34,6 +34,7 @@ EXPORTS = [
     "phx_dynamic_step", "phx_batch_solve", "phx_batch_dynamic_step", "phx_server_create", "phx_server_destroy",
     "phx_server_submit", "phx_server_progress", "phx_server_poll", "phx_profile_enable", "phx_profile_read",
     "phx_profile_reset", "phx_profile_bytes", "phx_kernel_launches", "phx_timer_mark", "phx_timer_elapsed",
+    "phx_hessian_blocks_noalloc",
 ]
 
 
@@ -125,6 +126,7 @@ def lib():
         "phx_kernel_launches": ([vp], i64),
         "phx_timer_mark": ([vp, i32], C.c_int),
         "phx_timer_elapsed": ([vp, i32, i32, C.POINTER(dbl)], C.c_int),
+        "phx_hessian_blocks_noalloc": ([i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "../../include/phx.h"
+#include "errors.h"
 #include "kernels.h"
 #include "newton_control.h"
 #include "pattern.h"
@@ -35,6 +36,12 @@ int set_err(int code, const std::string& msg) {
   g_err = msg;
   return code;
 }
+
+}  // namespace
+
+int phx::set_last_error(int code, const std::string& msg) { return set_err(code, msg); }
+
+namespace {
 
 #define CU(call)                                                                              \
   do {                                                                                        \
