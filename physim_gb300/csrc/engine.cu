@@ -242,7 +242,7 @@ int ensure_batch_cap(phx_context ctx, int num) {
   if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
   ctx->d_inst = nullptr; ctx->d_pre = nullptr; ctx->d_flags = nullptr; ctx->h_flags = nullptr;
   CU(cudaMalloc(&ctx->d_inst, sizeof(InstDev) * cap));
-  CU(cudaMalloc(&ctx->d_pre, sizeof(int32_t) * (3 * (cap + 1) + 1)));
+  CU(cudaMalloc(&ctx->d_pre, sizeof(int32_t) * (4 * (cap + 1) + 1)));
   CU(cudaMalloc(&ctx->d_flags, sizeof(int32_t) * (8 + cap)));
   CU(cudaMallocHost(&ctx->h_flags, sizeof(int32_t) * (8 + cap)));
   ctx->cap = cap;
@@ -258,23 +258,26 @@ int set_batch(phx_context ctx, const std::vector<phx_instance>& list, BatchDev& 
   TRY(ensure_batch_cap(ctx, std::max(num, 1)));
   std::vector<InstDev> d(num);
   std::vector<int32_t>& pre = ctx->h_pre;
-  pre.assign(3 * (ctx->cap + 1) + 1, 0);
+  pre.assign(4 * (ctx->cap + 1) + 1, 0);
   int32_t* pt = pre.data();
   int32_t* pn = pt + (ctx->cap + 1);
   int32_t* pl = pn + (ctx->cap + 1);
+  int32_t* pp = pl + (ctx->cap + 1);
   for (int i = 0; i < num; ++i) {
     d[i] = list[i]->dev;
     pt[i + 1] = pt[i] + tiles(list[i]->dev.m);
     pn[i + 1] = pn[i] + tiles(list[i]->dev.n);
     pl[i + 1] = pl[i] + tiles(list[i]->dev.nlo);
+    pp[i + 1] = pp[i] + (list[i]->dev.nchunks + list[i]->dev.cpt - 1) / list[i]->dev.cpt;
   }
-  pre[3 * (ctx->cap + 1)] = num;
+  pre[4 * (ctx->cap + 1)] = num;
   if (num) CU(cudaMemcpyAsync(ctx->d_inst, d.data(), sizeof(InstDev) * num, cudaMemcpyHostToDevice, ctx->stream));
   CU(cudaMemcpyAsync(ctx->d_pre, pre.data(), sizeof(int32_t) * pre.size(), cudaMemcpyHostToDevice, ctx->stream));
-  B.num = ctx->d_pre + 3 * (ctx->cap + 1);
+  B.num = ctx->d_pre + 4 * (ctx->cap + 1);
   B.pre_tet = ctx->d_pre;
   B.pre_node = ctx->d_pre + (ctx->cap + 1);
   B.pre_lob = ctx->d_pre + 2 * (ctx->cap + 1);
+  B.pre_pcg = ctx->d_pre + 3 * (ctx->cap + 1);
   B.inst = ctx->d_inst;
   B.flags = ctx->d_flags;
   B.algo_total = ctx->profiling ? ctx->d_algo : nullptr;
@@ -425,7 +428,7 @@ int ensure_engine(phx_context ctx) {
   if (ctx->act_cap < ctx->cap) {
     if (ctx->d_act) cudaFree(ctx->d_act);
     ctx->d_act = nullptr;
-    CU(cudaMalloc(&ctx->d_act, sizeof(int32_t) * (4 + ctx->cap + 3 * (ctx->cap + 1))));
+    CU(cudaMalloc(&ctx->d_act, sizeof(int32_t) * (4 + ctx->cap + 4 * (ctx->cap + 1))));
     ctx->act_cap = ctx->cap;
   }
   if (ctx->profiling && !ctx->d_stage) {
@@ -682,6 +685,9 @@ int phx_instance_create(phx_context ctx, const phx_mesh* mesh, phx_instance* out
   HostPattern& hp = inst->hp;
   InstDev& D = inst->dev;
   D.n = hp.n; D.m = hp.m; D.nlo = hp.nlo; D.nchunks = hp.nchunks; D.nslots = hp.nslots;
+  // PCG tiles: one SELL chunk for small instances (more SMs per instance, short per-tile
+  // latency), four for large ones (fewer partial sums per reduction)
+  D.cpt = hp.nchunks > 2048 ? 4 : 1;
   auto fail = [&](int rc) { phx_instance_destroy(inst); return rc; };
   cudaError_t e0 = cudaSuccess;
   int rc = PHX_OK;
@@ -721,7 +727,7 @@ int phx_instance_create(phx_context ctx, const phx_mesh* mesh, phx_instance* out
     if ((rc = arena_alloc(inst, pv, n4, true))) return fail(rc);
   if ((rc = arena_alloc(inst, &D.Eloc, (size_t)hp.m))) return fail(rc);
   if ((rc = arena_alloc(inst, &D.Gloc, 12 * (size_t)hp.m))) return fail(rc);
-  size_t maxt = std::max({tiles(hp.m), tiles(hp.n), tiles(hp.nlo)});
+  size_t maxt = std::max({tiles(hp.m), hp.nchunks, tiles(hp.nlo)});
   if ((rc = arena_alloc(inst, &D.partials, maxt * kPartials))) return fail(rc);
   if ((rc = arena_alloc(inst, &D.counter, 1, true))) return fail(rc);
   if ((rc = arena_alloc(inst, &D.log, 4 * (size_t)kLogCap, true))) return fail(rc);

@@ -27,6 +27,7 @@
 //                 on the FP32 path, FP64 residual refinement sweeps.
 #include <cfloat>
 #include <cstdint>
+#include <type_traits>
 
 #include "element.cuh"
 #include "kernels.h"
@@ -38,6 +39,8 @@ namespace phx {
 // small helpers
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ int tiles_of(int count) { return (count + kTile - 1) / kTile; }
+// PCG tiles: I.cpt SELL chunks (32 rows each) per tile
+__device__ __forceinline__ int pcg_tiles(const InstDev& I) { return (I.nchunks + I.cpt - 1) / I.cpt; }
 
 template <int K>
 __device__ __forceinline__ void block_sum(double (&v)[K], double* sm) {
@@ -206,7 +209,7 @@ __device__ __forceinline__ TileMap full_map(const BatchDev& B, const int32_t* pr
 // Runs the state machine of instance i up to its next device phase (called by the one
 // thread that finalises a stage for the instance) and publishes the phase.
 __device__ void advance(const BatchDev& B, int i) {
-  const InstDev& I = B.inst[i];
+  const InstDev I = B.inst[i];  // local copy: fields stay in registers across stores
   NState s = *I.st;
   ctl_advance(s, *I.opts);
   if (s.log_pending) {
@@ -231,7 +234,7 @@ __device__ __forceinline__ void st_vecop(const BatchDev& B, const TileMap& M, in
   for (int t = cta; t < total; t += ncta) {
     int i, lt;
     map_tile(M, t, i, lt);
-    const InstDev& I = B.inst[i];
+    const InstDev I = B.inst[i];  // local copy: fields stay in registers across stores
     NState* st = I.st;
     if (st->phase != PH_VEC) continue;
     const int ops = st->vecop;
@@ -362,7 +365,7 @@ __device__ __forceinline__ void st_elem_eg(const BatchDev& B, const TileMap& M, 
   for (int t = cta; t < total; t += ncta) {
     int i, lt;
     map_tile(M, t, i, lt);
-    const InstDev& I = B.inst[i];
+    const InstDev I = B.inst[i];  // local copy: fields stay in registers across stores
     NState* st = I.st;
     if (st->phase != PH_EVAL) continue;
     const int e = lt * kTile + threadIdx.x;
@@ -423,7 +426,7 @@ __device__ __forceinline__ void st_gather(const BatchDev& B, const TileMap& M, i
   for (int t = cta; t < total; t += ncta) {
     int i, lt;
     map_tile(M, t, i, lt);
-    const InstDev& I = B.inst[i];
+    const InstDev I = B.inst[i];  // local copy: fields stay in registers across stores
     NState* st = I.st;
     if (st->phase != PH_EVAL) continue;
     const int v = lt * kTile + threadIdx.x;
@@ -501,7 +504,7 @@ __device__ __forceinline__ void st_elem_hess(const BatchDev& B, const TileMap& M
   for (int t = cta; t < total; t += ncta) {
     int i, lt;
     map_tile(M, t, i, lt);
-    const InstDev& I = B.inst[i];
+    const InstDev I = B.inst[i];  // local copy: fields stay in registers across stores
     if (I.st->phase != PH_HESS) continue;
     const int e0 = lt * kTile;
     const int cnt = min(kTile, I.m - e0);
@@ -533,7 +536,7 @@ __device__ __forceinline__ void st_assemble(const BatchDev& B, const TileMap& M,
   for (int t = cta; t < total; t += ncta) {
     int i, lt;
     map_tile(M, t, i, lt);
-    const InstDev& I = B.inst[i];
+    const InstDev I = B.inst[i];  // local copy: fields stay in registers across stores
     NState* st = I.st;
     if (st->phase != PH_HESS) continue;
     const Real* Hloc = PcgBufs<Real>::Hloc(I);
@@ -581,7 +584,7 @@ __device__ __forceinline__ void st_jacobi(const BatchDev& B, const TileMap& M, i
   for (int t = cta; t < total; t += ncta) {
     int i, lt;
     map_tile(M, t, i, lt);
-    const InstDev& I = B.inst[i];
+    const InstDev I = B.inst[i];  // local copy: fields stay in registers across stores
     NState* st = I.st;
     if (st->phase != PH_HESS && st->phase != PH_JACOBI) continue;
     const int v = lt * kTile + threadIdx.x;
@@ -637,7 +640,7 @@ __device__ __forceinline__ void st_linsetup(const BatchDev& B, const TileMap& M,
   for (int t = cta; t < total; t += ncta) {
     int i, lt;
     map_tile(M, t, i, lt);
-    const InstDev& I = B.inst[i];
+    const InstDev I = B.inst[i];  // local copy: fields stay in registers across stores
     NState* st = I.st;
     if (st->phase != PH_LINSETUP) continue;
     const int v = lt * kTile + threadIdx.x;
@@ -712,6 +715,44 @@ __device__ __forceinline__ void sell_row(const InstDev& I, const Real* H, int v,
   }
 }
 
+// L lanes per row (L = 1, 2 or 4; lanes L*r .. L*r+L-1 of the calling warp share row v):
+// lane `sub` takes slots sub, sub+L, ..., so with L = 4 a row costs about two dependent
+// memory round trips; the partial sums are combined with xor-shuffles and every lane of
+// the group ends with the full row.  Used where a few rows per instance must finish fast.
+template <int L, typename Real, typename Acc, typename GetX>
+__device__ __forceinline__ void sell_row_lanes(const InstDev& I, const Real* H, int v, int sub, bool valid, GetX getx,
+                                               Acc (&acc)[3]) {
+  acc[0] = acc[1] = acc[2] = (Acc)0;
+  if (valid) {
+    const int c = v >> 5, lane = v & 31;
+    const int s0 = __ldg(I.chunk_off + c);
+    const int len = (__ldg(I.chunk_off + c + 1) - s0) >> 5;
+#pragma unroll(L == 1 ? 4 : 1)
+    for (int k = sub; k < len; k += L) {
+      const int64_t s = (int64_t)s0 + k * 32 + lane;
+      const int col = __ldg(I.slot_col + s);
+      const Real* hp = H + (s >> 5) * 288 + (s & 31);
+      Acc h[9];
+#pragma unroll
+      for (int q = 0; q < 9; ++q) h[q] = (Acc)hp[q * 32];
+      Acc xc[3];
+      getx(col, xc);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) acc[a] += h[3 * a] * xc[0] + h[3 * a + 1] * xc[1] + h[3 * a + 2] * xc[2];
+    }
+  }
+#pragma unroll
+  for (int off = 1; off < L; off <<= 1)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) acc[a] += __shfl_xor_sync(0xffffffffu, acc[a], off);
+}
+
+template <typename Real, typename Acc, typename GetX>
+__device__ __forceinline__ void sell_row_quad(const InstDev& I, const Real* H, int v, int sub, bool valid, GetX getx,
+                                              Acc (&acc)[3]) {
+  sell_row_lanes<4, Real, Acc>(I, H, v, sub, valid, getx, acc);
+}
+
 // r64 = b - (H + shift I) dx in FP64 (FP32 values promoted); starts an inner PCG on r
 template <typename Real>
 __device__ __forceinline__ void st_resid(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag) {
@@ -719,7 +760,7 @@ __device__ __forceinline__ void st_resid(const BatchDev& B, const TileMap& M, in
   for (int t = cta; t < total; t += ncta) {
     int i, lt;
     map_tile(M, t, i, lt);
-    const InstDev& I = B.inst[i];
+    const InstDev I = B.inst[i];  // local copy: fields stay in registers across stores
     NState* st = I.st;
     if (st->phase != PH_RESID) continue;
     const int v = lt * kTile + threadIdx.x;
@@ -759,8 +800,9 @@ __device__ __forceinline__ void st_resid(const BatchDev& B, const TileMap& M, in
       st->b_dot_dx = tot[1];
       st->dx_norm = sqrt(tot[2]);
       const bool conv = tot[0] < st->thr_final;
-      if (conv || st->sweeps >= I.opts->max_refine_sweeps) {
-        if (conv) st->lin_status = LIN_CONVERGED;
+      if (conv || st->sweeps >= I.opts->max_refine_sweeps || st->lin_status == LIN_TRUNCATED) {
+        if (st->lin_status == LIN_TRUNCATED) {
+        } else if (conv) st->lin_status = LIN_CONVERGED;
         else if (st->lin_status == LIN_RUNNING) st->lin_status = LIN_MAXITER;
         st->phase = PH_LIN_DONE;
       } else {
@@ -771,6 +813,7 @@ __device__ __forceinline__ void st_resid(const BatchDev& B, const TileMap& M, in
         st->pcg_iter = 0;
         st->pcg_parity = 0;
         st->beta = 0.0;
+        st->truncate = 0;
         st->lin_status = LIN_RUNNING;
         st->phase = PH_PCG;
       }
@@ -794,45 +837,58 @@ __device__ __forceinline__ void st_pcg_a(const BatchDev& B, const TileMap& M, in
   for (int t = cta; t < total; t += ncta) {
     int i, lt;
     map_tile(M, t, i, lt);
-    const InstDev& I = B.inst[i];
+    const InstDev I = B.inst[i];  // local copy: fields stay in registers across stores
     NState* st = I.st;
     if (st->phase != PH_PCG || I.pcg_cluster) continue;
-    const int v = lt * kTile + threadIdx.x;
     double p[1] = {0.0};
-    if (v < I.n) {
+    {
       const int par = st->pcg_parity;
       const Real* pold = par ? PcgBufs<Real>::pb(I) : PcgBufs<Real>::pa(I);
       Real* pnew = par ? PcgBufs<Real>::pa(I) : PcgBufs<Real>::pb(I);
       const Real* z = PcgBufs<Real>::z(I);
       const Real beta = (Real)st->beta, sh = (Real)st->shift;
-      Real acc[3];
-      sell_row<Real, Real>(I, PcgBufs<Real>::H(I), v,
-                           [&](int col, Real (&xc)[3]) {
-                             Real zc[3], pc[3];
-                             ld4(z, col, zc);
-                             ld4(pold, col, pc);
-                             for (int a = 0; a < 3; ++a) xc[a] = zc[a] + beta * pc[a];
-                           },
-                           acc);
-      Real zv[3], pv[3];
-      ld4(z, v, zv);
-      ld4(pold, v, pv);
-      for (int a = 0; a < 3; ++a) {
-        pv[a] = zv[a] + beta * pv[a];
-        acc[a] += sh * pv[a];
+      const int sub = threadIdx.x & 3, row = threadIdx.x >> 2;  // 32 rows x 4 lanes per pass
+      const int ch0 = lt * I.cpt, ch1 = min(ch0 + I.cpt, I.nchunks);
+      for (int ch = ch0; ch < ch1; ++ch) {
+        const int v = ch * 32 + row;
+        const bool valid = v < I.n;
+        Real acc[3];
+        sell_row_quad<Real, Real>(I, PcgBufs<Real>::H(I), v, sub, valid,
+                                  [&](int col, Real (&xc)[3]) {
+                                    Real zc[3], pc[3];
+                                    ld4(z, col, zc);
+                                    ld4(pold, col, pc);
+                                    for (int a = 0; a < 3; ++a) xc[a] = zc[a] + beta * pc[a];
+                                  },
+                                  acc);
+        if (valid && sub == 0) {
+          Real zv[3], pv[3];
+          ld4(z, v, zv);
+          ld4(pold, v, pv);
+          for (int a = 0; a < 3; ++a) {
+            pv[a] = zv[a] + beta * pv[a];
+            acc[a] += sh * pv[a];
+          }
+          st4(pnew, v, pv);
+          st4(PcgBufs<Real>::q(I), v, acc);
+          p[0] += (double)pv[0] * acc[0] + (double)pv[1] * acc[1] + (double)pv[2] * acc[2];
+        }
       }
-      st4(pnew, v, pv);
-      st4(PcgBufs<Real>::q(I), v, acc);
-      p[0] = (double)pv[0] * acc[0] + (double)pv[1] * acc[1] + (double)pv[2] * acc[2];
     }
     double tot[1];
-    if (tile_done<1>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
+    if (tile_done<1>(I, lt, pcg_tiles(I), p, tot, sm, &flag) && threadIdx.x == 0) {
       count_bytes(B, I, K_PCG_A);
       st->pq = tot[0];
       if (!(tot[0] > 0.0)) {  // not positive definite along p (or non-finite)
-        st->lin_status = LIN_BREAKDOWN;
-        st->phase = PH_LIN_DONE;
-        advance(B, i);
+        if (I.opts->precision != 0 && tot[0] < 0.0 && st->pcg_iter == 0) {
+          // truncated CG, first direction: step along p with |p.q| and stop
+          st->alpha = st->rz / -tot[0];
+          st->truncate = 1;
+        } else {
+          st->lin_status = (I.opts->precision != 0 && tot[0] < 0.0) ? LIN_TRUNCATED : LIN_BREAKDOWN;
+          st->phase = (st->lin_status == LIN_TRUNCATED) ? PH_ACCUM : PH_LIN_DONE;
+          advance(B, i);
+        }
       } else {
         st->alpha = st->rz / tot[0];
       }
@@ -844,7 +900,7 @@ template <typename Real>
 __global__ void __launch_bounds__(kTile) k_pcg_a(BatchDev B) {
   __shared__ double sm[32 * 5];
   __shared__ int flag;
-  st_pcg_a<Real>(B, full_map(B, B.pre_node), blockIdx.x, gridDim.x, sm, flag);
+  st_pcg_a<Real>(B, full_map(B, B.pre_pcg), blockIdx.x, gridDim.x, sm, flag);
 }
 
 // PCG step 2: e += alpha p, r -= alpha q, z = Minv r; convergence ||r||^2 < thr (Eigen's rule)
@@ -854,12 +910,12 @@ __device__ __forceinline__ void st_pcg_b(const BatchDev& B, const TileMap& M, in
   for (int t = cta; t < total; t += ncta) {
     int i, lt;
     map_tile(M, t, i, lt);
-    const InstDev& I = B.inst[i];
+    const InstDev I = B.inst[i];  // local copy: fields stay in registers across stores
     NState* st = I.st;
     if (st->phase != PH_PCG || I.pcg_cluster) continue;
-    const int v = lt * kTile + threadIdx.x;
+    const int v = lt * I.cpt * 32 + threadIdx.x;  // one row per thread over the tile's chunks
     double p[2] = {0.0, 0.0};
-    if (v < I.n) {
+    if ((int)threadIdx.x < I.cpt * 32 && v < I.n) {
       const Real alpha = (Real)st->alpha;
       const Real* pc = st->pcg_parity ? PcgBufs<Real>::pa(I) : PcgBufs<Real>::pb(I);
       Real pv[3], qv[3], ev[3], rv[3], z[3];
@@ -882,12 +938,16 @@ __device__ __forceinline__ void st_pcg_b(const BatchDev& B, const TileMap& M, in
       p[1] = (double)rv[0] * z[0] + (double)rv[1] * z[1] + (double)rv[2] * z[2];
     }
     double tot[2];
-    if (tile_done<2>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
+    if (tile_done<2>(I, lt, pcg_tiles(I), p, tot, sm, &flag) && threadIdx.x == 0) {
       count_bytes(B, I, K_PCG_B);
       st->pcg_iter++;
       st->pcg_total++;
       st->rr = tot[0];
-      if (tot[0] < st->thr_inner) {
+      if (st->truncate) {
+        st->truncate = 0;
+        st->lin_status = LIN_TRUNCATED;
+        st->phase = PH_ACCUM;
+      } else if (tot[0] < st->thr_inner) {
         st->lin_status = LIN_CONVERGED;
         st->phase = PH_ACCUM;
       } else if (st->pcg_iter >= I.opts->ls_num_max_iters) {
@@ -907,7 +967,7 @@ template <typename Real>
 __global__ void __launch_bounds__(kTile) k_pcg_b(BatchDev B) {
   __shared__ double sm[32 * 5];
   __shared__ int flag;
-  st_pcg_b<Real>(B, full_map(B, B.pre_node), blockIdx.x, gridDim.x, sm, flag);
+  st_pcg_b<Real>(B, full_map(B, B.pre_pcg), blockIdx.x, gridDim.x, sm, flag);
 }
 
 // dx += e (FP64), then back to the FP64 residual
@@ -917,7 +977,7 @@ __device__ __forceinline__ void st_accum(const BatchDev& B, const TileMap& M, in
   for (int t = cta; t < total; t += ncta) {
     int i, lt;
     map_tile(M, t, i, lt);
-    const InstDev& I = B.inst[i];
+    const InstDev I = B.inst[i];  // local copy: fields stay in registers across stores
     NState* st = I.st;
     if (st->phase != PH_ACCUM) continue;
     const int v = lt * kTile + threadIdx.x;
@@ -1008,6 +1068,7 @@ __device__ __forceinline__ bool grid_sync(GridBar* gb, unsigned int nblocks, int
 
 // block-wide exclusive scan of 4 ints; returns totals in tot (all threads)
 __device__ __forceinline__ void block_scan4(int (&v)[4], int (&tot)[4], int* sm /* [32*4] */) {
+  // (four running sums at once; compact() runs two of these passes)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
   int inc[4];
 #pragma unroll
@@ -1063,7 +1124,9 @@ __device__ void compact(const BatchDev& B, const EngineArgs& A) {
   int* pt = ids + A.cap;
   int* pn = pt + A.cap + 1;
   int* pl = pn + A.cap + 1;
+  int* pp = pl + A.cap + 1;
   int run[4] = {0, 0, 0, 0};
+  int run_pcg = 0;
   __shared__ int eng_pcg_tiles, cluster_waiting;
   if (threadIdx.x == 0) {
     eng_pcg_tiles = 0;
@@ -1073,28 +1136,33 @@ __device__ void compact(const BatchDev& B, const EngineArgs& A) {
   for (int base = 0; base < num; base += blockDim.x) {
     const int i = base + threadIdx.x;
     const bool act = i < num && B.flags[8 + i] != PH_DONE;
-    if (act && !B.inst[i].pcg_cluster) atomicAdd(&eng_pcg_tiles, tiles_of(B.inst[i].n));
+    const int ptiles = act ? pcg_tiles(B.inst[i]) : 0;
+    if (act && !B.inst[i].pcg_cluster) atomicAdd(&eng_pcg_tiles, ptiles);
     if (act && B.inst[i].pcg_cluster && B.flags[8 + i] == PH_PCG) atomicAdd(&cluster_waiting, 1);
     int c[4] = {act ? 1 : 0, act ? tiles_of(B.inst[i].m) : 0, act ? tiles_of(B.inst[i].n) : 0,
                 act ? tiles_of(B.inst[i].nlo) : 0};
     int ex[4] = {c[0], c[1], c[2], c[3]}, tot[4];
     block_scan4(ex, tot, scan_sm);
+    int e2[4] = {ptiles, 0, 0, 0}, t2[4];
+    block_scan4(e2, t2, scan_sm);
     if (act) {
       const int pos = run[0] + ex[0];
       ids[pos] = i;
       pt[pos + 1] = run[1] + ex[1] + c[1];
       pn[pos + 1] = run[2] + ex[2] + c[2];
       pl[pos + 1] = run[3] + ex[3] + c[3];
+      pp[pos + 1] = run_pcg + e2[0] + ptiles;
     }
 #pragma unroll
     for (int k = 0; k < 4; ++k) run[k] += tot[k];
+    run_pcg += t2[0];
   }
   if (threadIdx.x == 0) {
-    pt[0] = 0; pn[0] = 0; pl[0] = 0;
+    pt[0] = 0; pn[0] = 0; pl[0] = 0; pp[0] = 0;
     A.act[0] = run[0];
     B.flags[0] = run[0];
     const int alive = A.act[1];
-    int need = max(run[1], max(run[2], run[3]));
+    int need = max(max(run[1], run_pcg), max(run[2], run[3]));
     int p = min(alive, max(need, 1));
     A.act[1] = p;
     A.act[2] = min(p, eng_pcg_tiles);  // 0: no instance iterates its PCG in the engine
@@ -1114,7 +1182,7 @@ __device__ __forceinline__ void stage_clock(const EngineArgs& A, int kind, unsig
 }
 
 template <typename Real>
-__global__ void __launch_bounds__(kTile, (sizeof(Real) == 4 ? 4 : 2)) k_engine(BatchDev B, EngineArgs A) {
+__global__ void __launch_bounds__(kTile, (sizeof(Real) == 4 ? 3 : 2)) k_engine(BatchDev B, EngineArgs A) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ double sm[32 * 5];
   __shared__ int flag;
@@ -1123,6 +1191,7 @@ __global__ void __launch_bounds__(kTile, (sizeof(Real) == 4 ? 4 : 2)) k_engine(B
   int* pt = ids + A.cap;
   int* pn = pt + A.cap + 1;
   int* pl = pn + A.cap + 1;
+  int* pp = pl + A.cap + 1;
   unsigned long long t = 0;
   if (A.stage_ns && cta == 0 && threadIdx.x == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   // CTAs still running; the host sets act[1] = gridDim.x before the launch
@@ -1146,7 +1215,7 @@ __global__ void __launch_bounds__(kTile, (sizeof(Real) == 4 ? 4 : 2)) k_engine(B
     const int P = __ldcg(A.act + 1), Pp = __ldcg(A.act + 2);
     if (cta >= P) return;
     alive = P;
-    const TileMap Mt{pt, ids, na}, Mn{pn, ids, na}, Ml{pl, ids, na};
+    const TileMap Mt{pt, ids, na}, Mn{pn, ids, na}, Ml{pl, ids, na}, Mp{pp, ids, na};
     st_vecop(B, Mn, cta, P, sm, flag);
     PHX_SYNC(P, 2, K_VECOP);
     st_elem_eg(B, Mt, cta, P, sm, flag);
@@ -1168,9 +1237,9 @@ __global__ void __launch_bounds__(kTile, (sizeof(Real) == 4 ? 4 : 2)) k_engine(B
     if (cta < Pp) {
       // the PCG block only needs the CTAs that cover the node tiles
       for (int k = 0; k < A.pcg_chunk; ++k) {
-        st_pcg_a<Real>(B, Mn, cta, Pp, sm, flag);
+        st_pcg_a<Real>(B, Mp, cta, Pp, sm, flag);
         PHX_SYNC_PCG(Pp, 11, K_PCG_A);
-        st_pcg_b<Real>(B, Mn, cta, Pp, sm, flag);
+        st_pcg_b<Real>(B, Mp, cta, Pp, sm, flag);
         PHX_SYNC_PCG(Pp, 12, K_PCG_B);
       }
     }
@@ -1238,7 +1307,7 @@ __device__ __forceinline__ void ld4cg(const float* p, int64_t v, float (&o)[3]) 
   o[0] = a.x; o[1] = a.y; o[2] = a.z;
 }
 
-// Sums K values over the CTA (256 threads) into out[] of thread 0.
+// Sums K values over the CTA into v[] of thread 0 (fixed order: deterministic).
 template <int K>
 __device__ __forceinline__ void cta_sum256(double (&v)[K], double (*ws)[4]) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1260,16 +1329,15 @@ __device__ __forceinline__ void cta_sum256(double (&v)[K], double (*ws)[4]) {
 }
 
 template <typename Real>
-__global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(256) k_pcg_cluster(BatchDev B, const int32_t* list,
+__global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kClThreads) k_pcg_cluster(BatchDev B, const int32_t* list,
                                                                                   int count) {
   __shared__ double red[2][4];    // this CTA's partials, double-buffered by iteration
-  __shared__ double ws[8][4];
+  __shared__ double ws[kClThreads / 32][4];
   __shared__ double tot[4];
   const unsigned rank = cl_rank();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   for (int j = (int)cl_id(); j < count; j += (int)cl_count()) {
     const int i = __ldg(list + j);
-    const InstDev& I = B.inst[i];
+    const InstDev I = B.inst[i];  // local copy: fields stay in registers across stores
     NState* st = I.st;
     if (*(volatile int32_t*)&st->phase != PH_PCG) continue;  // uniform: state written before the launch
     const int n = I.n, nch = I.nchunks;
@@ -1293,28 +1361,42 @@ __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(256) k_pcg_cluster
       Real* pnew = parity ? PcgBufs<Real>::pa(I) : PcgBufs<Real>::pb(I);
       const Real bt = (Real)beta;
       double pa_[1] = {0.0};
-      for (int c = c0 + warp; c < c1; c += nwarps) {
-        const int v = c * 32 + lane;
-        if (v >= n) continue;
-        Real acc[3];
-        sell_row<Real, Real>(I, H, v,
-                             [&](int col, Real (&xc)[3]) {
-                               Real zc[3], pc[3];
-                               ld4cg(z, col, zc);
-                               ld4cg(pold, col, pc);
-                               for (int a = 0; a < 3; ++a) xc[a] = zc[a] + bt * pc[a];
-                             },
-                             acc);
-        Real zv[3], pv[3];
-        ld4cg(z, v, zv);
-        ld4cg(pold, v, pv);
-        for (int a = 0; a < 3; ++a) {
-          pv[a] = zv[a] + bt * pv[a];
-          acc[a] += sh * pv[a];
-        }
-        st4(pnew, v, pv);
-        st4(q, v, acc);
-        pa_[0] += (double)pv[0] * acc[0] + (double)pv[1] * acc[1] + (double)pv[2] * acc[2];
+      {
+        // L lanes per row: 4 when this CTA holds few rows (latency), 1 when it holds many
+        const int r0 = c0 * 32, r1 = min(c1 * 32, n);
+        const int rows = r1 - r0;
+        auto sweep = [&](auto lanes_tag) {
+          constexpr int L = decltype(lanes_tag)::value;
+          const int sub = threadIdx.x & (L - 1), grp = threadIdx.x / L;
+          for (int base = r0; base < r1; base += (int)(blockDim.x / L)) {
+            const int v = base + grp;
+            const bool valid = v < r1;
+            Real acc[3];
+            sell_row_lanes<L, Real, Real>(I, H, v, sub, valid,
+                                          [&](int col, Real (&xc)[3]) {
+                                            Real zc[3], pc[3];
+                                            ld4cg(z, col, zc);
+                                            ld4cg(pold, col, pc);
+                                            for (int a = 0; a < 3; ++a) xc[a] = zc[a] + bt * pc[a];
+                                          },
+                                          acc);
+            if (valid && sub == 0) {
+              Real zv[3], pv[3];
+              ld4cg(z, v, zv);
+              ld4cg(pold, v, pv);
+              for (int a = 0; a < 3; ++a) {
+                pv[a] = zv[a] + bt * pv[a];
+                acc[a] += sh * pv[a];
+              }
+              st4(pnew, v, pv);
+              st4(q, v, acc);
+              pa_[0] += (double)pv[0] * acc[0] + (double)pv[1] * acc[1] + (double)pv[2] * acc[2];
+            }
+          }
+        };
+        if (rows <= (int)blockDim.x / 4) sweep(std::integral_constant<int, 4>());
+        else if (rows <= (int)blockDim.x / 2) sweep(std::integral_constant<int, 2>());
+        else sweep(std::integral_constant<int, 1>());
       }
       cta_sum256<1>(pa_, ws);
       if (threadIdx.x == 0) red[buf][0] = pa_[0];
@@ -1326,16 +1408,21 @@ __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(256) k_pcg_cluster
       }
       __syncthreads();
       pq = tot[0];
+      bool last = false;
+      double pq_use = pq;
       if (!(pq > 0.0)) {
-        status = LIN_BREAKDOWN;
-        break;
+        if (I.opts->precision != 0 && pq < 0.0 && iter == 0) {
+          pq_use = -pq;  // truncated CG, first direction: step along p with |p.q| and stop
+          last = true;
+        } else {
+          status = (I.opts->precision != 0 && pq < 0.0) ? LIN_TRUNCATED : LIN_BREAKDOWN;
+          break;
+        }
       }
-      const Real alpha = (Real)(rz / pq);
+      const Real alpha = (Real)(rz / pq_use);
       // e += alpha p, r -= alpha q, z = Minv r
       double pb_[2] = {0.0, 0.0};
-      for (int c = c0 + warp; c < c1; c += nwarps) {
-        const int v = c * 32 + lane;
-        if (v >= n) continue;
+      for (int v = c0 * 32 + (int)threadIdx.x; v < min(c1 * 32, n); v += (int)blockDim.x) {
         Real pv[3], qv[3], ev[3], rr_[3], zz[3];
         ld4(pnew, v, pv);
         ld4(q, v, qv);
@@ -1375,6 +1462,10 @@ __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(256) k_pcg_cluster
       ++iter;
       ++done_iters;
       buf ^= 1;
+      if (last) {
+        status = LIN_TRUNCATED;
+        break;
+      }
       if (rr < thr) {
         status = LIN_CONVERGED;
         break;
@@ -1397,6 +1488,7 @@ __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(256) k_pcg_cluster
       st->pcg_parity = parity;
       st->lin_status = status;
       st->phase = (status == LIN_BREAKDOWN) ? PH_LIN_DONE : PH_ACCUM;
+      st->truncate = 0;
       if (B.algo_total) {
         atomicAdd(B.algo_total + K_PCG_A, I.algo[K_PCG_A] * done_iters);
         atomicAdd(B.algo_total + K_PCG_B, I.algo[K_PCG_B] * done_iters);
@@ -1436,8 +1528,8 @@ int engine_grid(bool fp64, int num_sms) {
 cudaError_t launch_pcg_cluster(bool fp64, cudaStream_t s, const BatchDev& B, const int32_t* list, int count) {
   if (count <= 0) return cudaSuccess;
   const int grid = count * kCl;
-  if (fp64) k_pcg_cluster<double><<<grid, 256, 0, s>>>(B, list, count);
-  else k_pcg_cluster<float><<<grid, 256, 0, s>>>(B, list, count);
+  if (fp64) k_pcg_cluster<double><<<grid, kClThreads, 0, s>>>(B, list, count);
+  else k_pcg_cluster<float><<<grid, kClThreads, 0, s>>>(B, list, count);
   return cudaGetLastError();
 }
 

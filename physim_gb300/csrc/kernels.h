@@ -34,8 +34,8 @@ struct GridBar {
 
 struct EngineArgs {
   GridBar* bar;                   // [2]: round-wide barrier, PCG-block barrier
-  int32_t* act;                   // [4 + cap + 3 (cap + 1)]: count, CTAs in the round, CTAs in the
-                                  // PCG block, pad; ids; tet/node/lob tile prefixes
+  int32_t* act;                   // [4 + cap + 4 (cap + 1)]: count, CTAs in the round, CTAs in the
+                                  // PCG block, cluster solves waiting; ids; tet/node/lob/PCG tile prefixes
   unsigned long long* stage_ns;   // [32]: ns per stage kind, then executions per kind; or null
   int cap;
   int rounds;

@@ -8,6 +8,7 @@
 //   OptimSolver::LineSearch_Simple  OptimSolver.cpp:688-736
 //   OptimSolver::UpdateStepResult   OptimSolver.cpp:402-466
 //   regularisation retry loop       source/PhySim/Solvers/LinearSolver_EigenCG.cpp:67-122,
+//                                   (a truncated FP32 solve, LIN_TRUNCATED, is kept as is)
 //                                   LinearSolver.cpp:57-66 (regT = 1e-6 ||A||_F, cumulative
 //                                   shift regT * 10^(i-1) at trial i)
 // The header is plain C++ so the same code is exercised on the host by the tests.

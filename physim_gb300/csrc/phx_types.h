@@ -28,6 +28,7 @@ constexpr int kTile = 128;       // tets / nodes / lower blocks per tile
 constexpr int kChunk = 32;       // SELL chunk height (one warp)
 constexpr int kPartials = 5;     // doubles reduced per tile (at most)
 constexpr int kCl = 8;           // CTAs per cluster of the cluster PCG
+constexpr int kClThreads = 512;  // threads per CTA of the cluster PCG
 constexpr int kClusterMaxNodes = 40000;  // instances up to this size solve their PCG in one cluster
 
 // Phases of the per-instance Newton state machine (see control in kernels.cu).
@@ -59,7 +60,9 @@ enum VecOp : int32_t {
   VO_ZERODX = 256,    // dx = 0
 };
 
-enum LinStatus : int32_t { LIN_RUNNING = 0, LIN_CONVERGED = 1, LIN_MAXITER = 2, LIN_BREAKDOWN = 3 };
+// LIN_TRUNCATED: the FP32 path met negative curvature and kept the iterate so far
+// (truncated CG); the plain path reports LIN_BREAKDOWN and regularises like the reference.
+enum LinStatus : int32_t { LIN_RUNNING = 0, LIN_CONVERGED = 1, LIN_MAXITER = 2, LIN_BREAKDOWN = 3, LIN_TRUNCATED = 4 };
 
 enum DevError : int32_t { DEV_OK = 0, DEV_NONFINITE = 1, DEV_BADSTATE = 2 };
 
@@ -79,7 +82,7 @@ struct NState {
   int32_t min_step_count, num_bis, total_bis, reg_trial;
   int32_t total_reg, sweeps, total_sweeps, lin_status;
   int32_t pcg_iter, pcg_parity, error, first_step;
-  int32_t step_result, nofix, hess_count, pad3;
+  int32_t step_result, nofix, hess_count, truncate;
   int64_t pcg_total;
   double obj, opt, opt0, obj_new;
   double alpha_trial, factor, scale, dx_norm;
@@ -100,7 +103,8 @@ constexpr int kLogCap = 256;                   // Newton iterations kept in the 
 struct InstDev {
   int32_t n, m, nlo, nchunks;
   int64_t nslots;
-  int32_t pcg_cluster, pad_i;  // 1: the instance's PCG runs in k_pcg_cluster
+  int32_t pcg_cluster;         // 1: the instance's PCG runs in k_pcg_cluster
+  int32_t cpt;                 // SELL chunks per PCG tile of the engine (1 small, 4 large instances)
   // mesh + rest data
   const int32_t* tets;        // [m][4]
   const double* rest64;       // [m][12]
@@ -150,6 +154,7 @@ struct BatchDev {
   const int32_t* pre_tet;     // [num+1]
   const int32_t* pre_node;
   const int32_t* pre_lob;
+  const int32_t* pre_pcg;     // PCG tiles (InstDev::cpt chunks each)
   InstDev* inst;              // [num]
   int32_t* flags;             // [8 + num]: [0] active count; [8 + i] phase of instance i
   double* algo_total;         // [16] algorithmic bytes summed per kernel kind, or null

@@ -185,7 +185,10 @@ def test_server_results_same_alone_and_in_the_mix(gpu_ctx):
 def test_warm_resolve_after_load_update(gpu_ctx):
     m = M.serving_request(11, 2)
     inst = px.Instance(gpu_ctx, m)
-    o = px.options(precision=px.PREC_FP32_REFINE, tol_max_error=1e-8, tol_min_impr=0.0, tol_min_step=0.0)
+    # the served FP32 path is specified at 1e-6 relative residual: its Newton steps use the
+    # FP32-stored Hessian, so convergence turns linear near kappa * 1e-7 on slender bars
+    o = px.options(precision=px.PREC_FP32_REFINE, tol_rel=1e-6, tol_max_error=0.0, tol_min_impr=0.0,
+                   tol_min_step=0.0)
     x1, r1 = inst.solve_static(o, m.X0.ravel())
     m2 = M.perturb_load(m, 11, 2)
     inst.update_load(m2.force, m2.gravity)
