@@ -268,7 +268,7 @@ int set_batch(phx_context ctx, const std::vector<phx_instance>& list, BatchDev& 
     pt[i + 1] = pt[i] + tiles(list[i]->dev.m);
     pn[i + 1] = pn[i] + tiles(list[i]->dev.n);
     pl[i + 1] = pl[i] + tiles(list[i]->dev.nlo);
-    pp[i + 1] = pp[i] + (list[i]->dev.nchunks + list[i]->dev.cpt - 1) / list[i]->dev.cpt;
+    pp[i + 1] = pp[i] + (list[i]->dev.nchunks + 3) / 4;  // per-kernel path: 4 chunks per PCG tile
   }
   pre[4 * (ctx->cap + 1)] = num;
   if (num) CU(cudaMemcpyAsync(ctx->d_inst, d.data(), sizeof(InstDev) * num, cudaMemcpyHostToDevice, ctx->stream));
@@ -281,6 +281,8 @@ int set_batch(phx_context ctx, const std::vector<phx_instance>& list, BatchDev& 
   B.inst = ctx->d_inst;
   B.flags = ctx->d_flags;
   B.algo_total = ctx->profiling ? ctx->d_algo : nullptr;
+  B.cpt = 4;
+  B.cluster_mode = 0;
   const int sms = std::max(1, ctx->num_sms);
   G.tet = std::min(pt[num], sms * 8);
   G.node = std::min(pn[num], sms * 16);
@@ -478,9 +480,20 @@ int set_cluster_list(phx_context ctx, const std::vector<phx_instance>& list, int
 }
 
 // One step of the device engine: engine rounds, then (if any) the per-cluster PCG solves.
-int run_step(phx_context ctx, const BatchDev& B, int num, bool fp64, int pcg_chunk, int ccount) {
+// PCG placement: FP32 instances small enough iterate inside wide clusters (measured
+// faster than the grid-wide PCG both while many instances are active and in the tail);
+// the rest iterate on the whole GPU, with one-chunk tiles while few small instances
+// remain so that a lone instance spreads over more SMs.
+int run_step(phx_context ctx, const BatchDev& B0, int num, bool fp64, int pcg_chunk, int ccount, int active,
+             int max_chunks) {
+  BatchDev B = B0;
+  const bool few = active <= kClWideBelow;
+  B.cluster_mode = ccount > 0 ? 1 : 0;
+  // one-chunk tiles only while few, small instances remain (a large one would pay for
+  // thousands of per-tile reductions on its counter)
+  B.cpt = (few && max_chunks <= 2048) ? 1 : 4;
   TRY(run_engine(ctx, B, num, fp64, kRoundsPerLaunch, pcg_chunk));
-  if (ccount > 0 && ctx->h_flags[0] > 0) {
+  if (B.cluster_mode && ctx->h_flags[0] > 0 && ctx->h_flags[1] > 0) {
     cudaEvent_t a = nullptr, b = nullptr;
     if (ctx->profiling) {
       if (ctx->pool.size() >= 2) {
@@ -492,7 +505,7 @@ int run_step(phx_context ctx, const BatchDev& B, int num, bool fp64, int pcg_chu
       }
       cudaEventRecord(a, ctx->stream);
     }
-    CU(launch_pcg_cluster(fp64, ctx->stream, B, ctx->d_clist, ccount));
+    CU(launch_pcg_cluster(fp64, ctx->stream, B, ctx->d_clist, ccount, true));
     ctx->launches++;
     if (ctx->profiling) {
       cudaEventRecord(b, ctx->stream);
@@ -511,9 +524,12 @@ int run_to_completion(phx_context ctx, const std::vector<phx_instance>& list, bo
   TRY(set_cluster_list(ctx, list, &ccount));
   const int num = (int)list.size();
   const auto t0 = clk::now();
+  int active = num, max_chunks = 0;
+  for (auto* in : list) max_chunks = std::max(max_chunks, in->dev.nchunks);
   for (int64_t r = 0;; ++r) {
-    TRY(run_step(ctx, B, num, fp64, pcg_chunk, ccount));
-    if (ctx->h_flags[0] == 0) return PHX_OK;
+    TRY(run_step(ctx, B, num, fp64, pcg_chunk, ccount, active, max_chunks));
+    active = ctx->h_flags[0];
+    if (active == 0) return PHX_OK;
     if (std::chrono::duration<double>(clk::now() - t0).count() > kSolveTimeLimit)
       return set_err(PHX_ETIMEOUT, "solver did not finish within " + std::to_string(kSolveTimeLimit) + " s");
   }
@@ -685,9 +701,6 @@ int phx_instance_create(phx_context ctx, const phx_mesh* mesh, phx_instance* out
   HostPattern& hp = inst->hp;
   InstDev& D = inst->dev;
   D.n = hp.n; D.m = hp.m; D.nlo = hp.nlo; D.nchunks = hp.nchunks; D.nslots = hp.nslots;
-  // PCG tiles: one SELL chunk for small instances (more SMs per instance, short per-tile
-  // latency), four for large ones (fewer partial sums per reduction)
-  D.cpt = hp.nchunks > 2048 ? 4 : 1;
   auto fail = [&](int rc) { phx_instance_destroy(inst); return rc; };
   cudaError_t e0 = cudaSuccess;
   int rc = PHX_OK;
@@ -1160,7 +1173,10 @@ int phx_server_progress(phx_server s, int32_t* active, int32_t* queued) {
       s->ctx->batch_owner = s;
       s->dirty = false;
     }
-    TRY(run_step(s->ctx, s->B, (int)s->active.size(), s->fp64, s->opts.pcg_chunk, s->ccount));
+    int max_chunks = 0;
+    for (auto& r : s->active) max_chunks = std::max(max_chunks, r.inst->dev.nchunks);
+    TRY(run_step(s->ctx, s->B, (int)s->active.size(), s->fp64, s->opts.pcg_chunk, s->ccount, (int)s->active.size(),
+                 max_chunks));
   }
   if (active) *active = (int32_t)s->active.size();
   if (queued) *queued = (int32_t)s->queue.size();

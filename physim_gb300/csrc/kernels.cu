@@ -39,8 +39,12 @@ namespace phx {
 // small helpers
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ int tiles_of(int count) { return (count + kTile - 1) / kTile; }
-// PCG tiles: I.cpt SELL chunks (32 rows each) per tile
-__device__ __forceinline__ int pcg_tiles(const InstDev& I) { return (I.nchunks + I.cpt - 1) / I.cpt; }
+// PCG tiles: B.cpt SELL chunks (32 rows each) per tile
+__device__ __forceinline__ int pcg_tiles(const BatchDev& B, const InstDev& I) { return (I.nchunks + B.cpt - 1) / B.cpt; }
+// true when this instance's PCG is left to the cluster kernel in this launch
+__device__ __forceinline__ bool cluster_owned(const BatchDev& B, const InstDev& I) {
+  return B.cluster_mode && I.pcg_cluster;
+}
 
 template <int K>
 __device__ __forceinline__ void block_sum(double (&v)[K], double* sm) {
@@ -839,7 +843,7 @@ __device__ __forceinline__ void st_pcg_a(const BatchDev& B, const TileMap& M, in
     map_tile(M, t, i, lt);
     const InstDev I = B.inst[i];  // local copy: fields stay in registers across stores
     NState* st = I.st;
-    if (st->phase != PH_PCG || I.pcg_cluster) continue;
+    if (st->phase != PH_PCG || cluster_owned(B, I)) continue;
     double p[1] = {0.0};
     {
       const int par = st->pcg_parity;
@@ -848,7 +852,7 @@ __device__ __forceinline__ void st_pcg_a(const BatchDev& B, const TileMap& M, in
       const Real* z = PcgBufs<Real>::z(I);
       const Real beta = (Real)st->beta, sh = (Real)st->shift;
       const int sub = threadIdx.x & 3, row = threadIdx.x >> 2;  // 32 rows x 4 lanes per pass
-      const int ch0 = lt * I.cpt, ch1 = min(ch0 + I.cpt, I.nchunks);
+      const int ch0 = lt * B.cpt, ch1 = min(ch0 + B.cpt, I.nchunks);
       for (int ch = ch0; ch < ch1; ++ch) {
         const int v = ch * 32 + row;
         const bool valid = v < I.n;
@@ -876,7 +880,7 @@ __device__ __forceinline__ void st_pcg_a(const BatchDev& B, const TileMap& M, in
       }
     }
     double tot[1];
-    if (tile_done<1>(I, lt, pcg_tiles(I), p, tot, sm, &flag) && threadIdx.x == 0) {
+    if (tile_done<1>(I, lt, pcg_tiles(B, I), p, tot, sm, &flag) && threadIdx.x == 0) {
       count_bytes(B, I, K_PCG_A);
       st->pq = tot[0];
       if (!(tot[0] > 0.0)) {  // not positive definite along p (or non-finite)
@@ -912,10 +916,10 @@ __device__ __forceinline__ void st_pcg_b(const BatchDev& B, const TileMap& M, in
     map_tile(M, t, i, lt);
     const InstDev I = B.inst[i];  // local copy: fields stay in registers across stores
     NState* st = I.st;
-    if (st->phase != PH_PCG || I.pcg_cluster) continue;
-    const int v = lt * I.cpt * 32 + threadIdx.x;  // one row per thread over the tile's chunks
+    if (st->phase != PH_PCG || cluster_owned(B, I)) continue;
+    const int v = lt * B.cpt * 32 + threadIdx.x;  // one row per thread over the tile's chunks
     double p[2] = {0.0, 0.0};
-    if ((int)threadIdx.x < I.cpt * 32 && v < I.n) {
+    if ((int)threadIdx.x < B.cpt * 32 && v < I.n) {
       const Real alpha = (Real)st->alpha;
       const Real* pc = st->pcg_parity ? PcgBufs<Real>::pa(I) : PcgBufs<Real>::pb(I);
       Real pv[3], qv[3], ev[3], rv[3], z[3];
@@ -938,7 +942,7 @@ __device__ __forceinline__ void st_pcg_b(const BatchDev& B, const TileMap& M, in
       p[1] = (double)rv[0] * z[0] + (double)rv[1] * z[1] + (double)rv[2] * z[2];
     }
     double tot[2];
-    if (tile_done<2>(I, lt, pcg_tiles(I), p, tot, sm, &flag) && threadIdx.x == 0) {
+    if (tile_done<2>(I, lt, pcg_tiles(B, I), p, tot, sm, &flag) && threadIdx.x == 0) {
       count_bytes(B, I, K_PCG_B);
       st->pcg_iter++;
       st->pcg_total++;
@@ -1136,9 +1140,9 @@ __device__ void compact(const BatchDev& B, const EngineArgs& A) {
   for (int base = 0; base < num; base += blockDim.x) {
     const int i = base + threadIdx.x;
     const bool act = i < num && B.flags[8 + i] != PH_DONE;
-    const int ptiles = act ? pcg_tiles(B.inst[i]) : 0;
-    if (act && !B.inst[i].pcg_cluster) atomicAdd(&eng_pcg_tiles, ptiles);
-    if (act && B.inst[i].pcg_cluster && B.flags[8 + i] == PH_PCG) atomicAdd(&cluster_waiting, 1);
+    const int ptiles = act ? pcg_tiles(B, B.inst[i]) : 0;
+    if (act && !cluster_owned(B, B.inst[i])) atomicAdd(&eng_pcg_tiles, ptiles);
+    if (act && cluster_owned(B, B.inst[i]) && B.flags[8 + i] == PH_PCG) atomicAdd(&cluster_waiting, 1);
     int c[4] = {act ? 1 : 0, act ? tiles_of(B.inst[i].m) : 0, act ? tiles_of(B.inst[i].n) : 0,
                 act ? tiles_of(B.inst[i].nlo) : 0};
     int ex[4] = {c[0], c[1], c[2], c[3]}, tot[4];
@@ -1167,6 +1171,7 @@ __device__ void compact(const BatchDev& B, const EngineArgs& A) {
     A.act[1] = p;
     A.act[2] = min(p, eng_pcg_tiles);  // 0: no instance iterates its PCG in the engine
     A.act[3] = cluster_waiting;        // instances waiting for the cluster PCG kernel
+    B.flags[1] = cluster_waiting;
   }
   __threadfence();
 }
@@ -1328,11 +1333,11 @@ __device__ __forceinline__ void cta_sum256(double (&v)[K], double (*ws)[4]) {
     }
 }
 
-template <typename Real>
-__global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kClThreads) k_pcg_cluster(BatchDev B, const int32_t* list,
-                                                                                  int count) {
+template <typename Real, int CL, int NT>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT) k_pcg_cluster(BatchDev B, const int32_t* list,
+                                                                                int count) {
   __shared__ double red[2][4];    // this CTA's partials, double-buffered by iteration
-  __shared__ double ws[kClThreads / 32][4];
+  __shared__ double ws[NT / 32][4];
   __shared__ double tot[4];
   const unsigned rank = cl_rank();
   for (int j = (int)cl_id(); j < count; j += (int)cl_count()) {
@@ -1341,7 +1346,7 @@ __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kClThreads) k_pcg_
     NState* st = I.st;
     if (*(volatile int32_t*)&st->phase != PH_PCG) continue;  // uniform: state written before the launch
     const int n = I.n, nch = I.nchunks;
-    const int c0 = (int)(((int64_t)nch * rank) / kCl), c1 = (int)(((int64_t)nch * (rank + 1)) / kCl);
+    const int c0 = (int)(((int64_t)nch * rank) / CL), c1 = (int)(((int64_t)nch * (rank + 1)) / CL);
     const Real* H = PcgBufs<Real>::H(I);
     const Real* z = PcgBufs<Real>::z(I);
     Real* q = PcgBufs<Real>::q(I);
@@ -1403,7 +1408,7 @@ __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kClThreads) k_pcg_
       cl_sync();
       if (threadIdx.x == 0) {
         double s = 0;
-        for (unsigned r = 0; r < kCl; ++r) s += cl_ld(&red[buf][0], r);
+        for (unsigned r = 0; r < CL; ++r) s += cl_ld(&red[buf][0], r);
         tot[0] = s;
       }
       __syncthreads();
@@ -1449,7 +1454,7 @@ __global__ void __cluster_dims__(kCl, 1, 1) __launch_bounds__(kClThreads) k_pcg_
       cl_sync();
       if (threadIdx.x == 0) {
         double s1 = 0, s2 = 0;
-        for (unsigned r = 0; r < kCl; ++r) {
+        for (unsigned r = 0; r < CL; ++r) {
           s1 += cl_ld(&red[buf][1], r);
           s2 += cl_ld(&red[buf][2], r);
         }
@@ -1525,11 +1530,20 @@ int engine_grid(bool fp64, int num_sms) {
   return nb * num_sms;
 }
 
-cudaError_t launch_pcg_cluster(bool fp64, cudaStream_t s, const BatchDev& B, const int32_t* list, int count) {
+cudaError_t launch_pcg_cluster(bool fp64, cudaStream_t s, const BatchDev& B, const int32_t* list, int count,
+                               bool wide) {
   if (count <= 0) return cudaSuccess;
-  const int grid = count * kCl;
-  if (fp64) k_pcg_cluster<double><<<grid, kClThreads, 0, s>>>(B, list, count);
-  else k_pcg_cluster<float><<<grid, kClThreads, 0, s>>>(B, list, count);
+  // wide: few instances waiting, spread each over 8 SMs for latency; narrow: many
+  // waiting, 2 CTAs each so that about 150 instances iterate at once
+  if (wide) {
+    const int grid = count * kCl;
+    if (fp64) k_pcg_cluster<double, kCl, kClThreads><<<grid, kClThreads, 0, s>>>(B, list, count);
+    else k_pcg_cluster<float, kCl, kClThreads><<<grid, kClThreads, 0, s>>>(B, list, count);
+  } else {
+    const int grid = count * kClNarrow;
+    if (fp64) k_pcg_cluster<double, kClNarrow, kClNarrowThreads><<<grid, kClNarrowThreads, 0, s>>>(B, list, count);
+    else k_pcg_cluster<float, kClNarrow, kClNarrowThreads><<<grid, kClNarrowThreads, 0, s>>>(B, list, count);
+  }
   return cudaGetLastError();
 }
 

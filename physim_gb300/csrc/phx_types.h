@@ -29,6 +29,9 @@ constexpr int kChunk = 32;       // SELL chunk height (one warp)
 constexpr int kPartials = 5;     // doubles reduced per tile (at most)
 constexpr int kCl = 8;           // CTAs per cluster of the cluster PCG
 constexpr int kClThreads = 512;  // threads per CTA of the cluster PCG
+constexpr int kClNarrow = 2;         // narrow variant: CTAs per cluster
+constexpr int kClNarrowThreads = 256;  // narrow variant: threads per CTA
+constexpr int kClWideBelow = 32;     // fewer waiting instances than this: wide clusters
 constexpr int kClusterMaxNodes = 40000;  // instances up to this size solve their PCG in one cluster
 
 // Phases of the per-instance Newton state machine (see control in kernels.cu).
@@ -103,8 +106,8 @@ constexpr int kLogCap = 256;                   // Newton iterations kept in the 
 struct InstDev {
   int32_t n, m, nlo, nchunks;
   int64_t nslots;
-  int32_t pcg_cluster;         // 1: the instance's PCG runs in k_pcg_cluster
-  int32_t cpt;                 // SELL chunks per PCG tile of the engine (1 small, 4 large instances)
+  int32_t pcg_cluster;         // 1: the instance may run its PCG in k_pcg_cluster (cluster mode)
+  int32_t pad_c;
   // mesh + rest data
   const int32_t* tets;        // [m][4]
   const double* rest64;       // [m][12]
@@ -158,6 +161,8 @@ struct BatchDev {
   InstDev* inst;              // [num]
   int32_t* flags;             // [8 + num]: [0] active count; [8 + i] phase of instance i
   double* algo_total;         // [16] algorithmic bytes summed per kernel kind, or null
+  int32_t cpt;                // SELL chunks per PCG tile in the engine (set per launch)
+  int32_t cluster_mode;       // 1: instances with pcg_cluster leave their PCG to k_pcg_cluster
 };
 
 PHX_HD inline int64_t sell_addr(int64_t s, int e) { return (s >> 5) * 288 + (int64_t)e * 32 + (s & 31); }
