@@ -182,6 +182,14 @@ def batch_meshes(count, seed):
     return [M.batch_instance(seed, i) for i in range(count)]
 
 
+def batch_config(args, count, tets):
+    return {"workload": f"batched uneven boxes: {count} instances, 6-tet hexes, {tets} tets", "instances": count,
+            "tets": tets, "tol_rel": args.tol_rel,
+            "l2": "inputs larger than L2 (per-step working set well above 129 MB)",
+            "inner_tol": args.inner_tol, "pcg_chunk": args.pcg_chunk,
+            "plain_pcg_max_per_newton_step": args.plain_pcg_max}
+
+
 def run_batch(args, world, rank, dist):
     import physim_gb300 as px
     from physim_gb300 import build
@@ -194,7 +202,7 @@ def run_batch(args, world, rank, dist):
     served = px.options(precision=px.PREC_FP32_REFINE, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0,
                         tol_min_step=0.0, pcg_chunk=args.pcg_chunk, inner_tol=args.inner_tol)
     plain = px.options(precision=px.PREC_FP64, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0,
-                       tol_min_step=0.0, pcg_chunk=args.pcg_chunk)
+                       tol_min_step=0.0, pcg_chunk=args.pcg_chunk, ls_num_max_iters=args.plain_pcg_max)
 
     def step():
         for it in insts:
@@ -303,10 +311,7 @@ def run_batch(args, world, rank, dist):
         "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (Hessian, PCG) + fp64 (gradient, residual, energy)",
         "data": "synthetic (seeded)",
-        "config": {"workload": f"batched uneven boxes: {count} instances, 6-tet hexes, {tets} tets "
-                               f"(configs[2])", "instances": count, "tets": tets, "tol_rel": args.tol_rel,
-                   "l2": "inputs larger than L2 (per-step working set well above 129 MB)",
-                   "inner_tol": args.inner_tol, "pcg_chunk": args.pcg_chunk},
+        "config": batch_config(args, count, tets),
         "e2e": {"value": round(e2e_value, 3), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "sample": f"{len(sub)} instances created from host meshes, "
                 "solved, downloaded and destroyed per step"},
@@ -375,8 +380,7 @@ def run_reference(args, world, rank):
                                            "vs plain FP64 GPU drop-in",
             "value": round(v, 4), "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded)",
-            "config": {"workload": f"batched uneven boxes: {args.count} instances (configs[2])",
-                       "tol_rel": args.tol_rel},
+            "config": batch_config(args, args.count, sum(m.m for m in meshes)),
             "cpu_baseline": {"value": round(v, 4), "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
                              "sample": f"{sum(samples)} instances across the size range, LDLT Newton"},
             "e2e": {"value": round(v, 4), "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -408,7 +412,7 @@ def run_cantilever(args, world, rank, dist):
            "value": round(args.steps / (ms / 1e3), 3), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
-           "config": {"workload": "cantilever 8x8x32 hexes x 6 tets (configs[0])"}, "report": r, "clocks": clk}
+           "config": {"workload": "cantilever 8x8x32 hexes x 6 tets, 12288 tets"}, "report": r, "clocks": clk}
     if rank == 0 and not args.no_cpu:
         orc = oracle.Oracle(m)
         g0 = float(np.linalg.norm(orc.gradient(x0)))
@@ -424,13 +428,261 @@ def run_cantilever(args, world, rank, dist):
     return out
 
 
+
+# ---------------------------------------------------------------------------
+# serving stream: open-loop Poisson arrivals, continuous batching vs plain FIFO
+# ---------------------------------------------------------------------------
+def serving_requests(count, seed, warm_frac=0.3):
+    """Request list: (mesh, base) where base is None for a cold request or the index of an
+    earlier request whose instance is re-solved warm with its load perturbed by up to 10%."""
+    from physim_gb300 import mesh as M
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(count):
+        if i > 4 and rng.uniform() < warm_frac:
+            base = int(rng.integers(0, i))
+            while reqs[base][1] is not None:
+                base = reqs[base][1]
+            reqs.append((M.perturb_load(reqs[base][0], seed, i), base))
+        else:
+            reqs.append((M.serving_request(seed, i), None))
+    return reqs
+
+
+def serve_stream(px, ctx, reqs, insts, rate, opts, seed, budget_bytes, slots):
+    """Runs the served path live at `rate` req/s; returns per-request latencies (s) and wall time."""
+    rng = np.random.default_rng(seed + 17)
+    n = len(reqs)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+    srv = px.Server(ctx, max_slots=slots, budget_bytes=budget_bytes, opts=opts)
+    owner = {}  # instance index -> request in flight
+    lat = np.zeros(n)
+    reps = [None] * n
+    done = 0
+    nxt = 0
+    waiting_warm = []
+    t0 = time.perf_counter()
+    while done < n:
+        now = time.perf_counter() - t0
+        while nxt < n and arrivals[nxt] <= now:
+            waiting_warm.append(nxt)
+            nxt += 1
+        still = []
+        for r in waiting_warm:
+            mesh, base = reqs[r]
+            key = base if base is not None else r
+            if key in owner:  # the instance is busy with an earlier request: wait for it
+                still.append(r)
+                continue
+            inst = insts[key]
+            if base is not None:
+                inst.update_load(mesh.force, mesh.gravity)
+            else:
+                inst.reset()
+            owner[key] = r
+            srv.submit(inst, r)
+        waiting_warm = still
+        active, queued = srv.progress()
+        for tag, rep in srv.poll():
+            lat[tag] = time.perf_counter() - t0 - arrivals[tag]
+            reps[tag] = rep
+            key = reqs[tag][1] if reqs[tag][1] is not None else tag
+            owner.pop(key, None)
+            done += 1
+        if active == 0 and queued == 0 and not waiting_warm and nxt < n:
+            time.sleep(max(0.0, min(0.002, arrivals[nxt] - (time.perf_counter() - t0))))
+    wall = time.perf_counter() - t0
+    srv.close()
+    return lat, wall, arrivals, reps
+
+
+def fifo_latency(arrivals, service):
+    """Exact single-server FIFO latencies from arrival times and measured service times."""
+    lat = np.zeros(len(arrivals))
+    free = 0.0
+    for i, (a, s) in enumerate(zip(arrivals, service)):
+        start = max(a, free)
+        free = start + s
+        lat[i] = free - a
+    return lat, free
+
+
+def run_serve(args, world, rank, dist, rates=None, count=None, source="stream"):
+    """Open-loop Poisson serving.  source "stream": the 1:1:4 request mix with 30% warm
+    re-solves; source "batch": cold requests drawn from the uneven-box batch instances."""
+    import physim_gb300 as px
+    from physim_gb300 import build, mesh as M
+    build.build()
+    rates = rates or [float(r) for r in args.rates.split(",")]
+    count = count or args.requests
+    if source == "batch":
+        reqs = [(M.batch_instance(3, i), None) for i in range(count)]
+    else:
+        reqs = serving_requests(count, seed=11)
+    ctx = px.Context(0, arena_bytes=int(args.arena_gb * (1 << 30)))
+    insts = {}
+    for i, (mesh, base) in enumerate(reqs):
+        if base is None:
+            insts[i] = px.Instance(ctx, mesh)
+    served = px.options(precision=px.PREC_FP32_REFINE, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0,
+                        tol_min_step=0.0)
+    plain = px.options(precision=px.PREC_FP64, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0,
+                       tol_min_step=0.0, ls_num_max_iters=args.plain_pcg_max)
+    budget = int(min(150.0, 0.9 * args.arena_gb) * (1 << 30))
+    # plain drop-in service times: one FP64 solve call per request, in request order
+    svc = np.zeros(count)
+    plain_reps = []
+    for i, (mesh, base) in enumerate(reqs):
+        key = base if base is not None else i
+        if base is not None:
+            insts[key].update_load(mesh.force, mesh.gravity)
+        else:
+            insts[key].reset()
+        t0 = time.perf_counter()
+        _, r = insts[key].solve_static(plain)
+        svc[i] = time.perf_counter() - t0
+        plain_reps.append(r["result_name"])
+    out = {"source": "uneven-box batch instances, cold" if source == "batch" else
+           "1:1:4 boxes, 1e3..2e5 tets, 30% warm re-solves",
+           "requests": count, "tets": [int(min(m.m for m, _ in reqs)), int(max(m.m for m, _ in reqs))],
+           "warm_fraction": round(sum(b is not None for _, b in reqs) / count, 3),
+           "budget_gb": round(budget / (1 << 30), 1), "slots": args.slots, "sweep": []}
+    served_res = []
+    for rate in rates:
+        # every sweep point starts from rest; warm requests re-solve their base's equilibrium
+        for i, (mesh, base) in enumerate(reqs):
+            if base is None:
+                insts[i].update_load(mesh.force, mesh.gravity)
+                insts[i].reset()
+        lat, wall, arrivals, reps = serve_stream(px, ctx, reqs, insts, rate, served, 5, budget, args.slots)
+        served_res += [r["result_name"] for r in reps]
+        flat, fwall = fifo_latency(arrivals, svc)
+        out["sweep"].append({
+            "rate": rate,
+            "served": {"p50_ms": round(1e3 * percentile(list(lat), 50), 2),
+                       "p99_ms": round(1e3 * percentile(list(lat), 99), 2),
+                       "solves_per_s": round(count / wall, 2)},
+            "plain_fifo": {"p50_ms": round(1e3 * percentile(list(flat), 50), 2),
+                           "p99_ms": round(1e3 * percentile(list(flat), 99), 2),
+                           "solves_per_s": round(count / fwall, 2)},
+        })
+    out["served_results"] = {k: served_res.count(k) for k in sorted(set(served_res))}
+    out["plain_results"] = {k: plain_reps.count(k) for k in sorted(set(plain_reps))}
+    out["plain_service_ms"] = {"median": round(1e3 * statistics.median(svc), 2), "sum": round(1e3 * svc.sum(), 1)}
+    out["plain_fifo_note"] = ("plain latencies: exact FIFO queue over the same arrival times with the measured "
+                              "one-call FP64 service time of each request")
+    ctx.close()
+    return out
+
+
+def run_large(args, world, rank, dist):
+    """48x48x192 cantilever with per-element E: plain FP64 vs FP32+refinement at 1e-6."""
+    import physim_gb300 as px
+    from physim_gb300 import build, mesh as M
+    build.build()
+    m = M.cantilever(48, 48, 192, seed=7)
+    ctx = px.Context(0, arena_bytes=int(args.arena_gb * (1 << 30)))
+    inst = px.Instance(ctx, m)
+    res = {}
+    for name, prec in (("served_fp32_refine", px.PREC_FP32_REFINE), ("plain_fp64", px.PREC_FP64)):
+        o = px.options(precision=prec, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0, tol_min_step=0.0)
+        if prec == px.PREC_FP64:
+            o.ls_num_max_iters = args.plain_pcg_max
+        inst.reset()
+        ctx.profile(True)
+        ctx.profile_reset()
+        ctx.mark(0)
+        x, r = inst.solve_static(o)
+        ctx.mark(1)
+        ms = ctx.elapsed_ms(0, 1)
+        eh_n, eh_ms = ctx.profile_read("elem_hess")
+        sp_n, sp_ms = ctx.profile_read("spmv")
+        sp_b = ctx.profile_bytes("spmv")
+        ctx.profile(False)
+        res[name] = {"seconds": round(ms / 1e3, 3), "report": r,
+                     "elements_per_s": round(r["hessian_evals"] * m.m / (eh_ms / 1e3), 1) if eh_ms else None,
+                     "spmv_gbs": round(sp_b / (sp_ms / 1e3) / 1e9, 1) if sp_ms else None}
+        res[name]["x"] = x
+    xs, xp = res["served_fp32_refine"].pop("x"), res["plain_fp64"].pop("x")
+    x0 = m.X0.ravel()
+    out = {"metric": "large single instance static solve (48x48x192, 2.65M tets) @%g rel" % args.tol_rel,
+           "value": res["served_fp32_refine"]["seconds"], "unit": "s", "higher_is_better": False,
+           "n_gpus": world, "data": "synthetic (seeded per-element E)",
+           "config": {"workload": "cantilever 48x48x192 x 6 tets, E log-uniform [1e4,1e6], 2654208 tets",
+                      "tets": m.m, "nodes": m.n},
+           "served_fp32_refine": res["served_fp32_refine"], "plain_fp64": res["plain_fp64"],
+           "served_vs_plain_rel_displacement": float(np.linalg.norm(xs - xp) / np.linalg.norm(xp - x0))}
+    ctx.close()
+    return out
+
+
+def run_dynamics(args, world, rank, dist):
+    """16 near-incompressible 32^3 blocks, implicit Euler: FP32 served steps vs FP64 steps."""
+    import physim_gb300 as px
+    from physim_gb300 import build, mesh as M
+    build.build()
+    n_inst = args.dyn_instances
+    meshes = [M.slab_block(5, i) for i in range(n_inst)]
+    ctx = px.Context(0, arena_bytes=int(args.arena_gb * (1 << 30)))
+    res = {}
+    traj = {}
+    for name, prec in (("served_fp32_refine", px.PREC_FP32_REFINE), ("plain_fp64", px.PREC_FP64)):
+        insts = [px.Instance(ctx, m) for m in meshes]
+        for it, m in zip(insts, meshes):
+            it.reset()
+            it.set_velocities(M.slab_initial_velocity(m))
+        o = px.options(precision=prec, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0, tol_min_step=0.0)
+        if prec == px.PREC_FP64:
+            o.ls_num_max_iters = args.plain_pcg_max
+        ctx.mark(0)
+        reps_all = []
+        xs = []
+        for step in range(args.dyn_steps):
+            reps = ctx.batch_dynamic_step(insts, o, 1e-3)
+            reps_all.append(reps)
+            xs.append([it.positions() for it in insts[:2]])
+        ctx.mark(1)
+        ms = ctx.elapsed_ms(0, 1)
+        res[name] = {"ms_per_step": round(ms / args.dyn_steps, 3),
+                     "non_success": sum(r["result_name"] != "SUCCESS" for rr in reps_all for r in rr),
+                     "newton_per_step": round(statistics.mean(r["iterations"] for rr in reps_all for r in rr), 2)}
+        traj[name] = xs
+        for it in insts:
+            it.close()
+    errs = []
+    for k in range(args.dyn_steps):
+        for j in range(min(2, n_inst)):
+            x0 = meshes[j].X0.ravel()
+            a, b = traj["served_fp32_refine"][k][j], traj["plain_fp64"][k][j]
+            errs.append(float(np.linalg.norm(a - b) / max(np.linalg.norm(b - x0), 1e-300)))
+    out = {"metric": "implicit-Euler steps/s, 16 blocks 32^3 x 6 tets, nu=0.495, 1e4 contrast",
+           "value": round(1e3 / res["served_fp32_refine"]["ms_per_step"], 3), "unit": "batched steps/s",
+           "higher_is_better": True, "n_gpus": world, "data": "synthetic (seeded slab orientation)",
+           "config": {"workload": "%d instances of a 32^3 block, 196608 tets each, %d steps" % (n_inst, args.dyn_steps)},
+           "served_fp32_refine": res["served_fp32_refine"], "plain_fp64": res["plain_fp64"],
+           "per_step_rel_err_served_vs_fp64": {"max": max(errs), "last": errs[-1]}}
+    ctx.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="batch", choices=["batch", "cantilever"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "cantilever", "large", "serve", "dynamics"])
+    ap.add_argument("--rates", default="200,500,1000,2000")
+    ap.add_argument("--requests", type=int, default=160)
+    ap.add_argument("--slots", type=int, default=256)
+    ap.add_argument("--dyn-instances", type=int, default=16)
+    ap.add_argument("--dyn-steps", type=int, default=10)
+    ap.add_argument("--plain-pcg-max", type=int, default=12000,
+                    help="PCG iterations per Newton step of the plain FP64 path (the served path's budget is "
+                         "max_refine_sweeps x ls_num_max_iters = 12 x 1000)")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--batch-rate", type=float, default=200.0)
+    ap.add_argument("--batch-requests", type=int, default=64)
     ap.add_argument("--count", type=int, default=512)
     ap.add_argument("--tol-rel", type=float, default=1e-6)
     ap.add_argument("--inner-tol", type=float, default=1e-3)
@@ -449,8 +701,18 @@ def main():
         return
     if args.workload == "cantilever":
         out = run_cantilever(args, world, rank, dist)
+    elif args.workload == "large":
+        out = run_large(args, world, rank, dist)
+    elif args.workload == "serve":
+        out = run_serve(args, world, rank, dist)
+    elif args.workload == "dynamics":
+        out = run_dynamics(args, world, rank, dist)
     else:
         out = run_batch(args, world, rank, dist)
+        if not args.no_serve:
+            # p50/p99 latency beside solves/s: a bounded serving sample at one rate
+            out["serving"] = run_serve(args, world, rank, dist, rates=[args.batch_rate], count=args.batch_requests,
+                                       source="batch")
     if rank == 0:
         print(json.dumps(out), flush=True)
 
