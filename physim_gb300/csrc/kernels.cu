@@ -1494,10 +1494,8 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT) k_pcg_cluster(B
       st->lin_status = status;
       st->phase = (status == LIN_BREAKDOWN) ? PH_LIN_DONE : PH_ACCUM;
       st->truncate = 0;
-      if (B.algo_total) {
-        atomicAdd(B.algo_total + K_PCG_A, I.algo[K_PCG_A] * done_iters);
-        atomicAdd(B.algo_total + K_PCG_B, I.algo[K_PCG_B] * done_iters);
-      }
+      if (B.algo_total)  // the same per-iteration bytes as the engine's spmv + pcg_update stages
+        atomicAdd(B.algo_total + K_PCG_CLUSTER, (I.algo[K_PCG_A] + I.algo[K_PCG_B]) * done_iters);
       advance(B, i);
     }
     cl_sync();  // partial buffers are reused by the next instance
