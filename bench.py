@@ -698,7 +698,7 @@ def main():
     ap.add_argument("--batch-requests", type=int, default=64)
     ap.add_argument("--count", type=int, default=512)
     ap.add_argument("--tol-rel", type=float, default=1e-6)
-    ap.add_argument("--inner-tol", type=float, default=1e-3)
+    ap.add_argument("--inner-tol", type=float, default=1e-4)
     ap.add_argument("--pcg-chunk", type=int, default=32)
     ap.add_argument("--plain-sample", type=int, default=24)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)

@@ -100,8 +100,10 @@ typedef struct phx_options {
   int32_t warm_guess;         /* 1: PCG starts from the previous accepted step (EigenCG solveWithGuess) */
   int32_t pcg_chunk;          /* PCG iterations per device round (launch granularity) */
   double tol_rel;             /* if > 0: stop at ||g|| <= max(tol_max_error, tol_rel * ||g0||), g0 after loading */
-  int32_t pcg_cluster;        /* 1: instances up to 40000 nodes run each PCG solve inside one 8-CTA cluster;
-                                 0: every PCG iteration runs on the whole GPU */
+  int32_t pcg_cluster;        /* FP32 instances up to 13000 nodes run each PCG solve inside one 8-CTA cluster:
+                                 1 rows in shared memory, z exchanged through distributed shared
+                                 memory (default); 2 rows in L2, two-reduction CG; 0: every PCG
+                                 iteration runs on the whole GPU */
   int32_t reserved0;
 } phx_options;
 

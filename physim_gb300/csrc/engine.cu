@@ -151,6 +151,7 @@ struct phx_context_s {
   int egrid[2] = {0, 0};
   int32_t* d_clist = nullptr;  // instances whose PCG runs per cluster (batch order)
   int clist_cap = 0;
+  int clist_kinds = 0;  // bit k: the cluster list holds instances of PCG kind k
 };
 
 struct phx_instance_s {
@@ -369,6 +370,7 @@ int validate_opts(const phx_options* o) {
   if (!(o->lsearch_alpha > 0 && o->lsearch_alpha < 1)) return set_err(PHX_EINVAL, "options: lsearch_alpha out of (0,1)");
   if (o->pcg_chunk < 1 || o->pcg_chunk > 4096) return set_err(PHX_EINVAL, "options: pcg_chunk out of [1,4096]");
   if (!(o->tol_rel >= 0.0)) return set_err(PHX_EINVAL, "options: tol_rel must be >= 0");
+  if (o->pcg_cluster < 0 || o->pcg_cluster > 2) return set_err(PHX_EINVAL, "options: pcg_cluster must be 0, 1 or 2");
   return PHX_OK;
 }
 
@@ -466,6 +468,8 @@ int set_cluster_list(phx_context ctx, const std::vector<phx_instance>& list, int
   std::vector<int32_t> ids;
   for (int i = 0; i < (int)list.size(); ++i)
     if (list[i]->dev.pcg_cluster) ids.push_back(i);
+  ctx->clist_kinds = 0;
+  for (int id : ids) ctx->clist_kinds |= 1 << list[id]->dev.pcg_cluster;
   std::stable_sort(ids.begin(), ids.end(), [&](int a, int b) { return list[a]->dev.nslots > list[b]->dev.nslots; });
   *count = (int)ids.size();
   if (ids.empty()) return PHX_OK;
@@ -505,8 +509,11 @@ int run_step(phx_context ctx, const BatchDev& B0, int num, bool fp64, int pcg_ch
       }
       cudaEventRecord(a, ctx->stream);
     }
-    CU(launch_pcg_cluster(fp64, ctx->stream, B, ctx->d_clist, ccount, true));
-    ctx->launches++;
+    for (int kind = 1; kind <= 2; ++kind) {
+      if (!(ctx->clist_kinds & (1 << kind))) continue;
+      CU(launch_pcg_cluster(ctx->stream, B, ctx->d_clist, ccount, kind));
+      ctx->launches++;
+    }
     if (ctx->profiling) {
       cudaEventRecord(b, ctx->stream);
       ctx->evs.push_back({(int)K_PCG_CLUSTER, a, b});
@@ -561,7 +568,9 @@ int start_solve(phx_instance inst, const phx_options* o, bool dynamic, double dt
   set_algo_bytes(inst->dev, fp64);
   // the cluster PCG serves the FP32 path: FP64 arithmetic is slow on this part and needs
   // every SM, so FP64 solves iterate on the whole GPU
-  inst->dev.pcg_cluster = (o->pcg_cluster && !fp64 && inst->dev.n <= kClusterMaxNodes) ? 1 : 0;
+  inst->dev.pcg_cluster = (o->pcg_cluster >= 1 && o->pcg_cluster <= 2 && !fp64 && inst->dev.n <= kClusterMaxNodes)
+                              ? o->pcg_cluster
+                              : 0;
   CU(cudaMemcpyAsync(inst->d_opts, &d, sizeof(DevOpts), cudaMemcpyHostToDevice, inst->ctx->stream));
   TRY(reset_state(inst, PH_START, 0, 0.0));
   return PHX_OK;
@@ -599,7 +608,7 @@ void phx_default_options(phx_options* o) {
   o->lsearch_num_try = 32;
   o->precision = PHX_PREC_FP64;
   o->precond = 1;
-  o->inner_tol = 1e-3;
+  o->inner_tol = 1e-4;
   o->max_refine_sweeps = 12;
   o->warm_guess = 1;
   o->pcg_chunk = 32;

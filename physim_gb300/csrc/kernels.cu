@@ -1344,7 +1344,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT) k_pcg_cluster(B
     const int i = __ldg(list + j);
     const InstDev I = B.inst[i];  // local copy: fields stay in registers across stores
     NState* st = I.st;
-    if (*(volatile int32_t*)&st->phase != PH_PCG) continue;  // uniform: state written before the launch
+    if (I.pcg_cluster != 2 || *(volatile int32_t*)&st->phase != PH_PCG) continue;  // uniform over the cluster
     const int n = I.n, nch = I.nchunks;
     const int c0 = (int)(((int64_t)nch * rank) / CL), c1 = (int)(((int64_t)nch * (rank + 1)) / CL);
     const Real* H = PcgBufs<Real>::H(I);
@@ -1503,6 +1503,393 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT) k_pcg_cluster(B
 }
 
 // ---------------------------------------------------------------------------
+// cluster PCG with shared-memory rows (FP32): k_pcg_cg
+// ---------------------------------------------------------------------------
+// The CG recurrence of A. T. Chronopoulos and C. W. Gear ("s-step iterative methods for
+// symmetric linear systems", J. Comput. Appl. Math. 25 (1989)): with s = A z and the extra
+// recurrence q = A p, an iteration needs one SpMV operand (z) and one pair of inner
+// products before it and one after it:
+//   p = z + b p, q = s + b q, e += a p, r -= a q, z = M^-1 r    (own rows, no exchange)
+//   gamma = (r, z), rho = (r, r)                                 -> cluster barrier 1
+//   s = (H + shift I) z  (z of other rows read from their CTA)   (own rows)
+//   delta = (z, s)                                               -> cluster barrier 2
+//   b = gamma / gamma_old, eta = delta - b gamma / a_old = (p, A p), a = gamma / eta
+// In exact arithmetic these are the iterates of the two-reduction CG above (Eigen's
+// order); in floating point the variant is known to be about as accurate, unlike the
+// pipelined forms, whose extra recurrences lose accuracy in FP32.
+//
+// Each of the CL CTAs owns contiguous SELL chunks.  Everything per row lives in its
+// shared memory for the whole solve: z (read by the other CTAs through distributed shared
+// memory, so the solve makes no global-memory exchange at all), r, e, p, s, q and the
+// 3x3 block-Jacobi inverse; the matrix slices go to shared memory as far as they fit
+// (chunk order), with the slot-row stride padded to 288 + 32/L floats so that the L lanes
+// of a row hit different banks; later chunks are read from global memory.  Each partial
+// sum slot is written before one barrier and read before the next one, so single buffers
+// suffice; z is overwritten only after barrier 2, when no CTA reads it any more.
+constexpr int kCgSmem = 220 * 1024;  // dynamic shared memory per CTA of k_pcg_cg
+constexpr int kCgMaxChunks = (kClusterMaxNodes + 31) / 32;
+constexpr int kCgMaxCpc = (kCgMaxChunks + kCl - 1) / kCl;
+static_assert(((4 * kCgMaxChunks + 15) & ~15) + ((4 * (kCgMaxCpc + 1) + 15) & ~15) + (6 * 16 + 9 * 4) * 32 * kCgMaxCpc <=
+                  kCgSmem,
+              "rows of the largest cluster instance must fit in shared memory");
+
+struct CgResult {  // FP32 like the solve; widened once when written to the instance state
+  int iter, done, status;
+  float rr, eta, gamma, beta;
+};
+struct CgShared {  // per-CTA layout, the same offsets in every CTA of the cluster
+  const uint32_t* tab;  // [nch] distributed-shared address of each chunk's z rows
+  const int* co;        // [cpc + 1] own chunk offsets (slots)
+  float4 *z, *r, *e, *p, *s, *q;  // [mrows]
+  float* mi;            // [9][mrows] block-Jacobi inverses, plane-major
+  int mrows;            // rows of every vector array (32 per owned chunk slot)
+  const float* hs;      // own matrix slices, slot-row stride hst (chunks c0 .. csplit-1)
+  const int* cs;        // their column ids, slot-row stride cst
+  int hst, cst, csplit;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ uint32_t cl_map(uint32_t a, unsigned rank) {
+  uint32_t d;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(rank));
+  return d;
+}
+__device__ __forceinline__ float4 cl_ld4f(uint32_t a) {
+  float4 v;
+  asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "r"(a));
+  return v;
+}
+
+// Cluster-wide sums of K <= 3 FP32 partials: warp shuffles, one __syncthreads, warp 0
+// pushes the CTA's sums into slot [rank] of every CTA, one cluster barrier, then every
+// thread adds the CL slots in rank order (the same sums, hence the same decisions,
+// everywhere).  FP32 throughout: this part has a small fraction of FP32's FP64 rate, and
+// the PCG accumulates in FP32 by design (the FP64 residual of the refinement sweep decides).
+template <int K, int CL, int NT>
+__device__ __forceinline__ void cg_reduce(float (&p)[K], unsigned rank, float (*red)[4], float (*ws)[4],
+                                          float (&tot)[K]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) p[k] += __shfl_down_sync(0xffffffffu, p[k], off);
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < K; ++k) ws[warp][k] = p[k];
+  __syncthreads();
+  if (warp == 0) {
+    float v[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      v[k] = lane < NT / 32 ? ws[lane][k] : 0.f;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], off);
+      v[k] = __shfl_sync(0xffffffffu, v[k], 0);
+    }
+    if (lane < CL) {
+      const uint32_t dst = cl_map(smem_u32(&red[rank][0]), (unsigned)lane);
+#pragma unroll
+      for (int k = 0; k < K; ++k) asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(dst + 4 * k), "f"(v[k]) : "memory");
+    }
+  }
+  cl_sync();
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    float s = 0.f;
+#pragma unroll
+    for (int r = 0; r < CL; ++r) s += red[r][k];
+    tot[k] = s;
+  }
+}
+
+// s = (H + shift I) z for the CTA's rows, L lanes per row, and the partial (z, s).
+// Four slots at a time per lane: column ids, then the z gathers, then the blocks.
+template <int L, int NT>
+__device__ __forceinline__ float cg_spmv(const InstDev& I, const CgShared& S, int c0, int row0, int row1, int64_t sb,
+                                          float sh) {
+  const int sub = threadIdx.x & (L - 1), grp = threadIdx.x / L;
+  const float* hg = I.H32 + (sb >> 5) * 288;
+  const int* cg = I.slot_col + sb;
+  float part = 0.f;
+  for (int base = row0; base < row1; base += NT / L) {
+    const int v = base + grp;
+    const bool ok = v < row1;
+    float acc[3] = {0.f, 0.f, 0.f};
+    if (ok) {
+      const int c = v >> 5, lane = v & 31;
+      const int s0 = S.co[c - c0], len = (S.co[c - c0 + 1] - s0) >> 5;
+      const int R0 = (int)((s0 - sb) >> 5);
+      const bool sm = c < S.csplit;
+      const float* hb = sm ? S.hs : hg;
+      const int* cb = sm ? S.cs : cg;
+      const int hst = sm ? S.hst : 288, cst = sm ? S.cst : 32;
+      for (int k0 = sub; k0 < len; k0 += 4 * L) {
+        int col[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int k = k0 + u * L;
+          col[u] = (k < len) ? cb[(R0 + k) * cst + lane] : -1;
+        }
+        float4 x[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          x[u] = col[u] >= 0 ? cl_ld4f(S.tab[col[u] >> 5] + ((uint32_t)(col[u] & 31) << 4)) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          if (col[u] >= 0) {
+            const float* hp = hb + (size_t)(R0 + k0 + u * L) * hst + lane;
+            float h[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) h[q] = hp[q * 32];
+            acc[0] += h[0] * x[u].x + h[1] * x[u].y + h[2] * x[u].z;
+            acc[1] += h[3] * x[u].x + h[4] * x[u].y + h[5] * x[u].z;
+            acc[2] += h[6] * x[u].x + h[7] * x[u].y + h[8] * x[u].z;
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int off = 1; off < L; off <<= 1)
+#pragma unroll
+      for (int a = 0; a < 3; ++a) acc[a] += __shfl_xor_sync(0xffffffffu, acc[a], off);
+    if (ok && sub == 0) {
+      const float4 z = S.z[v - row0];
+      const float4 s = make_float4(acc[0] + sh * z.x, acc[1] + sh * z.y, acc[2] + sh * z.z, 0.f);
+      const_cast<float4*>(S.s)[v - row0] = s;
+      part += z.x * s.x + z.y * s.y + z.z * s.z;
+    }
+  }
+  return part;
+}
+
+// One linear solve (the inner PCG of one refinement sweep) of instance I in this cluster.
+// Scalars and inner products in FP32; the results go back to the FP64 state.
+template <int L, int CL, int NT>
+__device__ __noinline__ CgResult cg_solve(const InstDev& I, const CgShared& S, unsigned rank, int c0, int row0,
+                                          int row1, int64_t sb, float (*red1)[4], float (*red2)[4], float (*ws)[4],
+                                          float sh, float thr, int maxit, bool trunc_ok, int iter0) {
+  const int nrow = row1 - row0, ms = S.mrows;
+  CgResult out{iter0, 0, LIN_RUNNING, 0.f, 0.f, 0.f, 0.f};
+  // start: r and z = M^-1 r from the residual stage, e = 0
+  float g1[2] = {0.f, 0.f};
+  for (int t = threadIdx.x; t < nrow; t += NT) {
+    float r[3], z[3];
+    ld4(I.r32, row0 + t, r);
+    ld4(I.z32, row0 + t, z);
+    S.r[t] = make_float4(r[0], r[1], r[2], 0.f);
+    S.z[t] = make_float4(z[0], z[1], z[2], 0.f);
+    S.e[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+    g1[0] += r[0] * z[0] + r[1] * z[1] + r[2] * z[2];
+    g1[1] += r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+  }
+  float t1[2];
+  cg_reduce<2, CL, NT>(g1, rank, red1, ws, t1);
+  float gam = t1[0];
+  out.rr = t1[1];
+  if (t1[1] < thr) {
+    out.status = LIN_CONVERGED;
+    return out;
+  }
+  float d2[1] = {cg_spmv<L, NT>(I, S, c0, row0, row1, sb, sh)};
+  float t2[1];
+  cg_reduce<1, CL, NT>(d2, rank, red2, ws, t2);
+  float eta = t2[0], beta = 0.f, alpha;
+  bool last = false;
+  out.eta = eta;
+  out.gamma = gam;
+  if (!(eta > 0.f)) {
+    if (trunc_ok && eta < 0.f && out.iter == 0) {
+      eta = -eta;  // truncated CG, first direction: one step along z with |z.Az| and stop
+      last = true;
+    } else {
+      out.status = (trunc_ok && eta < 0.f) ? LIN_TRUNCATED : LIN_BREAKDOWN;
+      return out;
+    }
+  }
+  alpha = gam / eta;
+  for (int it = 0;; ++it) {
+    if (out.iter >= maxit) {
+      out.status = LIN_MAXITER;
+      break;
+    }
+    const float a = alpha, b = beta;
+    const bool first = it == 0;
+    float g[2] = {0.f, 0.f};
+    for (int t = threadIdx.x; t < nrow; t += NT) {
+      const float4 z = S.z[t], s = S.s[t];
+      float4 p = first ? z : S.p[t], q = first ? s : S.q[t];
+      if (!first) {
+        p = make_float4(z.x + b * p.x, z.y + b * p.y, z.z + b * p.z, 0.f);
+        q = make_float4(s.x + b * q.x, s.y + b * q.y, s.z + b * q.z, 0.f);
+      }
+      float4 e = S.e[t];
+      e.x += a * p.x;
+      e.y += a * p.y;
+      e.z += a * p.z;
+      S.e[t] = e;
+      if (last) continue;
+      float4 r = S.r[t];
+      r.x -= a * q.x;
+      r.y -= a * q.y;
+      r.z -= a * q.z;
+      const float* m = S.mi + t;
+      const float zx = m[0] * r.x + m[ms] * r.y + m[2 * ms] * r.z;
+      const float zy = m[3 * ms] * r.x + m[4 * ms] * r.y + m[5 * ms] * r.z;
+      const float zz = m[6 * ms] * r.x + m[7 * ms] * r.y + m[8 * ms] * r.z;
+      S.p[t] = p;
+      S.q[t] = q;
+      S.r[t] = r;
+      S.z[t] = make_float4(zx, zy, zz, 0.f);
+      g[0] += r.x * zx + r.y * zy + r.z * zz;
+      g[1] += r.x * r.x + r.y * r.y + r.z * r.z;
+    }
+    ++out.iter;
+    ++out.done;
+    if (last) {
+      out.status = LIN_TRUNCATED;
+      break;
+    }
+    float tg[2];
+    cg_reduce<2, CL, NT>(g, rank, red1, ws, tg);
+    const float gam_new = tg[0];
+    out.rr = tg[1];
+    if (tg[1] < thr) {
+      out.status = LIN_CONVERGED;
+      break;
+    }
+    float d[1] = {cg_spmv<L, NT>(I, S, c0, row0, row1, sb, sh)};
+    float td[1];
+    cg_reduce<1, CL, NT>(d, rank, red2, ws, td);
+    beta = gam_new / gam;
+    eta = td[0] - beta * gam_new / alpha;
+    gam = gam_new;
+    out.eta = eta;
+    out.gamma = gam;
+    out.beta = beta;
+    if (!(eta > 0.f)) {  // not positive definite along p (or non-finite)
+      out.status = (trunc_ok && eta < 0.f) ? LIN_TRUNCATED : LIN_BREAKDOWN;
+      break;
+    }
+    alpha = gam / eta;
+  }
+  return out;
+}
+
+template <int CL, int NT>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_pcg_cg(BatchDev B, const int32_t* list,
+                                                                               int count) {
+  extern __shared__ __align__(16) unsigned char cg_smem[];
+  __shared__ float red1[CL][4], red2[CL][4];  // partial sums pushed by every CTA of the cluster
+  __shared__ float ws[NT / 32][4];
+  const unsigned rank = cl_rank();
+  const int tid = threadIdx.x;
+  for (int j = (int)cl_id(); j < count; j += (int)cl_count()) {
+    const int i = __ldg(list + j);
+    const InstDev& I = B.inst[i];  // fields are re-read (L1) where needed: registers go to the rows
+    NState* st = I.st;
+    if (I.pcg_cluster != 1 || *(volatile int32_t*)&st->phase != PH_PCG) continue;  // uniform over the cluster
+    const int n = I.n, nch = I.nchunks;
+    const int cpc = (nch + CL - 1) / CL;
+    const int c0 = min(nch, (int)rank * cpc), c1 = min(nch, c0 + cpc);
+    const int row0 = c0 * 32, row1 = max(row0, min(c1 * 32, n)), nrow = row1 - row0;
+    const int mrows = 32 * cpc;
+    const int L = nrow <= NT / 4 ? 4 : (nrow <= NT / 2 ? 2 : 1);
+    // shared layout: tab u32[nch] | co i32[cpc+1] | z r e p s q float4[mrows] | mi f32[9][mrows] | matrix
+    int64_t off = 0;
+    uint32_t* tab = reinterpret_cast<uint32_t*>(cg_smem);
+    off += ((int64_t)4 * nch + 15) & ~15;
+    int* co = reinterpret_cast<int*>(cg_smem + off);
+    off += ((int64_t)4 * (cpc + 1) + 15) & ~15;
+    float4* vz = reinterpret_cast<float4*>(cg_smem + off);
+    CgShared S;
+    S.tab = tab;
+    S.co = co;
+    S.z = vz;
+    S.r = vz + mrows;
+    S.e = vz + 2 * mrows;
+    S.p = vz + 3 * mrows;
+    S.s = vz + 4 * mrows;
+    S.q = vz + 5 * mrows;
+    off += (int64_t)6 * 16 * mrows;
+    S.mi = reinterpret_cast<float*>(cg_smem + off);
+    S.mrows = mrows;
+    off += (int64_t)9 * 4 * mrows;
+    off = (off + 15) & ~(int64_t)15;
+    const int64_t sb = __ldg(I.chunk_off + c0);
+    // matrix slices of chunks c0 .. csplit-1 in shared memory, slot-row stride padded per L
+    const int pad = L == 1 ? 0 : 32 / L;
+    S.hst = 288 + pad;
+    S.cst = 32 + pad;
+    const int64_t per_row = (int64_t)4 * (S.hst + S.cst);  // bytes per slot-row of 32 slots
+    const int64_t room = kCgSmem - off;
+    int csplit = c0;
+    while (csplit < c1 && (int64_t)((__ldg(I.chunk_off + csplit + 1) - sb) >> 5) * per_row <= room) ++csplit;
+    S.csplit = csplit;
+    const int nsr = (int)((__ldg(I.chunk_off + csplit) - sb) >> 5);  // slot-rows held in shared memory
+    float* hs = reinterpret_cast<float*>(cg_smem + off);
+    int* cs = reinterpret_cast<int*>(cg_smem + off + (int64_t)4 * S.hst * nsr);
+    S.hs = hs;
+    S.cs = cs;
+    // fill: chunk table, chunk offsets, inverses, matrix slices
+    const uint32_t zloc = smem_u32(vz);
+    for (int c = tid; c < nch; c += NT) {
+      const int owner = c / cpc;
+      tab[c] = cl_map(zloc, (unsigned)owner) + (uint32_t)((c - owner * cpc) * 32 * 16);
+    }
+    for (int c = tid; c <= c1 - c0; c += NT) co[c] = __ldg(I.chunk_off + c0 + c);
+    for (int k = tid; k < 9 * nrow; k += NT) {
+      const int plane = k / nrow, t = k - plane * nrow;
+      S.mi[plane * mrows + t] = __ldg(I.minv32 + (size_t)plane * n + row0 + t);
+    }
+    {
+      const float* hg = I.H32 + (sb >> 5) * 288;
+      const int* cg = I.slot_col + sb;
+      for (int k = tid; k < nsr * 72; k += NT) {  // 288 floats = 72 float4 per slot-row
+        const int R = k / 72, w = k - R * 72;
+        reinterpret_cast<float4*>(hs + (size_t)R * S.hst)[w] = __ldg(reinterpret_cast<const float4*>(hg + (size_t)R * 288) + w);
+      }
+      for (int k = tid; k < nsr * 8; k += NT) {  // 32 ids = 8 int4 per slot-row
+        const int R = k >> 3, w = k & 7;
+        reinterpret_cast<int4*>(cs + (size_t)R * S.cst)[w] = __ldg(reinterpret_cast<const int4*>(cg + (size_t)R * 32) + w);
+      }
+    }
+    __syncthreads();
+    const float sh = (float)st->shift;
+    const float thr = (float)st->thr_inner;
+    const int maxit = I.opts->ls_num_max_iters;
+    const bool trunc_ok = I.opts->precision != 0;
+    const int iter0 = st->pcg_iter;
+    CgResult out;
+    if (L == 4) out = cg_solve<4, CL, NT>(I, S, rank, c0, row0, row1, sb, red1, red2, ws, sh, thr, maxit, trunc_ok, iter0);
+    else if (L == 2) out = cg_solve<2, CL, NT>(I, S, rank, c0, row0, row1, sb, red1, red2, ws, sh, thr, maxit, trunc_ok, iter0);
+    else out = cg_solve<1, CL, NT>(I, S, rank, c0, row0, row1, sb, red1, red2, ws, sh, thr, maxit, trunc_ok, iter0);
+    for (int t = tid; t < nrow; t += NT) {
+      const float4 e = S.e[t];
+      const float ev[3] = {e.x, e.y, e.z};
+      st4(I.e32, row0 + t, ev);
+    }
+    if (rank == 0 && tid == 0) {
+      st->pcg_iter = out.iter;
+      st->pcg_total += out.done;
+      st->rr = out.rr;
+      st->pq = out.eta;
+      st->rz = out.gamma;
+      st->beta = out.beta;
+      st->pcg_parity = 0;
+      st->lin_status = out.status;
+      st->phase = (out.status == LIN_BREAKDOWN) ? PH_LIN_DONE : PH_ACCUM;
+      st->truncate = 0;
+      if (B.algo_total)  // the same per-iteration bytes as the engine's spmv + pcg_update stages
+        atomicAdd(B.algo_total + K_PCG_CLUSTER, (I.algo[K_PCG_A] + I.algo[K_PCG_B]) * out.done);
+      advance(B, i);
+    }
+    cl_sync();  // shared buffers and partial slots are reused by the next instance
+  }
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 template <typename Real>
@@ -1517,6 +1904,8 @@ cudaError_t setup_kernel_attributes() {
     e = cudaFuncSetAttribute(k_engine<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hess_smem<double>());
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_engine<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hess_smem<float>());
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_pcg_cg<kCl, kClThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, kCgSmem);
   return e;
 }
 
@@ -1528,20 +1917,11 @@ int engine_grid(bool fp64, int num_sms) {
   return nb * num_sms;
 }
 
-cudaError_t launch_pcg_cluster(bool fp64, cudaStream_t s, const BatchDev& B, const int32_t* list, int count,
-                               bool wide) {
+cudaError_t launch_pcg_cluster(cudaStream_t s, const BatchDev& B, const int32_t* list, int count, int kind) {
   if (count <= 0) return cudaSuccess;
-  // wide: few instances waiting, spread each over 8 SMs for latency; narrow: many
-  // waiting, 2 CTAs each so that about 150 instances iterate at once
-  if (wide) {
-    const int grid = count * kCl;
-    if (fp64) k_pcg_cluster<double, kCl, kClThreads><<<grid, kClThreads, 0, s>>>(B, list, count);
-    else k_pcg_cluster<float, kCl, kClThreads><<<grid, kClThreads, 0, s>>>(B, list, count);
-  } else {
-    const int grid = count * kClNarrow;
-    if (fp64) k_pcg_cluster<double, kClNarrow, kClNarrowThreads><<<grid, kClNarrowThreads, 0, s>>>(B, list, count);
-    else k_pcg_cluster<float, kClNarrow, kClNarrowThreads><<<grid, kClNarrowThreads, 0, s>>>(B, list, count);
-  }
+  const int grid = count * kCl;  // one cluster per listed instance; clusters skip the others
+  if (kind == 1) k_pcg_cg<kCl, kClThreads><<<grid, kClThreads, kCgSmem, s>>>(B, list, count);
+  else k_pcg_cluster<float, kCl, kClThreads><<<grid, kClThreads, 0, s>>>(B, list, count);
   return cudaGetLastError();
 }
 

@@ -46,8 +46,7 @@ cudaError_t setup_kernel_attributes();
 int engine_grid(bool fp64, int num_sms);
 cudaError_t launch_engine(bool fp64, int grid, cudaStream_t s, const BatchDev& B, const EngineArgs& A);
 // PCG of every listed instance that is in PH_PCG, one cluster per instance
-cudaError_t launch_pcg_cluster(bool fp64, cudaStream_t s, const BatchDev& B, const int32_t* list, int count,
-                               bool wide);
+cudaError_t launch_pcg_cluster(cudaStream_t s, const BatchDev& B, const int32_t* list, int count, int kind);
 void launch(KernelId id, int grid, cudaStream_t s, const BatchDev& B, bool fp64);
 const char* kernel_name(KernelId id);
 

@@ -32,7 +32,7 @@ constexpr int kClThreads = 512;  // threads per CTA of the cluster PCG
 constexpr int kClNarrow = 2;         // narrow variant: CTAs per cluster
 constexpr int kClNarrowThreads = 256;  // narrow variant: threads per CTA
 constexpr int kClWideBelow = 32;     // fewer waiting instances than this: wide clusters
-constexpr int kClusterMaxNodes = 40000;  // instances up to this size solve their PCG in one cluster
+constexpr int kClusterMaxNodes = 13000;  // instances up to this size solve their PCG in one cluster
 
 // Phases of the per-instance Newton state machine (see control in kernels.cu).
 enum Phase : int32_t {
@@ -106,7 +106,7 @@ constexpr int kLogCap = 256;                   // Newton iterations kept in the 
 struct InstDev {
   int32_t n, m, nlo, nchunks;
   int64_t nslots;
-  int32_t pcg_cluster;         // 1: the instance may run its PCG in k_pcg_cluster (cluster mode)
+  int32_t pcg_cluster;         // PCG inside one cluster: 0 no, 1 shared-memory rows (k_pcg_cg), 2 rows in L2 (k_pcg_cluster)
   int32_t pad_c;
   // mesh + rest data
   const int32_t* tets;        // [m][4]
