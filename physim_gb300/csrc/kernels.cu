@@ -1605,10 +1605,12 @@ __device__ __forceinline__ void cg_reduce(float (&p)[K], unsigned rank, float (*
 }
 
 // s = (H + shift I) z for the CTA's rows, L lanes per row, and the partial (z, s).
-// Four slots at a time per lane: column ids, then the z gathers, then the blocks.
+// Four slots at a time per lane: their column ids and blocks are loaded together, then
+// the z gathers (own rows from this CTA's shared memory, other rows through distributed
+// shared memory), then the arithmetic: two dependent round trips per four slots.
 template <int L, int NT>
 __device__ __forceinline__ float cg_spmv(const InstDev& I, const CgShared& S, int c0, int row0, int row1, int64_t sb,
-                                          float sh) {
+                                         float sh) {
   const int sub = threadIdx.x & (L - 1), grp = threadIdx.x / L;
   const float* hg = I.H32 + (sb >> 5) * 288;
   const int* cg = I.slot_col + sb;
@@ -1627,26 +1629,31 @@ __device__ __forceinline__ float cg_spmv(const InstDev& I, const CgShared& S, in
       const int hst = sm ? S.hst : 288, cst = sm ? S.cst : 32;
       for (int k0 = sub; k0 < len; k0 += 4 * L) {
         int col[4];
+        float h[4][9];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           const int k = k0 + u * L;
-          col[u] = (k < len) ? cb[(R0 + k) * cst + lane] : -1;
+          const bool in = k < len;
+          const int R = R0 + (in ? k : 0);
+          col[u] = in ? cb[R * cst + lane] : -1;
+          const float* hp = hb + (size_t)R * hst + lane;
+#pragma unroll
+          for (int q = 0; q < 9; ++q) h[u][q] = in ? hp[q * 32] : 0.f;
         }
         float4 x[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
-          x[u] = col[u] >= 0 ? cl_ld4f(S.tab[col[u] >> 5] + ((uint32_t)(col[u] & 31) << 4)) : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int u = 0; u < 4; ++u) {
+          const int cc = col[u];
+          const unsigned lr = (unsigned)(cc - row0);
+          if (cc < 0) x[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+          else if (lr < (unsigned)(row1 - row0)) x[u] = S.z[lr];
+          else x[u] = cl_ld4f(S.tab[cc >> 5] + ((uint32_t)(cc & 31) << 4));
+        }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-          if (col[u] >= 0) {
-            const float* hp = hb + (size_t)(R0 + k0 + u * L) * hst + lane;
-            float h[9];
-#pragma unroll
-            for (int q = 0; q < 9; ++q) h[q] = hp[q * 32];
-            acc[0] += h[0] * x[u].x + h[1] * x[u].y + h[2] * x[u].z;
-            acc[1] += h[3] * x[u].x + h[4] * x[u].y + h[5] * x[u].z;
-            acc[2] += h[6] * x[u].x + h[7] * x[u].y + h[8] * x[u].z;
-          }
+          acc[0] += h[u][0] * x[u].x + h[u][1] * x[u].y + h[u][2] * x[u].z;
+          acc[1] += h[u][3] * x[u].x + h[u][4] * x[u].y + h[u][5] * x[u].z;
+          acc[2] += h[u][6] * x[u].x + h[u][7] * x[u].y + h[u][8] * x[u].z;
         }
       }
     }
@@ -1667,7 +1674,7 @@ __device__ __forceinline__ float cg_spmv(const InstDev& I, const CgShared& S, in
 // One linear solve (the inner PCG of one refinement sweep) of instance I in this cluster.
 // Scalars and inner products in FP32; the results go back to the FP64 state.
 template <int L, int CL, int NT>
-__device__ __noinline__ CgResult cg_solve(const InstDev& I, const CgShared& S, unsigned rank, int c0, int row0,
+__device__ __forceinline__ CgResult cg_solve(const InstDev& I, const CgShared& S, unsigned rank, int c0, int row0,
                                           int row1, int64_t sb, float (*red1)[4], float (*red2)[4], float (*ws)[4],
                                           float sh, float thr, int maxit, bool trunc_ok, int iter0) {
   const int nrow = row1 - row0, ms = S.mrows;
