@@ -145,6 +145,7 @@ struct phx_context_s {
   cudaEvent_t marks[16] = {};
   // engine
   GridBar* d_bar = nullptr;
+  int32_t* d_phc = nullptr;  // [32] per-phase instance counts of the engine (live, snapshot)
   int32_t* d_act = nullptr;
   int act_cap = 0;
   unsigned long long* d_stage = nullptr;  // [32] stage ns + executions (profiling)
@@ -247,6 +248,10 @@ int ensure_batch_cap(phx_context ctx, int num) {
   CU(cudaMalloc(&ctx->d_flags, sizeof(int32_t) * (8 + cap)));
   CU(cudaMallocHost(&ctx->h_flags, sizeof(int32_t) * (8 + cap)));
   ctx->cap = cap;
+  if (!ctx->d_phc) {
+    CU(cudaMalloc(&ctx->d_phc, sizeof(int32_t) * 32));
+    CU(cudaMemsetAsync(ctx->d_phc, 0, sizeof(int32_t) * 32, ctx->stream));
+  }
   return PHX_OK;
 }
 
@@ -281,6 +286,7 @@ int set_batch(phx_context ctx, const std::vector<phx_instance>& list, BatchDev& 
   B.pre_pcg = ctx->d_pre + 3 * (ctx->cap + 1);
   B.inst = ctx->d_inst;
   B.flags = ctx->d_flags;
+  B.phase_live = ctx->d_phc;
   B.algo_total = ctx->profiling ? ctx->d_algo : nullptr;
   B.cpt = 4;
   B.cluster_mode = 0;
@@ -442,6 +448,19 @@ int ensure_engine(phx_context ctx) {
   return PHX_OK;
 }
 
+// A pair of timing events from the pool, the first recorded now on the library stream.
+int profile_events(phx_context ctx, cudaEvent_t* a, cudaEvent_t* b) {
+  if (ctx->pool.size() >= 2) {
+    *a = ctx->pool.back(); ctx->pool.pop_back();
+    *b = ctx->pool.back(); ctx->pool.pop_back();
+  } else {
+    CU(cudaEventCreate(a));
+    CU(cudaEventCreate(b));
+  }
+  CU(cudaEventRecord(*a, ctx->stream));
+  return PHX_OK;
+}
+
 // One cooperative launch of the engine: up to `rounds` Newton rounds over the batch.
 int run_engine(phx_context ctx, const BatchDev& B, int num, bool fp64, int rounds, int pcg_chunk) {
   TRY(ensure_engine(ctx));
@@ -452,8 +471,14 @@ int run_engine(phx_context ctx, const BatchDev& B, int num, bool fp64, int round
   const int32_t hdr[2] = {0, grid};  // active count (set by the kernel), CTAs running
   CU(cudaMemcpyAsync(ctx->d_act, hdr, sizeof(hdr), cudaMemcpyHostToDevice, ctx->stream));
   EngineArgs A{ctx->d_bar, ctx->d_act, ctx->profiling ? ctx->d_stage : nullptr, ctx->cap, rounds, pcg_chunk};
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (ctx->profiling) TRY(profile_events(ctx, &a, &b));
   CU(launch_engine(fp64, grid, ctx->stream, B, A));
   ctx->launches++;
+  if (ctx->profiling) {
+    cudaEventRecord(b, ctx->stream);
+    ctx->evs.push_back({(int)K_ENGINE, a, b});
+  }
   GridBar hb[2];
   CU(cudaMemcpyAsync(hb, ctx->d_bar, 2 * sizeof(GridBar), cudaMemcpyDeviceToHost, ctx->stream));
   TRY(read_flags(ctx, num));
@@ -468,9 +493,9 @@ int set_cluster_list(phx_context ctx, const std::vector<phx_instance>& list, int
   std::vector<int32_t> ids;
   for (int i = 0; i < (int)list.size(); ++i)
     if (list[i]->dev.pcg_cluster) ids.push_back(i);
+  std::stable_sort(ids.begin(), ids.end(), [&](int a, int b) { return list[a]->dev.nslots > list[b]->dev.nslots; });
   ctx->clist_kinds = 0;
   for (int id : ids) ctx->clist_kinds |= 1 << list[id]->dev.pcg_cluster;
-  std::stable_sort(ids.begin(), ids.end(), [&](int a, int b) { return list[a]->dev.nslots > list[b]->dev.nslots; });
   *count = (int)ids.size();
   if (ids.empty()) return PHX_OK;
   if (ctx->clist_cap < (int)ids.size()) {
@@ -499,16 +524,7 @@ int run_step(phx_context ctx, const BatchDev& B0, int num, bool fp64, int pcg_ch
   TRY(run_engine(ctx, B, num, fp64, kRoundsPerLaunch, pcg_chunk));
   if (B.cluster_mode && ctx->h_flags[0] > 0 && ctx->h_flags[1] > 0) {
     cudaEvent_t a = nullptr, b = nullptr;
-    if (ctx->profiling) {
-      if (ctx->pool.size() >= 2) {
-        a = ctx->pool.back(); ctx->pool.pop_back();
-        b = ctx->pool.back(); ctx->pool.pop_back();
-      } else {
-        cudaEventCreate(&a);
-        cudaEventCreate(&b);
-      }
-      cudaEventRecord(a, ctx->stream);
-    }
+    if (ctx->profiling) TRY(profile_events(ctx, &a, &b));
     for (int kind = 1; kind <= 2; ++kind) {
       if (!(ctx->clist_kinds & (1 << kind))) continue;
       CU(launch_pcg_cluster(ctx->stream, B, ctx->d_clist, ccount, kind));
@@ -656,6 +672,7 @@ int phx_context_destroy(phx_context ctx) {
   if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
   if (ctx->d_algo) cudaFree(ctx->d_algo);
   if (ctx->d_bar) cudaFree(ctx->d_bar);
+  if (ctx->d_phc) cudaFree(ctx->d_phc);
   if (ctx->d_act) cudaFree(ctx->d_act);
   if (ctx->d_stage) cudaFree(ctx->d_stage);
   if (ctx->d_clist) cudaFree(ctx->d_clist);

@@ -212,6 +212,12 @@ __device__ __forceinline__ TileMap full_map(const BatchDev& B, const int32_t* pr
 
 // Runs the state machine of instance i up to its next device phase (called by the one
 // thread that finalises a stage for the instance) and publishes the phase.
+// Phase bucket of an instance for the engine's stage counts: its phase, except that a PCG
+// solve left to the cluster kernel has a bucket of its own.
+__device__ __forceinline__ int phase_bucket(const BatchDev& B, const InstDev& I, int ph) {
+  return (ph == PH_PCG && cluster_owned(B, I)) ? kBucketClusterPcg : ph;
+}
+
 __device__ void advance(const BatchDev& B, int i) {
   const InstDev I = B.inst[i];  // local copy: fields stay in registers across stores
   NState s = *I.st;
@@ -227,6 +233,15 @@ __device__ void advance(const BatchDev& B, int i) {
     s.log_pending = 0;
   }
   *I.st = s;
+  if (B.phase_live) {  // move the instance between the per-phase counts the engine skips stages by
+    const int old = B.flags[8 + i];
+    const int ob = (old > PH_DONE && old < kBucketClusterPcg) ? phase_bucket(B, I, old) : -1;
+    const int nb = s.phase > PH_DONE ? phase_bucket(B, I, s.phase) : -1;
+    if (ob != nb) {
+      if (ob >= 0) atomicSub(B.phase_live + ob, 1);
+      if (nb >= 0) atomicAdd(B.phase_live + nb, 1);
+    }
+  }
   B.flags[8 + i] = s.phase;
 }
 
@@ -1039,7 +1054,10 @@ constexpr long long kBarrierLimit = 4000000000LL;  // about 2 s of SM clock
 // nblocks = the CTAs taking part (always the lowest-numbered ones).
 // `abort` is the launch-wide error flag (the round-wide barrier's): a timeout on either
 // barrier object raises it and every waiting CTA leaves.
-__device__ __forceinline__ bool grid_sync(GridBar* gb, unsigned int nblocks, int tag, int* abort) {
+// live: the per-phase counts; the last CTA to arrive copies them into the snapshot half
+// that every CTA reads after the barrier (null: no counts).
+__device__ __forceinline__ bool grid_sync(GridBar* gb, unsigned int nblocks, int tag, int* abort,
+                                          int32_t* live = nullptr) {
   __syncthreads();
   if (threadIdx.x == 0) {
     volatile unsigned int* vgen = &gb->gen;
@@ -1049,6 +1067,10 @@ __device__ __forceinline__ bool grid_sync(GridBar* gb, unsigned int nblocks, int
     const unsigned int a = atomicAdd(&gb->arrive, 1u);
     if (a == nblocks - 1) {
       gb->arrive = 0u;
+      if (live) {
+        __threadfence();
+        for (int k = 0; k < 16; ++k) live[16 + k] = *(volatile int32_t*)(live + k);
+      }
       __threadfence();
       atomicAdd(&gb->gen, 1u);
     } else {
@@ -1124,6 +1146,18 @@ __device__ void compact(const BatchDev& B, const EngineArgs& A) {
     else B.flags[8 + i] = ph;
   }
   __syncthreads();
+  __shared__ int cnt[16];
+  if (threadIdx.x < 16) cnt[threadIdx.x] = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < num; i += blockDim.x) {
+    const int ph = B.flags[8 + i];
+    if (ph > PH_DONE && ph < kBucketClusterPcg) atomicAdd(&cnt[phase_bucket(B, B.inst[i], ph)], 1);
+  }
+  __syncthreads();
+  if (B.phase_live && threadIdx.x < 16) {
+    B.phase_live[threadIdx.x] = cnt[threadIdx.x];
+    B.phase_live[16 + threadIdx.x] = cnt[threadIdx.x];
+  }
   int* ids = A.act + 4;
   int* pt = ids + A.cap;
   int* pn = pt + A.cap + 1;
@@ -1201,65 +1235,104 @@ __global__ void __launch_bounds__(kTile, (sizeof(Real) == 4 ? 3 : 2)) k_engine(B
   if (A.stage_ns && cta == 0 && threadIdx.x == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   // CTAs still running; the host sets act[1] = gridDim.x before the launch
   int alive = gridDim.x;
+  int first_wait = -1;  // round in which an instance first waited for the cluster kernel
   // two barrier objects: the PCG group synchronises on its own counter while the CTAs
   // that skip the PCG block are already arriving at the next round-wide barrier
-#define PHX_SYNC(n, tag, kind)                                          \
-  if (!grid_sync(A.bar, (unsigned)(n), tag, &A.bar->err)) return;      \
+#define PHX_SYNC(n, tag, kind)                                                     \
+  if (!grid_sync(A.bar, (unsigned)(n), tag, &A.bar->err, B.phase_live)) return;  \
   stage_clock(A, kind, t);
 #define PHX_SYNC_PCG(n, tag, kind)                                      \
   if (!grid_sync(A.bar + 1, (unsigned)(n), tag, &A.bar->err)) return;  \
   stage_clock(A, kind, t);
+  // a stage (and the barrier after it) runs only if an instance is in its phase at the
+  // last barrier's snapshot: every CTA reads the same snapshot, so all skip together
+#define PHX_NEED(ph) (!B.phase_live || __ldcg(B.phase_live + 16 + (ph)) > 0)
   for (int r = 0; r < A.rounds; ++r) {
     if (cta == 0) compact(B, A);
     PHX_SYNC(alive, 1, K_CONTROL);
     const int na = __ldcg(A.act);
     if (na == 0) break;
-    // hand over to the cluster PCG kernel as soon as an instance waits for it
-    if (r > 0 && __ldcg(A.act + 3) > 0) break;
+    // hand over to the cluster PCG kernel once half the active instances wait for it, or
+    // kWaitRounds rounds after the first one started waiting (the others keep going in
+    // between: line-search trials and element passes do not need the cluster kernel)
+    const int waiting = __ldcg(A.act + 3);
+    if (waiting > 0 && first_wait < 0) first_wait = r;
+    if (r > 0 && waiting > 0 && (2 * waiting >= na || r - first_wait >= kWaitRounds)) break;
     // this round needs only P CTAs (P never grows within a launch: the rest leave)
     const int P = __ldcg(A.act + 1), Pp = __ldcg(A.act + 2);
     if (cta >= P) return;
     alive = P;
     const TileMap Mt{pt, ids, na}, Mn{pn, ids, na}, Ml{pl, ids, na}, Mp{pp, ids, na};
-    st_vecop(B, Mn, cta, P, sm, flag);
-    PHX_SYNC(P, 2, K_VECOP);
-    st_elem_eg(B, Mt, cta, P, sm, flag);
-    PHX_SYNC(P, 3, K_ELEM_EG);
-    st_gather(B, Mn, cta, P, sm, flag);
-    PHX_SYNC(P, 4, K_GATHER);
-    st_vecop(B, Mn, cta, P, sm, flag);
-    PHX_SYNC(P, 5, K_VECOP);
-    st_elem_hess<Real>(B, Mt, cta, P, sm, flag, smraw);
-    PHX_SYNC(P, 6, K_ELEM_HESS);
-    st_assemble<Real>(B, Ml, cta, P, sm, flag);
-    PHX_SYNC(P, 7, K_ASSEMBLE);
-    st_jacobi<Real>(B, Mn, cta, P, sm, flag);
-    PHX_SYNC(P, 8, K_JACOBI);
-    st_linsetup(B, Mn, cta, P, sm, flag);
-    PHX_SYNC(P, 9, K_LINSETUP);
-    st_resid<Real>(B, Mn, cta, P, sm, flag);
-    PHX_SYNC(P, 10, K_RESID);
-    if (cta < Pp) {
-      // the PCG block only needs the CTAs that cover the node tiles
-      for (int k = 0; k < A.pcg_chunk; ++k) {
-        st_pcg_a<Real>(B, Mp, cta, Pp, sm, flag);
-        PHX_SYNC_PCG(Pp, 11, K_PCG_A);
-        st_pcg_b<Real>(B, Mp, cta, Pp, sm, flag);
-        PHX_SYNC_PCG(Pp, 12, K_PCG_B);
-      }
+    if (PHX_NEED(PH_VEC)) {
+      st_vecop(B, Mn, cta, P, sm, flag);
+      PHX_SYNC(P, 2, K_VECOP);
     }
-    PHX_SYNC(P, 18, K_CONTROL);
-    st_accum<Real>(B, Mn, cta, P, sm, flag);
-    PHX_SYNC(P, 13, K_ACCUM);
-    st_resid<Real>(B, Mn, cta, P, sm, flag);
-    PHX_SYNC(P, 14, K_RESID);
-    st_vecop(B, Mn, cta, P, sm, flag);
-    PHX_SYNC(P, 15, K_VECOP);
-    st_elem_eg(B, Mt, cta, P, sm, flag);
-    PHX_SYNC(P, 16, K_ELEM_EG);
-    st_gather(B, Mn, cta, P, sm, flag);
-    PHX_SYNC(P, 17, K_GATHER);
+    if (PHX_NEED(PH_EVAL)) {
+      st_elem_eg(B, Mt, cta, P, sm, flag);
+      PHX_SYNC(P, 3, K_ELEM_EG);
+    }
+    if (PHX_NEED(PH_EVAL)) {
+      st_gather(B, Mn, cta, P, sm, flag);
+      PHX_SYNC(P, 4, K_GATHER);
+    }
+    if (PHX_NEED(PH_VEC)) {
+      st_vecop(B, Mn, cta, P, sm, flag);
+      PHX_SYNC(P, 5, K_VECOP);
+    }
+    if (PHX_NEED(PH_HESS)) {
+      st_elem_hess<Real>(B, Mt, cta, P, sm, flag, smraw);
+      PHX_SYNC(P, 6, K_ELEM_HESS);
+    }
+    if (PHX_NEED(PH_HESS)) {
+      st_assemble<Real>(B, Ml, cta, P, sm, flag);
+      PHX_SYNC(P, 7, K_ASSEMBLE);
+    }
+    if (PHX_NEED(PH_HESS) || PHX_NEED(PH_JACOBI)) {
+      st_jacobi<Real>(B, Mn, cta, P, sm, flag);
+      PHX_SYNC(P, 8, K_JACOBI);
+    }
+    if (PHX_NEED(PH_LINSETUP)) {
+      st_linsetup(B, Mn, cta, P, sm, flag);
+      PHX_SYNC(P, 9, K_LINSETUP);
+    }
+    if (PHX_NEED(PH_RESID)) {
+      st_resid<Real>(B, Mn, cta, P, sm, flag);
+      PHX_SYNC(P, 10, K_RESID);
+    }
+    if (Pp > 0 && PHX_NEED(PH_PCG)) {
+      if (cta < Pp) {
+        // the PCG block only needs the CTAs that cover the node tiles
+        for (int k = 0; k < A.pcg_chunk; ++k) {
+          st_pcg_a<Real>(B, Mp, cta, Pp, sm, flag);
+          PHX_SYNC_PCG(Pp, 11, K_PCG_A);
+          st_pcg_b<Real>(B, Mp, cta, Pp, sm, flag);
+          PHX_SYNC_PCG(Pp, 12, K_PCG_B);
+        }
+      }
+      PHX_SYNC(P, 18, K_CONTROL);
+    }
+    if (PHX_NEED(PH_ACCUM)) {
+      st_accum<Real>(B, Mn, cta, P, sm, flag);
+      PHX_SYNC(P, 13, K_ACCUM);
+    }
+    if (PHX_NEED(PH_RESID)) {
+      st_resid<Real>(B, Mn, cta, P, sm, flag);
+      PHX_SYNC(P, 14, K_RESID);
+    }
+    if (PHX_NEED(PH_VEC)) {
+      st_vecop(B, Mn, cta, P, sm, flag);
+      PHX_SYNC(P, 15, K_VECOP);
+    }
+    if (PHX_NEED(PH_EVAL)) {
+      st_elem_eg(B, Mt, cta, P, sm, flag);
+      PHX_SYNC(P, 16, K_ELEM_EG);
+    }
+    if (PHX_NEED(PH_EVAL)) {
+      st_gather(B, Mn, cta, P, sm, flag);
+      PHX_SYNC(P, 17, K_GATHER);
+    }
   }
+#undef PHX_NEED
 #undef PHX_SYNC
 #undef PHX_SYNC_PCG
   if (cta == 0) compact(B, A);
@@ -1913,6 +1986,7 @@ cudaError_t setup_kernel_attributes() {
     e = cudaFuncSetAttribute(k_engine<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hess_smem<float>());
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_pcg_cg<kCl, kClThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, kCgSmem);
+
   return e;
 }
 
@@ -1926,9 +2000,9 @@ int engine_grid(bool fp64, int num_sms) {
 
 cudaError_t launch_pcg_cluster(cudaStream_t s, const BatchDev& B, const int32_t* list, int count, int kind) {
   if (count <= 0) return cudaSuccess;
-  const int grid = count * kCl;  // one cluster per listed instance; clusters skip the others
-  if (kind == 1) k_pcg_cg<kCl, kClThreads><<<grid, kClThreads, kCgSmem, s>>>(B, list, count);
-  else k_pcg_cluster<float, kCl, kClThreads><<<grid, kClThreads, 0, s>>>(B, list, count);
+  // one cluster per listed instance; clusters skip instances not waiting for them
+  if (kind == 1) k_pcg_cg<kCl, kClThreads><<<count * kCl, kClThreads, kCgSmem, s>>>(B, list, count);
+  else k_pcg_cluster<float, kCl, kClThreads><<<count * kCl, kClThreads, 0, s>>>(B, list, count);
   return cudaGetLastError();
 }
 
@@ -1992,6 +2066,7 @@ const char* kernel_name(KernelId id) {
     case K_PCG_B: return "pcg_update";
     case K_ACCUM: return "accum";
     case K_PCG_CLUSTER: return "pcg_cluster";
+    case K_ENGINE: return "engine";
     default: return "?";
   }
 }

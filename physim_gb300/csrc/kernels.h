@@ -21,6 +21,7 @@ enum KernelId : int {
   K_PCG_B,
   K_ACCUM,
   K_PCG_CLUSTER,
+  K_ENGINE,  // whole engine launches (profiling events only; no bytes)
   K_COUNT
 };
 static_assert(K_COUNT <= 16, "InstDev::algo holds 16 kernel kinds");

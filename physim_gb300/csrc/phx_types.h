@@ -33,6 +33,7 @@ constexpr int kClNarrow = 2;         // narrow variant: CTAs per cluster
 constexpr int kClNarrowThreads = 256;  // narrow variant: threads per CTA
 constexpr int kClWideBelow = 32;     // fewer waiting instances than this: wide clusters
 constexpr int kClusterMaxNodes = 13000;  // instances up to this size solve their PCG in one cluster
+constexpr int kWaitRounds = 4;           // engine rounds an instance may wait for the cluster kernel
 
 // Phases of the per-instance Newton state machine (see control in kernels.cu).
 enum Phase : int32_t {
@@ -161,9 +162,13 @@ struct BatchDev {
   InstDev* inst;              // [num]
   int32_t* flags;             // [8 + num]: [0] active count; [8 + i] phase of instance i
   double* algo_total;         // [16] algorithmic bytes summed per kernel kind, or null
+  int32_t* phase_live;        // [32] active instances per phase bucket: [0..15] kept current by
+                              // advance(), [16..31] the copy taken at the last grid barrier, or null
   int32_t cpt;                // SELL chunks per PCG tile in the engine (set per launch)
   int32_t cluster_mode;       // 1: instances with pcg_cluster leave their PCG to k_pcg_cluster
 };
+
+constexpr int kBucketClusterPcg = 13;  // phase bucket of instances waiting for the cluster PCG kernel
 
 PHX_HD inline int64_t sell_addr(int64_t s, int e) { return (s >> 5) * 288 + (int64_t)e * 32 + (s & 31); }
 
