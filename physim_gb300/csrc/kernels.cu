@@ -72,28 +72,53 @@ __device__ __forceinline__ void count_bytes(const BatchDev& B, const InstDev& I,
   if (B.algo_total) B.algo_total[k] += I.algo[k];  // single thread of the finalising CTA
 }
 
-// Records this tile's partial sums; in the CTA that completes the instance's
-// last tile, returns true and leaves the instance totals in thread 0's tot[].
+// Records this tile's partial sums; in the CTA that completes the instance's last tile,
+// returns true and leaves the instance totals in thread 0's tot[].  Tiles are dealt to the
+// ncta CTAs round-robin (t = cta, cta + ncta, ...), and the instance's tiles are
+// contiguous, so a CTA's last tile of the instance is the one with lt + ncta >= ntiles and
+// it has then done lt / ncta + 1 of them: only that tile publishes the count, with one
+// fence and one atomic per CTA and instance instead of per tile.  The totals are summed
+// from the per-tile partials in tile order, whatever the CTA count.
 template <int K>
-__device__ bool tile_done(const InstDev& I, int lt, int ntiles, double (&v)[K], double (&tot)[K],
+__device__ bool tile_done(const InstDev& I, int lt, int ntiles, int ncta, double (&v)[K], double (&tot)[K],
                           double* sm, int* flag) {
   block_sum<K>(v, sm);
+  const bool last_here = lt + ncta >= ntiles;
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int k = 0; k < K; ++k) I.partials[(size_t)lt * K + k] = v[k];
-    __threadfence();
-    unsigned prev = atomicAdd(I.counter, 1u);
-    *flag = (prev == (unsigned)(ntiles - 1));
+    if (last_here) {
+      const unsigned mine = (unsigned)(lt / ncta + 1);
+      __threadfence();
+      const unsigned prev = atomicAdd(I.counter, mine);
+      *flag = (prev + mine == (unsigned)ntiles);
+    }
   }
+  if (!last_here) return false;
   __syncthreads();
   if (!*flag) return false;
   __threadfence();
-  double acc[K];
+  // four independent running sums per thread (tiles t, t + bd, t + 2 bd, t + 3 bd) keep
+  // four loads in flight: an instance with thousands of tiles is summed by one CTA while
+  // the others wait at the next barrier.  The order depends on the tile count only.
+  double acc[K], a1[K], a2[K], a3[K];
 #pragma unroll
-  for (int k = 0; k < K; ++k) acc[k] = 0.0;
-  for (int t = threadIdx.x; t < ntiles; t += blockDim.x)
+  for (int k = 0; k < K; ++k) acc[k] = a1[k] = a2[k] = a3[k] = 0.0;
+  const int bd = blockDim.x;
+  int t = threadIdx.x;
+  for (; t + 3 * bd < ntiles; t += 4 * bd)
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      acc[k] += __ldcg(I.partials + (size_t)t * K + k);
+      a1[k] += __ldcg(I.partials + (size_t)(t + bd) * K + k);
+      a2[k] += __ldcg(I.partials + (size_t)(t + 2 * bd) * K + k);
+      a3[k] += __ldcg(I.partials + (size_t)(t + 3 * bd) * K + k);
+    }
+  for (; t < ntiles; t += bd)
 #pragma unroll
     for (int k = 0; k < K; ++k) acc[k] += __ldcg(I.partials + (size_t)t * K + k);
+#pragma unroll
+  for (int k = 0; k < K; ++k) acc[k] = (acc[k] + a1[k]) + (a2[k] + a3[k]);
   block_sum<K>(acc, sm);
   if (threadIdx.x == 0) {
 #pragma unroll
@@ -307,7 +332,7 @@ __device__ __forceinline__ void st_vecop(const BatchDev& B, const TileMap& M, in
       }
     }
     double p[1] = {0.0}, tot[1];
-    if (tile_done<1>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
+    if (tile_done<1>(I, lt, tiles_of(I.n), ncta, p, tot, sm, &flag) && threadIdx.x == 0) {
       count_bytes(B, I, K_VECOP);
       st->phase = st->next_phase;
       st->vecop = 0;
@@ -426,7 +451,7 @@ __device__ __forceinline__ void st_elem_eg(const BatchDev& B, const TileMap& M, 
       I.Eloc[e] = Ee;
     }
     double p[1] = {Ee}, tot[1];
-    if (tile_done<1>(I, lt, tiles_of(I.m), p, tot, sm, &flag) && threadIdx.x == 0) {
+    if (tile_done<1>(I, lt, tiles_of(I.m), ncta, p, tot, sm, &flag) && threadIdx.x == 0) {
       count_bytes(B, I, K_ELEM_EG);
       st->E_el = tot[0];
     }
@@ -484,7 +509,7 @@ __device__ __forceinline__ void st_gather(const BatchDev& B, const TileMap& M, i
       p[1] = g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
     }
     double tot[2];
-    if (tile_done<2>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
+    if (tile_done<2>(I, lt, tiles_of(I.n), ncta, p, tot, sm, &flag) && threadIdx.x == 0) {
       count_bytes(B, I, K_GATHER);
       st->E_eval = st->E_el + tot[0];
       st->gg_eval = tot[1];
@@ -580,7 +605,7 @@ __device__ __forceinline__ void st_assemble(const BatchDev& B, const TileMap& M,
       nrm += (double)s * (double)s;
     }
     double p[1] = {nrm}, tot[1];
-    if (tile_done<1>(I, lt, tiles_of(I.nlo), p, tot, sm, &flag) && threadIdx.x == 0) {
+    if (tile_done<1>(I, lt, tiles_of(I.nlo), ncta, p, tot, sm, &flag) && threadIdx.x == 0) {
       count_bytes(B, I, K_ELEM_HESS);  // the element kernel ran on this instance in the same round
       count_bytes(B, I, K_ASSEMBLE);
       st->normA2 = tot[0];
@@ -638,7 +663,7 @@ __device__ __forceinline__ void st_jacobi(const BatchDev& B, const TileMap& M, i
       for (int k = 0; k < 9; ++k) Mi[(size_t)k * I.n + v] = (Real)inv[k];
     }
     double p[1] = {0.0}, tot[1];
-    if (tile_done<1>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
+    if (tile_done<1>(I, lt, tiles_of(I.n), ncta, p, tot, sm, &flag) && threadIdx.x == 0) {
       count_bytes(B, I, K_JACOBI);
       st->phase = PH_LINSETUP;
       advance(B, i);
@@ -674,7 +699,7 @@ __device__ __forceinline__ void st_linsetup(const BatchDev& B, const TileMap& M,
       p[0] = g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
     }
     double tot[1];
-    if (tile_done<1>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
+    if (tile_done<1>(I, lt, tiles_of(I.n), ncta, p, tot, sm, &flag) && threadIdx.x == 0) {
       count_bytes(B, I, K_LINSETUP);
       const double tol = st->lin_tol;
       st->bb = tot[0];
@@ -735,9 +760,10 @@ __device__ __forceinline__ void sell_row(const InstDev& I, const Real* H, int v,
 }
 
 // L lanes per row (L = 1, 2 or 4; lanes L*r .. L*r+L-1 of the calling warp share row v):
-// lane `sub` takes slots sub, sub+L, ..., so with L = 4 a row costs about two dependent
-// memory round trips; the partial sums are combined with xor-shuffles and every lane of
-// the group ends with the full row.  Used where a few rows per instance must finish fast.
+// lane `sub` takes slots sub, sub+L, ..., four at a time -- their column ids and blocks
+// are loaded together, then the four gathers, then the arithmetic -- so four slots cost
+// two dependent memory round trips; the partial sums are combined with xor-shuffles and
+// every lane of the group ends with the full row.
 template <int L, typename Real, typename Acc, typename GetX>
 __device__ __forceinline__ void sell_row_lanes(const InstDev& I, const Real* H, int v, int sub, bool valid, GetX getx,
                                                Acc (&acc)[3]) {
@@ -746,18 +772,32 @@ __device__ __forceinline__ void sell_row_lanes(const InstDev& I, const Real* H, 
     const int c = v >> 5, lane = v & 31;
     const int s0 = __ldg(I.chunk_off + c);
     const int len = (__ldg(I.chunk_off + c + 1) - s0) >> 5;
-#pragma unroll(L == 1 ? 4 : 1)
-    for (int k = sub; k < len; k += L) {
-      const int64_t s = (int64_t)s0 + k * 32 + lane;
-      const int col = __ldg(I.slot_col + s);
-      const Real* hp = H + (s >> 5) * 288 + (s & 31);
-      Acc h[9];
+    for (int k0 = sub; k0 < len; k0 += 4 * L) {
+      int col[4];
+      Acc h[4][9];
 #pragma unroll
-      for (int q = 0; q < 9; ++q) h[q] = (Acc)hp[q * 32];
-      Acc xc[3];
-      getx(col, xc);
+      for (int u = 0; u < 4; ++u) {
+        const int k = k0 + u * L;
+        const bool in = k < len;
+        const int64_t s = (int64_t)s0 + (int64_t)(in ? k : 0) * 32 + lane;
+        col[u] = in ? __ldg(I.slot_col + s) : -1;
+        const Real* hp = H + (s >> 5) * 288 + (s & 31);
 #pragma unroll
-      for (int a = 0; a < 3; ++a) acc[a] += h[3 * a] * xc[0] + h[3 * a + 1] * xc[1] + h[3 * a + 2] * xc[2];
+        for (int q = 0; q < 9; ++q) h[u][q] = in ? (Acc)hp[q * 32] : (Acc)0;
+      }
+      Acc xc[4][3];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (col[u] >= 0) {
+          getx(col[u], xc[u]);
+        } else {
+          xc[u][0] = xc[u][1] = xc[u][2] = (Acc)0;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) acc[a] += h[u][3 * a] * xc[u][0] + h[u][3 * a + 1] * xc[u][1] + h[u][3 * a + 2] * xc[u][2];
     }
   }
 #pragma unroll
@@ -813,7 +853,7 @@ __device__ __forceinline__ void st_resid(const BatchDev& B, const TileMap& M, in
       p[4] = (double)(rr_[0] * rr_[0] + rr_[1] * rr_[1] + rr_[2] * rr_[2]);
     }
     double tot[5];
-    if (tile_done<5>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
+    if (tile_done<5>(I, lt, tiles_of(I.n), ncta, p, tot, sm, &flag) && threadIdx.x == 0) {
       count_bytes(B, I, K_RESID);
       st->rr64 = tot[0];
       st->b_dot_dx = tot[1];
@@ -895,7 +935,7 @@ __device__ __forceinline__ void st_pcg_a(const BatchDev& B, const TileMap& M, in
       }
     }
     double tot[1];
-    if (tile_done<1>(I, lt, pcg_tiles(B, I), p, tot, sm, &flag) && threadIdx.x == 0) {
+    if (tile_done<1>(I, lt, pcg_tiles(B, I), ncta, p, tot, sm, &flag) && threadIdx.x == 0) {
       count_bytes(B, I, K_PCG_A);
       st->pq = tot[0];
       if (!(tot[0] > 0.0)) {  // not positive definite along p (or non-finite)
@@ -957,7 +997,7 @@ __device__ __forceinline__ void st_pcg_b(const BatchDev& B, const TileMap& M, in
       p[1] = (double)rv[0] * z[0] + (double)rv[1] * z[1] + (double)rv[2] * z[2];
     }
     double tot[2];
-    if (tile_done<2>(I, lt, pcg_tiles(B, I), p, tot, sm, &flag) && threadIdx.x == 0) {
+    if (tile_done<2>(I, lt, pcg_tiles(B, I), ncta, p, tot, sm, &flag) && threadIdx.x == 0) {
       count_bytes(B, I, K_PCG_B);
       st->pcg_iter++;
       st->pcg_total++;
@@ -1009,7 +1049,7 @@ __device__ __forceinline__ void st_accum(const BatchDev& B, const TileMap& M, in
       st4(I.dx, v, d);
     }
     double p[1] = {0.0}, tot[1];
-    if (tile_done<1>(I, lt, tiles_of(I.n), p, tot, sm, &flag) && threadIdx.x == 0) {
+    if (tile_done<1>(I, lt, tiles_of(I.n), ncta, p, tot, sm, &flag) && threadIdx.x == 0) {
       count_bytes(B, I, K_ACCUM);
       st->sweeps++;
       st->total_sweeps++;
