@@ -182,12 +182,21 @@ def batch_meshes(count, seed):
     return [M.batch_instance(seed, i) for i in range(count)]
 
 
+def served_options(px, args):
+    """Served path: FP32 Hessian + PCG with FP64 refinement; the same PCG budget per Newton step
+    as the plain path (served_sweeps x served_pcg_max = plain_pcg_max), fewer, longer sweeps."""
+    return px.options(precision=px.PREC_FP32_REFINE, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0,
+                      tol_min_step=0.0, pcg_chunk=args.pcg_chunk, inner_tol=args.inner_tol,
+                      ls_num_max_iters=args.served_pcg_max, max_refine_sweeps=args.served_sweeps)
+
+
 def batch_config(args, count, tets):
     return {"workload": f"batched uneven boxes: {count} instances, 6-tet hexes, {tets} tets", "instances": count,
             "tets": tets, "tol_rel": args.tol_rel,
             "l2": "inputs larger than L2 (per-step working set well above 129 MB)",
             "inner_tol": args.inner_tol, "pcg_chunk": args.pcg_chunk,
-            "plain_pcg_max_per_newton_step": args.plain_pcg_max}
+            "plain_pcg_max_per_newton_step": args.plain_pcg_max,
+            "served_pcg_per_sweep_x_sweeps": [args.served_pcg_max, args.served_sweeps]}
 
 
 def run_batch(args, world, rank, dist):
@@ -199,8 +208,7 @@ def run_batch(args, world, rank, dist):
     tets = sum(m.m for m in meshes)
     ctx = px.Context(0, arena_bytes=int(args.arena_gb * (1 << 30)))
     insts = [px.Instance(ctx, m) for m in meshes]
-    served = px.options(precision=px.PREC_FP32_REFINE, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0,
-                        tol_min_step=0.0, pcg_chunk=args.pcg_chunk, inner_tol=args.inner_tol)
+    served = served_options(px, args)
     plain = px.options(precision=px.PREC_FP64, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0,
                        tol_min_step=0.0, pcg_chunk=args.pcg_chunk, ls_num_max_iters=args.plain_pcg_max)
 
@@ -539,8 +547,7 @@ def run_serve(args, world, rank, dist, rates=None, count=None, source="stream"):
     for i, (mesh, base) in enumerate(reqs):
         if base is None:
             insts[i] = px.Instance(ctx, mesh)
-    served = px.options(precision=px.PREC_FP32_REFINE, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0,
-                        tol_min_step=0.0)
+    served = served_options(px, args)
     plain = px.options(precision=px.PREC_FP64, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0,
                        tol_min_step=0.0, ls_num_max_iters=args.plain_pcg_max)
     budget = int(min(150.0, 0.9 * args.arena_gb) * (1 << 30))
@@ -603,6 +610,8 @@ def run_large(args, world, rank, dist):
         o = px.options(precision=prec, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0, tol_min_step=0.0)
         if prec == px.PREC_FP64:
             o.ls_num_max_iters = args.plain_pcg_max
+        else:
+            o = served_options(px, args)
         inst.reset()
         ctx.profile(True)
         ctx.profile_reset()
@@ -649,6 +658,8 @@ def run_dynamics(args, world, rank, dist):
         o = px.options(precision=prec, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0, tol_min_step=0.0)
         if prec == px.PREC_FP64:
             o.ls_num_max_iters = args.plain_pcg_max
+        else:
+            o = served_options(px, args)
         ctx.mark(0)
         reps_all = []
         xs = []
@@ -692,9 +703,11 @@ def main():
     ap.add_argument("--slots", type=int, default=256)
     ap.add_argument("--dyn-instances", type=int, default=16)
     ap.add_argument("--dyn-steps", type=int, default=10)
+    ap.add_argument("--served-pcg-max", type=int, default=3000)
+    ap.add_argument("--served-sweeps", type=int, default=4)
     ap.add_argument("--plain-pcg-max", type=int, default=12000,
                     help="PCG iterations per Newton step of the plain FP64 path (the served path's budget is "
-                         "max_refine_sweeps x ls_num_max_iters = 12 x 1000)")
+                         "served_sweeps x served_pcg_max = 4 x 3000)")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--batch-rate", type=float, default=200.0)
     ap.add_argument("--batch-requests", type=int, default=64)

@@ -104,7 +104,9 @@ typedef struct phx_options {
                                  1 rows in shared memory, z exchanged through distributed shared
                                  memory (default); 2 rows in L2, two-reduction CG; 0: every PCG
                                  iteration runs on the whole GPU */
-  int32_t reserved0;
+  int32_t fp64_finish;        /* 1 (default): an FP32 solve that stalls (line search, progress or iteration
+                                 limit) within 1000x of its tolerance is finished in FP64 from the
+                                 iterate it stopped at, to the same tolerance; static solves only */
 } phx_options;
 
 typedef struct phx_report {
@@ -120,7 +122,7 @@ typedef struct phx_report {
   double opt0;              /* ||g|| at the first step (after the loads are applied) */
   double seconds;           /* wall time of the call */
   int32_t hessian_evals;    /* element Hessian + assembly passes */
-  int32_t reserved;
+  int32_t fp64_iterations;  /* Newton iterations of the FP64 finish (0: none); included in iterations */
 } phx_report;
 
 /* ---- library ----------------------------------------------------------- */

@@ -60,14 +60,14 @@ class Options(C.Structure):
                 ("lsearch_alpha", C.c_double), ("lsearch_num_try", C.c_int32), ("precision", C.c_int32),
                 ("precond", C.c_int32), ("inner_tol", C.c_double), ("max_refine_sweeps", C.c_int32),
                 ("warm_guess", C.c_int32), ("pcg_chunk", C.c_int32), ("tol_rel", C.c_double),
-                ("pcg_cluster", C.c_int32), ("reserved0", C.c_int32)]
+                ("pcg_cluster", C.c_int32), ("fp64_finish", C.c_int32)]
 
 
 class Report(C.Structure):
     _fields_ = [("result", C.c_int32), ("iterations", C.c_int32), ("bisections", C.c_int32),
                 ("reg_trials", C.c_int32), ("pcg_iterations", C.c_int64), ("refine_sweeps", C.c_int32),
                 ("status", C.c_int32), ("obj", C.c_double), ("opt", C.c_double), ("opt0", C.c_double),
-                ("seconds", C.c_double), ("hessian_evals", C.c_int32), ("reserved", C.c_int32)]
+                ("seconds", C.c_double), ("hessian_evals", C.c_int32), ("fp64_iterations", C.c_int32)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}

@@ -377,6 +377,7 @@ int validate_opts(const phx_options* o) {
   if (o->pcg_chunk < 1 || o->pcg_chunk > 4096) return set_err(PHX_EINVAL, "options: pcg_chunk out of [1,4096]");
   if (!(o->tol_rel >= 0.0)) return set_err(PHX_EINVAL, "options: tol_rel must be >= 0");
   if (o->pcg_cluster < 0 || o->pcg_cluster > 2) return set_err(PHX_EINVAL, "options: pcg_cluster must be 0, 1 or 2");
+  if (o->fp64_finish < 0 || o->fp64_finish > 1) return set_err(PHX_EINVAL, "options: fp64_finish must be 0 or 1");
   return PHX_OK;
 }
 
@@ -430,7 +431,23 @@ void fill_report(const NState& s, bool step, double seconds, phx_report* r) {
   r->opt0 = s.opt0;
   r->seconds = seconds;
   r->hessian_evals = s.hess_count;
-  r->reserved = 0;
+  r->fp64_iterations = 0;
+}
+
+// Report of a static solve that an FP64 finish continued: counts of both parts, the
+// result, energy and gradient of the finish, the starting gradient of the first.
+void fill_report_finished(const NState& a, const NState& b, double seconds, phx_report* r) {
+  if (!r) return;
+  fill_report(b, false, seconds, r);
+  r->iterations += a.it;
+  r->bisections += a.total_bis;
+  r->reg_trials += a.total_reg;
+  r->pcg_iterations += a.pcg_total;
+  r->refine_sweeps += a.total_sweeps;
+  r->hessian_evals += a.hess_count;
+  r->opt0 = a.opt0;
+  r->fp64_iterations = b.it;
+  if (a.error) r->status = PHX_ETIMEOUT;
 }
 
 int ensure_engine(phx_context ctx) {
@@ -592,6 +609,37 @@ int start_solve(phx_instance inst, const phx_options* o, bool dynamic, double dt
   return PHX_OK;
 }
 
+// FP32 solves that stall within kFinishFactor of their tolerance: the FP32-stored Hessian
+// makes Newton converge linearly there, and near an equilibrium the energy decrease of
+// a step can fall below the FP64 energy comparison's resolution before the gradient
+// meets a tolerance taken relative to a small starting gradient (warm re-solves).
+constexpr double kFinishFactor = 1e3;
+
+bool wants_fp64_finish(const phx_options* o, const NState& s) {
+  if (!o->fp64_finish || o->precision != PHX_PREC_FP32_REFINE || s.error) return false;
+  const bool stalled = s.result == OS_NONDESC || s.result == OS_MINIMPR || s.result == OS_MINSTEP ||
+                       s.result == OS_MAXITER;
+  return stalled && std::isfinite(s.opt) && s.opt <= kFinishFactor * s.tol_eff;
+}
+
+// Continues the listed FP32 solves in FP64 from the iterates they stopped at, to the
+// same absolute tolerance, with the FP32 solve's PCG budget per Newton step in one solve.
+int finish_fp64(phx_context ctx, const std::vector<phx_instance>& list, const phx_options* o,
+                const std::vector<NState>& first, std::vector<NState>* second) {
+  for (size_t k = 0; k < list.size(); ++k) {
+    phx_options f = *o;
+    f.precision = PHX_PREC_FP64;
+    f.tol_rel = 0.0;
+    f.tol_max_error = first[k].tol_eff;
+    f.ls_num_max_iters = o->ls_num_max_iters * std::max(1, o->max_refine_sweeps);
+    TRY(start_solve(list[k], &f, false, 0.0, 0));
+  }
+  TRY(run_to_completion(ctx, list, true, o->pcg_chunk));
+  second->resize(list.size());
+  for (size_t k = 0; k < list.size(); ++k) TRY(read_state(list[k], &(*second)[k]));
+  return PHX_OK;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -630,7 +678,7 @@ void phx_default_options(phx_options* o) {
   o->pcg_chunk = 32;
   o->tol_rel = 0.0;
   o->pcg_cluster = 1;
-  o->reserved0 = 0;
+  o->fp64_finish = 1;
 }
 
 int phx_context_create(int32_t device, int64_t arena_bytes, phx_context* out) {
@@ -1018,6 +1066,13 @@ int phx_solve_static(phx_instance inst, const phx_options* o, double* x, phx_rep
   TRY(run_to_completion(inst->ctx, {inst}, o->precision == PHX_PREC_FP64, o->pcg_chunk));
   NState s;
   TRY(read_state(inst, &s));
+  if (wants_fp64_finish(o, s)) {
+    std::vector<NState> second;
+    TRY(finish_fp64(inst->ctx, {inst}, o, {s}, &second));
+    if (x) TRY(download_x(inst, inst->dev.x, x));
+    fill_report_finished(s, second[0], std::chrono::duration<double>(clk::now() - t0).count(), rep);
+    return PHX_OK;
+  }
   if (x) TRY(download_x(inst, inst->dev.x, x));
   fill_report(s, false, std::chrono::duration<double>(clk::now() - t0).count(), rep);
   return PHX_OK;
@@ -1069,12 +1124,24 @@ int phx_batch_solve(phx_context ctx, int32_t count, phx_instance* insts, const p
   }
   if (count == 0) return PHX_OK;
   TRY(run_to_completion(ctx, list, o->precision == PHX_PREC_FP64, o->pcg_chunk));
+  std::vector<NState> st(count), fin_first, fin_second;
+  std::vector<phx_instance> fin;
+  std::vector<int> fin_at(count, -1);
+  for (int i = 0; i < count; ++i) {
+    TRY(read_state(list[i], &st[i]));
+    if (wants_fp64_finish(o, st[i])) {
+      fin_at[i] = (int)fin.size();
+      fin.push_back(list[i]);
+      fin_first.push_back(st[i]);
+    }
+  }
+  if (!fin.empty()) TRY(finish_fp64(ctx, fin, o, fin_first, &fin_second));
   double secs = std::chrono::duration<double>(clk::now() - t0).count();
   for (int i = 0; i < count; ++i) {
-    NState s;
-    TRY(read_state(list[i], &s));
     if (x && x[i]) TRY(download_x(list[i], list[i]->dev.x, x[i]));
-    if (reps) fill_report(s, false, secs, &reps[i]);
+    if (!reps) continue;
+    if (fin_at[i] >= 0) fill_report_finished(st[i], fin_second[fin_at[i]], secs, &reps[i]);
+    else fill_report(st[i], false, secs, &reps[i]);
   }
   return PHX_OK;
 }
@@ -1162,12 +1229,18 @@ int phx_server_progress(phx_server s, int32_t* active, int32_t* queued) {
   if (!s) return set_err(PHX_EINVAL, "server is NULL");
   // retire finished requests (phases from the last round of this server)
   if (!s->active.empty() && !s->dirty && s->ctx->batch_owner == s) {
-    std::vector<phx_server_s::Req> keep;
+    std::vector<phx_server_s::Req> keep, fin;
+    std::vector<NState> fin_first, fin_second;
     for (size_t i = 0; i < s->active.size(); ++i) {
       if (s->ctx->h_flags[8 + i] == PH_DONE) {
         auto& r = s->active[i];
         NState st;
         TRY(read_state(r.inst, &st));
+        if (wants_fp64_finish(&s->opts, st)) {  // finished in FP64 below, then retired
+          fin.push_back(r);
+          fin_first.push_back(st);
+          continue;
+        }
         phx_report rep{};
         fill_report(st, false, std::chrono::duration<double>(clk::now() - r.t_submit).count(), &rep);
         s->done.push_back({r.tag, rep});
@@ -1179,6 +1252,20 @@ int phx_server_progress(phx_server s, int32_t* active, int32_t* queued) {
       }
     }
     s->active.swap(keep);
+    if (!fin.empty()) {
+      std::vector<phx_instance> insts;
+      for (auto& r : fin) insts.push_back(r.inst);
+      TRY(finish_fp64(s->ctx, insts, &s->opts, fin_first, &fin_second));
+      for (size_t k = 0; k < fin.size(); ++k) {
+        phx_report rep{};
+        fill_report_finished(fin_first[k], fin_second[k],
+                             std::chrono::duration<double>(clk::now() - fin[k].t_submit).count(), &rep);
+        s->done.push_back({fin[k].tag, rep});
+        fin[k].inst->in_server = false;
+        s->in_use -= fin[k].inst->bytes;
+      }
+      s->dirty = true;  // the FP64 finish used the context's batch buffers
+    }
   }
   // admit queued requests at this Newton-round boundary (slots + memory budget)
   while (!s->queue.empty() && (int)s->active.size() < s->max_slots) {

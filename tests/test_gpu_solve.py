@@ -197,3 +197,28 @@ def test_warm_resolve_after_load_update(gpu_ctx):
     assert r2["result_name"] == "SUCCESS"
     assert r2["iterations"] <= r1["iterations"]
     assert disp_err(x2, xr, x0) < 1e-6
+
+
+def test_fp32_stall_finishes_in_fp64(gpu_ctx):
+    """A warm re-solve at a tolerance below what FP32-Hessian Newton reaches: the FP32 solve
+    stalls near its tolerance and the FP64 finish takes it the rest of the way."""
+    m = M.serving_request(11, 2)
+    inst = px.Instance(gpu_ctx, m)
+    base = dict(tol_max_error=0.0, tol_min_impr=0.0, tol_min_step=0.0)
+    inst.solve_static(px.options(precision=px.PREC_FP64, tol_rel=1e-10, **base), m.X0.ravel())
+    m2 = M.perturb_load(m, 11, 2)
+    inst.update_load(m2.force, m2.gravity)
+    x_start = inst.positions()
+    o = px.options(precision=px.PREC_FP32_REFINE, tol_rel=1e-8, **base)
+    x2, r2 = inst.solve_static(o, x_start)
+    assert r2["result_name"] == "SUCCESS", r2
+    assert r2["opt"] <= 1e-8 * r2["opt0"] * (1 + 1e-12)
+    assert 0 <= r2["fp64_iterations"] <= r2["iterations"]
+    orc, x0, g0, xr, _ = oracle_solution(m2, 1e-10)
+    assert disp_err(x2, xr, x0) < 1e-6
+    # without the finish the same solve reports where FP32 stopped
+    o.fp64_finish = 0
+    _, r3 = inst.solve_static(o, x_start)
+    assert r3["fp64_iterations"] == 0
+    if r2["fp64_iterations"] > 0:
+        assert r3["result_name"] != "SUCCESS"
