@@ -105,8 +105,9 @@ typedef struct phx_options {
                                  memory (default); 2 rows in L2, two-reduction CG; 0: every PCG
                                  iteration runs on the whole GPU */
   int32_t fp64_finish;        /* 1 (default): an FP32 solve that stalls (line search, progress or iteration
-                                 limit) within 1000x of its tolerance is finished in FP64 from the
-                                 iterate it stopped at, to the same tolerance; static solves only */
+                                 limit) within 1000x of its tolerance, or after reducing ||g|| a
+                                 hundredfold, is finished in FP64 from the iterate it stopped at, to
+                                 the same tolerance; static solves only */
 } phx_options;
 
 typedef struct phx_report {

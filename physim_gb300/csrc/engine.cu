@@ -609,7 +609,8 @@ int start_solve(phx_instance inst, const phx_options* o, bool dynamic, double dt
   return PHX_OK;
 }
 
-// FP32 solves that stall within kFinishFactor of their tolerance: the FP32-stored Hessian
+// FP32 solves that stall within kFinishFactor of their tolerance, or after reducing the
+// gradient a hundredfold: the FP32-stored Hessian
 // makes Newton converge linearly there, and near an equilibrium the energy decrease of
 // a step can fall below the FP64 energy comparison's resolution before the gradient
 // meets a tolerance taken relative to a small starting gradient (warm re-solves).
@@ -619,7 +620,8 @@ bool wants_fp64_finish(const phx_options* o, const NState& s) {
   if (!o->fp64_finish || o->precision != PHX_PREC_FP32_REFINE || s.error) return false;
   const bool stalled = s.result == OS_NONDESC || s.result == OS_MINIMPR || s.result == OS_MINSTEP ||
                        s.result == OS_MAXITER;
-  return stalled && std::isfinite(s.opt) && s.opt <= kFinishFactor * s.tol_eff;
+  // close to the tolerance, or well on the way there (diverged solves stay failures)
+  return stalled && std::isfinite(s.opt) && (s.opt <= kFinishFactor * s.tol_eff || s.opt <= 1e-2 * s.opt0);
 }
 
 // Continues the listed FP32 solves in FP64 from the iterates they stopped at, to the

@@ -209,10 +209,10 @@ def test_fp32_stall_finishes_in_fp64(gpu_ctx):
     m2 = M.perturb_load(m, 11, 2)
     inst.update_load(m2.force, m2.gravity)
     x_start = inst.positions()
-    o = px.options(precision=px.PREC_FP32_REFINE, tol_rel=1e-8, **base)
+    o = px.options(precision=px.PREC_FP32_REFINE, tol_rel=1e-7, **base)
     x2, r2 = inst.solve_static(o, x_start)
     assert r2["result_name"] == "SUCCESS", r2
-    assert r2["opt"] <= 1e-8 * r2["opt0"] * (1 + 1e-12)
+    assert r2["opt"] <= 1e-7 * r2["opt0"] * (1 + 1e-12)
     assert 0 <= r2["fp64_iterations"] <= r2["iterations"]
     orc, x0, g0, xr, _ = oracle_solution(m2, 1e-10)
     assert disp_err(x2, xr, x0) < 1e-6
