@@ -115,8 +115,9 @@ def dist_setup():
     if world > 1:
         import torch
         import torch.distributed as dist
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-        torch.cuda.set_device(local)
     return world, rank, local, dist
 
 
@@ -206,7 +207,7 @@ def run_batch(args, world, rank, dist):
     count = args.count
     meshes = batch_meshes(count, seed=3 + 1000 * rank)
     tets = sum(m.m for m in meshes)
-    ctx = px.Context(0, arena_bytes=int(args.arena_gb * (1 << 30)))
+    ctx = px.Context(args.device, arena_bytes=int(args.arena_gb * (1 << 30)))
     insts = [px.Instance(ctx, m) for m in meshes]
     served = served_options(px, args)
     plain = px.options(precision=px.PREC_FP64, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0,
@@ -415,7 +416,7 @@ def run_cantilever(args, world, rank, dist):
     from physim_gb300 import build, mesh as M
     build.build()
     m = M.cantilever()
-    ctx = px.Context(0, arena_bytes=4 << 30)
+    ctx = px.Context(args.device, arena_bytes=4 << 30)
     inst = px.Instance(ctx, m)
     x0 = m.X0.ravel().copy()
     o = px.options(precision=px.PREC_FP64, tol_rel=1e-8, tol_max_error=0.0, tol_min_impr=0.0, tol_min_step=0.0,
@@ -542,7 +543,7 @@ def run_serve(args, world, rank, dist, rates=None, count=None, source="stream"):
         reqs = [(M.batch_instance(3, i), None) for i in range(count)]
     else:
         reqs = serving_requests(count, seed=11)
-    ctx = px.Context(0, arena_bytes=int(args.arena_gb * (1 << 30)))
+    ctx = px.Context(args.device, arena_bytes=int(args.arena_gb * (1 << 30)))
     insts = {}
     for i, (mesh, base) in enumerate(reqs):
         if base is None:
@@ -603,7 +604,7 @@ def run_large(args, world, rank, dist):
     from physim_gb300 import build, mesh as M
     build.build()
     m = M.cantilever(48, 48, 192, seed=7)
-    ctx = px.Context(0, arena_bytes=int(args.arena_gb * (1 << 30)))
+    ctx = px.Context(args.device, arena_bytes=int(args.arena_gb * (1 << 30)))
     inst = px.Instance(ctx, m)
     res = {}
     for name, prec in (("served_fp32_refine", px.PREC_FP32_REFINE), ("plain_fp64", px.PREC_FP64)):
@@ -647,7 +648,7 @@ def run_dynamics(args, world, rank, dist):
     build.build()
     n_inst = args.dyn_instances
     meshes = [M.slab_block(5, i) for i in range(n_inst)]
-    ctx = px.Context(0, arena_bytes=int(args.arena_gb * (1 << 30)))
+    ctx = px.Context(args.device, arena_bytes=int(args.arena_gb * (1 << 30)))
     res = {}
     traj = {}
     for name, prec in (("served_fp32_refine", px.PREC_FP32_REFINE), ("plain_fp64", px.PREC_FP64)):
@@ -722,6 +723,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     world, rank, local, dist = dist_setup()
+    args.device = local  # one replica per GPU: this rank's library context lives on its own device
     if args.impl == "reference":
         out = run_reference(args, world, rank)
         if out is not None:
