@@ -106,8 +106,9 @@ typedef struct phx_options {
                                  iteration runs on the whole GPU */
   int32_t fp64_finish;        /* 1 (default): an FP32 solve that stalls (line search, progress or iteration
                                  limit) within 1000x of its tolerance, or after reducing ||g|| a
-                                 hundredfold, is finished in FP64 from the iterate it stopped at, to
-                                 the same tolerance; static solves only */
+                                 hundredfold, is finished in FP64 from its last accepted iterate with
+                                 ||g|| above 100x the tolerance, to the same tolerance; static solves
+                                 only */
 } phx_options;
 
 typedef struct phx_report {

@@ -624,11 +624,18 @@ bool wants_fp64_finish(const phx_options* o, const NState& s) {
   return stalled && std::isfinite(s.opt) && (s.opt <= kFinishFactor * s.tol_eff || s.opt <= 1e-2 * s.opt0);
 }
 
-// Continues the listed FP32 solves in FP64 from the iterates they stopped at, to the
-// same absolute tolerance, with the FP32 solve's PCG budget per Newton step in one solve.
+// Continues the listed FP32 solves in FP64 from their restart points (the last accepted
+// iterate with ||g|| above kBackFactor x tolerance), to the same absolute tolerance, with
+// the FP32 solve's PCG budget per Newton step in one solve.
 int finish_fp64(phx_context ctx, const std::vector<phx_instance>& list, const phx_options* o,
                 const std::vector<NState>& first, std::vector<NState>* second) {
   for (size_t k = 0; k < list.size(); ++k) {
+    // restart from the last accepted iterate whose gradient was well above the tolerance:
+    // the iterate FP32 stalled at can sit where the energy comparison no longer resolves a
+    // step, which an exact Newton step from the restart point jumps over
+    InstDev& D = list[k]->dev;
+    if (!(first[k].opt > kBackFactor * first[k].tol_eff))  // else the last iterate itself is the restart point
+      CU(cudaMemcpyAsync(D.x, D.xback, 4 * sizeof(double) * (size_t)D.n, cudaMemcpyDeviceToDevice, ctx->stream));
     phx_options f = *o;
     f.precision = PHX_PREC_FP64;
     f.tol_rel = 0.0;
@@ -811,7 +818,7 @@ int phx_instance_create(phx_context ctx, const phx_mesh* mesh, phx_instance* out
     if ((rc = arena_alloc(inst, &xr, n4, true))) return fail(rc);
     D.xrest = xr;
   }
-  double** vecs[] = {&D.x, &D.xs, &D.dx, &D.g, &D.gn, &D.dxprev, &D.x0, &D.v0, &D.v, &D.r64, &D.bvec};
+  double** vecs[] = {&D.x, &D.xs, &D.dx, &D.g, &D.gn, &D.dxprev, &D.x0, &D.v0, &D.v, &D.r64, &D.bvec, &D.xback};
   for (double** pv : vecs)
     if ((rc = arena_alloc(inst, pv, n4, true))) return fail(rc);
   if ((rc = arena_alloc(inst, &D.Eloc, (size_t)hp.m))) return fail(rc);

@@ -308,6 +308,11 @@ __device__ __forceinline__ void st_vecop(const BatchDev& B, const TileMap& M, in
         for (int c = 0; c < 3; ++c) tmp2[c] = a * dx[c];
         st4(I.dxprev, v, tmp2);
       }
+      if (ops & VO_GCOPY) st4(I.xback, v, x);  // start of a solve
+      if (ops & VO_BACK) {                      // the accepted iterate being left
+        ld4(I.xs, v, tmp2);
+        st4(I.xback, v, tmp2);
+      }
       if (ops & VO_SAVE) st4(I.xs, v, x);
       if (ops & VO_ZERODX) {
         for (int c = 0; c < 3; ++c) tmp[c] = 0.0;

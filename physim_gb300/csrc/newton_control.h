@@ -20,6 +20,8 @@
 
 namespace phx {
 
+constexpr double kBackFactor = 1e2;  // restart points of the FP64 finish: ||g|| above this x tolerance
+
 enum OSResult : int32_t { OS_ONGOING = 0, OS_SUCCESS = 1, OS_MINSTEP = 2, OS_MINIMPR = 3,
                           OS_FAILURE = 4, OS_MAXITER = 5, OS_NONDESC = 6 };
 
@@ -170,12 +172,16 @@ PHX_HD inline void ctl_ls_check(NState& s, const DevOpts& o) {
       s.min_step_count = 0;
     }
     s.step_result = s.result;
+    // the iterate being left becomes the FP64 finish's restart point while its gradient is
+    // still well above the tolerance (an FP32 solve can stall inside the band where the
+    // energy comparison no longer resolves a step)
+    const int back = (s.opt > kBackFactor * s.tol_eff) ? VO_BACK : 0;
     s.obj = objNew;
     s.opt = optNew;
     s.total_bis += s.num_bis;
     s.log_step = step;
     s.log_pending = 1;
-    s.vecop = VO_ACCEPT | VO_SAVE;
+    s.vecop = VO_ACCEPT | VO_SAVE | back;
     ctl_goto(s, ctl_post_step(s, o));
     return;
   }

@@ -62,6 +62,7 @@ enum VecOp : int32_t {
   VO_PRED = 64,       // x0 = x ; v0 = v ; x = x0 + dt * v0
   VO_GCOPY = 128,     // g = gn
   VO_ZERODX = 256,    // dx = 0
+  VO_BACK = 512,     // keep the saved iterate as the restart point of an FP64 finish
 };
 
 // LIN_TRUNCATED: the FP32 path met negative curvature and kept the iterate so far
@@ -131,6 +132,7 @@ struct InstDev {
   // FP64 node vectors [n][4]
   const double* xrest;
   double* x; double* xs; double* dx; double* g; double* gn; double* dxprev;
+  double* xback;              // the accepted iterate one Newton step before xs (FP64 finish restarts there)
   double* x0; double* v0; double* v; double* r64; double* bvec;
   // element scratch
   double* Eloc;               // [m]

@@ -199,26 +199,21 @@ def test_warm_resolve_after_load_update(gpu_ctx):
     assert disp_err(x2, xr, x0) < 1e-6
 
 
-def test_fp32_stall_finishes_in_fp64(gpu_ctx):
-    """A warm re-solve at a tolerance below what FP32-Hessian Newton reaches: the FP32 solve
-    stalls near its tolerance and the FP64 finish takes it the rest of the way."""
-    m = M.serving_request(11, 2)
-    inst = px.Instance(gpu_ctx, m)
-    base = dict(tol_max_error=0.0, tol_min_impr=0.0, tol_min_step=0.0)
-    inst.solve_static(px.options(precision=px.PREC_FP64, tol_rel=1e-10, **base), m.X0.ravel())
-    m2 = M.perturb_load(m, 11, 2)
-    inst.update_load(m2.force, m2.gravity)
-    x_start = inst.positions()
-    o = px.options(precision=px.PREC_FP32_REFINE, tol_rel=1e-7, **base)
-    x2, r2 = inst.solve_static(o, x_start)
-    assert r2["result_name"] == "SUCCESS", r2
-    assert r2["opt"] <= 1e-7 * r2["opt0"] * (1 + 1e-12)
-    assert 0 <= r2["fp64_iterations"] <= r2["iterations"]
-    orc, x0, g0, xr, _ = oracle_solution(m2, 1e-10)
-    assert disp_err(x2, xr, x0) < 1e-6
-    # without the finish the same solve reports where FP32 stopped
-    o.fp64_finish = 0
-    _, r3 = inst.solve_static(o, x_start)
-    assert r3["fp64_iterations"] == 0
-    if r2["fp64_iterations"] > 0:
-        assert r3["result_name"] != "SUCCESS"
+def test_fp32_stall_finishes_in_fp64(gpu_ctx, c1_oracle):
+    """An FP32 solve that stops short (here: an iteration cap) after reducing the gradient a
+    hundredfold is finished in FP64 from its last iterate with ||g|| above 100x the tolerance,
+    to the same tolerance; without the finish it reports where FP32 stopped.  The tolerance
+    (1e-6 of the starting gradient) sits well above the band where the FP64 energy
+    comparison of the line search stops resolving a step on this mesh (about 1e-7)."""
+    orc, x0, g0, xr, rep = c1_oracle
+    inst = px.Instance(gpu_ctx, orc.mesh)
+    base = dict(precision=px.PREC_FP32_REFINE, tol_max_error=1e-6 * g0, tol_min_impr=0.0, tol_min_step=0.0,
+                num_max_iters=9)
+    x, r = inst.solve_static(px.options(fp64_finish=0, **base), x0)
+    assert r["result_name"] == "MAXITER" and r["fp64_iterations"] == 0
+    assert r["opt"] <= 1e-2 * r["opt0"]
+    x, r = inst.solve_static(px.options(fp64_finish=1, **base), x0)
+    assert r["result_name"] == "SUCCESS", r
+    assert r["fp64_iterations"] > 0 and r["iterations"] > r["fp64_iterations"]
+    assert r["opt"] <= 1e-6 * g0
+    assert disp_err(x, xr, x0) < 1e-5
