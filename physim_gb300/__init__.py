@@ -207,12 +207,21 @@ class Context:
         _check(lib().phx_profile_read(self.h, kind.encode(), C.byref(n), C.byref(ms)))
         return n.value, ms.value
 
-    def batch_solve(self, insts: Sequence["Instance"], opts: Options, xs: Optional[List[np.ndarray]] = None):
+    def batch_solve(self, insts: Sequence["Instance"], opts: Options, xs: Optional[List[np.ndarray]] = None,
+                    inplace: bool = False):
+        """Solves the instances together.  xs: starting positions, returned solved (copies,
+        or with inplace=True the caller's float64 contiguous arrays themselves, e.g. pinned)."""
         n = len(insts)
         arr = (C.c_void_p * n)(*[i.h.value for i in insts])
         reps = (Report * n)()
         if xs is not None:
-            xs = [np.array(x, dtype=np.float64, copy=True).ravel() for x in xs]
+            if inplace:
+                for x in xs:
+                    if x.dtype != np.float64 or not x.flags.c_contiguous:
+                        raise ValueError("inplace positions must be float64 and contiguous")
+                xs = [x.reshape(-1) for x in xs]
+            else:
+                xs = [np.array(x, dtype=np.float64, copy=True).ravel() for x in xs]
             xp = (C.c_void_p * n)(*[x.ctypes.data for x in xs])
         else:
             xp = None

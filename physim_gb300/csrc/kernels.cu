@@ -483,7 +483,22 @@ __device__ __forceinline__ void st_gather(const BatchDev& B, const TileMap& M, i
     if (v < I.n) {
       double g[3] = {0.0, 0.0, 0.0};
       const int c0 = I.nseg_ptr[v], c1 = I.nseg_ptr[v + 1];
-      for (int c = c0; c < c1; ++c) {
+      int c = c0;
+      // four contributions in flight (ids, then values), added in element order
+      for (; c + 4 <= c1; c += 4) {
+        int id[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) id[u] = I.nseg_c[c + u];
+        double val[4][3];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const double* src = I.Gloc + 3 * (size_t)id[u];
+          val[u][0] = src[0]; val[u][1] = src[1]; val[u][2] = src[2];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) { g[0] += val[u][0]; g[1] += val[u][1]; g[2] += val[u][2]; }
+      }
+      for (; c < c1; ++c) {
         const double* src = I.Gloc + 3 * (size_t)I.nseg_c[c];
         g[0] += src[0]; g[1] += src[1]; g[2] += src[2];
       }
@@ -598,7 +613,19 @@ __device__ __forceinline__ void st_assemble(const BatchDev& B, const TileMap& M,
       if (k >= I.nlo) break;
       Real s = 0;
       const int c0 = I.seg_ptr[k], c1 = I.seg_ptr[k + 1];
-      for (int c = c0; c < c1; ++c) s += Hloc[(size_t)I.seg_c[c] * 9 + ent];
+      int c = c0;
+      // four contributions in flight (ids, then values), added in element order
+      for (; c + 4 <= c1; c += 4) {
+        int id[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) id[u] = I.seg_c[c + u];
+        Real val[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) val[u] = Hloc[(size_t)id[u] * 9 + ent];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) s += val[u];
+      }
+      for (; c < c1; ++c) s += Hloc[(size_t)I.seg_c[c] * 9 + ent];
       const int R = I.lo_rc[2 * k], C = I.lo_rc[2 * k + 1];
       if (dyn && R == C && a == b) s += (Real)(I.mass[R] / (dt * dt));
       if (!nofix) {
