@@ -109,6 +109,10 @@ typedef struct phx_options {
                                  hundredfold, is finished in FP64 from its last accepted iterate with
                                  ||g|| above 100x the tolerance, to the same tolerance; static solves
                                  only */
+  int32_t lsearch_parallel;   /* once two trials of a line search were rejected, this many further trials
+                                 (the step lengths the one-at-a-time search would try) are evaluated
+                                 together and scanned in order with its rules: the same decisions in
+                                 fewer rounds; 0 or 1: one at a time; at most 8 (default 8) */
 } phx_options;
 
 typedef struct phx_report {

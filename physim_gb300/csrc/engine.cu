@@ -352,6 +352,7 @@ DevOpts make_opts(const phx_options* o, bool dynamic, double dt) {
   d.precond = o->precond;
   d.max_refine_sweeps = o->precision == PHX_PREC_FP64 ? 1 : std::max(1, o->max_refine_sweeps);
   d.warm_guess = o->warm_guess;
+  d.ls_parallel = o->lsearch_parallel;
   d.dynamic = dynamic ? 1 : 0;
   d.tol_max_error = o->tol_max_error;
   d.tol_min_step = o->tol_min_step;
@@ -378,6 +379,8 @@ int validate_opts(const phx_options* o) {
   if (!(o->tol_rel >= 0.0)) return set_err(PHX_EINVAL, "options: tol_rel must be >= 0");
   if (o->pcg_cluster < 0 || o->pcg_cluster > 2) return set_err(PHX_EINVAL, "options: pcg_cluster must be 0, 1 or 2");
   if (o->fp64_finish < 0 || o->fp64_finish > 1) return set_err(PHX_EINVAL, "options: fp64_finish must be 0 or 1");
+  if (o->lsearch_parallel < 0 || o->lsearch_parallel > kLsK)
+    return set_err(PHX_EINVAL, "options: lsearch_parallel out of [0,8]");
   return PHX_OK;
 }
 
@@ -688,6 +691,7 @@ void phx_default_options(phx_options* o) {
   o->tol_rel = 0.0;
   o->pcg_cluster = 1;
   o->fp64_finish = 1;
+  o->lsearch_parallel = 8;
 }
 
 int phx_context_create(int32_t device, int64_t arena_bytes, phx_context* out) {

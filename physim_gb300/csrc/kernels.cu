@@ -463,6 +463,130 @@ __device__ __forceinline__ void st_elem_eg(const BatchDev& B, const TileMap& M, 
   }
 }
 
+// Element energies of the line-search trials evaluated together (PH_EVALK): for each
+// trial k, x = xs + a_k dx is formed node by node exactly as the vector-op stage forms a
+// trial point, and the element energy exactly as st_elem_eg does, so each trial's total
+// has the bits a one-at-a-time evaluation would give.  Energies only (the accepted trial
+// is evaluated again with its gradient).
+__device__ __forceinline__ void st_elem_ek(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag) {
+  const int total = map_total(M);
+  for (int t = cta; t < total; t += ncta) {
+    int i, lt;
+    map_tile(M, t, i, lt);
+    const InstDev I = B.inst[i];  // local copy: fields stay in registers across stores
+    NState* st = I.st;
+    if (st->phase != PH_EVALK) continue;
+    const int K = st->lsk;
+    const int e = lt * kTile + threadIdx.x;
+    double Ek[kLsK];
+#pragma unroll
+    for (int k = 0; k < kLsK; ++k) Ek[k] = 0.0;
+    if (e < I.m) {
+      const int4 tt = reinterpret_cast<const int4*>(I.tets)[e];
+      const int nd[4] = {tt.x, tt.y, tt.z, tt.w};
+      double xs[4][3], dx[4][3], X[4][3];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        ld4(I.xs, nd[a], xs[a]);
+        ld4(I.dx, nd[a], dx[a]);
+        ld4(I.xrest, nd[a], X[a]);
+      }
+      double R[12];
+      const double2* r2 = reinterpret_cast<const double2*>(I.rest64 + 12 * (size_t)e);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) { double2 q = r2[k]; R[2 * k] = q.x; R[2 * k + 1] = q.y; }
+      const double w = R[9], lam = R[10], mu = R[11];
+      const int model = I.model[e];
+      for (int k = 0; k < K; ++k) {
+        const double ak = st->ls_a[k];
+        double x[4][3];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) x[a][c] = xs[a][c] + ak * dx[a][c];
+        double u0[3], Du[9];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) u0[r] = x[0][r] - X[0][r];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+          for (int r = 0; r < 3; ++r) Du[r + 3 * c] = (x[c + 1][r] - X[c + 1][r]) - u0[r];
+        double Hd[9];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+            Hd[r + 3 * c] = Du[r] * R[0 + 3 * c] + Du[r + 3] * R[1 + 3 * c] + Du[r + 6] * R[2 + 3 * c];
+        double psi, P[9];
+        bool inverted;
+        material_eg(model, lam, mu, Hd, &psi, P, &inverted);
+        Ek[k] = inverted ? __longlong_as_double(0x7ff0000000000000LL) : psi * w;
+      }
+    }
+    double tot[kLsK];
+    if (tile_done<kLsK>(I, lt, tiles_of(I.m), ncta, Ek, tot, sm, &flag) && threadIdx.x == 0) {
+      count_bytes(B, I, K_ELEM_EG);
+      for (int k = 0; k < K; ++k) st->ls_eel[k] = tot[k];
+      st->phase = PH_EVALK2;
+      advance(B, i);
+    }
+  }
+}
+
+// Linear-load (and inertia) energies of the trials, formed per node exactly as st_gather
+// forms them; then the trials' totals go to the line-search scan.
+__device__ __forceinline__ void st_lin_ek(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag) {
+  const int total = map_total(M);
+  for (int t = cta; t < total; t += ncta) {
+    int i, lt;
+    map_tile(M, t, i, lt);
+    const InstDev I = B.inst[i];  // local copy: fields stay in registers across stores
+    NState* st = I.st;
+    if (st->phase != PH_EVALK2) continue;
+    const int K = st->lsk;
+    const int v = lt * kTile + threadIdx.x;
+    double Lk[kLsK];
+#pragma unroll
+    for (int k = 0; k < kLsK; ++k) Lk[k] = 0.0;
+    if (v < I.n) {
+      double xs[3], dx[3], h[3];
+      ld4(I.xs, v, xs);
+      ld4(I.dx, v, dx);
+      ld4(I.hlin, v, h);
+      const bool dyn = I.opts->dynamic != 0;
+      double x0[3] = {0.0, 0.0, 0.0}, v0[3] = {0.0, 0.0, 0.0};
+      const double dt = I.opts->dt, m = dyn ? I.mass[v] : 0.0;
+      if (dyn) {
+        ld4(I.x0, v, x0);
+        ld4(I.v0, v, v0);
+      }
+      for (int k = 0; k < K; ++k) {
+        const double ak = st->ls_a[k];
+        double x[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) x[c] = xs[c] + ak * dx[c];
+        double elin = x[0] * h[0] + x[1] * h[1] + x[2] * h[2];
+        if (dyn) {
+          double acc = 0.0;
+          for (int c = 0; c < 3; ++c) {
+            double a = (x[c] - x0[c]) / (dt * dt) - v0[c] / dt;
+            acc += a * (m * a);
+          }
+          elin += (dt * dt / 2.0) * acc;
+        }
+        Lk[k] = elin;
+      }
+    }
+    double tot[kLsK];
+    if (tile_done<kLsK>(I, lt, tiles_of(I.n), ncta, Lk, tot, sm, &flag) && threadIdx.x == 0) {
+      count_bytes(B, I, K_GATHER);
+      for (int k = 0; k < K; ++k) st->ls_e[k] = st->ls_eel[k] + tot[k];
+      st->phase = PH_EVAL_DONE;  // purpose 2: the scan of ctl_lsk_check
+      advance(B, i);
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kTile) k_elem_eg(BatchDev B) {
   __shared__ double sm[32 * 5];
   __shared__ int flag;
@@ -1347,6 +1471,14 @@ __global__ void __launch_bounds__(kTile, (sizeof(Real) == 4 ? 3 : 2)) k_engine(B
       st_gather(B, Mn, cta, P, sm, flag);
       PHX_SYNC(P, 4, K_GATHER);
     }
+    if (PHX_NEED(PH_EVALK)) {
+      st_elem_ek(B, Mt, cta, P, sm, flag);
+      PHX_SYNC(P, 19, K_ELEM_EG);
+    }
+    if (PHX_NEED(PH_EVALK2)) {
+      st_lin_ek(B, Mn, cta, P, sm, flag);
+      PHX_SYNC(P, 20, K_GATHER);
+    }
     if (PHX_NEED(PH_VEC)) {
       st_vecop(B, Mn, cta, P, sm, flag);
       PHX_SYNC(P, 5, K_VECOP);
@@ -1402,6 +1534,14 @@ __global__ void __launch_bounds__(kTile, (sizeof(Real) == 4 ? 3 : 2)) k_engine(B
     if (PHX_NEED(PH_EVAL)) {
       st_gather(B, Mn, cta, P, sm, flag);
       PHX_SYNC(P, 17, K_GATHER);
+    }
+    if (PHX_NEED(PH_EVALK)) {
+      st_elem_ek(B, Mt, cta, P, sm, flag);
+      PHX_SYNC(P, 21, K_ELEM_EG);
+    }
+    if (PHX_NEED(PH_EVALK2)) {
+      st_lin_ek(B, Mn, cta, P, sm, flag);
+      PHX_SYNC(P, 22, K_GATHER);
     }
   }
 #undef PHX_NEED

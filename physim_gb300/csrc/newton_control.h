@@ -149,6 +149,50 @@ PHX_HD inline void ctl_lin_done(NState& s, const DevOpts& o) {
   ctl_goto(s, PH_EVAL);
 }
 
+// A rejected line-search trial (LineSearch_Simple, OptimSolver.cpp:688-736): sets up the
+// next, shorter trial and returns true, or applies the failure (state restored, step
+// rejected) and returns false.
+PHX_HD inline bool ctl_ls_reject(NState& s, const DevOpts& o) {
+  const double stepCur = s.alpha_trial * s.dx_norm;
+  s.factor *= o.lsearch_alpha;
+  if (stepCur > o.tol_min_step && s.num_bis <= o.lsearch_num_try) {
+    s.num_bis++;
+    s.alpha_trial = s.scale * s.factor;
+    return true;
+  }
+  s.result = OS_NONDESC;
+  s.step_result = OS_NONDESC;
+  s.total_bis += s.num_bis;
+  s.log_step = stepCur;
+  s.log_pending = 1;
+  s.vecop = VO_RESTORE;
+  ctl_goto(s, ctl_post_step(s, o));
+  return false;
+}
+
+// Evaluates the current trial step.  Once two trials of a search were rejected (long
+// searches are the rule there), the next ls_parallel trials (the same step lengths the
+// one-at-a-time search would try) are evaluated together, energies only.
+PHX_HD inline void ctl_ls_next(NState& s, const DevOpts& o) {
+  const int K = o.ls_parallel > kLsK ? kLsK : o.ls_parallel;
+  if (K > 1 && s.num_bis >= 2) {
+    double f = s.factor;
+    s.ls_a[0] = s.alpha_trial;
+    for (int k = 1; k < K; ++k) {
+      f *= o.lsearch_alpha;
+      s.ls_a[k] = s.scale * f;
+    }
+    s.lsk = K;
+    s.purpose = 2;
+    s.phase = PH_EVALK;
+    return;
+  }
+  s.vecop = VO_TRIAL;
+  ctl_goto(s, PH_EVAL);
+}
+
+PHX_HD inline void ctl_lsk_check(NState& s, const DevOpts& o);
+
 // Line-search trial evaluated: accept, bisect, or give up (LineSearch_Simple + UpdateStepResult).
 PHX_HD inline void ctl_ls_check(NState& s, const DevOpts& o) {
   double objNew = s.E_eval;
@@ -185,23 +229,24 @@ PHX_HD inline void ctl_ls_check(NState& s, const DevOpts& o) {
     ctl_goto(s, ctl_post_step(s, o));
     return;
   }
-  double stepCur = s.alpha_trial * s.dx_norm;
-  s.factor *= o.lsearch_alpha;
-  if (stepCur > o.tol_min_step && s.num_bis <= o.lsearch_num_try) {
-    s.num_bis++;
-    s.alpha_trial = s.scale * s.factor;
-    s.vecop = VO_TRIAL;
-    ctl_goto(s, PH_EVAL);
-    return;
+  if (ctl_ls_reject(s, o)) ctl_ls_next(s, o);
+}
+
+// Line-search trials evaluated together (PH_EVALK): scans them in order with the rules of
+// the one-at-a-time search, so it takes the same decisions: the first trial whose energy
+// is below the current one is evaluated again with its gradient (PH_EVAL) and checked as
+// usual; a rejected trial goes through ctl_ls_reject like a sequential one.
+PHX_HD inline void ctl_lsk_check(NState& s, const DevOpts& o) {
+  for (int k = 0; k < s.lsk; ++k) {
+    if (s.ls_e[k] < s.obj) {  // s.alpha_trial is trial k's step here (same recurrence)
+      s.purpose = 1;
+      s.vecop = VO_TRIAL;
+      ctl_goto(s, PH_EVAL);
+      return;
+    }
+    if (!ctl_ls_reject(s, o)) return;  // the search failed at trial k
   }
-  // line search failed: state restored, step rejected
-  s.result = OS_NONDESC;
-  s.step_result = OS_NONDESC;
-  s.total_bis += s.num_bis;
-  s.log_step = stepCur;
-  s.log_pending = 1;
-  s.vecop = VO_RESTORE;
-  ctl_goto(s, ctl_post_step(s, o));
+  ctl_ls_next(s, o);
 }
 
 // Advances one instance until it needs device work or is done.
@@ -239,7 +284,8 @@ PHX_HD inline void ctl_advance(NState& s, const DevOpts& o) {
           s.phase = PH_VEC;
           return;
         }
-        ctl_ls_check(s, o);
+        if (s.purpose == 2) ctl_lsk_check(s, o);
+        else ctl_ls_check(s, o);
         if (s.phase == PH_ITER) continue;
         return;
       case PH_ITER:

@@ -26,7 +26,7 @@ namespace phx {
 
 constexpr int kTile = 128;       // tets / nodes / lower blocks per tile
 constexpr int kChunk = 32;       // SELL chunk height (one warp)
-constexpr int kPartials = 5;     // doubles reduced per tile (at most)
+constexpr int kPartials = 8;     // doubles reduced per tile (at most)
 constexpr int kCl = 8;           // CTAs per cluster of the cluster PCG
 constexpr int kClThreads = 512;  // threads per CTA of the cluster PCG
 constexpr int kClNarrow = 2;         // narrow variant: CTAs per cluster
@@ -50,7 +50,10 @@ enum Phase : int32_t {
   PH_PCG = 10,        // device: PCG iterations
   PH_ACCUM = 11,      // device: dx += e, norms
   PH_LIN_DONE = 12,   // control: regularisation checks, clamp, line search start
+  PH_EVALK = 13,      // device: element energies at several line-search trial steps
+  PH_EVALK2 = 14,     // device: their linear-load (and inertia) energies, then the scan
 };
+constexpr int kLsK = 8;  // most line-search trial steps evaluated together
 
 enum VecOp : int32_t {
   VO_RESTORE = 1,     // x = xs
@@ -75,7 +78,7 @@ enum DevError : int32_t { DEV_OK = 0, DEV_NONFINITE = 1, DEV_BADSTATE = 2 };
 struct DevOpts {
   int32_t qp_solver, min_step_max_count, min_impr_max_count, num_max_iters, try_steepest;
   int32_t ls_num_max_iters, ls_num_reg_trials, lsearch_num_try, precision, precond;
-  int32_t max_refine_sweeps, warm_guess, dynamic, pad0;
+  int32_t max_refine_sweeps, warm_guess, dynamic, ls_parallel;  // ls_parallel: trials evaluated together
   double tol_max_error, tol_min_step, tol_min_impr, max_step_size, ls_tol_max_error;
   double lsearch_alpha, inner_tol, dt, tol_rel;
 };
@@ -100,6 +103,8 @@ struct NState {
   double eta, opt_prev;                        // forcing term state (FP32 path)
   double log_step;                             // ||dx_final|| of the step being logged
   int32_t log_pending, log_count;              // per-iteration log bookkeeping
+  int32_t lsk, pad_ls;                         // trials in the batch being evaluated (PH_EVALK)
+  double ls_a[8], ls_e[8], ls_eel[8];          // their step lengths, energies, element energies
 };
 
 constexpr int kLogCap = 256;                   // Newton iterations kept in the per-instance log
@@ -170,7 +175,7 @@ struct BatchDev {
   int32_t cluster_mode;       // 1: instances with pcg_cluster leave their PCG to k_pcg_cluster
 };
 
-constexpr int kBucketClusterPcg = 13;  // phase bucket of instances waiting for the cluster PCG kernel
+constexpr int kBucketClusterPcg = 15;  // phase bucket of instances waiting for the cluster PCG kernel
 
 PHX_HD inline int64_t sell_addr(int64_t s, int e) { return (s >> 5) * 288 + (int64_t)e * 32 + (s & 31); }
 

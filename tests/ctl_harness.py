@@ -10,7 +10,7 @@ import numpy as np
 import scipy.sparse as sp
 
 PH_DONE, PH_START, PH_VEC, PH_EVAL, PH_EVAL_DONE, PH_ITER, PH_HESS, PH_JACOBI, PH_LINSETUP, PH_RESID, PH_PCG, \
-    PH_ACCUM, PH_LIN_DONE = range(13)
+    PH_ACCUM, PH_LIN_DONE, PH_EVALK, PH_EVALK2 = range(15)
 VO_RESTORE, VO_ACCEPT, VO_SAVE, VO_STEEP, VO_TRIAL, VO_VEL, VO_PRED, VO_GCOPY, VO_ZERODX = \
     1, 2, 4, 8, 16, 32, 64, 128, 256
 LIN_RUNNING, LIN_CONVERGED, LIN_MAXITER, LIN_BREAKDOWN = range(4)
@@ -25,14 +25,15 @@ class NState(C.Structure):
             "obj", "opt", "opt0", "obj_new", "alpha_trial", "factor", "scale", "dx_norm", "b_dot_dx", "E_el",
             "E_eval", "gg_eval", "normA2", "shift", "regT", "bb", "rr64", "rz", "rr", "pq", "alpha", "beta",
             "thr_inner", "thr_final", "tol_eff", "lin_tol", "eta", "opt_prev", "log_step")] + \
-        [("log_pending", C.c_int32), ("log_count", C.c_int32)]
+        [("log_pending", C.c_int32), ("log_count", C.c_int32), ("lsk", C.c_int32), ("pad_ls", C.c_int32),
+         ("ls_a", C.c_double * 8), ("ls_e", C.c_double * 8), ("ls_eel", C.c_double * 8)]
 
 
 class DevOpts(C.Structure):
     _fields_ = [(n, C.c_int32) for n in (
         "qp_solver", "min_step_max_count", "min_impr_max_count", "num_max_iters", "try_steepest",
         "ls_num_max_iters", "ls_num_reg_trials", "lsearch_num_try", "precision", "precond",
-        "max_refine_sweeps", "warm_guess", "dynamic", "pad0")] + [(n, C.c_double) for n in (
+        "max_refine_sweeps", "warm_guess", "dynamic", "ls_parallel")] + [(n, C.c_double) for n in (
             "tol_max_error", "tol_min_step", "tol_min_impr", "max_step_size", "ls_tol_max_error",
             "lsearch_alpha", "inner_tol", "dt", "tol_rel")]
 
@@ -88,6 +89,9 @@ def pcg(A, b, x, thr, maxit, Minv):
     return x, it, LIN_MAXITER
 
 
+stats = {"evalk": 0}  # PH_EVALK visits of the last run
+
+
 def run(shim, orc, x0, opts, dynamic=False, v0=None, max_steps=200000):
     """Drives ctl_advance_c until PH_DONE; returns (x, v, NState)."""
     sizes = (C.c_int * 2)()
@@ -107,6 +111,7 @@ def run(shim, orc, x0, opts, dynamic=False, v0=None, max_steps=200000):
     v = np.zeros(N) if v0 is None else v0.copy()
     xo = np.zeros(N); vo = np.zeros(N)
     s = NState()
+    stats["evalk"] = 0
     s.phase = PH_START
     s.opt0 = -1.0
     o = opts
@@ -141,6 +146,17 @@ def run(shim, orc, x0, opts, dynamic=False, v0=None, max_steps=200000):
                 v = (x - xo) / dt
             s.phase = s.next_phase
             s.vecop = 0
+        elif ph == PH_EVALK:
+            # several line-search trials at once: energies only, then the scan
+            stats["evalk"] += 1
+            for k in range(s.lsk):
+                xk = xs + s.ls_a[k] * dx
+                E = orc.energy(xk)
+                if dynamic:
+                    acc = (xk - xo) / dt ** 2 - vo / dt
+                    E += dt * dt / 2 * np.sum(acc * mdof * acc)
+                s.ls_e[k] = E
+            s.phase = PH_EVAL_DONE
         elif ph == PH_EVAL:
             E = orc.energy(x)
             gg = orc.gradient(x, fix=False)

@@ -94,3 +94,23 @@ def test_inexact_newton_forcing_converges_to_the_same_point(ctl_shim):
     assert rel(x - x0, xo - x0) < 1e-8
     _, _, s64 = H.run(ctl_shim, orc, x0, H.make_opts(**kw))
     assert s.pcg_total < s64.pcg_total  # looser linear solves on the way
+
+
+def test_parallel_line_search_takes_the_same_decisions(ctl_shim):
+    """Trials evaluated eight at a time (after two rejections) and scanned in order give the
+    same iterates, bisection count and result as the one-at-a-time line search, on a StVK
+    box that needs hundreds of bisections."""
+    m = M.make_box(2, 2, 6, (0.04, 0.04, 0.12), 2e5, 0.35, 1000.0, 1, (0.0, -9.81, 0.0), clamp_face=4,
+                   load_face=5, traction=(20000.0, -30000.0, 10000.0))
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    g0 = np.linalg.norm(orc.gradient(x0))
+    runs = []
+    for k in (0, 8):
+        opts = H.make_opts(tol_max_error=1e-6 * g0, tol_min_impr=0.0, tol_min_step=0.0, ls_parallel=k)
+        x, _, s = H.run(ctl_shim, orc, x0, opts)
+        runs.append((x, s.result, s.it, s.total_bis, H.stats["evalk"]))
+    (xa, ra, ia, ba, ka), (xb, rb, ib, bb, kb) = runs
+    assert ba > 100 and ka == 0 and kb > 0 and kb < ba / 4
+    assert (ra, ia, ba) == (rb, ib, bb)
+    assert np.array_equal(xa, xb)
