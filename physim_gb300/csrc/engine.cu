@@ -150,8 +150,11 @@ struct phx_context_s {
   int act_cap = 0;
   unsigned long long* d_stage = nullptr;  // [32] stage ns + executions (profiling)
   int egrid[2] = {0, 0};
-  int32_t* d_clist = nullptr;  // instances whose PCG runs per cluster (batch order)
+  int32_t* d_clist = nullptr;  // instances waiting for a cluster PCG solve this step (uploaded per step)
+  int32_t* h_wait = nullptr;   // pinned staging of that list
   int clist_cap = 0;
+  std::vector<int32_t> h_clist;  // instances whose PCG runs per cluster, largest first
+  std::vector<int32_t> h_kind;   // their PCG kind, by batch position
   int clist_kinds = 0;  // bit k: the cluster list holds instances of PCG kind k
 };
 
@@ -517,14 +520,19 @@ int set_cluster_list(phx_context ctx, const std::vector<phx_instance>& list, int
   ctx->clist_kinds = 0;
   for (int id : ids) ctx->clist_kinds |= 1 << list[id]->dev.pcg_cluster;
   *count = (int)ids.size();
+  ctx->h_clist = ids;
+  ctx->h_kind.assign(list.size(), 0);
+  for (int i = 0; i < (int)list.size(); ++i) ctx->h_kind[i] = list[i]->dev.pcg_cluster;
   if (ids.empty()) return PHX_OK;
   if (ctx->clist_cap < (int)ids.size()) {
     if (ctx->d_clist) cudaFree(ctx->d_clist);
+    if (ctx->h_wait) cudaFreeHost(ctx->h_wait);
     ctx->d_clist = nullptr;
+    ctx->h_wait = nullptr;
     CU(cudaMalloc(&ctx->d_clist, sizeof(int32_t) * ids.size()));
+    CU(cudaMallocHost(&ctx->h_wait, sizeof(int32_t) * ids.size()));
     ctx->clist_cap = (int)ids.size();
   }
-  CU(cudaMemcpyAsync(ctx->d_clist, ids.data(), sizeof(int32_t) * ids.size(), cudaMemcpyHostToDevice, ctx->stream));
   return PHX_OK;
 }
 
@@ -545,9 +553,16 @@ int run_step(phx_context ctx, const BatchDev& B0, int num, bool fp64, int pcg_ch
   if (B.cluster_mode && ctx->h_flags[0] > 0 && ctx->h_flags[1] > 0) {
     cudaEvent_t a = nullptr, b = nullptr;
     if (ctx->profiling) TRY(profile_events(ctx, &a, &b));
+    // one cluster per waiting instance, largest first (the flags hold every instance's phase
+    // after the engine launch): no clusters are launched only to find nothing to do
     for (int kind = 1; kind <= 2; ++kind) {
       if (!(ctx->clist_kinds & (1 << kind))) continue;
-      CU(launch_pcg_cluster(ctx->stream, B, ctx->d_clist, ccount, kind));
+      int nw = 0;
+      for (int32_t id : ctx->h_clist)
+        if (ctx->h_flags[8 + id] == PH_PCG && ctx->h_kind[id] == kind) ctx->h_wait[nw++] = id;
+      if (nw == 0) continue;
+      CU(cudaMemcpyAsync(ctx->d_clist, ctx->h_wait, sizeof(int32_t) * nw, cudaMemcpyHostToDevice, ctx->stream));
+      CU(launch_pcg_cluster(ctx->stream, B, ctx->d_clist, nw, kind));
       ctx->launches++;
     }
     if (ctx->profiling) {
@@ -737,6 +752,7 @@ int phx_context_destroy(phx_context ctx) {
   if (ctx->d_act) cudaFree(ctx->d_act);
   if (ctx->d_stage) cudaFree(ctx->d_stage);
   if (ctx->d_clist) cudaFree(ctx->d_clist);
+  if (ctx->h_wait) cudaFreeHost(ctx->h_wait);
   for (auto& ev : ctx->marks)
     if (ev) cudaEventDestroy(ev);
   ctx->arena.release();
