@@ -192,20 +192,22 @@ __device__ __forceinline__ void load_du(const InstDev& I, int e, int (&nd)[4], d
 }
 
 // y - log(1 + y) without cancellation for small y (series up to y^9 when |y| < 1e-3)
-__device__ __forceinline__ double y_minus_log1p(double y) {
+// y - log1p(y) without cancellation; l1p = log1p(y), already computed by the caller.  For
+// |y| < 1e-3 the series sum_{k>=2} (-1)^k y^k / k, in Horner form with the coefficients as
+// constants (no FP64 divisions), truncated after y^9 (relative error below 1e-24 there).
+__device__ __forceinline__ double y_minus_log1p(double y, double l1p) {
   if (fabs(y) < 1e-3) {
-    double t = y * y, s = 0.0, p = y;
-    // y^2/2 - y^3/3 + y^4/4 - ... = sum_{k>=2} (-1)^k y^k / k
-    p = t;
-    s = p / 2.0;
-#pragma unroll
-    for (int k = 3; k <= 9; ++k) {
-      p *= -y;
-      s += p / (double)k;
-    }
-    return s;
+    double s = 1.0 / 9.0;
+    s = 1.0 / 8.0 - y * s;
+    s = 1.0 / 7.0 - y * s;
+    s = 1.0 / 6.0 - y * s;
+    s = 1.0 / 5.0 - y * s;
+    s = 1.0 / 4.0 - y * s;
+    s = 1.0 / 3.0 - y * s;
+    s = 1.0 / 2.0 - y * s;
+    return (y * y) * s;
   }
-  return y - log1p(y);
+  return y - l1p;
 }
 
 // ---------------------------------------------------------------------------
@@ -398,9 +400,10 @@ __device__ __forceinline__ void material_eg(int model, double lam, double mu, co
 #pragma unroll
     for (int k = 0; k < 9; ++k) hh += H[k] * H[k];
     const double J = 1.0 + j;
-    const double logJ2 = (j > -1.0) ? 2.0 * log1p(j) : log(J * J);
+    const double l1p = (j > -1.0) ? log1p(j) : 0.0;
+    const double logJ2 = (j > -1.0) ? 2.0 * l1p : log(J * J);
     const double lJ = 0.5 * logJ2;
-    *psi = 0.5 * mu * (hh - 2.0 * q + 2.0 * ((j > -1.0) ? y_minus_log1p(j) : j - lJ)) + 0.5 * lam * lJ * lJ;
+    *psi = 0.5 * mu * (hh - 2.0 * q + 2.0 * ((j > -1.0) ? y_minus_log1p(j, l1p) : j - lJ)) + 0.5 * lam * lJ * lJ;
     double C[9];
     cof3(F, C);
     double c = (0.5 * lam * logJ2 - mu) / J;
