@@ -236,3 +236,54 @@ def test_parallel_line_search_same_result_on_gpu(gpu_ctx):
     for key in ("result", "iterations", "bisections", "pcg_iterations"):
         assert ra[key] == rb[key], key
     assert np.array_equal(xa, xb)
+
+
+def _load_free(m):
+    out = m.copy()
+    out.force = np.zeros_like(m.force)
+    out.gravity = np.zeros(3)
+    return out
+
+
+@pytest.mark.parametrize("prec", [px.PREC_FP64, px.PREC_FP32_REFINE])
+def test_no_load_stays_at_rest(gpu_ctx, prec):
+    """Zero right-hand side: the solve returns the rest shape at once (SolveFull's first
+    check), for a free-standing loaded mesh with its loads removed."""
+    m = _load_free(M.cantilever(2, 2, 6))
+    inst = px.Instance(gpu_ctx, m)
+    x, r = inst.solve_static(px.options(precision=prec, tol_max_error=1e-12, tol_min_impr=0.0, tol_min_step=0.0),
+                             m.X0.ravel())
+    assert r["result_name"] == "SUCCESS" and r["iterations"] == 1
+    assert r["opt"] == 0.0 and np.array_equal(x, m.X0.ravel())
+
+
+def test_fully_clamped_instance(gpu_ctx):
+    """Every DoF fixed: the gradient is zero after fixing, the solve succeeds at once and
+    nothing moves, in a batch with a loaded instance.  (The stopping test is the reference's
+    strict ||g|| < tol, so a zero gradient needs a positive absolute floor: tol_rel times a
+    zero starting gradient is zero.)"""
+    m = M.cantilever(2, 2, 6)
+    clamped = m.copy()
+    clamped.fixed = np.ones_like(m.fixed)
+    a, b = px.Instance(gpu_ctx, clamped), px.Instance(gpu_ctx, m)
+    o = px.options(precision=px.PREC_FP32_REFINE, tol_rel=1e-6, tol_max_error=1e-14, tol_min_impr=0.0,
+                   tol_min_step=0.0)
+    reps, xs = gpu_ctx.batch_solve([a, b], o, [clamped.X0.ravel(), m.X0.ravel()])
+    assert reps[0]["result_name"] == "SUCCESS" and np.array_equal(xs[0], clamped.X0.ravel())
+    assert reps[1]["result_name"] == "SUCCESS" and reps[1]["iterations"] > 1
+
+
+def test_empty_batch(gpu_ctx):
+    reps, _ = gpu_ctx.batch_solve([], px.options())
+    assert reps == []
+    assert gpu_ctx.batch_dynamic_step([], px.options(), 1e-3) == []
+
+
+def test_dynamic_step_at_rest_without_load(gpu_ctx):
+    """Implicit Euler from rest with no load and no velocity: the step keeps rest."""
+    m = _load_free(M.cantilever(2, 2, 6))
+    inst = px.Instance(gpu_ctx, m)
+    inst.reset()
+    x, v, r = inst.dynamic_step(px.options(tol_max_error=1e-12, tol_min_impr=0.0, tol_min_step=0.0), 1e-3)
+    assert r["result_name"] == "SUCCESS"
+    assert np.array_equal(x, m.X0.ravel()) and not np.any(v)
