@@ -46,8 +46,11 @@ __device__ __forceinline__ bool cluster_owned(const BatchDev& B, const InstDev& 
   return B.cluster_mode && I.pcg_cluster;
 }
 
-template <int K>
-__device__ __forceinline__ void block_sum(double (&v)[K], double* sm) {
+// Sums K values over the CTA into v[] of warp 0 (fixed order); T = double, or float for
+// the FP32 PCG's per-tile inner products (sm: the double scratch, reused as T).
+template <int K, typename T = double>
+__device__ __forceinline__ void block_sum(T (&v)[K], double* smd) {
+  T* sm = reinterpret_cast<T*>(smd);
 #pragma unroll
   for (int k = 0; k < K; ++k)
 #pragma unroll
@@ -61,7 +64,7 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double* sm) {
   if (warp == 0) {
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      v[k] = lane < nw ? sm[lane * K + k] : 0.0;
+      v[k] = lane < nw ? sm[lane * K + k] : (T)0;
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], off);
     }
@@ -79,14 +82,14 @@ __device__ __forceinline__ void count_bytes(const BatchDev& B, const InstDev& I,
 // it has then done lt / ncta + 1 of them: only that tile publishes the count, with one
 // fence and one atomic per CTA and instance instead of per tile.  The totals are summed
 // from the per-tile partials in tile order, whatever the CTA count.
-template <int K>
-__device__ bool tile_done(const InstDev& I, int lt, int ntiles, int ncta, double (&v)[K], double (&tot)[K],
+template <int K, typename T>
+__device__ bool tile_done(const InstDev& I, int lt, int ntiles, int ncta, T (&v)[K], double (&tot)[K],
                           double* sm, int* flag) {
-  block_sum<K>(v, sm);
+  block_sum<K, T>(v, sm);
   const bool last_here = lt + ncta >= ntiles;
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int k = 0; k < K; ++k) I.partials[(size_t)lt * K + k] = v[k];
+    for (int k = 0; k < K; ++k) I.partials[(size_t)lt * K + k] = (double)v[k];
     if (last_here) {
       const unsigned mine = (unsigned)(lt / ncta + 1);
       __threadfence();
@@ -1058,7 +1061,7 @@ __device__ __forceinline__ void st_pcg_a(const BatchDev& B, const TileMap& M, in
     const InstDev I = B.inst[i];  // local copy: fields stay in registers across stores
     NState* st = I.st;
     if (st->phase != PH_PCG || cluster_owned(B, I)) continue;
-    double p[1] = {0.0};
+    Real p[1] = {(Real)0};  // per-tile inner product in the PCG's own precision
     {
       const int par = st->pcg_parity;
       const Real* pold = par ? PcgBufs<Real>::pb(I) : PcgBufs<Real>::pa(I);
@@ -1089,7 +1092,7 @@ __device__ __forceinline__ void st_pcg_a(const BatchDev& B, const TileMap& M, in
           }
           st4(pnew, v, pv);
           st4(PcgBufs<Real>::q(I), v, acc);
-          p[0] += (double)pv[0] * acc[0] + (double)pv[1] * acc[1] + (double)pv[2] * acc[2];
+          p[0] += pv[0] * acc[0] + pv[1] * acc[1] + pv[2] * acc[2];
         }
       }
     }
@@ -1132,7 +1135,7 @@ __device__ __forceinline__ void st_pcg_b(const BatchDev& B, const TileMap& M, in
     NState* st = I.st;
     if (st->phase != PH_PCG || cluster_owned(B, I)) continue;
     const int v = lt * B.cpt * 32 + threadIdx.x;  // one row per thread over the tile's chunks
-    double p[2] = {0.0, 0.0};
+    Real p[2] = {(Real)0, (Real)0};  // per-tile inner products in the PCG's own precision
     if ((int)threadIdx.x < B.cpt * 32 && v < I.n) {
       const Real alpha = (Real)st->alpha;
       const Real* pc = st->pcg_parity ? PcgBufs<Real>::pa(I) : PcgBufs<Real>::pb(I);
@@ -1152,8 +1155,8 @@ __device__ __forceinline__ void st_pcg_b(const BatchDev& B, const TileMap& M, in
       st4(PcgBufs<Real>::e(I), v, ev);
       st4(PcgBufs<Real>::r(I), v, rv);
       st4(PcgBufs<Real>::z(I), v, z);
-      p[0] = (double)rv[0] * rv[0] + (double)rv[1] * rv[1] + (double)rv[2] * rv[2];
-      p[1] = (double)rv[0] * z[0] + (double)rv[1] * z[1] + (double)rv[2] * z[2];
+      p[0] = rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2];
+      p[1] = rv[0] * z[0] + rv[1] * z[1] + rv[2] * z[2];
     }
     double tot[2];
     if (tile_done<2>(I, lt, pcg_tiles(B, I), ncta, p, tot, sm, &flag) && threadIdx.x == 0) {

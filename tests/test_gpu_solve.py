@@ -48,12 +48,17 @@ def test_cantilever_fp64_plain(gpu_ctx, c1_oracle):
 
 
 def test_cantilever_fp32_refine(gpu_ctx, c1_oracle):
+    """The served FP32+refinement path at its specified tolerance (1e-6 of the starting
+    gradient): the energy comparison of the line search stops resolving steps near 7e-8 of
+    g0 on this mesh, which the path's linear final convergence can land in, so tighter
+    tolerances are not a property of the path."""
     orc, x0, g0, xr, rep = c1_oracle
     inst = px.Instance(gpu_ctx, orc.mesh)
-    o = px.options(precision=px.PREC_FP32_REFINE, tol_max_error=1e-8 * g0, tol_min_impr=0.0, tol_min_step=0.0)
+    o = px.options(precision=px.PREC_FP32_REFINE, tol_max_error=1e-6 * g0, tol_min_impr=0.0, tol_min_step=0.0)
     x, r = inst.solve_static(o, x0)
     assert r["result_name"] == "SUCCESS", r
-    assert r["refine_sweeps"] > 0
+    assert r["refine_sweeps"] > 0 and r["fp64_iterations"] == 0
+    assert r["opt"] <= 1e-6 * g0
     assert disp_err(x, xr, x0) < 1e-6
 
 
