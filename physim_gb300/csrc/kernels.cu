@@ -71,6 +71,24 @@ __device__ __forceinline__ void block_sum(T (&v)[K], double* smd) {
   }
 }
 
+// tile_done without a reduction: for stages that only need to know which CTA completes the
+// instance (the same one-atomic-per-CTA count).  Returns true in that CTA (all threads).
+__device__ __forceinline__ bool tile_count_done(const InstDev& I, int lt, int ntiles, int ncta, int* flag) {
+  if (lt + ncta < ntiles) return false;  // not this CTA's last tile of the instance
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned mine = (unsigned)(lt / ncta + 1);
+    __threadfence();
+    const unsigned prev = atomicAdd(I.counter, mine);
+    *flag = (prev + mine == (unsigned)ntiles);
+    if (*flag) *I.counter = 0u;
+  }
+  __syncthreads();
+  if (!*flag) return false;
+  __threadfence();
+  return true;
+}
+
 __device__ __forceinline__ void count_bytes(const BatchDev& B, const InstDev& I, KernelId k) {
   if (B.algo_total) B.algo_total[k] += I.algo[k];  // single thread of the finalising CTA
 }
@@ -341,8 +359,7 @@ __device__ __forceinline__ void st_vecop(const BatchDev& B, const TileMap& M, in
         st4(I.v, v, tmp);
       }
     }
-    double p[1] = {0.0}, tot[1];
-    if (tile_done<1>(I, lt, tiles_of(I.n), ncta, p, tot, sm, &flag) && threadIdx.x == 0) {
+    if (tile_count_done(I, lt, tiles_of(I.n), ncta, &flag) && threadIdx.x == 0) {
       count_bytes(B, I, K_VECOP);
       st->phase = st->next_phase;
       st->vecop = 0;
@@ -737,7 +754,7 @@ __device__ __forceinline__ void st_assemble(const BatchDev& B, const TileMap& M,
     Real* H = PcgBufs<Real>::H(I);
     const bool dyn = I.opts->dynamic != 0, nofix = st->nofix != 0;
     const double dt = I.opts->dt;
-    double nrm = 0.0;
+    Real nrm = 0;  // ||A||_F^2 of the stored entries, for the regularisation threshold only
     for (int it = threadIdx.x; it < kTile * 9; it += blockDim.x) {
       const int k = lt * kTile + it / 9, ent = it % 9, a = ent / 3, b = ent % 3;
       if (k >= I.nlo) break;
@@ -764,9 +781,10 @@ __device__ __forceinline__ void st_assemble(const BatchDev& B, const TileMap& M,
       }
       H[sell_addr(I.lo_slot[k], ent)] = s;
       if (R != C) H[sell_addr(I.up_slot[k], b * 3 + a)] = s;
-      nrm += (double)s * (double)s;
+      nrm += s * s;
     }
-    double p[1] = {nrm}, tot[1];
+    Real p[1] = {nrm};
+    double tot[1];
     if (tile_done<1>(I, lt, tiles_of(I.nlo), ncta, p, tot, sm, &flag) && threadIdx.x == 0) {
       count_bytes(B, I, K_ELEM_HESS);  // the element kernel ran on this instance in the same round
       count_bytes(B, I, K_ASSEMBLE);
@@ -824,8 +842,7 @@ __device__ __forceinline__ void st_jacobi(const BatchDev& B, const TileMap& M, i
 #pragma unroll
       for (int k = 0; k < 9; ++k) Mi[(size_t)k * I.n + v] = (Real)inv[k];
     }
-    double p[1] = {0.0}, tot[1];
-    if (tile_done<1>(I, lt, tiles_of(I.n), ncta, p, tot, sm, &flag) && threadIdx.x == 0) {
+    if (tile_count_done(I, lt, tiles_of(I.n), ncta, &flag) && threadIdx.x == 0) {
       count_bytes(B, I, K_JACOBI);
       st->phase = PH_LINSETUP;
       advance(B, i);
@@ -1210,8 +1227,7 @@ __device__ __forceinline__ void st_accum(const BatchDev& B, const TileMap& M, in
       for (int a = 0; a < 3; ++a) d[a] += (double)ev[a];
       st4(I.dx, v, d);
     }
-    double p[1] = {0.0}, tot[1];
-    if (tile_done<1>(I, lt, tiles_of(I.n), ncta, p, tot, sm, &flag) && threadIdx.x == 0) {
+    if (tile_count_done(I, lt, tiles_of(I.n), ncta, &flag) && threadIdx.x == 0) {
       count_bytes(B, I, K_ACCUM);
       st->sweeps++;
       st->total_sweeps++;
