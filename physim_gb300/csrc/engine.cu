@@ -289,6 +289,7 @@ int set_batch(phx_context ctx, const std::vector<phx_instance>& list, BatchDev& 
   B.pre_pcg = ctx->d_pre + 3 * (ctx->cap + 1);
   B.inst = ctx->d_inst;
   B.flags = ctx->d_flags;
+  CU(cudaMemsetAsync(ctx->d_flags, 0, sizeof(int32_t) * 8, ctx->stream));  // [2]: cluster PCG wait gave up
   B.phase_live = ctx->d_phc;
   B.algo_total = ctx->profiling ? ctx->d_algo : nullptr;
   B.cpt = 4;
@@ -550,6 +551,7 @@ int run_step(phx_context ctx, const BatchDev& B0, int num, bool fp64, int pcg_ch
   // thousands of per-tile reductions on its counter)
   B.cpt = (few && max_chunks <= 2048) ? 1 : 4;
   TRY(run_engine(ctx, B, num, fp64, kRoundsPerLaunch, pcg_chunk));
+  if (ctx->h_flags[2]) return set_err(PHX_ETIMEOUT, "cluster PCG reduction wait timed out");
   if (B.cluster_mode && ctx->h_flags[0] > 0 && ctx->h_flags[1] > 0) {
     cudaEvent_t a = nullptr, b = nullptr;
     if (ctx->profiling) TRY(profile_events(ctx, &a, &b));

@@ -1814,25 +1814,27 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT) k_pcg_cluster(B
 // ---------------------------------------------------------------------------
 // The CG recurrence of A. T. Chronopoulos and C. W. Gear ("s-step iterative methods for
 // symmetric linear systems", J. Comput. Appl. Math. 25 (1989)): with s = A z and the extra
-// recurrence q = A p, an iteration needs one SpMV operand (z) and one pair of inner
-// products before it and one after it:
+// recurrence q = A p, all three inner products of an iteration are taken after its SpMV,
+// so an iteration has one cluster barrier (z published) and one reduction:
 //   p = z + b p, q = s + b q, e += a p, r -= a q, z = M^-1 r    (own rows, no exchange)
-//   gamma = (r, z), rho = (r, r)                                 -> cluster barrier 1
+//   partials of gamma = (r, z), rho = (r, r)                     -> cluster barrier
 //   s = (H + shift I) z  (z of other rows read from their CTA)   (own rows)
-//   delta = (z, s)                                               -> cluster barrier 2
+//   gamma, rho, delta = (z, s) summed over the cluster           -> one reduction
 //   b = gamma / gamma_old, eta = delta - b gamma / a_old = (p, A p), a = gamma / eta
-// In exact arithmetic these are the iterates of the two-reduction CG above (Eigen's
-// order); in floating point the variant is known to be about as accurate, unlike the
-// pipelined forms, whose extra recurrences lose accuracy in FP32.
+// In exact arithmetic these are the iterates of the two-reduction CG (Eigen's order); in
+// floating point the variant is known to be about as accurate, unlike the pipelined forms,
+// whose extra recurrences lose accuracy in FP32.  The convergence test on rho comes after
+// the SpMV of the same iteration, which the converged iteration thus computes in vain; the
+// sums and every decision are those of testing rho before it.
 //
 // Each of the CL CTAs owns contiguous SELL chunks.  Everything per row lives in its
 // shared memory for the whole solve: z (read by the other CTAs through distributed shared
 // memory, so the solve makes no global-memory exchange at all), r, e, p, s, q and the
 // 3x3 block-Jacobi inverse; the matrix slices go to shared memory as far as they fit
 // (chunk order), with the slot-row stride padded to 288 + 32/L floats so that the L lanes
-// of a row hit different banks; later chunks are read from global memory.  Each partial
-// sum slot is written before one barrier and read before the next one, so single buffers
-// suffice; z is overwritten only after barrier 2, when no CTA reads it any more.
+// of a row hit different banks; later chunks are read from global memory.  z is
+// overwritten only after the reduction, whose sums every CTA computes from its SpMV: no
+// CTA reads the previous z any more.
 constexpr int kCgSmem = 220 * 1024;  // dynamic shared memory per CTA of k_pcg_cg
 constexpr int kCgMaxChunks = (kClusterMaxNodes + 31) / 32;
 constexpr int kCgMaxCpc = (kCgMaxChunks + kCl - 1) / kCl;
@@ -1840,6 +1842,7 @@ static_assert(((4 * kCgMaxChunks + 15) & ~15) + ((4 * (kCgMaxCpc + 1) + 15) & ~1
                   kCgSmem,
               "rows of the largest cluster instance must fit in shared memory");
 
+constexpr int kLinAbort = -1;  // a reduction wait gave up: the kernel returns at once
 struct CgResult {  // FP32 like the solve; widened once when written to the instance state
   int iter, done, status;
   float rr, eta, gamma, beta;
@@ -1869,14 +1872,24 @@ __device__ __forceinline__ float4 cl_ld4f(uint32_t a) {
   return v;
 }
 
-// Cluster-wide sums of K <= 3 FP32 partials: warp shuffles, one __syncthreads, warp 0
-// pushes the CTA's sums into slot [rank] of every CTA, one cluster barrier, then every
-// thread adds the CL slots in rank order (the same sums, hence the same decisions,
-// everywhere).  FP32 throughout: this part has a small fraction of FP32's FP64 rate, and
-// the PCG accumulates in FP32 by design (the FP64 residual of the refinement sweep decides).
+// Cluster-wide sums of K <= 3 FP32 partials: warp shuffles, one __syncthreads, then lanes
+// 0..CL-1 of warp 0 push the CTA's sums with st.async into slot [rank] of every CTA, each
+// store completing bytes on the receiving CTA's mbarrier; every thread waits for its own
+// mbarrier's phase and adds the CL slots in rank order (the same sums, hence the same
+// decisions, everywhere).  No cluster barrier and no fence: the slots carry only the sums,
+// and the mbarrier makes them visible.  FP32 throughout: this part has a small fraction of
+// FP32's FP64 rate, and the PCG accumulates in FP32 by design (the FP64 residual of the
+// refinement sweep decides).
+//
+// Reuse of the single slot buffer, ws and the mbarrier needs no barrier of its own: a CTA
+// pushes the sums of the next reduction only after the cluster barrier that follows its
+// next update, which every CTA reaches only after reading this reduction's slots; warp 0
+// reads ws before its push, which every wait depends on.  The wait gives up after
+// kCgWaitCycles (the cluster is then broken): it flags the batch error and returns false.
+constexpr long long kCgWaitCycles = 2000000000LL;
 template <int K, int CL, int NT>
-__device__ __forceinline__ void cg_reduce(float (&p)[K], unsigned rank, float (*red)[4], float (*ws)[4],
-                                          float (&tot)[K]) {
+__device__ __forceinline__ bool cg_reduce(float (&p)[K], unsigned rank, float (*red)[4], float (*ws)[4], uint32_t mbar,
+                                          unsigned& phase, int32_t* err, float (&tot)[K]) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < K; ++k)
@@ -1887,7 +1900,7 @@ __device__ __forceinline__ void cg_reduce(float (&p)[K], unsigned rank, float (*
     for (int k = 0; k < K; ++k) ws[warp][k] = p[k];
   __syncthreads();
   if (warp == 0) {
-    float v[K];
+    float v[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int k = 0; k < K; ++k) {
       v[k] = lane < NT / 32 ? ws[lane][k] : 0.f;
@@ -1895,13 +1908,33 @@ __device__ __forceinline__ void cg_reduce(float (&p)[K], unsigned rank, float (*
       for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], off);
       v[k] = __shfl_sync(0xffffffffu, v[k], 0);
     }
+    if (lane == 0)
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(CL * 16) : "memory");
     if (lane < CL) {
       const uint32_t dst = cl_map(smem_u32(&red[rank][0]), (unsigned)lane);
-#pragma unroll
-      for (int k = 0; k < K; ++k) asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(dst + 4 * k), "f"(v[k]) : "memory");
+      const uint32_t mb = cl_map(mbar, (unsigned)lane);
+      asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.f32 [%0], {%1, %2, %3, %4}, [%5];"
+                   ::"r"(dst), "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "r"(mb)
+                   : "memory");
     }
   }
-  cl_sync();
+  const unsigned parity = phase & 1u;
+  ++phase;
+  const long long t0 = clock64();
+  for (;;) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (done) break;
+    if (clock64() - t0 > kCgWaitCycles) {
+      atomicExch(err, 1);
+      return false;
+    }
+  }
 #pragma unroll
   for (int k = 0; k < K; ++k) {
     float s = 0.f;
@@ -1909,6 +1942,7 @@ __device__ __forceinline__ void cg_reduce(float (&p)[K], unsigned rank, float (*
     for (int r = 0; r < CL; ++r) s += red[r][k];
     tot[k] = s;
   }
+  return true;
 }
 
 // s = (H + shift I) z for the CTA's rows, L lanes per row, and the partial (z, s).
@@ -1982,8 +2016,9 @@ __device__ __forceinline__ float cg_spmv(const InstDev& I, const CgShared& S, in
 // Scalars and inner products in FP32; the results go back to the FP64 state.
 template <int L, int CL, int NT>
 __device__ __forceinline__ CgResult cg_solve(const InstDev& I, const CgShared& S, unsigned rank, int c0, int row0,
-                                          int row1, int64_t sb, float (*red1)[4], float (*red2)[4], float (*ws)[4],
-                                          float sh, float thr, int maxit, bool trunc_ok, int iter0) {
+                                          int row1, int64_t sb, float (*red)[4], float (*ws)[4], uint32_t mbar,
+                                          unsigned& phase, int32_t* err, float sh, float thr, int maxit, bool trunc_ok,
+                                          int iter0) {
   const int nrow = row1 - row0, ms = S.mrows;
   CgResult out{iter0, 0, LIN_RUNNING, 0.f, 0.f, 0.f, 0.f};
   // start: r and z = M^-1 r from the residual stage, e = 0
@@ -1998,18 +2033,20 @@ __device__ __forceinline__ CgResult cg_solve(const InstDev& I, const CgShared& S
     g1[0] += r[0] * z[0] + r[1] * z[1] + r[2] * z[2];
     g1[1] += r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
   }
-  float t1[2];
-  cg_reduce<2, CL, NT>(g1, rank, red1, ws, t1);
-  float gam = t1[0];
-  out.rr = t1[1];
-  if (t1[1] < thr) {
+  cl_sync();  // z of every CTA written
+  float p3[3] = {g1[0], g1[1], cg_spmv<L, NT>(I, S, c0, row0, row1, sb, sh)};
+  float t3[3];
+  if (!cg_reduce<3, CL, NT>(p3, rank, red, ws, mbar, phase, err, t3)) {
+    out.status = kLinAbort;
+    return out;
+  }
+  float gam = t3[0];
+  out.rr = t3[1];
+  if (t3[1] < thr) {
     out.status = LIN_CONVERGED;
     return out;
   }
-  float d2[1] = {cg_spmv<L, NT>(I, S, c0, row0, row1, sb, sh)};
-  float t2[1];
-  cg_reduce<1, CL, NT>(d2, rank, red2, ws, t2);
-  float eta = t2[0], beta = 0.f, alpha;
+  float eta = t3[2], beta = 0.f, alpha;
   bool last = false;
   out.eta = eta;
   out.gamma = gam;
@@ -2065,19 +2102,21 @@ __device__ __forceinline__ CgResult cg_solve(const InstDev& I, const CgShared& S
       out.status = LIN_TRUNCATED;
       break;
     }
-    float tg[2];
-    cg_reduce<2, CL, NT>(g, rank, red1, ws, tg);
+    cl_sync();  // the new z of every CTA written; none reads the previous z any more
+    float pg[3] = {g[0], g[1], cg_spmv<L, NT>(I, S, c0, row0, row1, sb, sh)};
+    float tg[3];
+    if (!cg_reduce<3, CL, NT>(pg, rank, red, ws, mbar, phase, err, tg)) {
+      out.status = kLinAbort;
+      return out;
+    }
     const float gam_new = tg[0];
     out.rr = tg[1];
     if (tg[1] < thr) {
       out.status = LIN_CONVERGED;
       break;
     }
-    float d[1] = {cg_spmv<L, NT>(I, S, c0, row0, row1, sb, sh)};
-    float td[1];
-    cg_reduce<1, CL, NT>(d, rank, red2, ws, td);
     beta = gam_new / gam;
-    eta = td[0] - beta * gam_new / alpha;
+    eta = tg[2] - beta * gam_new / alpha;
     gam = gam_new;
     out.eta = eta;
     out.gamma = gam;
@@ -2095,10 +2134,19 @@ template <int CL, int NT>
 __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_pcg_cg(BatchDev B, const int32_t* list,
                                                                                int count) {
   extern __shared__ __align__(16) unsigned char cg_smem[];
-  __shared__ float red1[CL][4], red2[CL][4];  // partial sums pushed by every CTA of the cluster
+  __shared__ __align__(16) float red[CL][4];  // partial sums pushed by every CTA of the cluster
   __shared__ float ws[NT / 32][4];
+  __shared__ __align__(8) uint64_t mbar_obj;   // completes when all CL pushes of a reduction landed
   const unsigned rank = cl_rank();
   const int tid = threadIdx.x;
+  const uint32_t mbar = smem_u32(&mbar_obj);
+  unsigned phase = 0;  // reductions waited for so far (the mbarrier's phase)
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  cl_sync();  // every mbarrier initialised before any CTA pushes to it
+  int32_t* err = B.flags + 2;
   for (int j = (int)cl_id(); j < count; j += (int)cl_count()) {
     const int i = __ldg(list + j);
     const InstDev& I = B.inst[i];  // fields are re-read (L1) where needed: registers go to the rows
@@ -2176,9 +2224,13 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_pcg_cg(Bat
     const bool trunc_ok = I.opts->precision != 0;
     const int iter0 = st->pcg_iter;
     CgResult out;
-    if (L == 4) out = cg_solve<4, CL, NT>(I, S, rank, c0, row0, row1, sb, red1, red2, ws, sh, thr, maxit, trunc_ok, iter0);
-    else if (L == 2) out = cg_solve<2, CL, NT>(I, S, rank, c0, row0, row1, sb, red1, red2, ws, sh, thr, maxit, trunc_ok, iter0);
-    else out = cg_solve<1, CL, NT>(I, S, rank, c0, row0, row1, sb, red1, red2, ws, sh, thr, maxit, trunc_ok, iter0);
+    if (L == 4) out = cg_solve<4, CL, NT>(I, S, rank, c0, row0, row1, sb, red, ws, mbar, phase, err, sh, thr, maxit,
+                                           trunc_ok, iter0);
+    else if (L == 2) out = cg_solve<2, CL, NT>(I, S, rank, c0, row0, row1, sb, red, ws, mbar, phase, err, sh, thr, maxit,
+                                           trunc_ok, iter0);
+    else out = cg_solve<1, CL, NT>(I, S, rank, c0, row0, row1, sb, red, ws, mbar, phase, err, sh, thr, maxit,
+                                           trunc_ok, iter0);
+    if (out.status == kLinAbort) return;  // batch error flagged; the host reports a timeout
     for (int t = tid; t < nrow; t += NT) {
       const float4 e = S.e[t];
       const float ev[3] = {e.x, e.y, e.z};

@@ -167,7 +167,8 @@ struct BatchDev {
   const int32_t* pre_lob;
   const int32_t* pre_pcg;     // PCG tiles (InstDev::cpt chunks each)
   InstDev* inst;              // [num]
-  int32_t* flags;             // [8 + num]: [0] active count; [8 + i] phase of instance i
+  int32_t* flags;             // [8 + num]: [0] active count, [1] cluster solves waiting, [2] a cluster
+                              // PCG wait gave up; [8 + i] phase of instance i
   double* algo_total;         // [16] algorithmic bytes summed per kernel kind, or null
   int32_t* phase_live;        // [32] active instances per phase bucket: [0..15] kept current by
                               // advance(), [16..31] the copy taken at the last grid barrier, or null
