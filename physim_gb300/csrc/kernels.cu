@@ -1847,14 +1847,22 @@ struct CgResult {  // FP32 like the solve; widened once when written to the inst
   int iter, done, status;
   float rr, eta, gamma, beta;
 };
-struct CgShared {  // per-CTA layout, the same offsets in every CTA of the cluster
-  const uint32_t* tab;  // [nch] distributed-shared address of each chunk's z rows
-  const int* co;        // [cpc + 1] own chunk offsets (slots)
-  float4 *z, *r, *e, *p, *s, *q;  // [mrows]
-  float* mi;            // [9][mrows] block-Jacobi inverses, plane-major
-  int mrows;            // rows of every vector array (32 per owned chunk slot)
-  const float* hs;      // own matrix slices, slot-row stride hst (chunks c0 .. csplit-1)
-  const int* cs;        // their column ids, slot-row stride cst
+// Dynamic shared memory of k_pcg_cg, declared at file scope so that the helpers below form
+// their pointers from it: the compiler then knows every one of them is shared and issues
+// shared-memory loads and stores, rather than generic ones through the pointers of a struct.
+extern __shared__ __align__(16) unsigned char cg_smem[];
+template <typename T>
+__device__ __forceinline__ T* cgs(uint32_t off) {
+  return reinterpret_cast<T*>(cg_smem + off);
+}
+
+struct CgShared {  // per-CTA layout (byte offsets into cg_smem), the same in every CTA of the cluster
+  uint32_t tab;                // u32[nch] distributed-shared address of each chunk's z rows
+  uint32_t co;                 // i32[cpc + 1] own chunk offsets (slots)
+  uint32_t z, r, e, p, s, q;   // float4[mrows]
+  uint32_t mi;                 // f32[9][mrows] block-Jacobi inverses, plane-major
+  uint32_t hs, cs;             // own matrix slices (chunks c0 .. csplit-1), slot-row strides hst, cst
+  int mrows;                   // rows of every vector array (32 per owned chunk slot)
   int hst, cst, csplit;
 };
 
@@ -1945,16 +1953,62 @@ __device__ __forceinline__ bool cg_reduce(float (&p)[K], unsigned rank, float (*
   return true;
 }
 
-// s = (H + shift I) z for the CTA's rows, L lanes per row, and the partial (z, s).
-// Four slots at a time per lane: their column ids and blocks are loaded together, then
-// the z gathers (own rows from this CTA's shared memory, other rows through distributed
-// shared memory), then the arithmetic: two dependent round trips per four slots.
+// The slots k = sub, sub + L, ... < len of one row (lane `lane` of its chunk) from slot-row
+// R0 on, accumulated into acc: four slots at a time per lane, their column ids and blocks
+// loaded together, then the z gathers (own rows from this CTA's shared memory, other rows
+// through distributed shared memory), then the arithmetic.  SM: the slices are in shared
+// memory (stride hst, cst); otherwise in global memory (stride 288, 32), read-only.
+template <int L, bool SM>
+__device__ __forceinline__ void cg_row(const float* hb, const int* cb, int hst, int cst, int R0, int len, int lane,
+                                       int sub, const float4* Z, const uint32_t* tab, int row0, int nrow,
+                                       float (&acc)[3]) {
+  for (int k0 = sub; k0 < len; k0 += 4 * L) {
+    int col[4];
+    float h[4][9];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int k = k0 + u * L;
+      const bool in = k < len;
+      const int R = R0 + (in ? k : 0);
+      const float* hp = hb + (size_t)R * hst + lane;
+      if (SM) {
+        col[u] = in ? cb[R * cst + lane] : -1;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) h[u][q] = in ? hp[q * 32] : 0.f;
+      } else {
+        col[u] = in ? __ldg(cb + (size_t)R * cst + lane) : -1;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) h[u][q] = in ? __ldg(hp + q * 32) : 0.f;
+      }
+    }
+    float4 x[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int cc = col[u];
+      const unsigned lr = (unsigned)(cc - row0);
+      if (cc < 0) x[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+      else if (lr < (unsigned)nrow) x[u] = Z[lr];
+      else x[u] = cl_ld4f(tab[cc >> 5] + ((uint32_t)(cc & 31) << 4));
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      acc[0] += h[u][0] * x[u].x + h[u][1] * x[u].y + h[u][2] * x[u].z;
+      acc[1] += h[u][3] * x[u].x + h[u][4] * x[u].y + h[u][5] * x[u].z;
+      acc[2] += h[u][6] * x[u].x + h[u][7] * x[u].y + h[u][8] * x[u].z;
+    }
+  }
+}
+
+// s = (H + shift I) z for the CTA's rows, L lanes per row, and the partial (z, s): two
+// dependent round trips per four slots of a lane.
 template <int L, int NT>
 __device__ __forceinline__ float cg_spmv(const InstDev& I, const CgShared& S, int c0, int row0, int row1, int64_t sb,
                                          float sh) {
-  const int sub = threadIdx.x & (L - 1), grp = threadIdx.x / L;
-  const float* hg = I.H32 + (sb >> 5) * 288;
-  const int* cg = I.slot_col + sb;
+  const int sub = threadIdx.x & (L - 1), grp = threadIdx.x / L, nrow = row1 - row0;
+  const float4* Z = cgs<const float4>(S.z);
+  float4* Sv = cgs<float4>(S.s);
+  const int* co = cgs<const int>(S.co);
+  const uint32_t* tab = cgs<const uint32_t>(S.tab);
   float part = 0.f;
   for (int base = row0; base < row1; base += NT / L) {
     const int v = base + grp;
@@ -1962,50 +2016,23 @@ __device__ __forceinline__ float cg_spmv(const InstDev& I, const CgShared& S, in
     float acc[3] = {0.f, 0.f, 0.f};
     if (ok) {
       const int c = v >> 5, lane = v & 31;
-      const int s0 = S.co[c - c0], len = (S.co[c - c0 + 1] - s0) >> 5;
+      const int s0 = co[c - c0], len = (co[c - c0 + 1] - s0) >> 5;
       const int R0 = (int)((s0 - sb) >> 5);
-      const bool sm = c < S.csplit;
-      const float* hb = sm ? S.hs : hg;
-      const int* cb = sm ? S.cs : cg;
-      const int hst = sm ? S.hst : 288, cst = sm ? S.cst : 32;
-      for (int k0 = sub; k0 < len; k0 += 4 * L) {
-        int col[4];
-        float h[4][9];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int k = k0 + u * L;
-          const bool in = k < len;
-          const int R = R0 + (in ? k : 0);
-          col[u] = in ? cb[R * cst + lane] : -1;
-          const float* hp = hb + (size_t)R * hst + lane;
-#pragma unroll
-          for (int q = 0; q < 9; ++q) h[u][q] = in ? hp[q * 32] : 0.f;
-        }
-        float4 x[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int cc = col[u];
-          const unsigned lr = (unsigned)(cc - row0);
-          if (cc < 0) x[u] = make_float4(0.f, 0.f, 0.f, 0.f);
-          else if (lr < (unsigned)(row1 - row0)) x[u] = S.z[lr];
-          else x[u] = cl_ld4f(S.tab[cc >> 5] + ((uint32_t)(cc & 31) << 4));
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          acc[0] += h[u][0] * x[u].x + h[u][1] * x[u].y + h[u][2] * x[u].z;
-          acc[1] += h[u][3] * x[u].x + h[u][4] * x[u].y + h[u][5] * x[u].z;
-          acc[2] += h[u][6] * x[u].x + h[u][7] * x[u].y + h[u][8] * x[u].z;
-        }
-      }
+      if (c < S.csplit)
+        cg_row<L, true>(cgs<const float>(S.hs), cgs<const int>(S.cs), S.hst, S.cst, R0, len, lane, sub, Z, tab, row0,
+                        nrow, acc);
+      else
+        cg_row<L, false>(I.H32 + (sb >> 5) * 288, I.slot_col + sb, 288, 32, R0, len, lane, sub, Z, tab, row0, nrow,
+                         acc);
     }
 #pragma unroll
     for (int off = 1; off < L; off <<= 1)
 #pragma unroll
       for (int a = 0; a < 3; ++a) acc[a] += __shfl_xor_sync(0xffffffffu, acc[a], off);
     if (ok && sub == 0) {
-      const float4 z = S.z[v - row0];
+      const float4 z = Z[v - row0];
       const float4 s = make_float4(acc[0] + sh * z.x, acc[1] + sh * z.y, acc[2] + sh * z.z, 0.f);
-      const_cast<float4*>(S.s)[v - row0] = s;
+      Sv[v - row0] = s;
       part += z.x * s.x + z.y * s.y + z.z * s.z;
     }
   }
@@ -2020,6 +2047,13 @@ __device__ __forceinline__ CgResult cg_solve(const InstDev& I, const CgShared& S
                                           unsigned& phase, int32_t* err, float sh, float thr, int maxit, bool trunc_ok,
                                           int iter0) {
   const int nrow = row1 - row0, ms = S.mrows;
+  float4* const Z = cgs<float4>(S.z);
+  float4* const Rv = cgs<float4>(S.r);
+  float4* const Ev = cgs<float4>(S.e);
+  float4* const Pv = cgs<float4>(S.p);
+  float4* const Sv = cgs<float4>(S.s);
+  float4* const Qv = cgs<float4>(S.q);
+  const float* const Mi = cgs<const float>(S.mi);
   CgResult out{iter0, 0, LIN_RUNNING, 0.f, 0.f, 0.f, 0.f};
   // start: r and z = M^-1 r from the residual stage, e = 0
   float g1[2] = {0.f, 0.f};
@@ -2027,9 +2061,9 @@ __device__ __forceinline__ CgResult cg_solve(const InstDev& I, const CgShared& S
     float r[3], z[3];
     ld4(I.r32, row0 + t, r);
     ld4(I.z32, row0 + t, z);
-    S.r[t] = make_float4(r[0], r[1], r[2], 0.f);
-    S.z[t] = make_float4(z[0], z[1], z[2], 0.f);
-    S.e[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+    Rv[t] = make_float4(r[0], r[1], r[2], 0.f);
+    Z[t] = make_float4(z[0], z[1], z[2], 0.f);
+    Ev[t] = make_float4(0.f, 0.f, 0.f, 0.f);
     g1[0] += r[0] * z[0] + r[1] * z[1] + r[2] * z[2];
     g1[1] += r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
   }
@@ -2069,30 +2103,30 @@ __device__ __forceinline__ CgResult cg_solve(const InstDev& I, const CgShared& S
     const bool first = it == 0;
     float g[2] = {0.f, 0.f};
     for (int t = threadIdx.x; t < nrow; t += NT) {
-      const float4 z = S.z[t], s = S.s[t];
-      float4 p = first ? z : S.p[t], q = first ? s : S.q[t];
+      const float4 z = Z[t], s = Sv[t];
+      float4 p = first ? z : Pv[t], q = first ? s : Qv[t];
       if (!first) {
         p = make_float4(z.x + b * p.x, z.y + b * p.y, z.z + b * p.z, 0.f);
         q = make_float4(s.x + b * q.x, s.y + b * q.y, s.z + b * q.z, 0.f);
       }
-      float4 e = S.e[t];
+      float4 e = Ev[t];
       e.x += a * p.x;
       e.y += a * p.y;
       e.z += a * p.z;
-      S.e[t] = e;
+      Ev[t] = e;
       if (last) continue;
-      float4 r = S.r[t];
+      float4 r = Rv[t];
       r.x -= a * q.x;
       r.y -= a * q.y;
       r.z -= a * q.z;
-      const float* m = S.mi + t;
+      const float* m = Mi + t;
       const float zx = m[0] * r.x + m[ms] * r.y + m[2 * ms] * r.z;
       const float zy = m[3 * ms] * r.x + m[4 * ms] * r.y + m[5 * ms] * r.z;
       const float zz = m[6 * ms] * r.x + m[7 * ms] * r.y + m[8 * ms] * r.z;
-      S.p[t] = p;
-      S.q[t] = q;
-      S.r[t] = r;
-      S.z[t] = make_float4(zx, zy, zz, 0.f);
+      Pv[t] = p;
+      Qv[t] = q;
+      Rv[t] = r;
+      Z[t] = make_float4(zx, zy, zz, 0.f);
       g[0] += r.x * zx + r.y * zy + r.z * zz;
       g[1] += r.x * r.x + r.y * r.y + r.z * r.z;
     }
@@ -2133,7 +2167,6 @@ __device__ __forceinline__ CgResult cg_solve(const InstDev& I, const CgShared& S
 template <int CL, int NT>
 __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_pcg_cg(BatchDev B, const int32_t* list,
                                                                                int count) {
-  extern __shared__ __align__(16) unsigned char cg_smem[];
   __shared__ __align__(16) float red[CL][4];  // partial sums pushed by every CTA of the cluster
   __shared__ float ws[NT / 32][4];
   __shared__ __align__(8) uint64_t mbar_obj;   // completes when all CL pushes of a reduction landed
@@ -2159,43 +2192,43 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_pcg_cg(Bat
     const int mrows = 32 * cpc;
     const int L = nrow <= NT / 4 ? 4 : (nrow <= NT / 2 ? 2 : 1);
     // shared layout: tab u32[nch] | co i32[cpc+1] | z r e p s q float4[mrows] | mi f32[9][mrows] | matrix
-    int64_t off = 0;
-    uint32_t* tab = reinterpret_cast<uint32_t*>(cg_smem);
-    off += ((int64_t)4 * nch + 15) & ~15;
-    int* co = reinterpret_cast<int*>(cg_smem + off);
-    off += ((int64_t)4 * (cpc + 1) + 15) & ~15;
-    float4* vz = reinterpret_cast<float4*>(cg_smem + off);
     CgShared S;
-    S.tab = tab;
-    S.co = co;
-    S.z = vz;
-    S.r = vz + mrows;
-    S.e = vz + 2 * mrows;
-    S.p = vz + 3 * mrows;
-    S.s = vz + 4 * mrows;
-    S.q = vz + 5 * mrows;
-    off += (int64_t)6 * 16 * mrows;
-    S.mi = reinterpret_cast<float*>(cg_smem + off);
+    uint32_t off = 0;
+    S.tab = off;
+    off += (4u * nch + 15u) & ~15u;
+    S.co = off;
+    off += (4u * (cpc + 1) + 15u) & ~15u;
+    S.z = off;
+    S.r = S.z + 16u * mrows;
+    S.e = S.r + 16u * mrows;
+    S.p = S.e + 16u * mrows;
+    S.s = S.p + 16u * mrows;
+    S.q = S.s + 16u * mrows;
+    off = S.q + 16u * mrows;
+    S.mi = off;
     S.mrows = mrows;
-    off += (int64_t)9 * 4 * mrows;
-    off = (off + 15) & ~(int64_t)15;
+    off += 36u * mrows;
+    off = (off + 15u) & ~15u;
+    uint32_t* tab = cgs<uint32_t>(S.tab);
+    int* co = cgs<int>(S.co);
+    float* mi = cgs<float>(S.mi);
     const int64_t sb = __ldg(I.chunk_off + c0);
     // matrix slices of chunks c0 .. csplit-1 in shared memory, slot-row stride padded per L
     const int pad = L == 1 ? 0 : 32 / L;
     S.hst = 288 + pad;
     S.cst = 32 + pad;
     const int64_t per_row = (int64_t)4 * (S.hst + S.cst);  // bytes per slot-row of 32 slots
-    const int64_t room = kCgSmem - off;
+    const int64_t room = (int64_t)kCgSmem - off;
     int csplit = c0;
     while (csplit < c1 && (int64_t)((__ldg(I.chunk_off + csplit + 1) - sb) >> 5) * per_row <= room) ++csplit;
     S.csplit = csplit;
     const int nsr = (int)((__ldg(I.chunk_off + csplit) - sb) >> 5);  // slot-rows held in shared memory
-    float* hs = reinterpret_cast<float*>(cg_smem + off);
-    int* cs = reinterpret_cast<int*>(cg_smem + off + (int64_t)4 * S.hst * nsr);
-    S.hs = hs;
-    S.cs = cs;
+    S.hs = off;
+    S.cs = off + 4u * S.hst * nsr;
+    float* hs = cgs<float>(S.hs);
+    int* cs = cgs<int>(S.cs);
     // fill: chunk table, chunk offsets, inverses, matrix slices
-    const uint32_t zloc = smem_u32(vz);
+    const uint32_t zloc = smem_u32(cgs<float4>(S.z));
     for (int c = tid; c < nch; c += NT) {
       const int owner = c / cpc;
       tab[c] = cl_map(zloc, (unsigned)owner) + (uint32_t)((c - owner * cpc) * 32 * 16);
@@ -2203,7 +2236,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_pcg_cg(Bat
     for (int c = tid; c <= c1 - c0; c += NT) co[c] = __ldg(I.chunk_off + c0 + c);
     for (int k = tid; k < 9 * nrow; k += NT) {
       const int plane = k / nrow, t = k - plane * nrow;
-      S.mi[plane * mrows + t] = __ldg(I.minv32 + (size_t)plane * n + row0 + t);
+      mi[plane * mrows + t] = __ldg(I.minv32 + (size_t)plane * n + row0 + t);
     }
     {
       const float* hg = I.H32 + (sb >> 5) * 288;
@@ -2232,7 +2265,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_pcg_cg(Bat
                                            trunc_ok, iter0);
     if (out.status == kLinAbort) return;  // batch error flagged; the host reports a timeout
     for (int t = tid; t < nrow; t += NT) {
-      const float4 e = S.e[t];
+      const float4 e = cgs<float4>(S.e)[t];
       const float ev[3] = {e.x, e.y, e.z};
       st4(I.e32, row0 + t, ev);
     }
