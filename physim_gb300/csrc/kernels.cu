@@ -755,33 +755,52 @@ __device__ __forceinline__ void st_assemble(const BatchDev& B, const TileMap& M,
     const bool dyn = I.opts->dynamic != 0, nofix = st->nofix != 0;
     const double dt = I.opts->dt;
     Real nrm = 0;  // ||A||_F^2 of the stored entries, for the regularisation threshold only
-    for (int it = threadIdx.x; it < kTile * 9; it += blockDim.x) {
-      const int k = lt * kTile + it / 9, ent = it % 9, a = ent / 3, b = ent % 3;
-      if (k >= I.nlo) break;
-      Real s = 0;
+    // one thread per stored block, its nine entries together: the contributions' ids four at
+    // a time, then their nine values each, so that a block costs few dependent round trips;
+    // every entry adds its contributions in element order
+    const int k = lt * kTile + threadIdx.x;
+    if (k < I.nlo) {
+      Real s[9];
+#pragma unroll
+      for (int e = 0; e < 9; ++e) s[e] = 0;
       const int c0 = I.seg_ptr[k], c1 = I.seg_ptr[k + 1];
       int c = c0;
-      // four contributions in flight (ids, then values), added in element order
       for (; c + 4 <= c1; c += 4) {
         int id[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) id[u] = I.seg_c[c + u];
-        Real val[4];
+        Real val[4][9];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) val[u] = Hloc[(size_t)id[u] * 9 + ent];
+        for (int u = 0; u < 4; ++u)
 #pragma unroll
-        for (int u = 0; u < 4; ++u) s += val[u];
+          for (int e = 0; e < 9; ++e) val[u][e] = Hloc[(size_t)id[u] * 9 + e];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int e = 0; e < 9; ++e) s[e] += val[u][e];
       }
-      for (; c < c1; ++c) s += Hloc[(size_t)I.seg_c[c] * 9 + ent];
+      for (; c < c1; ++c) {
+        const Real* hv = Hloc + (size_t)I.seg_c[c] * 9;
+#pragma unroll
+        for (int e = 0; e < 9; ++e) s[e] += hv[e];
+      }
       const int R = I.lo_rc[2 * k], C = I.lo_rc[2 * k + 1];
-      if (dyn && R == C && a == b) s += (Real)(I.mass[R] / (dt * dt));
-      if (!nofix) {
-        const bool fr = (I.fixmask[R] >> a) & 1, fc = (I.fixmask[C] >> b) & 1;
-        if (fr || fc) s = (R == C && a == b) ? (Real)1 : (Real)0;
+      const int64_t lo = I.lo_slot[k], up = R != C ? I.up_slot[k] : -1;
+      Real* const Hlo = H + sell_addr(lo, 0);  // entry e of a slot at +32 e
+      Real* const Hup = up >= 0 ? H + sell_addr(up, 0) : nullptr;
+      const int fr = nofix ? 0 : I.fixmask[R], fc = nofix ? 0 : I.fixmask[C];
+      const bool diag = dyn && R == C;
+      const Real md = diag ? (Real)(I.mass[R] / (dt * dt)) : (Real)0;
+#pragma unroll
+      for (int e = 0; e < 9; ++e) {
+        const int a = e / 3, b = e % 3;
+        Real v = s[e];
+        if (diag && a == b) v += md;
+        if (((fr >> a) | (fc >> b)) & 1) v = (R == C && a == b) ? (Real)1 : (Real)0;
+        Hlo[32 * e] = v;
+        if (Hup) Hup[32 * (b * 3 + a)] = v;
+        nrm += v * v;
       }
-      H[sell_addr(I.lo_slot[k], ent)] = s;
-      if (R != C) H[sell_addr(I.up_slot[k], b * 3 + a)] = s;
-      nrm += s * s;
     }
     Real p[1] = {nrm};
     double tot[1];
@@ -795,7 +814,7 @@ __device__ __forceinline__ void st_assemble(const BatchDev& B, const TileMap& M,
 }
 
 template <typename Real>
-__global__ void __launch_bounds__(288) k_assemble(BatchDev B) {
+__global__ void __launch_bounds__(kTile) k_assemble(BatchDev B) {
   __shared__ double sm[32 * 5];
   __shared__ int flag;
   st_assemble<Real>(B, full_map(B, B.pre_lob), blockIdx.x, gridDim.x, sm, flag);
@@ -2348,7 +2367,7 @@ void launch(KernelId id, int grid, cudaStream_t s, const BatchDev& B, bool fp64)
       else k_elem_hess<float><<<grid, kTile, hess_smem<float>(), s>>>(B);
       break;
     case K_ASSEMBLE:
-      if (fp64) k_assemble<double><<<grid, 288, 0, s>>>(B); else k_assemble<float><<<grid, 288, 0, s>>>(B);
+      if (fp64) k_assemble<double><<<grid, kTile, 0, s>>>(B); else k_assemble<float><<<grid, kTile, 0, s>>>(B);
       break;
     case K_JACOBI:
       if (fp64) k_jacobi<double><<<grid, kTile, 0, s>>>(B); else k_jacobi<float><<<grid, kTile, 0, s>>>(B);
