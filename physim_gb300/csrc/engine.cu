@@ -494,7 +494,8 @@ int run_engine(phx_context ctx, const BatchDev& B, int num, bool fp64, int round
   CU(cudaMemsetAsync(ctx->d_bar, 0, 2 * sizeof(GridBar), ctx->stream));
   const int32_t hdr[2] = {0, grid};  // active count (set by the kernel), CTAs running
   CU(cudaMemcpyAsync(ctx->d_act, hdr, sizeof(hdr), cudaMemcpyHostToDevice, ctx->stream));
-  EngineArgs A{ctx->d_bar, ctx->d_act, ctx->profiling ? ctx->d_stage : nullptr, ctx->cap, rounds, pcg_chunk};
+  EngineArgs A{ctx->d_bar, ctx->d_act, ctx->profiling ? ctx->d_stage : nullptr, ctx->cap, rounds, pcg_chunk,
+               kWaitRounds, kWaitShare};
   cudaEvent_t a = nullptr, b = nullptr;
   if (ctx->profiling) TRY(profile_events(ctx, &a, &b));
   CU(launch_engine(fp64, grid, ctx->stream, B, A));

@@ -1489,12 +1489,12 @@ __global__ void __launch_bounds__(kTile, (sizeof(Real) == 4 ? 3 : 2)) k_engine(B
     PHX_SYNC(alive, 1, K_CONTROL);
     const int na = __ldcg(A.act);
     if (na == 0) break;
-    // hand over to the cluster PCG kernel once half the active instances wait for it, or
-    // kWaitRounds rounds after the first one started waiting (the others keep going in
+    // hand over to the cluster PCG kernel once 1/wait_share of the active instances wait for
+    // it, or wait_rounds rounds after the first one started waiting (the others keep going in
     // between: line-search trials and element passes do not need the cluster kernel)
     const int waiting = __ldcg(A.act + 3);
     if (waiting > 0 && first_wait < 0) first_wait = r;
-    if (r > 0 && waiting > 0 && (2 * waiting >= na || r - first_wait >= kWaitRounds)) break;
+    if (r > 0 && waiting > 0 && (A.wait_share * waiting >= na || r - first_wait >= A.wait_rounds)) break;
     // this round needs only P CTAs (P never grows within a launch: the rest leave)
     const int P = __ldcg(A.act + 1), Pp = __ldcg(A.act + 2);
     if (cta >= P) return;

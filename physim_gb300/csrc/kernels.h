@@ -41,6 +41,8 @@ struct EngineArgs {
   int cap;
   int rounds;
   int pcg_chunk;
+  int wait_rounds;  // hand the waiting instances to the cluster PCG kernel this many rounds after the
+  int wait_share;   // first one waited, or once waiting * wait_share >= active
 };
 
 cudaError_t setup_kernel_attributes();

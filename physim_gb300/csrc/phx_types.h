@@ -34,6 +34,7 @@ constexpr int kClNarrowThreads = 256;  // narrow variant: threads per CTA
 constexpr int kClWideBelow = 32;     // fewer waiting instances than this: wide clusters
 constexpr int kClusterMaxNodes = 13000;  // instances up to this size solve their PCG in one cluster
 constexpr int kWaitRounds = 4;           // engine rounds an instance may wait for the cluster kernel
+constexpr int kWaitShare = 2;            // ... or until 1/kWaitShare of the active instances wait
 
 // Phases of the per-instance Newton state machine (see control in kernels.cu).
 enum Phase : int32_t {
