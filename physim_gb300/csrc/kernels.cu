@@ -1976,7 +1976,8 @@ __device__ __forceinline__ bool cg_reduce(float (&p)[K], unsigned rank, float (*
 // R0 on, accumulated into acc: four slots at a time per lane, their column ids and blocks
 // loaded together, then the z gathers (own rows from this CTA's shared memory, other rows
 // through distributed shared memory), then the arithmetic.  SM: the slices are in shared
-// memory (stride hst, cst); otherwise in global memory (stride 288, 32), read-only.
+// memory (stride hst, cst; planes 0-3 and 4-7 of a slot-row as one float4 per lane, then
+// plane 8); otherwise in global memory (stride 288, 32; plane after plane), read-only.
 template <int L, bool SM>
 __device__ __forceinline__ void cg_row(const float* hb, const int* cb, int hst, int cst, int R0, int len, int lane,
                                        int sub, const float4* Z, const uint32_t* tab, int row0, int nrow,
@@ -1989,12 +1990,16 @@ __device__ __forceinline__ void cg_row(const float* hb, const int* cb, int hst, 
       const int k = k0 + u * L;
       const bool in = k < len;
       const int R = R0 + (in ? k : 0);
-      const float* hp = hb + (size_t)R * hst + lane;
-      if (SM) {
+      if (SM) {  // planes 0-3 and 4-7 as float4 per lane, then plane 8
         col[u] = in ? cb[R * cst + lane] : -1;
-#pragma unroll
-        for (int q = 0; q < 9; ++q) h[u][q] = in ? hp[q * 32] : 0.f;
+        const float* hr = hb + R * hst;
+        const float4 a = in ? reinterpret_cast<const float4*>(hr)[lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 b = in ? reinterpret_cast<const float4*>(hr + 128)[lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+        h[u][0] = a.x; h[u][1] = a.y; h[u][2] = a.z; h[u][3] = a.w;
+        h[u][4] = b.x; h[u][5] = b.y; h[u][6] = b.z; h[u][7] = b.w;
+        h[u][8] = in ? hr[256 + lane] : 0.f;
       } else {
+        const float* hp = hb + (size_t)R * hst + lane;
         col[u] = in ? __ldg(cb + (size_t)R * cst + lane) : -1;
 #pragma unroll
         for (int q = 0; q < 9; ++q) h[u][q] = in ? __ldg(hp + q * 32) : 0.f;
@@ -2260,9 +2265,19 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_pcg_cg(Bat
     {
       const float* hg = I.H32 + (sb >> 5) * 288;
       const int* cg = I.slot_col + sb;
-      for (int k = tid; k < nsr * 72; k += NT) {  // 288 floats = 72 float4 per slot-row
-        const int R = k / 72, w = k - R * 72;
-        reinterpret_cast<float4*>(hs + (size_t)R * S.hst)[w] = __ldg(reinterpret_cast<const float4*>(hg + (size_t)R * 288) + w);
+      // slot-row layout in shared memory: planes 0-3 as one float4 per lane, planes 4-7 as
+      // one float4 per lane, plane 8 (the global layout holds the nine planes one after
+      // the other): a slot's block is three loads, the same bytes
+      for (int k = tid; k < nsr * 32; k += NT) {
+        const int R = k >> 5, l = k & 31;
+        const float* src = hg + (size_t)R * 288 + l;
+        float q[9];
+#pragma unroll
+        for (int e = 0; e < 9; ++e) q[e] = __ldg(src + 32 * e);
+        float* dst = hs + (size_t)R * S.hst;
+        reinterpret_cast<float4*>(dst)[l] = make_float4(q[0], q[1], q[2], q[3]);
+        reinterpret_cast<float4*>(dst + 128)[l] = make_float4(q[4], q[5], q[6], q[7]);
+        dst[256 + l] = q[8];
       }
       for (int k = tid; k < nsr * 8; k += NT) {  // 32 ids = 8 int4 per slot-row
         const int R = k >> 3, w = k & 7;
