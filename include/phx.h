@@ -89,9 +89,11 @@ typedef struct phx_options {
   int32_t ls_num_max_iters;   /* PCG iterations per linear solve */
   double ls_tol_max_error;    /* PCG relative residual ||r|| < tol ||b|| */
   int32_t ls_num_reg_trials;
-  int32_t lsearch_type;       /* 1 Simple */
+  int32_t lsearch_type;       /* LSearchType: 0 None, 1 Simple, 2 Armijo, 3 WolfeWeak, 4 WolfeStrong */
   double lsearch_alpha;
   int32_t lsearch_num_try;
+  double lsearch_wolfe1;      /* Armijo / Wolfe sufficient-decrease constant c1 (1e-4) */
+  double lsearch_wolfe2;      /* Wolfe curvature constant c2 (0.9) */
   /* GPU path */
   int32_t precision;          /* PHX_PREC_* */
   int32_t precond;            /* 0 diagonal (Eigen DiagonalPreconditioner), 1 3x3 block Jacobi */

@@ -34,6 +34,7 @@ class OrcOptions(C.Structure):
                 ("ls_num_max_iters", C.c_int32), ("ls_tol_max_error", C.c_double),
                 ("ls_num_reg_trials", C.c_int32), ("lsearch_type", C.c_int32),
                 ("lsearch_alpha", C.c_double), ("lsearch_num_try", C.c_int32),
+                ("lsearch_wolfe1", C.c_double), ("lsearch_wolfe2", C.c_double),
                 ("cg_block_jacobi", C.c_int32), ("threads", C.c_int32)]
 
 

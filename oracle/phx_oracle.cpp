@@ -961,23 +961,48 @@ int solve_full(orc_handle_s* h, Problem& P, const orc_options* o, orc_report* re
         for (int i = 0; i < N; ++i) dx[i] = (dx[i] / len) * o->max_step_size;
       auto te = clk::now();
       P.tm.opt_sol += secs(ts, te);
-      // LineSearch_Simple
+      // LineSearch_{None,Simple,Armijo,WolfeWeak,WolfeStrong} (OptimSolver.cpp:688-900).
+      // m = dxIn . g with dxIn the clamped step; Armijo uses dxIn normalised (Eigen's
+      // normalized() leaves a zero vector as it is).
+      const int lst = o->lsearch_type;
+      double m = 0;
+      for (int i = 0; i < N; ++i) m += dx[i] * S.vg[i];
+      const double dlen = norm2(dx.data(), N);
+      const double tArm = o->lsearch_wolfe1 * (dlen > 0 ? m / dlen : 0.0);
+      const double t1 = o->lsearch_wolfe1 * m, t2 = -o->lsearch_wolfe2 * m, t3 = o->lsearch_wolfe2 * std::fabs(m);
       double factor = 1.0, objNew = 0;
       bool improved = false;
       P.restore();
-      numBis = -1;
-      do {
-        numBis++;
-        for (int i = 0; i < N; ++i) dxFin[i] = factor * dx[i];
+      if (lst == 0) {  // LineSearch_None: the full step, whatever it does
+        for (int i = 0; i < N; ++i) dxFin[i] = dx[i];
         for (int i = 0; i < N; ++i) P.x[i] += dxFin[i];
         P.pos_perform_step();
         objNew = P.energy();
         P.gradient(gNew);
-        if (objNew < S.obj) { improved = true; break; }
-        factor *= o->lsearch_alpha;
-        P.restore();
-      } while (norm2(dxFin.data(), N) > o->tol_min_step && numBis <= o->lsearch_num_try);
-      (void)improved;
+        numBis = 0;
+        improved = true;
+      } else {
+        numBis = -1;
+        do {
+          numBis++;
+          for (int i = 0; i < N; ++i) dxFin[i] = factor * dx[i];
+          for (int i = 0; i < N; ++i) P.x[i] += dxFin[i];
+          P.pos_perform_step();
+          objNew = P.energy();
+          P.gradient(gNew);
+          double dgn = 0;
+          for (int i = 0; i < N; ++i) dgn += dx[i] * gNew[i];
+          bool ok;
+          if (lst == 2) ok = objNew <= S.obj + factor * tArm;
+          else if (lst == 3) ok = objNew <= S.obj + factor * t1 && -dgn <= t2;
+          else if (lst == 4) ok = objNew <= S.obj + factor * t1 && -dgn <= t2 && std::fabs(dgn) <= t3;
+          else ok = objNew < S.obj;
+          if (ok) { improved = true; break; }
+          factor *= o->lsearch_alpha;
+          P.restore();
+        } while (norm2(dxFin.data(), N) > o->tol_min_step && numBis <= o->lsearch_num_try);
+      }
+      (void)improved;  // UpdateStepResult judges the last trial by its energy alone
       P.tm.opt_lis += secs(te, clk::now());
       // UpdateStepResult
       double impr = S.obj - objNew;
@@ -1084,6 +1109,8 @@ void orc_default_options(orc_options* o) {
   o->lsearch_type = 1;
   o->lsearch_alpha = 0.5;
   o->lsearch_num_try = 32;
+  o->lsearch_wolfe1 = 1e-4;
+  o->lsearch_wolfe2 = 0.9;
   o->cg_block_jacobi = 0;
   o->threads = 0;
 }

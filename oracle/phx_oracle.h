@@ -48,9 +48,11 @@ typedef struct orc_options {
   int32_t ls_num_max_iters;
   double ls_tol_max_error;
   int32_t ls_num_reg_trials;
-  int32_t lsearch_type;      /* 1 = Simple */
+  int32_t lsearch_type;      /* LSearchType: 0 None, 1 Simple, 2 Armijo, 3 WolfeWeak, 4 WolfeStrong */
   double lsearch_alpha;
   int32_t lsearch_num_try;
+  double lsearch_wolfe1;     /* Armijo / Wolfe c1 */
+  double lsearch_wolfe2;     /* Wolfe c2 */
   int32_t cg_block_jacobi;   /* CG preconditioner: 0 = diagonal (Eigen), 1 = 3x3 block Jacobi */
   int32_t threads;           /* OpenMP threads for element loops; <= 0 keeps the default */
 } orc_options;

@@ -57,7 +57,8 @@ class Options(C.Structure):
                 ("min_impr_max_count", C.c_int32), ("num_max_iters", C.c_int32), ("try_steepest", C.c_int32),
                 ("max_step_size", C.c_double), ("ls_solver", C.c_int32), ("ls_num_max_iters", C.c_int32),
                 ("ls_tol_max_error", C.c_double), ("ls_num_reg_trials", C.c_int32), ("lsearch_type", C.c_int32),
-                ("lsearch_alpha", C.c_double), ("lsearch_num_try", C.c_int32), ("precision", C.c_int32),
+                ("lsearch_alpha", C.c_double), ("lsearch_num_try", C.c_int32),
+                ("lsearch_wolfe1", C.c_double), ("lsearch_wolfe2", C.c_double), ("precision", C.c_int32),
                 ("precond", C.c_int32), ("inner_tol", C.c_double), ("max_refine_sweeps", C.c_int32),
                 ("warm_guess", C.c_int32), ("pcg_chunk", C.c_int32), ("tol_rel", C.c_double),
                 ("pcg_cluster", C.c_int32), ("fp64_finish", C.c_int32),

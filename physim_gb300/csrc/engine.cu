@@ -364,6 +364,9 @@ DevOpts make_opts(const phx_options* o, bool dynamic, double dt) {
   d.max_step_size = o->max_step_size;
   d.ls_tol_max_error = o->ls_tol_max_error;
   d.lsearch_alpha = o->lsearch_alpha;
+  d.lsearch_type = o->lsearch_type;
+  d.lsearch_wolfe1 = o->lsearch_wolfe1;
+  d.lsearch_wolfe2 = o->lsearch_wolfe2;
   d.inner_tol = o->inner_tol;
   d.dt = dt;
   d.tol_rel = o->tol_rel;
@@ -375,7 +378,10 @@ int validate_opts(const phx_options* o) {
   if (o->precision != PHX_PREC_FP64 && o->precision != PHX_PREC_FP32_REFINE)
     return set_err(PHX_EINVAL, "options: unknown precision");
   if (o->qp_solver != 0 && o->qp_solver != 1) return set_err(PHX_EINVAL, "options: qp_solver must be 0 (Steepest) or 1 (Newton)");
-  if (o->lsearch_type != 1) return set_err(PHX_EINVAL, "options: only the Simple line search runs on the device");
+  if (o->lsearch_type < 0 || o->lsearch_type > 4)
+    return set_err(PHX_EINVAL, "options: lsearch_type must be 0 (None) .. 4 (WolfeStrong)");
+  if (!(o->lsearch_wolfe1 > 0 && o->lsearch_wolfe1 < 1) || !(o->lsearch_wolfe2 > o->lsearch_wolfe1 && o->lsearch_wolfe2 < 1))
+    return set_err(PHX_EINVAL, "options: Wolfe constants need 0 < wolfe1 < wolfe2 < 1");
   if (o->ls_num_reg_trials < 1 || o->ls_num_max_iters < 0 || o->num_max_iters < 1)
     return set_err(PHX_EINVAL, "options: non-positive iteration limit");
   if (!(o->lsearch_alpha > 0 && o->lsearch_alpha < 1)) return set_err(PHX_EINVAL, "options: lsearch_alpha out of (0,1)");
@@ -677,7 +683,7 @@ int finish_fp64(phx_context ctx, const std::vector<phx_instance>& list, const ph
 // ===========================================================================
 extern "C" {
 
-int phx_version(void) { return 10000; }
+int phx_version(void) { return 10100; }
 
 const char* phx_last_error(void) { return g_err.c_str(); }
 
@@ -700,6 +706,8 @@ void phx_default_options(phx_options* o) {
   o->lsearch_type = 1;
   o->lsearch_alpha = 0.5;
   o->lsearch_num_try = 32;
+  o->lsearch_wolfe1 = 1e-4;
+  o->lsearch_wolfe2 = 0.9;
   o->precision = PHX_PREC_FP64;
   o->precond = 1;
   o->inner_tol = 1e-4;

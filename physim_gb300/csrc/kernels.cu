@@ -626,7 +626,7 @@ __device__ __forceinline__ void st_gather(const BatchDev& B, const TileMap& M, i
     NState* st = I.st;
     if (st->phase != PH_EVAL) continue;
     const int v = lt * kTile + threadIdx.x;
-    double p[2] = {0.0, 0.0};
+    double p[3] = {0.0, 0.0, 0.0};
     if (v < I.n) {
       double g[3] = {0.0, 0.0, 0.0};
       const int c0 = I.nseg_ptr[v], c1 = I.nseg_ptr[v + 1];
@@ -674,12 +674,18 @@ __device__ __forceinline__ void st_gather(const BatchDev& B, const TileMap& M, i
       st4(I.gn, v, g);
       p[0] = elin;
       p[1] = g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
+      if (I.opts->lsearch_type >= 3) {  // dx . g of the trial, for the Wolfe line searches
+        double d[3];
+        ld4(I.dx, v, d);
+        p[2] = d[0] * g[0] + d[1] * g[1] + d[2] * g[2];
+      }
     }
-    double tot[2];
-    if (tile_done<2>(I, lt, tiles_of(I.n), ncta, p, tot, sm, &flag) && threadIdx.x == 0) {
+    double tot[3];
+    if (tile_done<3>(I, lt, tiles_of(I.n), ncta, p, tot, sm, &flag) && threadIdx.x == 0) {
       count_bytes(B, I, K_GATHER);
       st->E_eval = st->E_el + tot[0];
       st->gg_eval = tot[1];
+      st->dg_eval = tot[2];
       st->phase = PH_EVAL_DONE;
       advance(B, i);
     }

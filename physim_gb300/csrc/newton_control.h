@@ -112,8 +112,9 @@ PHX_HD inline void ctl_iter_begin(NState& s, const DevOpts& o) {
   }
   int qp = s.steepest ? 0 : o.qp_solver;
   if (qp == 0) {
-    // Steepest: dx = -g, so ||dx|| = ||g||
+    // Steepest: dx = -g, so ||dx|| = ||g|| and dx . g = -||g||^2
     s.dx_norm = s.opt;
+    s.dg = -s.opt * s.opt;
     s.scale = (s.dx_norm > o.max_step_size) ? o.max_step_size / s.dx_norm : 1.0;
     s.factor = 1.0;
     s.alpha_trial = s.scale * s.factor;
@@ -144,15 +145,48 @@ PHX_HD inline void ctl_lin_done(NState& s, const DevOpts& o) {
   s.factor = 1.0;
   s.num_bis = 0;
   s.alpha_trial = s.scale * s.factor;
+  s.dg = -s.b_dot_dx;  // b = -g
   s.purpose = 1;
   s.vecop = VO_TRIAL;
   ctl_goto(s, PH_EVAL);
 }
 
-// A rejected line-search trial (LineSearch_Simple, OptimSolver.cpp:688-736): sets up the
-// next, shorter trial and returns true, or applies the failure (state restored, step
-// rejected) and returns false.
-PHX_HD inline bool ctl_ls_reject(NState& s, const DevOpts& o) {
+// Acceptance test of a line-search trial with energy objNew at bisection factor f, the
+// `if` inside each LineSearch_* loop (OptimSolver.cpp:688-884).  With dxIn = scale * dx the
+// clamped step and g the gradient at the search's start:
+//   None (0): always; Simple (1): objNew < obj;
+//   Armijo (2): objNew <= obj + f * c1 * (dxIn / |dxIn|) . g;
+//   WolfeWeak (3): objNew <= obj + f * c1 * m and -dxIn . gNew <= -c2 * m, m = dxIn . g;
+//   WolfeStrong (4): both, and |dxIn . gNew| <= c2 * |m|.
+// The Wolfe tests read dx . gNew of the trial (dg_eval), so those searches evaluate their
+// trials one at a time, with gradients.
+PHX_HD inline bool ctl_ls_accepts(const NState& s, const DevOpts& o, double objNew, double f) {
+  switch (o.lsearch_type) {
+    case 0:
+      return true;
+    case 2: {
+      const double t = s.dx_norm > 0.0 ? o.lsearch_wolfe1 * (s.dg / s.dx_norm) : 0.0;
+      return objNew <= s.obj + f * t;
+    }
+    case 3:
+    case 4: {
+      const double m = s.scale * s.dg, dgn = s.scale * s.dg_eval;
+      bool ok = objNew <= s.obj + f * (o.lsearch_wolfe1 * m) && -dgn <= -o.lsearch_wolfe2 * m;
+      if (o.lsearch_type == 4) ok = ok && fabs(dgn) <= o.lsearch_wolfe2 * fabs(m);
+      return ok;
+    }
+    default:
+      return objNew < s.obj;
+  }
+}
+
+// A rejected line-search trial of energy objNew (the LineSearch_* loops, OptimSolver.cpp:
+// 688-884): sets up the next, shorter trial and returns true, or applies the failure and
+// returns false.  On failure the state is restored, and UpdateStepResult (OptimSolver.cpp:
+// 404-430) judges the last trial: no improvement is NONDESC; an improvement that the
+// Armijo / Wolfe tests still refused counts as a step of its size (MINIMPR, MINSTEP or
+// ONGOING) although the restored state stays, so that the next step starts from it again.
+PHX_HD inline bool ctl_ls_reject(NState& s, const DevOpts& o, double objNew) {
   const double stepCur = s.alpha_trial * s.dx_norm;
   s.factor *= o.lsearch_alpha;
   if (stepCur > o.tol_min_step && s.num_bis <= o.lsearch_num_try) {
@@ -160,8 +194,23 @@ PHX_HD inline bool ctl_ls_reject(NState& s, const DevOpts& o) {
     s.alpha_trial = s.scale * s.factor;
     return true;
   }
-  s.result = OS_NONDESC;
-  s.step_result = OS_NONDESC;
+  const double impr = s.obj - objNew;
+  if (impr > 0) {
+    if (impr < o.tol_min_impr) {
+      s.min_impr_count++;
+      s.result = OS_MINIMPR;
+    } else if (stepCur < o.tol_min_step) {
+      s.min_step_count++;
+      s.result = OS_MINSTEP;
+    } else {  // SUCCESS or ONGOING there; the restored gradient is above the tolerance, so ONGOING
+      s.result = OS_ONGOING;
+      s.min_impr_count = 0;
+      s.min_step_count = 0;
+    }
+  } else {
+    s.result = OS_NONDESC;
+  }
+  s.step_result = s.result;
   s.total_bis += s.num_bis;
   s.log_step = stepCur;
   s.log_pending = 1;
@@ -175,7 +224,8 @@ PHX_HD inline bool ctl_ls_reject(NState& s, const DevOpts& o) {
 // one-at-a-time search would try) are evaluated together, energies only.
 PHX_HD inline void ctl_ls_next(NState& s, const DevOpts& o) {
   const int K = o.ls_parallel > kLsK ? kLsK : o.ls_parallel;
-  if (K > 1 && s.num_bis >= 2) {
+  const bool energy_only = o.lsearch_type == 1 || o.lsearch_type == 2;  // tests that need no gradient
+  if (K > 1 && s.num_bis >= 2 && energy_only) {
     double f = s.factor;
     s.ls_a[0] = s.alpha_trial;
     for (int k = 1; k < K; ++k) {
@@ -196,55 +246,71 @@ PHX_HD inline void ctl_lsk_check(NState& s, const DevOpts& o);
 // Line-search trial evaluated: accept, bisect, or give up (LineSearch_Simple + UpdateStepResult).
 PHX_HD inline void ctl_ls_check(NState& s, const DevOpts& o) {
   double objNew = s.E_eval;
-  if (objNew < s.obj) {
-    double impr = s.obj - objNew;
-    double step = s.alpha_trial * s.dx_norm;
-    double optNew = sqrt(s.gg_eval);
-    if (impr < o.tol_min_impr) {
-      s.min_impr_count++;
-      s.result = OS_MINIMPR;
-    } else if (step < o.tol_min_step) {
-      s.min_step_count++;
-      s.result = OS_MINSTEP;
-    } else if (optNew <= s.tol_eff) {
-      s.result = OS_SUCCESS;
-      s.min_impr_count = 0;
-      s.min_step_count = 0;
-    } else {
-      s.result = OS_ONGOING;
-      s.min_impr_count = 0;
-      s.min_step_count = 0;
-    }
-    s.step_result = s.result;
-    // the iterate being left becomes the FP64 finish's restart point while its gradient is
-    // still well above the tolerance (an FP32 solve can stall inside the band where the
-    // energy comparison no longer resolves a step)
-    const int back = (s.opt > kBackFactor * s.tol_eff) ? VO_BACK : 0;
+  if (!ctl_ls_accepts(s, o, objNew, s.factor)) {
+    if (ctl_ls_reject(s, o, objNew)) ctl_ls_next(s, o);
+    return;
+  }
+  double impr = s.obj - objNew;
+  double step = s.alpha_trial * s.dx_norm;
+  double optNew = sqrt(s.gg_eval);
+  if (!(impr > 0)) {
+    // accepted without improvement (None, or Armijo / Wolfe along a non-descent direction):
+    // NONDESC, and the trial stays applied; the next step starts from it
+    s.result = OS_NONDESC;
+    s.step_result = OS_NONDESC;
     s.obj = objNew;
     s.opt = optNew;
     s.total_bis += s.num_bis;
     s.log_step = step;
     s.log_pending = 1;
-    s.vecop = VO_ACCEPT | VO_SAVE | back;
+    s.vecop = VO_GCOPY | VO_SAVE;
     ctl_goto(s, ctl_post_step(s, o));
     return;
   }
-  if (ctl_ls_reject(s, o)) ctl_ls_next(s, o);
+  if (impr < o.tol_min_impr) {
+    s.min_impr_count++;
+    s.result = OS_MINIMPR;
+  } else if (step < o.tol_min_step) {
+    s.min_step_count++;
+    s.result = OS_MINSTEP;
+  } else if (optNew <= s.tol_eff) {
+    s.result = OS_SUCCESS;
+    s.min_impr_count = 0;
+    s.min_step_count = 0;
+  } else {
+    s.result = OS_ONGOING;
+    s.min_impr_count = 0;
+    s.min_step_count = 0;
+  }
+  s.step_result = s.result;
+  // the iterate being left becomes the FP64 finish's restart point while its gradient is
+  // still well above the tolerance (an FP32 solve can stall inside the band where the
+  // energy comparison no longer resolves a step)
+  const int back = (s.opt > kBackFactor * s.tol_eff) ? VO_BACK : 0;
+  s.obj = objNew;
+  s.opt = optNew;
+  s.total_bis += s.num_bis;
+  s.log_step = step;
+  s.log_pending = 1;
+  s.vecop = VO_ACCEPT | VO_SAVE | back;
+  ctl_goto(s, ctl_post_step(s, o));
 }
 
-// Line-search trials evaluated together (PH_EVALK): scans them in order with the rules of
-// the one-at-a-time search, so it takes the same decisions: the first trial whose energy
-// is below the current one is evaluated again with its gradient (PH_EVAL) and checked as
-// usual; a rejected trial goes through ctl_ls_reject like a sequential one.
+// Line-search trials evaluated together (PH_EVALK, Simple and Armijo searches, whose tests
+// read energies only): scans them in order with the rules of the one-at-a-time search, so
+// it takes the same decisions: the first trial the test accepts is evaluated again with its
+// gradient (PH_EVAL) and checked as usual; a rejected trial goes through ctl_ls_reject like
+// a sequential one.
 PHX_HD inline void ctl_lsk_check(NState& s, const DevOpts& o) {
   for (int k = 0; k < s.lsk; ++k) {
-    if (s.ls_e[k] < s.obj) {  // s.alpha_trial is trial k's step here (same recurrence)
+    // s.alpha_trial and s.factor are trial k's here (the same recurrence)
+    if (ctl_ls_accepts(s, o, s.ls_e[k], s.factor)) {
       s.purpose = 1;
       s.vecop = VO_TRIAL;
       ctl_goto(s, PH_EVAL);
       return;
     }
-    if (!ctl_ls_reject(s, o)) return;  // the search failed at trial k
+    if (!ctl_ls_reject(s, o, s.ls_e[k])) return;  // the search failed at trial k
   }
   ctl_ls_next(s, o);
 }

@@ -80,8 +80,10 @@ struct DevOpts {
   int32_t qp_solver, min_step_max_count, min_impr_max_count, num_max_iters, try_steepest;
   int32_t ls_num_max_iters, ls_num_reg_trials, lsearch_num_try, precision, precond;
   int32_t max_refine_sweeps, warm_guess, dynamic, ls_parallel;  // ls_parallel: trials evaluated together
+  int32_t lsearch_type, pad_o;                                   // LSearchType: 0 None .. 4 WolfeStrong
   double tol_max_error, tol_min_step, tol_min_impr, max_step_size, ls_tol_max_error;
   double lsearch_alpha, inner_tol, dt, tol_rel;
+  double lsearch_wolfe1, lsearch_wolfe2;                         // Armijo / Wolfe constants c1, c2
 };
 
 // Scalar state of one instance's solve (one thread of the control kernel owns it).
@@ -103,6 +105,7 @@ struct NState {
   double lin_tol;                              // relative residual target of this step's linear solve
   double eta, opt_prev;                        // forcing term state (FP32 path)
   double log_step;                             // ||dx_final|| of the step being logged
+  double dg, dg_eval;                          // dx . g at the search's start; dx . g at the trial
   int32_t log_pending, log_count;              // per-iteration log bookkeeping
   int32_t lsk, pad_ls;                         // trials in the batch being evaluated (PH_EVALK)
   double ls_a[8], ls_e[8], ls_eel[8];          // their step lengths, energies, element energies

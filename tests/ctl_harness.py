@@ -24,7 +24,7 @@ class NState(C.Structure):
         [("pcg_total", C.c_int64)] + [(n, C.c_double) for n in (
             "obj", "opt", "opt0", "obj_new", "alpha_trial", "factor", "scale", "dx_norm", "b_dot_dx", "E_el",
             "E_eval", "gg_eval", "normA2", "shift", "regT", "bb", "rr64", "rz", "rr", "pq", "alpha", "beta",
-            "thr_inner", "thr_final", "tol_eff", "lin_tol", "eta", "opt_prev", "log_step")] + \
+            "thr_inner", "thr_final", "tol_eff", "lin_tol", "eta", "opt_prev", "log_step", "dg", "dg_eval")] + \
         [("log_pending", C.c_int32), ("log_count", C.c_int32), ("lsk", C.c_int32), ("pad_ls", C.c_int32),
          ("ls_a", C.c_double * 8), ("ls_e", C.c_double * 8), ("ls_eel", C.c_double * 8)]
 
@@ -33,9 +33,10 @@ class DevOpts(C.Structure):
     _fields_ = [(n, C.c_int32) for n in (
         "qp_solver", "min_step_max_count", "min_impr_max_count", "num_max_iters", "try_steepest",
         "ls_num_max_iters", "ls_num_reg_trials", "lsearch_num_try", "precision", "precond",
-        "max_refine_sweeps", "warm_guess", "dynamic", "ls_parallel")] + [(n, C.c_double) for n in (
+        "max_refine_sweeps", "warm_guess", "dynamic", "ls_parallel", "lsearch_type", "pad_o")] + \
+        [(n, C.c_double) for n in (
             "tol_max_error", "tol_min_step", "tol_min_impr", "max_step_size", "ls_tol_max_error",
-            "lsearch_alpha", "inner_tol", "dt", "tol_rel")]
+            "lsearch_alpha", "inner_tol", "dt", "tol_rel", "lsearch_wolfe1", "lsearch_wolfe2")]
 
 
 def make_opts(**kw):
@@ -43,7 +44,7 @@ def make_opts(**kw):
                 ls_num_max_iters=1000, ls_num_reg_trials=10, lsearch_num_try=32, precision=0, precond=1,
                 max_refine_sweeps=1, warm_guess=1, dynamic=0, tol_max_error=1e-6, tol_min_step=1e-5,
                 tol_min_impr=1e-9, max_step_size=1000.0, ls_tol_max_error=1e-9, lsearch_alpha=0.5,
-                inner_tol=1e-3, dt=0.0, tol_rel=0.0)
+                inner_tol=1e-3, dt=0.0, tol_rel=0.0, lsearch_type=1, lsearch_wolfe1=1e-4, lsearch_wolfe2=0.9)
     for k, v in kw.items():
         setattr(o, k, v)
     return o
@@ -168,6 +169,7 @@ def run(shim, orc, x0, opts, dynamic=False, v0=None, max_steps=200000):
             gn = gg
             s.E_eval = E
             s.gg_eval = gn @ gn
+            s.dg_eval = dx @ gn
             s.phase = PH_EVAL_DONE
         elif ph in (PH_HESS, PH_JACOBI):
             if ph == PH_HESS:

@@ -36,6 +36,7 @@ def test_version_and_defaults_without_gpu():
     assert (o.tol_min_impr, o.min_impr_max_count, o.num_max_iters, o.try_steepest) == (1e-9, 3, 100, 1)
     assert (o.max_step_size, o.ls_num_max_iters, o.ls_tol_max_error, o.ls_num_reg_trials) == (1000, 1000, 1e-9, 10)
     assert (o.lsearch_type, o.lsearch_alpha, o.lsearch_num_try) == (1, 0.5, 32)
+    assert (o.lsearch_wolfe1, o.lsearch_wolfe2) == (1e-4, 0.9)
 
 
 def test_no_device_is_an_error_not_a_fallback():

@@ -114,3 +114,55 @@ def test_parallel_line_search_takes_the_same_decisions(ctl_shim):
     assert ba > 100 and ka == 0 and kb > 0 and kb < ba / 4
     assert (ra, ia, ba) == (rb, ib, bb)
     assert np.array_equal(xa, xb)
+
+
+@pytest.mark.parametrize("lst", [0, 2, 3, 4])
+@pytest.mark.parametrize("model", [0, 1])
+def test_line_search_types_match_oracle(ctl_shim, model, lst):
+    """LineSearch_None / Armijo / WolfeWeak / WolfeStrong (OptimSolver.cpp:738-900): the
+    state machine takes the oracle's decisions (result, iterations, bisections, iterate).
+    The reference's Armijo test uses the normalised direction, c1 (d/|d|).g, so once the
+    Newton step is shorter than about c1 no trial passes: both stall to MAXITER, failing
+    searches whose last trial lowered the energy counting as steps; their bisection counts
+    there are decided in rounding noise and are not compared."""
+    m = _case(model, (2, 2, 4))
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    g0 = np.linalg.norm(orc.gradient(x0))
+    kw = dict(tol_max_error=1e-6 * g0, tol_min_impr=0.0, tol_min_step=0.0, num_max_iters=40)
+    xo, ro = orc.solve_static(x0, ls_solver=1, cg_block_jacobi=1, lsearch_type=lst, **kw)
+    x, _, s = H.run(ctl_shim, orc, x0, H.make_opts(lsearch_type=lst, **kw))
+    assert (s.result, s.it) == (ro["result"], ro["iterations"])
+    if lst == 2 and ro["result_name"] == "MAXITER":  # stalled short of the tolerance
+        assert rel(x - x0, xo - x0) < 1e-4
+    else:
+        assert s.total_bis == ro["bisections"]
+        assert rel(x - x0, xo - x0) < 1e-8
+
+
+def test_armijo_parallel_trials_take_the_same_decisions(ctl_shim):
+    """The Armijo test reads energies only, so its trials may be evaluated eight at a time:
+    the same iterates, bisections and result as one at a time."""
+    m = M.make_box(2, 2, 6, (0.04, 0.04, 0.12), 2e5, 0.35, 1000.0, 1, (0.0, -9.81, 0.0), clamp_face=4,
+                   load_face=5, traction=(20000.0, -30000.0, 10000.0))
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    g0 = np.linalg.norm(orc.gradient(x0))
+    runs = []
+    for k in (0, 8):
+        opts = H.make_opts(tol_max_error=1e-6 * g0, tol_min_impr=0.0, tol_min_step=0.0, ls_parallel=k,
+                           lsearch_type=2)
+        x, _, s = H.run(ctl_shim, orc, x0, opts)
+        runs.append((x, s.result, s.it, s.total_bis, H.stats["evalk"]))
+    (xa, ra, ia, ba, ka), (xb, rb, ib, bb, kb) = runs
+    assert ba > 20 and ka == 0 and kb > 0
+    assert (ra, ia, ba) == (rb, ib, bb)
+    assert np.array_equal(xa, xb)
+
+
+def test_wolfe_searches_evaluate_one_trial_at_a_time(ctl_shim):
+    m = _case(1, (2, 2, 4))
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    H.run(ctl_shim, orc, x0, H.make_opts(lsearch_type=3, ls_parallel=8, num_max_iters=10))
+    assert H.stats["evalk"] == 0

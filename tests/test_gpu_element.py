@@ -131,4 +131,6 @@ def test_bad_options_rejected(gpu_ctx):
     with pytest.raises(px.PhxError):
         inst.solve_static(px.options(precision=7))
     with pytest.raises(px.PhxError):
-        inst.solve_static(px.options(lsearch_type=2))
+        inst.solve_static(px.options(lsearch_type=5))
+    with pytest.raises(px.PhxError):
+        inst.solve_static(px.options(lsearch_type=3, lsearch_wolfe1=0.5, lsearch_wolfe2=0.4))

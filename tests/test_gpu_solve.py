@@ -292,3 +292,45 @@ def test_dynamic_step_at_rest_without_load(gpu_ctx):
     x, v, r = inst.dynamic_step(px.options(tol_max_error=1e-12, tol_min_impr=0.0, tol_min_step=0.0), 1e-3)
     assert r["result_name"] == "SUCCESS"
     assert np.array_equal(x, m.X0.ravel()) and not np.any(v)
+
+
+def _ls_case(model):
+    if model == 0:
+        return M.cantilever(2, 2, 4)
+    return M.make_box(2, 2, 4, (0.04, 0.04, 0.08), 2e5, 0.35, 1000.0, 1, (0.0, -9.81, 0.0), clamp_face=4,
+                      load_face=5, traction=(300.0, -500.0, 200.0))
+
+
+@pytest.mark.parametrize("lst", [0, 2, 3, 4])
+@pytest.mark.parametrize("model", [0, 1])
+def test_line_search_types_on_gpu(gpu_ctx, model, lst):
+    """LineSearch_None / Armijo / WolfeWeak / WolfeStrong on the device (plain FP64 path):
+    the oracle's result, iteration and bisection counts and iterate.  Armijo's stall
+    (its normalised-direction test refuses every trial once the step is shorter than about
+    c1) ends at MAXITER in both; there only the result, the count and the iterate to 1e-4."""
+    m = _ls_case(model)
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    g0 = np.linalg.norm(orc.gradient(x0))
+    kw = dict(tol_max_error=1e-6 * g0, tol_min_impr=0.0, tol_min_step=0.0, num_max_iters=40, lsearch_type=lst)
+    xo, ro = orc.solve_static(x0, ls_solver=1, cg_block_jacobi=1, **kw)
+    inst = px.Instance(gpu_ctx, m)
+    x, r = inst.solve_static(px.options(**kw), x0)
+    assert (r["result"], r["iterations"]) == (ro["result"], ro["iterations"])
+    if lst == 2 and ro["result_name"] == "MAXITER":
+        assert disp_err(x, xo, x0) < 1e-4
+    else:
+        assert r["bisections"] == ro["bisections"]
+        assert disp_err(x, xo, x0) < 1e-8
+
+
+def test_wolfe_line_search_served_path(gpu_ctx):
+    """The served FP32 path with a strong-Wolfe search reaches the oracle's equilibrium."""
+    m = M.batch_instance(3, 11)
+    orc, x0, g0, xr, _ = oracle_solution(m, 1e-10)
+    o = px.options(precision=px.PREC_FP32_REFINE, tol_rel=1e-6, tol_max_error=0.0, tol_min_impr=0.0,
+                   tol_min_step=0.0, lsearch_type=4)
+    inst = px.Instance(gpu_ctx, m)
+    x, r = inst.solve_static(o, x0)
+    assert r["result_name"] == "SUCCESS"
+    assert disp_err(x, xr, x0) < 1e-6
