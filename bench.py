@@ -209,17 +209,21 @@ def pinned_mesh(m):
     return pm, ok
 
 
+LSEARCH = {"none": 0, "simple": 1, "armijo": 2, "wolfe-weak": 3, "wolfe-strong": 4}  # LSearchType
+
+
 def served_options(px, args):
     """Served path: FP32 Hessian + PCG with FP64 refinement; the same PCG budget per Newton step
     as the plain path (served_sweeps x served_pcg_max = plain_pcg_max), fewer, longer sweeps."""
     return px.options(precision=px.PREC_FP32_REFINE, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0,
                       tol_min_step=0.0, pcg_chunk=args.pcg_chunk, inner_tol=args.inner_tol,
-                      ls_num_max_iters=args.served_pcg_max, max_refine_sweeps=args.served_sweeps)
+                      ls_num_max_iters=args.served_pcg_max, max_refine_sweeps=args.served_sweeps,
+                      lsearch_type=LSEARCH[args.lsearch])
 
 
 def batch_config(args, count, tets):
     return {"workload": f"batched uneven boxes: {count} instances, 6-tet hexes, {tets} tets", "instances": count,
-            "tets": tets, "tol_rel": args.tol_rel,
+            "tets": tets, "tol_rel": args.tol_rel, "line_search": args.lsearch,
             "l2": "inputs larger than L2 (per-step working set well above 129 MB)",
             "inner_tol": args.inner_tol, "pcg_chunk": args.pcg_chunk,
             "plain_pcg_max_per_newton_step": args.plain_pcg_max,
@@ -237,7 +241,8 @@ def run_batch(args, world, rank, dist):
     insts = [px.Instance(ctx, m) for m in meshes]
     served = served_options(px, args)
     plain = px.options(precision=px.PREC_FP64, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0,
-                       tol_min_step=0.0, pcg_chunk=args.pcg_chunk, ls_num_max_iters=args.plain_pcg_max)
+                       tol_min_step=0.0, pcg_chunk=args.pcg_chunk, ls_num_max_iters=args.plain_pcg_max,
+                       lsearch_type=LSEARCH[args.lsearch])
 
     def step():
         for it in insts:
@@ -450,7 +455,7 @@ def run_cantilever(args, world, rank, dist):
     inst = px.Instance(ctx, m)
     x0 = m.X0.ravel().copy()
     o = px.options(precision=px.PREC_FP64, tol_rel=1e-8, tol_max_error=0.0, tol_min_impr=0.0, tol_min_step=0.0,
-                   pcg_chunk=args.pcg_chunk)
+                   pcg_chunk=args.pcg_chunk, lsearch_type=LSEARCH[args.lsearch])
     for _ in range(args.warmup):
         inst.reset(); inst.solve_static(o)
     ctx.profile(True); ctx.profile_reset()
@@ -466,7 +471,8 @@ def run_cantilever(args, world, rank, dist):
            "value": round(args.steps / (ms / 1e3), 3), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
-           "config": {"workload": "cantilever 8x8x32 hexes x 6 tets, 12288 tets"}, "report": r, "clocks": clk}
+           "config": {"workload": "cantilever 8x8x32 hexes x 6 tets, 12288 tets", "line_search": args.lsearch},
+           "report": r, "clocks": clk}
     if rank == 0 and not args.no_cpu:
         orc = oracle.Oracle(m)
         g0 = float(np.linalg.norm(orc.gradient(x0)))
@@ -751,6 +757,8 @@ def main():
     ap.add_argument("--arena-gb", type=float, default=48.0)
     ap.add_argument("--e2e-full", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--lsearch", default="simple", choices=sorted(LSEARCH),
+                    help="line search of the GPU solves (LSearchType; the CPU baseline keeps Simple)")
     args = ap.parse_args()
     world, rank, local, dist = dist_setup()
     args.device = local  # one replica per GPU: this rank's library context lives on its own device

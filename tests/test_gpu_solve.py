@@ -224,15 +224,17 @@ def test_fp32_stall_finishes_in_fp64(gpu_ctx, c1_oracle):
     assert disp_err(x, xr, x0) < 1e-5
 
 
-def test_parallel_line_search_same_result_on_gpu(gpu_ctx):
+@pytest.mark.parametrize("lst", [1, 2])
+def test_parallel_line_search_same_result_on_gpu(gpu_ctx, lst):
     """A StVK batch instance whose solve takes hundreds of line-search bisections: trials
-    evaluated together give the same iterations, bisections, result and positions."""
+    evaluated together (Simple and Armijo searches) give the same iterations, bisections,
+    result and positions."""
     m = M.batch_instance(3, 0)
     inst = px.Instance(gpu_ctx, m)
     out = []
     for k in (0, 8):
         o = px.options(precision=px.PREC_FP32_REFINE, tol_rel=1e-6, tol_max_error=0.0, tol_min_impr=0.0,
-                       tol_min_step=0.0, lsearch_parallel=k, fp64_finish=0)
+                       tol_min_step=0.0, lsearch_parallel=k, fp64_finish=0, lsearch_type=lst)
         inst.reset()
         x, r = inst.solve_static(o)
         out.append((x, r))
