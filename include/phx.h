@@ -71,6 +71,9 @@ typedef struct phx_mesh {
   const uint8_t* fixed;   /* [3*num_nodes] hard-fixed DoFs (BC_FixDoF hard mode); NULL = none */
   const double* force;    /* [3*num_nodes] EnergyElement_Force f (energy x.f); NULL = none */
   double gravity[3];      /* BC_Gravity value */
+  const double* soft_k;   /* [num_nodes] BC_FixDoF soft mode: stiffness k of each node's
+                             EnergyElement_SoftConstraint, E = k/2 |x - t|^2 (0 = none); NULL = none */
+  const double* soft_target; /* [3*num_nodes] their targets t; NULL = X0 */
 } phx_mesh;
 
 /* Mirrors OptimSolverOptions (include/PhySim/Solvers/OptimSolver.h:47-70)

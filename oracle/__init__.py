@@ -23,7 +23,8 @@ OS_NAMES = {0: "ONGOING", 1: "SUCCESS", 2: "MINSTEP", 3: "MINIMPR", 4: "FAILURE"
 class OrcMesh(C.Structure):
     _fields_ = [("n", C.c_int32), ("m", C.c_int32), ("X0", C.c_void_p), ("T", C.c_void_p),
                 ("lame", C.c_void_p), ("rho", C.c_void_p), ("model", C.c_void_p),
-                ("fixed", C.c_void_p), ("force", C.c_void_p), ("gravity", C.c_double * 3)]
+                ("fixed", C.c_void_p), ("force", C.c_void_p), ("gravity", C.c_double * 3),
+                ("soft_k", C.c_void_p), ("soft_target", C.c_void_p)]
 
 
 class OrcOptions(C.Structure):
@@ -131,6 +132,12 @@ class Oracle:
         d.X0, d.T, d.lame, d.rho, d.model, d.fixed, d.force = [a.ctypes.data for a in self._keep]
         for c in range(3):
             d.gravity[c] = float(mesh.gravity[c])
+        if getattr(mesh, "soft_k", None) is not None:
+            self._keep.append(np.ascontiguousarray(mesh.soft_k, dtype=np.float64).ravel())
+            d.soft_k = self._keep[-1].ctypes.data
+            if getattr(mesh, "soft_target", None) is not None:
+                self._keep.append(np.ascontiguousarray(mesh.soft_target, dtype=np.float64).ravel())
+                d.soft_target = self._keep[-1].ctypes.data
         self._desc = d
         h = C.c_void_p()
         if lib().orc_create(C.byref(d), C.byref(h)) != 0:

@@ -260,6 +260,7 @@ struct orc_handle_s {
   std::vector<int> T;
   std::vector<double> lame, rho;
   std::vector<uint8_t> model, fixed;
+  std::vector<double> soft_k, soft_t;  // BC_FixDoF soft mode: [n] stiffness, [3n] targets
   std::vector<double> force;
   double grav[3] = {0, 0, 0};
   std::vector<ElemRest> rest;
@@ -464,6 +465,19 @@ double model_energy(orc_handle_s* h, const double* x, Timers* tm) {
       for (int c = 0; c < 3; ++c) v += x[3 * i + c] * h->force[3 * i + c];
       E += v;
     }
+  // BC_FixDoF soft mode: EnergyElement_SoftConstraint::ComputeAndStore_Energy_Internal
+  // (EnergyElement_SoftConstraint.cpp:45-53), 0.5 k c.c with c = x - t
+  // (ConstraintSet_FixedPosition.cpp:44-46)
+  if (!h->soft_k.empty())
+    for (int i = 0; i < h->n; ++i) {
+      if (h->soft_k[i] == 0.0) continue;
+      double cc = 0;
+      for (int c = 0; c < 3; ++c) {
+        double d = x[3 * i + c] - h->soft_t[3 * i + c];
+        cc += d * d;
+      }
+      E += 0.5 * h->soft_k[i] * cc;
+    }
   if (tm) tm->cal_ene += secs(t0, t1);
   return E;
 }
@@ -488,6 +502,9 @@ void model_gradient(orc_handle_s* h, const double* x, double* g, bool fix, Timer
     }
   if (!h->force.empty())
     for (int i = 0; i < h->N; ++i) g[i] += h->force[i];
+  if (!h->soft_k.empty())  // k J^T c with J = I (EnergyElement_SoftConstraint.cpp:55-66)
+    for (int i = 0; i < h->n; ++i)
+      for (int c = 0; c < 3; ++c) g[3 * i + c] += h->soft_k[i] * (x[3 * i + c] - h->soft_t[3 * i + c]);
   if (fix && !h->fixed.empty())
     for (int i = 0; i < h->N; ++i)
       if (h->fixed[i]) g[i] = 0.0;
@@ -513,6 +530,13 @@ void model_hessian(orc_handle_s* h, const double* x, double* vals, bool fix, Tim
         for (int b = 0; b < 3; ++b) vals[mp[p * 9 + a * 3 + b]] += He[(3 * li + a) * 12 + 3 * lj + b];
     }
   }
+  if (!h->soft_k.empty())  // k J^T J = k I on the node's diagonal (EnergyElement_SoftConstraint.cpp:68-86)
+    for (int c = 0; c < h->N; ++c) {
+      const double k = h->soft_k[c / 3];
+      if (k == 0.0) continue;
+      for (int q = h->colptr[c]; q < h->colptr[c + 1]; ++q)
+        if (h->rowidx[q] == c) vals[q] += k;
+    }
   if (fix && !h->fixed.empty())
     for (int c = 0; c < h->N; ++c)
       for (int q = h->colptr[c]; q < h->colptr[c + 1]; ++q) {
@@ -1133,6 +1157,11 @@ int orc_create(const orc_mesh* mesh, orc_handle* out) {
   if (mesh->fixed) h->fixed.assign(mesh->fixed, mesh->fixed + h->N);
   if (mesh->force) h->force.assign(mesh->force, mesh->force + h->N);
   for (int c = 0; c < 3; ++c) h->grav[c] = mesh->gravity[c];
+  if (mesh->soft_k) {
+    h->soft_k.assign(mesh->soft_k, mesh->soft_k + h->n);
+    const double* t = mesh->soft_target ? mesh->soft_target : mesh->X0;
+    h->soft_t.assign(t, t + h->N);
+  }
   element_rest(h);
   build_pattern(h);
   *out = h;

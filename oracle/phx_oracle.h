@@ -31,6 +31,8 @@ typedef struct orc_mesh {
   const uint8_t* fixed;      /* [3n] hard-fixed DoFs, may be NULL */
   const double* force;       /* [3n] EnergyElement_Force f, may be NULL */
   double gravity[3];
+  const double* soft_k;      /* [n] BC_FixDoF soft mode stiffness per node (0: none), may be NULL */
+  const double* soft_target; /* [3n] its targets, NULL: X0 */
 } orc_mesh;
 
 /* Mirrors OptimSolverOptions (inc/Solvers/OptimSolver.h:47-70). */

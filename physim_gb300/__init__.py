@@ -47,7 +47,8 @@ class PhxError(RuntimeError):
 class Mesh_(C.Structure):
     _fields_ = [("num_nodes", C.c_int32), ("num_tets", C.c_int32), ("X0", C.c_void_p), ("tets", C.c_void_p),
                 ("lame", C.c_void_p), ("rho", C.c_void_p), ("model", C.c_void_p), ("fixed", C.c_void_p),
-                ("force", C.c_void_p), ("gravity", C.c_double * 3)]
+                ("force", C.c_void_p), ("gravity", C.c_double * 3), ("soft_k", C.c_void_p),
+                ("soft_target", C.c_void_p)]
 
 
 class Options(C.Structure):
@@ -257,6 +258,12 @@ class Instance:
         d.X0, d.tets, d.lame, d.rho, d.model, d.fixed, d.force = [a.ctypes.data for a in keep]
         for c in range(3):
             d.gravity[c] = float(m.gravity[c])
+        if getattr(m, "soft_k", None) is not None:
+            keep.append(np.ascontiguousarray(m.soft_k, dtype=np.float64).ravel())
+            d.soft_k = keep[-1].ctypes.data
+            if getattr(m, "soft_target", None) is not None:
+                keep.append(np.ascontiguousarray(m.soft_target, dtype=np.float64).ravel())
+                d.soft_target = keep[-1].ctypes.data
         h = C.c_void_p()
         _check(lib().phx_instance_create(ctx.h, C.byref(d), C.byref(h)))
         self.h = h

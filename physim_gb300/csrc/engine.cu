@@ -802,6 +802,8 @@ int phx_instance_create(phx_context ctx, const phx_mesh* mesh, phx_instance* out
   in.fixed = mesh->fixed;
   in.force = mesh->force;
   for (int c = 0; c < 3; ++c) in.gravity[c] = mesh->gravity[c];
+  in.soft_k = mesh->soft_k;
+  in.soft_target = mesh->soft_target;
   auto* inst = new phx_instance_s();
   inst->ctx = ctx;
   std::string err;
@@ -843,6 +845,7 @@ int phx_instance_create(phx_context ctx, const phx_mesh* mesh, phx_instance* out
   UP(fixmask, hp.fixmask);
   UP(mass, hp.mass);
   UP(hlin, hp.hlin);
+  if (!hp.soft.empty()) UP(soft, hp.soft);
 #undef UP
   {
     double* xr = nullptr;

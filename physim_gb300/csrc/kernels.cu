@@ -432,6 +432,29 @@ __device__ __forceinline__ void material_eg(int model, double lam, double mu, co
   }
 }
 
+// EnergyElement_SoftConstraint on one node's ConstraintSet_FixedPosition (BC_FixDoF soft
+// mode, EnergyElement_SoftConstraint.cpp:45-86): E = k/2 |x - t|^2, added gradient k (x - t)
+// (the Hessian's k I goes to the diagonal block in assembly).
+struct SoftNode {
+  double t[3], k;
+};
+__device__ __forceinline__ SoftNode ld_soft(const InstDev& I, int v) {
+  SoftNode s{{0.0, 0.0, 0.0}, 0.0};
+  if (I.soft) {
+    const double2* p = reinterpret_cast<const double2*>(I.soft + 4 * (size_t)v);
+    const double2 a = p[0], b = p[1];
+    s.t[0] = a.x; s.t[1] = a.y; s.t[2] = b.x; s.k = b.y;
+  }
+  return s;
+}
+__device__ __forceinline__ double soft_energy(const SoftNode& s, const double x[3], double* g) {
+  const double d[3] = {x[0] - s.t[0], x[1] - s.t[1], x[2] - s.t[2]};
+  if (g)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) g[c] += s.k * d[c];
+  return 0.5 * s.k * (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+}
+
 __device__ __forceinline__ void st_elem_eg(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag) {
   const int total = map_total(M);
   for (int t = cta; t < total; t += ncta) {
@@ -583,6 +606,7 @@ __device__ __forceinline__ void st_lin_ek(const BatchDev& B, const TileMap& M, i
         ld4(I.x0, v, x0);
         ld4(I.v0, v, v0);
       }
+      const SoftNode sk = ld_soft(I, v);
       for (int k = 0; k < K; ++k) {
         const double ak = st->ls_a[k];
         double x[3];
@@ -597,6 +621,7 @@ __device__ __forceinline__ void st_lin_ek(const BatchDev& B, const TileMap& M, i
           }
           elin += (dt * dt / 2.0) * acc;
         }
+        if (sk.k != 0.0) elin += soft_energy(sk, x, nullptr);
         Lk[k] = elin;
       }
     }
@@ -666,6 +691,8 @@ __device__ __forceinline__ void st_gather(const BatchDev& B, const TileMap& M, i
         }
         elin += (dt * dt / 2.0) * acc;
       }
+      const SoftNode sk = ld_soft(I, v);
+      if (sk.k != 0.0) elin += soft_energy(sk, x, g);
       if (!st->nofix) {
         const int fm = I.fixmask[v];
         for (int c = 0; c < 3; ++c)
@@ -795,8 +822,10 @@ __device__ __forceinline__ void st_assemble(const BatchDev& B, const TileMap& M,
       Real* const Hlo = H + sell_addr(lo, 0);  // entry e of a slot at +32 e
       Real* const Hup = up >= 0 ? H + sell_addr(up, 0) : nullptr;
       const int fr = nofix ? 0 : I.fixmask[R], fc = nofix ? 0 : I.fixmask[C];
-      const bool diag = dyn && R == C;
-      const Real md = diag ? (Real)(I.mass[R] / (dt * dt)) : (Real)0;
+      // diagonal blocks: + M/dt^2 of the dynamic problem, + k I of a soft fixed position
+      const double ks = (I.soft && R == C) ? I.soft[4 * (size_t)R + 3] : 0.0;
+      const bool diag = (dyn && R == C) || ks != 0.0;
+      const Real md = diag ? (Real)((dyn ? I.mass[R] / (dt * dt) : 0.0) + ks) : (Real)0;
 #pragma unroll
       for (int e = 0; e < 9; ++e) {
         const int a = e / 3, b = e % 3;

@@ -62,12 +62,38 @@ void rebuild_load(const MeshIn& in, HostPattern& hp) {
     }
 }
 
+// BC_FixDoF in soft mode (BC_FixDoF.cpp:51-66): one EnergyElement_SoftConstraint per node
+// with a nonzero stiffness, its target the given position or the node's rest position (the
+// value the condition reads when it is built).
+bool build_soft(const MeshIn& in, HostPattern& hp, std::string& err) {
+  hp.soft.clear();
+  if (!in.soft_k) return true;
+  bool any = false;
+  for (int v = 0; v < in.n; ++v) {
+    const double k = in.soft_k[v];
+    if (!(k >= 0.0) || !std::isfinite(k)) {
+      err = "mesh: soft_k must be finite and >= 0";
+      return false;
+    }
+    any = any || k > 0.0;
+  }
+  if (!any) return true;
+  hp.soft.assign(4 * (size_t)in.n, 0.0);
+  for (int v = 0; v < in.n; ++v) {
+    const double* t = in.soft_target ? in.soft_target + 3 * (size_t)v : in.X0 + 3 * (size_t)v;
+    for (int c = 0; c < 3; ++c) hp.soft[4 * (size_t)v + c] = t[c];
+    hp.soft[4 * (size_t)v + 3] = in.soft_k[v];
+  }
+  return true;
+}
+
 bool build_pattern(const MeshIn& in, HostPattern& hp, std::string& err) {
   const int n = in.n, m = in.m;
   if (n <= 0 || m <= 0 || !in.X0 || !in.T || !in.lame || !in.rho) {
     err = "mesh: empty or missing arrays";
     return false;
   }
+  if (!build_soft(in, hp, err)) return false;
   if ((int64_t)m * 10 > 2000000000LL) {
     err = "mesh: too many tets for 32-bit scatter indices";
     return false;

@@ -20,6 +20,8 @@ struct MeshIn {
   const uint8_t* fixed = nullptr;
   const double* force = nullptr;
   double gravity[3] = {0, 0, 0};
+  const double* soft_k = nullptr;       // [n] soft fixed-position stiffness per node (0: none), or null
+  const double* soft_target = nullptr;  // [3n] its targets; null: X0
 };
 
 // Everything the device needs, built once per mesh on the host.
@@ -45,6 +47,7 @@ struct HostPattern {
   std::vector<uint8_t> fixmask;       // [n]
   std::vector<double> mass;           // [n]
   std::vector<double> hlin;           // [4n]  f - m g
+  std::vector<double> soft;           // [4n]  soft fixed position (target, k) per node; empty: none
 };
 
 // Validates the mesh and builds the pattern; returns false with a message on bad input.

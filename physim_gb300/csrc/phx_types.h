@@ -138,6 +138,7 @@ struct InstDev {
   const uint8_t* fixmask;     // [n] bit d = DoF d fixed
   const double* mass;         // [n] lumped mass per node
   double* hlin;               // [n][4] f - m g : linear-load term of energy and gradient
+  const double* soft;         // [n][4] soft fixed position (target x, y, z, stiffness k) per node, or null
   // FP64 node vectors [n][4]
   const double* xrest;
   double* x; double* xs; double* dx; double* g; double* gn; double* dxprev;

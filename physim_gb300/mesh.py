@@ -77,6 +77,8 @@ class Mesh:
     gravity: np.ndarray       # float64 [3]
     dims: tuple = (0, 0, 0)   # hex grid dims when structured
     name: str = ""
+    soft_k: np.ndarray = None        # float64 [n] BC_FixDoF soft mode stiffness per node (0: none), or None
+    soft_target: np.ndarray = None   # float64 [n, 3] its targets, or None (rest positions)
 
     @property
     def n(self) -> int:
@@ -94,7 +96,9 @@ class Mesh:
         return dataclasses.replace(
             self, X0=self.X0.copy(), T=self.T.copy(), lame=self.lame.copy(), rho=self.rho.copy(),
             model=self.model.copy(), fixed=self.fixed.copy(), force=self.force.copy(),
-            gravity=self.gravity.copy())
+            gravity=self.gravity.copy(),
+            soft_k=None if self.soft_k is None else self.soft_k.copy(),
+            soft_target=None if self.soft_target is None else self.soft_target.copy())
 
 
 def lame_from_young_poisson(E, nu):
@@ -319,3 +323,15 @@ def signed_volumes(X, T) -> np.ndarray:
     p0 = X[T[:, 0]]
     d = np.stack([X[T[:, 1]] - p0, X[T[:, 2]] - p0, X[T[:, 3]] - p0], axis=2)
     return np.linalg.det(d) / 6.0
+
+
+def soft_clamped(m: Mesh, k: float, target_shift=(0.0, 0.0, 0.0)) -> Mesh:
+    """The mesh with its hard-fixed nodes held instead by soft fixed-position conditions of
+    stiffness k (BC_FixDoF soft mode), targets at their rest positions plus target_shift."""
+    out = m.copy()
+    fixed_nodes = m.fixed.reshape(-1, 3).any(axis=1)
+    out.fixed = np.zeros_like(m.fixed)
+    out.soft_k = np.where(fixed_nodes, float(k), 0.0)
+    out.soft_target = m.X0 + np.where(fixed_nodes[:, None], np.asarray(target_shift, dtype=np.float64), 0.0)
+    return out
+

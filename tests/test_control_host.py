@@ -166,3 +166,18 @@ def test_wolfe_searches_evaluate_one_trial_at_a_time(ctl_shim):
     x0 = orc.rest()
     H.run(ctl_shim, orc, x0, H.make_opts(lsearch_type=3, ls_parallel=8, num_max_iters=10))
     assert H.stats["evalk"] == 0
+
+
+def test_soft_fixed_position_matches_oracle(ctl_shim):
+    """A cantilever held by soft fixed-position conditions (BC_FixDoF soft mode) instead of
+    hard-fixed DoFs, with shifted targets: the oracle's decisions and iterate."""
+    m = M.soft_clamped(M.cantilever(2, 2, 4), 1e5, target_shift=(0.0, 2e-3, 0.0))
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    g0 = np.linalg.norm(orc.gradient(x0))
+    kw = dict(tol_max_error=1e-8 * g0, tol_min_impr=0.0, tol_min_step=0.0)
+    xo, ro = orc.solve_static(x0, ls_solver=1, cg_block_jacobi=1, **kw)
+    x, _, s = H.run(ctl_shim, orc, x0, H.make_opts(**kw))
+    assert ro["result_name"] == "SUCCESS"
+    assert (s.result, s.it, s.total_bis) == (ro["result"], ro["iterations"], ro["bisections"])
+    assert rel(x - x0, xo - x0) < 1e-9

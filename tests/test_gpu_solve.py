@@ -336,3 +336,32 @@ def test_wolfe_line_search_served_path(gpu_ctx):
     x, r = inst.solve_static(o, x0)
     assert r["result_name"] == "SUCCESS"
     assert disp_err(x, xr, x0) < 1e-6
+
+
+def test_soft_fixed_position_on_gpu(gpu_ctx):
+    """Soft fixed-position conditions (EnergyElement_SoftConstraint, k/2 |x - t|^2 per
+    node) on the device: energy, gradient and the assembled Hessian through the C ABI, the
+    FP64 solve at the oracle's iterates, and the served FP32 solve at its equilibrium."""
+    m = M.soft_clamped(M.cantilever(2, 2, 6), 1e5, target_shift=(1e-3, 2e-3, 0.0))
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    rng = np.random.default_rng(4)
+    x = x0 + 1e-3 * rng.standard_normal(orc.N)
+    inst = px.Instance(gpu_ctx, m)
+    E, g = inst.energy_gradient(x)
+    assert abs(E - orc.energy(x)) <= 1e-10 * max(1.0, abs(orc.energy(x)))
+    assert rel(g, orc.gradient(x)) < 1e-10
+    vals = inst.hessian(x)
+    assert rel(vals, orc.hessian(x)) < 1e-10
+    g0 = np.linalg.norm(orc.gradient(x0))
+    kw = dict(tol_max_error=1e-9 * g0, tol_min_impr=0.0, tol_min_step=0.0)
+    xo, ro = orc.solve_static(x0, ls_solver=1, cg_block_jacobi=1, **kw)
+    xg, r = px.Instance(gpu_ctx, m).solve_static(px.options(**kw), x0)
+    assert r["result_name"] == "SUCCESS" and ro["result_name"] == "SUCCESS"
+    assert (r["iterations"], r["bisections"]) == (ro["iterations"], ro["bisections"])
+    assert disp_err(xg, xo, x0) < 1e-9
+    o = px.options(precision=px.PREC_FP32_REFINE, tol_rel=1e-6, tol_max_error=0.0, tol_min_impr=0.0,
+                   tol_min_step=0.0)
+    xs, rs = px.Instance(gpu_ctx, m).solve_static(o, x0)
+    assert rs["result_name"] == "SUCCESS"
+    assert disp_err(xs, xo, x0) < 1e-5

@@ -227,3 +227,40 @@ def test_dynamic_step_against_explicit_energy():
     r[m.fixed.astype(bool)] = 0
     assert np.linalg.norm(r) < 1e-9
     assert np.allclose(v, (x - x0) / dt)
+
+
+def test_soft_fixed_position_fd_and_stiff_limit():
+    """BC_FixDoF soft mode (EnergyElement_SoftConstraint): the gradient and the Hessian's
+    diagonal term match finite differences of the energy with the reference's eps, and a
+    stiff soft clamp approaches the hard clamp's equilibrium."""
+    base = M.cantilever(2, 2, 4)
+    m = M.soft_clamped(base, 1e6, target_shift=(1e-3, 0.0, -2e-3))
+    o = oracle.Oracle(m)
+    rng = np.random.default_rng(5)
+    x = o.rest() + 1e-3 * rng.standard_normal(o.N)
+    g = o.gradient(x, fix=False)
+    eps = 1e-6
+    soft_dofs = np.flatnonzero(np.repeat(m.soft_k > 0, 3))
+    for d in list(soft_dofs[:9]) + [soft_dofs[-1] + 3]:
+        xp = x.copy(); xm = x.copy()
+        xp[d] += eps; xm[d] -= eps
+        fd = (o.energy(xp) - o.energy(xm)) / (2 * eps)
+        assert abs(fd - g[d]) <= 1e-6 * max(1.0, np.abs(g).max())
+        # the diagonal Hessian entry against the gradient's difference
+        cp, ri = o.pattern()
+        vals = o.hessian(x, fix=False)
+        q = [i for i in range(cp[d], cp[d + 1]) if ri[i] == d][0]
+        hfd = (o.gradient(xp, fix=False)[d] - o.gradient(xm, fix=False)[d]) / (2 * eps)
+        assert abs(hfd - vals[q]) <= 1e-5 * abs(vals[q])
+    # stiff limit: soft clamp with k -> large approaches the hard clamp
+    hard = oracle.Oracle(base)
+    x0 = hard.rest()
+    g0 = np.linalg.norm(hard.gradient(x0))
+    xh, rh = hard.solve_static(x0, tol_max_error=1e-8 * g0, tol_min_impr=0.0, tol_min_step=0.0)
+    errs = []
+    for k in (1e5, 1e7):
+        stiff = oracle.Oracle(M.soft_clamped(base, k))
+        xs, rs = stiff.solve_static(x0, tol_max_error=1e-8 * g0, tol_min_impr=0.0, tol_min_step=0.0)
+        assert rh["result_name"] == "SUCCESS" and rs["result_name"] == "SUCCESS"
+        errs.append(np.linalg.norm(xs - xh) / np.linalg.norm(xh - x0))
+    assert errs[1] < 1e-3 and errs[1] < errs[0] / 50  # the gap closes like 1/k
