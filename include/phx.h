@@ -152,6 +152,10 @@ int phx_context_memory(phx_context ctx, int64_t* used_bytes, int64_t* capacity_b
  * Validates the mesh (PHX_EINVAL on bad ids or non-positive rest volume),
  * builds the 3x3 block pattern and the scatter map, uploads everything. */
 int phx_instance_create(phx_context ctx, const phx_mesh* mesh, phx_instance* out);
+/* count instances at once (serving admission, batch set-up): the host parts (validation,
+ * pattern, scatter map) are built on several host threads, then each is set up on the
+ * device; out[i] for meshes[i].  On an error none is created. */
+int phx_instances_create(phx_context ctx, int32_t count, const phx_mesh* meshes, phx_instance* out);
 int phx_instance_destroy(phx_instance inst);
 int phx_instance_sizes(phx_instance inst, int64_t* num_dofs, int64_t* hessian_nnz,
                        int64_t* lower_blocks, int64_t* full_blocks);

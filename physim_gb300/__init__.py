@@ -27,7 +27,7 @@ PHX_OK, PHX_EINVAL, PHX_ENOMEM, PHX_ETIMEOUT, PHX_ECUDA, PHX_EBUSY, PHX_ENOTFOUN
 # every entry point include/phx.h declares
 EXPORTS = [
     "phx_version", "phx_last_error", "phx_default_options", "phx_context_create", "phx_context_destroy",
-    "phx_context_memory", "phx_instance_create", "phx_instance_destroy", "phx_instance_sizes",
+    "phx_context_memory", "phx_instance_create", "phx_instances_create", "phx_instance_destroy", "phx_instance_sizes",
     "phx_instance_reset", "phx_instance_set_positions", "phx_instance_get_positions", "phx_instance_set_velocities",
     "phx_instance_get_velocities", "phx_instance_update_load", "phx_energy_gradient", "phx_hessian",
     "phx_hessian_pattern", "phx_scatter_map", "phx_element_local", "phx_solve_static", "phx_solve_step", "phx_solve_log",
@@ -98,6 +98,7 @@ def lib():
         "phx_context_destroy": ([vp], C.c_int),
         "phx_context_memory": ([vp, C.POINTER(i64), C.POINTER(i64)], C.c_int),
         "phx_instance_create": ([vp, C.POINTER(Mesh_), C.POINTER(vp)], C.c_int),
+        "phx_instances_create": ([vp, C.c_int32, C.POINTER(Mesh_), C.POINTER(vp)], C.c_int),
         "phx_instance_destroy": ([vp], C.c_int),
         "phx_instance_sizes": ([vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)], C.c_int),
         "phx_instance_reset": ([vp], C.c_int),
@@ -182,6 +183,18 @@ class Context:
         _check(lib().phx_context_memory(self.h, C.byref(u), C.byref(c)))
         return u.value, c.value
 
+    def create_instances(self, meshes):
+        """Instances of many meshes at once (phx_instances_create: host parts in parallel)."""
+        meshes = list(meshes)
+        if not meshes:
+            return []
+        descs, keeps = zip(*(_mesh_desc(m) for m in meshes))
+        arr = (Mesh_ * len(meshes))(*descs)
+        hs = (C.c_void_p * len(meshes))()
+        _check(lib().phx_instances_create(self.h, len(meshes), arr, hs))
+        del keeps
+        return [Instance(self, m, _handle=C.c_void_p(h)) for m, h in zip(meshes, hs)]
+
     def mark(self, slot: int):
         """Records CUDA event `slot` on the library's stream."""
         _check(lib().phx_timer_mark(self.h, int(slot)))
@@ -239,34 +252,42 @@ class Context:
         return [r.as_dict() for r in reps]
 
 
+def _mesh_desc(m):
+    """phx_mesh of a mesh, and the arrays it points into (keep them alive for the call)."""
+    keep = [np.ascontiguousarray(m.X0, dtype=np.float64).ravel(),
+            np.ascontiguousarray(m.T, dtype=np.int32).ravel(),
+            np.ascontiguousarray(m.lame, dtype=np.float64).ravel(),
+            np.ascontiguousarray(m.rho, dtype=np.float64).ravel(),
+            np.ascontiguousarray(m.model, dtype=np.uint8).ravel(),
+            np.ascontiguousarray(m.fixed, dtype=np.uint8).ravel(),
+            np.ascontiguousarray(m.force, dtype=np.float64).ravel()]
+    d = Mesh_()
+    d.num_nodes = m.n
+    d.num_tets = m.m
+    d.X0, d.tets, d.lame, d.rho, d.model, d.fixed, d.force = [a.ctypes.data for a in keep]
+    for c in range(3):
+        d.gravity[c] = float(m.gravity[c])
+    if getattr(m, "soft_k", None) is not None:
+        keep.append(np.ascontiguousarray(m.soft_k, dtype=np.float64).ravel())
+        d.soft_k = keep[-1].ctypes.data
+        if getattr(m, "soft_target", None) is not None:
+            keep.append(np.ascontiguousarray(m.soft_target, dtype=np.float64).ravel())
+            d.soft_target = keep[-1].ctypes.data
+    return d, keep
+
+
 class Instance:
     """One FEM volume on the device (Simulable_FEM + boundary conditions)."""
 
-    def __init__(self, ctx: Context, m):
+    def __init__(self, ctx: Context, m, _handle=None):
         self.ctx = ctx
         self.mesh = m
-        keep = [np.ascontiguousarray(m.X0, dtype=np.float64).ravel(),
-                np.ascontiguousarray(m.T, dtype=np.int32).ravel(),
-                np.ascontiguousarray(m.lame, dtype=np.float64).ravel(),
-                np.ascontiguousarray(m.rho, dtype=np.float64).ravel(),
-                np.ascontiguousarray(m.model, dtype=np.uint8).ravel(),
-                np.ascontiguousarray(m.fixed, dtype=np.uint8).ravel(),
-                np.ascontiguousarray(m.force, dtype=np.float64).ravel()]
-        d = Mesh_()
-        d.num_nodes = m.n
-        d.num_tets = m.m
-        d.X0, d.tets, d.lame, d.rho, d.model, d.fixed, d.force = [a.ctypes.data for a in keep]
-        for c in range(3):
-            d.gravity[c] = float(m.gravity[c])
-        if getattr(m, "soft_k", None) is not None:
-            keep.append(np.ascontiguousarray(m.soft_k, dtype=np.float64).ravel())
-            d.soft_k = keep[-1].ctypes.data
-            if getattr(m, "soft_target", None) is not None:
-                keep.append(np.ascontiguousarray(m.soft_target, dtype=np.float64).ravel())
-                d.soft_target = keep[-1].ctypes.data
-        h = C.c_void_p()
-        _check(lib().phx_instance_create(ctx.h, C.byref(d), C.byref(h)))
-        self.h = h
+        if _handle is None:
+            d, keep = _mesh_desc(m)
+            h = C.c_void_p()
+            _check(lib().phx_instance_create(ctx.h, C.byref(d), C.byref(h)))
+            _handle = h
+        self.h = _handle
         self.N = 3 * m.n
 
     def close(self):

@@ -10,6 +10,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
+#include <thread>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -788,9 +790,11 @@ int phx_instance_destroy(phx_instance inst) {
   return PHX_OK;
 }
 
-int phx_instance_create(phx_context ctx, const phx_mesh* mesh, phx_instance* out) {
-  if (!ctx || !mesh || !out) return set_err(PHX_EINVAL, "NULL argument");
-  *out = nullptr;
+namespace {
+
+// Host part of creating an instance: validation, the pattern, the rest data and the loads
+// (no CUDA call, so instances can be built on several host threads at once).
+bool instance_build_host(const phx_mesh* mesh, phx_instance_s* inst, std::string& err) {
   MeshIn in;
   in.n = mesh->num_nodes;
   in.m = mesh->num_tets;
@@ -804,16 +808,15 @@ int phx_instance_create(phx_context ctx, const phx_mesh* mesh, phx_instance* out
   for (int c = 0; c < 3; ++c) in.gravity[c] = mesh->gravity[c];
   in.soft_k = mesh->soft_k;
   in.soft_target = mesh->soft_target;
-  auto* inst = new phx_instance_s();
-  inst->ctx = ctx;
-  std::string err;
-  if (!build_pattern(in, inst->hp, err)) {
-    delete inst;
-    return set_err(PHX_EINVAL, err);
-  }
+  if (!build_pattern(in, inst->hp, err)) return false;
   for (int c = 0; c < 3; ++c) inst->gravity[c] = mesh->gravity[c];
   if (mesh->force) inst->force.assign(mesh->force, mesh->force + 3 * (size_t)in.n);
-  CU(cudaSetDevice(ctx->device));
+  return true;
+}
+
+// Device part: arena allocations and uploads on the context stream (the caller
+// synchronises).  On failure the instance is destroyed.
+int instance_setup_device(phx_context ctx, const phx_mesh* mesh, phx_instance_s* inst) {
   HostPattern& hp = inst->hp;
   InstDev& D = inst->dev;
   D.n = hp.n; D.m = hp.m; D.nlo = hp.nlo; D.nchunks = hp.nchunks; D.nslots = hp.nslots;
@@ -875,9 +878,64 @@ int phx_instance_create(phx_context ctx, const phx_mesh* mesh, phx_instance* out
   hp.seg_c.clear(); hp.seg_c.shrink_to_fit();
   hp.nseg_c.clear(); hp.nseg_c.shrink_to_fit();
   hp.slot_col.clear(); hp.slot_col.shrink_to_fit();
-  cudaError_t e = cudaStreamSynchronize(ctx->stream);
-  if (e != cudaSuccess) return fail(set_err(PHX_ECUDA, cudaGetErrorString(e)));
-  *out = inst;
+  return PHX_OK;
+}
+
+}  // namespace
+
+int phx_instance_create(phx_context ctx, const phx_mesh* mesh, phx_instance* out) {
+  return phx_instances_create(ctx, 1, mesh, out);
+}
+
+// Builds the host parts of count instances on up to hardware_concurrency() threads, then
+// sets them up on the device one after the other with one synchronisation at the end.
+int phx_instances_create(phx_context ctx, int32_t count, const phx_mesh* meshes, phx_instance* out) {
+  if (!ctx || (count > 0 && (!meshes || !out)) || count < 0) return set_err(PHX_EINVAL, "NULL argument");
+  for (int32_t i = 0; i < count; ++i) out[i] = nullptr;
+  if (count == 0) return PHX_OK;
+  std::vector<phx_instance_s*> insts(count);
+  for (int32_t i = 0; i < count; ++i) {
+    insts[i] = new phx_instance_s();
+    insts[i]->ctx = ctx;
+  }
+  std::vector<std::string> errs(count);
+  std::vector<char> ok(count, 0);
+  std::atomic<int32_t> next{0};
+  auto work = [&]() {
+    for (int32_t i; (i = next.fetch_add(1)) < count;) ok[i] = instance_build_host(&meshes[i], insts[i], errs[i]);
+  };
+  const int nt = std::max(1, std::min<int>(count, (int)std::thread::hardware_concurrency()));
+  if (nt == 1) {
+    work();
+  } else {
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; ++t) pool.emplace_back(work);
+    for (auto& th : pool) th.join();
+  }
+  for (int32_t i = 0; i < count; ++i)
+    if (!ok[i]) {
+      for (auto* p : insts) delete p;
+      return set_err(PHX_EINVAL, count == 1 ? errs[i] : "mesh " + std::to_string(i) + ": " + errs[i]);
+    }
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) {
+    for (auto* p : insts) delete p;
+    return set_err(PHX_ECUDA, cudaGetErrorString(e));
+  }
+  for (int32_t i = 0; i < count; ++i) {
+    const int rc = instance_setup_device(ctx, &meshes[i], insts[i]);  // destroys insts[i] on failure
+    if (rc != PHX_OK) {
+      for (int32_t j = 0; j < i; ++j) phx_instance_destroy(insts[j]);
+      for (int32_t j = i + 1; j < count; ++j) delete insts[j];
+      return rc;
+    }
+  }
+  e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    for (auto* p : insts) phx_instance_destroy(p);
+    return set_err(PHX_ECUDA, cudaGetErrorString(e));
+  }
+  for (int32_t i = 0; i < count; ++i) out[i] = insts[i];
   return PHX_OK;
 }
 

@@ -145,7 +145,10 @@ bool build_pattern(const MeshIn& in, HostPattern& hp, std::string& err) {
   for (int v = 0; v < n; ++v)
     if (!used[v]) { err = "mesh: node " + std::to_string(v) + " belongs to no tet"; return false; }
 
-  // ---- lower blocks, column-major (C, R) -------------------------------
+  // ---- lower blocks, column-major (C, R), and the scatter map ---------------
+  // The tet pairs grouped by column C = min(node_i, node_j) (a counting sort); then per
+  // column its distinct rows R in ascending order (a stamp per row and a sort of the few
+  // distinct ones) and each pair's block index.
   std::vector<int32_t> cnt(n + 1, 0);
   for (int e = 0; e < m; ++e)
     for (int p = 0; p < 10; ++p) {
@@ -153,23 +156,37 @@ bool build_pattern(const MeshIn& in, HostPattern& hp, std::string& err) {
       cnt[std::min(ni, nj) + 1]++;
     }
   for (int v = 0; v < n; ++v) cnt[v + 1] += cnt[v];
-  std::vector<int32_t> rows(cnt[n]);
+  std::vector<int32_t> rows(cnt[n]), pairs(cnt[n]);  // row R and pair id 10 e + p, by column
   {
     std::vector<int32_t> pos(cnt.begin(), cnt.end() - 1);
     for (int e = 0; e < m; ++e)
       for (int p = 0; p < 10; ++p) {
         int ni = hp.tets[4 * (size_t)e + kPairI[p]], nj = hp.tets[4 * (size_t)e + kPairJ[p]];
-        rows[pos[std::min(ni, nj)]++] = std::max(ni, nj);
+        const int q = pos[std::min(ni, nj)]++;
+        rows[q] = std::max(ni, nj);
+        pairs[q] = 10 * e + p;
       }
   }
   hp.lo_colptr.assign(n + 1, 0);
+  hp.scatter.resize(10 * (size_t)m);
   std::vector<int32_t> lo_R;
   lo_R.reserve(cnt[n] / 3);
+  std::vector<int32_t> seen(n, -1), block_of(n, 0), uniq;
+  uniq.reserve(64);
   for (int C = 0; C < n; ++C) {
-    auto b = rows.begin() + cnt[C], en = rows.begin() + cnt[C + 1];
-    std::sort(b, en);
-    auto u = std::unique(b, en);
-    for (auto it = b; it != u; ++it) lo_R.push_back(*it);
+    uniq.clear();
+    for (int q = cnt[C]; q < cnt[C + 1]; ++q)
+      if (seen[rows[q]] != C) {
+        seen[rows[q]] = C;
+        uniq.push_back(rows[q]);
+      }
+    std::sort(uniq.begin(), uniq.end());
+    const int32_t base = (int32_t)lo_R.size();
+    for (size_t j = 0; j < uniq.size(); ++j) {
+      lo_R.push_back(uniq[j]);
+      block_of[uniq[j]] = base + (int32_t)j;
+    }
+    for (int q = cnt[C]; q < cnt[C + 1]; ++q) hp.scatter[pairs[q]] = block_of[rows[q]];
     hp.lo_colptr[C + 1] = (int32_t)lo_R.size();
   }
   hp.nlo = (int32_t)lo_R.size();
@@ -186,15 +203,7 @@ bool build_pattern(const MeshIn& in, HostPattern& hp, std::string& err) {
       return false;
     }
 
-  // ---- scatter map and its inverse (segments) --------------------------
-  hp.scatter.resize(10 * (size_t)m);
-  for (int e = 0; e < m; ++e)
-    for (int p = 0; p < 10; ++p) {
-      int ni = hp.tets[4 * (size_t)e + kPairI[p]], nj = hp.tets[4 * (size_t)e + kPairJ[p]];
-      int R = std::max(ni, nj), C = std::min(ni, nj);
-      auto b = lo_R.begin() + hp.lo_colptr[C], en = lo_R.begin() + hp.lo_colptr[C + 1];
-      hp.scatter[10 * (size_t)e + p] = (int32_t)(std::lower_bound(b, en, R) - lo_R.begin());
-    }
+  // ---- the scatter map's inverse (segments) ------------------------------
   hp.seg_ptr.assign(hp.nlo + 1, 0);
   for (size_t c = 0; c < hp.scatter.size(); ++c) hp.seg_ptr[hp.scatter[c] + 1]++;
   for (int k = 0; k < hp.nlo; ++k) hp.seg_ptr[k + 1] += hp.seg_ptr[k];

@@ -365,3 +365,22 @@ def test_soft_fixed_position_on_gpu(gpu_ctx):
     xs, rs = px.Instance(gpu_ctx, m).solve_static(o, x0)
     assert rs["result_name"] == "SUCCESS"
     assert disp_err(xs, xo, x0) < 1e-5
+
+
+def test_batch_creation_equals_one_at_a_time(gpu_ctx):
+    """phx_instances_create builds the host parts on several threads: the instances solve to
+    the same bits as ones created one at a time; a bad mesh fails the whole call."""
+    meshes = [M.batch_instance(3, i) for i in range(20, 26)]
+    o = px.options(precision=px.PREC_FP32_REFINE, tol_rel=1e-6, tol_max_error=0.0, tol_min_impr=0.0,
+                   tol_min_step=0.0)
+    a = gpu_ctx.create_instances(meshes)
+    b = [px.Instance(gpu_ctx, m) for m in meshes]
+    ra, xa = gpu_ctx.batch_solve(a, o, [m.X0.ravel().copy() for m in meshes])
+    rb, xb = gpu_ctx.batch_solve(b, o, [m.X0.ravel().copy() for m in meshes])
+    for u, v, p, q in zip(xa, xb, ra, rb):
+        assert np.array_equal(u, v) and p["iterations"] == q["iterations"]
+    bad = meshes[0].copy()
+    bad.T = bad.T.copy()
+    bad.T[0, 0] = bad.n + 5
+    with pytest.raises(px.PhxError):
+        gpu_ctx.create_instances([meshes[1], bad])
