@@ -1628,7 +1628,8 @@ __global__ void __launch_bounds__(kTile, (sizeof(Real) == 4 ? 3 : 2)) k_engine(B
 
 
 // ---------------------------------------------------------------------------
-// cluster PCG: one instance per thread-block cluster
+// cluster PCG with rows in L2: k_pcg_cluster (phx_options.pcg_cluster = 2; the default,
+// k_pcg_cg below, keeps the rows in shared memory)
 // ---------------------------------------------------------------------------
 // For instances up to kClusterMaxNodes nodes, the PCG iterations of a linear solve run
 // inside one cluster of kCl CTAs: rows are split into contiguous chunk ranges, the two
