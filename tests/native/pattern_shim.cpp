@@ -20,6 +20,22 @@ int pat_build(int n, int m, const double* X0, const int* T, const double* lame, 
   return phx::build_pattern(in, g_hp, g_err) ? 0 : -1;
 }
 
+// the same with BC_FixDoF soft-mode data (soft_k [n], soft_target [3n] or NULL)
+int pat_build_soft(int n, int m, const double* X0, const int* T, const double* lame, const double* rho,
+                   const unsigned char* model, const unsigned char* fixed, const double* force, const double* grav,
+                   const double* soft_k, const double* soft_target) {
+  phx::MeshIn in;
+  in.n = n; in.m = m; in.X0 = X0; in.T = T; in.lame = lame; in.rho = rho; in.model = model;
+  in.fixed = fixed; in.force = force;
+  for (int c = 0; c < 3; ++c) in.gravity[c] = grav[c];
+  in.soft_k = soft_k;
+  in.soft_target = soft_target;
+  g_hp = phx::HostPattern();
+  return phx::build_pattern(in, g_hp, g_err) ? 0 : -1;
+}
+
+long long pat_soft_size() { return (long long)g_hp.soft.size(); }
+
 const char* pat_error() { return g_err.c_str(); }
 
 // sizes: n, m, nlo, nchunks, nslots
@@ -47,4 +63,5 @@ GET(rest64, double)
 GET(mass, double)
 GET(hlin, double)
 GET(fixmask, unsigned char)
+GET(soft, double)
 }

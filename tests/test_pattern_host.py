@@ -159,3 +159,44 @@ def test_rejects_malformed_meshes(pattern_shim):
     assert "belongs to no tet" in build(pattern_shim, bad)[1]
     bad = base.copy(); bad.lame[4, 0] = np.nan
     assert "non-finite" in build(pattern_shim, bad)[1]
+
+
+def _build_soft(shim, m, soft_k, soft_target):
+    arrs = [np.ascontiguousarray(m.X0, dtype=np.float64).ravel(), np.ascontiguousarray(m.T, dtype=np.int32).ravel(),
+            np.ascontiguousarray(m.lame, dtype=np.float64).ravel(), np.ascontiguousarray(m.rho, dtype=np.float64),
+            np.ascontiguousarray(m.model, dtype=np.uint8), np.ascontiguousarray(m.fixed, dtype=np.uint8),
+            np.ascontiguousarray(m.force, dtype=np.float64), np.ascontiguousarray(m.gravity, dtype=np.float64)]
+    k = None if soft_k is None else np.ascontiguousarray(soft_k, dtype=np.float64)
+    t = None if soft_target is None else np.ascontiguousarray(soft_target, dtype=np.float64).ravel()
+    shim.pat_build_soft.argtypes = [C.c_int, C.c_int] + [C.c_void_p] * 10
+    shim.pat_soft_size.restype = C.c_longlong
+    shim.pat_error.restype = C.c_char_p
+    rc = shim.pat_build_soft(m.n, m.m, *[a.ctypes.data for a in arrs], None if k is None else k.ctypes.data,
+                             None if t is None else t.ctypes.data)
+    if rc != 0:
+        return None, shim.pat_error().decode()
+    soft = np.zeros(int(shim.pat_soft_size()))
+    shim.pat_soft(soft.ctypes.data_as(C.c_void_p))
+    return soft.reshape(-1, 4) if soft.size else soft, ""
+
+
+def test_soft_fixed_position_records(pattern_shim):
+    """BC_FixDoF soft mode: one (target, k) record per node, the target the rest position
+    unless given; no records when no node has a stiffness; bad stiffness rejected."""
+    m = M.cantilever(2, 2, 3)
+    k = np.zeros(m.n)
+    k[[0, 5, m.n - 1]] = [10.0, 2.5, 7.0]
+    soft, _ = _build_soft(pattern_shim, m, k, None)
+    assert soft.shape == (m.n, 4)
+    assert np.array_equal(soft[:, 3], k)
+    assert np.array_equal(soft[:, :3], m.X0)
+    tgt = m.X0 + 0.25
+    soft, _ = _build_soft(pattern_shim, m, k, tgt)
+    assert np.array_equal(soft[:, :3], tgt)
+    soft, _ = _build_soft(pattern_shim, m, np.zeros(m.n), None)
+    assert soft.size == 0
+    for bad in (-1.0, np.nan, np.inf):
+        kb = k.copy()
+        kb[3] = bad
+        soft, err = _build_soft(pattern_shim, m, kb, None)
+        assert soft is None and "soft_k" in err
