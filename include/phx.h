@@ -27,7 +27,7 @@ extern "C" {
 /* ---- status codes ------------------------------------------------------ */
 #define PHX_OK 0
 #define PHX_EINVAL (-1)   /* invalid argument or malformed mesh */
-#define PHX_ENOMEM (-2)   /* device arena exhausted / admission refused */
+#define PHX_ENOMEM (-2)   /* device arena or host memory exhausted / admission refused */
 #define PHX_ETIMEOUT (-3) /* a bounded device wait gave up */
 #define PHX_ECUDA (-4)    /* CUDA runtime error */
 #define PHX_EBUSY (-5)    /* object in use (e.g. instance already admitted) */

@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <new>
 #include <thread>
 #include <chrono>
 #include <cmath>
@@ -901,8 +902,16 @@ int phx_instances_create(phx_context ctx, int32_t count, const phx_mesh* meshes,
   std::vector<std::string> errs(count);
   std::vector<char> ok(count, 0);
   std::atomic<int32_t> next{0};
-  auto work = [&]() {
-    for (int32_t i; (i = next.fetch_add(1)) < count;) ok[i] = instance_build_host(&meshes[i], insts[i], errs[i]);
+  auto work = [&]() {  // nothing may leave a worker thread (or cross the C ABI) as an exception
+    for (int32_t i; (i = next.fetch_add(1)) < count;) {
+      try {
+        ok[i] = instance_build_host(&meshes[i], insts[i], errs[i]);
+      } catch (const std::bad_alloc&) {
+        errs[i] = "out of host memory building the pattern";
+      } catch (...) {
+        errs[i] = "unexpected error building the pattern";
+      }
+    }
   };
   const int nt = std::max(1, std::min<int>(count, (int)std::thread::hardware_concurrency()));
   if (nt == 1) {
@@ -915,7 +924,8 @@ int phx_instances_create(phx_context ctx, int32_t count, const phx_mesh* meshes,
   for (int32_t i = 0; i < count; ++i)
     if (!ok[i]) {
       for (auto* p : insts) delete p;
-      return set_err(PHX_EINVAL, count == 1 ? errs[i] : "mesh " + std::to_string(i) + ": " + errs[i]);
+      const int code = errs[i].rfind("out of host memory", 0) == 0 ? PHX_ENOMEM : PHX_EINVAL;
+      return set_err(code, count == 1 ? errs[i] : "mesh " + std::to_string(i) + ": " + errs[i]);
     }
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) {
