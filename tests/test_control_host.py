@@ -181,3 +181,22 @@ def test_soft_fixed_position_matches_oracle(ctl_shim):
     assert ro["result_name"] == "SUCCESS"
     assert (s.result, s.it, s.total_bis) == (ro["result"], ro["iterations"], ro["bisections"])
     assert rel(x - x0, xo - x0) < 1e-9
+
+
+@pytest.mark.parametrize("lst", [1, 3, 4])
+@pytest.mark.parametrize("idx", [16, 38, 46, 48, 57])
+def test_line_searches_on_batch_instances(ctl_shim, idx, lst):
+    """Small batch instances (CoNH and StVK, 196-455 nodes): Simple and the Wolfe searches
+    take the oracle's decisions exactly (result, iterations, bisections) and reach its
+    iterate.  (Armijo's decisions there are decided in rounding noise once its normalised
+    test stalls, see test_line_search_types_match_oracle.)"""
+    m = M.batch_instance(3, idx)
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    g0 = np.linalg.norm(orc.gradient(x0))
+    kw = dict(tol_max_error=1e-6 * g0, tol_min_impr=0.0, tol_min_step=0.0, num_max_iters=60, lsearch_type=lst)
+    xo, ro = orc.solve_static(x0, ls_solver=1, cg_block_jacobi=1, **kw)
+    x, _, s = H.run(ctl_shim, orc, x0, H.make_opts(**kw))
+    assert ro["result_name"] == "SUCCESS"
+    assert (s.result, s.it, s.total_bis) == (ro["result"], ro["iterations"], ro["bisections"])
+    assert rel(x - x0, xo - x0) < 1e-10
