@@ -200,3 +200,21 @@ def test_line_searches_on_batch_instances(ctl_shim, idx, lst):
     assert ro["result_name"] == "SUCCESS"
     assert (s.result, s.it, s.total_bis) == (ro["result"], ro["iterations"], ro["bisections"])
     assert rel(x - x0, xo - x0) < 1e-10
+
+
+@pytest.mark.parametrize("k", [1e4, 1e6])
+@pytest.mark.parametrize("idx", [16, 48])
+def test_soft_clamped_batch_instances(ctl_shim, idx, k):
+    """Batch instances with their clamped face held by soft fixed-position conditions of two
+    stiffnesses: the oracle's decisions and iterate."""
+    m = M.soft_clamped(M.batch_instance(3, idx), k)
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    g0 = np.linalg.norm(orc.gradient(x0))
+    # (below about 3e-7 g0 the energy comparison of the line search is in rounding noise)
+    kw = dict(tol_max_error=1e-6 * g0, tol_min_impr=0.0, tol_min_step=0.0, num_max_iters=60)
+    xo, ro = orc.solve_static(x0, ls_solver=1, cg_block_jacobi=1, **kw)
+    x, _, s = H.run(ctl_shim, orc, x0, H.make_opts(**kw))
+    assert ro["result_name"] == "SUCCESS"
+    assert (s.result, s.it, s.total_bis) == (ro["result"], ro["iterations"], ro["bisections"])
+    assert rel(x - x0, xo - x0) < 1e-9
