@@ -218,3 +218,26 @@ def test_soft_clamped_batch_instances(ctl_shim, idx, k):
     assert ro["result_name"] == "SUCCESS"
     assert (s.result, s.it, s.total_bis) == (ro["result"], ro["iterations"], ro["bisections"])
     assert rel(x - x0, xo - x0) < 1e-9
+
+
+@pytest.mark.parametrize("lst", [1, 4])
+def test_soft_clamped_implicit_euler_step(ctl_shim, lst):
+    """An implicit-Euler step of a box held by soft fixed-position conditions (inertia and
+    soft terms in one gradient), with the Simple and the strong-Wolfe search: the oracle's
+    result, iterations and state."""
+    base = M.make_box(2, 2, 3, (0.02, 0.02, 0.03), 1e5, 0.3, 1000.0, 0, (0.0, -9.81, 0.0), clamp_face=2)
+    m = M.soft_clamped(base, 1e5)
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    v0 = np.zeros(orc.N)
+    v0[1::3] = 0.2
+    dt = 1e-3
+    # ||g|| starts at about 69 here (the soft-held nodes move with v0); 1e-7 is above the
+    # band where the line search's energy comparison is in rounding noise
+    kw = dict(tol_max_error=1e-7, tol_min_impr=0.0, tol_min_step=0.0, lsearch_type=lst)
+    xo, vo, ro = orc.solve_dynamic(x0, v0, dt, ls_solver=1, cg_block_jacobi=1, **kw)
+    x, v, s = H.run(ctl_shim, orc, x0, H.make_opts(dynamic=1, dt=dt, **kw), dynamic=True, v0=v0)
+    assert ro["result_name"] == "SUCCESS"
+    assert (s.result, s.it, s.total_bis) == (ro["result"], ro["iterations"], ro["bisections"])
+    assert rel(x - x0, xo - x0) < 1e-9
+    assert rel(v, vo) < 1e-9
