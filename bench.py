@@ -238,7 +238,7 @@ def run_batch(args, world, rank, dist):
     meshes = batch_meshes(count, seed=3 + 1000 * rank)
     tets = sum(m.m for m in meshes)
     ctx = px.Context(args.device, arena_bytes=int(args.arena_gb * (1 << 30)))
-    insts = [px.Instance(ctx, m) for m in meshes]
+    insts = ctx.create_instances(meshes)  # host parts built in parallel; same instances as one by one
     served = served_options(px, args)
     plain = px.options(precision=px.PREC_FP64, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0,
                        tol_min_step=0.0, pcg_chunk=args.pcg_chunk, ls_num_max_iters=args.plain_pcg_max,
@@ -689,7 +689,7 @@ def run_dynamics(args, world, rank, dist):
     res = {}
     traj = {}
     for name, prec in (("served_fp32_refine", px.PREC_FP32_REFINE), ("plain_fp64", px.PREC_FP64)):
-        insts = [px.Instance(ctx, m) for m in meshes]
+        insts = ctx.create_instances(meshes)  # host parts built in parallel; same instances as one by one
         for it, m in zip(insts, meshes):
             it.reset()
             it.set_velocities(M.slab_initial_velocity(m))
