@@ -250,7 +250,7 @@ int ensure_batch_cap(phx_context ctx, int num) {
   if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
   ctx->d_inst = nullptr; ctx->d_pre = nullptr; ctx->d_flags = nullptr; ctx->h_flags = nullptr;
   CU(cudaMalloc(&ctx->d_inst, sizeof(InstDev) * cap));
-  CU(cudaMalloc(&ctx->d_pre, sizeof(int32_t) * (4 * (cap + 1) + 1)));
+  CU(cudaMalloc(&ctx->d_pre, sizeof(int32_t) * (3 * (cap + 1) + 1)));
   CU(cudaMalloc(&ctx->d_flags, sizeof(int32_t) * (8 + cap)));
   CU(cudaMallocHost(&ctx->h_flags, sizeof(int32_t) * (8 + cap)));
   ctx->cap = cap;
@@ -270,26 +270,23 @@ int set_batch(phx_context ctx, const std::vector<phx_instance>& list, BatchDev& 
   TRY(ensure_batch_cap(ctx, std::max(num, 1)));
   std::vector<InstDev> d(num);
   std::vector<int32_t>& pre = ctx->h_pre;
-  pre.assign(4 * (ctx->cap + 1) + 1, 0);
+  pre.assign(3 * (ctx->cap + 1) + 1, 0);
   int32_t* pt = pre.data();
   int32_t* pn = pt + (ctx->cap + 1);
   int32_t* pl = pn + (ctx->cap + 1);
-  int32_t* pp = pl + (ctx->cap + 1);
   for (int i = 0; i < num; ++i) {
     d[i] = list[i]->dev;
     pt[i + 1] = pt[i] + tiles(list[i]->dev.m);
     pn[i + 1] = pn[i] + tiles(list[i]->dev.n);
     pl[i + 1] = pl[i] + tiles(list[i]->dev.nlo);
-    pp[i + 1] = pp[i] + (list[i]->dev.nchunks + 3) / 4;  // per-kernel path: 4 chunks per PCG tile
   }
-  pre[4 * (ctx->cap + 1)] = num;
+  pre[3 * (ctx->cap + 1)] = num;
   if (num) CU(cudaMemcpyAsync(ctx->d_inst, d.data(), sizeof(InstDev) * num, cudaMemcpyHostToDevice, ctx->stream));
   CU(cudaMemcpyAsync(ctx->d_pre, pre.data(), sizeof(int32_t) * pre.size(), cudaMemcpyHostToDevice, ctx->stream));
-  B.num = ctx->d_pre + 4 * (ctx->cap + 1);
+  B.num = ctx->d_pre + 3 * (ctx->cap + 1);
   B.pre_tet = ctx->d_pre;
   B.pre_node = ctx->d_pre + (ctx->cap + 1);
   B.pre_lob = ctx->d_pre + 2 * (ctx->cap + 1);
-  B.pre_pcg = ctx->d_pre + 3 * (ctx->cap + 1);
   B.inst = ctx->d_inst;
   B.flags = ctx->d_flags;
   CU(cudaMemsetAsync(ctx->d_flags, 0, sizeof(int32_t) * 8, ctx->stream));  // [2]: cluster PCG wait gave up
@@ -323,20 +320,6 @@ void do_launch(phx_context ctx, KernelId id, int grid, const BatchDev& B, bool f
     launch(id, grid, ctx->stream, B, fp64);
   }
   ctx->launches++;
-}
-
-// One round of the device engine (see the phase sequence in newton_control.h).
-void run_round(phx_context ctx, const BatchDev& B, const Grids& G, bool fp64, int pcg_chunk) {
-  auto L = [&](KernelId id, int grid) { do_launch(ctx, id, grid, B, fp64); };
-  L(K_CONTROL, 1); L(K_VECOP, G.node); L(K_CONTROL, 1);
-  L(K_ELEM_EG, G.tet); L(K_GATHER, G.node);
-  L(K_CONTROL, 1); L(K_VECOP, G.node); L(K_CONTROL, 1);
-  L(K_ELEM_HESS, G.tet); L(K_ASSEMBLE, G.lob); L(K_JACOBI, G.node);
-  L(K_LINSETUP, G.node); L(K_RESID, G.node);
-  for (int k = 0; k < pcg_chunk; ++k) { L(K_PCG_A, G.node); L(K_PCG_B, G.node); }
-  L(K_ACCUM, G.node); L(K_RESID, G.node);
-  L(K_CONTROL, 1); L(K_VECOP, G.node); L(K_CONTROL, 1);
-  L(K_ELEM_EG, G.tet); L(K_GATHER, G.node);
 }
 
 int read_flags(phx_context ctx, int num) {
@@ -1056,7 +1039,6 @@ int run_kernels(phx_instance inst, const std::vector<KernelId>& ids, bool fp64) 
     switch (id) {
       case K_ELEM_EG: case K_ELEM_HESS: grid = G.tet; break;
       case K_ASSEMBLE: grid = G.lob; break;
-      case K_CONTROL: grid = 1; break;
       default: grid = G.node; break;
     }
     do_launch(ctx, id, grid, B, fp64);

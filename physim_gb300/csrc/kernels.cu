@@ -368,12 +368,6 @@ __device__ __forceinline__ void st_vecop(const BatchDev& B, const TileMap& M, in
   }
 }
 
-__global__ void __launch_bounds__(kTile) k_vecop(BatchDev B) {
-  __shared__ double sm[32 * 5];
-  __shared__ int flag;
-  st_vecop(B, full_map(B, B.pre_node), blockIdx.x, gridDim.x, sm, flag);
-}
-
 // ---------------------------------------------------------------------------
 // element energy + gradient (FP64)
 // ---------------------------------------------------------------------------
@@ -904,13 +898,6 @@ __device__ __forceinline__ void st_jacobi(const BatchDev& B, const TileMap& M, i
   }
 }
 
-template <typename Real>
-__global__ void __launch_bounds__(kTile) k_jacobi(BatchDev B) {
-  __shared__ double sm[32 * 5];
-  __shared__ int flag;
-  st_jacobi<Real>(B, full_map(B, B.pre_node), blockIdx.x, gridDim.x, sm, flag);
-}
-
 // b = -g, dx = guess (previous accepted step, EigenCG solveWithGuess) or 0
 __device__ __forceinline__ void st_linsetup(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag) {
   const int total = map_total(M);
@@ -954,11 +941,6 @@ __device__ __forceinline__ void st_linsetup(const BatchDev& B, const TileMap& M,
   }
 }
 
-__global__ void __launch_bounds__(kTile) k_linsetup(BatchDev B) {
-  __shared__ double sm[32 * 5];
-  __shared__ int flag;
-  st_linsetup(B, full_map(B, B.pre_node), blockIdx.x, gridDim.x, sm, flag);
-}
 
 // SELL-32 row sweep: acc = sum_k H(row, col_k) * X(col_k), X given per column by a functor.
 // Slots are taken 4 at a time: all column ids, then all gathers and block loads are issued
@@ -1114,12 +1096,6 @@ __device__ __forceinline__ void st_resid(const BatchDev& B, const TileMap& M, in
   }
 }
 
-template <typename Real>
-__global__ void __launch_bounds__(kTile) k_resid(BatchDev B) {
-  __shared__ double sm[32 * 5];
-  __shared__ int flag;
-  st_resid<Real>(B, full_map(B, B.pre_node), blockIdx.x, gridDim.x, sm, flag);
-}
 
 // PCG step 1: p = z + beta p_prev (formed on the fly for every column, written
 // for the own row into the other buffer), q = (H + shift I) p, pq = p.q
@@ -1188,12 +1164,6 @@ __device__ __forceinline__ void st_pcg_a(const BatchDev& B, const TileMap& M, in
   }
 }
 
-template <typename Real>
-__global__ void __launch_bounds__(kTile) k_pcg_a(BatchDev B) {
-  __shared__ double sm[32 * 5];
-  __shared__ int flag;
-  st_pcg_a<Real>(B, full_map(B, B.pre_pcg), blockIdx.x, gridDim.x, sm, flag);
-}
 
 // PCG step 2: e += alpha p, r -= alpha q, z = Minv r; convergence ||r||^2 < thr (Eigen's rule)
 template <typename Real>
@@ -1255,12 +1225,6 @@ __device__ __forceinline__ void st_pcg_b(const BatchDev& B, const TileMap& M, in
   }
 }
 
-template <typename Real>
-__global__ void __launch_bounds__(kTile) k_pcg_b(BatchDev B) {
-  __shared__ double sm[32 * 5];
-  __shared__ int flag;
-  st_pcg_b<Real>(B, full_map(B, B.pre_pcg), blockIdx.x, gridDim.x, sm, flag);
-}
 
 // dx += e (FP64), then back to the FP64 residual
 template <typename Real>
@@ -1289,27 +1253,6 @@ __device__ __forceinline__ void st_accum(const BatchDev& B, const TileMap& M, in
       advance(B, i);
     }
   }
-}
-
-template <typename Real>
-__global__ void __launch_bounds__(kTile) k_accum(BatchDev B) {
-  __shared__ double sm[32 * 5];
-  __shared__ int flag;
-  st_accum<Real>(B, full_map(B, B.pre_node), blockIdx.x, gridDim.x, sm, flag);
-}
-
-// the state machine: one thread per instance; writes the active count and phases
-__global__ void __launch_bounds__(256) k_control(BatchDev B) {
-  __shared__ double sm[32];
-  const int num = *B.num;
-  double active = 0.0;
-  for (int i = threadIdx.x; i < num; i += blockDim.x) {
-    advance(B, i);
-    active += (B.flags[8 + i] != PH_DONE) ? 1.0 : 0.0;
-  }
-  double v[1] = {active};
-  block_sum<1>(v, sm);
-  if (threadIdx.x == 0) B.flags[0] = (int)v[0];
 }
 
 
@@ -2409,8 +2352,6 @@ cudaError_t launch_engine(bool fp64, int grid, cudaStream_t s, const BatchDev& B
 void launch(KernelId id, int grid, cudaStream_t s, const BatchDev& B, bool fp64) {
   if (grid <= 0) return;
   switch (id) {
-    case K_CONTROL: k_control<<<1, 256, 0, s>>>(B); break;
-    case K_VECOP: k_vecop<<<grid, kTile, 0, s>>>(B); break;
     case K_ELEM_EG: k_elem_eg<<<grid, kTile, 0, s>>>(B); break;
     case K_GATHER: k_gather<<<grid, kTile, 0, s>>>(B); break;
     case K_ELEM_HESS:
@@ -2420,23 +2361,7 @@ void launch(KernelId id, int grid, cudaStream_t s, const BatchDev& B, bool fp64)
     case K_ASSEMBLE:
       if (fp64) k_assemble<double><<<grid, kTile, 0, s>>>(B); else k_assemble<float><<<grid, kTile, 0, s>>>(B);
       break;
-    case K_JACOBI:
-      if (fp64) k_jacobi<double><<<grid, kTile, 0, s>>>(B); else k_jacobi<float><<<grid, kTile, 0, s>>>(B);
-      break;
-    case K_LINSETUP: k_linsetup<<<grid, kTile, 0, s>>>(B); break;
-    case K_RESID:
-      if (fp64) k_resid<double><<<grid, kTile, 0, s>>>(B); else k_resid<float><<<grid, kTile, 0, s>>>(B);
-      break;
-    case K_PCG_A:
-      if (fp64) k_pcg_a<double><<<grid, kTile, 0, s>>>(B); else k_pcg_a<float><<<grid, kTile, 0, s>>>(B);
-      break;
-    case K_PCG_B:
-      if (fp64) k_pcg_b<double><<<grid, kTile, 0, s>>>(B); else k_pcg_b<float><<<grid, kTile, 0, s>>>(B);
-      break;
-    case K_ACCUM:
-      if (fp64) k_accum<double><<<grid, kTile, 0, s>>>(B); else k_accum<float><<<grid, kTile, 0, s>>>(B);
-      break;
-    default: break;
+    default: break;  // the other stages run only inside k_engine
   }
 }
 

@@ -50,6 +50,8 @@ int engine_grid(bool fp64, int num_sms);
 cudaError_t launch_engine(bool fp64, int grid, cudaStream_t s, const BatchDev& B, const EngineArgs& A);
 // PCG of every listed instance that is in PH_PCG, one cluster per instance
 cudaError_t launch_pcg_cluster(cudaStream_t s, const BatchDev& B, const int32_t* list, int count, int kind);
+// One stage as its own kernel, for the evaluation entry points: K_ELEM_EG, K_GATHER,
+// K_ELEM_HESS or K_ASSEMBLE (other ids launch nothing; their stages run inside k_engine)
 void launch(KernelId id, int grid, cudaStream_t s, const BatchDev& B, bool fp64);
 const char* kernel_name(KernelId id);
 

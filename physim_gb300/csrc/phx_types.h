@@ -170,7 +170,6 @@ struct BatchDev {
   const int32_t* pre_tet;     // [num+1]
   const int32_t* pre_node;
   const int32_t* pre_lob;
-  const int32_t* pre_pcg;     // PCG tiles (InstDev::cpt chunks each)
   InstDev* inst;              // [num]
   int32_t* flags;             // [8 + num]: [0] active count, [1] cluster solves waiting, [2] a cluster
                               // PCG wait gave up; [8 + i] phase of instance i
