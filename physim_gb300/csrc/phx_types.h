@@ -29,8 +29,6 @@ constexpr int kChunk = 32;       // SELL chunk height (one warp)
 constexpr int kPartials = 8;     // doubles reduced per tile (at most)
 constexpr int kCl = 8;           // CTAs per cluster of the cluster PCG
 constexpr int kClThreads = 512;  // threads per CTA of the cluster PCG
-constexpr int kClNarrow = 2;         // narrow variant: CTAs per cluster
-constexpr int kClNarrowThreads = 256;  // narrow variant: threads per CTA
 constexpr int kClWideBelow = 32;     // at most this many active instances: one-chunk PCG tiles in the engine
 constexpr int kClusterMaxNodes = 13000;  // instances up to this size solve their PCG in one cluster
 constexpr int kWaitRounds = 4;           // engine rounds an instance may wait for the cluster kernel
