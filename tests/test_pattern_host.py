@@ -200,3 +200,70 @@ def test_soft_fixed_position_records(pattern_shim):
         kb[3] = bad
         soft, err = _build_soft(pattern_shim, m, kb, None)
         assert soft is None and "soft_k" in err
+
+
+# (V + E lower blocks, V + 2E full blocks) of the 6-tet hex grids at their full sizes:
+# the 8x8x32 cantilever, the 32^3 dynamics block, the 48x48x192 cantilever
+FULL_SIZES = [
+    ((8, 8, 32), 18785, 34897),
+    ((32, 32, 32), 274625, 513313),
+    ((48, 48, 192), 3622465, 6781537),
+]
+
+
+@pytest.mark.parametrize("dims,nlo_expect,nfull_expect", FULL_SIZES, ids=["8x8x32", "32^3", "48x48x192"])
+def test_full_size_pattern_properties(pattern_shim, dims, nlo_expect, nfull_expect):
+    """Size-independent checks of the pattern, scatter map, segments and SELL layout at the
+    workloads' full sizes (the oracle comparison above covers small meshes bit for bit)."""
+    nx, ny, nz = dims
+    m = M.make_box(nx, ny, nz, M.CANTILEVER_SIZE, 1e5, 0.3, gravity=M.GRAVITY_Y, clamp_face=4)
+    P, err = build(pattern_shim, m)
+    assert err is None, err
+    n, nlo, T = P["n"], P["nlo"], m.T
+    assert (nlo, 2 * nlo - n) == (nlo_expect, nfull_expect)
+    assert nlo == n + len(M.unique_edges(T))
+
+    # Eigen lower CSC by node blocks: per column C the rows R >= C, ascending, diagonal first
+    R, Cn = P["lo_rc"][:, 0].astype(np.int64), P["lo_rc"][:, 1].astype(np.int64)
+    assert np.all(R >= Cn)
+    assert np.array_equal(P["lo_colptr"], np.concatenate([[0], np.cumsum(np.bincount(Cn, minlength=n))]))
+    same = Cn[1:] == Cn[:-1]
+    assert np.all(Cn[1:] >= Cn[:-1]) and np.all(R[1:][same] > R[:-1][same])
+    assert np.array_equal(R[P["lo_colptr"][:-1]], np.arange(n))
+
+    # scatter: local pair (i, j <= i) of every tet lands on the block (max, min) of its nodes
+    pi = np.array([0, 1, 1, 2, 2, 2, 3, 3, 3, 3])
+    pj = np.array([0, 0, 1, 0, 1, 2, 0, 1, 2, 3])
+    a, b = T[:, pi].astype(np.int64), T[:, pj].astype(np.int64)
+    blk = P["scatter"]
+    assert np.array_equal(R[blk], np.maximum(a, b)) and np.array_equal(Cn[blk], np.minimum(a, b))
+
+    # segments: the inverse of the scatter map, element order inside each block's segment
+    seg_c, seg_ptr = P["seg_c"].astype(np.int64), P["seg_ptr"]
+    assert seg_ptr[-1] == 10 * m.m
+    owner = np.repeat(np.arange(nlo), np.diff(seg_ptr))
+    assert np.array_equal(blk.ravel()[seg_c], owner)
+    assert np.all(seg_c[1:][owner[1:] == owner[:-1]] > seg_c[:-1][owner[1:] == owner[:-1]])
+    assert np.array_equal(np.bincount(seg_c, minlength=10 * m.m), np.ones(10 * m.m, dtype=np.int64))
+    nseg_c, nseg_ptr = P["nseg_c"].astype(np.int64), P["nseg_ptr"]
+    nown = np.repeat(np.arange(n), np.diff(nseg_ptr))
+    assert np.array_equal(T.ravel()[nseg_c], nown)
+    assert np.all(nseg_c[1:][nown[1:] == nown[:-1]] > nseg_c[:-1][nown[1:] == nown[:-1]])
+    assert np.array_equal(np.bincount(nseg_c, minlength=4 * m.m), np.ones(4 * m.m, dtype=np.int64))
+
+    # SELL: each full block (R, C) and its mirror in a distinct slot of row R / row C
+    off = P["chunk_off"]
+    assert np.all(np.diff(off) % 32 == 0) and off[-1] == P["nslots"]
+
+    def slot_row(s):
+        c = np.searchsorted(off, s, side="right") - 1
+        return c * 32 + (s - off[c]) % 32
+
+    lo, up = P["lo_slot"].astype(np.int64), P["up_slot"].astype(np.int64)
+    diag = R == Cn
+    assert np.array_equal(slot_row(lo), R) and np.array_equal(P["slot_col"][lo], Cn)
+    assert np.all(up[diag] == -1) and np.array_equal(P["diag_slot"], lo[diag])
+    u = up[~diag]
+    assert np.array_equal(slot_row(u), Cn[~diag]) and np.array_equal(P["slot_col"][u], R[~diag])
+    used = np.bincount(np.concatenate([lo, u]), minlength=P["nslots"])
+    assert used.max() == 1 and used.sum() == nfull_expect
