@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <atomic>
 #include <new>
+#include <system_error>
 #include <thread>
 #include <chrono>
 #include <cmath>
@@ -897,11 +898,15 @@ int phx_instances_create(phx_context ctx, int32_t count, const phx_mesh* meshes,
     }
   };
   const int nt = std::max(1, std::min<int>(count, (int)std::thread::hardware_concurrency()));
-  if (nt == 1) {
-    work();
-  } else {
+  {
+    // the calling thread works too; if the system refuses a thread, the ones started share
+    // the work (a thread left unjoined would end the process)
     std::vector<std::thread> pool;
-    for (int t = 0; t < nt; ++t) pool.emplace_back(work);
+    try {
+      for (int t = 1; t < nt; ++t) pool.emplace_back(work);
+    } catch (const std::system_error&) {
+    }
+    work();
     for (auto& th : pool) th.join();
   }
   for (int32_t i = 0; i < count; ++i)
