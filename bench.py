@@ -483,6 +483,13 @@ def run_cantilever(args, world, rank, dist):
         secs = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": round(1 / secs, 4), "unit": "solves/s", "cores": os.cpu_count(),
                                "kind": "port", "sample": "one LDLT Newton solve", "report": rr}
+        # the same solve on one thread (OpenMP covers only the element loops, as in the
+        # reference; the report's t_* fields are its per-phase timers)
+        t1 = time.perf_counter()
+        _, r1 = orc.solve_static(x0, tol_max_error=1e-8 * g0, tol_min_impr=0.0, tol_min_step=0.0, threads=1)
+        secs1 = time.perf_counter() - t1
+        out["cpu_baseline_1thread"] = {"value": round(1 / secs1, 4), "unit": "solves/s", "cores": 1,
+                                       "kind": "port", "sample": "one LDLT Newton solve", "report": r1}
         out["rel_displacement_err"] = float(np.linalg.norm(x - xr) / np.linalg.norm(xr - x0))
         out["speedup_vs_cpu"] = round(secs / (ms / 1e3 / args.steps), 1)
     ctx.close()
