@@ -1147,7 +1147,12 @@ __device__ __forceinline__ void st_pcg_a(const BatchDev& B, const TileMap& M, in
     if (tile_done<1>(I, lt, pcg_tiles(B, I), ncta, p, tot, sm, &flag) && threadIdx.x == 0) {
       count_bytes(B, I, K_PCG_A);
       st->pq = tot[0];
-      if (!(tot[0] > 0.0)) {  // not positive definite along p (or non-finite)
+      if (I.opts->precision == 0 && tot[0] < 0.0) {
+        // Eigen's ConjugateGradient has no curvature test: a negative p.q gives a negative
+        // step along p and the iteration goes on; LinearSolver_EigenCG regularises only
+        // when the result fails b.x >= 0 (LinearSolver_EigenCG.cpp:95-107)
+        st->alpha = st->rz / tot[0];
+      } else if (!(tot[0] > 0.0)) {  // not positive definite along p (or non-finite)
         if (I.opts->precision != 0 && tot[0] < 0.0 && st->pcg_iter == 0) {
           // truncated CG, first direction: step along p with |p.q| and stop
           st->alpha = st->rz / -tot[0];

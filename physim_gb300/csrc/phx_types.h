@@ -68,7 +68,8 @@ enum VecOp : int32_t {
 };
 
 // LIN_TRUNCATED: the FP32 path met negative curvature and kept the iterate so far
-// (truncated CG); the plain path reports LIN_BREAKDOWN and regularises like the reference.
+// (truncated CG).  The plain path goes on through negative curvature, as Eigen's CG does;
+// LIN_BREAKDOWN is p.q = 0 or a non-finite value, and regularises like a result with b.x < 0.
 enum LinStatus : int32_t { LIN_RUNNING = 0, LIN_CONVERGED = 1, LIN_MAXITER = 2, LIN_BREAKDOWN = 3, LIN_TRUNCATED = 4 };
 
 enum DevError : int32_t { DEV_OK = 0, DEV_NONFINITE = 1, DEV_BADSTATE = 2 };

@@ -61,7 +61,10 @@ def block_jacobi(H, n):
     return inv
 
 
-def pcg(A, b, x, thr, maxit, Minv):
+def pcg(A, b, x, thr, maxit, Minv, eigen=True):
+    """The device PCG.  eigen=True (the FP64 path): like Eigen's ConjugateGradient, a
+    negative p.q gives a negative step and the iteration goes on; only p.q = 0 or a
+    non-finite value stops it."""
     n = Minv.shape[0]
     apply = lambda r: np.einsum("vab,vb->va", Minv, r.reshape(n, 3)).ravel()
     r = b - A @ x
@@ -75,7 +78,7 @@ def pcg(A, b, x, thr, maxit, Minv):
     while it < maxit:
         q = A @ p
         pq = p @ q
-        if not pq > 0:
+        if not (pq > 0 or (eigen and pq < 0)):
             return x, it, LIN_BREAKDOWN
         alpha = rz / pq
         x = x + alpha * p
@@ -209,7 +212,7 @@ def run(shim, orc, x0, opts, dynamic=False, v0=None, max_steps=200000):
             else:
                 s.phase = PH_RESID
         elif ph == PH_RESID:
-            dx, it, st = pcg(A, b, dx, s.thr_final, o.ls_num_max_iters, Minv)
+            dx, it, st = pcg(A, b, dx, s.thr_final, o.ls_num_max_iters, Minv, eigen=o.precision == 0)
             s.pcg_total += it
             s.lin_status = st
             s.b_dot_dx = b @ dx

@@ -241,3 +241,39 @@ def test_soft_clamped_implicit_euler_step(ctl_shim, lst):
     assert (s.result, s.it, s.total_bis) == (ro["result"], ro["iterations"], ro["bisections"])
     assert rel(x - x0, xo - x0) < 1e-9
     assert rel(v, vo) < 1e-9
+
+
+def test_random_options_match_oracle(ctl_shim):
+    """Seeded option combinations on small boxes: step type, steepest fallback, line search
+    (None, Simple, WolfeWeak, WolfeStrong), its factor and try limit, step clamp, iteration
+    cap and the minimum-step / minimum-improvement tests.  Tolerances stop well above the
+    band where energy comparisons are decided by rounding; the decisions, counts and iterate
+    must then be the oracle's.  (Armijo compares against a normalised direction and stalls
+    into that band whenever the step is shorter than c1; it has its own tests above.)"""
+    rng = np.random.default_rng(7)
+    checked = 0
+    for case in range(120):
+        model = int(rng.integers(0, 2))
+        dims = (int(rng.integers(1, 3)), int(rng.integers(1, 3)), int(rng.integers(2, 6)))
+        E = 10 ** rng.uniform(4, 6)
+        nu = rng.uniform(0.2, 0.45)
+        trac = tuple(rng.uniform(-1, 1, 3) * 10 ** rng.uniform(2, 3.5))
+        grav = (0.0, -9.81, 0.0) if rng.random() < 0.5 else (0.0, 0.0, 0.0)
+        m = M.make_box(*dims, (0.01 * dims[0], 0.01 * dims[1], 0.01 * dims[2]), E, nu, 1000.0, model, grav,
+                       clamp_face=4, load_face=5, traction=trac)
+        orc = oracle.Oracle(m)
+        x0 = orc.rest()
+        g0 = float(np.linalg.norm(orc.gradient(x0)))
+        o = dict(qp_solver=int(rng.random() < 0.85), try_steepest=int(rng.integers(0, 2)),
+                 lsearch_type=int(rng.choice([0, 1, 3, 4])), lsearch_alpha=float(rng.choice([0.5, 0.3])),
+                 lsearch_num_try=int(rng.choice([3, 8, 32])),
+                 max_step_size=float(rng.choice([1000.0, 1e-3, 3e-4])), num_max_iters=int(rng.choice([6, 25, 60])),
+                 tol_max_error=float(rng.choice([1e-3, 1e-4])) * g0,
+                 tol_min_step=float(rng.choice([1e-5, 0.0])), tol_min_impr=float(rng.choice([1e-9, 0.0])))
+        xo, ro = orc.solve_static(x0, ls_solver=1, cg_block_jacobi=1, **o)
+        x, _, s = H.run(ctl_shim, orc, x0, H.make_opts(**o))
+        key = (case, o)
+        assert (s.result, s.it, s.total_bis) == (ro["result"], ro["iterations"], ro["bisections"]), key
+        assert rel(x - x0, xo - x0) < 1e-8, key
+        checked += 1
+    assert checked == 120

@@ -384,3 +384,25 @@ def test_batch_creation_equals_one_at_a_time(gpu_ctx):
     bad.T[0, 0] = bad.n + 5
     with pytest.raises(px.PhxError):
         gpu_ctx.create_instances([meshes[1], bad])
+
+
+def test_negative_curvature_follows_eigen_cg(gpu_ctx):
+    """A Newton step whose Hessian is indefinite: the FP64 PCG goes on through negative
+    curvature as Eigen's ConjugateGradient does, and regularises only if the result fails
+    b.x >= 0 (LinearSolver_EigenCG.cpp:95-107).  On this box the third step's PCG meets
+    p.q < 0 twice and still converges with b.x > 0, so neither side regularises and the
+    iterates stay the oracle's."""
+    m = M.make_box(2, 1, 5, (0.02, 0.01, 0.05), 1.7e4, 0.28, 1000.0, M.MODEL_CONH, (0.0, 0.0, 0.0),
+                   clamp_face=4, load_face=5, traction=(-2855.0, 2021.0, 2534.0))
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    g0 = np.linalg.norm(orc.gradient(x0))
+    kw = dict(tol_max_error=1e-8 * g0, tol_min_impr=0.0, tol_min_step=0.0, try_steepest=1)
+    xo, ro = orc.solve_static(x0, ls_solver=1, cg_block_jacobi=1, **kw)
+    assert ro["result_name"] == "SUCCESS" and ro["reg_trials"] == 0
+    inst = px.Instance(gpu_ctx, m)
+    x, r = inst.solve_static(px.options(**kw), x0)
+    assert r["result_name"] == "SUCCESS" and r["reg_trials"] == 0, r
+    assert r["iterations"] == ro["iterations"] and r["bisections"] == ro["bisections"]
+    assert abs(r["pcg_iterations"] - ro["lin_iterations"]) <= 2 * ro["iterations"]
+    assert disp_err(x, xo, x0) < 1e-9
