@@ -277,3 +277,43 @@ def test_random_options_match_oracle(ctl_shim):
         assert rel(x - x0, xo - x0) < 1e-8, key
         checked += 1
     assert checked == 120
+
+
+def test_random_dynamic_and_soft_cases_match_oracle(ctl_shim):
+    """Seeded implicit-Euler steps and static solves, half of them with soft fixed-position
+    clamps, under random options (as above): the same decisions, counts and iterate."""
+    rng = np.random.default_rng(5)
+    for case in range(80):
+        model = int(rng.integers(0, 2))
+        dims = (int(rng.integers(1, 3)), int(rng.integers(1, 3)), int(rng.integers(2, 5)))
+        E = 10 ** rng.uniform(4, 6)
+        nu = rng.uniform(0.2, 0.45)
+        trac = tuple(rng.uniform(-1, 1, 3) * 10 ** rng.uniform(2, 3.5))
+        m = M.make_box(*dims, (0.01 * dims[0], 0.01 * dims[1], 0.01 * dims[2]), E, nu, 1000.0, model,
+                       (0.0, -9.81, 0.0), clamp_face=4, load_face=5, traction=trac)
+        if rng.random() < 0.5:
+            m = M.soft_clamped(m, float(10 ** rng.uniform(1, 4)), tuple(rng.uniform(-1, 1, 3) * 1e-3))
+        orc = oracle.Oracle(m)
+        x0 = orc.rest()
+        dyn = rng.random() < 0.5
+        o = dict(qp_solver=int(rng.random() < 0.9), try_steepest=int(rng.integers(0, 2)),
+                 lsearch_type=int(rng.choice([0, 1, 3, 4])), lsearch_alpha=float(rng.choice([0.5, 0.3])),
+                 lsearch_num_try=int(rng.choice([3, 8, 32])), max_step_size=float(rng.choice([1000.0, 1e-3])),
+                 num_max_iters=int(rng.choice([6, 25])), tol_min_step=float(rng.choice([1e-5, 0.0])),
+                 tol_min_impr=float(rng.choice([1e-9, 0.0])))
+        if dyn:
+            dt = float(rng.choice([1e-3, 1e-2]))
+            v0 = np.zeros(orc.N)
+            v0[1::3] = rng.uniform(-0.5, 0.5)
+            v0[m.fixed.astype(bool)] = 0
+            o["tol_max_error"] = 1e-6
+            xo, vo, ro = orc.solve_dynamic(x0, v0, dt, ls_solver=1, cg_block_jacobi=1, **o)
+            x, v, s = H.run(ctl_shim, orc, x0, H.make_opts(dynamic=1, dt=dt, **o), dynamic=True, v0=v0)
+            assert rel(v, vo) < 1e-8, (case, o)
+        else:
+            g0 = float(np.linalg.norm(orc.gradient(x0)))
+            o["tol_max_error"] = float(rng.choice([1e-3, 1e-4])) * g0
+            xo, ro = orc.solve_static(x0, ls_solver=1, cg_block_jacobi=1, **o)
+            x, _, s = H.run(ctl_shim, orc, x0, H.make_opts(**o))
+        assert (s.result, s.it, s.total_bis) == (ro["result"], ro["iterations"], ro["bisections"]), (case, dyn, o)
+        assert rel(x - x0, xo - x0) < 1e-8, (case, dyn, o)
