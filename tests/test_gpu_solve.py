@@ -404,5 +404,6 @@ def test_negative_curvature_follows_eigen_cg(gpu_ctx):
     x, r = inst.solve_static(px.options(**kw), x0)
     assert r["result_name"] == "SUCCESS" and r["reg_trials"] == 0, r
     assert r["iterations"] == ro["iterations"] and r["bisections"] == ro["bisections"]
-    assert abs(r["pcg_iterations"] - ro["lin_iterations"]) <= 2 * ro["iterations"]
+    # CG through negative curvature is sensitive to the order of its sums: counts within 10 %
+    assert abs(r["pcg_iterations"] - ro["lin_iterations"]) <= 0.1 * ro["lin_iterations"]
     assert disp_err(x, xo, x0) < 1e-9
