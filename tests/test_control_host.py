@@ -245,8 +245,9 @@ def test_soft_clamped_implicit_euler_step(ctl_shim, lst):
 
 def test_random_options_match_oracle(ctl_shim):
     """Seeded option combinations on small boxes: step type, steepest fallback, line search
-    (None, Simple, WolfeWeak, WolfeStrong), its factor and try limit, step clamp, iteration
-    cap and the minimum-step / minimum-improvement tests.  Tolerances stop well above the
+    (None, Simple, WolfeWeak, WolfeStrong), its factor and try limit, trials one at a time or
+    eight per round, step clamp, iteration cap and the minimum-step / minimum-improvement
+    tests.  Tolerances stop well above the
     band where energy comparisons are decided by rounding; the decisions, counts and iterate
     must then be the oracle's.  (Armijo compares against a normalised direction and stalls
     into that band whenever the step is shorter than c1; it has its own tests above.)"""
@@ -271,8 +272,9 @@ def test_random_options_match_oracle(ctl_shim):
                  tol_max_error=float(rng.choice([1e-3, 1e-4])) * g0,
                  tol_min_step=float(rng.choice([1e-5, 0.0])), tol_min_impr=float(rng.choice([1e-9, 0.0])))
         xo, ro = orc.solve_static(x0, ls_solver=1, cg_block_jacobi=1, **o)
-        x, _, s = H.run(ctl_shim, orc, x0, H.make_opts(**o))
-        key = (case, o)
+        par = int(rng.choice([0, 8]))  # line-search trials one at a time or eight per round
+        x, _, s = H.run(ctl_shim, orc, x0, H.make_opts(ls_parallel=par, **o))
+        key = (case, par, o)
         assert (s.result, s.it, s.total_bis) == (ro["result"], ro["iterations"], ro["bisections"]), key
         assert rel(x - x0, xo - x0) < 1e-8, key
         checked += 1
