@@ -91,8 +91,9 @@ typedef struct phx_options {
   int32_t ls_solver;          /* 1 EigenCG semantics (the only linear solver on the device) */
   int32_t ls_num_max_iters;   /* PCG iterations per linear solve */
   double ls_tol_max_error;    /* PCG relative residual ||r|| < tol ||b|| */
-  int32_t ls_num_reg_trials;
-  int32_t lsearch_type;       /* LSearchType: 0 None, 1 Simple, 2 Armijo, 3 WolfeWeak, 4 WolfeStrong */
+  int32_t ls_num_reg_trials;  /* >= 1; as in the reference, the linear solve's own 10 regularisation
+                                 attempts (LinearSolverOptions::regIters) do not depend on it */
+  int32_t lsearch_type;      /* LSearchType: 0 None, 1 Simple, 2 Armijo, 3 WolfeWeak, 4 WolfeStrong */
   double lsearch_alpha;
   int32_t lsearch_num_try;
   double lsearch_wolfe1;      /* Armijo / Wolfe sufficient-decrease constant c1 (1e-4) */

@@ -131,10 +131,16 @@ PHX_HD inline void ctl_iter_begin(NState& s, const DevOpts& o) {
   }
 }
 
+// Solves a linear solver makes, the first unregularised: LinearSolverOptions::regIters
+// (include/PhySim/Solvers/LinearSolver.h:32).  OptimSolver::Init never sets it from
+// lsNumRegTrials (OptimSolver.cpp:59-62), whose loop in SolveStepInternal computes one step
+// because ComputeStep always succeeds (OptimSolver_USQP_LS.cpp:53-55, OptimSolver.cpp:312-352).
+constexpr int kLinRegIters = 10;
+
 // After a linear solve: regularise and retry, or clamp the step and start the line search.
 PHX_HD inline void ctl_lin_done(NState& s, const DevOpts& o) {
   bool bad = (s.lin_status == LIN_BREAKDOWN) || !(s.b_dot_dx >= 0.0) || !isfinite(s.dx_norm);
-  if (bad && s.reg_trial + 1 < o.ls_num_reg_trials) {
+  if (bad && s.reg_trial + 1 < kLinRegIters) {
     s.reg_trial++;
     s.total_reg++;
     s.shift += s.regT * pow(10.0, (double)(s.reg_trial - 1));

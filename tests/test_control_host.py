@@ -319,3 +319,21 @@ def test_random_dynamic_and_soft_cases_match_oracle(ctl_shim):
             x, _, s = H.run(ctl_shim, orc, x0, H.make_opts(**o))
         assert (s.result, s.it, s.total_bis) == (ro["result"], ro["iterations"], ro["bisections"]), (case, dyn, o)
         assert rel(x - x0, xo - x0) < 1e-8, (case, dyn, o)
+
+
+@pytest.mark.parametrize("trials", [1, 3, 10])
+def test_linear_solve_regularises_ten_times_whatever_ls_num_reg_trials(ctl_shim, trials):
+    """LinearSolver_EigenCG regularises up to LinearSolverOptions::regIters = 10 times, a
+    value OptimSolver never sets from lsNumRegTrials (its own loop computes one step): a
+    solve that needs five regularised retries takes them with any ls_num_reg_trials."""
+    m = M.make_box(2, 1, 3, (0.02, 0.01, 0.03), 23300.0, 0.43, 1000.0, M.MODEL_CONH, (0.0, 0.0, 0.0),
+                   clamp_face=4, load_face=5, traction=(2566.0, -1657.0, -2403.0))
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    g0 = np.linalg.norm(orc.gradient(x0))
+    kw = dict(tol_max_error=1e-6 * g0, tol_min_impr=0.0, tol_min_step=0.0, ls_num_reg_trials=trials)
+    xo, ro = orc.solve_static(x0, ls_solver=1, cg_block_jacobi=1, **kw)
+    x, _, s = H.run(ctl_shim, orc, x0, H.make_opts(**kw))
+    assert ro["result_name"] == "SUCCESS" and ro["reg_trials"] == 5
+    assert (s.result, s.it, s.total_bis, s.total_reg) == (ro["result"], ro["iterations"], ro["bisections"], 5)
+    assert rel(x - x0, xo - x0) < 1e-12

@@ -407,3 +407,22 @@ def test_negative_curvature_follows_eigen_cg(gpu_ctx):
     # CG through negative curvature is sensitive to the order of its sums: counts within 10 %
     assert abs(r["pcg_iterations"] - ro["lin_iterations"]) <= 0.1 * ro["lin_iterations"]
     assert disp_err(x, xo, x0) < 1e-9
+
+
+def test_regularised_retries_match_oracle(gpu_ctx):
+    """An FP64 solve whose linear solves need five regularised retries in all: the device
+    takes them as LinearSolver_EigenCG does (up to 10 per solve, whatever ls_num_reg_trials)
+    and keeps the oracle's iterates."""
+    m = M.make_box(2, 1, 3, (0.02, 0.01, 0.03), 23300.0, 0.43, 1000.0, M.MODEL_CONH, (0.0, 0.0, 0.0),
+                   clamp_face=4, load_face=5, traction=(2566.0, -1657.0, -2403.0))
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    g0 = np.linalg.norm(orc.gradient(x0))
+    kw = dict(tol_max_error=1e-6 * g0, tol_min_impr=0.0, tol_min_step=0.0, ls_num_reg_trials=1)
+    xo, ro = orc.solve_static(x0, ls_solver=1, cg_block_jacobi=1, **kw)
+    assert ro["result_name"] == "SUCCESS" and ro["reg_trials"] == 5
+    inst = px.Instance(gpu_ctx, m)
+    x, r = inst.solve_static(px.options(**kw), x0)
+    assert r["result_name"] == "SUCCESS" and r["reg_trials"] == 5, r
+    assert r["iterations"] == ro["iterations"] and r["bisections"] == ro["bisections"]
+    assert disp_err(x, xo, x0) < 1e-9
