@@ -426,3 +426,27 @@ def test_regularised_retries_match_oracle(gpu_ctx):
     assert r["result_name"] == "SUCCESS" and r["reg_trials"] == 5, r
     assert r["iterations"] == ro["iterations"] and r["bisections"] == ro["bisections"]
     assert disp_err(x, xo, x0) < 1e-9
+
+
+def test_renumbered_mesh_matches_oracle(gpu_ctx):
+    """Unstructured numbering (random node ids, tet order and corner order): the FP64 solve
+    keeps the oracle's iterates and the served solve reaches its equilibrium."""
+    from test_pattern_host import _renumbered
+    m = _renumbered(M.batch_instance(3, 42), 2)
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    g0 = np.linalg.norm(orc.gradient(x0))
+    inst = px.Instance(gpu_ctx, m)
+    E, g = inst.energy_gradient(x0)
+    assert abs(E - orc.energy(x0)) <= 1e-12 * max(1.0, abs(orc.energy(x0)))
+    assert rel(g, orc.gradient(x0)) < 1e-12
+    kw = dict(tol_max_error=1e-8 * g0, tol_min_impr=0.0, tol_min_step=0.0)
+    xo, ro = orc.solve_static(x0, ls_solver=1, cg_block_jacobi=1, **kw)
+    x, r = inst.solve_static(px.options(**kw), x0)
+    assert (r["result"], r["iterations"], r["bisections"]) == (ro["result"], ro["iterations"], ro["bisections"])
+    assert disp_err(x, xo, x0) < 1e-9
+    o = px.options(precision=px.PREC_FP32_REFINE, tol_rel=1e-6, tol_max_error=0.0, tol_min_impr=0.0, tol_min_step=0.0)
+    inst.reset()
+    x, r = inst.solve_static(o)
+    if ro["result_name"] == "SUCCESS":
+        assert r["result_name"] == "SUCCESS" and disp_err(x, xo, x0) < 1e-6
