@@ -8,6 +8,9 @@ Fv, as MaterialModel_3Din3D_* vectorises F).  Needs the reference tree, so it
 only runs where the reference is present; the committed file is what the
 tests read.
 
+material_extreme_golden.npz: the same code at strong compression, strong stretch,
+within 1e-6 of the identity, and I + N(0, 1), 40 of each per model.
+
 cantilever_small.npz: the oracle's converged static solve of a 2x2x8
 Neo-Hookean cantilever (LDLT Newton to ||g||/||g0|| < 1e-10), its Hessian
 pattern and scatter map -- a regression fixture for the oracle itself.
@@ -67,8 +70,53 @@ def cantilever_golden():
                         g0=g0)
 
 
+def material_extreme_golden(per_kind=40, seed=20261204):
+    """The reference's material code at four kinds of deformation gradient: strong
+    compression (singular values 1e-2..1), strong stretch (1..10^1.5), within 1e-6 of the
+    identity, and I + N(0, 1) -- each with a random rotation on both sides."""
+    R = oracle.ref_lib()
+    if R is None:
+        raise SystemExit("reference sources not present: cannot regenerate material_extreme_golden.npz")
+    rng = np.random.default_rng(seed)
+    out = {}
+    for fn, name in ((R.ref_conh, "conh"), (R.ref_stvk, "stvk")):
+        Fs, lames, kinds, psis, Ps, Ds = [], [], [], [], [], []
+        for kind in range(4):
+            for _ in range(per_kind):
+                if kind < 2:
+                    U, _ = np.linalg.qr(rng.standard_normal((3, 3)))
+                    V, _ = np.linalg.qr(rng.standard_normal((3, 3)))
+                    s = 10.0 ** (rng.uniform(-2, 0, 3) if kind == 0 else rng.uniform(0, 1.5, 3))
+                    F = U @ np.diag(s) @ V.T
+                elif kind == 2:
+                    F = np.eye(3) + 1e-6 * rng.standard_normal((3, 3))
+                else:
+                    F = np.eye(3) + rng.standard_normal((3, 3))
+                if np.linalg.det(F) <= 0:
+                    F[:, 0] *= -1.0
+                Fv = np.ascontiguousarray(F.T.ravel())  # column-major
+                lam, mu = 10.0 ** rng.uniform(3, 7), 10.0 ** rng.uniform(3, 7)
+                U1 = np.zeros(1); P = np.zeros(9); H = np.zeros(81)
+                fn(lam, mu, Fv.ctypes.data, U1.ctypes.data, P.ctypes.data, H.ctypes.data)
+                Fs.append(Fv); lames.append((lam, mu)); kinds.append(kind)
+                psis.append(U1[0]); Ps.append(P); Ds.append(H)
+        out[f"{name}_F"] = np.array(Fs)
+        out[f"{name}_lame"] = np.array(lames)
+        out[f"{name}_kind"] = np.array(kinds, dtype=np.int8)
+        out[f"{name}_psi"] = np.array(psis)
+        out[f"{name}_P"] = np.array(Ps)
+        out[f"{name}_dPdF"] = np.array(Ds).reshape(-1, 9, 9)
+    np.savez_compressed(os.path.join(HERE, "material_extreme_golden.npz"), **out)
+
+
 if __name__ == "__main__":
+    # python tests/golden/gen_golden.py [material cantilever extreme]  (default: all)
     oracle.build.build_all()
-    material_golden()
-    cantilever_golden()
+    which = set(sys.argv[1:]) or {"material", "cantilever", "extreme"}
+    if "material" in which:
+        material_golden()
+    if "cantilever" in which:
+        cantilever_golden()
+    if "extreme" in which:
+        material_extreme_golden()
     print("wrote", os.listdir(HERE))

@@ -450,3 +450,29 @@ def test_renumbered_mesh_matches_oracle(gpu_ctx):
     x, r = inst.solve_static(o)
     if ro["result_name"] == "SUCCESS":
         assert r["result_name"] == "SUCCESS" and disp_err(x, xo, x0) < 1e-6
+
+
+def test_element_local_at_extreme_deformations(gpu_ctx):
+    """The FP64 element kernels under a uniform deformation far from rest (every tet with
+    the same F): strong compression, strong stretch and a shear, CoNH and StVK, against the
+    oracle, whose material laws are pinned to the reference's code at such F."""
+    rng = np.random.default_rng(11)
+    U, _ = np.linalg.qr(rng.standard_normal((3, 3)))
+    V, _ = np.linalg.qr(rng.standard_normal((3, 3)))
+    if np.linalg.det(U) < 0:
+        U[:, 0] *= -1
+    if np.linalg.det(V) < 0:
+        V[:, 0] *= -1
+    maps = [U @ np.diag([0.05, 0.3, 0.8]) @ V.T, U @ np.diag([20.0, 3.0, 1.5]) @ V.T,
+            np.array([[1.0, 0.9, 0.0], [0.0, 1.0, 0.4], [0.0, 0.0, 1.0]])]
+    for model in (M.MODEL_CONH, M.MODEL_STVK):
+        m = M.make_box(2, 2, 3, (0.02, 0.02, 0.03), 2e5, 0.4, 1000.0, model, (0.0, 0.0, 0.0), clamp_face=None)
+        inst = px.Instance(gpu_ctx, m)
+        orc = oracle.Oracle(m)
+        for A in maps:
+            x = (m.X0 @ A.T).ravel()
+            E, g, H = inst.element_local(x, px.PREC_FP64)
+            Eo, go, Ho = orc.element_local(x)
+            assert np.max(np.abs(E - Eo) / np.maximum(np.abs(Eo), 1e-300)) < 1e-10
+            assert np.max(np.abs(g - go)) <= 1e-10 * np.abs(go).max()
+            assert np.max(np.abs(H - Ho)) <= 1e-10 * np.abs(Ho).max()

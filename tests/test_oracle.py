@@ -29,6 +29,24 @@ def test_material_matches_reference_mcg(model, name):
         assert rel(D, g[f"{name}_dPdF"][k]) < 1e-12
 
 
+@pytest.mark.parametrize("model,name", [(0, "conh"), (1, "stvk")])
+def test_material_extremes_match_reference_mcg(model, name):
+    """Strong compression, strong stretch, near-identity and large random deformation
+    gradients against the reference's generated code.  Within 1e-6 of the identity the
+    reference forms P and psi with cancellation, so there the bound is the stress scale
+    (lambda + mu) times a few ulps rather than |P| itself."""
+    g = np.load(os.path.join(GOLD, "material_extreme_golden.npz"))
+    F, lame, kind = g[f"{name}_F"], g[f"{name}_lame"], g[f"{name}_kind"]
+    assert sorted(set(kind.tolist())) == [0, 1, 2, 3]
+    for k in range(F.shape[0]):
+        psi, P, D = oracle.material(model, lame[k, 0], lame[k, 1], F[k])
+        scale = lame[k].sum()
+        gp, gP, gD = g[f"{name}_psi"][k], g[f"{name}_P"][k], g[f"{name}_dPdF"][k]
+        assert abs(psi - gp) <= 1e-13 * abs(gp) + 1e-15 * scale, (k, kind[k])
+        assert np.abs(P - gP).max() <= 1e-13 * np.abs(gP).max() + 1e-15 * scale, (k, kind[k])
+        assert np.abs(D - gD).max() <= 1e-13 * np.abs(gD).max(), (k, kind[k])
+
+
 @pytest.mark.skipif(oracle.ref_lib() is None, reason="reference sources not present")
 def test_golden_file_matches_reference_build():
     """Re-derive a few golden entries from the reference build itself (where it exists)."""
