@@ -43,9 +43,9 @@ void pat_sizes(long long* out) {
   out[0] = g_hp.n; out[1] = g_hp.m; out[2] = g_hp.nlo; out[3] = g_hp.nchunks; out[4] = g_hp.nslots;
 }
 
-#define GET(name, type)                                                      \
-  void pat_##name(type* out) {                                               \
-    std::memcpy(out, g_hp.name.data(), g_hp.name.size() * sizeof(type));     \
+#define GET(name, type)                                                                    \
+  void pat_##name(type* out) {                                                             \
+    if (!g_hp.name.empty()) std::memcpy(out, g_hp.name.data(), g_hp.name.size() * sizeof(type)); \
   }
 GET(lo_rc, int)
 GET(lo_colptr, int)
