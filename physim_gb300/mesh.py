@@ -335,3 +335,29 @@ def soft_clamped(m: Mesh, k: float, target_shift=(0.0, 0.0, 0.0)) -> Mesh:
     out.soft_target = m.X0 + np.where(fixed_nodes[:, None], np.asarray(target_shift, dtype=np.float64), 0.0)
     return out
 
+
+
+def renumbered(m: Mesh, seed: int) -> Mesh:
+    """The same mesh with unstructured numbering: nodes renumbered, tets reordered and each
+    tet's corners rotated by an even permutation (orientation kept), all from the seed."""
+    rng = np.random.default_rng(seed)
+    perm = rng.permutation(m.n)          # new id of old node v
+    inv = np.argsort(perm)               # old id of new node
+    order = rng.permutation(m.m)
+    even = np.array([[0, 1, 2, 3], [1, 2, 0, 3], [2, 0, 1, 3], [0, 2, 3, 1], [0, 3, 1, 2], [1, 0, 3, 2],
+                     [2, 3, 0, 1], [3, 2, 1, 0], [1, 3, 2, 0], [3, 0, 2, 1], [2, 1, 3, 0], [3, 1, 0, 2]])
+    T = perm[m.T[order]]
+    T = np.take_along_axis(T, even[rng.integers(0, 12, m.m)], axis=1).astype(np.int32)
+    out = m.copy()
+    out.X0 = m.X0[inv].copy()
+    out.T = T
+    out.lame = m.lame[order].copy()
+    out.rho = m.rho[order].copy()
+    out.model = m.model[order].copy()
+    out.fixed = m.fixed.reshape(-1, 3)[inv].ravel().copy()
+    out.force = m.force.reshape(-1, 3)[inv].ravel().copy()
+    if m.soft_k is not None:
+        out.soft_k = m.soft_k[inv].copy()
+    if m.soft_target is not None:
+        out.soft_target = m.soft_target[inv].copy()
+    return out

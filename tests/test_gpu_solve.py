@@ -431,8 +431,7 @@ def test_regularised_retries_match_oracle(gpu_ctx):
 def test_renumbered_mesh_matches_oracle(gpu_ctx):
     """Unstructured numbering (random node ids, tet order and corner order): the FP64 solve
     keeps the oracle's iterates and the served solve reaches its equilibrium."""
-    from test_pattern_host import _renumbered
-    m = _renumbered(M.batch_instance(3, 42), 2)
+    m = M.renumbered(M.batch_instance(3, 42), 2)
     orc = oracle.Oracle(m)
     x0 = orc.rest()
     g0 = np.linalg.norm(orc.gradient(x0))

@@ -269,33 +269,11 @@ def test_full_size_pattern_properties(pattern_shim, dims, nlo_expect, nfull_expe
     assert used.max() == 1 and used.sum() == nfull_expect
 
 
-def _renumbered(m, seed):
-    """The same mesh with its nodes renumbered, its tets reordered and each tet's corners
-    rotated by an even permutation (orientation kept), all from the seed."""
-    rng = np.random.default_rng(seed)
-    perm = rng.permutation(m.n)          # new id of old node v
-    inv = np.argsort(perm)               # old id of new node
-    order = rng.permutation(m.m)
-    even = np.array([[0, 1, 2, 3], [1, 2, 0, 3], [2, 0, 1, 3], [0, 2, 3, 1], [0, 3, 1, 2], [1, 0, 3, 2],
-                     [2, 3, 0, 1], [3, 2, 1, 0], [1, 3, 2, 0], [3, 0, 2, 1], [2, 1, 3, 0], [3, 1, 0, 2]])
-    T = perm[m.T[order]]
-    T = np.take_along_axis(T, even[rng.integers(0, 12, m.m)], axis=1).astype(np.int32)
-    out = m.copy()
-    out.X0 = m.X0[inv].copy()
-    out.T = T
-    out.lame = m.lame[order].copy()
-    out.rho = m.rho[order].copy()
-    out.model = m.model[order].copy()
-    out.fixed = m.fixed.reshape(-1, 3)[inv].ravel().copy()
-    out.force = m.force.reshape(-1, 3)[inv].ravel().copy()
-    return out
-
-
 @pytest.mark.parametrize("seed", [1, 2, 3])
 def test_pattern_bit_exact_on_renumbered_meshes(pattern_shim, seed):
     """Unstructured numbering: random node ids, tet order and corner order.  The lower
     pattern, the scatter map and the rest data still match the oracle bit for bit."""
-    m = _renumbered(M.batch_instance(3, 40 + seed), seed)
+    m = M.renumbered(M.batch_instance(3, 40 + seed), seed)
     assert np.all(M.signed_volumes(m.X0, m.T) > 0)
     P, err = build(pattern_shim, m)
     assert err is None, err
