@@ -438,7 +438,18 @@ def test_renumbered_mesh_matches_oracle(gpu_ctx):
     inst = px.Instance(gpu_ctx, m)
     E, g = inst.energy_gradient(x0)
     assert abs(E - orc.energy(x0)) <= 1e-12 * max(1.0, abs(orc.energy(x0)))
-    assert rel(g, orc.gradient(x0)) < 1e-12
+    # At rest the elastic gradient cancels to zero: the device's displacement form returns the
+    # load exactly, while the oracle's F = Ds Dm^-1 carries about 2.5e-11 of roundoff there.
+    # The 1e-12 element bound is therefore checked away from rest, where the elastic part is
+    # the gradient's own scale; at rest the bound is that roundoff's size.
+    assert rel(g, orc.gradient(x0)) < 1e-9
+    rng = np.random.default_rng(5)
+    h = np.min(np.linalg.norm(m.X0[m.T[:, 1]] - m.X0[m.T[:, 0]], axis=1))
+    xp = x0 + 0.03 * h * rng.standard_normal(x0.shape)
+    Ep, gp = inst.energy_gradient(xp)
+    gpo = orc.gradient(xp)
+    assert abs(Ep - orc.energy(xp)) <= 1e-11 * max(abs(Ep), 1e-300) + 1e-15 * np.abs(orc.element_local(xp)[0]).sum()
+    assert np.abs(gp - gpo).max() <= 1e-12 * np.abs(gpo).max()
     kw = dict(tol_max_error=1e-8 * g0, tol_min_impr=0.0, tol_min_step=0.0)
     xo, ro = orc.solve_static(x0, ls_solver=1, cg_block_jacobi=1, **kw)
     x, r = inst.solve_static(px.options(**kw), x0)
