@@ -76,8 +76,10 @@ typedef struct phx_mesh {
   const double* soft_target; /* [3*num_nodes] their targets t; NULL = X0 */
 } phx_mesh;
 
-/* Mirrors OptimSolverOptions (include/PhySim/Solvers/OptimSolver.h:47-70)
- * field for field, plus the GPU-path settings at the end. */
+/* Mirrors OptimSolverOptions (include/PhySim/Solvers/OptimSolver.h:23-70): every field
+ * with the same meaning and default, listed in the order of its constructor's
+ * assignments (:47-70) rather than its declaration order, plus the GPU-path settings
+ * at the end. */
 typedef struct phx_options {
   int32_t qp_solver;          /* 0 Steepest, 1 Newton (QPSolverType) */
   double tol_max_error;       /* absolute ||g|| */
@@ -147,6 +149,15 @@ void phx_default_options(phx_options* opts);
 int phx_context_create(int32_t device, int64_t arena_bytes, phx_context* out);
 int phx_context_destroy(phx_context ctx);
 int phx_context_memory(phx_context ctx, int64_t* used_bytes, int64_t* capacity_bytes);
+/* Test hook of the bounded device waits; no counterpart in the reference.  Every wait of
+ * the engine (a grid barrier between two stages) gives up after a cycle limit, flags the
+ * launch and the call returns PHX_ETIMEOUT with the context still usable.  With
+ * barrier_tag in 1..22, the engine's grid barrier of that number waits, in every launch
+ * that follows, for one arrival more than the CTAs taking part, so it runs out after
+ * limit_cycles SM cycles (1000 .. 4e9).  Tag 1 is the barrier after each round's
+ * bookkeeping, reached by every solve.  barrier_tag 0 switches the hook off and restores
+ * the default limit (4e9 cycles, about 2 s). */
+int phx_debug_unmet_barrier(phx_context ctx, int32_t barrier_tag, int64_t limit_cycles);
 
 /* ---- instances: Simulable_FEM set-up (replaces Simulable::Setup + the first
  * triplet assembly that fixes the Hessian pattern, source/PhySim/BasicTypes.cpp:118-145).
@@ -251,8 +262,12 @@ int64_t phx_kernel_launches(phx_context ctx);
  * Kernels are queued on `stream` (a cudaStream_t; NULL = legacy default stream) and the
  * call returns without waiting.  The scratch's device address is looked up on the first
  * call on each device (with that device current), so that call must precede any stream
- * capture.  Calls that overlap on the GPU race on the shared scratch.  More than
- * PHX_NOALLOC_MAX_TETS tets: PHX_EINVAL. */
+ * capture; the address is then kept for the life of the process, so the entry point
+ * assumes the device's primary context throughout (no use after cudaDeviceReset).
+ * Calls that overlap on the GPU race on the shared scratch.  More than
+ * PHX_NOALLOC_MAX_TETS tets: PHX_EINVAL.  The indices are trusted, not checked on the
+ * device: every tets entry lies in [0, num_nodes), seg_ptr rises from 0 to 10*num_tets
+ * and every seg_c entry lies in [0, 10*num_tets). */
 #define PHX_NOALLOC_MAX_TETS 32768
 int phx_hessian_blocks_noalloc(int32_t num_nodes, int32_t num_tets, int32_t num_lower_blocks, const int32_t* tets,
                                const double* rest, const uint8_t* model, const double* x, const double* X0,

@@ -2,8 +2,10 @@
 
 * ``liboracle.so``  -- the C++ restatement in phx_oracle.cpp (always built).
 * ``_ref/libref_mcg.so`` -- the reference's own generated material code, compiled
-  from the reference tree when it is present on this machine (it is not on the
-  GPU host).  It is only used to regenerate and re-check tests/golden/.
+  from the reference tree when it is present (it is not on the GPU host).  The
+  tree is the directory named by the environment variable PHYSIM_REFERENCE, or
+  by ``--reference DIR`` on the command line, or /root/reference by default.
+  It is only used to regenerate and re-check tests/golden/.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load these.
 """
@@ -14,7 +16,8 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_AUTO = "/root/reference/include/PhySim/Utils/Auto"
+DEFAULT_REFERENCE = "/root/reference"
+AUTO_SUBDIR = os.path.join("include", "PhySim", "Utils", "Auto")
 LIB = os.path.join(HERE, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref_mcg.so")
 
@@ -35,21 +38,30 @@ def build_oracle(force: bool = False) -> str:
     return LIB
 
 
-def build_ref(force: bool = False) -> str | None:
-    if not os.path.isdir(REF_AUTO):
+def reference_root(arg: str | None = None) -> str:
+    """The reference tree: an explicit argument, else $PHYSIM_REFERENCE, else the default."""
+    return arg or os.environ.get("PHYSIM_REFERENCE") or DEFAULT_REFERENCE
+
+
+def build_ref(force: bool = False, reference: str | None = None) -> str | None:
+    auto = os.path.join(reference_root(reference), AUTO_SUBDIR)
+    if not os.path.isdir(auto):
         return None
     os.makedirs(os.path.dirname(REF_LIB), exist_ok=True)
     src = os.path.join(HERE, "ref_mcg_shim.cpp")
     if force or _stale(REF_LIB, [src]):
-        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-w", "-I", REF_AUTO,
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-w", "-I", auto,
                "-o", REF_LIB, src]
         subprocess.check_call(cmd)
     return REF_LIB
 
 
-def build_all(force: bool = False):
-    return build_oracle(force), build_ref(force)
+def build_all(force: bool = False, reference: str | None = None):
+    return build_oracle(force), build_ref(force, reference)
 
 
 if __name__ == "__main__":
-    print(build_all(force="--force" in sys.argv))
+    ref = None
+    if "--reference" in sys.argv:
+        ref = sys.argv[sys.argv.index("--reference") + 1]
+    print(build_all(force="--force" in sys.argv, reference=ref))

@@ -34,7 +34,7 @@ EXPORTS = [
     "phx_dynamic_step", "phx_batch_solve", "phx_batch_dynamic_step", "phx_server_create", "phx_server_destroy",
     "phx_server_submit", "phx_server_progress", "phx_server_poll", "phx_profile_enable", "phx_profile_read",
     "phx_profile_reset", "phx_profile_bytes", "phx_kernel_launches", "phx_timer_mark", "phx_timer_elapsed",
-    "phx_hessian_blocks_noalloc",
+    "phx_hessian_blocks_noalloc", "phx_debug_unmet_barrier",
 ]
 
 
@@ -131,6 +131,7 @@ def lib():
         "phx_timer_mark": ([vp, i32], C.c_int),
         "phx_timer_elapsed": ([vp, i32, i32, C.POINTER(dbl)], C.c_int),
         "phx_hessian_blocks_noalloc": ([i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp], C.c_int),
+        "phx_debug_unmet_barrier": ([vp, i32, i64], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -203,6 +204,11 @@ class Context:
         ms = C.c_double()
         _check(lib().phx_timer_elapsed(self.h, int(a), int(b), C.byref(ms)))
         return ms.value
+
+    def debug_unmet_barrier(self, tag: int, limit_cycles: int = 0):
+        """Test hook: engine grid barrier `tag` waits for an arrival that never comes and gives
+        up after limit_cycles (tag 0: off)."""
+        _check(lib().phx_debug_unmet_barrier(self.h, int(tag), int(limit_cycles)))
 
     def kernel_launches(self) -> int:
         return int(lib().phx_kernel_launches(self.h))

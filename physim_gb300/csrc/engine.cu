@@ -160,6 +160,8 @@ struct phx_context_s {
   std::vector<int32_t> h_clist;  // instances whose PCG runs per cluster, largest first
   std::vector<int32_t> h_kind;   // their PCG kind, by batch position
   int clist_kinds = 0;  // bit k: the cluster list holds instances of PCG kind k
+  long long wait_limit = kBarrierLimit;  // grid-barrier wait limit of the engine (SM cycles)
+  int unmet_tag = 0;                     // test hook: grid barrier that waits for an arrival never made
 };
 
 struct phx_instance_s {
@@ -488,7 +490,7 @@ int run_engine(phx_context ctx, const BatchDev& B, int num, bool fp64, int round
   const int32_t hdr[2] = {0, grid};  // active count (set by the kernel), CTAs running
   CU(cudaMemcpyAsync(ctx->d_act, hdr, sizeof(hdr), cudaMemcpyHostToDevice, ctx->stream));
   EngineArgs A{ctx->d_bar, ctx->d_act, ctx->profiling ? ctx->d_stage : nullptr, ctx->cap, rounds, pcg_chunk,
-               kWaitRounds, kWaitShare};
+               kWaitRounds, kWaitShare, ctx->wait_limit, ctx->unmet_tag};
   cudaEvent_t a = nullptr, b = nullptr;
   if (ctx->profiling) TRY(profile_events(ctx, &a, &b));
   CU(launch_engine(fp64, grid, ctx->stream, B, A));
@@ -759,6 +761,21 @@ int phx_context_destroy(phx_context ctx) {
   return PHX_OK;
 }
 
+int phx_debug_unmet_barrier(phx_context ctx, int32_t barrier_tag, int64_t limit_cycles) {
+  if (!ctx) return set_err(PHX_EINVAL, "ctx is NULL");
+  if (barrier_tag < 0 || barrier_tag > 22) return set_err(PHX_EINVAL, "barrier_tag must be 0 (off) or 1..22");
+  if (barrier_tag == 0) {
+    ctx->unmet_tag = 0;
+    ctx->wait_limit = kBarrierLimit;
+    return PHX_OK;
+  }
+  if (limit_cycles < 1000 || limit_cycles > kBarrierLimit)
+    return set_err(PHX_EINVAL, "limit_cycles must lie in [1000, 4e9]");
+  ctx->unmet_tag = barrier_tag;
+  ctx->wait_limit = limit_cycles;
+  return PHX_OK;
+}
+
 int phx_context_memory(phx_context ctx, int64_t* used, int64_t* cap) {
   if (!ctx) return set_err(PHX_EINVAL, "ctx is NULL");
   if (used) *used = (int64_t)ctx->arena.used;
@@ -878,13 +895,21 @@ int phx_instances_create(phx_context ctx, int32_t count, const phx_mesh* meshes,
   if (!ctx || (count > 0 && (!meshes || !out)) || count < 0) return set_err(PHX_EINVAL, "NULL argument");
   for (int32_t i = 0; i < count; ++i) out[i] = nullptr;
   if (count == 0) return PHX_OK;
-  std::vector<phx_instance_s*> insts(count);
-  for (int32_t i = 0; i < count; ++i) {
-    insts[i] = new phx_instance_s();
-    insts[i]->ctx = ctx;
+  std::vector<phx_instance_s*> insts;
+  std::vector<std::string> errs;
+  std::vector<char> ok;
+  try {  // no exception may cross the C ABI: a refused host allocation is PHX_ENOMEM
+    insts.assign(count, nullptr);
+    errs.resize(count);
+    ok.assign(count, 0);
+    for (int32_t i = 0; i < count; ++i) {
+      insts[i] = new phx_instance_s();
+      insts[i]->ctx = ctx;
+    }
+  } catch (const std::bad_alloc&) {
+    for (auto* p : insts) delete p;
+    return set_err(PHX_ENOMEM, "out of host memory creating instances");
   }
-  std::vector<std::string> errs(count);
-  std::vector<char> ok(count, 0);
   std::atomic<int32_t> next{0};
   auto work = [&]() {  // nothing may leave a worker thread (or cross the C ABI) as an exception
     for (int32_t i; (i = next.fetch_add(1)) < count;) {

@@ -1265,19 +1265,21 @@ __device__ __forceinline__ void st_accum(const BatchDev& B, const TileMap& M, in
 // the persistent engine: whole Newton rounds in one cooperative launch
 // ---------------------------------------------------------------------------
 // Grid barrier over all CTAs of a cooperative launch (co-residency is guaranteed by
-// cudaLaunchCooperativeKernel).  The wait is bounded: after kBarrierLimit clock
-// cycles a CTA records a timeout and the stage it was in, and every CTA then leaves
-// the kernel at its next barrier, so a fault in the engine ends the launch instead
-// of hanging the device.
-constexpr long long kBarrierLimit = 4000000000LL;  // about 2 s of SM clock
+// cudaLaunchCooperativeKernel).  The wait is bounded: after `limit` clock cycles
+// (kBarrierLimit by default) a CTA records a timeout and the stage it was in, and every
+// CTA then leaves the kernel at its next barrier, so a fault in the engine ends the
+// launch instead of hanging the device.  The barrier touches global memory only.
 
 // nblocks = the CTAs taking part (always the lowest-numbered ones).
 // `abort` is the launch-wide error flag (the round-wide barrier's): a timeout on either
 // barrier object raises it and every waiting CTA leaves.
 // live: the per-phase counts; the last CTA to arrive copies them into the snapshot half
 // that every CTA reads after the barrier (null: no counts).
+// unmet: the barrier expects one arrival more than nblocks, which never comes (the test
+// hook of phx_debug_unmet_barrier): every CTA waits until the limit.
 __device__ __forceinline__ bool grid_sync(GridBar* gb, unsigned int nblocks, int tag, int* abort,
-                                          int32_t* live = nullptr) {
+                                          int32_t* live = nullptr, long long limit = kBarrierLimit,
+                                          bool unmet = false) {
   __syncthreads();
   if (threadIdx.x == 0) {
     volatile unsigned int* vgen = &gb->gen;
@@ -1285,7 +1287,7 @@ __device__ __forceinline__ bool grid_sync(GridBar* gb, unsigned int nblocks, int
     const unsigned int g = *vgen;
     __threadfence();
     const unsigned int a = atomicAdd(&gb->arrive, 1u);
-    if (a == nblocks - 1) {
+    if (!unmet && a == nblocks - 1) {
       gb->arrive = 0u;
       if (live) {
         __threadfence();
@@ -1298,7 +1300,7 @@ __device__ __forceinline__ bool grid_sync(GridBar* gb, unsigned int nblocks, int
       int polls = 0;
       while (*vgen == g) {
         if (*verr) break;
-        if (clock64() - t0 > kBarrierLimit) {
+        if (clock64() - t0 > limit) {
           if (atomicCAS(&gb->err, 0, 1) == 0) gb->stage = tag;
           atomicExch(abort, 1);
           break;
@@ -1458,11 +1460,13 @@ __global__ void __launch_bounds__(kTile, (sizeof(Real) == 4 ? 3 : 2)) k_engine(B
   int first_wait = -1;  // round in which an instance first waited for the cluster kernel
   // two barrier objects: the PCG group synchronises on its own counter while the CTAs
   // that skip the PCG block are already arriving at the next round-wide barrier
-#define PHX_SYNC(n, tag, kind)                                                     \
-  if (!grid_sync(A.bar, (unsigned)(n), tag, &A.bar->err, B.phase_live)) return;  \
+#define PHX_SYNC(n, tag, kind)                                                                             \
+  if (!grid_sync(A.bar, (unsigned)(n), tag, &A.bar->err, B.phase_live, A.wait_limit, A.unmet_tag == (tag))) \
+    return;                                                                                               \
   stage_clock(A, kind, t);
-#define PHX_SYNC_PCG(n, tag, kind)                                      \
-  if (!grid_sync(A.bar + 1, (unsigned)(n), tag, &A.bar->err)) return;  \
+#define PHX_SYNC_PCG(n, tag, kind)                                                                  \
+  if (!grid_sync(A.bar + 1, (unsigned)(n), tag, &A.bar->err, nullptr, A.wait_limit, A.unmet_tag == (tag))) \
+    return;                                                                                        \
   stage_clock(A, kind, t);
   // a stage (and the barrier after it) runs only if an instance is in its phase at the
   // last barrier's snapshot: every CTA reads the same snapshot, so all skip together
@@ -1845,7 +1849,7 @@ static_assert(((4 * kCgMaxChunks + 15) & ~15) + ((4 * (kCgMaxCpc + 1) + 15) & ~1
                   kCgSmem,
               "rows of the largest cluster instance must fit in shared memory");
 
-constexpr int kLinAbort = -1;  // a reduction wait gave up: the kernel returns at once
+constexpr int kLinAbort = -1;  // a reduction wait gave up: the cluster leaves together (cg_reduce)
 struct CgResult {  // FP32 like the solve; widened once when written to the instance state
   int iter, done, status;
   float rr, eta, gamma, beta;
@@ -1895,12 +1899,24 @@ __device__ __forceinline__ float4 cl_ld4f(uint32_t a) {
 // Reuse of the single slot buffer, ws and the mbarrier needs no barrier of its own: a CTA
 // pushes the sums of the next reduction only after the cluster barrier that follows its
 // next update, which every CTA reaches only after reading this reduction's slots; warp 0
-// reads ws before its push, which every wait depends on.  The wait gives up after
-// kCgWaitCycles (the cluster is then broken): it flags the batch error and returns false.
+// reads ws before its push, which every wait depends on.
+//
+// The wait gives up after kCgWaitCycles.  The decision is made uniform before any CTA
+// leaves, because a peer may still push into this CTA's slots or read its z rows:
+//  * within the CTA: __syncthreads_or over the threads' own waits, so all of them agree;
+//  * within the cluster: the CTA that gave up stores 1 into the abort word of every CTA
+//    of the cluster (its own included) and flags the batch error, then goes on to the
+//    next cluster barrier, the same one its peers reach next (an iteration's, or the end
+//    of the instance's; all CTAs pass the same barriers up to that point because their
+//    decisions come from the same sums).  The barrier's release/acquire makes the abort
+//    word visible to every CTA after it; each checks it right after each barrier that can
+//    follow a reduction and, if set, drains its own mbarrier (cg_drain: bounded) and
+//    returns, so no CTA touches another's shared memory after that barrier.
 constexpr long long kCgWaitCycles = 2000000000LL;
+constexpr long long kCgDrainCycles = 200000000LL;  // pushes in flight into this CTA at an abort
 template <int K, int CL, int NT>
 __device__ __forceinline__ bool cg_reduce(float (&p)[K], unsigned rank, float (*red)[4], float (*ws)[4], uint32_t mbar,
-                                          unsigned& phase, int32_t* err, float (&tot)[K]) {
+                                          unsigned& phase, int32_t* err, uint32_t abort_sm, float (&tot)[K]) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < K; ++k)
@@ -1932,6 +1948,7 @@ __device__ __forceinline__ bool cg_reduce(float (&p)[K], unsigned rank, float (*
   const unsigned parity = phase & 1u;
   ++phase;
   const long long t0 = clock64();
+  int gave_up = 0;
   for (;;) {
     uint32_t done;
     asm volatile(
@@ -1942,9 +1959,17 @@ __device__ __forceinline__ bool cg_reduce(float (&p)[K], unsigned rank, float (*
         : "memory");
     if (done) break;
     if (clock64() - t0 > kCgWaitCycles) {
-      atomicExch(err, 1);
-      return false;
+      gave_up = 1;
+      break;
     }
+  }
+  if (__syncthreads_or(gave_up)) {  // the whole CTA gives up; tell every CTA of the cluster
+    if (threadIdx.x < CL) {
+      const uint32_t dst = cl_map(abort_sm, threadIdx.x);
+      asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(dst), "r"(1) : "memory");
+    }
+    if (threadIdx.x == 0) atomicExch(err, 1);
+    return false;
   }
 #pragma unroll
   for (int k = 0; k < K; ++k) {
@@ -1954,6 +1979,34 @@ __device__ __forceinline__ bool cg_reduce(float (&p)[K], unsigned rank, float (*
     tot[k] = s;
   }
   return true;
+}
+
+// The abort word of this CTA (set by any CTA of the cluster that gave up a wait), read after
+// a cluster barrier: the same value in every thread and every CTA.
+__device__ __forceinline__ bool cg_aborted(uint32_t abort_sm) {
+  uint32_t v;
+  asm volatile("ld.volatile.shared::cta.u32 %0, [%1];" : "=r"(v) : "r"(abort_sm) : "memory");
+  return v != 0u;
+}
+
+// Before leaving after an abort: waits (bounded) for the phase of the last reduction to
+// complete, so that no push of a peer is still on its way into this CTA's shared memory.
+__device__ __forceinline__ void cg_drain(uint32_t mbar, unsigned phase) {
+  if (threadIdx.x == 0 && phase > 0) {
+    const unsigned parity = (phase - 1u) & 1u;
+    const long long t0 = clock64();
+    for (;;) {
+      uint32_t done;
+      asm volatile(
+          "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+          "selp.u32 %0, 1, 0, p;\n\t}"
+          : "=r"(done)
+          : "r"(mbar), "r"(parity)
+          : "memory");
+      if (done || clock64() - t0 > kCgDrainCycles) break;
+    }
+  }
+  __syncthreads();
 }
 
 // The slots k = sub, sub + L, ... < len of one row (lane `lane` of its chunk) from slot-row
@@ -2052,8 +2105,8 @@ __device__ __forceinline__ float cg_spmv(const InstDev& I, const CgShared& S, in
 template <int L, int CL, int NT>
 __device__ __forceinline__ CgResult cg_solve(const InstDev& I, const CgShared& S, unsigned rank, int c0, int row0,
                                           int row1, int64_t sb, float (*red)[4], float (*ws)[4], uint32_t mbar,
-                                          unsigned& phase, int32_t* err, float sh, float thr, int maxit, bool trunc_ok,
-                                          int iter0) {
+                                          unsigned& phase, int32_t* err, uint32_t abort_sm, float sh, float thr,
+                                          int maxit, bool trunc_ok, int iter0) {
   const int nrow = row1 - row0, ms = S.mrows;
   float4* const Z = cgs<float4>(S.z);
   float4* const Rv = cgs<float4>(S.r);
@@ -2078,7 +2131,8 @@ __device__ __forceinline__ CgResult cg_solve(const InstDev& I, const CgShared& S
   cl_sync();  // z of every CTA written
   float p3[3] = {g1[0], g1[1], cg_spmv<L, NT>(I, S, c0, row0, row1, sb, sh)};
   float t3[3];
-  if (!cg_reduce<3, CL, NT>(p3, rank, red, ws, mbar, phase, err, t3)) {
+  if (!cg_reduce<3, CL, NT>(p3, rank, red, ws, mbar, phase, err, abort_sm, t3)) {
+    cl_sync();  // the barrier the peers reach next; they see the abort word after it
     out.status = kLinAbort;
     return out;
   }
@@ -2145,9 +2199,14 @@ __device__ __forceinline__ CgResult cg_solve(const InstDev& I, const CgShared& S
       break;
     }
     cl_sync();  // the new z of every CTA written; none reads the previous z any more
+    if (cg_aborted(abort_sm)) {  // a CTA gave up the last reduction: leave together
+      out.status = kLinAbort;
+      return out;
+    }
     float pg[3] = {g[0], g[1], cg_spmv<L, NT>(I, S, c0, row0, row1, sb, sh)};
     float tg[3];
-    if (!cg_reduce<3, CL, NT>(pg, rank, red, ws, mbar, phase, err, tg)) {
+    if (!cg_reduce<3, CL, NT>(pg, rank, red, ws, mbar, phase, err, abort_sm, tg)) {
+      cl_sync();  // the barrier the peers reach next; they see the abort word after it
       out.status = kLinAbort;
       return out;
     }
@@ -2178,11 +2237,14 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_pcg_cg(Bat
   __shared__ __align__(16) float red[CL][4];  // partial sums pushed by every CTA of the cluster
   __shared__ float ws[NT / 32][4];
   __shared__ __align__(8) uint64_t mbar_obj;   // completes when all CL pushes of a reduction landed
+  __shared__ uint32_t abort_word;              // set by a CTA of the cluster that gave up a wait
   const unsigned rank = cl_rank();
   const int tid = threadIdx.x;
   const uint32_t mbar = smem_u32(&mbar_obj);
+  const uint32_t abort_sm = smem_u32(&abort_word);
   unsigned phase = 0;  // reductions waited for so far (the mbarrier's phase)
   if (tid == 0) {
+    abort_word = 0u;
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -2275,13 +2337,16 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_pcg_cg(Bat
     const bool trunc_ok = I.opts->precision != 0;
     const int iter0 = st->pcg_iter;
     CgResult out;
-    if (L == 4) out = cg_solve<4, CL, NT>(I, S, rank, c0, row0, row1, sb, red, ws, mbar, phase, err, sh, thr, maxit,
+    if (L == 4) out = cg_solve<4, CL, NT>(I, S, rank, c0, row0, row1, sb, red, ws, mbar, phase, err, abort_sm, sh, thr, maxit,
                                            trunc_ok, iter0);
-    else if (L == 2) out = cg_solve<2, CL, NT>(I, S, rank, c0, row0, row1, sb, red, ws, mbar, phase, err, sh, thr, maxit,
+    else if (L == 2) out = cg_solve<2, CL, NT>(I, S, rank, c0, row0, row1, sb, red, ws, mbar, phase, err, abort_sm, sh, thr, maxit,
                                            trunc_ok, iter0);
-    else out = cg_solve<1, CL, NT>(I, S, rank, c0, row0, row1, sb, red, ws, mbar, phase, err, sh, thr, maxit,
+    else out = cg_solve<1, CL, NT>(I, S, rank, c0, row0, row1, sb, red, ws, mbar, phase, err, abort_sm, sh, thr, maxit,
                                            trunc_ok, iter0);
-    if (out.status == kLinAbort) return;  // batch error flagged; the host reports a timeout
+    if (out.status == kLinAbort) {  // every CTA of the cluster leaves after the same barrier
+      cg_drain(mbar, phase);
+      return;                       // the batch error is flagged; the host reports a timeout
+    }
     for (int t = tid; t < nrow; t += NT) {
       const float4 e = cgs<float4>(S.e)[t];
       const float ev[3] = {e.x, e.y, e.z};
@@ -2303,6 +2368,10 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_pcg_cg(Bat
       advance(B, i);
     }
     cl_sync();  // shared buffers and partial slots are reused by the next instance
+    if (cg_aborted(abort_sm)) {  // a CTA gave up the solve's last reduction: leave together
+      cg_drain(mbar, phase);
+      return;
+    }
   }
 }
 

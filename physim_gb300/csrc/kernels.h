@@ -43,7 +43,11 @@ struct EngineArgs {
   int pcg_chunk;
   int wait_rounds;  // hand the waiting instances to the cluster PCG kernel this many rounds after the
   int wait_share;   // first one waited, or once waiting * wait_share >= active
+  long long wait_limit;  // SM cycles a grid-barrier wait lasts before it gives up
+  int unmet_tag;         // test hook: the grid barrier with this tag waits for one arrival more than
+                         // the CTAs taking part, so it gives up (0: none)
 };
+constexpr long long kBarrierLimit = 4000000000LL;  // default wait_limit: about 2 s of SM clock
 
 cudaError_t setup_kernel_attributes();
 int engine_grid(bool fp64, int num_sms);

@@ -21,7 +21,10 @@
 // stand-in for the device symbol.  Its device address is looked up once per device with
 // cudaGetSymbolAddress, on the first call made while that device is current; that first
 // call therefore has to happen before any stream capture that would record this entry
-// point.
+// point.  The address is kept per device index for the life of the process: the entry
+// point assumes the device's primary context throughout (after cudaDeviceReset the kept
+// address would be stale).  Indices are trusted (tets < num_nodes, seg_c < 10 num_tets),
+// as the header states; the kernels do not check them.
 #include <cuda_runtime.h>
 
 #include <mutex>
