@@ -175,6 +175,63 @@ def cpu_reference(meshes, budget_s, tol_rel, threads):
     return done, dt, sols
 
 
+def _oracle_batch_instance(job):
+    """One batch instance through the oracle (LDLT Newton, one thread): run in a spawned worker."""
+    seed, i, tol_rel = job
+    import oracle
+    from physim_gb300 import mesh as M
+    m = M.batch_instance(seed, i)
+    orc = oracle.Oracle(m)
+    x0 = orc.rest()
+    g0 = float(np.linalg.norm(orc.gradient(x0)))
+    t0 = time.perf_counter()
+    x, r = orc.solve_static(x0, tol_max_error=tol_rel * g0, tol_min_impr=0.0, tol_min_step=0.0, threads=1)
+    keep = {k: r[k] for k in ("result_name", "iterations", "bisections", "obj", "opt", "opt0")}
+    return i, x, keep, time.perf_counter() - t0
+
+
+def oracle_batch_parity(seed, sizes, tol_rel, gpu_x, gpu_reps, workers):
+    """Every batch instance solved by the oracle on the host cores (outside any timed region,
+    one single-threaded solve per worker process, largest first) and compared with the GPU's
+    result: relative displacement error where both succeed, and the outcome of each instance
+    that does not end SUCCESS on either side."""
+    import multiprocessing as mp
+    import oracle.build
+    oracle.build.build_oracle()  # built once here, not by every worker
+    order = sorted(range(len(sizes)), key=lambda i: -sizes[i])
+    t0 = time.perf_counter()
+    cpu = {}
+    with mp.get_context("spawn").Pool(workers) as pool:
+        for i, x, rep, secs in pool.imap_unordered(_oracle_batch_instance, [(seed, i, tol_rel) for i in order]):
+            cpu[i] = (x, rep, secs)
+    wall = time.perf_counter() - t0
+    errs, failures = [], []
+    for i in range(len(sizes)):
+        xr, rr, _ = cpu[i]
+        g = gpu_reps[i]
+        x0 = None
+        if rr["result_name"] == "SUCCESS" and g["result_name"] == "SUCCESS":
+            from physim_gb300 import mesh as M
+            x0 = M.batch_instance(seed, i).X0.ravel()
+            errs.append(float(np.linalg.norm(gpu_x[i] - xr) / max(np.linalg.norm(xr - x0), 1e-300)))
+        else:
+            failures.append({"instance": i, "tets": int(sizes[i]), "gpu": g["result_name"], "cpu": rr["result_name"],
+                             "gpu_rel_residual": g["opt"] / g["opt0"] if g["opt0"] > 0 else None,
+                             "cpu_rel_residual": rr["opt"] / rr["opt0"] if rr["opt0"] > 0 else None,
+                             "gpu_iterations": g["iterations"], "cpu_iterations": rr["iterations"]})
+    gpu_bad = [f for f in failures if f["gpu"] != "SUCCESS"]
+    agree = sum(f["cpu"] != "SUCCESS" for f in gpu_bad)
+    return {"compared": len(sizes), "success_both": len(errs),
+            "rel_displacement_err_max": max(errs) if errs else None,
+            "rel_displacement_err_median": statistics.median(errs) if errs else None,
+            "non_success_cpu_agree": f"{agree}/{len(gpu_bad)}",
+            "gpu_only_failures": [f["instance"] for f in failures if f["gpu"] != "SUCCESS" and f["cpu"] == "SUCCESS"],
+            "cpu_only_failures": [f["instance"] for f in failures if f["gpu"] == "SUCCESS" and f["cpu"] != "SUCCESS"],
+            "failures": failures,
+            "oracle": f"LDLT Newton (reference default linear solver), one thread per instance, {workers} "
+                      f"processes, {wall:.1f} s wall, {sum(v[2] for v in cpu.values()):.1f} s CPU"}
+
+
 # ---------------------------------------------------------------------------
 # workloads
 # ---------------------------------------------------------------------------
@@ -277,7 +334,10 @@ def run_batch(args, world, rank, dist):
     ms = dist_max(dist, ms)
     total = dist_sum(dist, float(count * args.steps))
     value = total / (ms / 1e3)
-    rel_res = [r["opt"] / r["opt0"] for r in reps if r["opt0"] > 0]
+    n_success = sum(r["result_name"] == "SUCCESS" for r in reps)
+    value_success = dist_sum(dist, float(n_success * args.steps)) / (ms / 1e3)
+    rel_res = [r["opt"] / r["opt0"] for r in reps if r["opt0"] > 0 and r["result_name"] == "SUCCESS"]
+    final_x = [it.positions() for it in insts]  # the last timed step's results, for the oracle comparison
     newton = [r["iterations"] for r in reps]
     pcg = [r["pcg_iterations"] for r in reps]
 
@@ -389,7 +449,10 @@ def run_batch(args, world, rank, dist):
         "kernels_ms": {k: round(v["ms"], 3) for k, v in prof.items()},
         "kernel_launches": {"k_engine": int(eng_launches), "k_pcg_cg": int(cl_launches), "cluster_steps": int(cl_steps)},
         "algorithmic_bytes": {k: v["bytes"] for k, v in prof.items()},
-        "accuracy": {"rel_residual_max": max(rel_res) if rel_res else None,
+        "value_success": round(value_success, 3),
+        "value_note": ("value counts every instance's solve; value_success only those that end SUCCESS (the "
+                       "others end as the oracle's LDLT Newton does on the same instance: accuracy.oracle_all)"),
+        "accuracy": {"rel_residual_max_success": max(rel_res) if rel_res else None,
                      "non_success": len(bad), "newton_median": statistics.median(newton),
                      "pcg_iters_median": statistics.median(pcg)},
         "clocks": clk, "gpu_launches": int(launches),
@@ -418,6 +481,7 @@ def run_batch(args, world, rank, dist):
         out["accuracy"]["compared"] = len(errs)
         out["accuracy"]["failed_on_both_cpu_and_gpu"] = int(both_failed)
     ctx.close()
+    out["_parity_inputs"] = (3 + 1000 * rank, [m.m for m in meshes], final_x, reps)
     return out
 
 
@@ -520,51 +584,58 @@ def serving_requests(count, seed, warm_frac=0.3):
     return reqs
 
 
-def serve_stream(px, ctx, reqs, insts, rate, opts, seed, budget_bytes, slots):
-    """Runs the served path live at `rate` req/s; returns per-request latencies (s) and wall time."""
+def serve_stream(px, ctx, reqs, rate, opts, seed, budget_bytes, slots):
+    """Runs the served path live at `rate` req/s (open-loop Poisson arrivals).  A cold request
+    hands its host mesh to the server, which builds the instance at admission (inside the
+    request's latency); a warm request re-solves the live instance of an earlier request
+    under its perturbed load, once that instance's earlier request has finished.  Returns
+    per-request latencies (s), the wall time, the arrivals, the reports and server stats."""
     rng = np.random.default_rng(seed + 17)
     n = len(reqs)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
     srv = px.Server(ctx, max_slots=slots, budget_bytes=budget_bytes, opts=opts)
-    owner = {}  # instance index -> request in flight
+    inst_of = {}  # cold request -> its instance
+    busy = set()  # instances (by cold request) with a request in flight
     lat = np.zeros(n)
     reps = [None] * n
     done = 0
     nxt = 0
-    waiting_warm = []
+    waiting = []
     t0 = time.perf_counter()
     while done < n:
         now = time.perf_counter() - t0
         while nxt < n and arrivals[nxt] <= now:
-            waiting_warm.append(nxt)
+            waiting.append(nxt)
             nxt += 1
         still = []
-        for r in waiting_warm:
+        for r in waiting:
             mesh, base = reqs[r]
-            key = base if base is not None else r
-            if key in owner:  # the instance is busy with an earlier request: wait for it
+            if base is None:
+                inst_of[r] = srv.submit_mesh(mesh, r)
+                busy.add(r)
+                continue
+            if base in busy or base not in inst_of:  # its instance is still busy: wait for it
                 still.append(r)
                 continue
-            inst = insts[key]
-            if base is not None:
-                inst.update_load(mesh.force, mesh.gravity)
-            else:
-                inst.reset()
-            owner[key] = r
-            srv.submit(inst, r)
-        waiting_warm = still
+            inst_of[base].update_load(mesh.force, mesh.gravity)
+            srv.submit(inst_of[base], r)
+            busy.add(base)
+        waiting = still
         active, queued = srv.progress()
         for tag, rep in srv.poll():
             lat[tag] = time.perf_counter() - t0 - arrivals[tag]
             reps[tag] = rep
-            key = reqs[tag][1] if reqs[tag][1] is not None else tag
-            owner.pop(key, None)
+            busy.discard(reqs[tag][1] if reqs[tag][1] is not None else tag)
             done += 1
-        if active == 0 and queued == 0 and not waiting_warm and nxt < n:
-            time.sleep(max(0.0, min(0.002, arrivals[nxt] - (time.perf_counter() - t0))))
+        if active == 0 and (queued > 0 or (not waiting and nxt < n)):
+            wait_to = arrivals[nxt] if (queued == 0 and nxt < n) else now + 5e-4
+            time.sleep(max(0.0, min(0.002, wait_to - (time.perf_counter() - t0))))
     wall = time.perf_counter() - t0
+    stats = srv.stats()
     srv.close()
-    return lat, wall, arrivals, reps
+    for inst in inst_of.values():
+        inst.close()
+    return lat, wall, arrivals, reps, stats
 
 
 def fifo_latency(arrivals, service):
@@ -578,60 +649,57 @@ def fifo_latency(arrivals, service):
     return lat, free
 
 
-def run_serve(args, world, rank, dist, rates=None, count=None, source="stream"):
-    """Open-loop Poisson serving.  source "stream": the 1:1:4 request mix with 30% warm
-    re-solves; source "batch": cold requests drawn from the uneven-box batch instances."""
+def run_serve(args, world, rank, dist, rates=None, count=None):
+    """Open-loop Poisson serving of the 1:1:4 request mix (1e3..2e5 tets, 30 % warm re-solves)
+    at each rate of the sweep: the served FP32+refine path with continuous batching and
+    admission by the memory budget, against the plain FP64 drop-in as a FIFO queue of one
+    solve call per request (a cold request's service time includes creating its instance)."""
     import physim_gb300 as px
-    from physim_gb300 import build, mesh as M
+    from physim_gb300 import build
     build.build()
     rates = rates or [float(r) for r in args.rates.split(",")]
     count = count or args.requests
-    if source == "batch":
-        reqs = [(M.batch_instance(3, i), None) for i in range(count)]
-    else:
-        reqs = serving_requests(count, seed=11)
-    ctx = px.Context(args.device, arena_bytes=int(args.arena_gb * (1 << 30)))
-    insts = {}
-    for i, (mesh, base) in enumerate(reqs):
-        if base is None:
-            insts[i] = px.Instance(ctx, mesh)
+    reqs = serving_requests(count, seed=11)
+    ctx = px.Context(args.device, arena_bytes=int(args.serve_arena_gb * (1 << 30)))
     served = served_options(px, args)
     plain = px.options(precision=px.PREC_FP64, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0,
                        tol_min_step=0.0, ls_num_max_iters=args.plain_pcg_max)
-    budget = int(min(150.0, 0.9 * args.arena_gb) * (1 << 30))
-    # plain drop-in service times: one FP64 solve call per request, in request order
+    budget = int(min(args.serve_budget_gb, 0.94 * args.serve_arena_gb) * (1 << 30))
+    # plain drop-in service times: one FP64 call per request, in request order
     svc = np.zeros(count)
     plain_reps = []
+    plain_inst = {}
     for i, (mesh, base) in enumerate(reqs):
-        key = base if base is not None else i
-        if base is not None:
-            insts[key].update_load(mesh.force, mesh.gravity)
-        else:
-            insts[key].reset()
         t0 = time.perf_counter()
-        _, r = insts[key].solve_static(plain)
+        if base is None:
+            plain_inst[i] = px.Instance(ctx, mesh)
+            key = i
+        else:
+            key = base
+            plain_inst[key].update_load(mesh.force, mesh.gravity)
+        _, r = plain_inst[key].solve_static(plain)
         svc[i] = time.perf_counter() - t0
         plain_reps.append(r["result_name"])
-    out = {"source": "uneven-box batch instances, cold" if source == "batch" else
-           "1:1:4 boxes, 1e3..2e5 tets, 30% warm re-solves",
-           "requests": count, "tets": [int(min(m.m for m, _ in reqs)), int(max(m.m for m, _ in reqs))],
+    for inst in plain_inst.values():
+        inst.close()
+    out = {"source": "1:1:4 boxes, 1e3..2e5 tets log-uniform, Neo-Hookean, gravity + face traction; "
+                     "30% warm re-solves of a live instance with its load perturbed by up to 10%",
+           "requests_per_rate": count, "tets": [int(min(m.m for m, _ in reqs)), int(max(m.m for m, _ in reqs))],
            "warm_fraction": round(sum(b is not None for _, b in reqs) / count, 3),
-           "budget_gb": round(budget / (1 << 30), 1), "slots": args.slots, "sweep": []}
+           "budget_gb": round(budget / (1 << 30), 1), "arena_gb": args.serve_arena_gb, "slots": args.slots,
+           "cold_requests": "instance built at admission (pattern on host workers, device set-up inside the latency)",
+           "sweep": []}
     served_res = []
     for rate in rates:
-        # every sweep point starts from rest; warm requests re-solve their base's equilibrium
-        for i, (mesh, base) in enumerate(reqs):
-            if base is None:
-                insts[i].update_load(mesh.force, mesh.gravity)
-                insts[i].reset()
-        lat, wall, arrivals, reps = serve_stream(px, ctx, reqs, insts, rate, served, 5, budget, args.slots)
+        lat, wall, arrivals, reps, st = serve_stream(px, ctx, reqs, rate, served, 5, budget, args.slots)
         served_res += [r["result_name"] for r in reps]
         flat, fwall = fifo_latency(arrivals, svc)
         out["sweep"].append({
             "rate": rate,
             "served": {"p50_ms": round(1e3 * percentile(list(lat), 50), 2),
                        "p99_ms": round(1e3 * percentile(list(lat), 99), 2),
-                       "solves_per_s": round(count / wall, 2)},
+                       "solves_per_s": round(count / wall, 2),
+                       "peak_gb": round(st["peak"] / (1 << 30), 2), "evictions": st["evictions"]},
             "plain_fifo": {"p50_ms": round(1e3 * percentile(list(flat), 50), 2),
                            "p99_ms": round(1e3 * percentile(list(flat), 99), 2),
                            "solves_per_s": round(count / fwall, 2)},
@@ -640,7 +708,7 @@ def run_serve(args, world, rank, dist, rates=None, count=None, source="stream"):
     out["plain_results"] = {k: plain_reps.count(k) for k in sorted(set(plain_reps))}
     out["plain_service_ms"] = {"median": round(1e3 * statistics.median(svc), 2), "sum": round(1e3 * svc.sum(), 1)}
     out["plain_fifo_note"] = ("plain latencies: exact FIFO queue over the same arrival times with the measured "
-                              "one-call FP64 service time of each request")
+                              "one-call FP64 service time of each request (cold: instance creation + solve)")
     ctx.close()
     return out
 
@@ -757,8 +825,8 @@ def main():
                     help="PCG iterations per Newton step of the plain FP64 path (the served path's budget is "
                          "served_sweeps x served_pcg_max = 4 x 3000)")
     ap.add_argument("--no-serve", action="store_true")
-    ap.add_argument("--batch-rate", type=float, default=200.0)
-    ap.add_argument("--batch-requests", type=int, default=64)
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0, help="serving admission budget (device bytes)")
+    ap.add_argument("--serve-arena-gb", type=float, default=160.0, help="device arena of the serving context")
     ap.add_argument("--count", type=int, default=512)
     ap.add_argument("--tol-rel", type=float, default=1e-6)
     ap.add_argument("--inner-tol", type=float, default=1e-4)
@@ -769,6 +837,8 @@ def main():
     ap.add_argument("--e2e-sample", action="store_true",
                     help="e2e on the first quarter of the instances instead of the whole workload")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-oracle-all", action="store_true",
+                    help="skip the comparison of every batch instance with the oracle (about a minute of host time)")
     ap.add_argument("--lsearch", default="simple", choices=sorted(LSEARCH),
                     help="line search of the GPU solves (LSearchType; the CPU baseline keeps Simple)")
     args = ap.parse_args()
@@ -789,10 +859,14 @@ def main():
         out = run_dynamics(args, world, rank, dist)
     else:
         out = run_batch(args, world, rank, dist)
+        seed, sizes, final_x, final_reps = out.pop("_parity_inputs")
         if not args.no_serve:
-            # p50/p99 latency beside solves/s: a bounded serving sample at one rate
-            out["serving"] = run_serve(args, world, rank, dist, rates=[args.batch_rate], count=args.batch_requests,
-                                       source="batch")
+            # p50/p99 latency beside solves/s: the serving stream's rate sweep
+            out["serving"] = run_serve(args, world, rank, dist)
+        if rank == 0 and not args.no_cpu and not args.no_oracle_all:
+            # every instance of the batch against the oracle, after all timed regions
+            out["accuracy"]["oracle_all"] = oracle_batch_parity(seed, sizes, args.tol_rel, final_x, final_reps,
+                                                                max(1, os.cpu_count() or 1))
     if rank == 0:
         print(json.dumps(out), flush=True)
 

@@ -218,14 +218,37 @@ int phx_batch_dynamic_step(phx_context ctx, int32_t count, phx_instance* insts, 
                            double dt, phx_report* reps);
 
 /* ---- serving: continuous batching over the same device engine ----------
- * Requests are admitted at Newton-iteration boundaries while the device is
- * busy with others, bounded by free slots and the memory budget. */
+ * No counterpart in the reference (its solver runs one object per call).  Requests are
+ * admitted at Newton-round boundaries while the device is busy with others, bounded by
+ * free slots and a device-memory budget; admitted requests are solved together in the
+ * engine's rounds, each instance with its own reduction order, so a result is the same
+ * alone and in the mix.  Instances the server creates for cold requests stay on the
+ * device while idle (mesh, pattern and last solution kept for warm re-solves) and count
+ * against the budget; when a request does not fit, idle ones are evicted, least recently
+ * used first (positions and velocities kept on the host; the instance is rebuilt on its
+ * next request).  A request larger than the whole budget is refused with PHX_ENOMEM: at
+ * submission for a caller's instance, through its report (status PHX_ENOMEM, result
+ * FAILURE) for a cold request, whose size is known once its pattern is built. */
 typedef struct phx_server_s* phx_server;
 int phx_server_create(phx_context ctx, int32_t max_slots, int64_t budget_bytes, const phx_options* opts,
                       phx_server* out);
+/* Instances created by phx_server_submit_mesh stay valid (the caller destroys them); one
+ * that is off the device then keeps only its host state. */
 int phx_server_destroy(phx_server srv);
-/* Queue a static solve of inst (from its current positions); tag is returned by poll. */
+/* Queue a static solve of inst from its current positions (a warm re-solve when it holds a
+ * previous solution, e.g. after phx_instance_update_load); tag is returned by poll. */
 int phx_server_submit(phx_server srv, phx_instance inst, int64_t tag);
+/* Queue one implicit-Euler step of inst (OptimProblem_BasicDynamic), time step dt. */
+int phx_server_submit_step(phx_server srv, phx_instance inst, double dt, int64_t tag);
+/* A cold request: the server copies the mesh, builds its pattern and scatter map on host
+ * worker threads, and creates the instance on the device when the request is admitted;
+ * then a static solve from rest.  *out is the new instance (for warm re-solves and for
+ * reading the result; the caller destroys it).  Until admitted, and after an eviction, calls
+ * that need its device part return PHX_EBUSY; its positions and velocities stay readable. */
+int phx_server_submit_mesh(phx_server srv, const phx_mesh* mesh, int64_t tag, phx_instance* out);
+/* Device bytes the server holds now and at most so far, instances it created that are on
+ * the device, and evictions so far; any pointer may be NULL. */
+int phx_server_stats(phx_server srv, int64_t* in_use, int64_t* peak, int64_t* resident, int64_t* evictions);
 /* Advance the device by one round; admits queued requests first. */
 int phx_server_progress(phx_server srv, int32_t* active, int32_t* queued);
 /* Pop up to cap finished requests: tags, reports. Returns the number popped (>= 0) or an error. */

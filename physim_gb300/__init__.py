@@ -32,7 +32,8 @@ EXPORTS = [
     "phx_instance_get_velocities", "phx_instance_update_load", "phx_energy_gradient", "phx_hessian",
     "phx_hessian_pattern", "phx_scatter_map", "phx_element_local", "phx_solve_static", "phx_solve_step", "phx_solve_log",
     "phx_dynamic_step", "phx_batch_solve", "phx_batch_dynamic_step", "phx_server_create", "phx_server_destroy",
-    "phx_server_submit", "phx_server_progress", "phx_server_poll", "phx_profile_enable", "phx_profile_read",
+    "phx_server_submit", "phx_server_submit_step", "phx_server_submit_mesh", "phx_server_stats",
+    "phx_server_progress", "phx_server_poll", "phx_profile_enable", "phx_profile_read",
     "phx_profile_reset", "phx_profile_bytes", "phx_kernel_launches", "phx_timer_mark", "phx_timer_elapsed",
     "phx_hessian_blocks_noalloc", "phx_debug_unmet_barrier",
 ]
@@ -121,6 +122,9 @@ def lib():
         "phx_server_create": ([vp, i32, i64, C.POINTER(Options), C.POINTER(vp)], C.c_int),
         "phx_server_destroy": ([vp], C.c_int),
         "phx_server_submit": ([vp, vp, i64], C.c_int),
+        "phx_server_submit_step": ([vp, vp, dbl, i64], C.c_int),
+        "phx_server_submit_mesh": ([vp, C.POINTER(Mesh_), i64, C.POINTER(vp)], C.c_int),
+        "phx_server_stats": ([vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)], C.c_int),
         "phx_server_progress": ([vp, C.POINTER(i32), C.POINTER(i32)], C.c_int),
         "phx_server_poll": ([vp, vp, vp, i32], C.c_int),
         "phx_profile_enable": ([vp, i32], C.c_int),
@@ -426,7 +430,26 @@ class Server:
             pass
 
     def submit(self, inst: Instance, tag: int):
+        """A static solve of a live instance from its current positions (warm re-solve)."""
         _check(lib().phx_server_submit(self.h, inst.h, int(tag)))
+
+    def submit_step(self, inst: Instance, dt: float, tag: int):
+        """One implicit-Euler step of a live instance."""
+        _check(lib().phx_server_submit_step(self.h, inst.h, float(dt), int(tag)))
+
+    def submit_mesh(self, m, tag: int) -> Instance:
+        """A cold request: the server builds the instance of mesh m at admission, then solves it
+        from rest.  Returns the instance (destroy it when done with it)."""
+        d, keep = _mesh_desc(m)
+        h = C.c_void_p()
+        _check(lib().phx_server_submit_mesh(self.h, C.byref(d), int(tag), C.byref(h)))
+        del keep  # the server copied the mesh
+        return Instance(self.ctx, m, _handle=h)
+
+    def stats(self):
+        a, b, c, d = (C.c_int64() for _ in range(4))
+        _check(lib().phx_server_stats(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
+        return {"in_use": a.value, "peak": b.value, "resident": c.value, "evictions": d.value}
 
     def progress(self):
         a = C.c_int32(); q = C.c_int32()

@@ -11,6 +11,9 @@
 
 #include <algorithm>
 #include <atomic>
+#include <condition_variable>
+#include <memory>
+#include <mutex>
 #include <new>
 #include <system_error>
 #include <thread>
@@ -29,6 +32,7 @@
 #include "kernels.h"
 #include "newton_control.h"
 #include "pattern.h"
+#include "serve_admission.h"
 
 using namespace phx;
 
@@ -164,6 +168,35 @@ struct phx_context_s {
   int unmet_tag = 0;                     // test hook: grid barrier that waits for an arrival never made
 };
 
+// A server's own copy of a cold request's mesh: the instance is built from it at admission
+// and rebuilt from it after an eviction.
+struct KeptMesh {
+  int32_t n = 0, m = 0;
+  std::vector<double> X0, lame, rho, force, soft_k, soft_target;
+  std::vector<int32_t> T;
+  std::vector<uint8_t> model, fixed;
+  double gravity[3] = {0, 0, 0};
+  phx_mesh view() const {
+    phx_mesh v{};
+    v.num_nodes = n;
+    v.num_tets = m;
+    v.X0 = X0.data();
+    v.tets = T.data();
+    v.lame = lame.data();
+    v.rho = rho.data();
+    v.model = model.empty() ? nullptr : model.data();
+    v.fixed = fixed.empty() ? nullptr : fixed.data();
+    v.force = force.empty() ? nullptr : force.data();
+    for (int c = 0; c < 3; ++c) v.gravity[c] = gravity[c];
+    v.soft_k = soft_k.empty() ? nullptr : soft_k.data();
+    v.soft_target = soft_target.empty() ? nullptr : soft_target.data();
+    return v;
+  }
+};
+
+// Host part of a server instance: not built, being built on a worker, ready, or failed.
+enum HostState : int { HOST_NONE = 0, HOST_BUILDING = 1, HOST_READY = 2, HOST_FAILED = 3 };
+
 struct phx_instance_s {
   phx_context ctx = nullptr;
   HostPattern hp;
@@ -176,9 +209,30 @@ struct phx_instance_s {
   bool in_server = false;
   double gravity[3] = {0, 0, 0};
   std::vector<double> force;
+  // instances a server created for cold requests (phx_server_submit_mesh): its budget holds
+  // their device memory while they are resident, idle ones included
+  phx_server owner = nullptr;
+  std::unique_ptr<KeptMesh> kept;
+  bool resident = true;                    // the device part exists
+  std::atomic<int> host_state{HOST_READY};
+  std::string host_err;
+  std::vector<double> saved_x, saved_v;    // positions and velocities kept on the host by an eviction
+  uint64_t last_used = 0;                  // server tick of the last request (eviction order)
 };
 
+// Drops a server-created instance from its server's bookkeeping (defined with the server).
+void server_forget(phx_server s, phx_instance inst);
+
 namespace {
+
+// Calls that need the instance's device part: refused while a server has evicted it (or has
+// not yet admitted it); the server re-creates it on the instance's next request.
+int require_resident(phx_instance inst) {
+  if (!inst->resident)
+    return set_err(PHX_EBUSY, "instance is not on the device (evicted by its server, or not yet admitted): "
+                              "submit it to its server again");
+  return PHX_OK;
+}
 
 template <typename T>
 int arena_alloc(phx_instance inst, T** out, size_t count, bool zero = false) {
@@ -209,7 +263,37 @@ int upload(phx_instance inst, T** out, const std::vector<T>& v) {
     if (rc_) return rc_;  \
   } while (0)
 
+// Device bytes of the arena blocks of `count` elements of `elem` bytes (256-byte granules).
+int64_t arena_bytes_of(size_t count, size_t elem) {
+  return (int64_t)(((std::max<size_t>(count, 1) * elem) + 255) & ~(size_t)255);
+}
+
+// Bytes ensure_precision allocates for one arithmetic (element size s).
+int64_t precision_bytes(int64_t n, int64_t m, int64_t nslots, size_t s) {
+  const size_t n4 = 4 * (size_t)n;
+  return arena_bytes_of(90 * (size_t)m, s) + arena_bytes_of(9 * (size_t)nslots, s) + 6 * arena_bytes_of(n4, s) +
+         arena_bytes_of(9 * (size_t)n, s);
+}
+
+int ensure_precision_impl(phx_instance inst, bool fp64);
+
+// Allocates the Hessian, PCG and preconditioner buffers of one arithmetic; on failure the
+// blocks allocated by this call are released again.
 int ensure_precision(phx_instance inst, bool fp64) {
+  const size_t nblk = inst->blocks.size();
+  const int64_t b0 = inst->bytes;
+  const InstDev keep = inst->dev;
+  const int rc = ensure_precision_impl(inst, fp64);
+  if (rc != PHX_OK) {
+    for (size_t k = nblk; k < inst->blocks.size(); ++k) inst->ctx->arena.free(inst->blocks[k]);
+    inst->blocks.resize(nblk);
+    inst->bytes = b0;
+    inst->dev = keep;
+  }
+  return rc;
+}
+
+int ensure_precision_impl(phx_instance inst, bool fp64) {
   InstDev& D = inst->dev;
   const size_t n4 = 4 * (size_t)D.n, m = D.m;
   if (fp64 && !inst->have64) {
@@ -786,6 +870,7 @@ int phx_context_memory(phx_context ctx, int64_t* used, int64_t* cap) {
 int phx_instance_destroy(phx_instance inst) {
   if (!inst) return PHX_OK;
   if (inst->in_server) return set_err(PHX_EBUSY, "instance is admitted to a server");
+  if (inst->owner) server_forget(inst->owner, inst);  // its bytes leave the server's budget
   cudaStreamSynchronize(inst->ctx->stream);
   for (void* p : inst->blocks) inst->ctx->arena.free(p);
   delete inst;
@@ -816,13 +901,57 @@ bool instance_build_host(const phx_mesh* mesh, phx_instance_s* inst, std::string
   return true;
 }
 
+// Device bytes instance_setup_device allocates for a built host part, plus the buffers of
+// the arithmetic(s) asked for (the serving admission's estimate; equal to the instance's
+// bytes after the set-up, which a GPU test checks).
+int64_t device_bytes(const HostPattern& hp, bool fp32, bool fp64) {
+  const size_t n = hp.n, m = hp.m, n4 = 4 * n;
+  int64_t b = arena_bytes_of(hp.tets.size(), 4) + arena_bytes_of(hp.rest64.size(), 8) +
+              arena_bytes_of(hp.rest32.size(), 4) + arena_bytes_of(hp.model.size(), 1) +
+              arena_bytes_of(hp.chunk_off.size(), 4) + arena_bytes_of(hp.slot_col.size(), 4) +
+              arena_bytes_of(hp.diag_slot.size(), 4) + arena_bytes_of(hp.lo_rc.size(), 4) +
+              arena_bytes_of(hp.lo_slot.size(), 4) + arena_bytes_of(hp.up_slot.size(), 4) +
+              arena_bytes_of(hp.seg_ptr.size(), 4) + arena_bytes_of(hp.seg_c.size(), 4) +
+              arena_bytes_of(hp.nseg_ptr.size(), 4) + arena_bytes_of(hp.nseg_c.size(), 4) +
+              arena_bytes_of(hp.fixmask.size(), 1) + arena_bytes_of(hp.mass.size(), 8) +
+              arena_bytes_of(hp.hlin.size(), 8) + (hp.soft.empty() ? 0 : arena_bytes_of(hp.soft.size(), 8));
+  b += 13 * arena_bytes_of(n4, 8);  // rest positions and the twelve FP64 node vectors
+  const size_t maxt = std::max({tiles(hp.m), hp.nchunks, tiles(hp.nlo)});
+  b += arena_bytes_of(m, 8) + arena_bytes_of(12 * m, 8) + arena_bytes_of(maxt * kPartials, 8) + arena_bytes_of(1, 4) +
+       arena_bytes_of(4 * (size_t)kLogCap, 8) + arena_bytes_of(1, sizeof(NState)) + arena_bytes_of(1, sizeof(DevOpts));
+  if (fp32) b += precision_bytes(hp.n, hp.m, hp.nslots, 4);
+  if (fp64) b += precision_bytes(hp.n, hp.m, hp.nslots, 8);
+  return b;
+}
+
+// Releases an instance's device part (arena blocks) and keeps its host part.
+int instance_free_device(phx_instance inst) {
+  cudaError_t e = cudaStreamSynchronize(inst->ctx->stream);
+  for (void* p : inst->blocks) inst->ctx->arena.free(p);
+  inst->blocks.clear();
+  inst->dev = InstDev{};
+  inst->d_st = nullptr;
+  inst->d_opts = nullptr;
+  inst->have32 = inst->have64 = false;
+  inst->bytes = 0;
+  inst->resident = false;
+  if (e != cudaSuccess) return set_err(PHX_ECUDA, cudaGetErrorString(e));
+  return PHX_OK;
+}
+
 // Device part: arena allocations and uploads on the context stream (the caller
-// synchronises).  On failure the instance is destroyed.
-int instance_setup_device(phx_context ctx, const phx_mesh* mesh, phx_instance_s* inst) {
+// synchronises).  On failure the instance is destroyed, or with keep_on_fail only its
+// device part is released.
+int instance_setup_device(phx_context ctx, const phx_mesh* mesh, phx_instance_s* inst, bool keep_on_fail = false) {
   HostPattern& hp = inst->hp;
   InstDev& D = inst->dev;
   D.n = hp.n; D.m = hp.m; D.nlo = hp.nlo; D.nchunks = hp.nchunks; D.nslots = hp.nslots;
-  auto fail = [&](int rc) { phx_instance_destroy(inst); return rc; };
+  inst->resident = true;
+  auto fail = [&](int rc) {
+    if (keep_on_fail) instance_free_device(inst);
+    else phx_instance_destroy(inst);
+    return rc;
+  };
   cudaError_t e0 = cudaSuccess;
   int rc = PHX_OK;
   const size_t n4 = 4 * (size_t)hp.n;
@@ -964,16 +1093,20 @@ int phx_instances_create(phx_context ctx, int32_t count, const phx_mesh* meshes,
 
 int phx_instance_sizes(phx_instance inst, int64_t* ndof, int64_t* nnz, int64_t* nlo, int64_t* nfull) {
   if (!inst) return set_err(PHX_EINVAL, "inst is NULL");
-  if (ndof) *ndof = 3 * (int64_t)inst->dev.n;
-  if (nnz) *nnz = 9 * (int64_t)inst->dev.nlo;
-  if (nlo) *nlo = inst->dev.nlo;
-  if (nfull) *nfull = 2 * (int64_t)inst->dev.nlo - inst->dev.n;
+  if (inst->host_state.load(std::memory_order_acquire) != HOST_READY && !inst->resident)
+    return set_err(PHX_EBUSY, "instance's pattern is not built yet");
+  const HostPattern& hp = inst->hp;
+  if (ndof) *ndof = 3 * (int64_t)hp.n;
+  if (nnz) *nnz = 9 * (int64_t)hp.nlo;
+  if (nlo) *nlo = hp.nlo;
+  if (nfull) *nfull = 2 * (int64_t)hp.nlo - hp.n;
   return PHX_OK;
 }
 
 int phx_instance_reset(phx_instance inst) {
   if (!inst) return set_err(PHX_EINVAL, "inst is NULL");
   if (inst->in_server) return set_err(PHX_EBUSY, "instance is admitted to a server");
+  TRY(require_resident(inst));
   const size_t bytes = 4 * (size_t)inst->dev.n * sizeof(double);
   cudaStream_t st = inst->ctx->stream;
   CU(cudaMemcpyAsync(inst->dev.x, inst->dev.xrest, bytes, cudaMemcpyDeviceToDevice, st));
@@ -984,18 +1117,34 @@ int phx_instance_reset(phx_instance inst) {
 
 int phx_instance_set_positions(phx_instance inst, const double* x) {
   if (!inst || !x) return set_err(PHX_EINVAL, "NULL argument");
+  TRY(require_resident(inst));
   return upload_x(inst, x, inst->dev.x);
 }
+// An instance off the device reports the state its server kept on the host (its rest
+// shape and zero velocity if it was never admitted).
 int phx_instance_get_positions(phx_instance inst, double* x) {
   if (!inst || !x) return set_err(PHX_EINVAL, "NULL argument");
+  if (!inst->resident) {
+    if (!inst->saved_x.empty()) std::copy(inst->saved_x.begin(), inst->saved_x.end(), x);
+    else if (inst->kept) std::copy(inst->kept->X0.begin(), inst->kept->X0.end(), x);
+    else return require_resident(inst);
+    return PHX_OK;
+  }
   return download_x(inst, inst->dev.x, x);
 }
 int phx_instance_set_velocities(phx_instance inst, const double* v) {
   if (!inst || !v) return set_err(PHX_EINVAL, "NULL argument");
+  TRY(require_resident(inst));
   return upload_x(inst, v, inst->dev.v);
 }
 int phx_instance_get_velocities(phx_instance inst, double* v) {
   if (!inst || !v) return set_err(PHX_EINVAL, "NULL argument");
+  if (!inst->resident) {
+    if (!inst->saved_v.empty()) std::copy(inst->saved_v.begin(), inst->saved_v.end(), v);
+    else if (inst->kept) std::fill(v, v + 3 * (size_t)inst->kept->n, 0.0);
+    else return require_resident(inst);
+    return PHX_OK;
+  }
   return download_x(inst, inst->dev.v, v);
 }
 
@@ -1003,6 +1152,15 @@ int phx_instance_update_load(phx_instance inst, const double* force, const doubl
   if (!inst) return set_err(PHX_EINVAL, "inst is NULL");
   if (inst->in_server) return set_err(PHX_EBUSY, "instance is admitted to a server");
   HostPattern& hp = inst->hp;
+  if (inst->kept) {  // a server instance is (re)built from its kept mesh: keep its loads there too
+    if (force) inst->kept->force.assign(force, force + 3 * (size_t)inst->kept->n);
+    if (gravity) for (int c = 0; c < 3; ++c) inst->kept->gravity[c] = gravity[c];
+  }
+  if (!inst->resident) {  // applied when the server builds the instance again
+    if (force) inst->force.assign(force, force + 3 * (size_t)inst->kept->n);
+    if (gravity) for (int c = 0; c < 3; ++c) inst->gravity[c] = gravity[c];
+    return PHX_OK;
+  }
   if (force) inst->force.assign(force, force + 3 * (size_t)hp.n);
   if (gravity) for (int c = 0; c < 3; ++c) inst->gravity[c] = gravity[c];
   MeshIn in;
@@ -1018,6 +1176,7 @@ int phx_instance_update_load(phx_instance inst, const double* force, const doubl
 
 int phx_solve_log(phx_instance inst, double* obj, double* opt, int32_t* bis, double* step, int32_t cap) {
   if (!inst) return set_err(PHX_EINVAL, "inst is NULL");
+  TRY(require_resident(inst));
   NState s;
   TRY(read_state(inst, &s));
   std::vector<double> lg(4 * (size_t)kLogCap);
@@ -1034,6 +1193,8 @@ int phx_solve_log(phx_instance inst, double* obj, double* opt, int32_t* bis, dou
 
 int phx_hessian_pattern(phx_instance inst, int32_t* colptr, int32_t* rowidx) {
   if (!inst || !colptr || !rowidx) return set_err(PHX_EINVAL, "NULL argument");
+  if (inst->host_state.load(std::memory_order_acquire) != HOST_READY && !inst->resident)
+    return set_err(PHX_EBUSY, "instance's pattern is not built yet");
   const HostPattern& hp = inst->hp;
   int64_t q = 0;
   for (int C = 0; C < hp.n; ++C)
@@ -1050,6 +1211,8 @@ int phx_hessian_pattern(phx_instance inst, int32_t* colptr, int32_t* rowidx) {
 
 int phx_scatter_map(phx_instance inst, int32_t* map) {
   if (!inst || !map) return set_err(PHX_EINVAL, "NULL argument");
+  if (inst->host_state.load(std::memory_order_acquire) != HOST_READY && !inst->resident)
+    return set_err(PHX_EBUSY, "instance's pattern is not built yet");
   std::copy(inst->hp.scatter.begin(), inst->hp.scatter.end(), map);
   return PHX_OK;
 }
@@ -1105,6 +1268,7 @@ extern "C" {
 
 int phx_energy_gradient(phx_instance inst, const double* x, double* energy, double* gradient, int32_t fix) {
   if (!inst) return set_err(PHX_EINVAL, "inst is NULL");
+  TRY(require_resident(inst));
   NState s;
   TRY(eval_eg(inst, x, fix ? 0 : 1, &s));
   if (energy) *energy = s.E_eval;
@@ -1115,6 +1279,7 @@ int phx_energy_gradient(phx_instance inst, const double* x, double* energy, doub
 int phx_hessian(phx_instance inst, const double* x, int32_t precision, double* values, int32_t fix) {
   if (!inst || !values) return set_err(PHX_EINVAL, "NULL argument");
   if (precision != PHX_PREC_FP64 && precision != PHX_PREC_FP32_REFINE) return set_err(PHX_EINVAL, "precision");
+  TRY(require_resident(inst));
   const bool fp64 = precision == PHX_PREC_FP64;
   TRY(eval_hess(inst, x, fp64, fix ? 0 : 1));
   const HostPattern& hp = inst->hp;
@@ -1143,6 +1308,7 @@ int phx_hessian(phx_instance inst, const double* x, int32_t precision, double* v
 int phx_element_local(phx_instance inst, const double* x, int32_t precision, double* E, double* g, double* Hout) {
   if (!inst) return set_err(PHX_EINVAL, "inst is NULL");
   if (precision != PHX_PREC_FP64 && precision != PHX_PREC_FP32_REFINE) return set_err(PHX_EINVAL, "precision");
+  TRY(require_resident(inst));
   const int m = inst->dev.m;
   NState s;
   TRY(eval_eg(inst, x, 0, &s));
@@ -1183,6 +1349,7 @@ int phx_element_local(phx_instance inst, const double* x, int32_t precision, dou
 int phx_solve_static(phx_instance inst, const phx_options* o, double* x, phx_report* rep) {
   if (!inst) return set_err(PHX_EINVAL, "inst is NULL");
   if (inst->in_server) return set_err(PHX_EBUSY, "instance is admitted to a server");
+  TRY(require_resident(inst));
   auto t0 = clk::now();
   if (x) TRY(upload_x(inst, x, inst->dev.x));
   TRY(start_solve(inst, o, false, 0.0, 0));
@@ -1204,6 +1371,7 @@ int phx_solve_static(phx_instance inst, const phx_options* o, double* x, phx_rep
 int phx_solve_step(phx_instance inst, const phx_options* o, double* x, phx_report* rep) {
   if (!inst) return set_err(PHX_EINVAL, "inst is NULL");
   if (inst->in_server) return set_err(PHX_EBUSY, "instance is admitted to a server");
+  TRY(require_resident(inst));
   auto t0 = clk::now();
   if (x) TRY(upload_x(inst, x, inst->dev.x));
   TRY(start_solve(inst, o, false, 0.0, 1));
@@ -1219,6 +1387,7 @@ int phx_dynamic_step(phx_instance inst, const phx_options* o, double dt, double*
   if (!inst) return set_err(PHX_EINVAL, "inst is NULL");
   if (!(dt > 0)) return set_err(PHX_EINVAL, "dt must be positive");
   if (inst->in_server) return set_err(PHX_EBUSY, "instance is admitted to a server");
+  TRY(require_resident(inst));
   auto t0 = clk::now();
   if (x) TRY(upload_x(inst, x, inst->dev.x));
   if (v) TRY(upload_x(inst, v, inst->dev.v));
@@ -1240,6 +1409,7 @@ int phx_batch_solve(phx_context ctx, int32_t count, phx_instance* insts, const p
   for (int i = 0; i < count; ++i) {
     if (!list[i] || list[i]->ctx != ctx) return set_err(PHX_EINVAL, "instance from another context");
     if (list[i]->in_server) return set_err(PHX_EBUSY, "instance is admitted to a server");
+    TRY(require_resident(list[i]));
     for (int j = 0; j < i; ++j)
       if (list[j] == list[i]) return set_err(PHX_EINVAL, "instance listed twice");
     if (x && x[i]) TRY(upload_x(list[i], x[i], list[i]->dev.x));
@@ -1278,6 +1448,7 @@ int phx_batch_dynamic_step(phx_context ctx, int32_t count, phx_instance* insts, 
   for (int i = 0; i < count; ++i) {
     if (!list[i] || list[i]->ctx != ctx) return set_err(PHX_EINVAL, "instance from another context");
     if (list[i]->in_server) return set_err(PHX_EBUSY, "instance is admitted to a server");
+    TRY(require_resident(list[i]));
     for (int j = 0; j < i; ++j)
       if (list[j] == list[i]) return set_err(PHX_EINVAL, "instance listed twice");
     TRY(start_solve(list[i], o, true, dt, 0));
@@ -1301,10 +1472,19 @@ int phx_batch_dynamic_step(phx_context ctx, int32_t count, phx_instance* insts, 
 struct phx_server_s {
   phx_context ctx = nullptr;
   int max_slots = 0;
-  int64_t budget = 0, in_use = 0;
+  int64_t budget = 0, in_use = 0, peak = 0;  // device bytes this server holds
+  int64_t evictions = 0, cold_admitted = 0, refused = 0;
   phx_options opts{};
   bool fp64 = true;
-  struct Req { phx_instance inst; int64_t tag; clk::time_point t_submit; };
+  enum Kind { REQ_STATIC = 0, REQ_STEP = 1 };
+  struct Req {
+    phx_instance inst;
+    int64_t tag;
+    clk::time_point t_submit;
+    int kind;
+    double dt;
+    int64_t counted;  // bytes added to in_use for a caller's instance while it is active
+  };
   std::deque<Req> queue;
   std::vector<Req> active;
   struct Done { int64_t tag; phx_report rep; };
@@ -1313,14 +1493,134 @@ struct phx_server_s {
   BatchDev B{};
   Grids G;
   int ccount = 0;
+  uint64_t tick = 0;
+  std::vector<phx_instance> owned;  // instances this server created for cold requests
+  // host parts of cold requests (validation, pattern, scatter map) are built on workers
+  std::mutex mu;
+  std::condition_variable cv;
+  std::deque<phx_instance> jobs;
+  bool stop = false;
+  std::vector<std::thread> workers;
 };
+
+void server_forget(phx_server s, phx_instance inst) {
+  auto it = std::find(s->owned.begin(), s->owned.end(), inst);
+  if (it == s->owned.end()) return;
+  if (inst->resident) s->in_use -= inst->bytes;
+  s->owned.erase(it);
+  inst->owner = nullptr;
+}
+
+namespace {
+
+void server_worker(phx_server s) {
+  for (;;) {
+    phx_instance inst = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      s->cv.wait(lk, [&] { return s->stop || !s->jobs.empty(); });
+      if (s->stop) return;
+      inst = s->jobs.front();
+      s->jobs.pop_front();
+    }
+    std::string err;
+    bool ok = false;
+    try {
+      inst->hp = HostPattern{};
+      const phx_mesh v = inst->kept->view();
+      ok = instance_build_host(&v, inst, err);
+    } catch (const std::bad_alloc&) {
+      err = "out of host memory building the pattern";
+    } catch (...) {
+      err = "unexpected error building the pattern";
+    }
+    inst->host_err = err;
+    inst->host_state.store(ok ? HOST_READY : HOST_FAILED, std::memory_order_release);
+  }
+}
+
+// Queues the (re)build of a server instance's host part on the workers.
+int server_build_host(phx_server s, phx_instance inst) {
+  if (inst->host_state.load(std::memory_order_acquire) != HOST_NONE) return PHX_OK;
+  inst->host_state.store(HOST_BUILDING, std::memory_order_release);
+  try {
+    if (s->workers.empty()) {
+      const int nt = std::max(1, std::min(8, (int)std::thread::hardware_concurrency()));
+      for (int t = 0; t < nt; ++t) s->workers.emplace_back(server_worker, s);
+    }
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->jobs.push_back(inst);
+  } catch (...) {
+    inst->host_state.store(HOST_NONE, std::memory_order_release);
+    if (s->workers.empty()) return set_err(PHX_ENOMEM, "cannot start a host-build thread");
+    return set_err(PHX_ENOMEM, "out of host memory queueing a request");
+  }
+  s->cv.notify_one();
+  return PHX_OK;
+}
+
+// Moves an idle instance of the server off the device: its positions and velocities stay on
+// the host, its arena blocks are freed and its host part is rebuilt on its next request.
+int server_evict(phx_server s, phx_instance inst) {
+  const size_t N = 3 * (size_t)inst->dev.n;
+  inst->saved_x.resize(N);
+  inst->saved_v.resize(N);
+  TRY(download_x(inst, inst->dev.x, inst->saved_x.data()));
+  TRY(download_x(inst, inst->dev.v, inst->saved_v.data()));
+  s->in_use -= inst->bytes;
+  TRY(instance_free_device(inst));
+  inst->host_state.store(HOST_NONE, std::memory_order_release);
+  s->evictions++;
+  return PHX_OK;
+}
+
+// Puts a finished request on the done list with a failure report (no solve ran).
+void server_fail(phx_server s, const phx_server_s::Req& r, int status) {
+  phx_report rep{};
+  rep.result = OS_FAILURE;
+  rep.status = status;
+  rep.seconds = std::chrono::duration<double>(clk::now() - r.t_submit).count();
+  s->done.push_back({r.tag, rep});
+  r.inst->in_server = false;
+  s->refused++;
+}
+
+// Device part of an admitted request: the instance set up on the device if it is not, with
+// the buffers of the server's arithmetic.  Returns PHX_ENOMEM (nothing kept) when the arena
+// cannot hold it.
+int server_allocate(phx_server s, phx_instance inst) {
+  const bool fresh = !inst->resident;
+  if (fresh) {
+    const phx_mesh v = inst->kept->view();
+    TRY(instance_setup_device(s->ctx, &v, inst, true));  // on failure the host part is intact
+  }
+  const int rc = ensure_precision(inst, s->fp64);
+  if (rc != PHX_OK) {
+    if (fresh) {  // no room for its arithmetic: leave nothing behind; the set-up released the
+      instance_free_device(inst);  // pattern's host copies, so it is built again
+      inst->host_state.store(HOST_NONE, std::memory_order_release);
+    }
+    return rc;
+  }
+  if (fresh) {
+    if (!inst->saved_x.empty()) TRY(upload_x(inst, inst->saved_x.data(), inst->dev.x));
+    if (!inst->saved_v.empty()) TRY(upload_x(inst, inst->saved_v.data(), inst->dev.v));
+    inst->saved_x.clear();
+    inst->saved_v.clear();
+    s->cold_admitted++;
+  }
+  return PHX_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
 int phx_server_create(phx_context ctx, int32_t max_slots, int64_t budget, const phx_options* o, phx_server* out) {
   if (!ctx || !out || max_slots < 1) return set_err(PHX_EINVAL, "bad arguments");
   TRY(validate_opts(o));
-  auto* s = new phx_server_s();
+  auto* s = new (std::nothrow) phx_server_s();
+  if (!s) return set_err(PHX_ENOMEM, "out of host memory");
   s->ctx = ctx;
   s->max_slots = max_slots;
   s->budget = budget > 0 ? budget : (int64_t)ctx->arena.cap;
@@ -1332,19 +1632,112 @@ int phx_server_create(phx_context ctx, int32_t max_slots, int64_t budget, const 
 
 int phx_server_destroy(phx_server s) {
   if (!s) return PHX_OK;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+  }
+  s->cv.notify_all();
+  for (auto& t : s->workers) t.join();
+  for (phx_instance inst : s->jobs)  // queued builds that never ran
+    inst->host_state.store(HOST_NONE, std::memory_order_release);
   cudaStreamSynchronize(s->ctx->stream);
   for (auto& r : s->active) r.inst->in_server = false;
   for (auto& r : s->queue) r.inst->in_server = false;
+  for (phx_instance inst : s->owned) inst->owner = nullptr;  // the caller keeps (and destroys) them
   delete s;
   return PHX_OK;
 }
 
-int phx_server_submit(phx_server s, phx_instance inst, int64_t tag) {
+namespace {
+
+int server_enqueue(phx_server s, phx_instance inst, int64_t tag, int kind, double dt) {
   if (!s || !inst || inst->ctx != s->ctx) return set_err(PHX_EINVAL, "bad arguments");
   if (inst->in_server) return set_err(PHX_EBUSY, "instance already queued or active");
-  if (inst->bytes > s->budget) return set_err(PHX_ENOMEM, "instance larger than the server budget");
+  if (inst->owner && inst->owner != s) return set_err(PHX_EINVAL, "instance belongs to another server");
+  if (!inst->resident && !inst->owner) return set_err(PHX_EINVAL, "instance has no device part and no server");
+  if (inst->resident && !inst->owner) {
+    // a caller's instance: its bytes count while it is active
+    const int64_t need = inst->bytes + (s->fp64 ? (inst->have64 ? 0 : precision_bytes(inst->dev.n, inst->dev.m,
+                                                                                      inst->dev.nslots, 8))
+                                                : (inst->have32 ? 0 : precision_bytes(inst->dev.n, inst->dev.m,
+                                                                                      inst->dev.nslots, 4)));
+    if (need > s->budget) {
+      s->refused++;
+      return set_err(PHX_ENOMEM, "instance larger than the server budget");
+    }
+  }
+  if (!inst->resident) TRY(server_build_host(s, inst));
   inst->in_server = true;
-  s->queue.push_back({inst, tag, clk::now()});
+  s->queue.push_back({inst, tag, clk::now(), kind, dt, 0});
+  return PHX_OK;
+}
+
+}  // namespace
+
+int phx_server_submit(phx_server s, phx_instance inst, int64_t tag) {
+  return server_enqueue(s, inst, tag, phx_server_s::REQ_STATIC, 0.0);
+}
+
+int phx_server_submit_step(phx_server s, phx_instance inst, double dt, int64_t tag) {
+  if (!(dt > 0)) return set_err(PHX_EINVAL, "dt must be positive");
+  return server_enqueue(s, inst, tag, phx_server_s::REQ_STEP, dt);
+}
+
+int phx_server_submit_mesh(phx_server s, const phx_mesh* mesh, int64_t tag, phx_instance* out) {
+  if (!s || !mesh || !out) return set_err(PHX_EINVAL, "NULL argument");
+  *out = nullptr;
+  if (mesh->num_nodes <= 0 || mesh->num_tets <= 0 || !mesh->X0 || !mesh->tets || !mesh->lame || !mesh->rho)
+    return set_err(PHX_EINVAL, "mesh: empty or missing arrays");
+  phx_instance_s* inst = nullptr;
+  try {
+    inst = new phx_instance_s();
+    inst->ctx = s->ctx;
+    inst->owner = s;
+    inst->resident = false;
+    inst->host_state.store(HOST_NONE, std::memory_order_relaxed);
+    auto k = std::make_unique<KeptMesh>();
+    const size_t n = mesh->num_nodes, m = mesh->num_tets;
+    k->n = mesh->num_nodes;
+    k->m = mesh->num_tets;
+    k->X0.assign(mesh->X0, mesh->X0 + 3 * n);
+    k->T.assign(mesh->tets, mesh->tets + 4 * m);
+    k->lame.assign(mesh->lame, mesh->lame + 2 * m);
+    k->rho.assign(mesh->rho, mesh->rho + m);
+    if (mesh->model) k->model.assign(mesh->model, mesh->model + m);
+    if (mesh->fixed) k->fixed.assign(mesh->fixed, mesh->fixed + 3 * n);
+    if (mesh->force) k->force.assign(mesh->force, mesh->force + 3 * n);
+    if (mesh->soft_k) k->soft_k.assign(mesh->soft_k, mesh->soft_k + n);
+    if (mesh->soft_target) k->soft_target.assign(mesh->soft_target, mesh->soft_target + 3 * n);
+    for (int c = 0; c < 3; ++c) k->gravity[c] = mesh->gravity[c];
+    inst->kept = std::move(k);
+    s->owned.push_back(inst);
+  } catch (const std::bad_alloc&) {
+    if (inst) {
+      if (!s->owned.empty() && s->owned.back() == inst) s->owned.pop_back();
+      delete inst;
+    }
+    return set_err(PHX_ENOMEM, "out of host memory copying the mesh");
+  }
+  const int rc = server_enqueue(s, inst, tag, phx_server_s::REQ_STATIC, 0.0);
+  if (rc != PHX_OK) {
+    s->owned.pop_back();
+    delete inst;
+    return rc;
+  }
+  *out = inst;
+  return PHX_OK;
+}
+
+int phx_server_stats(phx_server s, int64_t* in_use, int64_t* peak, int64_t* resident, int64_t* evictions) {
+  if (!s) return set_err(PHX_EINVAL, "server is NULL");
+  if (in_use) *in_use = s->in_use;
+  if (peak) *peak = s->peak;
+  if (resident) {
+    int64_t r = 0;
+    for (phx_instance inst : s->owned) r += inst->resident ? 1 : 0;
+    *resident = r;
+  }
+  if (evictions) *evictions = s->evictions;
   return PHX_OK;
 }
 
@@ -1354,22 +1747,26 @@ int phx_server_progress(phx_server s, int32_t* active, int32_t* queued) {
   if (!s->active.empty() && !s->dirty && s->ctx->batch_owner == s) {
     std::vector<phx_server_s::Req> keep, fin;
     std::vector<NState> fin_first, fin_second;
+    auto retire = [&](phx_server_s::Req& r, const phx_report& rep) {
+      s->done.push_back({r.tag, rep});
+      r.inst->in_server = false;
+      r.inst->last_used = ++s->tick;
+      s->in_use -= r.counted;
+      s->dirty = true;
+    };
     for (size_t i = 0; i < s->active.size(); ++i) {
       if (s->ctx->h_flags[8 + i] == PH_DONE) {
         auto& r = s->active[i];
         NState st;
         TRY(read_state(r.inst, &st));
-        if (wants_fp64_finish(&s->opts, st)) {  // finished in FP64 below, then retired
+        if (r.kind == phx_server_s::REQ_STATIC && wants_fp64_finish(&s->opts, st)) {  // finished in FP64 below
           fin.push_back(r);
           fin_first.push_back(st);
           continue;
         }
         phx_report rep{};
         fill_report(st, false, std::chrono::duration<double>(clk::now() - r.t_submit).count(), &rep);
-        s->done.push_back({r.tag, rep});
-        r.inst->in_server = false;
-        s->in_use -= r.inst->bytes;
-        s->dirty = true;
+        retire(r, rep);
       } else {
         keep.push_back(s->active[i]);
       }
@@ -1377,29 +1774,104 @@ int phx_server_progress(phx_server s, int32_t* active, int32_t* queued) {
     s->active.swap(keep);
     if (!fin.empty()) {
       std::vector<phx_instance> insts;
-      for (auto& r : fin) insts.push_back(r.inst);
+      std::vector<int64_t> before;
+      for (auto& r : fin) {
+        insts.push_back(r.inst);
+        before.push_back(r.inst->bytes);
+      }
       TRY(finish_fp64(s->ctx, insts, &s->opts, fin_first, &fin_second));
       for (size_t k = 0; k < fin.size(); ++k) {
+        if (fin[k].inst->owner == s) s->in_use += fin[k].inst->bytes - before[k];  // its FP64 buffers
         phx_report rep{};
         fill_report_finished(fin_first[k], fin_second[k],
                              std::chrono::duration<double>(clk::now() - fin[k].t_submit).count(), &rep);
-        s->done.push_back({fin[k].tag, rep});
-        fin[k].inst->in_server = false;
-        s->in_use -= fin[k].inst->bytes;
+        retire(fin[k], rep);
       }
       s->dirty = true;  // the FP64 finish used the context's batch buffers
     }
   }
-  // admit queued requests at this Newton-round boundary (slots + memory budget)
-  while (!s->queue.empty() && (int)s->active.size() < s->max_slots) {
-    auto& r = s->queue.front();
-    if (s->in_use + r.inst->bytes > s->budget) break;
-    TRY(start_solve(r.inst, &s->opts, false, 0.0, 0));
-    s->in_use += r.inst->bytes;
-    s->active.push_back(r);
+  // admit queued requests at this Newton-round boundary: by slots, then by the memory
+  // budget (evicting idle instances, least recently used first), in arrival order; a
+  // request whose host part is still being built lets the ones behind it go first, one
+  // that waits for memory holds them (large requests are not starved)
+  std::deque<phx_server_s::Req> still;
+  bool blocked = false;
+  while (!s->queue.empty()) {
+    phx_server_s::Req r = s->queue.front();
     s->queue.pop_front();
+    if (blocked || (int)s->active.size() >= s->max_slots) {
+      still.push_back(r);
+      continue;
+    }
+    phx_instance inst = r.inst;
+    const int hs = inst->host_state.load(std::memory_order_acquire);
+    if (!inst->resident && hs == HOST_FAILED) {
+      set_err(PHX_EINVAL, inst->host_err);
+      server_fail(s, r, PHX_EINVAL);
+      continue;
+    }
+    if (!inst->resident && hs != HOST_READY) {
+      if (hs == HOST_NONE) TRY(server_build_host(s, inst));  // released by a failed admission
+      still.push_back(r);
+      continue;
+    }
+    const bool owned = inst->owner == s;
+    const size_t es = s->fp64 ? 8 : 4;
+    const bool have = s->fp64 ? inst->have64 : inst->have32;
+    int64_t need;
+    if (!inst->resident) need = device_bytes(inst->hp, !s->fp64, s->fp64);
+    else need = (owned ? 0 : inst->bytes) + (have ? 0 : precision_bytes(inst->dev.n, inst->dev.m, inst->dev.nslots, es));
+    std::vector<Resident> res;
+    std::vector<phx_instance> cand;
+    for (phx_instance o : s->owned)
+      if (o != inst && o->resident) {
+        res.push_back({o->bytes, o->last_used, !o->in_server});
+        cand.push_back(o);
+      }
+    std::vector<int> plan;
+    const int verdict = admit_decision((int)s->active.size(), s->max_slots, s->in_use, s->budget, need, res, &plan);
+    if (verdict == NEVER) {
+      set_err(PHX_ENOMEM, "instance larger than the server budget");
+      server_fail(s, r, PHX_ENOMEM);
+      continue;
+    }
+    if (verdict == WAIT_SLOTS || verdict == WAIT_MEMORY) {
+      blocked = true;
+      still.push_back(r);
+      continue;
+    }
+    for (int k : plan) TRY(server_evict(s, cand[k]));
+    const int64_t b0 = inst->bytes;
+    int rc = server_allocate(s, inst);
+    if (rc == PHX_ENOMEM) {
+      // the arena itself is short (fragmentation, or memory outside this server's budget):
+      // evict the remaining idle instances, least recently used first, and try once more
+      std::vector<int> idle;
+      for (int k = 0; k < (int)cand.size(); ++k)
+        if (cand[k]->resident && !cand[k]->in_server) idle.push_back(k);
+      std::stable_sort(idle.begin(), idle.end(), [&](int a, int b) { return res[a].last_used < res[b].last_used; });
+      for (int k : idle) TRY(server_evict(s, cand[k]));
+      if (!idle.empty()) rc = server_allocate(s, inst);
+    }
+    if (rc == PHX_ENOMEM) {
+      blocked = true;
+      still.push_back(r);
+      continue;
+    }
+    TRY(rc);
+    if (owned) {
+      s->in_use += inst->bytes - b0;  // resident from now on, idle or not
+    } else {
+      r.counted = inst->bytes;        // a caller's instance counts while it is active
+      s->in_use += r.counted;
+    }
+    s->peak = std::max(s->peak, s->in_use);
+    TRY(start_solve(inst, &s->opts, r.kind == phx_server_s::REQ_STEP, r.dt, 0));
+    inst->last_used = ++s->tick;
+    s->active.push_back(r);
     s->dirty = true;
   }
+  s->queue.swap(still);
   if (!s->active.empty()) {
     if (s->dirty || s->ctx->batch_owner != s) {
       std::vector<phx_instance> list;

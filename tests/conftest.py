@@ -44,6 +44,16 @@ def ctl_shim():
 
 
 @pytest.fixture(scope="session")
+def admission_shim():
+    import ctypes as C
+    path = _build_shim("admission_shim", ["admission_shim.cpp"])
+    L = C.CDLL(path)
+    L.adm_decide.argtypes = [C.c_int, C.c_int, C.c_longlong, C.c_longlong, C.c_longlong, C.c_int, C.c_void_p,
+                             C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]
+    return L
+
+
+@pytest.fixture(scope="session")
 def gpu_ctx():
     import physim_gb300 as px
     from physim_gb300 import build
