@@ -181,6 +181,36 @@ int phx_instance_get_velocities(phx_instance inst, double* v);
 /* Replace the nodal loads (EnergyElement_Force f, BC_Gravity g) of a live instance; warm re-solves. */
 int phx_instance_update_load(phx_instance inst, const double* force, const double* gravity);
 
+/* ---- staged boundary conditions ----------------------------------------
+ * BCondition stages (include/PhySim/Physics/Boundary/BCondition.h:85-155, BCondition.cpp:42-67):
+ * every condition advances one stage at each Newton iteration start of a static solve
+ * (OptimProblem_BasicStatic::OnIterStart) and at each dynamic step's start
+ * (OptimProblem_BasicDynamic::OnSolveStart), up to its own num_stages; SolveFull applies its
+ * stop rules only once every condition is at its last stage (IsFullyConstrained,
+ * OptimSolver.cpp:213).  A group is one BC_FixDoF on a node set (BC_FixDoF.cpp:51-121):
+ * hard (its nodes must be fixed in all three DoFs; the static problem moves them to the
+ * targets) or soft (its nodes need a soft record; targets and stiffness change).  Its
+ * targets follow VectorAnimator_LerpT3D (include/PhySim/Utils/VectorAnimators.h:103-145):
+ *   target(a) = a * shift + (I + a * move) * v,   a = min(stage, num_stages) / num_stages,
+ * v the node's position when phx_instance_set_staging is called; a soft stiffness is
+ * k_start + a (k_end - k_start).  (The reference's scene loader builds `move` as R*S from
+ * the animation's rotation and scale, so a full stage applies I + R*S, not R*S.) */
+typedef struct phx_stage_group {
+  int32_t num_stages;  /* BCondition::m_numStage (>= 1) */
+  int32_t soft;        /* 0 hard, 1 soft */
+  double k_start, k_end;
+  double move[9];      /* row-major 3x3 */
+  double shift[3];
+  int32_t num_nodes;
+  const int32_t* nodes;
+} phx_stage_group;
+/* Sets the groups (a node in one group at most) and num_stages, the largest m_numStage over
+ * all the model's conditions (a condition without targets, e.g. BC_Gravity with numStep, only
+ * delays full constraint); the stage goes back to 0.  count 0 and num_stages 0: no staging.
+ * phx_instance_reset also takes the stage back to 0 (Simulable::ResetBoundaryConditions). */
+int phx_instance_set_staging(phx_instance inst, int32_t count, const phx_stage_group* groups, int32_t num_stages);
+int phx_instance_stage(phx_instance inst, int32_t* stage, int32_t* num_stages);
+
 /* ---- model evaluation (ISimulable::GetEnergy / GetGradient / GetHessian) --- */
 /* Energy and gradient at x[3n] (x == NULL: current positions).  fix != 0 applies
  * FixVectorDoFs (Simulable.cpp:735-744). */

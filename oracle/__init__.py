@@ -39,6 +39,36 @@ class OrcOptions(C.Structure):
                 ("cg_block_jacobi", C.c_int32), ("threads", C.c_int32)]
 
 
+class OrcStageGroup(C.Structure):
+    _fields_ = [("num_stages", C.c_int32), ("soft", C.c_int32), ("k_start", C.c_double), ("k_end", C.c_double),
+                ("move", C.c_double * 9), ("shift", C.c_double * 3), ("num_nodes", C.c_int32),
+                ("nodes", C.c_void_p)]
+
+
+def stage_groups(groups, struct=None):
+    """ctypes array of stage groups from dicts (num_stages, soft, k_start, k_end, move, shift,
+    nodes); returns the array and the node arrays it points into."""
+    struct = struct or OrcStageGroup
+    keep = []
+    arr = (struct * max(1, len(groups)))()
+    for g, d in zip(arr, groups):
+        nodes = np.ascontiguousarray(d["nodes"], dtype=np.int32)
+        keep.append(nodes)
+        g.num_stages = int(d.get("num_stages", 1))
+        g.soft = int(d.get("soft", 0))
+        g.k_start = float(d.get("k_start", 1e9))
+        g.k_end = float(d.get("k_end", 1e9))
+        mv = np.asarray(d.get("move", np.zeros((3, 3))), dtype=np.float64).ravel()
+        for k in range(9):
+            g.move[k] = mv[k]
+        sh = np.asarray(d.get("shift", np.zeros(3)), dtype=np.float64)
+        for k in range(3):
+            g.shift[k] = sh[k]
+        g.num_nodes = len(nodes)
+        g.nodes = nodes.ctypes.data
+    return arr, keep
+
+
 class OrcReport(C.Structure):
     _fields_ = [("result", C.c_int32), ("iterations", C.c_int32), ("bisections", C.c_int32),
                 ("reg_trials", C.c_int32), ("lin_iterations", C.c_int64), ("obj", C.c_double),
@@ -76,6 +106,9 @@ def lib():
         L.orc_linear_solve.argtypes = [vp, C.POINTER(OrcOptions), vp, vp, vp, C.POINTER(C.c_int32),
                                        C.POINTER(C.c_int64)]
         L.orc_last_log.argtypes = [vp, vp, vp, vp, vp, C.c_int32]
+        L.orc_set_staging.argtypes = [vp, C.c_int32, vp, C.c_int32, vp]
+        L.orc_stage.argtypes = [vp]
+        L.orc_set_soft.argtypes = [vp, vp, vp]
         _lib = L
     return _lib
 
@@ -212,6 +245,24 @@ class Oracle:
         res = C.c_int32(); it = C.c_int64()
         lib().orc_linear_solve(self.h, C.byref(o), _p(x), _p(b), _p(dx), C.byref(res), C.byref(it))
         return dx, res.value, it.value
+
+    def set_staging(self, groups, num_stages=0, x_ini=None):
+        """Staged boundary conditions (see orc_set_staging); the stage goes back to 0."""
+        arr, keep = stage_groups(groups)
+        xi = np.ascontiguousarray(self.rest() if x_ini is None else x_ini, dtype=np.float64)
+        if lib().orc_set_staging(self.h, len(groups), arr, int(num_stages), _p(xi)) != 0:
+            raise ValueError("oracle rejected the staging")
+        del keep
+
+    def stage(self) -> int:
+        return int(lib().orc_stage(self.h))
+
+    def set_soft(self, k, t):
+        """Soft records of the nodes that have one: stiffness k[n], targets t[3n]."""
+        k = np.ascontiguousarray(k, dtype=np.float64)
+        t = np.ascontiguousarray(t, dtype=np.float64)
+        if lib().orc_set_soft(self.h, _p(k), _p(t)) != 0:
+            raise ValueError("the mesh has no soft records")
 
     def last_log(self):
         n = lib().orc_last_log(self.h, None, None, None, None, 0)

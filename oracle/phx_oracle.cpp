@@ -277,6 +277,16 @@ struct orc_handle_s {
 
   // element buffers
   std::vector<double> Ee, ge, He;
+
+  // staged loading (BCondition stages): groups, their start values, the stage counter
+  struct Group {
+    int num_stages, soft;
+    double k0, k1, M[9], b[3];
+    std::vector<int> nodes;
+    std::vector<double> ini;  // [3 * nodes]
+  };
+  std::vector<Group> groups;
+  int num_stages = 0, stage = 0;
 };
 
 namespace {
@@ -916,6 +926,38 @@ struct Problem {
 
 enum { ONGOING = 0, SUCCESS = 1, MINSTEP = 2, MINIMPR = 3, FAILURE = 4, MAXITER = 5, NONDESC = 6 };
 
+// Simulable::StepBoundaryConditions (Simulable.cpp:1496-1500): one more stage (while not all
+// boundary conditions are loaded), then each group's BC_FixDoF::Update (BC_FixDoF.cpp:80-121)
+// at its own a = min(stage, N) / N: hard groups set their DoFs (positions) to the targets,
+// soft groups set targets and the ramped stiffness.  VectorAnimator_LerpT3D::Evaluate
+// (VectorAnimators.h:135-145) maps a start value v to (I + a Mt) [v; 1] with Mt the
+// animator's 4x4 (its translation b and linear part M), i.e. a b + (I + a M) v.
+bool step_stage(orc_handle_s* h, std::vector<double>& x) {
+  if (h->num_stages <= 0 || h->stage >= h->num_stages) return false;
+  h->stage++;
+  for (auto& G : h->groups) {
+    const double a = (double)std::min(h->stage, G.num_stages) / (double)G.num_stages;
+    for (size_t k = 0; k < G.nodes.size(); ++k) {
+      const int i = G.nodes[k];
+      const double* v = &G.ini[3 * k];
+      double t[3];
+      for (int r = 0; r < 3; ++r)
+        t[r] = a * G.b[r] + v[r] + a * (G.M[3 * r] * v[0] + G.M[3 * r + 1] * v[1] + G.M[3 * r + 2] * v[2]);
+      if (G.soft) {
+        for (int r = 0; r < 3; ++r) h->soft_t[3 * i + r] = t[r];
+        h->soft_k[i] = G.k0 + a * (G.k1 - G.k0);
+      } else {
+        for (int r = 0; r < 3; ++r) x[3 * i + r] = t[r];
+      }
+    }
+  }
+  return true;
+}
+
+// OptimProblem_BasicStatic::IsFullyConstrained (OptimProblem_BasicStatic.cpp:119-121):
+// Simulable::BoundaryConditionsLoaded, every condition at its last stage.
+bool fully_constrained(const orc_handle_s* h) { return h->num_stages <= 1 || h->stage >= h->num_stages; }
+
 struct State {
   std::vector<double> vx, v0, vg;
   double obj = 0, opt = 0;
@@ -932,9 +974,11 @@ int solve_full(orc_handle_s* h, Problem& P, const orc_options* o, orc_report* re
   S.vx = P.x;
   S.v0 = S.vx;
   if (P.dynamic) {
-    // OnSolveStart: predictor x = x0 + dt v0
+    // OnSolveStart (OptimProblem_BasicDynamic.cpp:121-135): x0, v0, the boundary conditions'
+    // next stage, then the predictor x = x0 + dt v0 over every DoF (hard-fixed ones included)
     P.x0 = P.x;
     P.v0 = P.v;
+    step_stage(h, P.x);
     for (int i = 0; i < N; ++i) P.x[i] = P.x0[i] + P.dt * P.v0[i];
     S.vx = P.x;
     S.v0 = S.vx;
@@ -952,6 +996,7 @@ int solve_full(orc_handle_s* h, Problem& P, const orc_options* o, orc_report* re
     itCount++;
     // ---- SolveStep -> OptimSolver_USQP_LS::SolveStepInternal
     int qp = S.steepest ? 0 : o->qp_solver;
+    if (!P.dynamic) step_stage(h, P.x);  // OnIterStart: StepBoundaryConditions (static problem)
     P.save();  // OnIterStart: GetState
     S.obj = P.energy();
     P.gradient(S.vg);
@@ -1066,26 +1111,30 @@ int solve_full(orc_handle_s* h, Problem& P, const orc_options* o, orc_report* re
     // ---- back in SolveFull
     P.gradient(S.vg);
     S.opt = norm2(S.vg.data(), N);
-    // IsFullyConstrained: loads are applied in one stage, so it is true from the first step
+    // SolveFull applies its stop rules only while IsFullyConstrained (OptimSolver.cpp:213):
+    // always for the dynamic problem, once every stage is loaded for the static one
     bool brk = false;
-    if (S.result == NONDESC) {
+    const bool loaded = P.dynamic || fully_constrained(h);
+    if (!loaded) {
+      // no rule applies; the result of the step stays as it is
+    } else if (S.result == NONDESC) {
       if (!o->try_steepest) brk = true;
       else if (S.steepest) brk = true;
       else S.steepest = true;
     }
-    if (!brk && S.result == MINIMPR) {
+    if (loaded && !brk && S.result == MINIMPR) {
       if (S.minImprCount == o->min_impr_max_count) brk = true;
       else if (o->try_steepest) S.steepest = !S.steepest;
     }
-    if (!brk && S.result == MINSTEP) {
+    if (loaded && !brk && S.result == MINSTEP) {
       if (S.minStepCount == o->min_step_max_count) brk = true;
       else if (o->try_steepest) S.steepest = !S.steepest;
     }
-    if (!brk && S.result == SUCCESS) {
+    if (loaded && !brk && S.result == SUCCESS) {
       if (S.opt <= o->tol_max_error) brk = true;
       else S.result = ONGOING;
     }
-    if (!brk && S.result == ONGOING) S.steepest = false;
+    if (loaded && !brk && S.result == ONGOING) S.steepest = false;
     if (brk) break;
     if (itCount + 1 > o->num_max_iters) {
       S.result = MAXITER;
@@ -1295,6 +1344,49 @@ int64_t orc_ldl_nnz(orc_handle h, int natural) {
   }
   if (!h->ldl.analysed) ldl_analyse(h);
   return h->ldl.Lp[h->N];
+}
+
+int orc_set_staging(orc_handle h, int32_t count, const orc_stage_group* groups, int32_t num_stages,
+                    const double* x_ini) {
+  if (count < 0 || num_stages < 0 || (count > 0 && (!groups || !x_ini))) return -1;
+  std::vector<orc_handle_s::Group> gs;
+  int most = num_stages;
+  for (int g = 0; g < count; ++g) {
+    const orc_stage_group& G = groups[g];
+    if (G.num_stages < 1 || G.num_nodes < 0 || (G.num_nodes > 0 && !G.nodes)) return -1;
+    orc_handle_s::Group q;
+    q.num_stages = G.num_stages;
+    q.soft = G.soft ? 1 : 0;
+    q.k0 = G.k_start;
+    q.k1 = G.k_end;
+    std::copy(G.move, G.move + 9, q.M);
+    std::copy(G.shift, G.shift + 3, q.b);
+    for (int k = 0; k < G.num_nodes; ++k) {
+      const int i = G.nodes[k];
+      if (i < 0 || i >= h->n) return -1;
+      if (q.soft && (h->soft_k.empty() || h->soft_k[i] == 0.0)) return -1;
+      q.nodes.push_back(i);
+      for (int r = 0; r < 3; ++r) q.ini.push_back(x_ini[3 * i + r]);
+    }
+    most = std::max(most, G.num_stages);
+    gs.push_back(std::move(q));
+  }
+  h->groups = std::move(gs);
+  h->num_stages = most;
+  h->stage = 0;
+  return 0;
+}
+
+int orc_stage(orc_handle h) { return h->stage; }
+
+int orc_set_soft(orc_handle h, const double* k, const double* t) {
+  if (h->soft_k.empty() || !k || !t) return -1;
+  for (int i = 0; i < h->n; ++i) {
+    if (h->soft_k[i] == 0.0) continue;
+    h->soft_k[i] = k[i];
+    for (int c = 0; c < 3; ++c) h->soft_t[3 * i + c] = t[3 * i + c];
+  }
+  return 0;
 }
 
 int orc_last_log(orc_handle h, double* obj, double* opt, int32_t* bis, double* step, int32_t cap) {

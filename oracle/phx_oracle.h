@@ -73,6 +73,21 @@ typedef struct orc_report {
   double t_cal_ene, t_cal_gra, t_cal_hes, t_ass_gra, t_ass_hes, t_opt_sol, t_opt_lis;
 } orc_report;
 
+/* One staged boundary condition (BCondition, inc/Physics/Boundary/BCondition.h:85-155):
+ * BC_FixDoF on a node set, hard or soft, loaded over num_stages stages with its targets
+ * animated by VectorAnimator_LerpT3D (inc/Utils/VectorAnimators.h:103-145):
+ *   target(a) = a * shift + (I + a * move) * x_ini,   a = stage / num_stages,
+ * and, when soft, the stiffness k_start + a (k_end - k_start) (BC_FixDoF.cpp:85-110). */
+typedef struct orc_stage_group {
+  int32_t num_stages;        /* m_numStage (>= 1) */
+  int32_t soft;              /* 0: hard (the DoFs take the targets), 1: soft (targets and stiffness) */
+  double k_start, k_end;     /* m_kAini, m_kAend */
+  double move[9];            /* row-major 3x3 */
+  double shift[3];
+  int32_t num_nodes;
+  const int32_t* nodes;
+} orc_stage_group;
+
 typedef struct orc_handle_s* orc_handle;
 
 void orc_default_options(orc_options* o);
@@ -106,6 +121,17 @@ int orc_solve_dynamic(orc_handle h, const orc_options* opt, double dt, double* x
 /* One linear solve H dx = b with the configured linear solver (regularisation loop included). */
 int orc_linear_solve(orc_handle h, const orc_options* opt, const double* x, const double* b,
                      double* dx, int32_t* lsresult, int64_t* iters);
+
+/* Staged loading: the groups (their targets start from x_ini [3n]) and num_stages, the largest
+ * m_numStage of all the model's boundary conditions (0 or 1: loaded from the first step).  The
+ * stage counter goes back to 0; each static Newton iteration start (OnIterStart) and each
+ * dynamic solve start (OnSolveStart) advances it, as StepBoundaryConditions does.  Soft groups
+ * need soft records on their nodes (orc_mesh.soft_k > 0). */
+int orc_set_staging(orc_handle h, int32_t count, const orc_stage_group* groups, int32_t num_stages,
+                    const double* x_ini);
+int orc_stage(orc_handle h);
+/* Replaces the soft records (stiffness k[n], targets t[3n]) of nodes that have one. */
+int orc_set_soft(orc_handle h, const double* k, const double* t);
 
 /* Per-iteration log of the last solve: obj, opt, bisections, step norm per iteration. */
 int orc_last_log(orc_handle h, double* obj, double* opt, int32_t* bis, double* step, int32_t cap);

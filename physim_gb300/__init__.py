@@ -29,7 +29,7 @@ EXPORTS = [
     "phx_version", "phx_last_error", "phx_default_options", "phx_context_create", "phx_context_destroy",
     "phx_context_memory", "phx_instance_create", "phx_instances_create", "phx_instance_destroy", "phx_instance_sizes",
     "phx_instance_reset", "phx_instance_set_positions", "phx_instance_get_positions", "phx_instance_set_velocities",
-    "phx_instance_get_velocities", "phx_instance_update_load", "phx_energy_gradient", "phx_hessian",
+    "phx_instance_get_velocities", "phx_instance_update_load", "phx_instance_set_staging", "phx_instance_stage", "phx_energy_gradient", "phx_hessian",
     "phx_hessian_pattern", "phx_scatter_map", "phx_element_local", "phx_solve_static", "phx_solve_step", "phx_solve_log",
     "phx_dynamic_step", "phx_batch_solve", "phx_batch_dynamic_step", "phx_server_create", "phx_server_destroy",
     "phx_server_submit", "phx_server_submit_step", "phx_server_submit_mesh", "phx_server_stats",
@@ -65,6 +65,13 @@ class Options(C.Structure):
                 ("warm_guess", C.c_int32), ("pcg_chunk", C.c_int32), ("tol_rel", C.c_double),
                 ("pcg_cluster", C.c_int32), ("fp64_finish", C.c_int32),
                 ("lsearch_parallel", C.c_int32)]
+
+
+class StageGroup_(C.Structure):
+    """phx_stage_group: one BC_FixDoF group loaded over stages with animated targets."""
+    _fields_ = [("num_stages", C.c_int32), ("soft", C.c_int32), ("k_start", C.c_double), ("k_end", C.c_double),
+                ("move", C.c_double * 9), ("shift", C.c_double * 3), ("num_nodes", C.c_int32),
+                ("nodes", C.c_void_p)]
 
 
 class Report(C.Structure):
@@ -108,6 +115,8 @@ def lib():
         "phx_instance_set_velocities": ([vp, vp], C.c_int),
         "phx_instance_get_velocities": ([vp, vp], C.c_int),
         "phx_instance_update_load": ([vp, vp, vp], C.c_int),
+        "phx_instance_set_staging": ([vp, i32, vp, i32], C.c_int),
+        "phx_instance_stage": ([vp, C.POINTER(i32), C.POINTER(i32)], C.c_int),
         "phx_energy_gradient": ([vp, vp, C.POINTER(dbl), vp, i32], C.c_int),
         "phx_hessian": ([vp, vp, i32, vp, i32], C.c_int),
         "phx_hessian_pattern": ([vp, vp, vp], C.c_int),
@@ -342,6 +351,34 @@ class Instance:
         f = None if force is None else np.ascontiguousarray(force, dtype=np.float64)
         g = None if gravity is None else np.ascontiguousarray(gravity, dtype=np.float64)
         _check(lib().phx_instance_update_load(self.h, _p(f), _p(g)))
+
+    def set_staging(self, groups, num_stages=0):
+        """Staged boundary conditions: groups are dicts (num_stages, soft, k_start, k_end, move,
+        shift, nodes); their targets start from the current positions.  The stage goes to 0."""
+        keep = []
+        arr = (StageGroup_ * max(1, len(groups)))()
+        for g, d in zip(arr, groups):
+            nodes = np.ascontiguousarray(d["nodes"], dtype=np.int32)
+            keep.append(nodes)
+            g.num_stages = int(d.get("num_stages", 1))
+            g.soft = int(d.get("soft", 0))
+            g.k_start = float(d.get("k_start", 1e9))
+            g.k_end = float(d.get("k_end", 1e9))
+            mv = np.asarray(d.get("move", np.zeros((3, 3))), dtype=np.float64).ravel()
+            sh = np.asarray(d.get("shift", np.zeros(3)), dtype=np.float64)
+            for k in range(9):
+                g.move[k] = mv[k]
+            for k in range(3):
+                g.shift[k] = sh[k]
+            g.num_nodes = len(nodes)
+            g.nodes = nodes.ctypes.data
+        _check(lib().phx_instance_set_staging(self.h, len(groups), arr, int(num_stages)))
+        del keep
+
+    def stage(self):
+        a = C.c_int32(); b = C.c_int32()
+        _check(lib().phx_instance_stage(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def energy_gradient(self, x=None, fix=True):
         xx = None if x is None else np.ascontiguousarray(x, dtype=np.float64)

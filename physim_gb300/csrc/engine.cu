@@ -102,6 +102,11 @@ struct Arena {
     }
     return nullptr;
   }
+  size_t size_of(const void* p) const {
+    if (!p) return 0;
+    auto it = live_.find((size_t)((const char*)p - base));
+    return it == live_.end() ? 0 : it->second;
+  }
   void free(void* p) {
     if (!p) return;
     size_t off = (char*)p - base;
@@ -218,10 +223,18 @@ struct phx_instance_s {
   std::string host_err;
   std::vector<double> saved_x, saved_v;    // positions and velocities kept on the host by an eviction
   uint64_t last_used = 0;                  // server tick of the last request (eviction order)
+  // staged boundary conditions (phx_instance_set_staging): the stage persists across solves
+  int32_t stage = 0, num_stages = 0;
+  bool stage_values = false;               // a stage moves targets or changes a soft stiffness
+  std::vector<double> soft0;               // soft records at stage 0, restored by phx_instance_reset
+  std::vector<int32_t> stage_grp;          // host copies of the staging arrays (uploaded again when a
+  std::vector<double> stage_ini, stage_par;  // server re-creates the instance after an eviction)
 };
 
 // Drops a server-created instance from its server's bookkeeping (defined with the server).
 void server_forget(phx_server s, phx_instance inst);
+// Adds device bytes of one of its instances to a server's count.
+void server_account(phx_server s, int64_t delta);
 
 namespace {
 
@@ -493,6 +506,7 @@ int reset_state(phx_instance inst, int phase, int nofix, double shift) {
   s.nofix = nofix;
   s.shift = shift;
   s.opt0 = -1.0;
+  s.stage = inst->stage;
   CU(cudaMemcpyAsync(inst->d_st, &s, sizeof(NState), cudaMemcpyHostToDevice, inst->ctx->stream));
   return PHX_OK;
 }
@@ -500,6 +514,7 @@ int reset_state(phx_instance inst, int phase, int nofix, double shift) {
 int read_state(phx_instance inst, NState* s) {
   CU(cudaMemcpyAsync(s, inst->d_st, sizeof(NState), cudaMemcpyDeviceToHost, inst->ctx->stream));
   CU(cudaStreamSynchronize(inst->ctx->stream));
+  inst->stage = s->stage;  // the boundary conditions keep their stage after a solve
   return PHX_OK;
 }
 
@@ -698,6 +713,8 @@ int start_solve(phx_instance inst, const phx_options* o, bool dynamic, double dt
   TRY(ensure_precision(inst, fp64));
   DevOpts d = make_opts(o, dynamic, dt);
   if (max_iters_override > 0) d.num_max_iters = max_iters_override;
+  d.num_stages = inst->num_stages;
+  d.stage_values = inst->stage_values ? 1 : 0;
   set_algo_bytes(inst->dev, fp64);
   // the cluster PCG serves the FP32 path: FP64 arithmetic is slow on this part and needs
   // every SM, so FP64 solves iterate on the whole GPU
@@ -1112,6 +1129,140 @@ int phx_instance_reset(phx_instance inst) {
   CU(cudaMemcpyAsync(inst->dev.x, inst->dev.xrest, bytes, cudaMemcpyDeviceToDevice, st));
   CU(cudaMemsetAsync(inst->dev.v, 0, bytes, st));
   CU(cudaMemsetAsync(inst->dev.dxprev, 0, bytes, st));
+  // staged boundary conditions back to stage 0 (Simulable::ResetBoundaryConditions)
+  inst->stage = 0;
+  if (!inst->soft0.empty())
+    CU(cudaMemcpyAsync(inst->dev.soft, inst->soft0.data(), inst->soft0.size() * sizeof(double),
+                       cudaMemcpyHostToDevice, st));
+  return PHX_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Frees the device copies of an instance's staging arrays (the host copies stay).
+int release_staging(phx_instance inst) {
+  int64_t freed = 0;
+  InstDev& D = inst->dev;
+  CU(cudaStreamSynchronize(inst->ctx->stream));
+  for (const void* p : {(const void*)D.stage_grp, (const void*)D.stage_ini, (const void*)D.stage_par}) {
+    if (!p) continue;
+    auto it = std::find(inst->blocks.begin(), inst->blocks.end(), p);
+    if (it == inst->blocks.end()) continue;
+    const int64_t b = (int64_t)inst->ctx->arena.size_of(p);
+    inst->ctx->arena.free(*it);
+    inst->blocks.erase(it);
+    inst->bytes -= b;
+    freed += b;
+  }
+  if (inst->owner) server_account(inst->owner, -freed);
+  D.stage_grp = nullptr;
+  D.stage_ini = nullptr;
+  D.stage_par = nullptr;
+  return PHX_OK;
+}
+
+// Uploads the instance's staging arrays and its stage-0 soft records; `account`: the bytes
+// count against the instance's server at once (a server that sets an instance up counts them
+// itself).
+int upload_staging(phx_instance inst, bool account = true) {
+  if (inst->stage_grp.empty()) return PHX_OK;
+  InstDev& D = inst->dev;
+  const int64_t b0 = inst->bytes;
+  int32_t* dg = nullptr;
+  double* di = nullptr;
+  double* dp = nullptr;
+  TRY(upload(inst, &dg, inst->stage_grp));
+  TRY(upload(inst, &di, inst->stage_ini));
+  TRY(upload(inst, &dp, inst->stage_par));
+  D.stage_grp = dg;
+  D.stage_ini = di;
+  D.stage_par = dp;
+  if (inst->owner && account) server_account(inst->owner, inst->bytes - b0);
+  if (!inst->soft0.empty() && D.soft)
+    CU(cudaMemcpyAsync(D.soft, inst->soft0.data(), inst->soft0.size() * sizeof(double), cudaMemcpyHostToDevice,
+                       inst->ctx->stream));
+  CU(cudaStreamSynchronize(inst->ctx->stream));
+  return PHX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Staged boundary conditions: BCondition stages (BCondition.cpp:42-67) over groups of
+// BC_FixDoF nodes with VectorAnimator_LerpT3D targets (BC_FixDoF.cpp:80-121).
+int phx_instance_set_staging(phx_instance inst, int32_t count, const phx_stage_group* groups, int32_t num_stages) {
+  if (!inst || count < 0 || num_stages < 0 || (count > 0 && !groups)) return set_err(PHX_EINVAL, "bad arguments");
+  if (inst->in_server) return set_err(PHX_EBUSY, "instance is admitted to a server");
+  TRY(require_resident(inst));
+  if (count > 64) return set_err(PHX_EINVAL, "staging: at most 64 groups");
+  const HostPattern& hp = inst->hp;
+  const int n = hp.n;
+  std::vector<int32_t> grp(n, -1);
+  std::vector<double> par(16 * (size_t)std::max(count, 1), 0.0);
+  int most = num_stages;
+  bool values = false;
+  for (int g = 0; g < count; ++g) {
+    const phx_stage_group& G = groups[g];
+    if (G.num_stages < 1 || G.num_nodes < 0 || (G.num_nodes > 0 && !G.nodes))
+      return set_err(PHX_EINVAL, "staging: group " + std::to_string(g) + " needs num_stages >= 1 and its nodes");
+    for (int k = 0; k < G.num_nodes; ++k) {
+      const int v = G.nodes[k];
+      if (v < 0 || v >= n) return set_err(PHX_EINVAL, "staging: node id out of range");
+      if (grp[v] >= 0) return set_err(PHX_EINVAL, "staging: node " + std::to_string(v) + " in two groups");
+      if (G.soft) {
+        if (hp.soft.empty() || hp.soft[4 * (size_t)v + 3] == 0.0)
+          return set_err(PHX_EINVAL, "staging: soft group node " + std::to_string(v) + " has no soft record");
+      } else if ((hp.fixmask[v] & 7) != 7) {
+        return set_err(PHX_EINVAL, "staging: hard group node " + std::to_string(v) + " is not fixed");
+      }
+      grp[v] = g;
+    }
+    double* P = &par[16 * (size_t)g];
+    P[0] = G.num_stages;
+    P[1] = G.soft ? 1.0 : 0.0;
+    P[2] = G.k_start;
+    P[3] = G.k_end;
+    for (int k = 0; k < 9; ++k) P[4 + k] = G.move[k];
+    for (int k = 0; k < 3; ++k) P[13 + k] = G.shift[k];
+    bool moves = false;
+    for (int k = 0; k < 12; ++k) moves = moves || P[4 + k] != 0.0;
+    values = values || G.soft || moves;
+    most = std::max(most, G.num_stages);
+  }
+  // start values: the nodes' positions now (BC_FixDoF holds the DoFs' values when it is made)
+  std::vector<double> x(3 * (size_t)n), ini(4 * (size_t)n, 0.0);
+  TRY(download_x(inst, inst->dev.x, x.data()));
+  for (int v = 0; v < n; ++v)
+    if (grp[v] >= 0)
+      for (int c = 0; c < 3; ++c) ini[4 * (size_t)v + c] = x[3 * (size_t)v + c];
+  TRY(release_staging(inst));
+  inst->num_stages = most;
+  inst->stage = 0;
+  inst->stage_values = values;
+  inst->soft0.clear();
+  if (count == 0) return PHX_OK;
+  inst->stage_grp = std::move(grp);
+  inst->stage_ini = std::move(ini);
+  inst->stage_par = std::move(par);
+  // stage 0 of the soft groups: targets at their start values, stiffness k_start
+  if (!hp.soft.empty()) {
+    inst->soft0 = hp.soft;
+    for (int v = 0; v < n; ++v)
+      if (inst->stage_grp[v] >= 0 && groups[inst->stage_grp[v]].soft) {
+        for (int c = 0; c < 3; ++c) inst->soft0[4 * (size_t)v + c] = inst->stage_ini[4 * (size_t)v + c];
+        inst->soft0[4 * (size_t)v + 3] = groups[inst->stage_grp[v]].k_start;
+      }
+  }
+  return upload_staging(inst);
+}
+
+int phx_instance_stage(phx_instance inst, int32_t* stage, int32_t* num_stages) {
+  if (!inst) return set_err(PHX_EINVAL, "inst is NULL");
+  if (stage) *stage = inst->stage;
+  if (num_stages) *num_stages = inst->num_stages;
   return PHX_OK;
 }
 
@@ -1503,6 +1654,11 @@ struct phx_server_s {
   std::vector<std::thread> workers;
 };
 
+void server_account(phx_server s, int64_t delta) {
+  s->in_use += delta;
+  s->peak = std::max(s->peak, s->in_use);
+}
+
 void server_forget(phx_server s, phx_instance inst) {
   auto it = std::find(s->owned.begin(), s->owned.end(), inst);
   if (it == s->owned.end()) return;
@@ -1603,6 +1759,7 @@ int server_allocate(phx_server s, phx_instance inst) {
     return rc;
   }
   if (fresh) {
+    TRY(upload_staging(inst, false));  // counted with the rest of the set-up by the caller
     if (!inst->saved_x.empty()) TRY(upload_x(inst, inst->saved_x.data(), inst->dev.x));
     if (!inst->saved_v.empty()) TRY(upload_x(inst, inst->saved_v.data(), inst->dev.v));
     inst->saved_x.clear();
@@ -1819,7 +1976,12 @@ int phx_server_progress(phx_server s, int32_t* active, int32_t* queued) {
     const size_t es = s->fp64 ? 8 : 4;
     const bool have = s->fp64 ? inst->have64 : inst->have32;
     int64_t need;
-    if (!inst->resident) need = device_bytes(inst->hp, !s->fp64, s->fp64);
+    if (!inst->resident) {
+      need = device_bytes(inst->hp, !s->fp64, s->fp64);
+      if (!inst->stage_grp.empty())
+        need += arena_bytes_of(inst->stage_grp.size(), 4) + arena_bytes_of(inst->stage_ini.size(), 8) +
+                arena_bytes_of(inst->stage_par.size(), 8);
+    }
     else need = (owned ? 0 : inst->bytes) + (have ? 0 : precision_bytes(inst->dev.n, inst->dev.m, inst->dev.nslots, es));
     std::vector<Resident> res;
     std::vector<phx_instance> cand;

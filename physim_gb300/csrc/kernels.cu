@@ -296,6 +296,43 @@ __device__ void advance(const BatchDev& B, int i) {
 // ---------------------------------------------------------------------------
 // vector ops of the state machine
 // ---------------------------------------------------------------------------
+// One node's boundary-condition values at `stage` (BC_FixDoF::Update, BC_FixDoF.cpp:80-121):
+// its group's a = min(stage, N) / N; the target a b + (I + a M) v of the start value v
+// (VectorAnimator_LerpT3D::Evaluate, VectorAnimators.h:135-145); a hard group's node takes
+// it as its position (the static problem: the dynamic one's predictor overwrites positions),
+// a soft group's node takes it as its target with the stiffness k0 + a (k1 - k0).  Called on
+// the iteration's start state (x = the last accepted iterate).
+__device__ __forceinline__ void stage_node(const InstDev& I, int v, int stage, double (&x)[3]) {
+  if (!I.stage_grp) return;
+  const int g = I.stage_grp[v];
+  if (g < 0) return;
+  const double* P = I.stage_par + 16 * g;
+  const int N = (int)P[0];
+  const double a = (double)min(stage, N) / (double)N;
+  double u[3], t[3];
+  ld4(I.stage_ini, v, u);
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+    t[r] = a * P[13 + r] + u[r] + a * (P[4 + 3 * r] * u[0] + P[5 + 3 * r] * u[1] + P[6 + 3 * r] * u[2]);
+  if (P[1] != 0.0) {
+    double* q = I.soft + 4 * (size_t)v;
+    q[0] = t[0]; q[1] = t[1]; q[2] = t[2];
+    q[3] = P[2] + a * (P[3] - P[2]);
+  } else if (!I.opts->dynamic) {
+    // the Newton step's start guess, x - x at the last accepted step (OptimSolver.cpp:488),
+    // includes the move of the staged DoFs
+    double d[3];
+    ld4(I.dxprev, v, d);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      d[r] += t[r] - x[r];
+      x[r] = t[r];
+    }
+    st4(I.dxprev, v, d);
+    st4(I.x, v, x);
+  }
+}
+
 __device__ __forceinline__ void st_vecop(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag) {
   const int total = map_total(M);
   for (int t = cta; t < total; t += ncta) {
@@ -322,7 +359,8 @@ __device__ __forceinline__ void st_vecop(const BatchDev& B, const TileMap& M, in
         ld4(I.xs, v, x);
         st4(I.x, v, x);
       }
-      if (ops & (VO_ACCEPT | VO_GCOPY)) {
+      if (ops & VO_STAGE) stage_node(I, v, st->stage, x);
+      if (ops & (VO_ACCEPT | VO_GCOPY | VO_GNEW)) {
         ld4(I.gn, v, tmp);
         st4(I.g, v, tmp);
       }

@@ -25,9 +25,25 @@ constexpr double kBackFactor = 1e2;  // restart points of the FP64 finish: ||g||
 enum OSResult : int32_t { OS_ONGOING = 0, OS_SUCCESS = 1, OS_MINSTEP = 2, OS_MINIMPR = 3,
                           OS_FAILURE = 4, OS_MAXITER = 5, OS_NONDESC = 6 };
 
-// SolveFull's decisions after one SolveStep; returns the next phase.
+// OptimProblem_BasicStatic::IsFullyConstrained (OptimProblem_BasicStatic.cpp:119-121): every
+// boundary condition at its last stage (Simulable::BoundaryConditionsLoaded); always true for
+// the dynamic problem (OptimProblem_BasicDynamic.cpp:117-119).
+PHX_HD inline bool ctl_fully_constrained(const NState& s, const DevOpts& o) {
+  return o.dynamic || o.num_stages <= 1 || s.stage >= o.num_stages;
+}
+
+// SolveFull's decisions after one SolveStep; returns the next phase.  Its stop rules apply
+// only while the problem is fully constrained (OptimSolver.cpp:213); before that, only the
+// iteration limit ends a solve.
 PHX_HD inline int32_t ctl_post_step(NState& s, const DevOpts& o) {
   bool brk = false;
+  if (!ctl_fully_constrained(s, o)) {
+    if (s.it + 1 > o.num_max_iters) {
+      s.result = OS_MAXITER;
+      return PH_DONE;
+    }
+    return PH_ITER;
+  }
   if (s.result == OS_NONDESC) {
     if (!o.try_steepest) brk = true;
     else if (s.steepest) brk = true;
@@ -348,10 +364,26 @@ PHX_HD inline void ctl_advance(NState& s, const DevOpts& o) {
         s.log_pending = 0;
         s.tol_eff = o.tol_max_error;
         s.purpose = 0;
+        s.iter_staged = 0;
         s.vecop = o.dynamic ? VO_PRED : 0;
+        if (o.dynamic && o.num_stages > 0 && s.stage < o.num_stages) {
+          // OnSolveStart of the dynamic problem (OptimProblem_BasicDynamic.cpp:121-135): the
+          // conditions' next stage, before the predictor overwrites every position (so only
+          // the soft targets and stiffness of the stage take effect)
+          s.stage++;
+          if (o.stage_values) s.vecop |= VO_STAGE;
+        }
         ctl_goto(s, PH_EVAL);
         return;
       case PH_EVAL_DONE:
+        if (s.purpose == 3) {  // re-evaluated at the iteration start after a stage moved its targets
+          s.obj = s.E_eval;
+          s.opt = sqrt(s.gg_eval);
+          s.vecop = VO_GNEW | VO_SAVE;
+          s.next_phase = PH_ITER;
+          s.phase = PH_VEC;
+          return;
+        }
         if (s.purpose == 0) {
           s.obj = s.E_eval;
           s.opt = sqrt(s.gg_eval);
@@ -365,6 +397,18 @@ PHX_HD inline void ctl_advance(NState& s, const DevOpts& o) {
         if (s.phase == PH_ITER) continue;
         return;
       case PH_ITER:
+        if (!o.dynamic && !s.iter_staged && o.num_stages > 0 && s.stage < o.num_stages) {
+          // OnIterStart of the static problem: StepBoundaryConditions (Simulable.cpp:1496-1500)
+          s.stage++;
+          s.iter_staged = 1;
+          if (o.stage_values) {  // new targets or stiffness: energy and gradient again
+            s.purpose = 3;
+            s.vecop = VO_STAGE;
+            ctl_goto(s, PH_EVAL);
+            return;
+          }
+        }
+        s.iter_staged = 0;
         ctl_iter_begin(s, o);
         if (s.phase == PH_ITER) continue;
         return;

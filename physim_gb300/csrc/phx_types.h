@@ -65,6 +65,8 @@ enum VecOp : int32_t {
   VO_GCOPY = 128,     // g = gn
   VO_ZERODX = 256,    // dx = 0
   VO_BACK = 512,     // keep the saved iterate as the restart point of an FP64 finish
+  VO_STAGE = 1024,   // staged boundary conditions: targets (and soft stiffness) of the current stage
+  VO_GNEW = 2048,    // g = gn (re-evaluation at the start of an iteration)
 };
 
 // LIN_TRUNCATED: the FP32 path met negative curvature and kept the iterate so far
@@ -83,6 +85,8 @@ struct DevOpts {
   double tol_max_error, tol_min_step, tol_min_impr, max_step_size, ls_tol_max_error;
   double lsearch_alpha, inner_tol, dt, tol_rel;
   double lsearch_wolfe1, lsearch_wolfe2;                         // Armijo / Wolfe constants c1, c2
+  int32_t num_stages, stage_values;  // staged loading: stages until fully constrained (0, 1: none);
+                                     // 1 if a stage changes targets or stiffness (re-evaluate)
 };
 
 // Scalar state of one instance's solve (one thread of the control kernel owns it).
@@ -108,6 +112,7 @@ struct NState {
   int32_t log_pending, log_count;              // per-iteration log bookkeeping
   int32_t lsk, pad_ls;                         // trials in the batch being evaluated (PH_EVALK)
   double ls_a[8], ls_e[8], ls_eel[8];          // their step lengths, energies, element energies
+  int32_t stage, iter_staged;                  // boundary-condition stage; 1 once this iteration stepped it
 };
 
 constexpr int kLogCap = 256;                   // Newton iterations kept in the per-instance log
@@ -137,7 +142,10 @@ struct InstDev {
   const uint8_t* fixmask;     // [n] bit d = DoF d fixed
   const double* mass;         // [n] lumped mass per node
   double* hlin;               // [n][4] f - m g : linear-load term of energy and gradient
-  const double* soft;         // [n][4] soft fixed position (target x, y, z, stiffness k) per node, or null
+  double* soft;               // [n][4] soft fixed position (target x, y, z, stiffness k) per node, or null
+  const int32_t* stage_grp;   // [n] staged group of each node (-1: none), or null
+  const double* stage_ini;    // [n][4] the start value its targets are animated from
+  const double* stage_par;    // [groups][16]: num_stages, soft, k_start, k_end, move (9, row-major), shift (3)
   // FP64 node vectors [n][4]
   const double* xrest;
   double* x; double* xs; double* dx; double* g; double* gn; double* dxprev;

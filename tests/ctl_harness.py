@@ -13,6 +13,7 @@ PH_DONE, PH_START, PH_VEC, PH_EVAL, PH_EVAL_DONE, PH_ITER, PH_HESS, PH_JACOBI, P
     PH_ACCUM, PH_LIN_DONE, PH_EVALK, PH_EVALK2 = range(15)
 VO_RESTORE, VO_ACCEPT, VO_SAVE, VO_STEEP, VO_TRIAL, VO_VEL, VO_PRED, VO_GCOPY, VO_ZERODX = \
     1, 2, 4, 8, 16, 32, 64, 128, 256
+VO_STAGE, VO_GNEW = 1024, 2048
 LIN_RUNNING, LIN_CONVERGED, LIN_MAXITER, LIN_BREAKDOWN = range(4)
 
 
@@ -26,7 +27,8 @@ class NState(C.Structure):
             "E_eval", "gg_eval", "normA2", "shift", "regT", "bb", "rr64", "rz", "rr", "pq", "alpha", "beta",
             "thr_inner", "thr_final", "tol_eff", "lin_tol", "eta", "opt_prev", "log_step", "dg", "dg_eval")] + \
         [("log_pending", C.c_int32), ("log_count", C.c_int32), ("lsk", C.c_int32), ("pad_ls", C.c_int32),
-         ("ls_a", C.c_double * 8), ("ls_e", C.c_double * 8), ("ls_eel", C.c_double * 8)]
+         ("ls_a", C.c_double * 8), ("ls_e", C.c_double * 8), ("ls_eel", C.c_double * 8),
+         ("stage", C.c_int32), ("iter_staged", C.c_int32)]
 
 
 class DevOpts(C.Structure):
@@ -36,7 +38,8 @@ class DevOpts(C.Structure):
         "max_refine_sweeps", "warm_guess", "dynamic", "ls_parallel", "lsearch_type", "pad_o")] + \
         [(n, C.c_double) for n in (
             "tol_max_error", "tol_min_step", "tol_min_impr", "max_step_size", "ls_tol_max_error",
-            "lsearch_alpha", "inner_tol", "dt", "tol_rel", "lsearch_wolfe1", "lsearch_wolfe2")]
+            "lsearch_alpha", "inner_tol", "dt", "tol_rel", "lsearch_wolfe1", "lsearch_wolfe2")] + \
+        [("num_stages", C.c_int32), ("stage_values", C.c_int32)]
 
 
 def make_opts(**kw):
@@ -96,8 +99,27 @@ def pcg(A, b, x, thr, maxit, Minv, eigen=True):
 stats = {"evalk": 0}  # PH_EVALK visits of the last run
 
 
-def run(shim, orc, x0, opts, dynamic=False, v0=None, max_steps=200000):
-    """Drives ctl_advance_c until PH_DONE; returns (x, v, NState)."""
+def stage_values(groups, ini, stage):
+    """The staged targets and soft stiffness of every group node at `stage`, as the device's
+    stage_node computes them: {node: (target[3], soft, k)}."""
+    out = {}
+    for g in groups:
+        N = int(g.get("num_stages", 1))
+        a = min(stage, N) / N
+        M = np.asarray(g.get("move", np.zeros((3, 3))), dtype=np.float64).reshape(3, 3)
+        b = np.asarray(g.get("shift", np.zeros(3)), dtype=np.float64)
+        k0, k1 = float(g.get("k_start", 1e9)), float(g.get("k_end", 1e9))
+        for i in g["nodes"]:
+            v = ini[3 * i:3 * i + 3]
+            t = np.array([a * b[r] + v[r] + a * (M[r, 0] * v[0] + M[r, 1] * v[1] + M[r, 2] * v[2]) for r in range(3)])
+            out[int(i)] = (t, int(g.get("soft", 0)), k0 + a * (k1 - k0))
+    return out
+
+
+def run(shim, orc, x0, opts, dynamic=False, v0=None, max_steps=200000, staging=None, stage=0):
+    """Drives ctl_advance_c until PH_DONE; returns (x, v, NState).  staging: (groups, x_ini)
+    of staged boundary conditions (opts.num_stages and opts.stage_values set by the caller),
+    stage: the stage the solve starts from."""
     sizes = (C.c_int * 2)()
     shim.ctl_sizes(sizes)
     assert sizes[0] == C.sizeof(NState) and sizes[1] == C.sizeof(DevOpts), "struct layout mismatch"
@@ -118,6 +140,12 @@ def run(shim, orc, x0, opts, dynamic=False, v0=None, max_steps=200000):
     stats["evalk"] = 0
     s.phase = PH_START
     s.opt0 = -1.0
+    s.stage = stage
+    soft_k = None if getattr(m, "soft_k", None) is None else np.array(m.soft_k, dtype=np.float64)
+    soft_t = None
+    if soft_k is not None:
+        st0 = getattr(m, "soft_target", None)
+        soft_t = np.array(m.X0.ravel() if st0 is None else st0, dtype=np.float64).ravel()
     o = opts
     A = None
     Minv = None
@@ -134,7 +162,18 @@ def run(shim, orc, x0, opts, dynamic=False, v0=None, max_steps=200000):
                 xo = x.copy(); vo = v.copy(); x = xo + dt * vo
             if ops & VO_RESTORE:
                 x = xs.copy()
-            if ops & (VO_ACCEPT | VO_GCOPY):
+            if ops & VO_STAGE:
+                groups, ini = staging
+                for i, (t, soft, k) in stage_values(groups, ini, s.stage).items():
+                    if soft:
+                        soft_t[3 * i:3 * i + 3] = t
+                        soft_k[i] = k
+                    elif not dynamic:
+                        dxprev[3 * i:3 * i + 3] += t - x[3 * i:3 * i + 3]
+                        x[3 * i:3 * i + 3] = t
+                if soft_k is not None:
+                    orc.set_soft(soft_k, soft_t)
+            if ops & (VO_ACCEPT | VO_GCOPY | VO_GNEW):
                 g = gn.copy()
             if ops & VO_ACCEPT:
                 dxprev = a * dx
