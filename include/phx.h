@@ -211,6 +211,33 @@ typedef struct phx_stage_group {
 int phx_instance_set_staging(phx_instance inst, int32_t count, const phx_stage_group* groups, int32_t num_stages);
 int phx_instance_stage(phx_instance inst, int32_t* stage, int32_t* num_stages);
 
+/* ---- scene files -----------------------------------------------------------
+ * The reference's XML vocabulary (source/PhySim/Utils/Serializer_XML.cpp): the element read by
+ * LoadSimulable_VolumeFEM (:1199-1325) as <simulable type="VolumeFEM">, LoadOptimProblem's
+ * (:1327-1354) as <problem>, LoadOptimSolver's (:1356-1505) as <solver> and LoadBoundary's
+ * <bc> list (:1507-1647) inside <boundary>, all under one root element (the reference has
+ * no top-level reader; this is the layout that holds its loaders' elements).  meshInit /
+ * meshRest are FILEVOLUME TetGen meshes (<base>.node + <base>.ele; the reference declares
+ * Serializer_Mesh::ReadVolume_TET without a body), relative to the scene file; TET4 with
+ * TET_LIN / TET_1, CONH / STVK, CONSTANT or VARIABLE distributions; Gravity and FixPosition
+ * (hard or soft, numStep, Transform3D animation, AllNodes / BoundaryNodes / IndexNodes /
+ * BoxNodes selections).  Anything else is refused with PHX_EINVAL and a message. */
+typedef struct phx_scene_s* phx_scene;
+int phx_scene_load(const char* path, phx_scene* out);
+int phx_scene_destroy(phx_scene sc);
+/* counts; reoriented: tetrahedra of negative volume in the file whose corners 1, 2 were swapped */
+int phx_scene_info(phx_scene sc, int32_t* num_nodes, int32_t* num_tets, int32_t* dynamic, double* dt,
+                   int32_t* num_groups, int32_t* num_stages, int32_t* reoriented);
+/* The model as a phx_mesh (pointers into the scene, valid while it lives) and, if x_init is
+ * not NULL, its start positions [3n] (meshInit; the rest shape is meshRest, else meshInit). */
+int phx_scene_mesh(phx_scene sc, phx_mesh* mesh, double* x_init);
+/* phx_default_options with the scene's <solver> attributes applied */
+int phx_scene_options(phx_scene sc, phx_options* opts);
+/* Up to cap staged groups (animated FixPosition conditions); returns their count. */
+int phx_scene_staging(phx_scene sc, phx_stage_group* groups, int32_t cap);
+/* Creates the scene's instance: the mesh, its start positions and its staging. */
+int phx_scene_instance(phx_context ctx, phx_scene sc, phx_instance* out);
+
 /* ---- model evaluation (ISimulable::GetEnergy / GetGradient / GetHessian) --- */
 /* Energy and gradient at x[3n] (x == NULL: current positions).  fix != 0 applies
  * FixVectorDoFs (Simulable.cpp:735-744). */

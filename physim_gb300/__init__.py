@@ -36,6 +36,8 @@ EXPORTS = [
     "phx_server_progress", "phx_server_poll", "phx_profile_enable", "phx_profile_read",
     "phx_profile_reset", "phx_profile_bytes", "phx_kernel_launches", "phx_timer_mark", "phx_timer_elapsed",
     "phx_hessian_blocks_noalloc", "phx_debug_unmet_barrier",
+    "phx_scene_load", "phx_scene_destroy", "phx_scene_info", "phx_scene_mesh", "phx_scene_options",
+    "phx_scene_staging", "phx_scene_instance",
 ]
 
 
@@ -145,6 +147,14 @@ def lib():
         "phx_timer_elapsed": ([vp, i32, i32, C.POINTER(dbl)], C.c_int),
         "phx_hessian_blocks_noalloc": ([i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp], C.c_int),
         "phx_debug_unmet_barrier": ([vp, i32, i64], C.c_int),
+        "phx_scene_load": ([C.c_char_p, C.POINTER(vp)], C.c_int),
+        "phx_scene_destroy": ([vp], C.c_int),
+        "phx_scene_info": ([vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), C.POINTER(dbl), C.POINTER(i32),
+                            C.POINTER(i32), C.POINTER(i32)], C.c_int),
+        "phx_scene_mesh": ([vp, C.POINTER(Mesh_), vp], C.c_int),
+        "phx_scene_options": ([vp, C.POINTER(Options)], C.c_int),
+        "phx_scene_staging": ([vp, vp, i32], C.c_int),
+        "phx_scene_instance": ([vp, vp, C.POINTER(vp)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -500,3 +510,86 @@ class Server:
         if n < 0:
             _check(n)
         return [(int(tags[i]), reps[i].as_dict()) for i in range(n)]
+
+
+class Scene:
+    """A scene file in the reference's XML vocabulary (phx_scene_*): the model, the problem,
+    the solver options and the boundary conditions, with TetGen volume meshes."""
+
+    def __init__(self, path: str):
+        h = C.c_void_p()
+        _check(lib().phx_scene_load(os.fsencode(path), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().phx_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self):
+        n, m, dyn, ng, ns, fl = (C.c_int32() for _ in range(6))
+        dt = C.c_double()
+        _check(lib().phx_scene_info(self.h, C.byref(n), C.byref(m), C.byref(dyn), C.byref(dt), C.byref(ng),
+                                    C.byref(ns), C.byref(fl)))
+        return {"nodes": n.value, "tets": m.value, "dynamic": bool(dyn.value), "dt": dt.value, "groups": ng.value,
+                "num_stages": ns.value, "reoriented": fl.value}
+
+    def mesh(self):
+        """(mesh, x_init): the model as a physim_gb300.mesh.Mesh (copies) and its start positions."""
+        d = Mesh_()
+        info = self.info()
+        x = np.zeros(3 * info["nodes"])
+        _check(lib().phx_scene_mesh(self.h, C.byref(d), _p(x)))
+        n, m = d.num_nodes, d.num_tets
+
+        def arr(ptr, count, ctype, dtype):
+            if not ptr:
+                return None
+            return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(ctype)), shape=(count,)).astype(dtype).copy()
+
+        out = mesh.Mesh(X0=arr(d.X0, 3 * n, C.c_double, np.float64).reshape(n, 3),
+                        T=arr(d.tets, 4 * m, C.c_int32, np.int32).reshape(m, 4),
+                        lame=arr(d.lame, 2 * m, C.c_double, np.float64).reshape(m, 2),
+                        rho=arr(d.rho, m, C.c_double, np.float64),
+                        model=arr(d.model, m, C.c_uint8, np.uint8),
+                        fixed=arr(d.fixed, 3 * n, C.c_uint8, np.uint8),
+                        force=np.zeros(3 * n), gravity=np.array([d.gravity[k] for k in range(3)]),
+                        dims=None, name="scene")
+        if d.soft_k:
+            out.soft_k = arr(d.soft_k, n, C.c_double, np.float64)
+            out.soft_target = arr(d.soft_target, 3 * n, C.c_double, np.float64)
+        return out, x
+
+    def options(self) -> Options:
+        o = Options()
+        _check(lib().phx_scene_options(self.h, C.byref(o)))
+        return o
+
+    def staging(self):
+        """The animated FixPosition groups as dicts (num_stages, soft, k_start, k_end, move, shift, nodes)."""
+        k = lib().phx_scene_staging(self.h, None, 0)
+        if k < 0:
+            _check(k)
+        arr = (StageGroup_ * max(1, k))()
+        lib().phx_scene_staging(self.h, arr, k)
+        out = []
+        for g in arr[:k]:
+            nodes = np.ctypeslib.as_array(C.cast(g.nodes, C.POINTER(C.c_int32)), shape=(g.num_nodes,)).copy() \
+                if g.num_nodes else np.zeros(0, dtype=np.int32)
+            out.append({"num_stages": g.num_stages, "soft": g.soft, "k_start": g.k_start, "k_end": g.k_end,
+                        "move": np.array(list(g.move)).reshape(3, 3), "shift": np.array(list(g.shift)),
+                        "nodes": nodes})
+        return out
+
+    def instance(self, ctx: Context) -> "Instance":
+        """The scene's instance on the device: mesh, start positions and staging."""
+        m, _ = self.mesh()
+        h = C.c_void_p()
+        _check(lib().phx_scene_instance(ctx.h, self.h, C.byref(h)))
+        return Instance(ctx, m, _handle=h)

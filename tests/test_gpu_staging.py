@@ -107,3 +107,38 @@ def test_staging_rejects_inconsistent_groups(gpu_ctx):
         inst.set_staging([dict(num_stages=2, soft=1, nodes=free)], 2)
     with pytest.raises(px.PhxError):  # num_stages >= 1
         inst.set_staging([dict(num_stages=0, soft=0, nodes=free)], 2)
+
+
+def test_scene_file_solves_like_the_oracle(gpu_ctx, tmp_path):
+    """A scene file (TetGen mesh, FixPosition clamp moved by a Transform3D animation over 3
+    stages, gravity) through phx_scene_instance, against the oracle given the scene's mesh and
+    staging.  Scale 0 in the animation makes the reference's I + a R S a pure translation."""
+    import os
+    from test_scene import scene_xml, write_tetgen
+    ref = M.cantilever(2, 2, 6)
+    write_tetgen(os.path.join(tmp_path, "bar"), ref.X0, ref.T)
+    bc = ('<bc type="FixPosition" soft="false" numStep="3"><selection type="BoxNodes" field="Pos0">'
+          '<minCorner>-1e-9, -1e-9, -1e-9</minCorner><maxCorner>1, 1, 1e-9</maxCorner></selection>'
+          '<animation type="Transform3D"><position>0, 0.004, 0</position><scale>0, 0, 0</scale></animation></bc>'
+          '<bc type="Gravity"><gravity>0, -9.81, 0</gravity></bc>')
+    p = os.path.join(tmp_path, "scene.xml")
+    with open(p, "w") as f:
+        f.write(scene_xml(boundary=bc))
+    sc = px.Scene(p)
+    m, x0 = sc.mesh()
+    groups = sc.staging()
+    info = sc.info()
+    orc = oracle.Oracle(m)
+    g0 = np.linalg.norm(orc.gradient(x0))
+    tol = 1e-6 * g0
+    orc.set_staging(groups, info["num_stages"], x0)
+    xo, ro = orc.solve_static(x0, ls_solver=1, cg_block_jacobi=1, tol_max_error=tol, **KW)
+    inst = sc.instance(gpu_ctx)
+    o = sc.options()
+    o.tol_max_error, o.tol_min_impr, o.tol_min_step = tol, 0.0, 0.0
+    x, r = inst.solve_static(o)
+    assert (r["result"], r["iterations"], r["bisections"]) == (ro["result"], ro["iterations"], ro["bisections"])
+    assert inst.stage() == (orc.stage(), 3)
+    assert disp_err(x, xo, x0) < 1e-9
+    clamp = groups[0]["nodes"]
+    assert np.abs(x.reshape(-1, 3)[clamp] - (m.X0[clamp] + [0.0, 0.004, 0.0])).max() < 1e-10
