@@ -30,18 +30,24 @@ def test_engine_barrier_wait_runs_out(gpu_ctx, tag, prec):
     m = M.cantilever(2, 2, 6)
     inst = px.Instance(gpu_ctx, m)
     o = px.options(precision=prec, tol_rel=1e-8, tol_max_error=0.0, tol_min_impr=0.0, tol_min_step=0.0)
-    x_ref, r_ref = inst.solve_static(o, m.X0.ravel())
+    inst.reset()  # each solve from rest with no warm PCG guess, so the two solves are the same
+    x_ref, r_ref = inst.solve_static(o)
     assert r_ref["result_name"] == "SUCCESS"
+    inst.reset()
     gpu_ctx.debug_unmet_barrier(tag, LIMIT)
     try:
         with pytest.raises(px.PhxError) as ei:
-            inst.solve_static(o, m.X0.ravel())
+            inst.solve_static(o)
     finally:
         gpu_ctx.debug_unmet_barrier(0)
     assert ei.value.code == px.PHX_ETIMEOUT
-    assert f"stage {tag})" in str(ei.value)
+    # tag 11 holds the whole-GPU PCG group; CTAs outside it wait at the round barrier 18,
+    # and whichever wait gives up first is named
+    names = {f"stage {tag})"} | ({"stage 18)"} if tag == 11 else set())
+    assert any(nm in str(ei.value) for nm in names), str(ei.value)
     # the context is still usable: the same solve gives the same bits
-    x2, r2 = inst.solve_static(o, m.X0.ravel())
+    inst.reset()
+    x2, r2 = inst.solve_static(o)
     assert np.array_equal(x2, x_ref) and _same(r2, r_ref)
 
 

@@ -49,10 +49,12 @@ def test_staged_clamp_rotation_matches_oracle(gpu_ctx):
     assert (r["result"], r["iterations"], r["bisections"]) == (ro["result"], ro["iterations"], ro["bisections"])
     assert inst.stage() == (stage, 4) == (4, 4)
     assert disp_err(x, xo, x0) < 1e-9
-    # the served path from stage 0 again (phx_instance_reset takes the stage back)
+    # the served path from stage 0 again (phx_instance_reset takes the stage back), to the
+    # oracle's absolute tolerance: a relative one would be taken after the first stage, whose
+    # moved clamp makes ||g0|| far larger than the loads alone
     inst.reset()
     assert inst.stage()[0] == 0
-    o = px.options(precision=px.PREC_FP32_REFINE, tol_rel=1e-6, tol_max_error=0.0, **KW)
+    o = px.options(precision=px.PREC_FP32_REFINE, tol_max_error=tol, **KW)
     x32, r32 = inst.solve_static(o)
     assert r32["result_name"] == "SUCCESS" and inst.stage()[0] == 4
     assert disp_err(x32, xo, x0) < 5e-6
