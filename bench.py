@@ -275,14 +275,14 @@ def served_options(px, args):
     return px.options(precision=px.PREC_FP32_REFINE, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0,
                       tol_min_step=0.0, pcg_chunk=args.pcg_chunk, inner_tol=args.inner_tol,
                       ls_num_max_iters=args.served_pcg_max, max_refine_sweeps=args.served_sweeps,
-                      lsearch_type=LSEARCH[args.lsearch])
+                      lsearch_type=LSEARCH[args.lsearch], negative_curvature=args.curvature)
 
 
 def batch_config(args, count, tets):
     return {"workload": f"batched uneven boxes: {count} instances, 6-tet hexes, {tets} tets", "instances": count,
             "tets": tets, "tol_rel": args.tol_rel, "line_search": args.lsearch,
             "l2": "inputs larger than L2 (per-step working set well above 129 MB)",
-            "inner_tol": args.inner_tol, "pcg_chunk": args.pcg_chunk,
+            "inner_tol": args.inner_tol, "pcg_chunk": args.pcg_chunk, "negative_curvature": args.curvature,
             "plain_pcg_max_per_newton_step": args.plain_pcg_max,
             "served_pcg_per_sweep_x_sweeps": [args.served_pcg_max, args.served_sweeps]}
 
@@ -836,6 +836,8 @@ def main():
     ap.add_argument("--arena-gb", type=float, default=48.0)
     ap.add_argument("--e2e-sample", action="store_true",
                     help="e2e on the first quarter of the instances instead of the whole workload")
+    ap.add_argument("--curvature", type=int, default=0, choices=[0, 1],
+                    help="served FP32 PCG at negative curvature: 0 truncate, 1 go on like Eigen's CG")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-oracle-all", action="store_true",
                     help="skip the comparison of every batch instance with the oracle (about a minute of host time)")

@@ -121,6 +121,10 @@ typedef struct phx_options {
                                  (the step lengths the one-at-a-time search would try) are evaluated
                                  together and scanned in order with its rules: the same decisions in
                                  fewer rounds; 0 or 1: one at a time; at most 8 (default 8) */
+  int32_t negative_curvature; /* FP32 path when the PCG meets p.Ap < 0 (an indefinite Hessian): 0 (default)
+                                 truncates the solve there (Steihaug); 1 goes on with a negative step
+                                 as Eigen's ConjugateGradient does, which the FP64 path always does,
+                                 and regularises when the step is not a descent direction */
 } phx_options;
 
 typedef struct phx_report {

@@ -456,6 +456,7 @@ DevOpts make_opts(const phx_options* o, bool dynamic, double dt) {
   d.inner_tol = o->inner_tol;
   d.dt = dt;
   d.tol_rel = o->tol_rel;
+  d.curv_through = o->negative_curvature == 1 ? 1 : 0;
   return d;
 }
 
@@ -477,6 +478,8 @@ int validate_opts(const phx_options* o) {
   if (o->fp64_finish < 0 || o->fp64_finish > 1) return set_err(PHX_EINVAL, "options: fp64_finish must be 0 or 1");
   if (o->lsearch_parallel < 0 || o->lsearch_parallel > kLsK)
     return set_err(PHX_EINVAL, "options: lsearch_parallel out of [0,8]");
+  if (o->negative_curvature < 0 || o->negative_curvature > 1)
+    return set_err(PHX_EINVAL, "options: negative_curvature must be 0 or 1");
   return PHX_OK;
 }
 

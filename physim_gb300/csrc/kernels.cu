@@ -1185,7 +1185,7 @@ __device__ __forceinline__ void st_pcg_a(const BatchDev& B, const TileMap& M, in
     if (tile_done<1>(I, lt, pcg_tiles(B, I), ncta, p, tot, sm, &flag) && threadIdx.x == 0) {
       count_bytes(B, I, K_PCG_A);
       st->pq = tot[0];
-      if (I.opts->precision == 0 && tot[0] < 0.0) {
+      if ((I.opts->precision == 0 || I.opts->curv_through) && tot[0] < 0.0) {
         // Eigen's ConjugateGradient has no curvature test: a negative p.q gives a negative
         // step along p and the iteration goes on; LinearSolver_EigenCG regularises only
         // when the result fails b.x >= 0 (LinearSolver_EigenCG.cpp:95-107)
@@ -1768,7 +1768,9 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT) k_pcg_cluster(B
       bool last = false;
       double pq_use = pq;
       if (!(pq > 0.0)) {
-        if (I.opts->precision != 0 && pq < 0.0 && iter == 0) {
+        if (I.opts->curv_through && pq < 0.0) {
+          // as Eigen's CG: a negative step along p, and on
+        } else if (I.opts->precision != 0 && pq < 0.0 && iter == 0) {
           pq_use = -pq;  // truncated CG, first direction: step along p with |p.q| and stop
           last = true;
         } else {
@@ -2185,7 +2187,9 @@ __device__ __forceinline__ CgResult cg_solve(const InstDev& I, const CgShared& S
   out.eta = eta;
   out.gamma = gam;
   if (!(eta > 0.f)) {
-    if (trunc_ok && eta < 0.f && out.iter == 0) {
+    if (!trunc_ok && eta < 0.f) {
+      // Eigen's ConjugateGradient has no curvature test: a negative step along p, and on
+    } else if (trunc_ok && eta < 0.f && out.iter == 0) {
       eta = -eta;  // truncated CG, first direction: one step along z with |z.Az| and stop
       last = true;
     } else {
@@ -2260,7 +2264,7 @@ __device__ __forceinline__ CgResult cg_solve(const InstDev& I, const CgShared& S
     out.eta = eta;
     out.gamma = gam;
     out.beta = beta;
-    if (!(eta > 0.f)) {  // not positive definite along p (or non-finite)
+    if (!(eta > 0.f) && !(!trunc_ok && eta < 0.f)) {  // not positive definite along p (or non-finite)
       out.status = (trunc_ok && eta < 0.f) ? LIN_TRUNCATED : LIN_BREAKDOWN;
       break;
     }
@@ -2372,7 +2376,8 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_pcg_cg(Bat
     const float sh = (float)st->shift;
     const float thr = (float)st->thr_inner;
     const int maxit = I.opts->ls_num_max_iters;
-    const bool trunc_ok = I.opts->precision != 0;
+    // FP32 path at negative curvature: truncate (Steihaug), or go on as Eigen's CG does
+    const bool trunc_ok = I.opts->precision != 0 && !I.opts->curv_through;
     const int iter0 = st->pcg_iter;
     CgResult out;
     if (L == 4) out = cg_solve<4, CL, NT>(I, S, rank, c0, row0, row1, sb, red, ws, mbar, phase, err, abort_sm, sh, thr, maxit,

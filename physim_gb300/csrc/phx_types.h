@@ -87,6 +87,7 @@ struct DevOpts {
   double lsearch_wolfe1, lsearch_wolfe2;                         // Armijo / Wolfe constants c1, c2
   int32_t num_stages, stage_values;  // staged loading: stages until fully constrained (0, 1: none);
                                      // 1 if a stage changes targets or stiffness (re-evaluate)
+  int32_t curv_through, pad_cv;      // FP32 PCG at negative curvature: 1 goes on like Eigen's CG
 };
 
 // Scalar state of one instance's solve (one thread of the control kernel owns it).

@@ -39,7 +39,8 @@ class DevOpts(C.Structure):
         [(n, C.c_double) for n in (
             "tol_max_error", "tol_min_step", "tol_min_impr", "max_step_size", "ls_tol_max_error",
             "lsearch_alpha", "inner_tol", "dt", "tol_rel", "lsearch_wolfe1", "lsearch_wolfe2")] + \
-        [("num_stages", C.c_int32), ("stage_values", C.c_int32)]
+        [("num_stages", C.c_int32), ("stage_values", C.c_int32), ("curv_through", C.c_int32),
+         ("pad_cv", C.c_int32)]
 
 
 def make_opts(**kw):
