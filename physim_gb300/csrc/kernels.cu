@@ -953,6 +953,15 @@ __device__ __forceinline__ void st_linsetup(const BatchDev& B, const TileMap& M,
       for (int c = 0; c < 3; ++c) g[c] = -g[c];
       st4(I.bvec, v, g);
       if (I.opts->warm_guess) ld4(I.dxprev, v, d);
+      if (I.opts->precision != 0 && !st->nofix) {
+        // the served path's inexact FP32 solves start the fixed DoFs at their exact step, 0:
+        // their rows and columns are the identity and their right-hand side is 0, so the PCG
+        // keeps them at 0 and a clamp never drifts by the inner tolerance times a guess (a
+        // staged clamp's move enters the guess as x - x_prev does in the reference)
+        const int fm = I.fixmask[v];
+        for (int c = 0; c < 3; ++c)
+          if (fm & (1 << c)) d[c] = 0.0;
+      }
       st4(I.dx, v, d);
       p[0] = g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
     }

@@ -68,7 +68,6 @@ def test_admission_refuses_a_request_above_the_budget(gpu_ctx):
     x_alone, _ = i_small.solve_static(o, small.X0.ravel())
     i_small.reset()
     # a budget between the two instances' device footprints
-    u0, _ = gpu_ctx.memory()
     srv = px.Server(gpu_ctx, max_slots=4, budget_bytes=1 << 20, opts=o)
     try:
         with pytest.raises(px.PhxError) as ei:
@@ -83,6 +82,8 @@ def test_admission_refuses_a_request_above_the_budget(gpu_ctx):
                 break
         assert done[2]["result_name"] == "SUCCESS"
         assert np.array_equal(i_small.positions(), x_alone)
+        # a caller's instance counts against the budget only while it is active
+        st = srv.stats()
+        assert st["in_use"] == 0 and 0 < st["peak"] <= 1 << 20
     finally:
         srv.close()
-    assert gpu_ctx.memory()[0] == u0
