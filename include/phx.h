@@ -254,7 +254,9 @@ int phx_hessian_pattern(phx_instance inst, int32_t* colptr /* 3n+1 */, int32_t* 
  * of every tet, blocks counted column-major over the pattern (DerivativeAssembler.cpp:205-300). */
 int phx_scatter_map(phx_instance inst, int32_t* map /* 10*num_tets */);
 /* Per-element values (IEnergyElement::GetLocal*, EnergyElement_FEM.cpp:125-222):
- * E[m], g[12m], H[144m] row-major 12x12; any output may be NULL. */
+ * E[m], g[12m], H[144m] row-major 12x12; any output may be NULL.  PHX_PREC_FP64: FP64
+ * elements.  PHX_PREC_FP32_REFINE: the served path's elements (energy and gradient in
+ * double-float on the FP32 pipe, about 1e-12 relative; Hessian in FP32). */
 int phx_element_local(phx_instance inst, const double* x, int32_t precision, double* E, double* g, double* H);
 
 /* ---- solver (IOptimSolver::SolveFull / SolveStep, OptimSolver.cpp:148-311,

@@ -927,7 +927,9 @@ bool instance_build_host(const phx_mesh* mesh, phx_instance_s* inst, std::string
 int64_t device_bytes(const HostPattern& hp, bool fp32, bool fp64) {
   const size_t n = hp.n, m = hp.m, n4 = 4 * n;
   int64_t b = arena_bytes_of(hp.tets.size(), 4) + arena_bytes_of(hp.rest64.size(), 8) +
-              arena_bytes_of(hp.rest32.size(), 4) + arena_bytes_of(hp.model.size(), 1) +
+              arena_bytes_of(hp.rest32.size(), 4) + arena_bytes_of(hp.rest32lo.size(), 4) +
+              arena_bytes_of(hp.tile_nptr.size(), 4) + arena_bytes_of(hp.tile_nodes.size(), 4) +
+              arena_bytes_of(hp.tet_loc.size(), 2) + arena_bytes_of(hp.model.size(), 1) +
               arena_bytes_of(hp.chunk_off.size(), 4) + arena_bytes_of(hp.slot_col.size(), 4) +
               arena_bytes_of(hp.diag_slot.size(), 4) + arena_bytes_of(hp.lo_rc.size(), 4) +
               arena_bytes_of(hp.lo_slot.size(), 4) + arena_bytes_of(hp.up_slot.size(), 4) +
@@ -985,6 +987,10 @@ int instance_setup_device(phx_context ctx, const phx_mesh* mesh, phx_instance_s*
   UP(tets, hp.tets);
   UP(rest64, hp.rest64);
   UP(rest32, hp.rest32);
+  UP(rest32lo, hp.rest32lo);
+  UP(tile_nptr, hp.tile_nptr);
+  UP(tile_nodes, hp.tile_nodes);
+  UP(tet_loc, hp.tet_loc);
   UP(model, hp.model);
   UP(chunk_off, hp.chunk_off);
   UP(slot_col, hp.slot_col);
@@ -1026,6 +1032,9 @@ int instance_setup_device(phx_context ctx, const phx_mesh* mesh, phx_instance_s*
   // keep only what later calls need on the host
   hp.rest64.clear(); hp.rest64.shrink_to_fit();
   hp.rest32.clear(); hp.rest32.shrink_to_fit();
+  hp.rest32lo.clear(); hp.rest32lo.shrink_to_fit();
+  hp.tile_nodes.clear(); hp.tile_nodes.shrink_to_fit();
+  hp.tet_loc.clear(); hp.tet_loc.shrink_to_fit();
   hp.seg_c.clear(); hp.seg_c.shrink_to_fit();
   hp.nseg_c.clear(); hp.nseg_c.shrink_to_fit();
   hp.slot_col.clear(); hp.slot_col.shrink_to_fit();
@@ -1395,10 +1404,12 @@ int run_kernels(phx_instance inst, const std::vector<KernelId>& ids, bool fp64) 
   return PHX_OK;
 }
 
-int eval_eg(phx_instance inst, const double* x, int nofix, NState* s) {
+// Energy and gradient at x: FP64 elements (served = false) or the served path's double-float
+// elements, whose per-element gradients are left as (hi, lo) float pairs.
+int eval_eg(phx_instance inst, const double* x, int nofix, NState* s, bool served = false) {
   if (x) TRY(upload_x(inst, x, inst->dev.x));
   DevOpts d{};
-  d.precision = 0;
+  d.precision = served ? 1 : 0;
   CU(cudaMemcpyAsync(inst->d_opts, &d, sizeof(DevOpts), cudaMemcpyHostToDevice, inst->ctx->stream));
   TRY(reset_state(inst, PH_EVAL, nofix, 0.0));
   TRY(run_kernels(inst, {K_ELEM_EG, K_GATHER}, true));
@@ -1464,12 +1475,17 @@ int phx_element_local(phx_instance inst, const double* x, int32_t precision, dou
   if (precision != PHX_PREC_FP64 && precision != PHX_PREC_FP32_REFINE) return set_err(PHX_EINVAL, "precision");
   TRY(require_resident(inst));
   const int m = inst->dev.m;
+  const bool fp64 = precision == PHX_PREC_FP64;
   NState s;
-  TRY(eval_eg(inst, x, 0, &s));
+  TRY(eval_eg(inst, x, 0, &s, !fp64));
   if (E) CU(cudaMemcpy(E, inst->dev.Eloc, m * sizeof(double), cudaMemcpyDeviceToHost));
-  if (g) CU(cudaMemcpy(g, inst->dev.Gloc, 12 * (size_t)m * sizeof(double), cudaMemcpyDeviceToHost));
+  if (g && fp64) CU(cudaMemcpy(g, inst->dev.Gloc, 12 * (size_t)m * sizeof(double), cudaMemcpyDeviceToHost));
+  if (g && !fp64) {  // double-float pairs: component = hi + lo
+    std::vector<float> G2(24 * (size_t)m);
+    CU(cudaMemcpy(G2.data(), inst->dev.Gloc, G2.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    for (size_t k = 0; k < 12 * (size_t)m; ++k) g[k] = (double)G2[2 * k] + (double)G2[2 * k + 1];
+  }
   if (Hout) {
-    const bool fp64 = precision == PHX_PREC_FP64;
     TRY(eval_hess(inst, nullptr, fp64, 0));
     std::vector<double> Hl(90 * (size_t)m);
     if (fp64) {

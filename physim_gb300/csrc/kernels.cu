@@ -30,6 +30,7 @@
 #include <type_traits>
 
 #include "element.cuh"
+#include "ffmath.cuh"
 #include "kernels.h"
 #include "newton_control.h"
 
@@ -487,7 +488,98 @@ __device__ __forceinline__ double soft_energy(const SoftNode& s, const double x[
   return 0.5 * s.k * (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
 }
 
-__device__ __forceinline__ void st_elem_eg(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag) {
+// ---------------------------------------------------------------------------
+// served path (FP32 + refinement): element energy and gradient in double-float
+// ---------------------------------------------------------------------------
+// The tile's distinct nodes are staged once in shared memory as u = x - X0 in FP64 (node
+// lists built with the pattern), each tet's displacement differences are taken there in FP64
+// (so a large rigid motion costs no digits) and converted to double-float, and the rest of
+// the element (F, the material law, the gradient) runs on the FP32 pipe.  Results: the
+// element energy in FP64, the gradient as double-float pairs (float2 per component) that
+// the gather sums in double-float.
+constexpr int kTileNodeCap = 4 * kTile;  // distinct nodes of a tile, at most
+
+// Stages u = x - X0 (x given per node by the functor) of the tile's distinct nodes into
+// shared memory, [3][kTileNodeCap] doubles; returns the node count.  Ends with a barrier.
+template <typename GetX>
+__device__ __forceinline__ int ff_stage_nodes(const InstDev& I, int lt, double* U, GetX getx) {
+  const int p0 = __ldg(I.tile_nptr + lt), cnt = __ldg(I.tile_nptr + lt + 1) - p0;
+  __syncthreads();  // the previous tile's readers are done with U
+  for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
+    const int v = __ldg(I.tile_nodes + p0 + k);
+    double x[3], X[3];
+    getx(v, x);
+    ld4(I.xrest, v, X);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) U[r * kTileNodeCap + k] = x[r] - X[r];
+  }
+  __syncthreads();
+  return cnt;
+}
+
+// Energy (and, with grad, the gradient) of tet e from the staged displacements.  Returns the
+// energy; an inverted element (J <= 0) has +inf and a zero gradient.
+__device__ __forceinline__ double ff_element(const InstDev& I, int e, const double* U, bool grad, float2* gout) {
+  const ushort4 lc = reinterpret_cast<const ushort4*>(I.tet_loc)[e];
+  const int loc[4] = {lc.x, lc.y, lc.z, lc.w};
+  ff Du[9];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+      Du[r + 3 * c] = ff_of_d(U[r * kTileNodeCap + loc[c + 1]] - U[r * kTileNodeCap + loc[0]]);
+  ff R[12];
+  {
+    const float4* h = reinterpret_cast<const float4*>(I.rest32 + 12 * (size_t)e);
+    const float4* l = reinterpret_cast<const float4*>(I.rest32lo + 12 * (size_t)e);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float4 a = __ldg(h + k), b = __ldg(l + k);
+      R[4 * k] = ff{a.x, b.x};
+      R[4 * k + 1] = ff{a.y, b.y};
+      R[4 * k + 2] = ff{a.z, b.z};
+      R[4 * k + 3] = ff{a.w, b.w};
+    }
+  }
+  ff Hd[9];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+      Hd[r + 3 * c] = ff_fma(Du[r + 6], R[2 + 3 * c], ff_fma(Du[r + 3], R[1 + 3 * c], ff_mul(Du[r], R[3 * c])));
+  const ff w = R[9];
+  ff psi, P[9];
+  const bool ok = ff_material(I.model[e], R[10], R[11], Hd, &psi, P);
+  if (grad) {
+    float2 g[12];
+    if (ok) {
+      // g_a = w P B_a, B_a = row (a-1) of Dm^-1, B_0 = -(B_1 + B_2 + B_3)
+      const ff b0 = ff_neg(ff_add(ff_add(R[0], R[1]), R[2])), b1 = ff_neg(ff_add(ff_add(R[3], R[4]), R[5]));
+      const ff b2 = ff_neg(ff_add(ff_add(R[6], R[7]), R[8]));
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        const ff v0 = ff_mul(ff_fma(P[r + 6], b2, ff_fma(P[r + 3], b1, ff_mul(P[r], b0))), w);
+        g[r] = make_float2(v0.hi, v0.lo);
+#pragma unroll
+        for (int a = 1; a < 4; ++a) {
+          const ff va = ff_mul(
+              ff_fma(P[r + 6], R[(a - 1) + 6], ff_fma(P[r + 3], R[(a - 1) + 3], ff_mul(P[r], R[a - 1]))), w);
+          g[3 * a + r] = make_float2(va.hi, va.lo);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < 12; ++k) g[k] = make_float2(0.f, 0.f);
+    }
+    float4* go = reinterpret_cast<float4*>(gout);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) go[k] = make_float4(g[2 * k].x, g[2 * k].y, g[2 * k + 1].x, g[2 * k + 1].y);
+  }
+  return ok ? ff_to_d(ff_mul(psi, w)) : __longlong_as_double(0x7ff0000000000000LL);
+}
+
+__device__ __forceinline__ void st_elem_eg(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag,
+                                           unsigned char* smraw) {
   const int total = map_total(M);
   for (int t = cta; t < total; t += ncta) {
     int i, lt;
@@ -497,7 +589,14 @@ __device__ __forceinline__ void st_elem_eg(const BatchDev& B, const TileMap& M, 
     if (st->phase != PH_EVAL) continue;
     const int e = lt * kTile + threadIdx.x;
     double Ee = 0.0;
-    if (e < I.m) {
+    if (I.opts->precision != 0) {  // served path: double-float, nodes staged per tile
+      double* U = reinterpret_cast<double*>(smraw);
+      ff_stage_nodes(I, lt, U, [&](int v, double (&x)[3]) { ld4(I.x, v, x); });
+      if (e < I.m) {
+        Ee = ff_element(I, e, U, true, reinterpret_cast<float2*>(I.Gloc) + 12 * (size_t)e);
+        I.Eloc[e] = Ee;
+      }
+    } else if (e < I.m) {
       int nd[4];
       double Du[9];
       load_du(I, e, nd, Du);
@@ -546,7 +645,8 @@ __device__ __forceinline__ void st_elem_eg(const BatchDev& B, const TileMap& M, 
 // trial point, and the element energy exactly as st_elem_eg does, so each trial's total
 // has the bits a one-at-a-time evaluation would give.  Energies only (the accepted trial
 // is evaluated again with its gradient).
-__device__ __forceinline__ void st_elem_ek(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag) {
+__device__ __forceinline__ void st_elem_ek(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag,
+                                           unsigned char* smraw) {
   const int total = map_total(M);
   for (int t = cta; t < total; t += ncta) {
     int i, lt;
@@ -559,7 +659,25 @@ __device__ __forceinline__ void st_elem_ek(const BatchDev& B, const TileMap& M, 
     double Ek[kLsK];
 #pragma unroll
     for (int k = 0; k < kLsK; ++k) Ek[k] = 0.0;
-    if (e < I.m) {
+    if (I.opts->precision != 0) {
+      // served path: each trial's nodes x = xs + a_k dx, formed as the vector-op stage forms a
+      // trial point, staged per tile, and the element energy as st_elem_eg computes it
+      double* U = reinterpret_cast<double*>(smraw);
+      for (int k = 0; k < K; ++k) {
+        const double ak = st->ls_a[k];
+        ff_stage_nodes(I, lt, U, [&](int v, double (&x)[3]) {
+          double xs[3], dx[3];
+          ld4(I.xs, v, xs);
+          ld4(I.dx, v, dx);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) x[c] = xs[c] + ak * dx[c];
+        });
+        const double Ee = e < I.m ? ff_element(I, e, U, false, nullptr) : 0.0;
+#pragma unroll
+        for (int q = 0; q < kLsK; ++q)
+          if (q == k) Ek[q] = Ee;
+      }
+    } else if (e < I.m) {
       const int4 tt = reinterpret_cast<const int4*>(I.tets)[e];
       const int nd[4] = {tt.x, tt.y, tt.z, tt.w};
       double xs[4][3], dx[4][3], X[4][3];
@@ -668,9 +786,10 @@ __device__ __forceinline__ void st_lin_ek(const BatchDev& B, const TileMap& M, i
 }
 
 __global__ void __launch_bounds__(kTile) k_elem_eg(BatchDev B) {
+  extern __shared__ __align__(16) unsigned char smraw[];  // staged nodes of the served path
   __shared__ double sm[32 * 5];
   __shared__ int flag;
-  st_elem_eg(B, full_map(B, B.pre_tet), blockIdx.x, gridDim.x, sm, flag);
+  st_elem_eg(B, full_map(B, B.pre_tet), blockIdx.x, gridDim.x, sm, flag, smraw);
 }
 
 // node gather of element gradients + linear loads (+ inertia), energy and ||g||^2
@@ -688,6 +807,33 @@ __device__ __forceinline__ void st_gather(const BatchDev& B, const TileMap& M, i
       double g[3] = {0.0, 0.0, 0.0};
       const int c0 = I.nseg_ptr[v], c1 = I.nseg_ptr[v + 1];
       int c = c0;
+      if (I.opts->precision != 0) {
+        // served path: double-float element gradients, summed in double-float in element order
+        ff a3[3] = {ff_of(0.f), ff_of(0.f), ff_of(0.f)};
+        const float2* G2 = reinterpret_cast<const float2*>(I.Gloc);
+        for (; c + 4 <= c1; c += 4) {
+          int id[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) id[u] = I.nseg_c[c + u];
+          float2 val[4][3];
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) val[u][k] = G2[3 * (size_t)id[u] + k];
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) a3[k] = ff_add(a3[k], ff{val[u][k].x, val[u][k].y});
+        }
+        for (; c < c1; ++c) {
+          const float2* src = G2 + 3 * (size_t)I.nseg_c[c];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) a3[k] = ff_add(a3[k], ff{src[k].x, src[k].y});
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) g[k] = ff_to_d(a3[k]);
+        c = c1;
+      }
       // four contributions in flight (ids, then values), added in element order
       for (; c + 4 <= c1; c += 4) {
         int id[4];
@@ -1539,7 +1685,7 @@ __global__ void __launch_bounds__(kTile, (sizeof(Real) == 4 ? 3 : 2)) k_engine(B
       PHX_SYNC(P, 2, K_VECOP);
     }
     if (PHX_NEED(PH_EVAL)) {
-      st_elem_eg(B, Mt, cta, P, sm, flag);
+      st_elem_eg(B, Mt, cta, P, sm, flag, smraw);
       PHX_SYNC(P, 3, K_ELEM_EG);
     }
     if (PHX_NEED(PH_EVAL)) {
@@ -1547,7 +1693,7 @@ __global__ void __launch_bounds__(kTile, (sizeof(Real) == 4 ? 3 : 2)) k_engine(B
       PHX_SYNC(P, 4, K_GATHER);
     }
     if (PHX_NEED(PH_EVALK)) {
-      st_elem_ek(B, Mt, cta, P, sm, flag);
+      st_elem_ek(B, Mt, cta, P, sm, flag, smraw);
       PHX_SYNC(P, 19, K_ELEM_EG);
     }
     if (PHX_NEED(PH_EVALK2)) {
@@ -1603,7 +1749,7 @@ __global__ void __launch_bounds__(kTile, (sizeof(Real) == 4 ? 3 : 2)) k_engine(B
       PHX_SYNC(P, 15, K_VECOP);
     }
     if (PHX_NEED(PH_EVAL)) {
-      st_elem_eg(B, Mt, cta, P, sm, flag);
+      st_elem_eg(B, Mt, cta, P, sm, flag, smraw);
       PHX_SYNC(P, 16, K_ELEM_EG);
     }
     if (PHX_NEED(PH_EVAL)) {
@@ -1611,7 +1757,7 @@ __global__ void __launch_bounds__(kTile, (sizeof(Real) == 4 ? 3 : 2)) k_engine(B
       PHX_SYNC(P, 17, K_GATHER);
     }
     if (PHX_NEED(PH_EVALK)) {
-      st_elem_ek(B, Mt, cta, P, sm, flag);
+      st_elem_ek(B, Mt, cta, P, sm, flag, smraw);
       PHX_SYNC(P, 21, K_ELEM_EG);
     }
     if (PHX_NEED(PH_EVALK2)) {
@@ -2478,7 +2624,7 @@ cudaError_t launch_engine(bool fp64, int grid, cudaStream_t s, const BatchDev& B
 void launch(KernelId id, int grid, cudaStream_t s, const BatchDev& B, bool fp64) {
   if (grid <= 0) return;
   switch (id) {
-    case K_ELEM_EG: k_elem_eg<<<grid, kTile, 0, s>>>(B); break;
+    case K_ELEM_EG: k_elem_eg<<<grid, kTile, 3 * kTileNodeCap * sizeof(double), s>>>(B); break;
     case K_GATHER: k_gather<<<grid, kTile, 0, s>>>(B); break;
     case K_ELEM_HESS:
       if (fp64) k_elem_hess<double><<<grid, kTile, hess_smem<double>(), s>>>(B);

@@ -110,6 +110,7 @@ bool build_pattern(const MeshIn& in, HostPattern& hp, std::string& err) {
   std::vector<char> used(n, 0);
   hp.rest64.resize(12 * (size_t)m);
   hp.rest32.resize(12 * (size_t)m);
+  hp.rest32lo.resize(12 * (size_t)m);
   hp.mass.assign(n, 0.0);
   for (int e = 0; e < m; ++e) {
     const int32_t* t = &hp.tets[4 * (size_t)e];
@@ -137,7 +138,11 @@ bool build_pattern(const MeshIn& in, HostPattern& hp, std::string& err) {
     R[9] = d / 6.0;  // quadrature weight (1/6) * det J (EnergyElement_FEM.cpp:87-91)
     R[10] = lam;
     R[11] = mu;
-    for (int k = 0; k < 12; ++k) hp.rest32[12 * (size_t)e + k] = (float)R[k];
+    for (int k = 0; k < 12; ++k) {
+      const float hi = (float)R[k];
+      hp.rest32[12 * (size_t)e + k] = hi;
+      hp.rest32lo[12 * (size_t)e + k] = (float)(R[k] - (double)hi);
+    }
     // MassElement_Lumped::ComputeAndStore_Mass: rho * V / 4 per node
     double me = rho * (d / 6.0) / 4.0;
     for (int a = 0; a < 4; ++a) hp.mass[t[a]] += me;
@@ -289,6 +294,33 @@ bool build_pattern(const MeshIn& in, HostPattern& hp, std::string& err) {
   if (hp.nslots >= (int64_t)2000000000) {
     err = "pattern: too many blocks for 32-bit slot ids";
     return false;
+  }
+  // ---- per-tile node lists (shared-memory staging of the element stages) ---
+  // Each tile of kTile consecutive tets lists its distinct nodes in ascending order (at most
+  // 4 kTile, so a corner's index fits 16 bits); the element kernels load these once per tile.
+  {
+    const int nt = (m + kTile - 1) / kTile;
+    hp.tile_nptr.assign(nt + 1, 0);
+    hp.tile_nodes.clear();
+    hp.tile_nodes.reserve((size_t)m);
+    hp.tet_loc.resize(4 * (size_t)m);
+    std::vector<int32_t> loc(n, -1), ids;
+    ids.reserve(4 * kTile);
+    for (int t = 0; t < nt; ++t) {
+      const int e0 = t * kTile, e1 = std::min(m, e0 + kTile);
+      ids.clear();
+      for (size_t q = 4 * (size_t)e0; q < 4 * (size_t)e1; ++q)
+        if (loc[hp.tets[q]] < 0) {
+          loc[hp.tets[q]] = 0;
+          ids.push_back(hp.tets[q]);
+        }
+      std::sort(ids.begin(), ids.end());
+      for (size_t k = 0; k < ids.size(); ++k) loc[ids[k]] = (int32_t)k;
+      for (size_t q = 4 * (size_t)e0; q < 4 * (size_t)e1; ++q) hp.tet_loc[q] = (uint16_t)loc[hp.tets[q]];
+      for (int32_t v : ids) loc[v] = -1;
+      hp.tile_nodes.insert(hp.tile_nodes.end(), ids.begin(), ids.end());
+      hp.tile_nptr[t + 1] = (int32_t)hp.tile_nodes.size();
+    }
   }
   // ---- boundary conditions ------------------------------------------------
   hp.fixmask.assign(n, 0);
