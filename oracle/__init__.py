@@ -36,7 +36,7 @@ class OrcOptions(C.Structure):
                 ("ls_num_reg_trials", C.c_int32), ("lsearch_type", C.c_int32),
                 ("lsearch_alpha", C.c_double), ("lsearch_num_try", C.c_int32),
                 ("lsearch_wolfe1", C.c_double), ("lsearch_wolfe2", C.c_double),
-                ("cg_block_jacobi", C.c_int32), ("threads", C.c_int32)]
+                ("cg_block_jacobi", C.c_int32), ("threads", C.c_int32), ("cg_parallel", C.c_int32)]
 
 
 class OrcStageGroup(C.Structure):

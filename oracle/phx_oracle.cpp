@@ -287,6 +287,12 @@ struct orc_handle_s {
   };
   std::vector<Group> groups;
   int num_stages = 0, stage = 0;
+
+  // cg_parallel: full rows of the lower pattern (built once), for the row-parallel CG
+  int cg_par = 0;
+  std::vector<int64_t> fr_ptr;
+  std::vector<int> fr_col;
+  std::vector<int64_t> fr_src;  // index of each row entry in the lower CSC values
 };
 
 namespace {
@@ -753,10 +759,80 @@ int solve_ldlt(orc_handle_s* h, std::vector<double>& A, const std::vector<double
   return 1;  // LSResult::FAILURE
 }
 
-// Jacobi / block-Jacobi preconditioned CG with Eigen's ConjugateGradient rules
+// Full rows of the symmetric matrix stored as its lower CSC: for each row, its columns in
+// ascending order and where each value sits in the lower CSC array.
+void full_rows(orc_handle_s* h) {
+  if (!h->fr_ptr.empty()) return;
+  const int N = h->N;
+  std::vector<int64_t> cnt(N + 1, 0);
+  for (int c = 0; c < N; ++c)
+    for (int q = h->colptr[c]; q < h->colptr[c + 1]; ++q) {
+      const int r = h->rowidx[q];
+      if (r < c) continue;
+      cnt[r + 1]++;
+      if (r != c) cnt[c + 1]++;
+    }
+  for (int i = 0; i < N; ++i) cnt[i + 1] += cnt[i];
+  h->fr_ptr = cnt;
+  h->fr_col.resize(cnt[N]);
+  h->fr_src.resize(cnt[N]);
+  std::vector<int64_t> pos(cnt.begin(), cnt.end() - 1);
+  // columns ascending per row: entries (r, c) with c < r come from columns c < r in order, then
+  // the diagonal, then the transposed entries (c, r) with r > c, in increasing row order
+  for (int c = 0; c < N; ++c)
+    for (int q = h->colptr[c]; q < h->colptr[c + 1]; ++q) {
+      const int r = h->rowidx[q];
+      if (r < c) continue;
+      if (r != c) { h->fr_col[pos[r]] = c; h->fr_src[pos[r]++] = q; }
+    }
+  for (int c = 0; c < N; ++c)
+    for (int q = h->colptr[c]; q < h->colptr[c + 1]; ++q) {
+      const int r = h->rowidx[q];
+      if (r < c) continue;
+      h->fr_col[pos[c]] = r;
+      h->fr_src[pos[c]++] = q;
+    }
+}
+
+// Inner product in fixed blocks of 4096 entries, block sums added in order: the same bits
+// for any number of threads.
+double dot_blocked(const double* a, const double* b, int N) {
+  const int nb = (N + 4095) / 4096;
+  std::vector<double> part(nb);
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < nb; ++k) {
+    double s = 0;
+    const int i1 = std::min(N, (k + 1) * 4096);
+    for (int i = k * 4096; i < i1; ++i) s += a[i] * b[i];
+    part[k] = s;
+  }
+  double s = 0;
+  for (double v : part) s += v;
+  return s;
+}
+
+// Jacobi / block-Jacobi preconditioned CG with Eigen's ConjugateGradient rules.  With
+// h->cg_par the products run row-parallel over full rows and the inner products in fixed
+// blocks (the same iteration, summed in another order; used for systems of millions of DoFs).
 int64_t pcg(const orc_handle_s* h, const std::vector<double>& A, const std::vector<double>& b,
             std::vector<double>& x, double tol, int maxIters, bool block) {
   int N = h->N;
+  const bool par = h->cg_par != 0;
+  auto mv = [&](const double* in, double* out) {
+    if (!par) { symv_lower(h, A.data(), in, out); return; }
+#pragma omp parallel for schedule(static, 1024)
+    for (int r = 0; r < N; ++r) {
+      double s = 0;
+      for (int64_t k = h->fr_ptr[r]; k < h->fr_ptr[r + 1]; ++k) s += A[h->fr_src[k]] * in[h->fr_col[k]];
+      out[r] = s;
+    }
+  };
+  auto dot = [&](const std::vector<double>& a, const std::vector<double>& c) {
+    if (par) return dot_blocked(a.data(), c.data(), N);
+    double s = 0;
+    for (int i = 0; i < N; ++i) s += a[i] * c[i];
+    return s;
+  };
   std::vector<double> inv(block ? (size_t)N * 3 : (size_t)N, 0.0);
   if (!block) {
     for (int c = 0; c < N; ++c) {
@@ -784,8 +860,10 @@ int64_t pcg(const orc_handle_s* h, const std::vector<double>& A, const std::vect
   }
   auto apply = [&](const std::vector<double>& r, std::vector<double>& z) {
     if (!block) {
+#pragma omp parallel for schedule(static) if (par)
       for (int i = 0; i < N; ++i) z[i] = inv[i] * r[i];
     } else {
+#pragma omp parallel for schedule(static) if (par)
       for (int v = 0; v < h->n; ++v)
         for (int a = 0; a < 3; ++a) {
           double s = 0;
@@ -795,33 +873,29 @@ int64_t pcg(const orc_handle_s* h, const std::vector<double>& A, const std::vect
     }
   };
   std::vector<double> r(N), z(N), p(N), q(N);
-  symv_lower(h, A.data(), x.data(), q.data());
+  mv(x.data(), q.data());
   for (int i = 0; i < N; ++i) r[i] = b[i] - q[i];
-  double rhs2 = 0;
-  for (int i = 0; i < N; ++i) rhs2 += b[i] * b[i];
+  double rhs2 = dot(b, b);
   if (rhs2 == 0) { std::fill(x.begin(), x.end(), 0.0); return 0; }
   double thr = std::max(tol * tol * rhs2, DBL_MIN);
-  double rr = 0;
-  for (int i = 0; i < N; ++i) rr += r[i] * r[i];
+  double rr = dot(r, r);
   if (rr < thr) return 0;
   apply(r, p);
-  double rz = 0;
-  for (int i = 0; i < N; ++i) rz += r[i] * p[i];
+  double rz = dot(r, p);
   int64_t it = 0;
   while (it < maxIters) {
-    symv_lower(h, A.data(), p.data(), q.data());
-    double pq = 0;
-    for (int i = 0; i < N; ++i) pq += p[i] * q[i];
+    mv(p.data(), q.data());
+    double pq = dot(p, q);
     double alpha = rz / pq;
+#pragma omp parallel for schedule(static) if (par)
     for (int i = 0; i < N; ++i) { x[i] += alpha * p[i]; r[i] -= alpha * q[i]; }
-    rr = 0;
-    for (int i = 0; i < N; ++i) rr += r[i] * r[i];
+    rr = dot(r, r);
     if (rr < thr) { ++it; break; }
     apply(r, z);
     double rzo = rz;
-    rz = 0;
-    for (int i = 0; i < N; ++i) rz += r[i] * z[i];
+    rz = dot(r, z);
     double beta = rz / rzo;
+#pragma omp parallel for schedule(static) if (par)
     for (int i = 0; i < N; ++i) p[i] = z[i] + beta * p[i];
     ++it;
   }
@@ -1186,6 +1260,7 @@ void orc_default_options(orc_options* o) {
   o->lsearch_wolfe2 = 0.9;
   o->cg_block_jacobi = 0;
   o->threads = 0;
+  o->cg_parallel = 0;
 }
 
 int orc_create(const orc_mesh* mesh, orc_handle* out) {
@@ -1278,6 +1353,8 @@ int orc_scatter_map(orc_handle h, int32_t* map) {
 }
 
 int orc_solve_static(orc_handle h, const orc_options* o, double* x, orc_report* rep) {
+  h->cg_par = o->cg_parallel;
+  if (h->cg_par) full_rows(h);
 #ifdef _OPENMP
   int saved = omp_get_max_threads();
   if (o->threads > 0) omp_set_num_threads(o->threads);
@@ -1295,6 +1372,8 @@ int orc_solve_static(orc_handle h, const orc_options* o, double* x, orc_report* 
 }
 
 int orc_solve_dynamic(orc_handle h, const orc_options* o, double dt, double* x, double* v, orc_report* rep) {
+  h->cg_par = o->cg_parallel;
+  if (h->cg_par) full_rows(h);
 #ifdef _OPENMP
   int saved = omp_get_max_threads();
   if (o->threads > 0) omp_set_num_threads(o->threads);
@@ -1316,6 +1395,8 @@ int orc_solve_dynamic(orc_handle h, const orc_options* o, double dt, double* x, 
 
 int orc_linear_solve(orc_handle h, const orc_options* o, const double* x, const double* b, double* dx,
                      int32_t* lsresult, int64_t* iters) {
+  h->cg_par = o->cg_parallel;
+  if (h->cg_par) full_rows(h);
   std::vector<double> H(h->rowidx.size());
   model_hessian(h, x, H.data(), true, nullptr);
   std::vector<double> bb(b, b + h->N), xs(dx, dx + h->N);

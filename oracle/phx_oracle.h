@@ -57,6 +57,7 @@ typedef struct orc_options {
   double lsearch_wolfe2;     /* Wolfe c2 */
   int32_t cg_block_jacobi;   /* CG preconditioner: 0 = diagonal (Eigen), 1 = 3x3 block Jacobi */
   int32_t threads;           /* OpenMP threads for element loops; <= 0 keeps the default */
+  int32_t cg_parallel;       /* 1: row-parallel CG products and blocked inner products (large systems) */
 } orc_options;
 
 typedef struct orc_report {

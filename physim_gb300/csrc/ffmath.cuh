@@ -137,8 +137,17 @@ __device__ __forceinline__ ff ff_det3(const ff* A) {
   return ff_add(ff_sub(ff_mul(A[0], m0), ff_mul(A[3], m1)), ff_mul(A[6], m2));
 }
 
-// returns false for an inverted element (j < -1); P is then not used
+// Returns false for an inverted element (J - 1 = j < -1, both models, as the FP64 kernels
+// test it); psi and P are then not set.
 __device__ __forceinline__ bool ff_material(int model, ff lam, ff mu, const ff* H, ff* psi, ff* P) {
+  const ff trH = ff_add(ff_add(H[0], H[4]), H[8]);
+  ff I2 = ff_sub(ff_mul(H[0], H[4]), ff_mul(H[3], H[1]));
+  I2 = ff_add(I2, ff_sub(ff_mul(H[0], H[8]), ff_mul(H[6], H[2])));
+  I2 = ff_add(I2, ff_sub(ff_mul(H[4], H[8]), ff_mul(H[7], H[5])));
+  const ff q = ff_add(I2, ff_det3(H));
+  const ff j = ff_add(trH, q);  // J - 1
+  // J = 0 exactly: inverted for CoNH (log J), a finite StVK energy, as in FP64
+  if (j.hi < -1.f || (j.hi == -1.f && (j.lo < 0.f || (j.lo == 0.f && model != 1)))) return false;
   ff F[9];
 #pragma unroll
   for (int k = 0; k < 9; ++k) F[k] = H[k];
@@ -176,13 +185,6 @@ __device__ __forceinline__ bool ff_material(int model, ff lam, ff mu, const ff* 
         P[i + 3 * jj] = ff_fma(F[i + 6], S[2 + 3 * jj], ff_fma(F[i + 3], S[1 + 3 * jj], ff_mul(F[i], S[3 * jj])));
     return true;
   }
-  const ff trH = ff_add(ff_add(H[0], H[4]), H[8]);
-  ff I2 = ff_sub(ff_mul(H[0], H[4]), ff_mul(H[3], H[1]));
-  I2 = ff_add(I2, ff_sub(ff_mul(H[0], H[8]), ff_mul(H[6], H[2])));
-  I2 = ff_add(I2, ff_sub(ff_mul(H[4], H[8]), ff_mul(H[7], H[5])));
-  const ff q = ff_add(I2, ff_det3(H));
-  const ff j = ff_add(trH, q);  // J - 1
-  if (j.hi < -1.f || (j.hi == -1.f && j.lo <= 0.f)) return false;
   ff hh = ff_sqr(H[0]);
 #pragma unroll
   for (int k = 1; k < 9; ++k) hh = ff_fma(H[k], H[k], hh);

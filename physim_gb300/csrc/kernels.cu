@@ -517,8 +517,39 @@ __device__ __forceinline__ int ff_stage_nodes(const InstDev& I, int lt, double* 
   return cnt;
 }
 
+// The gradient of an inverted element (+inf energy) in FP64, from the FP64 material law, so
+// that it has the FP64 kernels' values; out of line, as it is rare.
+__device__ __noinline__ void ff_inverted_grad(int model, const ff* R, const ff* Hd, float2* gout) {
+  float2 g[12];
+  double H[9], P[9], psi;
+  bool inverted;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) H[k] = ff_to_d(Hd[k]);
+  material_eg(model, ff_to_d(R[10]), ff_to_d(R[11]), H, &psi, P, &inverted);
+  double B[12];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) B[k] = ff_to_d(R[k]);
+  const double w = ff_to_d(R[9]);
+#pragma unroll
+  for (int a = 1; a < 4; ++a)
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      const ff v = ff_of_d((P[r] * B[(a - 1)] + P[r + 3] * B[(a - 1) + 3] + P[r + 6] * B[(a - 1) + 6]) * w);
+      g[3 * a + r] = make_float2(v.hi, v.lo);
+    }
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    const double b0 = -(B[0] + B[1] + B[2]), b1 = -(B[3] + B[4] + B[5]), b2 = -(B[6] + B[7] + B[8]);
+    const ff v = ff_of_d((P[r] * b0 + P[r + 3] * b1 + P[r + 6] * b2) * w);
+    g[r] = make_float2(v.hi, v.lo);
+  }
+  float4* go = reinterpret_cast<float4*>(gout);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) go[k] = make_float4(g[2 * k].x, g[2 * k].y, g[2 * k + 1].x, g[2 * k + 1].y);
+}
+
 // Energy (and, with grad, the gradient) of tet e from the staged displacements.  Returns the
-// energy; an inverted element (J <= 0) has +inf and a zero gradient.
+// energy; an inverted element (J - 1 < -1) has +inf and the FP64 kernels' gradient.
 __device__ __forceinline__ double ff_element(const InstDev& I, int e, const double* U, bool grad, float2* gout) {
   const ushort4 lc = reinterpret_cast<const ushort4*>(I.tet_loc)[e];
   const int loc[4] = {lc.x, lc.y, lc.z, lc.w};
@@ -550,9 +581,10 @@ __device__ __forceinline__ double ff_element(const InstDev& I, int e, const doub
   const ff w = R[9];
   ff psi, P[9];
   const bool ok = ff_material(I.model[e], R[10], R[11], Hd, &psi, P);
-  if (grad) {
+  if (grad && !ok) ff_inverted_grad(I.model[e], R, Hd, gout);
+  if (grad && ok) {
     float2 g[12];
-    if (ok) {
+    {
       // g_a = w P B_a, B_a = row (a-1) of Dm^-1, B_0 = -(B_1 + B_2 + B_3)
       const ff b0 = ff_neg(ff_add(ff_add(R[0], R[1]), R[2])), b1 = ff_neg(ff_add(ff_add(R[3], R[4]), R[5]));
       const ff b2 = ff_neg(ff_add(ff_add(R[6], R[7]), R[8]));
@@ -567,9 +599,6 @@ __device__ __forceinline__ double ff_element(const InstDev& I, int e, const doub
           g[3 * a + r] = make_float2(va.hi, va.lo);
         }
       }
-    } else {
-#pragma unroll
-      for (int k = 0; k < 12; ++k) g[k] = make_float2(0.f, 0.f);
     }
     float4* go = reinterpret_cast<float4*>(gout);
 #pragma unroll

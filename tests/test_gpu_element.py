@@ -60,9 +60,12 @@ def test_element_local_served_double_float(gpu_ctx, name, scale):
         return
     x = perturbed(m, scale, seed=6)
     Eo, go, _ = orc.element_local(x)
+    inv = np.isinf(Eo)  # inverted elements (at scale 0.3): +inf in both, FP64 gradients
+    assert inv.any() == (scale == 0.3)
     for xx in (x, x + np.tile([1.0, -1.0, 1.0], m.n)):
         E, g, _ = inst.element_local(xx, px.PREC_FP32_REFINE)
-        assert np.max(np.abs(E - Eo) / np.maximum(np.abs(Eo), 1e-300)) < 1e-11
+        assert np.array_equal(np.isinf(E), inv) and np.all(E[inv] > 0)
+        assert np.max(np.abs(E[~inv] - Eo[~inv]) / np.maximum(np.abs(Eo[~inv]), 1e-300)) < 1e-11
         assert np.max(np.abs(g - go)) <= 1e-11 * np.abs(go).max()
 
 

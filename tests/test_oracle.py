@@ -214,6 +214,24 @@ def test_ldlt_and_cg_agree():
     assert rel(xc - x0, xl - x0) < 1e-8
 
 
+def test_parallel_cg_matches_serial_cg():
+    """The row-parallel CG (full rows, blocked inner products) runs the same iteration as the
+    serial one in another summation order: the same Newton path to the CG tolerance's scale,
+    and the same bits for any thread count."""
+    m = M.cantilever(3, 3, 10)
+    o = oracle.Oracle(m)
+    x0 = o.rest()
+    g0 = np.linalg.norm(o.gradient(x0))
+    kw = dict(tol_max_error=1e-9 * g0, tol_min_impr=0.0, tol_min_step=0.0, ls_solver=1, ls_tol_max_error=1e-10)
+    xs, rs = o.solve_static(x0, **kw)
+    xp, rp = o.solve_static(x0, cg_parallel=1, threads=4, **kw)
+    xq, rq = o.solve_static(x0, cg_parallel=1, threads=1, **kw)
+    assert rs["result_name"] == rp["result_name"] == "SUCCESS"
+    assert rel(xp - x0, xs - x0) < 1e-8
+    assert abs(rp["lin_iterations"] - rs["lin_iterations"]) <= 0.02 * rs["lin_iterations"] + 2
+    assert np.array_equal(xp, xq) and rp["lin_iterations"] == rq["lin_iterations"]
+
+
 def test_dynamic_step_conserves_at_rest():
     # no load, no velocity: the implicit step must keep the rest state
     m = M.make_box(2, 2, 2, (0.02, 0.02, 0.02), 1e5, 0.3, clamp_face=2)
