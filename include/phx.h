@@ -163,6 +163,37 @@ int phx_context_memory(phx_context ctx, int64_t* used_bytes, int64_t* capacity_b
  * the default limit (4e9 cycles, about 2 s). */
 int phx_debug_unmet_barrier(phx_context ctx, int32_t barrier_tag, int64_t limit_cycles);
 
+/* ---- launch settings and the batch tuner (no counterpart in the reference) -----------
+ * How a context schedules its batch solves.  None of them changes a result: every instance
+ * runs the same state machine whatever the schedule (a batch solve gives the bits of solving
+ * each instance alone).
+ *   graph        1: the solve loop runs as CUDA-graph launches (a device while-loop of
+ *                k_prep, the engine, the cluster PCG kernels and the loop test; the host
+ *                looks in every 256 passes); 0: one host step per engine launch.
+ *                Profiling (phx_context_profile) always takes the host loop.
+ *   wait_rounds  engine rounds an instance may wait for the cluster PCG kernel ...
+ *   wait_share   ... or until 1/wait_share of the active instances wait for it
+ *   rounds       engine rounds per engine launch */
+typedef struct phx_launch_settings {
+  int32_t graph;
+  int32_t wait_rounds;
+  int32_t wait_share;
+  int32_t rounds;
+} phx_launch_settings;
+/* Reads the context's default settings into *get (if not NULL), then sets them from *set (if
+ * not NULL; values checked: graph 0/1, wait_rounds 1..64, wait_share 1..64, rounds 1..1024). */
+int phx_context_launch_settings(phx_context ctx, phx_launch_settings* get, const phx_launch_settings* set);
+/* Tunes the settings for a batch: times phx_batch_solve-style solves of the instances from
+ * their current positions under the default settings and candidates around them (one
+ * setting changed at a time, kept when at least 1 % faster), then puts the instances back as
+ * they were (positions and warm-start steps).  The best settings are cached under the
+ * batch's mix key (precision and the count of instances per power-of-two node-count bucket):
+ * later batch solves of the context with that key use them.  Instances with staged boundary
+ * conditions are refused (a trial would advance their stages).  chosen, default_seconds,
+ * best_seconds and trials may be NULL. */
+int phx_tune_batch(phx_context ctx, int32_t count, phx_instance* insts, const phx_options* opts,
+                   phx_launch_settings* chosen, double* default_seconds, double* best_seconds, int32_t* trials);
+
 /* ---- instances: Simulable_FEM set-up (replaces Simulable::Setup + the first
  * triplet assembly that fixes the Hessian pattern, source/PhySim/BasicTypes.cpp:118-145).
  * Validates the mesh (PHX_EINVAL on bad ids or non-positive rest volume),
@@ -254,9 +285,8 @@ int phx_hessian_pattern(phx_instance inst, int32_t* colptr /* 3n+1 */, int32_t* 
  * of every tet, blocks counted column-major over the pattern (DerivativeAssembler.cpp:205-300). */
 int phx_scatter_map(phx_instance inst, int32_t* map /* 10*num_tets */);
 /* Per-element values (IEnergyElement::GetLocal*, EnergyElement_FEM.cpp:125-222):
- * E[m], g[12m], H[144m] row-major 12x12; any output may be NULL.  PHX_PREC_FP64: FP64
- * elements.  PHX_PREC_FP32_REFINE: the served path's elements (energy and gradient in
- * double-float on the FP32 pipe, about 1e-12 relative; Hessian in FP32). */
+ * E[m], g[12m], H[144m] row-major 12x12; any output may be NULL.  Energy and gradient are
+ * FP64 on both paths; precision selects the Hessian kernel (PHX_PREC_FP32_REFINE: FP32). */
 int phx_element_local(phx_instance inst, const double* x, int32_t precision, double* E, double* g, double* H);
 
 /* ---- solver (IOptimSolver::SolveFull / SolveStep, OptimSolver.cpp:148-311,

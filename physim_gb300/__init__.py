@@ -35,7 +35,7 @@ EXPORTS = [
     "phx_server_submit", "phx_server_submit_step", "phx_server_submit_mesh", "phx_server_stats",
     "phx_server_progress", "phx_server_poll", "phx_profile_enable", "phx_profile_read",
     "phx_profile_reset", "phx_profile_bytes", "phx_kernel_launches", "phx_timer_mark", "phx_timer_elapsed",
-    "phx_hessian_blocks_noalloc", "phx_debug_unmet_barrier",
+    "phx_hessian_blocks_noalloc", "phx_debug_unmet_barrier", "phx_context_launch_settings", "phx_tune_batch",
     "phx_scene_load", "phx_scene_destroy", "phx_scene_info", "phx_scene_mesh", "phx_scene_options",
     "phx_scene_staging", "phx_scene_instance",
 ]
@@ -52,6 +52,14 @@ class Mesh_(C.Structure):
                 ("lame", C.c_void_p), ("rho", C.c_void_p), ("model", C.c_void_p), ("fixed", C.c_void_p),
                 ("force", C.c_void_p), ("gravity", C.c_double * 3), ("soft_k", C.c_void_p),
                 ("soft_target", C.c_void_p)]
+
+
+class LaunchSettings_(C.Structure):
+    """phx_launch_settings: scheduling of a context's batch solves (changes no result)."""
+    _fields_ = [("graph", C.c_int32), ("wait_rounds", C.c_int32), ("wait_share", C.c_int32), ("rounds", C.c_int32)]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
 
 
 class Options(C.Structure):
@@ -147,6 +155,9 @@ def lib():
         "phx_timer_elapsed": ([vp, i32, i32, C.POINTER(dbl)], C.c_int),
         "phx_hessian_blocks_noalloc": ([i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp], C.c_int),
         "phx_debug_unmet_barrier": ([vp, i32, i64], C.c_int),
+        "phx_context_launch_settings": ([vp, C.POINTER(LaunchSettings_), C.POINTER(LaunchSettings_)], C.c_int),
+        "phx_tune_batch": ([vp, i32, vp, C.POINTER(Options), C.POINTER(LaunchSettings_), C.POINTER(dbl),
+                            C.POINTER(dbl), C.POINTER(i32)], C.c_int),
         "phx_scene_load": ([C.c_char_p, C.POINTER(vp)], C.c_int),
         "phx_scene_destroy": ([vp], C.c_int),
         "phx_scene_info": ([vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), C.POINTER(dbl), C.POINTER(i32),
@@ -232,6 +243,28 @@ class Context:
         """Test hook: engine grid barrier `tag` waits for an arrival that never comes and gives
         up after limit_cycles (tag 0: off)."""
         _check(lib().phx_debug_unmet_barrier(self.h, int(tag), int(limit_cycles)))
+
+    def launch_settings(self, **changes) -> dict:
+        """The context's default launch settings (graph, wait_rounds, wait_share, rounds); keyword
+        arguments change them.  Returns the settings in force after the call."""
+        cur = LaunchSettings_()
+        _check(lib().phx_context_launch_settings(self.h, C.byref(cur), None))
+        if changes:
+            for k, v in changes.items():
+                if k not in cur.as_dict():
+                    raise KeyError(k)
+                setattr(cur, k, int(v))
+            _check(lib().phx_context_launch_settings(self.h, None, C.byref(cur)))
+        return cur.as_dict()
+
+    def tune_batch(self, insts: Sequence["Instance"], opts: "Options") -> dict:
+        """Tunes the launch settings for this batch (cached under its mix key); the instances are
+        left as they were.  Returns the chosen settings, the default and best batch times."""
+        n = len(insts)
+        arr = (C.c_void_p * n)(*[i.h.value for i in insts])
+        ch, td, tb, nt = LaunchSettings_(), C.c_double(), C.c_double(), C.c_int32()
+        _check(lib().phx_tune_batch(self.h, n, arr, C.byref(opts), C.byref(ch), C.byref(td), C.byref(tb), C.byref(nt)))
+        return {"chosen": ch.as_dict(), "default_seconds": td.value, "best_seconds": tb.value, "trials": nt.value}
 
     def kernel_launches(self) -> int:
         return int(lib().phx_kernel_launches(self.h))

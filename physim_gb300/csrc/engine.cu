@@ -163,12 +163,21 @@ struct phx_context_s {
   int act_cap = 0;
   unsigned long long* d_stage = nullptr;  // [32] stage ns + executions (profiling)
   int egrid[2] = {0, 0};
-  int32_t* d_clist = nullptr;  // instances waiting for a cluster PCG solve this step (uploaded per step)
-  int32_t* h_wait = nullptr;   // pinned staging of that list
-  int clist_cap = 0;
-  std::vector<int32_t> h_clist;  // instances whose PCG runs per cluster, largest first
-  std::vector<int32_t> h_kind;   // their PCG kind, by batch position
-  int clist_kinds = 0;  // bit k: the cluster list holds instances of PCG kind k
+  // cluster PCG: the batch's cluster instances (largest first) and the waiting lists the
+  // engine writes for the cluster kernels
+  int32_t* d_corder = nullptr;  // [cap]
+  int32_t* d_wait = nullptr;    // [4 + 2 cap]
+  int32_t* d_cfg = nullptr;     // [4]: [0] PCG tile width (k_prep), [1] graph loop passes
+  int ccount = 0;               // cluster instances in the batch
+  int ckind_count[3] = {0, 0, 0};  // ... of each PCG kind (1, 2)
+  int gmax[3] = {-1, -1, -1};   // clusters of each kind resident at once (-1: not queried yet)
+  // scheduling of batch solves (defaults, and tuned settings per batch mix)
+  phx_launch_settings launch{1, kWaitRounds, kWaitShare, kRoundsPerLaunch};
+  std::map<std::string, phx_launch_settings> tuned;
+  // the whole solve loop as one graph, kept while the batch and launch parameters stay the same
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  std::string gkey;
   long long wait_limit = kBarrierLimit;  // grid-barrier wait limit of the engine (SM cycles)
   int unmet_tag = 0;                     // test hook: grid barrier that waits for an arrival never made
 };
@@ -353,6 +362,12 @@ int ensure_batch_cap(phx_context ctx, int num) {
   CU(cudaMalloc(&ctx->d_pre, sizeof(int32_t) * (3 * (cap + 1) + 1)));
   CU(cudaMalloc(&ctx->d_flags, sizeof(int32_t) * (8 + cap)));
   CU(cudaMallocHost(&ctx->h_flags, sizeof(int32_t) * (8 + cap)));
+  if (ctx->d_corder) cudaFree(ctx->d_corder);
+  if (ctx->d_wait) cudaFree(ctx->d_wait);
+  ctx->d_corder = nullptr; ctx->d_wait = nullptr;
+  CU(cudaMalloc(&ctx->d_corder, sizeof(int32_t) * cap));
+  CU(cudaMalloc(&ctx->d_wait, sizeof(int32_t) * (4 + 2 * cap)));
+  CU(cudaMemsetAsync(ctx->d_wait, 0, sizeof(int32_t) * 4, ctx->stream));
   ctx->cap = cap;
   if (!ctx->d_phc) {
     CU(cudaMalloc(&ctx->d_phc, sizeof(int32_t) * 32));
@@ -389,7 +404,10 @@ int set_batch(phx_context ctx, const std::vector<phx_instance>& list, BatchDev& 
   B.pre_lob = ctx->d_pre + 2 * (ctx->cap + 1);
   B.inst = ctx->d_inst;
   B.flags = ctx->d_flags;
-  CU(cudaMemsetAsync(ctx->d_flags, 0, sizeof(int32_t) * 8, ctx->stream));  // [2]: cluster PCG wait gave up
+  // [0]: active instances (the batch size until the engine has run), [2]: a cluster PCG wait
+  // gave up, [4], [5]: instances waiting for each cluster PCG kind
+  const int32_t hdr[8] = {num, 0, 0, 0, 0, 0, 0, 0};
+  CU(cudaMemcpyAsync(ctx->d_flags, hdr, sizeof(hdr), cudaMemcpyHostToDevice, ctx->stream));
   B.phase_live = ctx->d_phc;
   B.algo_total = ctx->profiling ? ctx->d_algo : nullptr;
   B.cpt = 4;
@@ -556,6 +574,10 @@ void fill_report_finished(const NState& a, const NState& b, double seconds, phx_
 
 int ensure_engine(phx_context ctx) {
   if (!ctx->d_bar) CU(cudaMalloc(&ctx->d_bar, 2 * sizeof(GridBar)));
+  if (!ctx->d_cfg) {
+    CU(cudaMalloc(&ctx->d_cfg, 4 * sizeof(int32_t)));
+    CU(cudaMemsetAsync(ctx->d_cfg, 0, 4 * sizeof(int32_t), ctx->stream));
+  }
   if (ctx->act_cap < ctx->cap) {
     if (ctx->d_act) cudaFree(ctx->d_act);
     ctx->d_act = nullptr;
@@ -582,21 +604,45 @@ int profile_events(phx_context ctx, cudaEvent_t* a, cudaEvent_t* b) {
   return PHX_OK;
 }
 
+int engine_grid_of(phx_context ctx, bool fp64, int* grid) {
+  int& g = ctx->egrid[fp64 ? 1 : 0];
+  if (g == 0) g = engine_grid(fp64, ctx->num_sms);
+  if (g <= 0) return set_err(PHX_ECUDA, "engine kernel cannot be made resident");
+  *grid = g;
+  return PHX_OK;
+}
+
+EngineArgs engine_args(phx_context ctx, const phx_launch_settings& S, int pcg_chunk) {
+  EngineArgs A{};
+  A.bar = ctx->d_bar;
+  A.act = ctx->d_act;
+  A.stage_ns = ctx->profiling ? ctx->d_stage : nullptr;
+  A.cap = ctx->cap;
+  A.rounds = S.rounds;
+  A.pcg_chunk = pcg_chunk;
+  A.wait_rounds = S.wait_rounds;
+  A.wait_share = S.wait_share;
+  A.wait_limit = ctx->wait_limit;
+  A.unmet_tag = ctx->unmet_tag;
+  A.cfg = ctx->d_cfg;
+  A.corder = ctx->d_corder;
+  A.ccount = ctx->ccount;
+  A.wait = ctx->d_wait;
+  return A;
+}
+
 // One cooperative launch of the engine: up to `rounds` Newton rounds over the batch.
-int run_engine(phx_context ctx, const BatchDev& B, int num, bool fp64, int rounds, int pcg_chunk) {
+int run_engine(phx_context ctx, const BatchDev& B, int num, bool fp64, const phx_launch_settings& S, int pcg_chunk,
+               int max_chunks) {
   TRY(ensure_engine(ctx));
-  int& grid = ctx->egrid[fp64 ? 1 : 0];
-  if (grid == 0) grid = engine_grid(fp64, ctx->num_sms);
-  if (grid <= 0) return set_err(PHX_ECUDA, "engine kernel cannot be made resident");
-  CU(cudaMemsetAsync(ctx->d_bar, 0, 2 * sizeof(GridBar), ctx->stream));
-  const int32_t hdr[2] = {0, grid};  // active count (set by the kernel), CTAs running
-  CU(cudaMemcpyAsync(ctx->d_act, hdr, sizeof(hdr), cudaMemcpyHostToDevice, ctx->stream));
-  EngineArgs A{ctx->d_bar, ctx->d_act, ctx->profiling ? ctx->d_stage : nullptr, ctx->cap, rounds, pcg_chunk,
-               kWaitRounds, kWaitShare, ctx->wait_limit, ctx->unmet_tag};
+  int grid;
+  TRY(engine_grid_of(ctx, fp64, &grid));
+  const EngineArgs A = engine_args(ctx, S, pcg_chunk);
+  CU(launch_prep(ctx->stream, B, A, grid, max_chunks));
   cudaEvent_t a = nullptr, b = nullptr;
   if (ctx->profiling) TRY(profile_events(ctx, &a, &b));
   CU(launch_engine(fp64, grid, ctx->stream, B, A));
-  ctx->launches++;
+  ctx->launches += 2;
   if (ctx->profiling) {
     cudaEventRecord(b, ctx->stream);
     ctx->evs.push_back({(int)K_ENGINE, a, b});
@@ -611,28 +657,27 @@ int run_engine(phx_context ctx, const BatchDev& B, int num, bool fp64, int round
 }
 
 // Uploads the batch positions of the instances whose PCG runs per cluster, largest first.
+// Uploads the batch positions of the instances whose PCG runs per cluster, largest first (the
+// order in which the engine lists them for the cluster kernels).
 int set_cluster_list(phx_context ctx, const std::vector<phx_instance>& list, int* count) {
   std::vector<int32_t> ids;
   for (int i = 0; i < (int)list.size(); ++i)
     if (list[i]->dev.pcg_cluster) ids.push_back(i);
   std::stable_sort(ids.begin(), ids.end(), [&](int a, int b) { return list[a]->dev.nslots > list[b]->dev.nslots; });
-  ctx->clist_kinds = 0;
-  for (int id : ids) ctx->clist_kinds |= 1 << list[id]->dev.pcg_cluster;
   *count = (int)ids.size();
-  ctx->h_clist = ids;
-  ctx->h_kind.assign(list.size(), 0);
-  for (int i = 0; i < (int)list.size(); ++i) ctx->h_kind[i] = list[i]->dev.pcg_cluster;
-  if (ids.empty()) return PHX_OK;
-  if (ctx->clist_cap < (int)ids.size()) {
-    if (ctx->d_clist) cudaFree(ctx->d_clist);
-    if (ctx->h_wait) cudaFreeHost(ctx->h_wait);
-    ctx->d_clist = nullptr;
-    ctx->h_wait = nullptr;
-    CU(cudaMalloc(&ctx->d_clist, sizeof(int32_t) * ids.size()));
-    CU(cudaMallocHost(&ctx->h_wait, sizeof(int32_t) * ids.size()));
-    ctx->clist_cap = (int)ids.size();
-  }
+  ctx->ccount = (int)ids.size();
+  for (int k = 0; k < 3; ++k) ctx->ckind_count[k] = 0;
+  for (int id : ids) ctx->ckind_count[list[id]->dev.pcg_cluster]++;
+  if (!ids.empty())  // pageable source: copied before the call returns
+    CU(cudaMemcpyAsync(ctx->d_corder, ids.data(), sizeof(int32_t) * ids.size(), cudaMemcpyHostToDevice, ctx->stream));
   return PHX_OK;
+}
+
+// Clusters to launch for `waiting` instances of PCG kind `kind`: one per instance, at most as
+// many as are resident at once (each cluster takes instances from the list until none is left).
+int cluster_count(phx_context ctx, int kind, int waiting) {
+  if (ctx->gmax[kind] < 0) ctx->gmax[kind] = max_active_clusters(kind);
+  return ctx->gmax[kind] > 0 ? std::min(waiting, ctx->gmax[kind]) : waiting;
 }
 
 // One step of the device engine: engine rounds, then (if any) the per-cluster PCG solves.
@@ -641,28 +686,23 @@ int set_cluster_list(phx_context ctx, const std::vector<phx_instance>& list, int
 // the rest iterate on the whole GPU, with one-chunk tiles while few small instances
 // remain so that a lone instance spreads over more SMs.
 int run_step(phx_context ctx, const BatchDev& B0, int num, bool fp64, int pcg_chunk, int ccount, int active,
-             int max_chunks) {
+             int max_chunks, const phx_launch_settings& S) {
   BatchDev B = B0;
-  const bool few = active <= kClWideBelow;
+  (void)active;
   B.cluster_mode = ccount > 0 ? 1 : 0;
-  // one-chunk tiles only while few, small instances remain (a large one would pay for
-  // thousands of per-tile reductions on its counter)
-  B.cpt = (few && max_chunks <= 2048) ? 1 : 4;
-  TRY(run_engine(ctx, B, num, fp64, kRoundsPerLaunch, pcg_chunk));
+  // (the engine takes its PCG tile width from k_prep: one-chunk tiles only while few, small
+  // instances remain, as a large one would pay for thousands of per-tile reductions)
+  TRY(run_engine(ctx, B, num, fp64, S, pcg_chunk, max_chunks));
   if (ctx->h_flags[2]) return set_err(PHX_ETIMEOUT, "cluster PCG reduction wait timed out");
   if (B.cluster_mode && ctx->h_flags[0] > 0 && ctx->h_flags[1] > 0) {
     cudaEvent_t a = nullptr, b = nullptr;
     if (ctx->profiling) TRY(profile_events(ctx, &a, &b));
-    // one cluster per waiting instance, largest first (the flags hold every instance's phase
-    // after the engine launch): no clusters are launched only to find nothing to do
+    // the engine listed the waiting instances of each kind, largest first; the clusters take
+    // them from the list in that order
     for (int kind = 1; kind <= 2; ++kind) {
-      if (!(ctx->clist_kinds & (1 << kind))) continue;
-      int nw = 0;
-      for (int32_t id : ctx->h_clist)
-        if (ctx->h_flags[8 + id] == PH_PCG && ctx->h_kind[id] == kind) ctx->h_wait[nw++] = id;
+      const int nw = ctx->h_flags[3 + kind];
       if (nw == 0) continue;
-      CU(cudaMemcpyAsync(ctx->d_clist, ctx->h_wait, sizeof(int32_t) * nw, cudaMemcpyHostToDevice, ctx->stream));
-      CU(launch_pcg_cluster(ctx->stream, B, ctx->d_clist, nw, kind));
+      CU(launch_pcg_cluster(ctx->stream, B, ctx->d_wait, ctx->cap, cluster_count(ctx, kind, nw), kind));
       ctx->launches++;
     }
     if (ctx->profiling) {
@@ -673,8 +713,82 @@ int run_step(phx_context ctx, const BatchDev& B0, int num, bool fp64, int pcg_ch
   return PHX_OK;
 }
 
-// Runs a set of instances (states already reset to PH_START) until all are done.
-int run_to_completion(phx_context ctx, const std::vector<phx_instance>& list, bool fp64, int pcg_chunk) {
+// The solve loop as graph launches: each launch runs up to kGraphPasses passes of k_prep, the
+// engine, the cluster PCG kernels and k_loop_end on the device, with no host step between them;
+// the host checks the outcome (and the time limit) between launches.
+constexpr int kGraphPasses = 256;
+
+int run_graph(phx_context ctx, const BatchDev& B0, int num, bool fp64, int pcg_chunk, int max_chunks,
+              const phx_launch_settings& S, clk::time_point t0) {
+  TRY(ensure_engine(ctx));
+  int grid;
+  TRY(engine_grid_of(ctx, fp64, &grid));
+  BatchDev B = B0;
+  B.cluster_mode = ctx->ccount > 0 ? 1 : 0;
+  const EngineArgs A = engine_args(ctx, S, pcg_chunk);
+  int clusters[2] = {0, 0};
+  for (int kind = 1; kind <= 2; ++kind)
+    if (B.cluster_mode && ctx->ckind_count[kind] > 0) clusters[kind - 1] = cluster_count(ctx, kind, ctx->ckind_count[kind]);
+  // the graph holds its kernels' arguments: rebuilt when any of them changes
+  std::string key;
+  auto put = [&](const void* p, size_t n) { key.append(static_cast<const char*>(p), n); };
+  put(&fp64, sizeof(fp64)); put(&grid, sizeof(grid)); put(&B, sizeof(B)); put(&A, sizeof(A));
+  put(&max_chunks, sizeof(max_chunks)); put(clusters, sizeof(clusters));
+  if (!ctx->gexec || key != ctx->gkey) {
+    if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+    if (ctx->graph) cudaGraphDestroy(ctx->graph);
+    ctx->gexec = nullptr;
+    ctx->graph = nullptr;
+    ctx->gkey.clear();
+    CU(build_solve_graph(fp64, grid, B, A, max_chunks, clusters, ctx->d_cfg + 1, kGraphPasses, &ctx->graph,
+                         &ctx->gexec));
+    ctx->gkey = key;
+  }
+  const int per_pass = 3 + (clusters[0] > 0) + (clusters[1] > 0);
+  for (;;) {
+    CU(cudaMemsetAsync(ctx->d_cfg + 1, 0, sizeof(int32_t), ctx->stream));
+    CU(cudaGraphLaunch(ctx->gexec, ctx->stream));
+    GridBar hb[2];
+    int32_t passes = 0;
+    CU(cudaMemcpyAsync(hb, ctx->d_bar, 2 * sizeof(GridBar), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaMemcpyAsync(&passes, ctx->d_cfg + 1, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    TRY(read_flags(ctx, num));
+    ctx->launches += (int64_t)passes * per_pass;
+    if (hb[0].err || hb[1].err)
+      return set_err(PHX_ETIMEOUT, "engine grid barrier timed out (stage " +
+                                       std::to_string(hb[1].err ? hb[1].stage : hb[0].stage) + ")");
+    if (ctx->h_flags[2]) return set_err(PHX_ETIMEOUT, "cluster PCG reduction wait timed out");
+    if (ctx->h_flags[0] == 0) return PHX_OK;
+    if (std::chrono::duration<double>(clk::now() - t0).count() > kSolveTimeLimit)
+      return set_err(PHX_ETIMEOUT, "solver did not finish within " + std::to_string(kSolveTimeLimit) + " s");
+  }
+}
+
+// Batch mix key of the tuned-settings cache: precision, then instances per power-of-two
+// node-count bucket.
+std::string mix_key(const std::vector<phx_instance>& list, bool fp64) {
+  std::map<int, int> buckets;
+  for (auto* in : list) {
+    int b = 0;
+    while ((1 << (b + 1)) <= in->dev.n && b < 30) ++b;
+    buckets[b]++;
+  }
+  std::string k = fp64 ? "f64" : "f32";
+  for (auto& kv : buckets) k += "|" + std::to_string(kv.first) + ":" + std::to_string(kv.second);
+  return k;
+}
+
+// Runs a set of instances (states already reset to PH_START) until all are done, with the
+// given launch settings, else those tuned for the batch's mix, else the context's defaults.
+int run_to_completion(phx_context ctx, const std::vector<phx_instance>& list, bool fp64, int pcg_chunk,
+                      const phx_launch_settings* force = nullptr) {
+  phx_launch_settings S = ctx->launch;
+  if (force) {
+    S = *force;
+  } else if (!ctx->tuned.empty()) {
+    auto it = ctx->tuned.find(mix_key(list, fp64));
+    if (it != ctx->tuned.end()) S = it->second;
+  }
   BatchDev B{};
   Grids G;
   TRY(set_batch(ctx, list, B, G));
@@ -684,8 +798,10 @@ int run_to_completion(phx_context ctx, const std::vector<phx_instance>& list, bo
   const auto t0 = clk::now();
   int active = num, max_chunks = 0;
   for (auto* in : list) max_chunks = std::max(max_chunks, in->dev.nchunks);
+  // per-launch timing events need the host between launches: profiling runs the host loop
+  if (S.graph && !ctx->profiling) return run_graph(ctx, B, num, fp64, pcg_chunk, max_chunks, S, t0);
   for (int64_t r = 0;; ++r) {
-    TRY(run_step(ctx, B, num, fp64, pcg_chunk, ccount, active, max_chunks));
+    TRY(run_step(ctx, B, num, fp64, pcg_chunk, ccount, active, max_chunks, S));
     active = ctx->h_flags[0];
     if (active == 0) return PHX_OK;
     if (std::chrono::duration<double>(clk::now() - t0).count() > kSolveTimeLimit)
@@ -855,8 +971,11 @@ int phx_context_destroy(phx_context ctx) {
   if (ctx->d_phc) cudaFree(ctx->d_phc);
   if (ctx->d_act) cudaFree(ctx->d_act);
   if (ctx->d_stage) cudaFree(ctx->d_stage);
-  if (ctx->d_clist) cudaFree(ctx->d_clist);
-  if (ctx->h_wait) cudaFreeHost(ctx->h_wait);
+  if (ctx->d_corder) cudaFree(ctx->d_corder);
+  if (ctx->d_wait) cudaFree(ctx->d_wait);
+  if (ctx->d_cfg) cudaFree(ctx->d_cfg);
+  if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+  if (ctx->graph) cudaGraphDestroy(ctx->graph);
   for (auto& ev : ctx->marks)
     if (ev) cudaEventDestroy(ev);
   ctx->arena.release();
@@ -927,7 +1046,7 @@ bool instance_build_host(const phx_mesh* mesh, phx_instance_s* inst, std::string
 int64_t device_bytes(const HostPattern& hp, bool fp32, bool fp64) {
   const size_t n = hp.n, m = hp.m, n4 = 4 * n;
   int64_t b = arena_bytes_of(hp.tets.size(), 4) + arena_bytes_of(hp.rest64.size(), 8) +
-              arena_bytes_of(hp.rest32.size(), 4) + arena_bytes_of(hp.rest32lo.size(), 4) +
+              arena_bytes_of(hp.rest32.size(), 4) +
               arena_bytes_of(hp.tile_nptr.size(), 4) + arena_bytes_of(hp.tile_nodes.size(), 4) +
               arena_bytes_of(hp.tet_loc.size(), 2) + arena_bytes_of(hp.model.size(), 1) +
               arena_bytes_of(hp.chunk_off.size(), 4) + arena_bytes_of(hp.slot_col.size(), 4) +
@@ -987,7 +1106,6 @@ int instance_setup_device(phx_context ctx, const phx_mesh* mesh, phx_instance_s*
   UP(tets, hp.tets);
   UP(rest64, hp.rest64);
   UP(rest32, hp.rest32);
-  UP(rest32lo, hp.rest32lo);
   UP(tile_nptr, hp.tile_nptr);
   UP(tile_nodes, hp.tile_nodes);
   UP(tet_loc, hp.tet_loc);
@@ -1032,7 +1150,6 @@ int instance_setup_device(phx_context ctx, const phx_mesh* mesh, phx_instance_s*
   // keep only what later calls need on the host
   hp.rest64.clear(); hp.rest64.shrink_to_fit();
   hp.rest32.clear(); hp.rest32.shrink_to_fit();
-  hp.rest32lo.clear(); hp.rest32lo.shrink_to_fit();
   hp.tile_nodes.clear(); hp.tile_nodes.shrink_to_fit();
   hp.tet_loc.clear(); hp.tet_loc.shrink_to_fit();
   hp.seg_c.clear(); hp.seg_c.shrink_to_fit();
@@ -1404,12 +1521,10 @@ int run_kernels(phx_instance inst, const std::vector<KernelId>& ids, bool fp64) 
   return PHX_OK;
 }
 
-// Energy and gradient at x: FP64 elements (served = false) or the served path's double-float
-// elements, whose per-element gradients are left as (hi, lo) float pairs.
-int eval_eg(phx_instance inst, const double* x, int nofix, NState* s, bool served = false) {
+int eval_eg(phx_instance inst, const double* x, int nofix, NState* s) {
   if (x) TRY(upload_x(inst, x, inst->dev.x));
   DevOpts d{};
-  d.precision = served ? 1 : 0;
+  d.precision = 0;
   CU(cudaMemcpyAsync(inst->d_opts, &d, sizeof(DevOpts), cudaMemcpyHostToDevice, inst->ctx->stream));
   TRY(reset_state(inst, PH_EVAL, nofix, 0.0));
   TRY(run_kernels(inst, {K_ELEM_EG, K_GATHER}, true));
@@ -1477,14 +1592,9 @@ int phx_element_local(phx_instance inst, const double* x, int32_t precision, dou
   const int m = inst->dev.m;
   const bool fp64 = precision == PHX_PREC_FP64;
   NState s;
-  TRY(eval_eg(inst, x, 0, &s, !fp64));
+  TRY(eval_eg(inst, x, 0, &s));
   if (E) CU(cudaMemcpy(E, inst->dev.Eloc, m * sizeof(double), cudaMemcpyDeviceToHost));
-  if (g && fp64) CU(cudaMemcpy(g, inst->dev.Gloc, 12 * (size_t)m * sizeof(double), cudaMemcpyDeviceToHost));
-  if (g && !fp64) {  // double-float pairs: component = hi + lo
-    std::vector<float> G2(24 * (size_t)m);
-    CU(cudaMemcpy(G2.data(), inst->dev.Gloc, G2.size() * sizeof(float), cudaMemcpyDeviceToHost));
-    for (size_t k = 0; k < 12 * (size_t)m; ++k) g[k] = (double)G2[2 * k] + (double)G2[2 * k + 1];
-  }
+  if (g) CU(cudaMemcpy(g, inst->dev.Gloc, 12 * (size_t)m * sizeof(double), cudaMemcpyDeviceToHost));
   if (Hout) {
     TRY(eval_hess(inst, nullptr, fp64, 0));
     std::vector<double> Hl(90 * (size_t)m);
@@ -1606,6 +1716,106 @@ int phx_batch_solve(phx_context ctx, int32_t count, phx_instance* insts, const p
     if (fin_at[i] >= 0) fill_report_finished(st[i], fin_second[fin_at[i]], secs, &reps[i]);
     else fill_report(st[i], false, secs, &reps[i]);
   }
+  return PHX_OK;
+}
+
+int phx_context_launch_settings(phx_context ctx, phx_launch_settings* get, const phx_launch_settings* set) {
+  if (!ctx) return set_err(PHX_EINVAL, "ctx is NULL");
+  if (get) *get = ctx->launch;
+  if (set) {
+    if ((set->graph != 0 && set->graph != 1) || set->wait_rounds < 1 || set->wait_rounds > 64 ||
+        set->wait_share < 1 || set->wait_share > 64 || set->rounds < 1 || set->rounds > 1024)
+      return set_err(PHX_EINVAL, "launch settings out of range");
+    ctx->launch = *set;
+  }
+  return PHX_OK;
+}
+
+int phx_tune_batch(phx_context ctx, int32_t count, phx_instance* insts, const phx_options* o,
+                   phx_launch_settings* chosen, double* default_seconds, double* best_seconds, int32_t* trials) {
+  if (!ctx || !o || count <= 0 || !insts) return set_err(PHX_EINVAL, "bad arguments");
+  std::vector<phx_instance> list(insts, insts + count);
+  for (int i = 0; i < count; ++i) {
+    if (!list[i] || list[i]->ctx != ctx) return set_err(PHX_EINVAL, "instance from another context");
+    if (list[i]->in_server) return set_err(PHX_EBUSY, "instance is admitted to a server");
+    if (list[i]->num_stages > 1) return set_err(PHX_EINVAL, "instances with staged boundary conditions are not tuned");
+    TRY(require_resident(list[i]));
+    for (int j = 0; j < i; ++j)
+      if (list[j] == list[i]) return set_err(PHX_EINVAL, "instance listed twice");
+  }
+  TRY(validate_opts(o));
+  const bool fp64 = o->precision == PHX_PREC_FP64;
+  // every trial starts from the same positions and warm-start steps, put back at the end
+  std::vector<std::vector<double>> x0(count), d0(count);
+  for (int i = 0; i < count; ++i) {
+    x0[i].resize(3 * (size_t)list[i]->dev.n);
+    d0[i].resize(3 * (size_t)list[i]->dev.n);
+    TRY(download_x(list[i], list[i]->dev.x, x0[i].data()));
+    TRY(download_x(list[i], list[i]->dev.dxprev, d0[i].data()));
+  }
+  auto restore = [&]() -> int {
+    for (int i = 0; i < count; ++i) {
+      TRY(upload_x(list[i], x0[i].data(), list[i]->dev.x));
+      TRY(upload_x(list[i], d0[i].data(), list[i]->dev.dxprev));
+    }
+    return PHX_OK;
+  };
+  int ntrials = 0;
+  auto trial = [&](const phx_launch_settings& S, double* secs) -> int {
+    TRY(restore());
+    for (int i = 0; i < count; ++i) TRY(start_solve(list[i], o, false, 0.0, 0));
+    CU(cudaStreamSynchronize(ctx->stream));
+    const auto t = clk::now();
+    TRY(run_to_completion(ctx, list, fp64, o->pcg_chunk, &S));
+    CU(cudaStreamSynchronize(ctx->stream));
+    *secs = std::chrono::duration<double>(clk::now() - t).count();
+    ++ntrials;
+    return PHX_OK;
+  };
+  phx_launch_settings best = ctx->launch;
+  double t_def = 0.0, t;
+  TRY(trial(best, &t_def));  // the first run pays one-time costs (graph, caches)
+  TRY(trial(best, &t_def));
+  double t_best = t_def;
+  // one setting at a time around the best so far
+  auto consider = [&](phx_launch_settings c) -> int {
+    TRY(trial(c, &t));
+    if (t < 0.99 * t_best) {
+      best = c;
+      t_best = t;
+    }
+    return PHX_OK;
+  };
+  {
+    phx_launch_settings c = best;
+    c.graph = 1 - c.graph;
+    TRY(consider(c));
+  }
+  for (int v : {2, 8, 16}) {
+    phx_launch_settings c = best;
+    if (v == c.wait_rounds) continue;
+    c.wait_rounds = v;
+    TRY(consider(c));
+  }
+  for (int v : {1, 4, 8}) {
+    phx_launch_settings c = best;
+    if (v == c.wait_share) continue;
+    c.wait_share = v;
+    TRY(consider(c));
+  }
+  for (int v : {8, 32, 64}) {
+    phx_launch_settings c = best;
+    if (v == c.rounds) continue;
+    c.rounds = v;
+    TRY(consider(c));
+  }
+  TRY(restore());
+  CU(cudaStreamSynchronize(ctx->stream));
+  ctx->tuned[mix_key(list, fp64)] = best;
+  if (chosen) *chosen = best;
+  if (default_seconds) *default_seconds = t_def;
+  if (best_seconds) *best_seconds = t_best;
+  if (trials) *trials = ntrials;
   return PHX_OK;
 }
 
@@ -2065,7 +2275,7 @@ int phx_server_progress(phx_server s, int32_t* active, int32_t* queued) {
     int max_chunks = 0;
     for (auto& r : s->active) max_chunks = std::max(max_chunks, r.inst->dev.nchunks);
     TRY(run_step(s->ctx, s->B, (int)s->active.size(), s->fp64, s->opts.pcg_chunk, s->ccount, (int)s->active.size(),
-                 max_chunks));
+                 max_chunks, s->ctx->launch));
   }
   if (active) *active = (int32_t)s->active.size();
   if (queued) *queued = (int32_t)s->queue.size();

@@ -30,7 +30,6 @@
 #include <type_traits>
 
 #include "element.cuh"
-#include "ffmath.cuh"
 #include "kernels.h"
 #include "newton_control.h"
 
@@ -488,21 +487,16 @@ __device__ __forceinline__ double soft_energy(const SoftNode& s, const double x[
   return 0.5 * s.k * (d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
 }
 
-// ---------------------------------------------------------------------------
-// served path (FP32 + refinement): element energy and gradient in double-float
-// ---------------------------------------------------------------------------
-// The tile's distinct nodes are staged once in shared memory as u = x - X0 in FP64 (node
-// lists built with the pattern), each tet's displacement differences are taken there in FP64
-// (so a large rigid motion costs no digits) and converted to double-float, and the rest of
-// the element (F, the material law, the gradient) runs on the FP32 pipe.  Results: the
-// element energy in FP64, the gradient as double-float pairs (float2 per component) that
-// the gather sums in double-float.
+// Node staging of the element stage: a tile's distinct nodes (node lists built with the
+// pattern, ascending) are loaded once, coalesced, and their displacements u = x - X0 kept in
+// shared memory in FP64; each tet then takes its displacement differences from there
+// (Du = u_c - u_0, the same bits as gathering the four corners).
 constexpr int kTileNodeCap = 4 * kTile;  // distinct nodes of a tile, at most
 
 // Stages u = x - X0 (x given per node by the functor) of the tile's distinct nodes into
 // shared memory, [3][kTileNodeCap] doubles; returns the node count.  Ends with a barrier.
 template <typename GetX>
-__device__ __forceinline__ int ff_stage_nodes(const InstDev& I, int lt, double* U, GetX getx) {
+__device__ __forceinline__ int stage_nodes(const InstDev& I, int lt, double* U, GetX getx) {
   const int p0 = __ldg(I.tile_nptr + lt), cnt = __ldg(I.tile_nptr + lt + 1) - p0;
   __syncthreads();  // the previous tile's readers are done with U
   for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
@@ -517,94 +511,14 @@ __device__ __forceinline__ int ff_stage_nodes(const InstDev& I, int lt, double* 
   return cnt;
 }
 
-// The gradient of an inverted element (+inf energy) in FP64, from the FP64 material law, so
-// that it has the FP64 kernels' values; out of line, as it is rare.
-__device__ __noinline__ void ff_inverted_grad(int model, const ff* R, const ff* Hd, float2* gout) {
-  float2 g[12];
-  double H[9], P[9], psi;
-  bool inverted;
-#pragma unroll
-  for (int k = 0; k < 9; ++k) H[k] = ff_to_d(Hd[k]);
-  material_eg(model, ff_to_d(R[10]), ff_to_d(R[11]), H, &psi, P, &inverted);
-  double B[12];
-#pragma unroll
-  for (int k = 0; k < 9; ++k) B[k] = ff_to_d(R[k]);
-  const double w = ff_to_d(R[9]);
-#pragma unroll
-  for (int a = 1; a < 4; ++a)
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-      const ff v = ff_of_d((P[r] * B[(a - 1)] + P[r + 3] * B[(a - 1) + 3] + P[r + 6] * B[(a - 1) + 6]) * w);
-      g[3 * a + r] = make_float2(v.hi, v.lo);
-    }
-#pragma unroll
-  for (int r = 0; r < 3; ++r) {
-    const double b0 = -(B[0] + B[1] + B[2]), b1 = -(B[3] + B[4] + B[5]), b2 = -(B[6] + B[7] + B[8]);
-    const ff v = ff_of_d((P[r] * b0 + P[r + 3] * b1 + P[r + 6] * b2) * w);
-    g[r] = make_float2(v.hi, v.lo);
-  }
-  float4* go = reinterpret_cast<float4*>(gout);
-#pragma unroll
-  for (int k = 0; k < 6; ++k) go[k] = make_float4(g[2 * k].x, g[2 * k].y, g[2 * k + 1].x, g[2 * k + 1].y);
-}
-
-// Energy (and, with grad, the gradient) of tet e from the staged displacements.  Returns the
-// energy; an inverted element (J - 1 < -1) has +inf and the FP64 kernels' gradient.
-__device__ __forceinline__ double ff_element(const InstDev& I, int e, const double* U, bool grad, float2* gout) {
+// Displacement differences of tet e from the staged nodes.
+__device__ __forceinline__ void staged_du(const InstDev& I, int e, const double* U, double (&Du)[9]) {
   const ushort4 lc = reinterpret_cast<const ushort4*>(I.tet_loc)[e];
   const int loc[4] = {lc.x, lc.y, lc.z, lc.w};
-  ff Du[9];
 #pragma unroll
   for (int c = 0; c < 3; ++c)
 #pragma unroll
-    for (int r = 0; r < 3; ++r)
-      Du[r + 3 * c] = ff_of_d(U[r * kTileNodeCap + loc[c + 1]] - U[r * kTileNodeCap + loc[0]]);
-  ff R[12];
-  {
-    const float4* h = reinterpret_cast<const float4*>(I.rest32 + 12 * (size_t)e);
-    const float4* l = reinterpret_cast<const float4*>(I.rest32lo + 12 * (size_t)e);
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const float4 a = __ldg(h + k), b = __ldg(l + k);
-      R[4 * k] = ff{a.x, b.x};
-      R[4 * k + 1] = ff{a.y, b.y};
-      R[4 * k + 2] = ff{a.z, b.z};
-      R[4 * k + 3] = ff{a.w, b.w};
-    }
-  }
-  ff Hd[9];
-#pragma unroll
-  for (int c = 0; c < 3; ++c)
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
-      Hd[r + 3 * c] = ff_fma(Du[r + 6], R[2 + 3 * c], ff_fma(Du[r + 3], R[1 + 3 * c], ff_mul(Du[r], R[3 * c])));
-  const ff w = R[9];
-  ff psi, P[9];
-  const bool ok = ff_material(I.model[e], R[10], R[11], Hd, &psi, P);
-  if (grad && !ok) ff_inverted_grad(I.model[e], R, Hd, gout);
-  if (grad && ok) {
-    float2 g[12];
-    {
-      // g_a = w P B_a, B_a = row (a-1) of Dm^-1, B_0 = -(B_1 + B_2 + B_3)
-      const ff b0 = ff_neg(ff_add(ff_add(R[0], R[1]), R[2])), b1 = ff_neg(ff_add(ff_add(R[3], R[4]), R[5]));
-      const ff b2 = ff_neg(ff_add(ff_add(R[6], R[7]), R[8]));
-#pragma unroll
-      for (int r = 0; r < 3; ++r) {
-        const ff v0 = ff_mul(ff_fma(P[r + 6], b2, ff_fma(P[r + 3], b1, ff_mul(P[r], b0))), w);
-        g[r] = make_float2(v0.hi, v0.lo);
-#pragma unroll
-        for (int a = 1; a < 4; ++a) {
-          const ff va = ff_mul(
-              ff_fma(P[r + 6], R[(a - 1) + 6], ff_fma(P[r + 3], R[(a - 1) + 3], ff_mul(P[r], R[a - 1]))), w);
-          g[3 * a + r] = make_float2(va.hi, va.lo);
-        }
-      }
-    }
-    float4* go = reinterpret_cast<float4*>(gout);
-#pragma unroll
-    for (int k = 0; k < 6; ++k) go[k] = make_float4(g[2 * k].x, g[2 * k].y, g[2 * k + 1].x, g[2 * k + 1].y);
-  }
-  return ok ? ff_to_d(ff_mul(psi, w)) : __longlong_as_double(0x7ff0000000000000LL);
+    for (int r = 0; r < 3; ++r) Du[r + 3 * c] = U[r * kTileNodeCap + loc[c + 1]] - U[r * kTileNodeCap + loc[0]];
 }
 
 __device__ __forceinline__ void st_elem_eg(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag,
@@ -618,17 +532,11 @@ __device__ __forceinline__ void st_elem_eg(const BatchDev& B, const TileMap& M, 
     if (st->phase != PH_EVAL) continue;
     const int e = lt * kTile + threadIdx.x;
     double Ee = 0.0;
-    if (I.opts->precision != 0) {  // served path: double-float, nodes staged per tile
-      double* U = reinterpret_cast<double*>(smraw);
-      ff_stage_nodes(I, lt, U, [&](int v, double (&x)[3]) { ld4(I.x, v, x); });
-      if (e < I.m) {
-        Ee = ff_element(I, e, U, true, reinterpret_cast<float2*>(I.Gloc) + 12 * (size_t)e);
-        I.Eloc[e] = Ee;
-      }
-    } else if (e < I.m) {
-      int nd[4];
+    double* U = reinterpret_cast<double*>(smraw);
+    stage_nodes(I, lt, U, [&](int v, double (&x)[3]) { ld4(I.x, v, x); });
+    if (e < I.m) {
       double Du[9];
-      load_du(I, e, nd, Du);
+      staged_du(I, e, U, Du);
       double R[12];
       const double2* r2 = reinterpret_cast<const double2*>(I.rest64 + 12 * (size_t)e);
 #pragma unroll
@@ -674,8 +582,7 @@ __device__ __forceinline__ void st_elem_eg(const BatchDev& B, const TileMap& M, 
 // trial point, and the element energy exactly as st_elem_eg does, so each trial's total
 // has the bits a one-at-a-time evaluation would give.  Energies only (the accepted trial
 // is evaluated again with its gradient).
-__device__ __forceinline__ void st_elem_ek(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag,
-                                           unsigned char* smraw) {
+__device__ __forceinline__ void st_elem_ek(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag) {
   const int total = map_total(M);
   for (int t = cta; t < total; t += ncta) {
     int i, lt;
@@ -688,25 +595,7 @@ __device__ __forceinline__ void st_elem_ek(const BatchDev& B, const TileMap& M, 
     double Ek[kLsK];
 #pragma unroll
     for (int k = 0; k < kLsK; ++k) Ek[k] = 0.0;
-    if (I.opts->precision != 0) {
-      // served path: each trial's nodes x = xs + a_k dx, formed as the vector-op stage forms a
-      // trial point, staged per tile, and the element energy as st_elem_eg computes it
-      double* U = reinterpret_cast<double*>(smraw);
-      for (int k = 0; k < K; ++k) {
-        const double ak = st->ls_a[k];
-        ff_stage_nodes(I, lt, U, [&](int v, double (&x)[3]) {
-          double xs[3], dx[3];
-          ld4(I.xs, v, xs);
-          ld4(I.dx, v, dx);
-#pragma unroll
-          for (int c = 0; c < 3; ++c) x[c] = xs[c] + ak * dx[c];
-        });
-        const double Ee = e < I.m ? ff_element(I, e, U, false, nullptr) : 0.0;
-#pragma unroll
-        for (int q = 0; q < kLsK; ++q)
-          if (q == k) Ek[q] = Ee;
-      }
-    } else if (e < I.m) {
+    if (e < I.m) {
       const int4 tt = reinterpret_cast<const int4*>(I.tets)[e];
       const int nd[4] = {tt.x, tt.y, tt.z, tt.w};
       double xs[4][3], dx[4][3], X[4][3];
@@ -836,33 +725,6 @@ __device__ __forceinline__ void st_gather(const BatchDev& B, const TileMap& M, i
       double g[3] = {0.0, 0.0, 0.0};
       const int c0 = I.nseg_ptr[v], c1 = I.nseg_ptr[v + 1];
       int c = c0;
-      if (I.opts->precision != 0) {
-        // served path: double-float element gradients, summed in double-float in element order
-        ff a3[3] = {ff_of(0.f), ff_of(0.f), ff_of(0.f)};
-        const float2* G2 = reinterpret_cast<const float2*>(I.Gloc);
-        for (; c + 4 <= c1; c += 4) {
-          int id[4];
-#pragma unroll
-          for (int u = 0; u < 4; ++u) id[u] = I.nseg_c[c + u];
-          float2 val[4][3];
-#pragma unroll
-          for (int u = 0; u < 4; ++u)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) val[u][k] = G2[3 * (size_t)id[u] + k];
-#pragma unroll
-          for (int u = 0; u < 4; ++u)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) a3[k] = ff_add(a3[k], ff{val[u][k].x, val[u][k].y});
-        }
-        for (; c < c1; ++c) {
-          const float2* src = G2 + 3 * (size_t)I.nseg_c[c];
-#pragma unroll
-          for (int k = 0; k < 3; ++k) a3[k] = ff_add(a3[k], ff{src[k].x, src[k].y});
-        }
-#pragma unroll
-        for (int k = 0; k < 3; ++k) g[k] = ff_to_d(a3[k]);
-        c = c1;
-      }
       // four contributions in flight (ids, then values), added in element order
       for (; c + 4 <= c1; c += 4) {
         int id[4];
@@ -1639,6 +1501,31 @@ __device__ void compact(const BatchDev& B, const EngineArgs& A) {
     for (int k = 0; k < 4; ++k) run[k] += tot[k];
     run_pcg += t2[0];
   }
+  if (A.wait) {
+    // the instances waiting for each cluster PCG kind, in corder's order (largest first), and
+    // their take counters reset: the cluster kernels launched next work through these lists
+    int r1 = 0, r2 = 0;
+    for (int base = 0; base < A.ccount; base += blockDim.x) {
+      const int j = base + threadIdx.x;
+      const int i = j < A.ccount ? A.corder[j] : -1;
+      const bool w = i >= 0 && B.cluster_mode && B.flags[8 + i] == PH_PCG;
+      const int kind = w ? B.inst[i].pcg_cluster : 0;
+      int v[4] = {kind == 1 ? 1 : 0, kind == 2 ? 1 : 0, 0, 0}, t[4];
+      block_scan4(v, t, scan_sm);
+      if (kind == 1) A.wait[4 + r1 + v[0]] = i;
+      if (kind == 2) A.wait[4 + A.cap + r2 + v[1]] = i;
+      r1 += t[0];
+      r2 += t[1];
+    }
+    if (threadIdx.x == 0) {
+      A.wait[0] = r1;
+      A.wait[1] = r2;
+      A.wait[2] = 0;
+      A.wait[3] = 0;
+      B.flags[4] = r1;
+      B.flags[5] = r2;
+    }
+  }
   if (threadIdx.x == 0) {
     pt[0] = 0; pn[0] = 0; pl[0] = 0; pp[0] = 0;
     A.act[0] = run[0];
@@ -1664,12 +1551,20 @@ __device__ __forceinline__ void stage_clock(const EngineArgs& A, int kind, unsig
   }
 }
 
+__device__ __forceinline__ void engine_gave_up(const EngineArgs& A) {
+  if (threadIdx.x == 0 && A.wait) {
+    A.wait[0] = 0;
+    A.wait[1] = 0;
+  }
+}
+
 template <typename Real>
 __global__ void __launch_bounds__(kTile, (sizeof(Real) == 4 ? 3 : 2)) k_engine(BatchDev B, EngineArgs A) {
   extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ double sm[32 * 5];
   __shared__ int flag;
   const int cta = blockIdx.x;
+  if (A.cfg) B.cpt = __ldcg(A.cfg);  // written by k_prep before the launch, the same for every CTA
   int* ids = A.act + 4;
   int* pt = ids + A.cap;
   int* pn = pt + A.cap + 1;
@@ -1682,13 +1577,19 @@ __global__ void __launch_bounds__(kTile, (sizeof(Real) == 4 ? 3 : 2)) k_engine(B
   int first_wait = -1;  // round in which an instance first waited for the cluster kernel
   // two barrier objects: the PCG group synchronises on its own counter while the CTAs
   // that skip the PCG block are already arriving at the next round-wide barrier
+  // a CTA whose barrier wait gave up empties the waiting lists (no cluster PCG runs after a
+  // failed launch) and leaves
 #define PHX_SYNC(n, tag, kind)                                                                             \
-  if (!grid_sync(A.bar, (unsigned)(n), tag, &A.bar->err, B.phase_live, A.wait_limit, A.unmet_tag == (tag))) \
+  if (!grid_sync(A.bar, (unsigned)(n), tag, &A.bar->err, B.phase_live, A.wait_limit, A.unmet_tag == (tag))) { \
+    engine_gave_up(A);                                                                                    \
     return;                                                                                               \
+  }                                                                                                       \
   stage_clock(A, kind, t);
 #define PHX_SYNC_PCG(n, tag, kind)                                                                  \
-  if (!grid_sync(A.bar + 1, (unsigned)(n), tag, &A.bar->err, nullptr, A.wait_limit, A.unmet_tag == (tag))) \
+  if (!grid_sync(A.bar + 1, (unsigned)(n), tag, &A.bar->err, nullptr, A.wait_limit, A.unmet_tag == (tag))) { \
+    engine_gave_up(A);                                                                             \
     return;                                                                                        \
+  }                                                                                                \
   stage_clock(A, kind, t);
   // a stage (and the barrier after it) runs only if an instance is in its phase at the
   // last barrier's snapshot: every CTA reads the same snapshot, so all skip together
@@ -1722,7 +1623,7 @@ __global__ void __launch_bounds__(kTile, (sizeof(Real) == 4 ? 3 : 2)) k_engine(B
       PHX_SYNC(P, 4, K_GATHER);
     }
     if (PHX_NEED(PH_EVALK)) {
-      st_elem_ek(B, Mt, cta, P, sm, flag, smraw);
+      st_elem_ek(B, Mt, cta, P, sm, flag);
       PHX_SYNC(P, 19, K_ELEM_EG);
     }
     if (PHX_NEED(PH_EVALK2)) {
@@ -1786,7 +1687,7 @@ __global__ void __launch_bounds__(kTile, (sizeof(Real) == 4 ? 3 : 2)) k_engine(B
       PHX_SYNC(P, 17, K_GATHER);
     }
     if (PHX_NEED(PH_EVALK)) {
-      st_elem_ek(B, Mt, cta, P, sm, flag, smraw);
+      st_elem_ek(B, Mt, cta, P, sm, flag);
       PHX_SYNC(P, 21, K_ELEM_EG);
     }
     if (PHX_NEED(PH_EVALK2)) {
@@ -1817,18 +1718,29 @@ __device__ __forceinline__ unsigned cl_rank() {
   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
   return r;
 }
-__device__ __forceinline__ unsigned cl_id() {
-  unsigned r;
-  asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
-  return r;
-}
-__device__ __forceinline__ unsigned cl_count() {
-  unsigned r;
-  asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
-  return r;
-}
 __device__ __forceinline__ void cl_sync() {
   asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// The cluster's next position in a waiting list: thread 0 of rank 0 takes it from the list's
+// counter and stores it into slot[par] of every CTA of the cluster; the cluster barrier
+// publishes it.  Two slots, used in turn: a slot is written again only after every CTA has
+// passed the barrier that follows its last read of it.  All CTAs get the same value.
+template <int CL>
+__device__ __forceinline__ int cl_next_job(int32_t* next, int* slot, unsigned& par) {
+  if (cl_rank() == 0 && threadIdx.x == 0) {
+    const int j = atomicAdd(next, 1);
+    const unsigned a = (unsigned)__cvta_generic_to_shared(slot + par);
+#pragma unroll
+    for (unsigned r = 0; r < (unsigned)CL; ++r) {
+      unsigned d;
+      asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(r));
+      asm volatile("st.shared::cluster.s32 [%0], %1;" ::"r"(d), "r"(j) : "memory");
+    }
+  }
+  cl_sync();
+  const int j = *(volatile int*)(slot + par);
+  par ^= 1u;
+  return j;
 }
 __device__ __forceinline__ double cl_ld(const double* local, unsigned rank) {
   unsigned src = (unsigned)__cvta_generic_to_shared(local), dst;
@@ -1871,13 +1783,19 @@ __device__ __forceinline__ void cta_sum256(double (&v)[K], double (*ws)[4]) {
 
 template <typename Real, int CL, int NT>
 __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT) k_pcg_cluster(BatchDev B, const int32_t* list,
-                                                                                int count) {
+                                                                                const int32_t* countp, int32_t* next) {
   __shared__ double red[2][4];    // this CTA's partials, double-buffered by iteration
   __shared__ double ws[NT / 32][4];
   __shared__ double tot[4];
+  __shared__ int jslot[2];
   const unsigned rank = cl_rank();
-  for (int j = (int)cl_id(); j < count; j += (int)cl_count()) {
-    const int i = __ldg(list + j);
+  const int count = __ldcg(countp);
+  unsigned jpar = 0;
+  cl_sync();  // every CTA of the cluster runs before rank 0 stores into their shared memory
+  for (;;) {
+    const int j = cl_next_job<CL>(next, jslot, jpar);
+    if (j >= count) break;
+    const int i = __ldcg(list + j);
     const InstDev I = B.inst[i];  // local copy: fields stay in registers across stores
     NState* st = I.st;
     if (I.pcg_cluster != 2 || *(volatile int32_t*)&st->phase != PH_PCG) continue;  // uniform over the cluster
@@ -2459,7 +2377,7 @@ __device__ __forceinline__ CgResult cg_solve(const InstDev& I, const CgShared& S
 
 template <int CL, int NT>
 __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_pcg_cg(BatchDev B, const int32_t* list,
-                                                                               int count) {
+                                                                               const int32_t* countp, int32_t* next) {
   __shared__ __align__(16) float red[CL][4];  // partial sums pushed by every CTA of the cluster
   __shared__ float ws[NT / 32][4];
   __shared__ __align__(8) uint64_t mbar_obj;   // completes when all CL pushes of a reduction landed
@@ -2476,8 +2394,13 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_pcg_cg(Bat
   }
   cl_sync();  // every mbarrier initialised before any CTA pushes to it
   int32_t* err = B.flags + 2;
-  for (int j = (int)cl_id(); j < count; j += (int)cl_count()) {
-    const int i = __ldg(list + j);
+  __shared__ int jslot[2];
+  const int count = __ldcg(countp);
+  unsigned jpar = 0;
+  for (;;) {
+    const int j = cl_next_job<CL>(next, jslot, jpar);
+    if (j >= count) break;
+    const int i = __ldcg(list + j);
     const InstDev& I = B.inst[i];  // fields are re-read (L1) where needed: registers go to the rows
     NState* st = I.st;
     if (I.pcg_cluster != 1 || *(volatile int32_t*)&st->phase != PH_PCG) continue;  // uniform over the cluster
@@ -2631,12 +2554,134 @@ int engine_grid(bool fp64, int num_sms) {
   return nb * num_sms;
 }
 
-cudaError_t launch_pcg_cluster(cudaStream_t s, const BatchDev& B, const int32_t* list, int count, int kind) {
-  if (count <= 0) return cudaSuccess;
-  // one cluster per listed instance; clusters skip instances not waiting for them
-  if (kind == 1) k_pcg_cg<kCl, kClThreads><<<count * kCl, kClThreads, kCgSmem, s>>>(B, list, count);
-  else k_pcg_cluster<float, kCl, kClThreads><<<count * kCl, kClThreads, 0, s>>>(B, list, count);
+// Before an engine launch (one thread): both grid barriers cleared, the round's CTA count, and
+// the PCG tile width for the launch from the active count the previous launch left in
+// flags[0] (set_batch puts the batch size there first).
+__global__ void k_prep(BatchDev B, EngineArgs A, int grid, int max_chunks) {
+  if (threadIdx.x != 0) return;
+  for (int k = 0; k < 2; ++k) A.bar[k] = GridBar{0u, 0u, 0, 0};
+  A.act[0] = 0;
+  A.act[1] = grid;
+  const int active = B.flags[0];
+  *A.cfg = (active <= kClWideBelow && max_chunks <= 2048) ? 1 : 4;
+}
+
+// End of one pass of the graph's solve loop (one thread): go on while instances are active and
+// no bounded wait gave up, for at most loop_cap passes.
+__global__ void k_loop_end(BatchDev B, EngineArgs A, cudaGraphConditionalHandle h, int32_t* loops, int loop_cap) {
+  if (threadIdx.x != 0) return;
+  const bool failed = A.bar[0].err || A.bar[1].err || B.flags[2];
+  const int pass = ++loops[0];
+  cudaGraphSetConditional(h, (!failed && B.flags[0] > 0 && pass < loop_cap) ? 1u : 0u);
+}
+
+cudaError_t launch_prep(cudaStream_t s, const BatchDev& B, const EngineArgs& A, int grid, int max_chunks) {
+  k_prep<<<1, 32, 0, s>>>(B, A, grid, max_chunks);
   return cudaGetLastError();
+}
+
+cudaError_t launch_pcg_cluster(cudaStream_t s, const BatchDev& B, int32_t* wait, int cap, int clusters, int kind) {
+  if (clusters <= 0) return cudaSuccess;
+  const int32_t* list = wait + 4 + (kind - 1) * cap;
+  if (kind == 1) k_pcg_cg<kCl, kClThreads><<<clusters * kCl, kClThreads, kCgSmem, s>>>(B, list, wait, wait + 2);
+  else k_pcg_cluster<float, kCl, kClThreads><<<clusters * kCl, kClThreads, 0, s>>>(B, list, wait + 1, wait + 3);
+  return cudaGetLastError();
+}
+
+int max_active_clusters(int kind) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kCl * 256);
+  cfg.blockDim = dim3(kClThreads);
+  cfg.dynamicSmemBytes = kind == 1 ? kCgSmem : 0;
+  int n = 0;
+  cudaError_t e = kind == 1 ? cudaOccupancyMaxActiveClusters(&n, (const void*)k_pcg_cg<kCl, kClThreads>, &cfg)
+                            : cudaOccupancyMaxActiveClusters(&n, (const void*)k_pcg_cluster<float, kCl, kClThreads>, &cfg);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+namespace {
+cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, cudaGraphNode_t* dep, const void* fn, dim3 grid,
+                       dim3 block, size_t smem, void** args) {
+  cudaKernelNodeParams p = {};
+  p.func = const_cast<void*>(fn);
+  p.gridDim = grid;
+  p.blockDim = block;
+  p.sharedMemBytes = (unsigned)smem;
+  p.kernelParams = args;
+  return cudaGraphAddKernelNode(node, g, dep, dep ? 1 : 0, &p);
+}
+}  // namespace
+
+cudaError_t build_solve_graph(bool fp64, int grid, const BatchDev& B, const EngineArgs& A, int max_chunks,
+                              const int clusters[2], int32_t* loops, int loop_cap, cudaGraph_t* graph,
+                              cudaGraphExec_t* exec) {
+  *graph = nullptr;
+  *exec = nullptr;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaGraphCreate(&g, 0);
+  if (e != cudaSuccess) return e;
+  cudaGraphConditionalHandle h;
+  cudaGraphNode_t cnode;
+  cudaGraphNodeParams cp = {};
+  e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+  if (e == cudaSuccess) {
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    e = cudaGraphAddNode(&cnode, g, nullptr, nullptr, 0, &cp);
+  }
+  // kernel arguments are copied when the nodes are added
+  BatchDev b = B;
+  EngineArgs a = A;
+  int gr = grid, mc = max_chunks, cap = loop_cap;
+  int32_t* lp = loops;
+  cudaGraphNode_t prev = nullptr, node = nullptr;
+  if (e == cudaSuccess) {
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    void* pa[] = {&b, &a, &gr, &mc};
+    e = add_kernel(body, &node, nullptr, (const void*)k_prep, dim3(1), dim3(32), 0, pa);
+    prev = node;
+    if (e == cudaSuccess) {
+      void* ea[] = {&b, &a};
+      const void* fn = fp64 ? (const void*)k_engine<double> : (const void*)k_engine<float>;
+      e = add_kernel(body, &node, &prev, fn, dim3(grid), dim3(kTile), fp64 ? hess_smem<double>() : hess_smem<float>(),
+                     ea);
+      if (e == cudaSuccess) {
+        cudaLaunchAttributeValue v = {};
+        v.cooperative = 1;
+        e = cudaGraphKernelNodeSetAttribute(node, cudaLaunchAttributeCooperative, &v);
+      }
+      prev = node;
+    }
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+      if (clusters[k] <= 0) continue;
+      int32_t* list = A.wait + 4 + k * A.cap;
+      const int32_t* countp = A.wait + k;
+      int32_t* next = A.wait + 2 + k;
+      void* ca[] = {&b, &list, &countp, &next};
+      const void* fn = k == 0 ? (const void*)k_pcg_cg<kCl, kClThreads> : (const void*)k_pcg_cluster<float, kCl, kClThreads>;
+      e = add_kernel(body, &node, &prev, fn, dim3(clusters[k] * kCl), dim3(kClThreads), k == 0 ? kCgSmem : 0, ca);
+      prev = node;
+    }
+    if (e == cudaSuccess) {
+      void* la[] = {&b, &a, &h, &lp, &cap};
+      e = add_kernel(body, &node, &prev, (const void*)k_loop_end, dim3(1), dim3(32), 0, la);
+    }
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(exec, g, 0);
+  if (e != cudaSuccess) {
+    if (*exec) cudaGraphExecDestroy(*exec);
+    *exec = nullptr;
+    cudaGraphDestroy(g);
+    return e;
+  }
+  *graph = g;
+  return cudaSuccess;
 }
 
 cudaError_t launch_engine(bool fp64, int grid, cudaStream_t s, const BatchDev& B, const EngineArgs& A) {

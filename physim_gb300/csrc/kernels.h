@@ -46,14 +46,32 @@ struct EngineArgs {
   long long wait_limit;  // SM cycles a grid-barrier wait lasts before it gives up
   int unmet_tag;         // test hook: the grid barrier with this tag waits for one arrival more than
                          // the CTAs taking part, so it gives up (0: none)
+  int32_t* cfg;          // [1] PCG tile width in chunks for this launch (set by k_prep, read only here)
+  const int32_t* corder; // [ccount] batch positions of the cluster-PCG instances, largest first
+  int ccount;
+  int32_t* wait;         // [4 + 2 cap]: instances waiting for the cluster PCG, per kind (1, 2): counts,
+                         // take counters, then the two lists in corder's order (written by the engine)
 };
 constexpr long long kBarrierLimit = 4000000000LL;  // default wait_limit: about 2 s of SM clock
 
 cudaError_t setup_kernel_attributes();
 int engine_grid(bool fp64, int num_sms);
 cudaError_t launch_engine(bool fp64, int grid, cudaStream_t s, const BatchDev& B, const EngineArgs& A);
-// PCG of every listed instance that is in PH_PCG, one cluster per instance
-cudaError_t launch_pcg_cluster(cudaStream_t s, const BatchDev& B, const int32_t* list, int count, int kind);
+// Before each engine launch: barrier state cleared, the round's CTA count, the PCG tile width
+// from the active count the last launch left (one-chunk tiles while few, small instances remain)
+cudaError_t launch_prep(cudaStream_t s, const BatchDev& B, const EngineArgs& A, int grid, int max_chunks);
+// PCG of the instances the engine listed as waiting for PCG kind `kind` (1: rows in shared
+// memory, 2: rows in L2): `clusters` clusters take them in list order until none is left
+cudaError_t launch_pcg_cluster(cudaStream_t s, const BatchDev& B, int32_t* wait, int cap, int clusters, int kind);
+// Clusters of PCG kind `kind` that fit on the device at once (0 if the query fails)
+int max_active_clusters(int kind);
+// The whole solve loop as one graph: while instances are active, k_prep, k_engine, the cluster
+// PCG kernels (clusters[k] clusters of kind k + 1; 0 leaves it out) and k_loop_end, which sets
+// the loop condition from the engine's flags (no instance active, a barrier or cluster wait gave
+// up, or loop_cap passes) and counts the passes in loops[0].
+cudaError_t build_solve_graph(bool fp64, int grid, const BatchDev& B, const EngineArgs& A, int max_chunks,
+                              const int clusters[2], int32_t* loops, int loop_cap, cudaGraph_t* graph,
+                              cudaGraphExec_t* exec);
 // One stage as its own kernel, for the evaluation entry points: K_ELEM_EG, K_GATHER,
 // K_ELEM_HESS or K_ASSEMBLE (other ids launch nothing; their stages run inside k_engine)
 void launch(KernelId id, int grid, cudaStream_t s, const BatchDev& B, bool fp64);

@@ -110,7 +110,6 @@ bool build_pattern(const MeshIn& in, HostPattern& hp, std::string& err) {
   std::vector<char> used(n, 0);
   hp.rest64.resize(12 * (size_t)m);
   hp.rest32.resize(12 * (size_t)m);
-  hp.rest32lo.resize(12 * (size_t)m);
   hp.mass.assign(n, 0.0);
   for (int e = 0; e < m; ++e) {
     const int32_t* t = &hp.tets[4 * (size_t)e];
@@ -138,11 +137,7 @@ bool build_pattern(const MeshIn& in, HostPattern& hp, std::string& err) {
     R[9] = d / 6.0;  // quadrature weight (1/6) * det J (EnergyElement_FEM.cpp:87-91)
     R[10] = lam;
     R[11] = mu;
-    for (int k = 0; k < 12; ++k) {
-      const float hi = (float)R[k];
-      hp.rest32[12 * (size_t)e + k] = hi;
-      hp.rest32lo[12 * (size_t)e + k] = (float)(R[k] - (double)hi);
-    }
+    for (int k = 0; k < 12; ++k) hp.rest32[12 * (size_t)e + k] = (float)R[k];
     // MassElement_Lumped::ComputeAndStore_Mass: rho * V / 4 per node
     double me = rho * (d / 6.0) / 4.0;
     for (int a = 0; a < 4; ++a) hp.mass[t[a]] += me;

@@ -31,7 +31,6 @@ struct HostPattern {
   std::vector<int32_t> tets;          // [4m]
   std::vector<double> rest64;         // [12m]
   std::vector<float> rest32;          // [12m]
-  std::vector<float> rest32lo;        // [12m] rest64 - rest32: with rest32, a double-float copy
   std::vector<int32_t> tile_nptr;     // [tiles(m)+1] unique nodes of each 128-tet tile ...
   std::vector<int32_t> tile_nodes;    // ... ascending, concatenated
   std::vector<uint16_t> tet_loc;      // [4m] each corner's index in its tile's node list

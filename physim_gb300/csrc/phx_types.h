@@ -128,7 +128,6 @@ struct InstDev {
   const int32_t* tets;        // [m][4]
   const double* rest64;       // [m][12]
   const float* rest32;        // [m][12]
-  const float* rest32lo;      // [m][12] rest64 - rest32 (double-float rest data of the served path)
   const int32_t* tile_nptr;   // [tiles(m)+1] unique nodes of each tet tile, ascending ...
   const int32_t* tile_nodes;  // ... concatenated
   const uint16_t* tet_loc;    // [m][4] each corner's index in its tile's node list

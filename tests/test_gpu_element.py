@@ -43,33 +43,6 @@ def test_element_local_fp64(gpu_ctx, name):
 
 
 @pytest.mark.parametrize("name", list(CASES))
-@pytest.mark.parametrize("scale", [0.0, 0.05, 0.3])
-def test_element_local_served_double_float(gpu_ctx, name, scale):
-    """The served path's element energy and gradient (double-float on the FP32 pipe, displacement
-    differences staged per tile in FP64) against the oracle: 1e-11 relative per element energy,
-    1e-11 of the largest gradient entry.  Scale 0 is the rest state (zero energy and gradient
-    from the displacement form), 0.3 a strong distortion; a rigid translation of 1 m, many
-    times the elements' size, is checked as well (positions far from the element's scale cost
-    the double-float no more than the FP64 differences they start from)."""
-    m = CASES[name]()
-    inst = px.Instance(gpu_ctx, m)
-    orc = oracle.Oracle(m)
-    if scale == 0.0:
-        E, g, _ = inst.element_local(m.X0.ravel().copy(), px.PREC_FP32_REFINE)
-        assert np.all(E == 0.0) and np.all(g == 0.0)
-        return
-    x = perturbed(m, scale, seed=6)
-    Eo, go, _ = orc.element_local(x)
-    inv = np.isinf(Eo)  # inverted elements (at scale 0.3): +inf in both, FP64 gradients
-    assert inv.any() == (scale == 0.3)
-    for xx in (x, x + np.tile([1.0, -1.0, 1.0], m.n)):
-        E, g, _ = inst.element_local(xx, px.PREC_FP32_REFINE)
-        assert np.array_equal(np.isinf(E), inv) and np.all(E[inv] > 0)
-        assert np.max(np.abs(E[~inv] - Eo[~inv]) / np.maximum(np.abs(Eo[~inv]), 1e-300)) < 1e-11
-        assert np.max(np.abs(g - go)) <= 1e-11 * np.abs(go).max()
-
-
-@pytest.mark.parametrize("name", list(CASES))
 def test_element_hessian_fp32(gpu_ctx, name):
     m = CASES[name]()
     inst = px.Instance(gpu_ctx, m)
