@@ -731,8 +731,32 @@ def run_serve(args, world, rank, dist, rates=None, count=None):
     return out
 
 
+def _large_oracle_worker(tol_factor, threads, q):
+    """The 48x48x192 cantilever through the oracle (Jacobi-PCG Newton, row-parallel CG), in a
+    spawned process that runs on the host cores beside the GPU solves."""
+    import oracle
+    from physim_gb300 import mesh as M
+    t0 = time.perf_counter()
+    m = M.cantilever(48, 48, 192, seed=7)
+    o = oracle.Oracle(m)
+    x0 = o.rest()
+    g0 = float(np.linalg.norm(o.gradient(x0)))
+    x, r = o.solve_static(x0, tol_max_error=tol_factor * g0, tol_min_impr=0.0, tol_min_step=0.0, ls_solver=1,
+                          cg_block_jacobi=1, ls_num_max_iters=12000, cg_parallel=1, threads=threads)
+    q.put((x - x0, {k: r[k] for k in ("result_name", "iterations", "lin_iterations", "opt", "opt0")},
+           time.perf_counter() - t0))
+
+
 def run_large(args, world, rank, dist):
     """48x48x192 cantilever with per-element E: plain FP64 vs FP32+refinement at 1e-6."""
+    import multiprocessing as mp
+    orc_proc = None
+    if args.large_oracle:  # started before the first GPU call (a spawned process)
+        ctxm = mp.get_context("spawn")
+        orc_q = ctxm.Queue()
+        orc_proc = ctxm.Process(target=_large_oracle_worker,
+                                args=(args.large_oracle_tol, max(1, (os.cpu_count() or 2) - 1), orc_q))
+        orc_proc.start()
     import physim_gb300 as px
     from physim_gb300 import build, mesh as M
     build.build()
@@ -771,6 +795,14 @@ def run_large(args, world, rank, dist):
            "served_fp32_refine": res["served_fp32_refine"], "plain_fp64": res["plain_fp64"],
            "served_vs_plain_rel_displacement": float(np.linalg.norm(xs - xp) / np.linalg.norm(xp - x0))}
     ctx.close()
+    if orc_proc is not None:
+        du, rep, secs = orc_q.get()
+        orc_proc.join()
+        nd = float(np.linalg.norm(du))
+        out["oracle"] = {"solver": "oracle Newton, Jacobi(3x3)-PCG (row-parallel), ||g|| <= %g ||g0||" % args.large_oracle_tol,
+                         "report": rep, "seconds": round(secs, 1),
+                         "served_rel_displacement_err": float(np.linalg.norm((xs - x0) - du) / nd),
+                         "plain_rel_displacement_err": float(np.linalg.norm((xp - x0) - du) / nd)}
     return out
 
 
@@ -938,6 +970,10 @@ def main():
                     help="served FP32 PCG at negative curvature: 0 truncate, 1 go on like Eigen's CG")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch settings (no batch tuner)")
+    ap.add_argument("--large-oracle", action="store_true",
+                    help="large workload: solve it with the oracle on the host cores too and compare")
+    ap.add_argument("--large-oracle-tol", type=float, default=1e-8,
+                    help="the oracle's stopping rule, ||g|| <= tol ||g0|| (tighter than the GPU's, as the reference)")
     ap.add_argument("--no-oracle-all", action="store_true",
                     help="skip the comparison of every batch instance with the oracle (about a minute of host time)")
     ap.add_argument("--lsearch", default="simple", choices=sorted(LSEARCH),

@@ -110,8 +110,10 @@ typedef struct phx_options {
   double tol_rel;             /* if > 0: stop at ||g|| <= max(tol_max_error, tol_rel * ||g0||), g0 after loading */
   int32_t pcg_cluster;        /* FP32 instances up to 13000 nodes run each PCG solve inside one 8-CTA cluster:
                                  1 rows in shared memory, z exchanged through distributed shared
-                                 memory (default); 2 rows in L2, two-reduction CG; 0: every PCG
-                                 iteration runs on the whole GPU */
+                                 memory (default); 2 rows in L2, two-reduction CG.  Larger FP32
+                                 instances then iterate in the whole-GPU PCG kernels (k_gpcg_a/b,
+                                 the engine's PCG stages at the occupancy of a small kernel, the
+                                 same bits).  0: every PCG iteration runs inside the engine */
   int32_t fp64_finish;        /* 1 (default): an FP32 solve that stalls (line search, progress or iteration
                                  limit) within 1000x of its tolerance, or after reducing ||g|| a
                                  hundredfold, is finished in FP64 from its last accepted iterate with

@@ -166,11 +166,13 @@ struct phx_context_s {
   // cluster PCG: the batch's cluster instances (largest first) and the waiting lists the
   // engine writes for the cluster kernels
   int32_t* d_corder = nullptr;  // [cap]
-  int32_t* d_wait = nullptr;    // [4 + 2 cap]
-  int32_t* d_cfg = nullptr;     // [4]: [0] PCG tile width (k_prep), [1] graph loop passes
-  int ccount = 0;               // cluster instances in the batch
-  int ckind_count[3] = {0, 0, 0};  // ... of each PCG kind (1, 2)
-  int gmax[3] = {-1, -1, -1};   // clusters of each kind resident at once (-1: not queried yet)
+  int32_t* d_wait = nullptr;    // [wait_size(cap)]
+  int32_t* d_cfg = nullptr;     // [4]: [0] PCG tile width (k_prep), [1] graph loop passes,
+                                // [2] whole-GPU PCG iterations run by the graph
+  int ccount = 0;               // instances of the batch whose PCG runs outside the engine
+  int ckind_count[4] = {0, 0, 0, 0};  // ... of each PCG kind (1, 2: clusters, 3: whole-GPU kernels)
+  int gmax[3] = {-1, -1, -1};   // clusters of kinds 1, 2 resident at once (-1: not queried yet)
+  int ggrid = 0;                // CTAs of the whole-GPU PCG kernels
   // scheduling of batch solves (defaults, and tuned settings per batch mix)
   phx_launch_settings launch{1, kWaitRounds, kWaitShare, kRoundsPerLaunch};
   std::map<std::string, phx_launch_settings> tuned;
@@ -366,8 +368,8 @@ int ensure_batch_cap(phx_context ctx, int num) {
   if (ctx->d_wait) cudaFree(ctx->d_wait);
   ctx->d_corder = nullptr; ctx->d_wait = nullptr;
   CU(cudaMalloc(&ctx->d_corder, sizeof(int32_t) * cap));
-  CU(cudaMalloc(&ctx->d_wait, sizeof(int32_t) * (4 + 2 * cap)));
-  CU(cudaMemsetAsync(ctx->d_wait, 0, sizeof(int32_t) * 4, ctx->stream));
+  CU(cudaMalloc(&ctx->d_wait, sizeof(int32_t) * wait_size(cap)));
+  CU(cudaMemsetAsync(ctx->d_wait, 0, sizeof(int32_t) * kWaitLists, ctx->stream));
   ctx->cap = cap;
   if (!ctx->d_phc) {
     CU(cudaMalloc(&ctx->d_phc, sizeof(int32_t) * 32));
@@ -666,7 +668,7 @@ int set_cluster_list(phx_context ctx, const std::vector<phx_instance>& list, int
   std::stable_sort(ids.begin(), ids.end(), [&](int a, int b) { return list[a]->dev.nslots > list[b]->dev.nslots; });
   *count = (int)ids.size();
   ctx->ccount = (int)ids.size();
-  for (int k = 0; k < 3; ++k) ctx->ckind_count[k] = 0;
+  for (int k = 0; k < 4; ++k) ctx->ckind_count[k] = 0;
   for (int id : ids) ctx->ckind_count[list[id]->dev.pcg_cluster]++;
   if (!ids.empty())  // pageable source: copied before the call returns
     CU(cudaMemcpyAsync(ctx->d_corder, ids.data(), sizeof(int32_t) * ids.size(), cudaMemcpyHostToDevice, ctx->stream));
@@ -678,6 +680,36 @@ int set_cluster_list(phx_context ctx, const std::vector<phx_instance>& list, int
 int cluster_count(phx_context ctx, int kind, int waiting) {
   if (ctx->gmax[kind] < 0) ctx->gmax[kind] = max_active_clusters(kind);
   return ctx->gmax[kind] > 0 ? std::min(waiting, ctx->gmax[kind]) : waiting;
+}
+
+// The whole-GPU PCG of the listed kind-3 instances, until each has left its PCG: blocks of
+// kGpcgBlock iterations, the host reading the count left between blocks.  Profiling puts a
+// pair of events around every kernel.
+constexpr int kGpcgBlock = 16;
+
+int run_gpcg(phx_context ctx, const BatchDev& B, const phx_launch_settings& S, int pcg_chunk) {
+  if (ctx->ggrid == 0) ctx->ggrid = gpcg_grid(ctx->num_sms);
+  const EngineArgs A = engine_args(ctx, S, pcg_chunk);
+  for (int64_t it = 0;; it += kGpcgBlock) {
+    for (int k = 0; k < kGpcgBlock; ++k) {
+      if (ctx->profiling) {
+        cudaEvent_t ev[4];
+        TRY(profile_events(ctx, &ev[0], &ev[1]));  // records ev[0]
+        TRY(profile_events(ctx, &ev[2], &ev[3]));  // records ev[2]: the pair is recorded again below
+        CU(launch_gpcg(ctx->stream, B, A, ctx->ggrid, 1, ev));
+        ctx->evs.push_back({(int)K_PCG_A, ev[0], ev[1]});
+        ctx->evs.push_back({(int)K_PCG_B, ev[2], ev[3]});
+      } else {
+        CU(launch_gpcg(ctx->stream, B, A, ctx->ggrid, 1));
+      }
+      ctx->launches += 2;
+    }
+    int32_t left = 0;
+    CU(cudaMemcpyAsync(&left, ctx->d_wait + kWaitLeft, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    if (left <= 0) return PHX_OK;
+    if (it >= (int64_t)1 << 20) return set_err(PHX_ETIMEOUT, "whole-GPU PCG did not finish");
+  }
 }
 
 // One step of the device engine: engine rounds, then (if any) the per-cluster PCG solves.
@@ -705,6 +737,7 @@ int run_step(phx_context ctx, const BatchDev& B0, int num, bool fp64, int pcg_ch
       CU(launch_pcg_cluster(ctx->stream, B, ctx->d_wait, ctx->cap, cluster_count(ctx, kind, nw), kind));
       ctx->launches++;
     }
+    if (ctx->h_flags[6] > 0) TRY(run_gpcg(ctx, B, S, pcg_chunk));
     if (ctx->profiling) {
       cudaEventRecord(b, ctx->stream);
       ctx->evs.push_back({(int)K_PCG_CLUSTER, a, b});
@@ -729,31 +762,33 @@ int run_graph(phx_context ctx, const BatchDev& B0, int num, bool fp64, int pcg_c
   int clusters[2] = {0, 0};
   for (int kind = 1; kind <= 2; ++kind)
     if (B.cluster_mode && ctx->ckind_count[kind] > 0) clusters[kind - 1] = cluster_count(ctx, kind, ctx->ckind_count[kind]);
+  if (ctx->ggrid == 0) ctx->ggrid = gpcg_grid(ctx->num_sms);
+  const int gpcg = (B.cluster_mode && ctx->ckind_count[3] > 0) ? ctx->ggrid : 0;
   // the graph holds its kernels' arguments: rebuilt when any of them changes
   std::string key;
   auto put = [&](const void* p, size_t n) { key.append(static_cast<const char*>(p), n); };
   put(&fp64, sizeof(fp64)); put(&grid, sizeof(grid)); put(&B, sizeof(B)); put(&A, sizeof(A));
-  put(&max_chunks, sizeof(max_chunks)); put(clusters, sizeof(clusters));
+  put(&max_chunks, sizeof(max_chunks)); put(clusters, sizeof(clusters)); put(&gpcg, sizeof(gpcg));
   if (!ctx->gexec || key != ctx->gkey) {
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
     if (ctx->graph) cudaGraphDestroy(ctx->graph);
     ctx->gexec = nullptr;
     ctx->graph = nullptr;
     ctx->gkey.clear();
-    CU(build_solve_graph(fp64, grid, B, A, max_chunks, clusters, ctx->d_cfg + 1, kGraphPasses, &ctx->graph,
+    CU(build_solve_graph(fp64, grid, B, A, max_chunks, clusters, gpcg, ctx->d_cfg + 1, kGraphPasses, &ctx->graph,
                          &ctx->gexec));
     ctx->gkey = key;
   }
-  const int per_pass = 3 + (clusters[0] > 0) + (clusters[1] > 0);
+  const int per_pass = 3 + (clusters[0] > 0) + (clusters[1] > 0) + (gpcg > 0);
   for (;;) {
-    CU(cudaMemsetAsync(ctx->d_cfg + 1, 0, sizeof(int32_t), ctx->stream));
+    CU(cudaMemsetAsync(ctx->d_cfg + 1, 0, 2 * sizeof(int32_t), ctx->stream));
     CU(cudaGraphLaunch(ctx->gexec, ctx->stream));
     GridBar hb[2];
-    int32_t passes = 0;
+    int32_t passes[2] = {0, 0};
     CU(cudaMemcpyAsync(hb, ctx->d_bar, 2 * sizeof(GridBar), cudaMemcpyDeviceToHost, ctx->stream));
-    CU(cudaMemcpyAsync(&passes, ctx->d_cfg + 1, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaMemcpyAsync(passes, ctx->d_cfg + 1, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
     TRY(read_flags(ctx, num));
-    ctx->launches += (int64_t)passes * per_pass;
+    ctx->launches += (int64_t)passes[0] * per_pass + 3 * (int64_t)passes[1];
     if (hb[0].err || hb[1].err)
       return set_err(PHX_ETIMEOUT, "engine grid barrier timed out (stage " +
                                        std::to_string(hb[1].err ? hb[1].stage : hb[0].stage) + ")");
@@ -837,9 +872,10 @@ int start_solve(phx_instance inst, const phx_options* o, bool dynamic, double dt
   set_algo_bytes(inst->dev, fp64);
   // the cluster PCG serves the FP32 path: FP64 arithmetic is slow on this part and needs
   // every SM, so FP64 solves iterate on the whole GPU
-  inst->dev.pcg_cluster = (o->pcg_cluster >= 1 && o->pcg_cluster <= 2 && !fp64 && inst->dev.n <= kClusterMaxNodes)
-                              ? o->pcg_cluster
-                              : 0;
+  // larger FP32 instances iterate in the whole-GPU PCG kernels (kind 3)
+  inst->dev.pcg_cluster = (o->pcg_cluster < 1 || o->pcg_cluster > 2 || fp64) ? 0
+                          : inst->dev.n <= kClusterMaxNodes                 ? o->pcg_cluster
+                                                                              : 3;
   CU(cudaMemcpyAsync(inst->d_opts, &d, sizeof(DevOpts), cudaMemcpyHostToDevice, inst->ctx->stream));
   TRY(reset_state(inst, PH_START, 0, 0.0));
   return PHX_OK;

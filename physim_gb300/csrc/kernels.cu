@@ -27,6 +27,7 @@
 //                 on the FP32 path, FP64 residual refinement sweeps.
 #include <cfloat>
 #include <cstdint>
+#include <algorithm>
 #include <type_traits>
 
 #include "element.cuh"
@@ -1183,15 +1184,34 @@ __device__ __forceinline__ void st_resid(const BatchDev& B, const TileMap& M, in
 
 // PCG step 1: p = z + beta p_prev (formed on the fly for every column, written
 // for the own row into the other buffer), q = (H + shift I) p, pq = p.q
-template <typename Real>
-__device__ __forceinline__ void st_pcg_a(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag) {
+// kGrid: run by k_gpcg_a (the whole-GPU PCG kernel, instances of PCG kind 3) instead of the
+// engine (instances not left to a cluster or grid kernel); the iteration is the same.
+template <typename Real, bool kGrid = false>
+__device__ __forceinline__ bool pcg_here(const BatchDev& B, const InstDev& I) {
+  return kGrid ? I.pcg_cluster == 3 : !cluster_owned(B, I);
+}
+// an instance of PCG kind 3 leaves the grid kernel's loop
+__device__ __forceinline__ void gpcg_left(int32_t* left) {
+  if (left) atomicSub(left, 1);
+}
+// advance() out of line, for the small kernels: its state copy stays off their registers
+__device__ __noinline__ void advance_ool(const BatchDev& B, int i) { advance(B, i); }
+template <bool kGrid>
+__device__ __forceinline__ void advance_pcg(const BatchDev& B, int i) {
+  if (kGrid) advance_ool(B, i);
+  else advance(B, i);
+}
+
+template <typename Real, bool kGrid = false>
+__device__ __forceinline__ void st_pcg_a(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag,
+                                         int32_t* left = nullptr) {
   const int total = map_total(M);
   for (int t = cta; t < total; t += ncta) {
     int i, lt;
     map_tile(M, t, i, lt);
-    const InstDev I = B.inst[i];  // local copy: fields stay in registers across stores
+    std::conditional_t<kGrid, const InstDev&, const InstDev> I = B.inst[i];  // the engine keeps a copy in registers
     NState* st = I.st;
-    if (st->phase != PH_PCG || cluster_owned(B, I)) continue;
+    if (st->phase != PH_PCG || !pcg_here<Real, kGrid>(B, I)) continue;
     Real p[1] = {(Real)0};  // per-tile inner product in the PCG's own precision
     {
       const int par = st->pcg_parity;
@@ -1244,7 +1264,8 @@ __device__ __forceinline__ void st_pcg_a(const BatchDev& B, const TileMap& M, in
         } else {
           st->lin_status = (I.opts->precision != 0 && tot[0] < 0.0) ? LIN_TRUNCATED : LIN_BREAKDOWN;
           st->phase = (st->lin_status == LIN_TRUNCATED) ? PH_ACCUM : PH_LIN_DONE;
-          advance(B, i);
+          advance_pcg<kGrid>(B, i);
+          if (kGrid) gpcg_left(left);
         }
       } else {
         st->alpha = st->rz / tot[0];
@@ -1255,15 +1276,16 @@ __device__ __forceinline__ void st_pcg_a(const BatchDev& B, const TileMap& M, in
 
 
 // PCG step 2: e += alpha p, r -= alpha q, z = Minv r; convergence ||r||^2 < thr (Eigen's rule)
-template <typename Real>
-__device__ __forceinline__ void st_pcg_b(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag) {
+template <typename Real, bool kGrid = false>
+__device__ __forceinline__ void st_pcg_b(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag,
+                                         int32_t* left = nullptr) {
   const int total = map_total(M);
   for (int t = cta; t < total; t += ncta) {
     int i, lt;
     map_tile(M, t, i, lt);
-    const InstDev I = B.inst[i];  // local copy: fields stay in registers across stores
+    std::conditional_t<kGrid, const InstDev&, const InstDev> I = B.inst[i];  // the engine keeps a copy in registers
     NState* st = I.st;
-    if (st->phase != PH_PCG || cluster_owned(B, I)) continue;
+    if (st->phase != PH_PCG || !pcg_here<Real, kGrid>(B, I)) continue;
     const int v = lt * B.cpt * 32 + threadIdx.x;  // one row per thread over the tile's chunks
     Real p[2] = {(Real)0, (Real)0};  // per-tile inner products in the PCG's own precision
     if ((int)threadIdx.x < B.cpt * 32 && v < I.n) {
@@ -1309,7 +1331,10 @@ __device__ __forceinline__ void st_pcg_b(const BatchDev& B, const TileMap& M, in
         st->rz = tot[1];
         st->pcg_parity ^= 1;
       }
-      if (st->phase != PH_PCG) advance(B, i);
+      if (st->phase != PH_PCG) {
+        advance_pcg<kGrid>(B, i);
+        if (kGrid) gpcg_left(left);
+      }
     }
   }
 }
@@ -1502,28 +1527,35 @@ __device__ void compact(const BatchDev& B, const EngineArgs& A) {
     run_pcg += t2[0];
   }
   if (A.wait) {
-    // the instances waiting for each cluster PCG kind, in corder's order (largest first), and
-    // their take counters reset: the cluster kernels launched next work through these lists
-    int r1 = 0, r2 = 0;
+    // the instances waiting for each PCG kind, in corder's order (largest first), the kind-3
+    // PCG tile prefix, and the counters reset: the cluster and grid PCG kernels launched next
+    // work through these lists
+    int32_t* W = A.wait;
+    int32_t* pre3 = W + kWaitLists + 3 * A.cap;
+    int r[4] = {0, 0, 0, 0};
     for (int base = 0; base < A.ccount; base += blockDim.x) {
       const int j = base + threadIdx.x;
       const int i = j < A.ccount ? A.corder[j] : -1;
       const bool w = i >= 0 && B.cluster_mode && B.flags[8 + i] == PH_PCG;
       const int kind = w ? B.inst[i].pcg_cluster : 0;
-      int v[4] = {kind == 1 ? 1 : 0, kind == 2 ? 1 : 0, 0, 0}, t[4];
+      const int pt3 = kind == 3 ? pcg_tiles(B, B.inst[i]) : 0;
+      int v[4] = {kind == 1 ? 1 : 0, kind == 2 ? 1 : 0, kind == 3 ? 1 : 0, pt3}, t[4];
       block_scan4(v, t, scan_sm);
-      if (kind == 1) A.wait[4 + r1 + v[0]] = i;
-      if (kind == 2) A.wait[4 + A.cap + r2 + v[1]] = i;
-      r1 += t[0];
-      r2 += t[1];
+      if (kind >= 1 && kind <= 3) W[kWaitLists + (kind - 1) * A.cap + r[kind - 1] + v[kind - 1]] = i;
+      if (kind == 3) pre3[r[2] + v[2] + 1] = r[3] + v[3] + pt3;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) r[k] += t[k];
     }
     if (threadIdx.x == 0) {
-      A.wait[0] = r1;
-      A.wait[1] = r2;
-      A.wait[2] = 0;
-      A.wait[3] = 0;
-      B.flags[4] = r1;
-      B.flags[5] = r2;
+      for (int k = 0; k < 3; ++k) {
+        W[kWaitCount + k] = r[k];
+        B.flags[4 + k] = r[k];
+      }
+      W[kWaitTake] = 0;
+      W[kWaitTake + 1] = 0;
+      W[kWaitLeft] = r[2];
+      W[kWaitPass] = 0;
+      pre3[0] = 0;
     }
   }
   if (threadIdx.x == 0) {
@@ -1552,10 +1584,9 @@ __device__ __forceinline__ void stage_clock(const EngineArgs& A, int kind, unsig
 }
 
 __device__ __forceinline__ void engine_gave_up(const EngineArgs& A) {
-  if (threadIdx.x == 0 && A.wait) {
-    A.wait[0] = 0;
-    A.wait[1] = 0;
-  }
+  if (threadIdx.x == 0 && A.wait)
+    for (int k = 0; k < 3; ++k) A.wait[kWaitCount + k] = 0;
+  if (threadIdx.x == 0 && A.wait) A.wait[kWaitLeft] = 0;
 }
 
 template <typename Real>
@@ -2582,9 +2613,76 @@ cudaError_t launch_prep(cudaStream_t s, const BatchDev& B, const EngineArgs& A, 
 
 cudaError_t launch_pcg_cluster(cudaStream_t s, const BatchDev& B, int32_t* wait, int cap, int clusters, int kind) {
   if (clusters <= 0) return cudaSuccess;
-  const int32_t* list = wait + 4 + (kind - 1) * cap;
-  if (kind == 1) k_pcg_cg<kCl, kClThreads><<<clusters * kCl, kClThreads, kCgSmem, s>>>(B, list, wait, wait + 2);
-  else k_pcg_cluster<float, kCl, kClThreads><<<clusters * kCl, kClThreads, 0, s>>>(B, list, wait + 1, wait + 3);
+  const int32_t* list = wait + kWaitLists + (kind - 1) * cap;
+  const int32_t* count = wait + kWaitCount + (kind - 1);
+  int32_t* take = wait + kWaitTake + (kind - 1);
+  if (kind == 1) k_pcg_cg<kCl, kClThreads><<<clusters * kCl, kClThreads, kCgSmem, s>>>(B, list, count, take);
+  else k_pcg_cluster<float, kCl, kClThreads><<<clusters * kCl, kClThreads, 0, s>>>(B, list, count, take);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// whole-GPU PCG of the FP32 instances above the cluster size (PCG kind 3)
+// ---------------------------------------------------------------------------
+// The engine's two PCG stages as kernels of their own, so that they run at the occupancy of
+// a small kernel (the engine holds 12 warps per SM) and the kernel boundary is the grid-wide
+// synchronisation.  Tiles, partial sums and decisions are the engine's (same tile width from
+// k_prep, per-tile partials summed in tile order), so an instance gets the bits it gets when
+// the engine iterates its PCG.
+constexpr int kGpcgBlocks = 6;  // resident CTAs per SM the whole-GPU PCG kernels are built for (24 warps)
+
+__device__ __forceinline__ TileMap gpcg_map(const EngineArgs& A) {
+  const int32_t* W = A.wait;
+  return TileMap{W + kWaitLists + 3 * A.cap, W + kWaitLists + 2 * A.cap, __ldcg(W + kWaitCount + 2)};
+}
+
+__global__ void __launch_bounds__(kTile, kGpcgBlocks) k_gpcg_a(BatchDev B, EngineArgs A) {
+  __shared__ double sm[32 * 5];
+  __shared__ int flag;
+  B.cpt = __ldcg(A.cfg);
+  st_pcg_a<float, true>(B, gpcg_map(A), blockIdx.x, gridDim.x, sm, flag, A.wait + kWaitLeft);
+}
+
+__global__ void __launch_bounds__(kTile, kGpcgBlocks) k_gpcg_b(BatchDev B, EngineArgs A) {
+  __shared__ double sm[32 * 5];
+  __shared__ int flag;
+  B.cpt = __ldcg(A.cfg);
+  st_pcg_b<float, true>(B, gpcg_map(A), blockIdx.x, gridDim.x, sm, flag, A.wait + kWaitLeft);
+}
+
+// graph form: the loop runs while a kind-3 instance iterates (at most cap passes per launch)
+__global__ void k_gpcg_begin(EngineArgs A, cudaGraphConditionalHandle h) {
+  if (threadIdx.x != 0) return;
+  A.wait[kWaitPass] = 0;
+  cudaGraphSetConditional(h, A.wait[kWaitLeft] > 0 ? 1u : 0u);
+}
+__global__ void k_gpcg_loop(EngineArgs A, cudaGraphConditionalHandle h, int cap) {
+  if (threadIdx.x != 0) return;
+  A.cfg[2]++;  // iterations of the graph's kind-3 loops since the host last cleared it
+  const int pass = ++A.wait[kWaitPass];
+  cudaGraphSetConditional(h, (A.wait[kWaitLeft] > 0 && pass < cap) ? 1u : 0u);
+}
+
+int gpcg_grid(int num_sms) {
+  int na = 0, nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&na, k_gpcg_a, kTile, 0) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_gpcg_b, kTile, 0) != cudaSuccess) {
+    cudaGetLastError();
+    return num_sms;
+  }
+  return std::max(1, std::min(na, nb)) * num_sms;
+}
+
+cudaError_t launch_gpcg(cudaStream_t s, const BatchDev& B, const EngineArgs& A, int grid, int pairs,
+                        cudaEvent_t* ev) {
+  for (int k = 0; k < pairs; ++k) {
+    if (ev) cudaEventRecord(ev[4 * k], s);
+    k_gpcg_a<<<grid, kTile, 0, s>>>(B, A);
+    if (ev) cudaEventRecord(ev[4 * k + 1], s);
+    if (ev) cudaEventRecord(ev[4 * k + 2], s);
+    k_gpcg_b<<<grid, kTile, 0, s>>>(B, A);
+    if (ev) cudaEventRecord(ev[4 * k + 3], s);
+  }
   return cudaGetLastError();
 }
 
@@ -2617,7 +2715,7 @@ cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, cudaGraphNode_t* de
 }  // namespace
 
 cudaError_t build_solve_graph(bool fp64, int grid, const BatchDev& B, const EngineArgs& A, int max_chunks,
-                              const int clusters[2], int32_t* loops, int loop_cap, cudaGraph_t* graph,
+                              const int clusters[2], int gpcg, int32_t* loops, int loop_cap, cudaGraph_t* graph,
                               cudaGraphExec_t* exec) {
   *graph = nullptr;
   *exec = nullptr;
@@ -2667,6 +2765,36 @@ cudaError_t build_solve_graph(bool fp64, int grid, const BatchDev& B, const Engi
       const void* fn = k == 0 ? (const void*)k_pcg_cg<kCl, kClThreads> : (const void*)k_pcg_cluster<float, kCl, kClThreads>;
       e = add_kernel(body, &node, &prev, fn, dim3(clusters[k] * kCl), dim3(kClThreads), k == 0 ? kCgSmem : 0, ca);
       prev = node;
+    }
+    if (gpcg > 0 && e == cudaSuccess) {
+      // the kind-3 PCG: a while-loop inside the pass, its condition set by k_gpcg_begin and
+      // k_gpcg_loop (at most loop_cap iterations before the engine runs again)
+      cudaGraphConditionalHandle gh;
+      cudaGraphNodeParams gp = {};
+      e = cudaGraphConditionalHandleCreate(&gh, g, 0, 0);
+      if (e == cudaSuccess) {
+        void* ba[] = {&a, &gh};
+        e = add_kernel(body, &node, &prev, (const void*)k_gpcg_begin, dim3(1), dim3(32), 0, ba);
+        prev = node;
+      }
+      if (e == cudaSuccess) {
+        gp.type = cudaGraphNodeTypeConditional;
+        gp.conditional.handle = gh;
+        gp.conditional.type = cudaGraphCondTypeWhile;
+        gp.conditional.size = 1;
+        e = cudaGraphAddNode(&node, body, &prev, nullptr, 1, &gp);
+        prev = node;
+      }
+      if (e == cudaSuccess) {
+        cudaGraph_t inner = gp.conditional.phGraph_out[0];
+        cudaGraphNode_t n1, n2, n3;
+        void* ka[] = {&b, &a};
+        e = add_kernel(inner, &n1, nullptr, (const void*)k_gpcg_a, dim3(gpcg), dim3(kTile), 0, ka);
+        if (e == cudaSuccess) e = add_kernel(inner, &n2, &n1, (const void*)k_gpcg_b, dim3(gpcg), dim3(kTile), 0, ka);
+        int icap = 1 << 20;
+        void* la2[] = {&a, &gh, &icap};
+        if (e == cudaSuccess) e = add_kernel(inner, &n3, &n2, (const void*)k_gpcg_loop, dim3(1), dim3(32), 0, la2);
+      }
     }
     if (e == cudaSuccess) {
       void* la[] = {&b, &a, &h, &lp, &cap};

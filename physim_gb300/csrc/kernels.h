@@ -49,9 +49,16 @@ struct EngineArgs {
   int32_t* cfg;          // [1] PCG tile width in chunks for this launch (set by k_prep, read only here)
   const int32_t* corder; // [ccount] batch positions of the cluster-PCG instances, largest first
   int ccount;
-  int32_t* wait;         // [4 + 2 cap]: instances waiting for the cluster PCG, per kind (1, 2): counts,
-                         // take counters, then the two lists in corder's order (written by the engine)
+  int32_t* wait;         // [wait_size(cap)]: instances waiting for the cluster and grid PCG kernels
+                         // (layout below; written by the engine at the end of each launch)
 };
+// Layout of EngineArgs::wait: at kWaitCount the waiting counts of PCG kinds 1..3 (1, 2: one
+// cluster per instance, 3: the whole-GPU kernels k_gpcg_a/b); at kWaitTake the take counters
+// of kinds 1 and 2; at kWaitLeft the kind-3 instances still iterating; at kWaitPass the kind-3
+// loop's passes; from kWaitLists the three lists (cap each, corder's order) and the kind-3
+// PCG tile prefix (cap + 1).
+constexpr int kWaitCount = 0, kWaitTake = 3, kWaitLeft = 5, kWaitPass = 6, kWaitLists = 8;
+inline int wait_size(int cap) { return kWaitLists + 4 * cap + 1; }
 constexpr long long kBarrierLimit = 4000000000LL;  // default wait_limit: about 2 s of SM clock
 
 cudaError_t setup_kernel_attributes();
@@ -65,12 +72,21 @@ cudaError_t launch_prep(cudaStream_t s, const BatchDev& B, const EngineArgs& A, 
 cudaError_t launch_pcg_cluster(cudaStream_t s, const BatchDev& B, int32_t* wait, int cap, int clusters, int kind);
 // Clusters of PCG kind `kind` that fit on the device at once (0 if the query fails)
 int max_active_clusters(int kind);
+// The whole-GPU PCG of the FP32 instances of kind 3 (above the cluster size): `pairs` PCG
+// iterations (k_gpcg_a: p update + SpMV + p.q; k_gpcg_b: vector update + r.r, r.z) over the
+// instances the engine listed; an instance that leaves its PCG is skipped from then on and
+// counted off wait[kWaitLeft].  grid: CTAs of 128 threads (gpcg_grid).
+int gpcg_grid(int num_sms);
+cudaError_t launch_gpcg(cudaStream_t s, const BatchDev& B, const EngineArgs& A, int grid, int pairs,
+                        cudaEvent_t* ev = nullptr);
 // The whole solve loop as one graph: while instances are active, k_prep, k_engine, the cluster
 // PCG kernels (clusters[k] clusters of kind k + 1; 0 leaves it out) and k_loop_end, which sets
 // the loop condition from the engine's flags (no instance active, a barrier or cluster wait gave
 // up, or loop_cap passes) and counts the passes in loops[0].
+// gpcg > 0 adds the kind-3 loop (k_gpcg_begin, then while instances iterate: k_gpcg_a,
+// k_gpcg_b, k_gpcg_loop) with gpcg CTAs per kernel.
 cudaError_t build_solve_graph(bool fp64, int grid, const BatchDev& B, const EngineArgs& A, int max_chunks,
-                              const int clusters[2], int32_t* loops, int loop_cap, cudaGraph_t* graph,
+                              const int clusters[2], int gpcg, int32_t* loops, int loop_cap, cudaGraph_t* graph,
                               cudaGraphExec_t* exec);
 // One stage as its own kernel, for the evaluation entry points: K_ELEM_EG, K_GATHER,
 // K_ELEM_HESS or K_ASSEMBLE (other ids launch nothing; their stages run inside k_engine)

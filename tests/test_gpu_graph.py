@@ -89,3 +89,29 @@ def test_tuner_leaves_instances_and_results_unchanged(gpu_ctx, defaults):
     reps, xs = gpu_ctx.batch_solve(insts, o, [m.X0.ravel().copy() for m in meshes])
     _same(ref, (reps, xs))
     assert gpu_ctx.launch_settings() == defaults  # the defaults themselves are not changed
+
+
+def test_whole_gpu_pcg_kernels_give_the_engine_bits(gpu_ctx, defaults):
+    """An FP32 instance above the cluster size (15,379 nodes) iterates its PCG in k_gpcg_a/b
+    (pcg_cluster 1, the default) or inside the engine (pcg_cluster 0): the same tiles, partial
+    sums and decisions, so the same bits; alone and beside cluster instances, on the graph and
+    on the host loop."""
+    big = M.cantilever(12, 12, 90)
+    assert big.n > 13000
+    small = [M.batch_instance(3, i) for i in range(60, 63)]
+    kw = dict(precision=px.PREC_FP32_REFINE, tol_rel=1e-6, tol_max_error=0.0, tol_min_impr=0.0, tol_min_step=0.0)
+    ref = _solve(gpu_ctx, [big], px.options(pcg_cluster=0, **kw))
+    assert ref[0][0]["result_name"] == "SUCCESS"
+    for graph in (1, 0):
+        gpu_ctx.launch_settings(graph=graph)
+        _same(ref, _solve(gpu_ctx, [big], px.options(**kw)))
+        mixed = _solve(gpu_ctx, small + [big], px.options(**kw))
+        _same(ref, ([mixed[0][-1]], [mixed[1][-1]]))
+    # profiling (host loop, events around each kernel): the kernels' time and bytes are recorded
+    gpu_ctx.profile(True)
+    gpu_ctx.profile_reset()
+    _same(ref, _solve(gpu_ctx, [big], px.options(**kw)))
+    n, ms = gpu_ctx.profile_read("spmv")
+    nbytes = gpu_ctx.profile_bytes("spmv")
+    gpu_ctx.profile(False)
+    assert n > 0 and ms > 0 and nbytes > 0
