@@ -2611,11 +2611,23 @@ cudaError_t launch_prep(cudaStream_t s, const BatchDev& B, const EngineArgs& A, 
   return cudaGetLastError();
 }
 
+// The waiting list, its count and its take counter for cluster PCG kind 1 or 2 (one place for
+// the host launch and the graph).
+struct ClusterArgs {
+  const int32_t* list;
+  const int32_t* count;
+  int32_t* take;
+};
+ClusterArgs cluster_args(int32_t* wait, int cap, int kind) {
+  return ClusterArgs{wait + kWaitLists + (kind - 1) * cap, wait + kWaitCount + (kind - 1), wait + kWaitTake + (kind - 1)};
+}
+
 cudaError_t launch_pcg_cluster(cudaStream_t s, const BatchDev& B, int32_t* wait, int cap, int clusters, int kind) {
   if (clusters <= 0) return cudaSuccess;
-  const int32_t* list = wait + kWaitLists + (kind - 1) * cap;
-  const int32_t* count = wait + kWaitCount + (kind - 1);
-  int32_t* take = wait + kWaitTake + (kind - 1);
+  const ClusterArgs c = cluster_args(wait, cap, kind);
+  const int32_t* list = c.list;
+  const int32_t* count = c.count;
+  int32_t* take = c.take;
   if (kind == 1) k_pcg_cg<kCl, kClThreads><<<clusters * kCl, kClThreads, kCgSmem, s>>>(B, list, count, take);
   else k_pcg_cluster<float, kCl, kClThreads><<<clusters * kCl, kClThreads, 0, s>>>(B, list, count, take);
   return cudaGetLastError();
@@ -2758,9 +2770,10 @@ cudaError_t build_solve_graph(bool fp64, int grid, const BatchDev& B, const Engi
     }
     for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
       if (clusters[k] <= 0) continue;
-      int32_t* list = A.wait + 4 + k * A.cap;
-      const int32_t* countp = A.wait + k;
-      int32_t* next = A.wait + 2 + k;
+      const ClusterArgs c = cluster_args(A.wait, A.cap, k + 1);
+      const int32_t* list = c.list;
+      const int32_t* countp = c.count;
+      int32_t* next = c.take;
       void* ca[] = {&b, &list, &countp, &next};
       const void* fn = k == 0 ? (const void*)k_pcg_cg<kCl, kClThreads> : (const void*)k_pcg_cluster<float, kCl, kClThreads>;
       e = add_kernel(body, &node, &prev, fn, dim3(clusters[k] * kCl), dim3(kClThreads), k == 0 ? kCgSmem : 0, ca);
