@@ -461,6 +461,7 @@ def run_batch(args, world, rank, dist):
         "spmv_gbs": None if spmv_gbs is None else round(spmv_gbs, 1),
         "pcg_cluster_gbs": pcg_gbs,
         "kernels_ms": {k: round(v["ms"], 3) for k, v in prof.items()},
+        "kernels_n": {k: int(v["launches"]) for k, v in prof.items()},
         "kernel_launches": {"k_engine": int(eng_launches), "k_pcg_cg": int(cl_launches), "cluster_steps": int(cl_steps),
                             "note": "profiled pass (host-driven loop with per-launch events): "
                                     "ms_per_step_profiled"},
