@@ -296,6 +296,8 @@ def run_batch(args, world, rank, dist):
     tets = sum(m.m for m in meshes)
     ctx = px.Context(args.device, arena_bytes=int(args.arena_gb * (1 << 30)))
     insts = ctx.create_instances(meshes)  # host parts built in parallel; same instances as one by one
+    if args.no_graph:
+        ctx.launch_settings(graph=0)
     served = served_options(px, args)
     plain = px.options(precision=px.PREC_FP64, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0,
                        tol_min_step=0.0, pcg_chunk=args.pcg_chunk, ls_num_max_iters=args.plain_pcg_max,
@@ -990,6 +992,8 @@ def main():
                     help="served FP32 PCG at negative curvature: 0 truncate, 1 go on like Eigen's CG")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch settings (no batch tuner)")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="host-driven solve loop instead of graph launches (a profiler then sees the engine)")
     ap.add_argument("--large-oracle", action="store_true",
                     help="large workload: solve it with the oracle on the host cores too and compare")
     ap.add_argument("--large-oracle-tol", type=float, default=1e-8,
