@@ -1190,33 +1190,6 @@ template <typename Real, bool kGrid = false>
 __device__ __forceinline__ bool pcg_here(const BatchDev& B, const InstDev& I) {
   return kGrid ? I.pcg_cluster == 3 : !cluster_owned(B, I);
 }
-// Bulk prefetch of [p, p + bytes) into L2 (TMA, no registers or shared memory involved): the
-// range starts on a 16-byte boundary (rounded down) and is covered in pieces of at most 32 KB
-// rounded up to 16 bytes (device buffers come from the arena in 256-byte blocks, so the
-// rounding stays inside the buffer).
-__device__ __forceinline__ void prefetch_l2(const void* p, uint64_t bytes) {
-  uint64_t a = reinterpret_cast<uint64_t>(p);
-  const uint64_t end = a + bytes;
-  a &= ~(uint64_t)15;
-  while (a < end) {
-    const uint32_t n = (uint32_t)min((uint64_t)32768, (end - a + 15) & ~(uint64_t)15);
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"(n) : "memory");
-    a += n;
-  }
-}
-
-// The matrix slice and column ids of PCG tile t of map M (FP32 rows), prefetched into L2.
-__device__ __forceinline__ void prefetch_pcg_tile(const BatchDev& B, const TileMap& M, int t) {
-  if (t >= map_total(M)) return;
-  int i, lt;
-  map_tile(M, t, i, lt);
-  const InstDev& I = B.inst[i];
-  const int ch0 = lt * B.cpt, ch1 = min(ch0 + B.cpt, I.nchunks);
-  const int64_t s0 = __ldg(I.chunk_off + ch0), s1 = __ldg(I.chunk_off + ch1);
-  prefetch_l2(I.H32 + (s0 >> 5) * 288, (uint64_t)((s1 - s0) >> 5) * 288 * sizeof(float));
-  prefetch_l2(I.slot_col + s0, (uint64_t)(s1 - s0) * sizeof(int32_t));
-}
-
 // an instance of PCG kind 3 leaves the grid kernel's loop
 __device__ __forceinline__ void gpcg_left(int32_t* left) {
   if (left) atomicSub(left, 1);
@@ -1239,9 +1212,6 @@ __device__ __forceinline__ void st_pcg_a(const BatchDev& B, const TileMap& M, in
     std::conditional_t<kGrid, const InstDev&, const InstDev> I = B.inst[i];  // the engine keeps a copy in registers
     NState* st = I.st;
     if (st->phase != PH_PCG || !pcg_here<Real, kGrid>(B, I)) continue;
-    // the whole-GPU kernel streams the matrix: the CTA's next tile is fetched into L2 while
-    // this one is worked on
-    if (kGrid && threadIdx.x == 0) prefetch_pcg_tile(B, M, t + ncta);
     Real p[1] = {(Real)0};  // per-tile inner product in the PCG's own precision
     {
       const int par = st->pcg_parity;
@@ -2689,10 +2659,7 @@ __global__ void __launch_bounds__(kTile, kGpcgBlocks) k_gpcg_b(BatchDev B, Engin
   __shared__ double sm[32 * 5];
   __shared__ int flag;
   B.cpt = __ldcg(A.cfg);
-  const TileMap M = gpcg_map(A);
-  // the first tile this CTA's k_gpcg_a will take next (same grid, same map) goes to L2 now
-  if (threadIdx.x == 0) prefetch_pcg_tile(B, M, blockIdx.x);
-  st_pcg_b<float, true>(B, M, blockIdx.x, gridDim.x, sm, flag, A.wait + kWaitLeft);
+  st_pcg_b<float, true>(B, gpcg_map(A), blockIdx.x, gridDim.x, sm, flag, A.wait + kWaitLeft);
 }
 
 // graph form: the loop runs while a kind-3 instance iterates (at most cap passes per launch)
