@@ -172,7 +172,7 @@ struct phx_context_s {
   int ccount = 0;               // instances of the batch whose PCG runs outside the engine
   int ckind_count[4] = {0, 0, 0, 0};  // ... of each PCG kind (1, 2: clusters, 3: whole-GPU kernels)
   int gmax[3] = {-1, -1, -1};   // clusters of kinds 1, 2 resident at once (-1: not queried yet)
-  int ggrid[2] = {0, 0};        // CTAs of the whole-GPU PCG kernels k_gpcg_a, k_gpcg_b
+  int ggrid = 0;                // CTAs of the whole-GPU PCG kernels
   // scheduling of batch solves (defaults, and tuned settings per batch mix)
   phx_launch_settings launch{1, kWaitRounds, kWaitShare, kRoundsPerLaunch};
   std::map<std::string, phx_launch_settings> tuned;
@@ -688,8 +688,7 @@ int cluster_count(phx_context ctx, int kind, int waiting) {
 constexpr int kGpcgBlock = 16;
 
 int run_gpcg(phx_context ctx, const BatchDev& B, const phx_launch_settings& S, int pcg_chunk) {
-  if (ctx->ggrid[0] == 0)
-    for (int k = 0; k < 2; ++k) ctx->ggrid[k] = gpcg_grid(ctx->num_sms, k);
+  if (ctx->ggrid == 0) ctx->ggrid = gpcg_grid(ctx->num_sms);
   const EngineArgs A = engine_args(ctx, S, pcg_chunk);
   for (int64_t it = 0;; it += kGpcgBlock) {
     for (int k = 0; k < kGpcgBlock; ++k) {
@@ -763,15 +762,13 @@ int run_graph(phx_context ctx, const BatchDev& B0, int num, bool fp64, int pcg_c
   int clusters[2] = {0, 0};
   for (int kind = 1; kind <= 2; ++kind)
     if (B.cluster_mode && ctx->ckind_count[kind] > 0) clusters[kind - 1] = cluster_count(ctx, kind, ctx->ckind_count[kind]);
-  if (ctx->ggrid[0] == 0)
-    for (int k = 0; k < 2; ++k) ctx->ggrid[k] = gpcg_grid(ctx->num_sms, k);
-  const bool kind3 = B.cluster_mode && ctx->ckind_count[3] > 0;
-  const int gpcg[2] = {kind3 ? ctx->ggrid[0] : 0, kind3 ? ctx->ggrid[1] : 0};
+  if (ctx->ggrid == 0) ctx->ggrid = gpcg_grid(ctx->num_sms);
+  const int gpcg = (B.cluster_mode && ctx->ckind_count[3] > 0) ? ctx->ggrid : 0;
   // the graph holds its kernels' arguments: rebuilt when any of them changes
   std::string key;
   auto put = [&](const void* p, size_t n) { key.append(static_cast<const char*>(p), n); };
   put(&fp64, sizeof(fp64)); put(&grid, sizeof(grid)); put(&B, sizeof(B)); put(&A, sizeof(A));
-  put(&max_chunks, sizeof(max_chunks)); put(clusters, sizeof(clusters)); put(gpcg, sizeof(gpcg));
+  put(&max_chunks, sizeof(max_chunks)); put(clusters, sizeof(clusters)); put(&gpcg, sizeof(gpcg));
   if (!ctx->gexec || key != ctx->gkey) {
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
     if (ctx->graph) cudaGraphDestroy(ctx->graph);
@@ -782,7 +779,7 @@ int run_graph(phx_context ctx, const BatchDev& B0, int num, bool fp64, int pcg_c
                          &ctx->gexec));
     ctx->gkey = key;
   }
-  const int per_pass = 3 + (clusters[0] > 0) + (clusters[1] > 0) + (gpcg[0] > 0);
+  const int per_pass = 3 + (clusters[0] > 0) + (clusters[1] > 0) + (gpcg > 0);
   for (;;) {
     CU(cudaMemsetAsync(ctx->d_cfg + 1, 0, 2 * sizeof(int32_t), ctx->stream));
     CU(cudaGraphLaunch(ctx->gexec, ctx->stream));

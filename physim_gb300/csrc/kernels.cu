@@ -1202,33 +1202,6 @@ __device__ __forceinline__ void advance_pcg(const BatchDev& B, int i) {
   else advance(B, i);
 }
 
-// The decisions after p.q of an instance (one thread of the CTA that completed its tiles).
-template <bool kGrid>
-__device__ __forceinline__ void pcg_a_finish(const BatchDev& B, const InstDev& I, int i, double pq, int32_t* left) {
-  NState* st = I.st;
-  count_bytes(B, I, K_PCG_A);
-  st->pq = pq;
-  if ((I.opts->precision == 0 || I.opts->curv_through) && pq < 0.0) {
-    // Eigen's ConjugateGradient has no curvature test: a negative p.q gives a negative
-    // step along p and the iteration goes on; LinearSolver_EigenCG regularises only
-    // when the result fails b.x >= 0 (LinearSolver_EigenCG.cpp:95-107)
-    st->alpha = st->rz / pq;
-  } else if (!(pq > 0.0)) {  // not positive definite along p (or non-finite)
-    if (I.opts->precision != 0 && pq < 0.0 && st->pcg_iter == 0) {
-      // truncated CG, first direction: step along p with |p.q| and stop
-      st->alpha = st->rz / -pq;
-      st->truncate = 1;
-    } else {
-      st->lin_status = (I.opts->precision != 0 && pq < 0.0) ? LIN_TRUNCATED : LIN_BREAKDOWN;
-      st->phase = (st->lin_status == LIN_TRUNCATED) ? PH_ACCUM : PH_LIN_DONE;
-      advance_pcg<kGrid>(B, i);
-      if (kGrid) gpcg_left(left);
-    }
-  } else {
-    st->alpha = st->rz / pq;
-  }
-}
-
 template <typename Real, bool kGrid = false>
 __device__ __forceinline__ void st_pcg_a(const BatchDev& B, const TileMap& M, int cta, int ncta, double* sm, int& flag,
                                          int32_t* left = nullptr) {
@@ -1275,8 +1248,29 @@ __device__ __forceinline__ void st_pcg_a(const BatchDev& B, const TileMap& M, in
       }
     }
     double tot[1];
-    if (tile_done<1>(I, lt, pcg_tiles(B, I), ncta, p, tot, sm, &flag) && threadIdx.x == 0)
-      pcg_a_finish<kGrid>(B, I, i, tot[0], left);
+    if (tile_done<1>(I, lt, pcg_tiles(B, I), ncta, p, tot, sm, &flag) && threadIdx.x == 0) {
+      count_bytes(B, I, K_PCG_A);
+      st->pq = tot[0];
+      if ((I.opts->precision == 0 || I.opts->curv_through) && tot[0] < 0.0) {
+        // Eigen's ConjugateGradient has no curvature test: a negative p.q gives a negative
+        // step along p and the iteration goes on; LinearSolver_EigenCG regularises only
+        // when the result fails b.x >= 0 (LinearSolver_EigenCG.cpp:95-107)
+        st->alpha = st->rz / tot[0];
+      } else if (!(tot[0] > 0.0)) {  // not positive definite along p (or non-finite)
+        if (I.opts->precision != 0 && tot[0] < 0.0 && st->pcg_iter == 0) {
+          // truncated CG, first direction: step along p with |p.q| and stop
+          st->alpha = st->rz / -tot[0];
+          st->truncate = 1;
+        } else {
+          st->lin_status = (I.opts->precision != 0 && tot[0] < 0.0) ? LIN_TRUNCATED : LIN_BREAKDOWN;
+          st->phase = (st->lin_status == LIN_TRUNCATED) ? PH_ACCUM : PH_LIN_DONE;
+          advance_pcg<kGrid>(B, i);
+          if (kGrid) gpcg_left(left);
+        }
+      } else {
+        st->alpha = st->rz / tot[0];
+      }
+    }
   }
 }
 
@@ -2568,8 +2562,6 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_pcg_cg(Bat
 template <typename Real>
 size_t hess_smem() { return (size_t)kTile * 90 * sizeof(Real); }
 
-cudaError_t setup_gpcg_attributes();  // below, with the whole-GPU PCG kernels
-
 cudaError_t setup_kernel_attributes() {
   cudaError_t e = cudaFuncSetAttribute(k_elem_hess<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)hess_smem<double>());
@@ -2581,7 +2573,6 @@ cudaError_t setup_kernel_attributes() {
     e = cudaFuncSetAttribute(k_engine<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hess_smem<float>());
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_pcg_cg<kCl, kClThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, kCgSmem);
-  if (e == cudaSuccess) e = setup_gpcg_attributes();
 
   return e;
 }
@@ -2650,234 +2641,18 @@ cudaError_t launch_pcg_cluster(cudaStream_t s, const BatchDev& B, int32_t* wait,
 // synchronisation.  Tiles, partial sums and decisions are the engine's (same tile width from
 // k_prep, per-tile partials summed in tile order), so an instance gets the bits it gets when
 // the engine iterates its PCG.
-constexpr int kGpcgBlocks = 6;  // resident CTAs per SM k_gpcg_b is built for (24 warps; 8 spills and is slower)
+constexpr int kGpcgBlocks = 6;  // resident CTAs per SM the whole-GPU PCG kernels are built for (24 warps)
 
 __device__ __forceinline__ TileMap gpcg_map(const EngineArgs& A) {
   const int32_t* W = A.wait;
   return TileMap{W + kWaitLists + 3 * A.cap, W + kWaitLists + 2 * A.cap, __ldcg(W + kWaitCount + 2)};
 }
 
-// k_gpcg_a streams the matrix through shared memory.  Each CTA walks its chunks (its tiles
-// t = cta, cta + ncta, ..., each tile's chunks in order) with kGsStages chunks in flight: thread
-// 0 copies a chunk's SELL slot-rows (values, then column ids) into a stage with two TMA bulk
-// copies completing on the stage's mbarrier, and refills the stage once the CTA has used it.
-// A chunk longer than kGsSlots slot-rows is read from global memory instead.  The arithmetic
-// is the engine's SpMV stage's, term for term: lane sub of a row takes slots sub, sub + 4, ...,
-// the four lane sums are added as (l0 + l1) + (l2 + l3), and the tile's p.q partials enter the
-// tile reduction in the engine's thread layout, so the results keep the engine's bits.  Here
-// warp w holds lane w of 32 rows (one slot-row of 32 values per load, no bank conflicts).
-constexpr int kGsStages = 4;                                   // chunks in flight per CTA
-constexpr int kGsSlots = 20;                                   // slot-rows a stage holds
-constexpr int kGsValBytes = kGsSlots * 288 * 4;                // 9 planes x 32 rows of FP32 per slot-row
-constexpr int kGsStageBytes = kGsValBytes + kGsSlots * 32 * 4; // + the column ids
-constexpr int kGsSmem = kGsStages * kGsStageBytes;             // 100 KB: two CTAs per SM
-constexpr long long kGsWaitCycles = 2000000000LL;              // a stage wait gives up after about 1 s
-
-struct GsItem {
-  int t, i, lt, ch, ch1;  // tile t (instance i, its tile lt), chunk ch of the tile's [.., ch1)
-};
-
-// The CTA's next tile from t on whose instance iterates its PCG in this kernel.
-__device__ __forceinline__ bool gs_tile(const BatchDev& B, const TileMap& M, int total, int ncta, int t, GsItem& it) {
-  for (; t < total; t += ncta) {
-    int i, lt;
-    map_tile(M, t, i, lt);
-    const InstDev& I = B.inst[i];
-    // an instance's phase changes only after all its tiles are done, so every read here agrees
-    if (I.pcg_cluster != 3 || *(volatile int32_t*)&I.st->phase != PH_PCG) continue;
-    it.t = t;
-    it.i = i;
-    it.lt = lt;
-    it.ch = lt * B.cpt;
-    it.ch1 = min(it.ch + B.cpt, I.nchunks);
-    return true;
-  }
-  return false;
-}
-__device__ __forceinline__ bool gs_next(const BatchDev& B, const TileMap& M, int total, int ncta, GsItem& it) {
-  if (++it.ch < it.ch1) return true;
-  return gs_tile(B, M, total, ncta, it.t + ncta, it);
-}
-
-// Thread 0: chunk it.ch into stage stg (or, for a long chunk, just complete the stage's phase).
-__device__ __forceinline__ void gs_issue(const BatchDev& B, const GsItem& it, int stg, unsigned char* gs,
-                                         uint64_t* mbar, int* glen) {
-  const InstDev& I = B.inst[it.i];
-  const int64_t s0 = __ldg(I.chunk_off + it.ch), s1 = __ldg(I.chunk_off + it.ch + 1);
-  const int len = (int)((s1 - s0) >> 5);
-  const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[stg]);
-  if (len > kGsSlots || len == 0) {
-    glen[stg] = -1;
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mb) : "memory");
-    return;
-  }
-  glen[stg] = len;
-  const uint32_t dv = (uint32_t)__cvta_generic_to_shared(gs + (size_t)stg * kGsStageBytes);
-  const uint32_t dc = dv + kGsValBytes;
-  const uint32_t bv = (uint32_t)len * 288 * 4, bc = (uint32_t)len * 32 * 4;
-  // source and destination 16-byte aligned (chunks are whole slot-rows of 1152 and 128 bytes
-  // in 256-byte aligned buffers), sizes multiples of 16
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bv + bc) : "memory");
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-               ::"r"(dv), "l"(I.H32 + (s0 >> 5) * 288), "r"(bv), "r"(mb) : "memory");
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-               ::"r"(dc), "l"(I.slot_col + s0), "r"(bc), "r"(mb) : "memory");
-}
-
-__device__ __forceinline__ bool gs_wait(uint64_t* bar, unsigned parity, long long limit) {
-  const uint32_t mb = (uint32_t)__cvta_generic_to_shared(bar);
-  const long long t0 = clock64();
-  for (;;) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(mb), "r"(parity)
-        : "memory");
-    if (done) return true;
-    if (clock64() - t0 > limit) return false;
-  }
-}
-
-__global__ void __launch_bounds__(kTile, 2) k_gpcg_a(BatchDev B, EngineArgs A) {
-  extern __shared__ __align__(128) unsigned char gs[];  // kGsStages stages
-  __shared__ __align__(8) uint64_t mbar[kGsStages];
-  __shared__ float racc[3][3][32];  // lanes 1..3 of each row: their partial sums
-  __shared__ float prow[32];        // each row position's p.q over the tile's chunks
-  __shared__ int glen[kGsStages];   // slot-rows staged, -1: the chunk is read from global memory
+__global__ void __launch_bounds__(kTile, kGpcgBlocks) k_gpcg_a(BatchDev B, EngineArgs A) {
   __shared__ double sm[32 * 5];
   __shared__ int flag;
   B.cpt = __ldcg(A.cfg);
-  const TileMap M = gpcg_map(A);
-  const int total = map_total(M), ncta = gridDim.x, tid = threadIdx.x;
-  const int r = tid & 31, sub = tid >> 5;
-  int32_t* left = A.wait + kWaitLeft;
-  if (tid == 0) {
-    for (int k = 0; k < kGsStages; ++k)
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&mbar[k]))
-                   : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  __syncthreads();
-  GsItem pit;  // producer (thread 0): the next chunk to copy
-  bool pmore = false;
-  int issued = 0;
-  if (tid == 0) {
-    pmore = gs_tile(B, M, total, ncta, blockIdx.x, pit);
-    for (; issued < kGsStages && pmore; ++issued) {
-      gs_issue(B, pit, issued, gs, mbar, glen);
-      pmore = gs_next(B, M, total, ncta, pit);
-    }
-  }
-  GsItem it;
-  bool more = gs_tile(B, M, total, ncta, blockIdx.x, it);
-  float pacc = 0.f;  // lane 0 of row r: its p.q terms over the tile's chunks (the engine's order)
-  for (int j = 0; more; ++j) {
-    const int stg = j % kGsStages;
-    const bool ok = gs_wait(&mbar[stg], (unsigned)(j / kGsStages) & 1u, kGsWaitCycles);
-    if (__syncthreads_or(!ok)) {
-      // a stage never arrived: flag the batch (the host reports PHX_ETIMEOUT), wait a bounded
-      // time for the copies still in flight into this CTA's stages, and leave
-      if (tid == 0) {
-        atomicExch(B.flags + 2, 1);
-        for (int q = j; q < issued; ++q) gs_wait(&mbar[q % kGsStages], (unsigned)(q / kGsStages) & 1u, kCgDrainCycles);
-      }
-      return;
-    }
-    const InstDev& I = B.inst[it.i];
-    NState* st = I.st;
-    const int par = st->pcg_parity;
-    const float* pold = par ? I.p32b : I.p32a;
-    float* pnew = par ? I.p32a : I.p32b;
-    const float* z = I.z32;
-    const float beta = (float)st->beta, sh = (float)st->shift;
-    const int v = it.ch * 32 + r;
-    const bool valid = v < I.n;
-    const int len = glen[stg];
-    const float* hs = reinterpret_cast<const float*>(gs + (size_t)stg * kGsStageBytes);
-    const int* cs = reinterpret_cast<const int*>(gs + (size_t)stg * kGsStageBytes + kGsValBytes);
-    float acc[3] = {0.f, 0.f, 0.f};
-    if (valid) {
-      const int64_t s0 = __ldg(I.chunk_off + it.ch);
-      const int n_slots = len >= 0 ? len : (int)((__ldg(I.chunk_off + it.ch + 1) - s0) >> 5);
-      for (int k0 = sub; k0 < n_slots; k0 += 16) {
-        int col[4];
-        float h[4][9];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int k = k0 + u * 4;
-          const bool in = k < n_slots;
-          if (len >= 0) {
-            col[u] = in ? cs[k * 32 + r] : -1;
-#pragma unroll
-            for (int q = 0; q < 9; ++q) h[u][q] = in ? hs[k * 288 + q * 32 + r] : 0.f;
-          } else {
-            const int64_t sl = s0 + (int64_t)(in ? k : 0) * 32 + r;
-            col[u] = in ? __ldg(I.slot_col + sl) : -1;
-            const float* hp = I.H32 + (sl >> 5) * 288 + (sl & 31);
-#pragma unroll
-            for (int q = 0; q < 9; ++q) h[u][q] = in ? hp[q * 32] : 0.f;
-          }
-        }
-        float xc[4][3];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          if (col[u] >= 0) {
-            float zc[3], pc[3];
-            ld4(z, col[u], zc);
-            ld4(pold, col[u], pc);
-            for (int a = 0; a < 3; ++a) xc[u][a] = zc[a] + beta * pc[a];
-          } else {
-            xc[u][0] = xc[u][1] = xc[u][2] = 0.f;
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-#pragma unroll
-          for (int a = 0; a < 3; ++a) acc[a] += h[u][3 * a] * xc[u][0] + h[u][3 * a + 1] * xc[u][1] + h[u][3 * a + 2] * xc[u][2];
-      }
-    }
-    if (sub > 0)
-#pragma unroll
-      for (int a = 0; a < 3; ++a) racc[sub - 1][a][r] = acc[a];
-    __syncthreads();
-    if (sub == 0 && valid) {
-      float pv[3], zv[3];
-      ld4(z, v, zv);
-      ld4(pold, v, pv);
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        acc[a] = (acc[a] + racc[0][a][r]) + (racc[1][a][r] + racc[2][a][r]);
-        pv[a] = zv[a] + beta * pv[a];
-        acc[a] += sh * pv[a];
-      }
-      st4(pnew, v, pv);
-      st4(I.q32, v, acc);
-      pacc += pv[0] * acc[0] + pv[1] * acc[1] + pv[2] * acc[2];
-    }
-    const bool tile_end = it.ch + 1 >= it.ch1;
-    const GsItem cur = it;
-    more = gs_next(B, M, total, ncta, it);
-    __syncthreads();  // the stage and racc are free again
-    if (tid == 0 && pmore) {
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // our reads before the async writes
-      gs_issue(B, pit, issued % kGsStages, gs, mbar, glen);
-      ++issued;
-      pmore = gs_next(B, M, total, ncta, pit);
-    }
-    if (tile_end) {
-      if (sub == 0) prow[r] = pacc;
-      pacc = 0.f;
-      __syncthreads();
-      // the engine's layout: thread 4 * row holds the row's partial, the others zero
-      float p[1] = {(tid & 3) == 0 ? prow[tid >> 2] : 0.f};
-      double tot[1];
-      const InstDev& Ic = B.inst[cur.i];
-      if (tile_done<1>(Ic, cur.lt, pcg_tiles(B, Ic), ncta, p, tot, sm, &flag) && tid == 0)
-        pcg_a_finish<true>(B, Ic, cur.i, tot[0], left);
-    }
-  }
+  st_pcg_a<float, true>(B, gpcg_map(A), blockIdx.x, gridDim.x, sm, flag, A.wait + kWaitLeft);
 }
 
 __global__ void __launch_bounds__(kTile, kGpcgBlocks) k_gpcg_b(BatchDev B, EngineArgs A) {
@@ -2900,29 +2675,24 @@ __global__ void k_gpcg_loop(EngineArgs A, cudaGraphConditionalHandle h, int cap)
   cudaGraphSetConditional(h, (A.wait[kWaitLeft] > 0 && pass < cap) ? 1u : 0u);
 }
 
-cudaError_t setup_gpcg_attributes() {
-  return cudaFuncSetAttribute(k_gpcg_a, cudaFuncAttributeMaxDynamicSharedMemorySize, kGsSmem);
-}
-
-int gpcg_grid(int num_sms, int which) {
-  int nb = 0;
-  const cudaError_t e = which == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_gpcg_a, kTile, kGsSmem)
-                                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_gpcg_b, kTile, 0);
-  if (e != cudaSuccess) {
+int gpcg_grid(int num_sms) {
+  int na = 0, nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&na, k_gpcg_a, kTile, 0) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_gpcg_b, kTile, 0) != cudaSuccess) {
     cudaGetLastError();
     return num_sms;
   }
-  return std::max(1, nb) * num_sms;
+  return std::max(1, std::min(na, nb)) * num_sms;
 }
 
-cudaError_t launch_gpcg(cudaStream_t s, const BatchDev& B, const EngineArgs& A, const int grid[2], int pairs,
+cudaError_t launch_gpcg(cudaStream_t s, const BatchDev& B, const EngineArgs& A, int grid, int pairs,
                         cudaEvent_t* ev) {
   for (int k = 0; k < pairs; ++k) {
     if (ev) cudaEventRecord(ev[4 * k], s);
-    k_gpcg_a<<<grid[0], kTile, kGsSmem, s>>>(B, A);
+    k_gpcg_a<<<grid, kTile, 0, s>>>(B, A);
     if (ev) cudaEventRecord(ev[4 * k + 1], s);
     if (ev) cudaEventRecord(ev[4 * k + 2], s);
-    k_gpcg_b<<<grid[1], kTile, 0, s>>>(B, A);
+    k_gpcg_b<<<grid, kTile, 0, s>>>(B, A);
     if (ev) cudaEventRecord(ev[4 * k + 3], s);
   }
   return cudaGetLastError();
@@ -2957,8 +2727,8 @@ cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, cudaGraphNode_t* de
 }  // namespace
 
 cudaError_t build_solve_graph(bool fp64, int grid, const BatchDev& B, const EngineArgs& A, int max_chunks,
-                              const int clusters[2], const int gpcg[2], int32_t* loops, int loop_cap,
-                              cudaGraph_t* graph, cudaGraphExec_t* exec) {
+                              const int clusters[2], int gpcg, int32_t* loops, int loop_cap, cudaGraph_t* graph,
+                              cudaGraphExec_t* exec) {
   *graph = nullptr;
   *exec = nullptr;
   cudaGraph_t g = nullptr;
@@ -3009,7 +2779,7 @@ cudaError_t build_solve_graph(bool fp64, int grid, const BatchDev& B, const Engi
       e = add_kernel(body, &node, &prev, fn, dim3(clusters[k] * kCl), dim3(kClThreads), k == 0 ? kCgSmem : 0, ca);
       prev = node;
     }
-    if (gpcg[0] > 0 && e == cudaSuccess) {
+    if (gpcg > 0 && e == cudaSuccess) {
       // the kind-3 PCG: a while-loop inside the pass, its condition set by k_gpcg_begin and
       // k_gpcg_loop (at most loop_cap iterations before the engine runs again)
       cudaGraphConditionalHandle gh;
@@ -3032,9 +2802,8 @@ cudaError_t build_solve_graph(bool fp64, int grid, const BatchDev& B, const Engi
         cudaGraph_t inner = gp.conditional.phGraph_out[0];
         cudaGraphNode_t n1, n2, n3;
         void* ka[] = {&b, &a};
-        e = add_kernel(inner, &n1, nullptr, (const void*)k_gpcg_a, dim3(gpcg[0]), dim3(kTile), kGsSmem, ka);
-        if (e == cudaSuccess)
-          e = add_kernel(inner, &n2, &n1, (const void*)k_gpcg_b, dim3(gpcg[1]), dim3(kTile), 0, ka);
+        e = add_kernel(inner, &n1, nullptr, (const void*)k_gpcg_a, dim3(gpcg), dim3(kTile), 0, ka);
+        if (e == cudaSuccess) e = add_kernel(inner, &n2, &n1, (const void*)k_gpcg_b, dim3(gpcg), dim3(kTile), 0, ka);
         int icap = 1 << 20;
         void* la2[] = {&a, &gh, &icap};
         if (e == cudaSuccess) e = add_kernel(inner, &n3, &n2, (const void*)k_gpcg_loop, dim3(1), dim3(32), 0, la2);

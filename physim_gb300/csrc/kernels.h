@@ -75,20 +75,19 @@ int max_active_clusters(int kind);
 // The whole-GPU PCG of the FP32 instances of kind 3 (above the cluster size): `pairs` PCG
 // iterations (k_gpcg_a: p update + SpMV + p.q; k_gpcg_b: vector update + r.r, r.z) over the
 // instances the engine listed; an instance that leaves its PCG is skipped from then on and
-// counted off wait[kWaitLeft].  grid: CTAs of 128 threads of k_gpcg_a and k_gpcg_b
-// (gpcg_grid(num_sms, 0 / 1): as many as are resident at once).
-int gpcg_grid(int num_sms, int which);
-cudaError_t launch_gpcg(cudaStream_t s, const BatchDev& B, const EngineArgs& A, const int grid[2], int pairs,
+// counted off wait[kWaitLeft].  grid: CTAs of 128 threads (gpcg_grid).
+int gpcg_grid(int num_sms);
+cudaError_t launch_gpcg(cudaStream_t s, const BatchDev& B, const EngineArgs& A, int grid, int pairs,
                         cudaEvent_t* ev = nullptr);
 // The whole solve loop as one graph: while instances are active, k_prep, k_engine, the cluster
 // PCG kernels (clusters[k] clusters of kind k + 1; 0 leaves it out) and k_loop_end, which sets
 // the loop condition from the engine's flags (no instance active, a barrier or cluster wait gave
 // up, or loop_cap passes) and counts the passes in loops[0].
-// gpcg[0] > 0 adds the kind-3 loop (k_gpcg_begin, then while instances iterate: k_gpcg_a,
-// k_gpcg_b, k_gpcg_loop) with gpcg[0] and gpcg[1] CTAs.
+// gpcg > 0 adds the kind-3 loop (k_gpcg_begin, then while instances iterate: k_gpcg_a,
+// k_gpcg_b, k_gpcg_loop) with gpcg CTAs per kernel.
 cudaError_t build_solve_graph(bool fp64, int grid, const BatchDev& B, const EngineArgs& A, int max_chunks,
-                              const int clusters[2], const int gpcg[2], int32_t* loops, int loop_cap,
-                              cudaGraph_t* graph, cudaGraphExec_t* exec);
+                              const int clusters[2], int gpcg, int32_t* loops, int loop_cap, cudaGraph_t* graph,
+                              cudaGraphExec_t* exec);
 // One stage as its own kernel, for the evaluation entry points: K_ELEM_EG, K_GATHER,
 // K_ELEM_HESS or K_ASSEMBLE (other ids launch nothing; their stages run inside k_engine)
 void launch(KernelId id, int grid, cudaStream_t s, const BatchDev& B, bool fp64);
