@@ -275,7 +275,8 @@ def served_options(px, args):
     return px.options(precision=px.PREC_FP32_REFINE, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0,
                       tol_min_step=0.0, pcg_chunk=args.pcg_chunk, inner_tol=args.inner_tol,
                       ls_num_max_iters=args.served_pcg_max, max_refine_sweeps=args.served_sweeps,
-                      lsearch_type=LSEARCH[args.lsearch], negative_curvature=args.curvature)
+                      lsearch_type=LSEARCH[args.lsearch], negative_curvature=args.curvature,
+                      pcg_grid=args.pcg_grid)
 
 
 def batch_config(args, count, tets):
@@ -991,6 +992,8 @@ def main():
     ap.add_argument("--curvature", type=int, default=0, choices=[0, 1],
                     help="served FP32 PCG at negative curvature: 0 truncate, 1 go on like Eigen's CG")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--pcg-grid", type=int, default=1, choices=[0, 1],
+                    help="FP32 instances above 13,000 nodes: 1 PCG in the whole-GPU kernels, 0 in the engine")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch settings (no batch tuner)")
     ap.add_argument("--no-graph", action="store_true",
                     help="host-driven solve loop instead of graph launches (a profiler then sees the engine)")

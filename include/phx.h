@@ -127,6 +127,9 @@ typedef struct phx_options {
                                  truncates the solve there (Steihaug); 1 goes on with a negative step
                                  as Eigen's ConjugateGradient does, which the FP64 path always does,
                                  and regularises when the step is not a descent direction */
+  int32_t pcg_grid;           /* FP32 instances above the cluster size: 1 (default) their PCG iterates in
+                                 the whole-GPU PCG kernels k_gpcg_a/b; 0: inside the engine's PCG stages
+                                 (the same bits; a scheduling choice) */
 } phx_options;
 
 typedef struct phx_report {

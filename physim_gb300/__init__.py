@@ -74,7 +74,8 @@ class Options(C.Structure):
                 ("precond", C.c_int32), ("inner_tol", C.c_double), ("max_refine_sweeps", C.c_int32),
                 ("warm_guess", C.c_int32), ("pcg_chunk", C.c_int32), ("tol_rel", C.c_double),
                 ("pcg_cluster", C.c_int32), ("fp64_finish", C.c_int32),
-                ("lsearch_parallel", C.c_int32), ("negative_curvature", C.c_int32)]
+                ("lsearch_parallel", C.c_int32), ("negative_curvature", C.c_int32),
+                ("pcg_grid", C.c_int32)]
 
 
 class StageGroup_(C.Structure):

@@ -500,6 +500,7 @@ int validate_opts(const phx_options* o) {
     return set_err(PHX_EINVAL, "options: lsearch_parallel out of [0,8]");
   if (o->negative_curvature < 0 || o->negative_curvature > 1)
     return set_err(PHX_EINVAL, "options: negative_curvature must be 0 or 1");
+  if (o->pcg_grid < 0 || o->pcg_grid > 1) return set_err(PHX_EINVAL, "options: pcg_grid must be 0 or 1");
   return PHX_OK;
 }
 
@@ -875,7 +876,8 @@ int start_solve(phx_instance inst, const phx_options* o, bool dynamic, double dt
   // larger FP32 instances iterate in the whole-GPU PCG kernels (kind 3)
   inst->dev.pcg_cluster = (o->pcg_cluster < 1 || o->pcg_cluster > 2 || fp64) ? 0
                           : inst->dev.n <= kClusterMaxNodes                 ? o->pcg_cluster
-                                                                              : 3;
+                          : o->pcg_grid                                     ? 3
+                                                                              : 0;
   CU(cudaMemcpyAsync(inst->d_opts, &d, sizeof(DevOpts), cudaMemcpyHostToDevice, inst->ctx->stream));
   TRY(reset_state(inst, PH_START, 0, 0.0));
   return PHX_OK;
@@ -963,6 +965,7 @@ void phx_default_options(phx_options* o) {
   o->pcg_cluster = 1;
   o->fp64_finish = 1;
   o->lsearch_parallel = 8;
+  o->pcg_grid = 1;
 }
 
 int phx_context_create(int32_t device, int64_t arena_bytes, phx_context* out) {
