@@ -275,8 +275,7 @@ def served_options(px, args):
     return px.options(precision=px.PREC_FP32_REFINE, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0,
                       tol_min_step=0.0, pcg_chunk=args.pcg_chunk, inner_tol=args.inner_tol,
                       ls_num_max_iters=args.served_pcg_max, max_refine_sweeps=args.served_sweeps,
-                      lsearch_type=LSEARCH[args.lsearch], negative_curvature=args.curvature,
-                      pcg_grid=args.pcg_grid)
+                      lsearch_type=LSEARCH[args.lsearch], negative_curvature=args.curvature)
 
 
 def batch_config(args, count, tets):
@@ -296,6 +295,8 @@ def run_batch(args, world, rank, dist):
     meshes = batch_meshes(count, seed=3 + 1000 * rank)
     tets = sum(m.m for m in meshes)
     ctx = px.Context(args.device, arena_bytes=int(args.arena_gb * (1 << 30)))
+    if args.pcg_grid >= 0:
+        ctx.launch_settings(pcg_grid=args.pcg_grid)
     insts = ctx.create_instances(meshes)  # host parts built in parallel; same instances as one by one
     if args.no_graph:
         ctx.launch_settings(graph=0)
@@ -683,6 +684,8 @@ def run_serve(args, world, rank, dist, rates=None, count=None):
     count = count or args.requests
     reqs = serving_requests(count, seed=11)
     ctx = px.Context(args.device, arena_bytes=int(args.serve_arena_gb * (1 << 30)))
+    if args.pcg_grid >= 0:
+        ctx.launch_settings(pcg_grid=args.pcg_grid)
     served = served_options(px, args)
     plain = px.options(precision=px.PREC_FP64, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0,
                        tol_min_step=0.0, ls_num_max_iters=args.plain_pcg_max)
@@ -768,17 +771,18 @@ def run_large(args, world, rank, dist):
     ctx = px.Context(args.device, arena_bytes=int(args.arena_gb * (1 << 30)))
     inst = px.Instance(ctx, m)
     res = {}
-    # served: PCG in the whole-GPU kernels (default) and, for comparison, inside the engine
-    # (the same bits); each timed without profiling, then solved again with per-kernel events
-    for name, prec, pcg_cluster in (("served_fp32_refine", px.PREC_FP32_REFINE, 1),
-                                    ("served_engine_pcg", px.PREC_FP32_REFINE, 0),
-                                    ("plain_fp64", px.PREC_FP64, 0)):
+    # served: PCG in the whole-GPU kernels (launch setting pcg_grid 1) and, for comparison,
+    # inside the engine (pcg_grid 0, the same bits); each timed without profiling, then solved
+    # again with per-kernel events
+    for name, prec, pcg_grid in (("served_fp32_refine", px.PREC_FP32_REFINE, 1),
+                                 ("served_engine_pcg", px.PREC_FP32_REFINE, 0),
+                                 ("plain_fp64", px.PREC_FP64, 0)):
         o = px.options(precision=prec, tol_rel=args.tol_rel, tol_max_error=0.0, tol_min_impr=0.0, tol_min_step=0.0)
         if prec == px.PREC_FP64:
             o.ls_num_max_iters = args.plain_pcg_max
         else:
             o = served_options(px, args)
-        o.pcg_cluster = pcg_cluster
+        ctx.launch_settings(pcg_grid=pcg_grid)
         inst.reset()
         ctx.mark(0)
         x, r = inst.solve_static(o)
@@ -857,6 +861,9 @@ def run_dynamics(args, world, rank, dist):
     n_inst = args.dyn_instances
     meshes = [M.slab_block(5, i) for i in range(n_inst)]
     ctx = px.Context(args.device, arena_bytes=int(args.arena_gb * (1 << 30)))
+    # homogeneous large blocks: their PCG in the whole-GPU kernels (measured 2.6 % faster per
+    # step than inside the engine)
+    ctx.launch_settings(pcg_grid=1 if args.pcg_grid != 0 else 0)
 
     def opts(prec):
         if prec == px.PREC_FP64:
@@ -992,8 +999,10 @@ def main():
     ap.add_argument("--curvature", type=int, default=0, choices=[0, 1],
                     help="served FP32 PCG at negative curvature: 0 truncate, 1 go on like Eigen's CG")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--pcg-grid", type=int, default=1, choices=[0, 1],
-                    help="FP32 instances above 13,000 nodes: 1 PCG in the whole-GPU kernels, 0 in the engine")
+    ap.add_argument("--pcg-grid", type=int, default=-1, choices=[-1, 0, 1],
+                    help="launch setting pcg_grid for FP32 instances above 13,000 nodes: 1 PCG in the whole-GPU "
+                         "kernels, 0 in the engine; -1: the workload's default (dynamics 1, the others the "
+                         "context's default 0; the large workload times both)")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch settings (no batch tuner)")
     ap.add_argument("--no-graph", action="store_true",
                     help="host-driven solve loop instead of graph launches (a profiler then sees the engine)")

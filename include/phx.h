@@ -127,9 +127,6 @@ typedef struct phx_options {
                                  truncates the solve there (Steihaug); 1 goes on with a negative step
                                  as Eigen's ConjugateGradient does, which the FP64 path always does,
                                  and regularises when the step is not a descent direction */
-  int32_t pcg_grid;           /* FP32 instances above the cluster size: 1 (default) their PCG iterates in
-                                 the whole-GPU PCG kernels k_gpcg_a/b; 0: inside the engine's PCG stages
-                                 (the same bits; a scheduling choice) */
 } phx_options;
 
 typedef struct phx_report {
@@ -178,15 +175,21 @@ int phx_debug_unmet_barrier(phx_context ctx, int32_t barrier_tag, int64_t limit_
  *                Profiling (phx_context_profile) always takes the host loop.
  *   wait_rounds  engine rounds an instance may wait for the cluster PCG kernel ...
  *   wait_share   ... or until 1/wait_share of the active instances wait for it
- *   rounds       engine rounds per engine launch */
+ *   rounds       engine rounds per engine launch
+ *   pcg_grid     1: FP32 instances above the cluster size (13,000 nodes) iterate their PCG in the
+ *                whole-GPU kernels k_gpcg_a/b, which run until each such instance has finished
+ *                its linear solve; 0 (default): inside the engine's PCG stages, interleaved with
+ *                the other instances' work (lower latency for small requests beside large ones) */
 typedef struct phx_launch_settings {
   int32_t graph;
   int32_t wait_rounds;
   int32_t wait_share;
   int32_t rounds;
+  int32_t pcg_grid;
 } phx_launch_settings;
 /* Reads the context's default settings into *get (if not NULL), then sets them from *set (if
- * not NULL; values checked: graph 0/1, wait_rounds 1..64, wait_share 1..64, rounds 1..1024). */
+ * not NULL; values checked: graph 0/1, wait_rounds 1..64, wait_share 1..64, rounds 1..1024,
+ * pcg_grid 0/1).  The serving calls use the context's defaults. */
 int phx_context_launch_settings(phx_context ctx, phx_launch_settings* get, const phx_launch_settings* set);
 /* Tunes the settings for a batch: times phx_batch_solve-style solves of the instances from
  * their current positions under the default settings and candidates around them (one

@@ -56,7 +56,8 @@ class Mesh_(C.Structure):
 
 class LaunchSettings_(C.Structure):
     """phx_launch_settings: scheduling of a context's batch solves (changes no result)."""
-    _fields_ = [("graph", C.c_int32), ("wait_rounds", C.c_int32), ("wait_share", C.c_int32), ("rounds", C.c_int32)]
+    _fields_ = [("graph", C.c_int32), ("wait_rounds", C.c_int32), ("wait_share", C.c_int32), ("rounds", C.c_int32),
+                ("pcg_grid", C.c_int32)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
@@ -74,8 +75,7 @@ class Options(C.Structure):
                 ("precond", C.c_int32), ("inner_tol", C.c_double), ("max_refine_sweeps", C.c_int32),
                 ("warm_guess", C.c_int32), ("pcg_chunk", C.c_int32), ("tol_rel", C.c_double),
                 ("pcg_cluster", C.c_int32), ("fp64_finish", C.c_int32),
-                ("lsearch_parallel", C.c_int32), ("negative_curvature", C.c_int32),
-                ("pcg_grid", C.c_int32)]
+                ("lsearch_parallel", C.c_int32), ("negative_curvature", C.c_int32)]
 
 
 class StageGroup_(C.Structure):
@@ -246,7 +246,7 @@ class Context:
         _check(lib().phx_debug_unmet_barrier(self.h, int(tag), int(limit_cycles)))
 
     def launch_settings(self, **changes) -> dict:
-        """The context's default launch settings (graph, wait_rounds, wait_share, rounds); keyword
+        """The context's default launch settings (graph, wait_rounds, wait_share, rounds, pcg_grid); keyword
         arguments change them.  Returns the settings in force after the call."""
         cur = LaunchSettings_()
         _check(lib().phx_context_launch_settings(self.h, C.byref(cur), None))

@@ -174,7 +174,7 @@ struct phx_context_s {
   int gmax[3] = {-1, -1, -1};   // clusters of kinds 1, 2 resident at once (-1: not queried yet)
   int ggrid = 0;                // CTAs of the whole-GPU PCG kernels
   // scheduling of batch solves (defaults, and tuned settings per batch mix)
-  phx_launch_settings launch{1, kWaitRounds, kWaitShare, kRoundsPerLaunch};
+  phx_launch_settings launch{1, kWaitRounds, kWaitShare, kRoundsPerLaunch, 0};
   std::map<std::string, phx_launch_settings> tuned;
   // the whole solve loop as one graph, kept while the batch and launch parameters stay the same
   cudaGraph_t graph = nullptr;
@@ -235,6 +235,7 @@ struct phx_instance_s {
   std::vector<double> saved_x, saved_v;    // positions and velocities kept on the host by an eviction
   uint64_t last_used = 0;                  // server tick of the last request (eviction order)
   // staged boundary conditions (phx_instance_set_staging): the stage persists across solves
+  bool grid_eligible = false;              // FP32 above the cluster size: PCG kind 3 when the launch settings allow
   int32_t stage = 0, num_stages = 0;
   bool stage_values = false;               // a stage moves targets or changes a soft stiffness
   std::vector<double> soft0;               // soft records at stage 0, restored by phx_instance_reset
@@ -500,7 +501,6 @@ int validate_opts(const phx_options* o) {
     return set_err(PHX_EINVAL, "options: lsearch_parallel out of [0,8]");
   if (o->negative_curvature < 0 || o->negative_curvature > 1)
     return set_err(PHX_EINVAL, "options: negative_curvature must be 0 or 1");
-  if (o->pcg_grid < 0 || o->pcg_grid > 1) return set_err(PHX_EINVAL, "options: pcg_grid must be 0 or 1");
   return PHX_OK;
 }
 
@@ -800,6 +800,13 @@ int run_graph(phx_context ctx, const BatchDev& B0, int num, bool fp64, int pcg_c
   }
 }
 
+// The PCG kind of FP32 instances above the cluster size for this run: the whole-GPU kernels
+// (kind 3) or the engine's stages (kind 0); start_solve marks them 3 and sets grid_eligible.
+void apply_pcg_grid(const std::vector<phx_instance>& list, const phx_launch_settings& S) {
+  for (auto* in : list)
+    if (in->grid_eligible) in->dev.pcg_cluster = S.pcg_grid ? 3 : 0;
+}
+
 // Batch mix key of the tuned-settings cache: precision, then instances per power-of-two
 // node-count bucket.
 std::string mix_key(const std::vector<phx_instance>& list, bool fp64) {
@@ -825,6 +832,7 @@ int run_to_completion(phx_context ctx, const std::vector<phx_instance>& list, bo
     auto it = ctx->tuned.find(mix_key(list, fp64));
     if (it != ctx->tuned.end()) S = it->second;
   }
+  apply_pcg_grid(list, S);
   BatchDev B{};
   Grids G;
   TRY(set_batch(ctx, list, B, G));
@@ -874,10 +882,11 @@ int start_solve(phx_instance inst, const phx_options* o, bool dynamic, double dt
   // the cluster PCG serves the FP32 path: FP64 arithmetic is slow on this part and needs
   // every SM, so FP64 solves iterate on the whole GPU
   // larger FP32 instances iterate in the whole-GPU PCG kernels (kind 3)
+  // (kind 3 becomes 0, the engine's PCG stages, unless the launch settings pick the grid kernels)
   inst->dev.pcg_cluster = (o->pcg_cluster < 1 || o->pcg_cluster > 2 || fp64) ? 0
                           : inst->dev.n <= kClusterMaxNodes                 ? o->pcg_cluster
-                          : o->pcg_grid                                     ? 3
-                                                                              : 0;
+                                                                              : 3;
+  inst->grid_eligible = inst->dev.pcg_cluster == 3;
   CU(cudaMemcpyAsync(inst->d_opts, &d, sizeof(DevOpts), cudaMemcpyHostToDevice, inst->ctx->stream));
   TRY(reset_state(inst, PH_START, 0, 0.0));
   return PHX_OK;
@@ -965,7 +974,6 @@ void phx_default_options(phx_options* o) {
   o->pcg_cluster = 1;
   o->fp64_finish = 1;
   o->lsearch_parallel = 8;
-  o->pcg_grid = 1;
 }
 
 int phx_context_create(int32_t device, int64_t arena_bytes, phx_context* out) {
@@ -1763,7 +1771,8 @@ int phx_context_launch_settings(phx_context ctx, phx_launch_settings* get, const
   if (get) *get = ctx->launch;
   if (set) {
     if ((set->graph != 0 && set->graph != 1) || set->wait_rounds < 1 || set->wait_rounds > 64 ||
-        set->wait_share < 1 || set->wait_share > 64 || set->rounds < 1 || set->rounds > 1024)
+        set->wait_share < 1 || set->wait_share > 64 || set->rounds < 1 || set->rounds > 1024 ||
+        (set->pcg_grid != 0 && set->pcg_grid != 1))
       return set_err(PHX_EINVAL, "launch settings out of range");
     ctx->launch = *set;
   }
@@ -1828,6 +1837,13 @@ int phx_tune_batch(phx_context ctx, int32_t count, phx_instance* insts, const ph
   {
     phx_launch_settings c = best;
     c.graph = 1 - c.graph;
+    TRY(consider(c));
+  }
+  bool eligible = false;  // FP32 instances above the cluster size: try the other place for their PCG
+  for (auto* in : list) eligible = eligible || in->grid_eligible;
+  if (eligible) {
+    phx_launch_settings c = best;
+    c.pcg_grid = 1 - c.pcg_grid;
     TRY(consider(c));
   }
   for (int v : {2, 8, 16}) {
@@ -2306,6 +2322,7 @@ int phx_server_progress(phx_server s, int32_t* active, int32_t* queued) {
     if (s->dirty || s->ctx->batch_owner != s) {
       std::vector<phx_instance> list;
       for (auto& r : s->active) list.push_back(r.inst);
+      apply_pcg_grid(list, s->ctx->launch);
       TRY(set_batch(s->ctx, list, s->B, s->G));
       TRY(set_cluster_list(s->ctx, list, &s->ccount));
       s->ctx->batch_owner = s;

@@ -64,7 +64,7 @@ def test_launch_settings_change_no_result(gpu_ctx, defaults):
 
 
 def test_launch_settings_are_checked(gpu_ctx, defaults):
-    for bad in ({"graph": 2}, {"wait_rounds": 0}, {"wait_share": 65}, {"rounds": 0}):
+    for bad in ({"graph": 2}, {"wait_rounds": 0}, {"wait_share": 65}, {"rounds": 0}, {"pcg_grid": 2}):
         with pytest.raises(px.PhxError) as ei:
             gpu_ctx.launch_settings(**bad)
         assert ei.value.code == px.PHX_EINVAL
@@ -82,7 +82,7 @@ def test_tuner_leaves_instances_and_results_unchanged(gpu_ctx, defaults):
         i.set_positions(x)
     t = gpu_ctx.tune_batch(insts, o)
     assert t["trials"] >= 3 and t["best_seconds"] <= t["default_seconds"]
-    assert set(t["chosen"]) == {"graph", "wait_rounds", "wait_share", "rounds"}
+    assert set(t["chosen"]) == {"graph", "wait_rounds", "wait_share", "rounds", "pcg_grid"}
     for i, x in zip(insts, start):
         assert np.array_equal(i.positions(), x)
     # the tuned settings serve this mix now; results are those of the default settings
@@ -93,15 +93,17 @@ def test_tuner_leaves_instances_and_results_unchanged(gpu_ctx, defaults):
 
 def test_whole_gpu_pcg_kernels_give_the_engine_bits(gpu_ctx, defaults):
     """An FP32 instance above the cluster size (15,379 nodes) iterates its PCG in k_gpcg_a/b
-    (pcg_cluster 1, the default) or inside the engine (pcg_cluster 0): the same tiles, partial
-    sums and decisions, so the same bits; alone and beside cluster instances, on the graph and
-    on the host loop."""
+    (launch setting pcg_grid 1) or inside the engine (pcg_grid 0, the default): the same tiles,
+    partial sums and decisions, so the same bits; alone and beside cluster instances, on the
+    graph and on the host loop."""
     big = M.cantilever(12, 12, 90)
     assert big.n > 13000
     small = [M.batch_instance(3, i) for i in range(60, 63)]
     kw = dict(precision=px.PREC_FP32_REFINE, tol_rel=1e-6, tol_max_error=0.0, tol_min_impr=0.0, tol_min_step=0.0)
-    ref = _solve(gpu_ctx, [big], px.options(pcg_cluster=0, **kw))
+    gpu_ctx.launch_settings(pcg_grid=0)
+    ref = _solve(gpu_ctx, [big], px.options(**kw))
     assert ref[0][0]["result_name"] == "SUCCESS"
+    gpu_ctx.launch_settings(pcg_grid=1)
     for graph in (1, 0):
         gpu_ctx.launch_settings(graph=graph)
         _same(ref, _solve(gpu_ctx, [big], px.options(**kw)))
