@@ -176,6 +176,10 @@ struct phx_context_s {
   // scheduling of batch solves (defaults, and tuned settings per batch mix)
   phx_launch_settings launch{1, kWaitRounds, kWaitShare, kRoundsPerLaunch, 0};
   std::map<std::string, phx_launch_settings> tuned;
+  // pinned staging of instance set-ups (grown as needed, reused once its last copy is done)
+  char* stage = nullptr;
+  size_t stage_cap = 0;
+  cudaEvent_t stage_ev = nullptr;
   // the whole solve loop as one graph, kept while the batch and launch parameters stay the same
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -1023,6 +1027,8 @@ int phx_context_destroy(phx_context ctx) {
   if (ctx->d_cfg) cudaFree(ctx->d_cfg);
   if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
   if (ctx->graph) cudaGraphDestroy(ctx->graph);
+  if (ctx->stage) cudaFreeHost(ctx->stage);
+  if (ctx->stage_ev) cudaEventDestroy(ctx->stage_ev);
   for (auto& ev : ctx->marks)
     if (ev) cudaEventDestroy(ev);
   ctx->arena.release();
@@ -1090,23 +1096,106 @@ bool instance_build_host(const phx_mesh* mesh, phx_instance_s* inst, std::string
 // Device bytes instance_setup_device allocates for a built host part, plus the buffers of
 // the arithmetic(s) asked for (the serving admission's estimate; equal to the instance's
 // bytes after the set-up, which a GPU test checks).
-int64_t device_bytes(const HostPattern& hp, bool fp32, bool fp64) {
-  const size_t n = hp.n, m = hp.m, n4 = 4 * n;
-  int64_t b = arena_bytes_of(hp.tets.size(), 4) + arena_bytes_of(hp.rest64.size(), 8) +
-              arena_bytes_of(hp.rest32.size(), 4) +
-              arena_bytes_of(hp.tile_nptr.size(), 4) + arena_bytes_of(hp.tile_nodes.size(), 4) +
-              arena_bytes_of(hp.tet_loc.size(), 2) + arena_bytes_of(hp.model.size(), 1) +
-              arena_bytes_of(hp.chunk_off.size(), 4) + arena_bytes_of(hp.slot_col.size(), 4) +
-              arena_bytes_of(hp.diag_slot.size(), 4) + arena_bytes_of(hp.lo_rc.size(), 4) +
-              arena_bytes_of(hp.lo_slot.size(), 4) + arena_bytes_of(hp.up_slot.size(), 4) +
-              arena_bytes_of(hp.seg_ptr.size(), 4) + arena_bytes_of(hp.seg_c.size(), 4) +
-              arena_bytes_of(hp.nseg_ptr.size(), 4) + arena_bytes_of(hp.nseg_c.size(), 4) +
-              arena_bytes_of(hp.fixmask.size(), 1) + arena_bytes_of(hp.mass.size(), 8) +
-              arena_bytes_of(hp.hlin.size(), 8) + (hp.soft.empty() ? 0 : arena_bytes_of(hp.soft.size(), 8));
-  b += 13 * arena_bytes_of(n4, 8);  // rest positions and the twelve FP64 node vectors
+// An instance's base block in the arena: the arrays uploaded from its host pattern (and its
+// positions, twice: current and rest), then the arrays that start at zero, then per-element
+// scratch, each at a 256-byte aligned offset.  One copy from pinned memory and one memset set
+// it up.
+struct BaseLayout {
+  struct Part {
+    size_t off = 0, bytes = 0;
+  };
+  Part tets, rest64, rest32, tile_nptr, tile_nodes, tet_loc, model, chunk_off, slot_col, diag_slot, lo_rc, lo_slot,
+      up_slot, seg_ptr, seg_c, nseg_ptr, nseg_c, fixmask, mass, hlin, soft, x, xrest;
+  size_t upload_end = 0;
+  Part vec[11], counter, log, st, opts;  // vec: xs, dx, g, gn, dxprev, x0, v0, v, r64, bvec, xback
+  size_t zero_end = 0;
+  Part eloc, gloc, partials;
+  size_t total = 0;
+};
+
+BaseLayout base_layout(const HostPattern& hp) {
+  BaseLayout L;
+  size_t off = 0;
+  auto part = [&](BaseLayout::Part& p, size_t count, size_t elem) {
+    p.off = off;
+    p.bytes = std::max<size_t>(count, 1) * elem;
+    off += (p.bytes + 255) & ~(size_t)255;
+  };
+  const size_t n4 = 4 * (size_t)hp.n, m = hp.m;
+  part(L.tets, hp.tets.size(), 4);
+  part(L.rest64, hp.rest64.size(), 8);
+  part(L.rest32, hp.rest32.size(), 4);
+  part(L.tile_nptr, hp.tile_nptr.size(), 4);
+  part(L.tile_nodes, hp.tile_nodes.size(), 4);
+  part(L.tet_loc, hp.tet_loc.size(), 2);
+  part(L.model, hp.model.size(), 1);
+  part(L.chunk_off, hp.chunk_off.size(), 4);
+  part(L.slot_col, hp.slot_col.size(), 4);
+  part(L.diag_slot, hp.diag_slot.size(), 4);
+  part(L.lo_rc, hp.lo_rc.size(), 4);
+  part(L.lo_slot, hp.lo_slot.size(), 4);
+  part(L.up_slot, hp.up_slot.size(), 4);
+  part(L.seg_ptr, hp.seg_ptr.size(), 4);
+  part(L.seg_c, hp.seg_c.size(), 4);
+  part(L.nseg_ptr, hp.nseg_ptr.size(), 4);
+  part(L.nseg_c, hp.nseg_c.size(), 4);
+  part(L.fixmask, hp.fixmask.size(), 1);
+  part(L.mass, hp.mass.size(), 8);
+  part(L.hlin, hp.hlin.size(), 8);
+  if (!hp.soft.empty()) part(L.soft, hp.soft.size(), 8);
+  part(L.x, n4, 8);
+  part(L.xrest, n4, 8);
+  L.upload_end = off;
+  for (auto& v : L.vec) part(v, n4, 8);
+  part(L.counter, 1, 4);
+  part(L.log, 4 * (size_t)kLogCap, 8);
+  part(L.st, 1, sizeof(NState));
+  part(L.opts, 1, sizeof(DevOpts));
+  L.zero_end = off;
   const size_t maxt = std::max({tiles(hp.m), hp.nchunks, tiles(hp.nlo)});
-  b += arena_bytes_of(m, 8) + arena_bytes_of(12 * m, 8) + arena_bytes_of(maxt * kPartials, 8) + arena_bytes_of(1, 4) +
-       arena_bytes_of(4 * (size_t)kLogCap, 8) + arena_bytes_of(1, sizeof(NState)) + arena_bytes_of(1, sizeof(DevOpts));
+  part(L.eloc, m, 8);
+  part(L.gloc, 12 * m, 8);
+  part(L.partials, maxt * kPartials, 8);
+  L.total = off;
+  return L;
+}
+
+// The uploaded part of the base block, [0, upload_end), written into dst.
+void pack_base(const HostPattern& hp, const double* X0, const BaseLayout& L, char* dst) {
+  auto put = [&](const BaseLayout::Part& p, const void* src, size_t bytes) {
+    if (bytes) std::memcpy(dst + p.off, src, bytes);
+  };
+  put(L.tets, hp.tets.data(), hp.tets.size() * 4);
+  put(L.rest64, hp.rest64.data(), hp.rest64.size() * 8);
+  put(L.rest32, hp.rest32.data(), hp.rest32.size() * 4);
+  put(L.tile_nptr, hp.tile_nptr.data(), hp.tile_nptr.size() * 4);
+  put(L.tile_nodes, hp.tile_nodes.data(), hp.tile_nodes.size() * 4);
+  put(L.tet_loc, hp.tet_loc.data(), hp.tet_loc.size() * 2);
+  put(L.model, hp.model.data(), hp.model.size());
+  put(L.chunk_off, hp.chunk_off.data(), hp.chunk_off.size() * 4);
+  put(L.slot_col, hp.slot_col.data(), hp.slot_col.size() * 4);
+  put(L.diag_slot, hp.diag_slot.data(), hp.diag_slot.size() * 4);
+  put(L.lo_rc, hp.lo_rc.data(), hp.lo_rc.size() * 4);
+  put(L.lo_slot, hp.lo_slot.data(), hp.lo_slot.size() * 4);
+  put(L.up_slot, hp.up_slot.data(), hp.up_slot.size() * 4);
+  put(L.seg_ptr, hp.seg_ptr.data(), hp.seg_ptr.size() * 4);
+  put(L.seg_c, hp.seg_c.data(), hp.seg_c.size() * 4);
+  put(L.nseg_ptr, hp.nseg_ptr.data(), hp.nseg_ptr.size() * 4);
+  put(L.nseg_c, hp.nseg_c.data(), hp.nseg_c.size() * 4);
+  put(L.fixmask, hp.fixmask.data(), hp.fixmask.size());
+  put(L.mass, hp.mass.data(), hp.mass.size() * 8);
+  put(L.hlin, hp.hlin.data(), hp.hlin.size() * 8);
+  if (!hp.soft.empty()) put(L.soft, hp.soft.data(), hp.soft.size() * 8);
+  double* x = reinterpret_cast<double*>(dst + L.x.off);
+  for (int v = 0; v < hp.n; ++v) {
+    for (int c = 0; c < 3; ++c) x[4 * (size_t)v + c] = X0[3 * (size_t)v + c];
+    x[4 * (size_t)v + 3] = 0.0;
+  }
+  std::memcpy(dst + L.xrest.off, x, 4 * (size_t)hp.n * sizeof(double));
+}
+
+int64_t device_bytes(const HostPattern& hp, bool fp32, bool fp64) {
+  int64_t b = (int64_t)base_layout(hp).total;
   if (fp32) b += precision_bytes(hp.n, hp.m, hp.nslots, 4);
   if (fp64) b += precision_bytes(hp.n, hp.m, hp.nslots, 8);
   return b;
@@ -1130,7 +1219,12 @@ int instance_free_device(phx_instance inst) {
 // Device part: arena allocations and uploads on the context stream (the caller
 // synchronises).  On failure the instance is destroyed, or with keep_on_fail only its
 // device part is released.
-int instance_setup_device(phx_context ctx, const phx_mesh* mesh, phx_instance_s* inst, bool keep_on_fail = false) {
+// Device part from an already packed upload (base_layout / pack_base): one arena block, one
+// copy from `staged` (the context's pinned staging, or pageable memory) and one memset, on the
+// context stream (the caller synchronises).  On failure the instance is
+// destroyed, or with keep_on_fail only its device part is freed.
+int setup_from_stage(phx_context ctx, phx_instance_s* inst, const BaseLayout& L, const char* staged,
+                     bool keep_on_fail) {
   HostPattern& hp = inst->hp;
   InstDev& D = inst->dev;
   D.n = hp.n; D.m = hp.m; D.nlo = hp.nlo; D.nchunks = hp.nchunks; D.nslots = hp.nslots;
@@ -1140,60 +1234,47 @@ int instance_setup_device(phx_context ctx, const phx_mesh* mesh, phx_instance_s*
     else phx_instance_destroy(inst);
     return rc;
   };
-  cudaError_t e0 = cudaSuccess;
-  int rc = PHX_OK;
-  const size_t n4 = 4 * (size_t)hp.n;
-#define UP(field, vec)                                          \
-  do {                                                          \
-    std::remove_const_t<std::remove_pointer_t<decltype(D.field)>>* p_;  \
-    rc = upload(inst, &p_, vec);                                \
-    if (rc) return fail(rc);                                    \
-    D.field = p_;                                               \
-  } while (0)
-  UP(tets, hp.tets);
-  UP(rest64, hp.rest64);
-  UP(rest32, hp.rest32);
-  UP(tile_nptr, hp.tile_nptr);
-  UP(tile_nodes, hp.tile_nodes);
-  UP(tet_loc, hp.tet_loc);
-  UP(model, hp.model);
-  UP(chunk_off, hp.chunk_off);
-  UP(slot_col, hp.slot_col);
-  UP(diag_slot, hp.diag_slot);
-  UP(lo_rc, hp.lo_rc);
-  UP(lo_slot, hp.lo_slot);
-  UP(up_slot, hp.up_slot);
-  UP(seg_ptr, hp.seg_ptr);
-  UP(seg_c, hp.seg_c);
-  UP(nseg_ptr, hp.nseg_ptr);
-  UP(nseg_c, hp.nseg_c);
-  UP(fixmask, hp.fixmask);
-  UP(mass, hp.mass);
-  UP(hlin, hp.hlin);
-  if (!hp.soft.empty()) UP(soft, hp.soft);
-#undef UP
-  {
-    double* xr = nullptr;
-    if ((rc = arena_alloc(inst, &xr, n4, true))) return fail(rc);
-    D.xrest = xr;
-  }
-  double** vecs[] = {&D.x, &D.xs, &D.dx, &D.g, &D.gn, &D.dxprev, &D.x0, &D.v0, &D.v, &D.r64, &D.bvec, &D.xback};
-  for (double** pv : vecs)
-    if ((rc = arena_alloc(inst, pv, n4, true))) return fail(rc);
-  if ((rc = arena_alloc(inst, &D.Eloc, (size_t)hp.m))) return fail(rc);
-  if ((rc = arena_alloc(inst, &D.Gloc, 12 * (size_t)hp.m))) return fail(rc);
-  size_t maxt = std::max({tiles(hp.m), hp.nchunks, tiles(hp.nlo)});
-  if ((rc = arena_alloc(inst, &D.partials, maxt * kPartials))) return fail(rc);
-  if ((rc = arena_alloc(inst, &D.counter, 1, true))) return fail(rc);
-  if ((rc = arena_alloc(inst, &D.log, 4 * (size_t)kLogCap, true))) return fail(rc);
-  if ((rc = arena_alloc(inst, &inst->d_st, 1, true))) return fail(rc);
-  if ((rc = arena_alloc(inst, &inst->d_opts, 1, true))) return fail(rc);
+  char* base = nullptr;
+  int rc = arena_alloc(inst, &base, L.total);
+  if (rc) return fail(rc);
+  cudaError_t e = cudaMemcpyAsync(base, staged, L.upload_end, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(base + L.upload_end, 0, L.zero_end - L.upload_end, ctx->stream);
+  if (e != cudaSuccess) return fail(set_err(PHX_ECUDA, cudaGetErrorString(e)));
+  auto at = [&](const BaseLayout::Part& p) { return base + p.off; };
+  D.tets = reinterpret_cast<const int32_t*>(at(L.tets));
+  D.rest64 = reinterpret_cast<const double*>(at(L.rest64));
+  D.rest32 = reinterpret_cast<const float*>(at(L.rest32));
+  D.tile_nptr = reinterpret_cast<const int32_t*>(at(L.tile_nptr));
+  D.tile_nodes = reinterpret_cast<const int32_t*>(at(L.tile_nodes));
+  D.tet_loc = reinterpret_cast<const uint16_t*>(at(L.tet_loc));
+  D.model = reinterpret_cast<const uint8_t*>(at(L.model));
+  D.chunk_off = reinterpret_cast<const int32_t*>(at(L.chunk_off));
+  D.slot_col = reinterpret_cast<const int32_t*>(at(L.slot_col));
+  D.diag_slot = reinterpret_cast<const int32_t*>(at(L.diag_slot));
+  D.lo_rc = reinterpret_cast<const int32_t*>(at(L.lo_rc));
+  D.lo_slot = reinterpret_cast<const int32_t*>(at(L.lo_slot));
+  D.up_slot = reinterpret_cast<const int32_t*>(at(L.up_slot));
+  D.seg_ptr = reinterpret_cast<const int32_t*>(at(L.seg_ptr));
+  D.seg_c = reinterpret_cast<const int32_t*>(at(L.seg_c));
+  D.nseg_ptr = reinterpret_cast<const int32_t*>(at(L.nseg_ptr));
+  D.nseg_c = reinterpret_cast<const int32_t*>(at(L.nseg_c));
+  D.fixmask = reinterpret_cast<const uint8_t*>(at(L.fixmask));
+  D.mass = reinterpret_cast<const double*>(at(L.mass));
+  D.hlin = reinterpret_cast<double*>(at(L.hlin));
+  D.soft = hp.soft.empty() ? nullptr : reinterpret_cast<double*>(at(L.soft));
+  D.x = reinterpret_cast<double*>(at(L.x));
+  D.xrest = reinterpret_cast<const double*>(at(L.xrest));
+  double** vecs[11] = {&D.xs, &D.dx, &D.g, &D.gn, &D.dxprev, &D.x0, &D.v0, &D.v, &D.r64, &D.bvec, &D.xback};
+  for (int k = 0; k < 11; ++k) *vecs[k] = reinterpret_cast<double*>(at(L.vec[k]));
+  D.counter = reinterpret_cast<uint32_t*>(at(L.counter));
+  D.log = reinterpret_cast<double*>(at(L.log));
+  inst->d_st = reinterpret_cast<NState*>(at(L.st));
+  inst->d_opts = reinterpret_cast<DevOpts*>(at(L.opts));
   D.st = inst->d_st;
   D.opts = inst->d_opts;
-  // rest positions
-  if ((rc = upload_x(inst, mesh->X0, D.x))) return fail(rc);
-  e0 = cudaMemcpyAsync((void*)D.xrest, D.x, n4 * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream);
-  if (e0 != cudaSuccess) return fail(set_err(PHX_ECUDA, cudaGetErrorString(e0)));
+  D.Eloc = reinterpret_cast<double*>(at(L.eloc));
+  D.Gloc = reinterpret_cast<double*>(at(L.gloc));
+  D.partials = reinterpret_cast<double*>(at(L.partials));
   // keep only what later calls need on the host
   hp.rest64.clear(); hp.rest64.shrink_to_fit();
   hp.rest32.clear(); hp.rest32.shrink_to_fit();
@@ -1203,6 +1284,47 @@ int instance_setup_device(phx_context ctx, const phx_mesh* mesh, phx_instance_s*
   hp.nseg_c.clear(); hp.nseg_c.shrink_to_fit();
   hp.slot_col.clear(); hp.slot_col.shrink_to_fit();
   return PHX_OK;
+}
+
+// Makes the context's pinned staging hold `bytes`, once the last copy from it is done.
+// Returns false if pinned memory cannot be had (the caller then stages in pageable memory).
+bool stage_reserve(phx_context ctx, size_t bytes) {
+  if (ctx->stage_ev && cudaEventSynchronize(ctx->stage_ev) != cudaSuccess) return false;
+  if (bytes <= ctx->stage_cap) return true;
+  if (ctx->stage) cudaFreeHost(ctx->stage);
+  ctx->stage = nullptr;
+  ctx->stage_cap = 0;
+  const size_t cap = (bytes + ((size_t)1 << 20) - 1) & ~(((size_t)1 << 20) - 1);
+  if (cudaMallocHost(&ctx->stage, cap) != cudaSuccess) {
+    cudaGetLastError();
+    ctx->stage = nullptr;
+    return false;
+  }
+  ctx->stage_cap = cap;
+  return true;
+}
+int stage_done(phx_context ctx) {  // after the copies from the staging buffer are queued
+  if (!ctx->stage_ev) CU(cudaEventCreateWithFlags(&ctx->stage_ev, cudaEventDisableTiming));
+  CU(cudaEventRecord(ctx->stage_ev, ctx->stream));
+  return PHX_OK;
+}
+
+// One instance's device part from its host pattern and rest positions (single set-ups: the
+// server's admissions and rebuilds, which must not wait for the kernels running on the stream).
+// The packed upload is pageable: the runtime copies it into its own staging before the call
+// returns, so the buffer may be released at once and nothing waits for the stream.
+int instance_setup_device(phx_context ctx, const phx_mesh* mesh, phx_instance_s* inst, bool keep_on_fail = false) {
+  const BaseLayout L = base_layout(inst->hp);
+  std::vector<char> buf;
+  try {
+    buf.resize(L.upload_end);
+  } catch (const std::bad_alloc&) {
+    if (keep_on_fail) instance_free_device(inst);
+    else phx_instance_destroy(inst);
+    return set_err(PHX_ENOMEM, "out of host memory staging an instance");
+  }
+  pack_base(inst->hp, mesh->X0, L, buf.data());
+  return setup_from_stage(ctx, inst, L, buf.data(), keep_on_fail);
 }
 
 }  // namespace
@@ -1267,14 +1389,40 @@ int phx_instances_create(phx_context ctx, int32_t count, const phx_mesh* meshes,
     for (auto* p : insts) delete p;
     return set_err(PHX_ECUDA, cudaGetErrorString(e));
   }
+  // every instance's upload packed into one pinned staging buffer (on the host threads), then
+  // one arena block, one copy and one memset per instance
+  std::vector<BaseLayout> lay(count);
+  std::vector<size_t> at(count + 1, 0);
   for (int32_t i = 0; i < count; ++i) {
-    const int rc = instance_setup_device(ctx, &meshes[i], insts[i]);  // destroys insts[i] on failure
+    lay[i] = base_layout(insts[i]->hp);
+    at[i + 1] = at[i] + ((lay[i].upload_end + 255) & ~(size_t)255);
+  }
+  const bool staged = stage_reserve(ctx, at[count]);
+  if (staged) {
+    std::atomic<int32_t> nxt{0};
+    auto pack = [&]() {
+      for (int32_t i; (i = nxt.fetch_add(1)) < count;) pack_base(insts[i]->hp, meshes[i].X0, lay[i], ctx->stage + at[i]);
+    };
+    std::vector<std::thread> pool;
+    try {
+      for (int t = 1; t < nt; ++t) pool.emplace_back(pack);
+    } catch (const std::system_error&) {
+    }
+    pack();
+    for (auto& th : pool) th.join();
+  }
+  for (int32_t i = 0; i < count; ++i) {
+    // destroys insts[i] on failure
+    const int rc = staged ? setup_from_stage(ctx, insts[i], lay[i], ctx->stage + at[i], false)
+                          : instance_setup_device(ctx, &meshes[i], insts[i]);
     if (rc != PHX_OK) {
       for (int32_t j = 0; j < i; ++j) phx_instance_destroy(insts[j]);
       for (int32_t j = i + 1; j < count; ++j) delete insts[j];
+      if (staged) stage_done(ctx);
       return rc;
     }
   }
+  if (staged) TRY(stage_done(ctx));
   e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) {
     for (auto* p : insts) phx_instance_destroy(p);
