@@ -176,6 +176,9 @@ struct phx_context_s {
   // scheduling of batch solves (defaults, and tuned settings per batch mix)
   phx_launch_settings launch{1, kWaitRounds, kWaitShare, kRoundsPerLaunch, 0};
   std::map<std::string, phx_launch_settings> tuned;
+  // pinned landing area of batch downloads (states and positions of a batch, one synchronisation)
+  char* down = nullptr;
+  size_t down_cap = 0;
   // pinned staging of instance set-ups (grown as needed, reused once its last copy is done)
   char* stage = nullptr;
   size_t stage_cap = 0;
@@ -508,13 +511,14 @@ int validate_opts(const phx_options* o) {
   return PHX_OK;
 }
 
+// (A copy from pageable memory to the device is staged by the runtime before the call returns,
+// so the local buffer may go at once; nothing waits for the stream.)
 int upload_x(phx_instance inst, const double* x3, double* dst) {
   const int n = inst->dev.n;
   std::vector<double> buf(4 * (size_t)n, 0.0);
   for (int v = 0; v < n; ++v)
     for (int c = 0; c < 3; ++c) buf[4 * (size_t)v + c] = x3[3 * (size_t)v + c];
   CU(cudaMemcpyAsync(dst, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice, inst->ctx->stream));
-  CU(cudaStreamSynchronize(inst->ctx->stream));
   return PHX_OK;
 }
 
@@ -543,6 +547,55 @@ int read_state(phx_instance inst, NState* s) {
   CU(cudaMemcpyAsync(s, inst->d_st, sizeof(NState), cudaMemcpyDeviceToHost, inst->ctx->stream));
   CU(cudaStreamSynchronize(inst->ctx->stream));
   inst->stage = s->stage;  // the boundary conditions keep their stage after a solve
+  return PHX_OK;
+}
+
+// The states of a batch (and, where x is given, its positions) copied to the host with one
+// synchronisation: device-to-host copies into the context's pinned landing area, then unpacked.
+int read_batch(phx_context ctx, const std::vector<phx_instance>& list, std::vector<NState>& st, double* const* x) {
+  const size_t k = list.size();
+  std::vector<size_t> off(k + 1, 0);
+  size_t s_bytes = ((k * sizeof(NState)) + 255) & ~(size_t)255;
+  off[0] = s_bytes;
+  for (size_t i = 0; i < k; ++i)
+    off[i + 1] = off[i] + ((x && x[i]) ? ((4 * (size_t)list[i]->dev.n * sizeof(double) + 255) & ~(size_t)255) : 0);
+  const size_t need = off[k];
+  if (need > ctx->down_cap) {
+    if (ctx->down) cudaFreeHost(ctx->down);
+    ctx->down = nullptr;
+    ctx->down_cap = 0;
+    const size_t cap = (need + ((size_t)1 << 20) - 1) & ~(((size_t)1 << 20) - 1);
+    if (cudaMallocHost(&ctx->down, cap) != cudaSuccess) {
+      cudaGetLastError();
+      ctx->down = nullptr;
+      // pageable fallback: one instance at a time
+      st.resize(k);
+      for (size_t i = 0; i < k; ++i) {
+        TRY(read_state(list[i], &st[i]));
+        if (x && x[i]) TRY(download_x(list[i], list[i]->dev.x, x[i]));
+      }
+      return PHX_OK;
+    }
+    ctx->down_cap = cap;
+  }
+  NState* hs = reinterpret_cast<NState*>(ctx->down);
+  for (size_t i = 0; i < k; ++i) {
+    CU(cudaMemcpyAsync(hs + i, list[i]->d_st, sizeof(NState), cudaMemcpyDeviceToHost, ctx->stream));
+    if (x && x[i])
+      CU(cudaMemcpyAsync(ctx->down + off[i], list[i]->dev.x, 4 * (size_t)list[i]->dev.n * sizeof(double),
+                         cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  CU(cudaStreamSynchronize(ctx->stream));
+  st.resize(k);
+  for (size_t i = 0; i < k; ++i) {
+    st[i] = hs[i];
+    list[i]->stage = st[i].stage;  // the boundary conditions keep their stage after a solve
+    if (x && x[i]) {
+      const double* b = reinterpret_cast<const double*>(ctx->down + off[i]);
+      for (int v = 0; v < list[i]->dev.n; ++v)
+        for (int c = 0; c < 3; ++c) x[i][3 * (size_t)v + c] = b[4 * (size_t)v + c];
+    }
+  }
   return PHX_OK;
 }
 
@@ -1029,6 +1082,7 @@ int phx_context_destroy(phx_context ctx) {
   if (ctx->graph) cudaGraphDestroy(ctx->graph);
   if (ctx->stage) cudaFreeHost(ctx->stage);
   if (ctx->stage_ev) cudaEventDestroy(ctx->stage_ev);
+  if (ctx->down) cudaFreeHost(ctx->down);
   for (auto& ev : ctx->marks)
     if (ev) cudaEventDestroy(ev);
   ctx->arena.release();
@@ -1892,11 +1946,11 @@ int phx_batch_solve(phx_context ctx, int32_t count, phx_instance* insts, const p
   }
   if (count == 0) return PHX_OK;
   TRY(run_to_completion(ctx, list, o->precision == PHX_PREC_FP64, o->pcg_chunk));
-  std::vector<NState> st(count), fin_first, fin_second;
+  std::vector<NState> st, fin_first, fin_second;
   std::vector<phx_instance> fin;
   std::vector<int> fin_at(count, -1);
+  TRY(read_batch(ctx, list, st, nullptr));
   for (int i = 0; i < count; ++i) {
-    TRY(read_state(list[i], &st[i]));
     if (wants_fp64_finish(o, st[i])) {
       fin_at[i] = (int)fin.size();
       fin.push_back(list[i]);
@@ -1904,9 +1958,12 @@ int phx_batch_solve(phx_context ctx, int32_t count, phx_instance* insts, const p
     }
   }
   if (!fin.empty()) TRY(finish_fp64(ctx, fin, o, fin_first, &fin_second));
+  if (x) {  // positions of the whole batch, one synchronisation
+    std::vector<NState> after;
+    TRY(read_batch(ctx, list, after, x));
+  }
   double secs = std::chrono::duration<double>(clk::now() - t0).count();
   for (int i = 0; i < count; ++i) {
-    if (x && x[i]) TRY(download_x(list[i], list[i]->dev.x, x[i]));
     if (!reps) continue;
     if (fin_at[i] >= 0) fill_report_finished(st[i], fin_second[fin_at[i]], secs, &reps[i]);
     else fill_report(st[i], false, secs, &reps[i]);
@@ -2039,11 +2096,10 @@ int phx_batch_dynamic_step(phx_context ctx, int32_t count, phx_instance* insts, 
   if (count == 0) return PHX_OK;
   TRY(run_to_completion(ctx, list, o->precision == PHX_PREC_FP64, o->pcg_chunk));
   double secs = std::chrono::duration<double>(clk::now() - t0).count();
-  for (int i = 0; i < count; ++i) {
-    NState s;
-    TRY(read_state(list[i], &s));
-    if (reps) fill_report(s, false, secs, &reps[i]);
-  }
+  std::vector<NState> st;
+  TRY(read_batch(ctx, list, st, nullptr));
+  for (int i = 0; i < count; ++i)
+    if (reps) fill_report(st[i], false, secs, &reps[i]);
   return PHX_OK;
 }
 
