@@ -167,12 +167,18 @@ bool build_pattern(const MeshIn& in, HostPattern& hp, std::string& err) {
         pairs[q] = 10 * e + p;
       }
   }
+  // The scatter map's inverse (segments: each block's pairs in ascending pair id) comes out of
+  // the same pass: a column's pairs are in ascending pair id, and its blocks are consecutive.
   hp.lo_colptr.assign(n + 1, 0);
   hp.scatter.resize(10 * (size_t)m);
+  hp.seg_c.resize(10 * (size_t)m);
+  hp.seg_ptr.assign(1, 0);
+  hp.seg_ptr.reserve(cnt[n] / 3 + 2);
   std::vector<int32_t> lo_R;
   lo_R.reserve(cnt[n] / 3);
-  std::vector<int32_t> seen(n, -1), block_of(n, 0), uniq;
+  std::vector<int32_t> seen(n, -1), block_of(n, 0), uniq, segpos;
   uniq.reserve(64);
+  segpos.reserve(64);
   for (int C = 0; C < n; ++C) {
     uniq.clear();
     for (int q = cnt[C]; q < cnt[C + 1]; ++q)
@@ -186,7 +192,18 @@ bool build_pattern(const MeshIn& in, HostPattern& hp, std::string& err) {
       lo_R.push_back(uniq[j]);
       block_of[uniq[j]] = base + (int32_t)j;
     }
-    for (int q = cnt[C]; q < cnt[C + 1]; ++q) hp.scatter[pairs[q]] = block_of[rows[q]];
+    segpos.assign(uniq.size() + 1, 0);
+    for (int q = cnt[C]; q < cnt[C + 1]; ++q) {
+      const int32_t k = block_of[rows[q]];
+      hp.scatter[pairs[q]] = k;
+      segpos[k - base + 1]++;
+    }
+    segpos[0] = cnt[C];
+    for (size_t j = 0; j < uniq.size(); ++j) {
+      segpos[j + 1] += segpos[j];
+      hp.seg_ptr.push_back(segpos[j + 1]);
+    }
+    for (int q = cnt[C]; q < cnt[C + 1]; ++q) hp.seg_c[segpos[block_of[rows[q]] - base]++] = pairs[q];
     hp.lo_colptr[C + 1] = (int32_t)lo_R.size();
   }
   hp.nlo = (int32_t)lo_R.size();
@@ -203,15 +220,7 @@ bool build_pattern(const MeshIn& in, HostPattern& hp, std::string& err) {
       return false;
     }
 
-  // ---- the scatter map's inverse (segments) ------------------------------
-  hp.seg_ptr.assign(hp.nlo + 1, 0);
-  for (size_t c = 0; c < hp.scatter.size(); ++c) hp.seg_ptr[hp.scatter[c] + 1]++;
-  for (int k = 0; k < hp.nlo; ++k) hp.seg_ptr[k + 1] += hp.seg_ptr[k];
-  hp.seg_c.resize(hp.scatter.size());
-  {
-    std::vector<int32_t> pos(hp.seg_ptr.begin(), hp.seg_ptr.end() - 1);
-    for (size_t c = 0; c < hp.scatter.size(); ++c) hp.seg_c[pos[hp.scatter[c]]++] = (int32_t)c;
-  }
+  // ---- the node segments (each node's tet corners, in element order) -----
   hp.nseg_ptr.assign(n + 1, 0);
   for (size_t c = 0; c < 4 * (size_t)m; ++c) hp.nseg_ptr[hp.tets[c] + 1]++;
   for (int v = 0; v < n; ++v) hp.nseg_ptr[v + 1] += hp.nseg_ptr[v];
