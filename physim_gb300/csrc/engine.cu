@@ -598,8 +598,6 @@ int read_batch(phx_context ctx, const std::vector<phx_instance>& list, std::vect
   const size_t need = off[k];
   if (need > ctx->down_cap) {
     if (ctx->down) cudaFreeHost(ctx->down);
-  if (ctx->small) cudaFreeHost(ctx->small);
-  if (ctx->small_ev) cudaEventDestroy(ctx->small_ev);
     ctx->down = nullptr;
     ctx->down_cap = 0;
     const size_t cap = (need + ((size_t)1 << 20) - 1) & ~(((size_t)1 << 20) - 1);
@@ -1190,104 +1188,6 @@ bool instance_build_host(const phx_mesh* mesh, phx_instance_s* inst, std::string
 // Device bytes instance_setup_device allocates for a built host part, plus the buffers of
 // the arithmetic(s) asked for (the serving admission's estimate; equal to the instance's
 // bytes after the set-up, which a GPU test checks).
-// An instance's base block in the arena: the arrays uploaded from its host pattern (and its
-// positions, twice: current and rest), then the arrays that start at zero, then per-element
-// scratch, each at a 256-byte aligned offset.  One copy from pinned memory and one memset set
-// it up.
-struct BaseLayout {
-  struct Part {
-    size_t off = 0, bytes = 0;
-  };
-  Part tets, rest64, rest32, tile_nptr, tile_nodes, tet_loc, model, chunk_off, slot_col, diag_slot, lo_rc, lo_slot,
-      up_slot, seg_ptr, seg_c, nseg_ptr, nseg_c, fixmask, mass, hlin, soft, x, xrest;
-  size_t upload_end = 0;
-  Part vec[11], counter, log, st, opts;  // vec: xs, dx, g, gn, dxprev, x0, v0, v, r64, bvec, xback
-  size_t zero_end = 0;
-  Part eloc, gloc, partials;
-  size_t total = 0;
-};
-
-BaseLayout base_layout(const HostPattern& hp) {
-  BaseLayout L;
-  size_t off = 0;
-  auto part = [&](BaseLayout::Part& p, size_t count, size_t elem) {
-    p.off = off;
-    p.bytes = std::max<size_t>(count, 1) * elem;
-    off += (p.bytes + 255) & ~(size_t)255;
-  };
-  const size_t n4 = 4 * (size_t)hp.n, m = hp.m;
-  part(L.tets, hp.tets.size(), 4);
-  part(L.rest64, hp.rest64.size(), 8);
-  part(L.rest32, hp.rest32.size(), 4);
-  part(L.tile_nptr, hp.tile_nptr.size(), 4);
-  part(L.tile_nodes, hp.tile_nodes.size(), 4);
-  part(L.tet_loc, hp.tet_loc.size(), 2);
-  part(L.model, hp.model.size(), 1);
-  part(L.chunk_off, hp.chunk_off.size(), 4);
-  part(L.slot_col, hp.slot_col.size(), 4);
-  part(L.diag_slot, hp.diag_slot.size(), 4);
-  part(L.lo_rc, hp.lo_rc.size(), 4);
-  part(L.lo_slot, hp.lo_slot.size(), 4);
-  part(L.up_slot, hp.up_slot.size(), 4);
-  part(L.seg_ptr, hp.seg_ptr.size(), 4);
-  part(L.seg_c, hp.seg_c.size(), 4);
-  part(L.nseg_ptr, hp.nseg_ptr.size(), 4);
-  part(L.nseg_c, hp.nseg_c.size(), 4);
-  part(L.fixmask, hp.fixmask.size(), 1);
-  part(L.mass, hp.mass.size(), 8);
-  part(L.hlin, hp.hlin.size(), 8);
-  if (!hp.soft.empty()) part(L.soft, hp.soft.size(), 8);
-  part(L.x, n4, 8);
-  part(L.xrest, n4, 8);
-  L.upload_end = off;
-  for (auto& v : L.vec) part(v, n4, 8);
-  part(L.counter, 1, 4);
-  part(L.log, 4 * (size_t)kLogCap, 8);
-  part(L.st, 1, sizeof(NState));
-  part(L.opts, 1, sizeof(DevOpts));
-  L.zero_end = off;
-  const size_t maxt = std::max({tiles(hp.m), hp.nchunks, tiles(hp.nlo)});
-  part(L.eloc, m, 8);
-  part(L.gloc, 12 * m, 8);
-  part(L.partials, maxt * kPartials, 8);
-  L.total = off;
-  return L;
-}
-
-// The uploaded part of the base block, [0, upload_end), written into dst.
-void pack_base(const HostPattern& hp, const double* X0, const BaseLayout& L, char* dst) {
-  auto put = [&](const BaseLayout::Part& p, const void* src, size_t bytes) {
-    if (bytes) std::memcpy(dst + p.off, src, bytes);
-  };
-  put(L.tets, hp.tets.data(), hp.tets.size() * 4);
-  put(L.rest64, hp.rest64.data(), hp.rest64.size() * 8);
-  put(L.rest32, hp.rest32.data(), hp.rest32.size() * 4);
-  put(L.tile_nptr, hp.tile_nptr.data(), hp.tile_nptr.size() * 4);
-  put(L.tile_nodes, hp.tile_nodes.data(), hp.tile_nodes.size() * 4);
-  put(L.tet_loc, hp.tet_loc.data(), hp.tet_loc.size() * 2);
-  put(L.model, hp.model.data(), hp.model.size());
-  put(L.chunk_off, hp.chunk_off.data(), hp.chunk_off.size() * 4);
-  put(L.slot_col, hp.slot_col.data(), hp.slot_col.size() * 4);
-  put(L.diag_slot, hp.diag_slot.data(), hp.diag_slot.size() * 4);
-  put(L.lo_rc, hp.lo_rc.data(), hp.lo_rc.size() * 4);
-  put(L.lo_slot, hp.lo_slot.data(), hp.lo_slot.size() * 4);
-  put(L.up_slot, hp.up_slot.data(), hp.up_slot.size() * 4);
-  put(L.seg_ptr, hp.seg_ptr.data(), hp.seg_ptr.size() * 4);
-  put(L.seg_c, hp.seg_c.data(), hp.seg_c.size() * 4);
-  put(L.nseg_ptr, hp.nseg_ptr.data(), hp.nseg_ptr.size() * 4);
-  put(L.nseg_c, hp.nseg_c.data(), hp.nseg_c.size() * 4);
-  put(L.fixmask, hp.fixmask.data(), hp.fixmask.size());
-  put(L.mass, hp.mass.data(), hp.mass.size() * 8);
-  put(L.hlin, hp.hlin.data(), hp.hlin.size() * 8);
-  if (!hp.soft.empty()) put(L.soft, hp.soft.data(), hp.soft.size() * 8);
-  double* x = reinterpret_cast<double*>(dst + L.x.off);
-  for (int v = 0; v < hp.n; ++v) {
-    for (int c = 0; c < 3; ++c) x[4 * (size_t)v + c] = X0[3 * (size_t)v + c];
-    x[4 * (size_t)v + 3] = 0.0;
-  }
-  std::memcpy(dst + L.xrest.off, x, 4 * (size_t)hp.n * sizeof(double));
-}
-
 int64_t device_bytes(const HostPattern& hp, bool fp32, bool fp64) {
   int64_t b = (int64_t)base_layout(hp).total;
   if (fp32) b += precision_bytes(hp.n, hp.m, hp.nslots, 4);

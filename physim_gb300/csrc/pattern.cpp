@@ -336,4 +336,86 @@ bool build_pattern(const MeshIn& in, HostPattern& hp, std::string& err) {
   return true;
 }
 
+BaseLayout base_layout(const HostPattern& hp) {
+  BaseLayout L;
+  size_t off = 0;
+  auto part = [&](BaseLayout::Part& p, size_t count, size_t elem) {
+    p.off = off;
+    p.bytes = std::max<size_t>(count, 1) * elem;
+    off += (p.bytes + 255) & ~(size_t)255;
+  };
+  const size_t n4 = 4 * (size_t)hp.n, m = hp.m;
+  part(L.tets, hp.tets.size(), 4);
+  part(L.rest64, hp.rest64.size(), 8);
+  part(L.rest32, hp.rest32.size(), 4);
+  part(L.tile_nptr, hp.tile_nptr.size(), 4);
+  part(L.tile_nodes, hp.tile_nodes.size(), 4);
+  part(L.tet_loc, hp.tet_loc.size(), 2);
+  part(L.model, hp.model.size(), 1);
+  part(L.chunk_off, hp.chunk_off.size(), 4);
+  part(L.slot_col, hp.slot_col.size(), 4);
+  part(L.diag_slot, hp.diag_slot.size(), 4);
+  part(L.lo_rc, hp.lo_rc.size(), 4);
+  part(L.lo_slot, hp.lo_slot.size(), 4);
+  part(L.up_slot, hp.up_slot.size(), 4);
+  part(L.seg_ptr, hp.seg_ptr.size(), 4);
+  part(L.seg_c, hp.seg_c.size(), 4);
+  part(L.nseg_ptr, hp.nseg_ptr.size(), 4);
+  part(L.nseg_c, hp.nseg_c.size(), 4);
+  part(L.fixmask, hp.fixmask.size(), 1);
+  part(L.mass, hp.mass.size(), 8);
+  part(L.hlin, hp.hlin.size(), 8);
+  if (!hp.soft.empty()) part(L.soft, hp.soft.size(), 8);
+  part(L.x, n4, 8);
+  part(L.xrest, n4, 8);
+  L.upload_end = off;
+  for (auto& v : L.vec) part(v, n4, 8);
+  part(L.counter, 1, 4);
+  part(L.log, 4 * (size_t)kLogCap, 8);
+  part(L.st, 1, sizeof(NState));
+  part(L.opts, 1, sizeof(DevOpts));
+  L.zero_end = off;
+  auto tiles = [](int count) { return (size_t)((count + kTile - 1) / kTile); };
+  const size_t maxt = std::max({tiles(hp.m), (size_t)hp.nchunks, tiles(hp.nlo)});
+  part(L.eloc, m, 8);
+  part(L.gloc, 12 * m, 8);
+  part(L.partials, maxt * kPartials, 8);
+  L.total = off;
+  return L;
+}
+
+// The uploaded part of the base block, [0, upload_end), written into dst.
+void pack_base(const HostPattern& hp, const double* X0, const BaseLayout& L, char* dst) {
+  auto put = [&](const BaseLayout::Part& p, const void* src, size_t bytes) {
+    if (bytes) std::memcpy(dst + p.off, src, bytes);
+  };
+  put(L.tets, hp.tets.data(), hp.tets.size() * 4);
+  put(L.rest64, hp.rest64.data(), hp.rest64.size() * 8);
+  put(L.rest32, hp.rest32.data(), hp.rest32.size() * 4);
+  put(L.tile_nptr, hp.tile_nptr.data(), hp.tile_nptr.size() * 4);
+  put(L.tile_nodes, hp.tile_nodes.data(), hp.tile_nodes.size() * 4);
+  put(L.tet_loc, hp.tet_loc.data(), hp.tet_loc.size() * 2);
+  put(L.model, hp.model.data(), hp.model.size());
+  put(L.chunk_off, hp.chunk_off.data(), hp.chunk_off.size() * 4);
+  put(L.slot_col, hp.slot_col.data(), hp.slot_col.size() * 4);
+  put(L.diag_slot, hp.diag_slot.data(), hp.diag_slot.size() * 4);
+  put(L.lo_rc, hp.lo_rc.data(), hp.lo_rc.size() * 4);
+  put(L.lo_slot, hp.lo_slot.data(), hp.lo_slot.size() * 4);
+  put(L.up_slot, hp.up_slot.data(), hp.up_slot.size() * 4);
+  put(L.seg_ptr, hp.seg_ptr.data(), hp.seg_ptr.size() * 4);
+  put(L.seg_c, hp.seg_c.data(), hp.seg_c.size() * 4);
+  put(L.nseg_ptr, hp.nseg_ptr.data(), hp.nseg_ptr.size() * 4);
+  put(L.nseg_c, hp.nseg_c.data(), hp.nseg_c.size() * 4);
+  put(L.fixmask, hp.fixmask.data(), hp.fixmask.size());
+  put(L.mass, hp.mass.data(), hp.mass.size() * 8);
+  put(L.hlin, hp.hlin.data(), hp.hlin.size() * 8);
+  if (!hp.soft.empty()) put(L.soft, hp.soft.data(), hp.soft.size() * 8);
+  double* x = reinterpret_cast<double*>(dst + L.x.off);
+  for (int v = 0; v < hp.n; ++v) {
+    for (int c = 0; c < 3; ++c) x[4 * (size_t)v + c] = X0[3 * (size_t)v + c];
+    x[4 * (size_t)v + 3] = 0.0;
+  }
+  std::memcpy(dst + L.xrest.off, x, 4 * (size_t)hp.n * sizeof(double));
+}
+
 }  // namespace phx

@@ -63,4 +63,25 @@ void rebuild_load(const MeshIn& in, HostPattern& hp);
 extern const int kPairI[10];
 extern const int kPairJ[10];
 
+// An instance's base block in the arena: the arrays uploaded from its host pattern (and its
+// positions, twice: current and rest), then the arrays that start at zero, then per-element
+// scratch, each at a 256-byte aligned offset.  One copy from pinned memory and one memset set
+// it up.
+struct BaseLayout {
+  struct Part {
+    size_t off = 0, bytes = 0;
+  };
+  Part tets, rest64, rest32, tile_nptr, tile_nodes, tet_loc, model, chunk_off, slot_col, diag_slot, lo_rc, lo_slot,
+      up_slot, seg_ptr, seg_c, nseg_ptr, nseg_c, fixmask, mass, hlin, soft, x, xrest;
+  size_t upload_end = 0;
+  Part vec[11], counter, log, st, opts;  // vec: xs, dx, g, gn, dxprev, x0, v0, v, r64, bvec, xback
+  size_t zero_end = 0;
+  Part eloc, gloc, partials;
+  size_t total = 0;
+};
+
+BaseLayout base_layout(const HostPattern& hp);
+// The uploaded part of the base block, [0, upload_end), written into dst (X0: rest positions [3n]).
+void pack_base(const HostPattern& hp, const double* X0, const BaseLayout& L, char* dst);
+
 }  // namespace phx

@@ -64,4 +64,29 @@ GET(mass, double)
 GET(hlin, double)
 GET(fixmask, unsigned char)
 GET(soft, double)
+
+// The device base block of the last pattern: every part's (offset, bytes) in declaration order
+// (23 uploaded parts, 11 zeroed vectors, counter, log, state, options, 3 scratch parts: 41), then
+// upload_end, zero_end, total.  Returns the number of values written (85).
+int pat_layout(long long* out) {
+  const phx::BaseLayout L = phx::base_layout(g_hp);
+  const phx::BaseLayout::Part* parts[] = {
+      &L.tets, &L.rest64, &L.rest32, &L.tile_nptr, &L.tile_nodes, &L.tet_loc, &L.model, &L.chunk_off,
+      &L.slot_col, &L.diag_slot, &L.lo_rc, &L.lo_slot, &L.up_slot, &L.seg_ptr, &L.seg_c, &L.nseg_ptr,
+      &L.nseg_c, &L.fixmask, &L.mass, &L.hlin, &L.soft, &L.x, &L.xrest,
+      &L.vec[0], &L.vec[1], &L.vec[2], &L.vec[3], &L.vec[4], &L.vec[5], &L.vec[6], &L.vec[7], &L.vec[8],
+      &L.vec[9], &L.vec[10], &L.counter, &L.log, &L.st, &L.opts, &L.eloc, &L.gloc, &L.partials};
+  int k = 0;
+  for (auto* p : parts) {
+    out[k++] = (long long)p->off;
+    out[k++] = (long long)p->bytes;
+  }
+  out[k++] = (long long)L.upload_end;
+  out[k++] = (long long)L.zero_end;
+  out[k++] = (long long)L.total;
+  return k;
+}
+
+// The packed upload of the last pattern (upload_end bytes) with rest positions X0.
+void pat_pack(const double* X0, char* dst) { phx::pack_base(g_hp, X0, phx::base_layout(g_hp), dst); }
 }

@@ -283,3 +283,49 @@ def test_pattern_bit_exact_on_renumbered_meshes(pattern_shim, seed):
     assert np.array_equal(cp, mcp) and np.array_equal(ri, mri)
     assert np.array_equal(P["scatter"], o.scatter_map())
     assert P["nlo"] == m.n + len(M.unique_edges(m.T))
+
+
+@pytest.mark.parametrize("make", MESHES)
+def test_base_block_layout_and_packing(pattern_shim, make):
+    """An instance's device base block (one arena block, one copy, one memset): parts at
+    256-byte offsets, in order, without overlap; the uploaded parts before the zeroed ones;
+    the total is the sum of the parts rounded to 256 bytes (the serving admission's estimate);
+    the packed upload holds the pattern arrays and the positions (4-wide, twice)."""
+    m = make()
+    P, err = build(pattern_shim, m)
+    assert err is None
+    out = np.zeros(90, dtype=np.int64)
+    k = pattern_shim.pat_layout(out.ctypes.data_as(C.c_void_p))
+    assert k == 85
+    parts = out[:82].reshape(-1, 2)
+    upload_end, zero_end, total = (int(v) for v in out[82:85])
+    has_soft = parts[20, 1] > 0
+    end = 0
+    for i, (off, nb) in enumerate(parts):
+        if i == 20 and not has_soft:  # no soft records: the part takes no room
+            continue
+        assert off % 256 == 0 and off == end and nb > 0
+        end = off + ((nb + 255) // 256) * 256
+        if i == 22:
+            assert end == upload_end
+        if i == 37:
+            assert end == zero_end
+    assert end == total
+    n, mm = P["n"], P["m"]
+    assert parts[0, 1] == 16 * mm and parts[21, 1] == 32 * n and parts[22, 1] == 32 * n
+    buf = np.zeros(upload_end, dtype=np.uint8)
+    X0 = np.ascontiguousarray(m.X0, dtype=np.float64).ravel()
+    pattern_shim.pat_pack(X0.ctypes.data_as(C.c_void_p), buf.ctypes.data_as(C.c_void_p))
+
+    def view(i, dtype, count):
+        off = int(parts[i, 0])
+        return np.frombuffer(buf[off:off + count * np.dtype(dtype).itemsize].tobytes(), dtype=dtype)
+
+    assert np.array_equal(view(0, np.int32, 4 * mm), np.ascontiguousarray(m.T, dtype=np.int32).ravel())
+    assert np.array_equal(view(1, np.float64, 12 * mm), P["rest64"].ravel())
+    assert np.array_equal(view(14, np.int32, 10 * mm), P["seg_c"])
+    assert np.array_equal(view(19, np.float64, 4 * n), P["hlin"].ravel())
+    x4 = np.zeros((n, 4))
+    x4[:, :3] = m.X0
+    assert np.array_equal(view(21, np.float64, 4 * n), x4.ravel())
+    assert np.array_equal(view(22, np.float64, 4 * n), x4.ravel())
