@@ -176,11 +176,6 @@ struct phx_context_s {
   // scheduling of batch solves (defaults, and tuned settings per batch mix)
   phx_launch_settings launch{1, kWaitRounds, kWaitShare, kRoundsPerLaunch, 0};
   std::map<std::string, phx_launch_settings> tuned;
-  // pinned source of the small per-instance uploads (options, state) of solve starts: a ring
-  // reused once the copies queued from its previous pass are done
-  char* small = nullptr;
-  size_t small_cap = 0, small_used = 0;
-  cudaEvent_t small_ev = nullptr;
   // pinned landing area of batch downloads (states and positions of a batch, one synchronisation)
   char* down = nullptr;
   size_t down_cap = 0;
@@ -537,37 +532,6 @@ int download_x(phx_instance inst, const double* src, double* x3) {
   return PHX_OK;
 }
 
-// A small host-to-device copy through the pinned ring (truly asynchronous, a few us per call
-// instead of a pageable copy's staging); pageable when the ring is full or unavailable.
-int small_upload(phx_context ctx, void* dst, const void* src, size_t bytes) {
-  constexpr size_t kSmallRing = (size_t)1 << 20;
-  const size_t need = (bytes + 15) & ~(size_t)15;
-  if (!ctx->small && !ctx->small_ev) {
-    if (cudaMallocHost(&ctx->small, kSmallRing) == cudaSuccess) {
-      ctx->small_cap = kSmallRing;
-      CU(cudaEventCreateWithFlags(&ctx->small_ev, cudaEventDisableTiming));
-    } else {
-      cudaGetLastError();
-      ctx->small = nullptr;
-    }
-  }
-  if (ctx->small && ctx->small_used + need > ctx->small_cap) {
-    // wrap: the copies queued from the ring so far must be done before it is written again
-    CU(cudaEventRecord(ctx->small_ev, ctx->stream));
-    CU(cudaEventSynchronize(ctx->small_ev));
-    ctx->small_used = 0;
-  }
-  if (!ctx->small || need > ctx->small_cap) {
-    CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
-    return PHX_OK;
-  }
-  char* p = ctx->small + ctx->small_used;
-  std::memcpy(p, src, bytes);
-  ctx->small_used += need;
-  CU(cudaMemcpyAsync(dst, p, bytes, cudaMemcpyHostToDevice, ctx->stream));
-  return PHX_OK;
-}
-
 int reset_state(phx_instance inst, int phase, int nofix, double shift) {
   NState s{};
   s.phase = phase;
@@ -575,7 +539,7 @@ int reset_state(phx_instance inst, int phase, int nofix, double shift) {
   s.shift = shift;
   s.opt0 = -1.0;
   s.stage = inst->stage;
-  TRY(small_upload(inst->ctx, inst->d_st, &s, sizeof(NState)));
+  CU(cudaMemcpyAsync(inst->d_st, &s, sizeof(NState), cudaMemcpyHostToDevice, inst->ctx->stream));
   return PHX_OK;
 }
 
@@ -980,7 +944,7 @@ int start_solve(phx_instance inst, const phx_options* o, bool dynamic, double dt
                           : inst->dev.n <= kClusterMaxNodes                 ? o->pcg_cluster
                                                                               : 3;
   inst->grid_eligible = inst->dev.pcg_cluster == 3;
-  TRY(small_upload(inst->ctx, inst->d_opts, &d, sizeof(DevOpts)));
+  CU(cudaMemcpyAsync(inst->d_opts, &d, sizeof(DevOpts), cudaMemcpyHostToDevice, inst->ctx->stream));
   TRY(reset_state(inst, PH_START, 0, 0.0));
   return PHX_OK;
 }
@@ -1119,8 +1083,6 @@ int phx_context_destroy(phx_context ctx) {
   if (ctx->stage) cudaFreeHost(ctx->stage);
   if (ctx->stage_ev) cudaEventDestroy(ctx->stage_ev);
   if (ctx->down) cudaFreeHost(ctx->down);
-  if (ctx->small) cudaFreeHost(ctx->small);
-  if (ctx->small_ev) cudaEventDestroy(ctx->small_ev);
   for (auto& ev : ctx->marks)
     if (ev) cudaEventDestroy(ev);
   ctx->arena.release();
