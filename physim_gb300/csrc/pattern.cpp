@@ -149,23 +149,30 @@ bool build_pattern(const MeshIn& in, HostPattern& hp, std::string& err) {
   // The tet pairs grouped by column C = min(node_i, node_j) (a counting sort); then per
   // column its distinct rows R in ascending order (a stamp per row and a sort of the few
   // distinct ones) and each pair's block index.
+  // (each tet's four node ids are loaded once and its ten pairs unrolled)
   std::vector<int32_t> cnt(n + 1, 0);
-  for (int e = 0; e < m; ++e)
-    for (int p = 0; p < 10; ++p) {
-      int ni = hp.tets[4 * (size_t)e + kPairI[p]], nj = hp.tets[4 * (size_t)e + kPairJ[p]];
-      cnt[std::min(ni, nj) + 1]++;
-    }
+  const int32_t* tt = hp.tets.data();
+  for (int e = 0; e < m; ++e) {
+    int32_t t[4];
+    for (int a = 0; a < 4; ++a) t[a] = tt[4 * (size_t)e + a];
+#pragma GCC unroll 10
+    for (int p = 0; p < 10; ++p) cnt[std::min(t[kPairI[p]], t[kPairJ[p]]) + 1]++;
+  }
   for (int v = 0; v < n; ++v) cnt[v + 1] += cnt[v];
   std::vector<int32_t> rows(cnt[n]), pairs(cnt[n]);  // row R and pair id 10 e + p, by column
   {
     std::vector<int32_t> pos(cnt.begin(), cnt.end() - 1);
-    for (int e = 0; e < m; ++e)
+    for (int e = 0; e < m; ++e) {
+      int32_t t[4];
+      for (int a = 0; a < 4; ++a) t[a] = tt[4 * (size_t)e + a];
+#pragma GCC unroll 10
       for (int p = 0; p < 10; ++p) {
-        int ni = hp.tets[4 * (size_t)e + kPairI[p]], nj = hp.tets[4 * (size_t)e + kPairJ[p]];
+        const int32_t ni = t[kPairI[p]], nj = t[kPairJ[p]];
         const int q = pos[std::min(ni, nj)]++;
         rows[q] = std::max(ni, nj);
         pairs[q] = 10 * e + p;
       }
+    }
   }
   // The scatter map's inverse (segments: each block's pairs in ascending pair id) comes out of
   // the same pass: a column's pairs are in ascending pair id, and its blocks are consecutive.
@@ -186,7 +193,13 @@ bool build_pattern(const MeshIn& in, HostPattern& hp, std::string& err) {
         seen[rows[q]] = C;
         uniq.push_back(rows[q]);
       }
-    std::sort(uniq.begin(), uniq.end());
+    // a column has a few distinct rows (about 8-15): insertion sort
+    for (size_t a = 1; a < uniq.size(); ++a) {
+      const int32_t key = uniq[a];
+      size_t b = a;
+      for (; b > 0 && uniq[b - 1] > key; --b) uniq[b] = uniq[b - 1];
+      uniq[b] = key;
+    }
     const int32_t base = (int32_t)lo_R.size();
     for (size_t j = 0; j < uniq.size(); ++j) {
       lo_R.push_back(uniq[j]);
