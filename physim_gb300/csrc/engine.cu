@@ -1928,48 +1928,59 @@ int phx_tune_batch(phx_context ctx, int32_t count, phx_instance* insts, const ph
     return PHX_OK;
   };
   phx_launch_settings best = ctx->launch;
-  double t_def = 0.0, t;
-  TRY(trial(best, &t_def));  // the first run pays one-time costs (graph, caches)
-  TRY(trial(best, &t_def));
-  double t_best = t_def;
-  // one setting at a time around the best so far
-  auto consider = [&](phx_launch_settings c) -> int {
-    TRY(trial(c, &t));
-    if (t < 0.99 * t_best) {
-      best = c;
-      t_best = t;
+  double t_def = 0.0, t = 0.0, t_best = 0.0;
+  // the search; a trial that fails ends it, and the instances are put back all the same
+  auto search = [&]() -> int {
+    TRY(trial(best, &t_def));  // the first run pays one-time costs (graph, caches)
+    TRY(trial(best, &t_def));
+    t_best = t_def;
+    // one setting at a time around the best so far
+    auto consider = [&](phx_launch_settings c) -> int {
+      TRY(trial(c, &t));
+      if (t < 0.99 * t_best) {
+        best = c;
+        t_best = t;
+      }
+      return PHX_OK;
+    };
+    {
+      phx_launch_settings c = best;
+      c.graph = 1 - c.graph;
+      TRY(consider(c));
+    }
+    bool eligible = false;  // FP32 instances above the cluster size: try the other place for their PCG
+    for (auto* in : list) eligible = eligible || in->grid_eligible;
+    if (eligible) {
+      phx_launch_settings c = best;
+      c.pcg_grid = 1 - c.pcg_grid;
+      TRY(consider(c));
+    }
+    for (int v : {2, 8, 16}) {
+      phx_launch_settings c = best;
+      if (v == c.wait_rounds) continue;
+      c.wait_rounds = v;
+      TRY(consider(c));
+    }
+    for (int v : {1, 4, 8}) {
+      phx_launch_settings c = best;
+      if (v == c.wait_share) continue;
+      c.wait_share = v;
+      TRY(consider(c));
+    }
+    for (int v : {8, 32, 64}) {
+      phx_launch_settings c = best;
+      if (v == c.rounds) continue;
+      c.rounds = v;
+      TRY(consider(c));
     }
     return PHX_OK;
   };
-  {
-    phx_launch_settings c = best;
-    c.graph = 1 - c.graph;
-    TRY(consider(c));
-  }
-  bool eligible = false;  // FP32 instances above the cluster size: try the other place for their PCG
-  for (auto* in : list) eligible = eligible || in->grid_eligible;
-  if (eligible) {
-    phx_launch_settings c = best;
-    c.pcg_grid = 1 - c.pcg_grid;
-    TRY(consider(c));
-  }
-  for (int v : {2, 8, 16}) {
-    phx_launch_settings c = best;
-    if (v == c.wait_rounds) continue;
-    c.wait_rounds = v;
-    TRY(consider(c));
-  }
-  for (int v : {1, 4, 8}) {
-    phx_launch_settings c = best;
-    if (v == c.wait_share) continue;
-    c.wait_share = v;
-    TRY(consider(c));
-  }
-  for (int v : {8, 32, 64}) {
-    phx_launch_settings c = best;
-    if (v == c.rounds) continue;
-    c.rounds = v;
-    TRY(consider(c));
+  const int rc = search();
+  if (rc != PHX_OK) {
+    const std::string why = phx_last_error();
+    restore();
+    cudaStreamSynchronize(ctx->stream);
+    return set_err(rc, why);
   }
   TRY(restore());
   CU(cudaStreamSynchronize(ctx->stream));

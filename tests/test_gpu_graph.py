@@ -117,3 +117,28 @@ def test_whole_gpu_pcg_kernels_give_the_engine_bits(gpu_ctx, defaults):
     nbytes = gpu_ctx.profile_bytes("spmv")
     gpu_ctx.profile(False)
     assert n > 0 and ms > 0 and nbytes > 0
+
+
+def test_tuner_puts_instances_back_when_a_trial_fails(gpu_ctx, defaults):
+    """A trial that gives up (the engine's round barrier made to wait for an arrival that never
+    comes, a short limit) ends the tuning with PHX_ETIMEOUT, the instances back where they
+    were, and nothing cached for the mix."""
+    meshes = [M.batch_instance(3, i) for i in range(64, 67)]
+    o = px.options(precision=px.PREC_FP32_REFINE, tol_rel=1e-6, tol_max_error=0.0, tol_min_impr=0.0,
+                   tol_min_step=0.0)
+    insts = [px.Instance(gpu_ctx, m) for m in meshes]
+    start = [m.X0.ravel() + 1e-4 * np.cos(np.arange(3 * m.n)) for m in meshes]
+    for i, x in zip(insts, start):
+        i.set_positions(x)
+    gpu_ctx.debug_unmet_barrier(1, 20_000_000)
+    try:
+        with pytest.raises(px.PhxError) as ei:
+            gpu_ctx.tune_batch(insts, o)
+    finally:
+        gpu_ctx.debug_unmet_barrier(0)
+    assert ei.value.code == px.PHX_ETIMEOUT
+    for i, x in zip(insts, start):
+        assert np.array_equal(i.positions(), x)
+    # the context still solves the batch (no tuned settings were kept for it)
+    reps, _ = gpu_ctx.batch_solve(insts, o, [x.copy() for x in start])
+    assert all(r["status"] == px.PHX_OK for r in reps)
