@@ -281,6 +281,53 @@ int phx_scene_staging(phx_scene sc, phx_stage_group* groups, int32_t cap);
 /* Creates the scene's instance: the mesh, its start positions and its staging. */
 int phx_scene_instance(phx_context ctx, phx_scene sc, phx_instance* out);
 
+/* ---- field output: SVL scalar grids ---------------------------------------
+ * Serializer_Field::ReadGrid_SVL / WriteGrid_SVL (source/PhySim/Utils/Serializer_Field.cpp:
+ * 50-112, 114-140) on ScalarField_Grid (include/PhySim/Geometry/Volumes/ScalarField_Grid.h):
+ * a header of shape (3 int32), origin (3 double), delta (3 double) and the value type (int32,
+ * PHX_SVL_*), then shape[0]*shape[1]*shape[2] values in native byte order, x fastest (the
+ * column-major order of the grid's Eigen tensor: value (i, j, k) at i + s0*(j + s1*k)).
+ * Value (i, j, k) belongs to the cell centre origin + (i + 1/2, j + 1/2, k + 1/2) * delta
+ * (ScalarField_Grid::Sample's coordinates). */
+#define PHX_SVL_INT8 0    /* "char": read and written as signed 8-bit */
+#define PHX_SVL_INT16 1
+#define PHX_SVL_INT32 2
+#define PHX_SVL_FLOAT 3
+#define PHX_SVL_DOUBLE 4
+typedef struct phx_grid {
+  int32_t shape[3];  /* >= 1 each (ScalarField_Grid::Setup) */
+  double origin[3];
+  double delta[3];
+} phx_grid;
+/* Writes a grid file; values holds prod(shape) values of the given format. */
+int phx_svl_write(const char* path, const phx_grid* grid, int32_t format, const void* values);
+/* Reads a grid file's header (grid may be NULL) and value type (format may be NULL). */
+int phx_svl_read_header(const char* path, phx_grid* grid, int32_t* format);
+/* Reads a grid file's values as `as_format` into values (room for `capacity` values).  A file
+ * of another value type is converted value by value, as the reference's
+ * readBinaryArrayWithCast does; a value the target type cannot hold (out of range, or NaN to
+ * an integer type) is refused with PHX_EINVAL instead of converted.  A short file, a shape
+ * below 1 or an unknown value type is PHX_EINVAL. */
+int phx_svl_read(const char* path, int32_t as_format, void* values, int64_t capacity);
+
+/* Fields of a solve sampled on a grid (phx_instance_sample_grid). */
+#define PHX_FIELD_DISPLACEMENT_X 0     /* u = x - X0, interpolated linearly in the owning tet */
+#define PHX_FIELD_DISPLACEMENT_Y 1
+#define PHX_FIELD_DISPLACEMENT_Z 2
+#define PHX_FIELD_DISPLACEMENT_NORM 3  /* |u| of the interpolated u */
+#define PHX_FIELD_VOLUME_RATIO 4       /* J = det F of the owning tet */
+#define PHX_FIELD_ENERGY_DENSITY 5     /* the owning tet's elastic energy / rest volume */
+/* Samples a field of the instance on the cell centres of a grid laid over the REST shape,
+ * on the device.  A centre belongs to the tet of lowest index that contains it: the four
+ * sub-volumes it cuts the tet into are each >= -1e-12 of the tet's (six times) volume; a
+ * centre that no tet contains gets `fill` and owner -1 (ScalarField_Grid::Sample returns -1
+ * outside its box).  x[3n] are the positions to sample (NULL: the instance's current ones;
+ * like phx_energy_gradient, a given x becomes the instance's positions).  values
+ * [prod(shape)] as in an SVL file; owner (may be NULL) the owning tet of each value.  At
+ * most 2^31 - 1 values. */
+int phx_instance_sample_grid(phx_instance inst, const double* x, int32_t field, const phx_grid* grid,
+                             double fill, double* values, int32_t* owner);
+
 /* ---- model evaluation (ISimulable::GetEnergy / GetGradient / GetHessian) --- */
 /* Energy and gradient at x[3n] (x == NULL: current positions).  fix != 0 applies
  * FixVectorDoFs (Simulable.cpp:735-744). */

@@ -109,6 +109,8 @@ def lib():
         L.orc_set_staging.argtypes = [vp, C.c_int32, vp, C.c_int32, vp]
         L.orc_stage.argtypes = [vp]
         L.orc_set_soft.argtypes = [vp, vp, vp]
+        L.orc_sample_grid.argtypes = [C.c_int32, C.c_int32, vp, vp, vp, vp, C.c_int32, vp, vp, vp,
+                                      C.c_double, vp, vp]
         _lib = L
     return _lib
 
@@ -269,3 +271,23 @@ class Oracle:
         obj = np.zeros(n); opt = np.zeros(n); bis = np.zeros(n, dtype=np.int32); step = np.zeros(n)
         lib().orc_last_log(self.h, _p(obj), _p(opt), _p(bis), _p(step), n)
         return {"obj": obj, "opt": opt, "bis": bis, "step": step}
+
+
+def sample_grid(X0, T, x, field, shape, origin, delta, fill=0.0, E=None):
+    """Restatement of the device grid sampler (field_oracle.cpp): values and owning tets of a
+    grid of `shape` cells, x fastest, as flat arrays."""
+    X0 = np.ascontiguousarray(X0, dtype=np.float64).ravel()
+    T = np.ascontiguousarray(T, dtype=np.int32).ravel()
+    x = np.ascontiguousarray(x, dtype=np.float64).ravel()
+    E = None if E is None else np.ascontiguousarray(E, dtype=np.float64)
+    sh = np.asarray(shape, dtype=np.int32)
+    org = np.asarray(origin, dtype=np.float64)
+    dl = np.asarray(delta, dtype=np.float64)
+    count = int(np.prod(sh.astype(np.int64)))
+    vals = np.empty(count, dtype=np.float64)
+    own = np.empty(count, dtype=np.int32)
+    rc = lib().orc_sample_grid(len(X0) // 3, len(T) // 4, _p(X0), _p(T), _p(x), _p(E), int(field), _p(sh),
+                               _p(org), _p(dl), float(fill), _p(vals), _p(own))
+    if rc != 0:
+        raise ValueError("orc_sample_grid: bad field or missing energies")
+    return vals, own

@@ -1,6 +1,7 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
-* ``liboracle.so``  -- the C++ restatement in phx_oracle.cpp (always built).
+* ``liboracle.so``  -- the C++ restatement in phx_oracle.cpp and the grid sampler's in
+  field_oracle.cpp (always built).
 * ``_ref/libref_mcg.so`` -- the reference's own generated material code, compiled
   from the reference tree when it is present (it is not on the GPU host).  The
   tree is the directory named by the environment variable PHYSIM_REFERENCE, or
@@ -30,11 +31,17 @@ def _stale(out, srcs):
 
 
 def build_oracle(force: bool = False) -> str:
-    srcs = [os.path.join(HERE, "phx_oracle.cpp"), os.path.join(HERE, "phx_oracle.h")]
+    """liboracle.so from phx_oracle.cpp and field_oracle.cpp.  The grid sampler's file is
+    compiled with -ffp-contract=off: each product and sum rounds on its own, as the device
+    sampler's explicitly rounded operations do, so the two agree bit for bit on any host."""
+    srcs = [os.path.join(HERE, f) for f in ("phx_oracle.cpp", "field_oracle.cpp", "phx_oracle.h")]
     if force or _stale(LIB, srcs):
-        cmd = ["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared",
-               "-o", LIB, srcs[0]]
-        subprocess.check_call(cmd)
+        obj = os.path.join(HERE, "_field_oracle.o")
+        subprocess.check_call(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-c",
+                               "-o", obj, srcs[1]])
+        subprocess.check_call(["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared",
+                               "-o", LIB, srcs[0], obj])
+        os.remove(obj)
     return LIB
 
 

@@ -37,7 +37,8 @@ EXPORTS = [
     "phx_profile_reset", "phx_profile_bytes", "phx_kernel_launches", "phx_timer_mark", "phx_timer_elapsed",
     "phx_hessian_blocks_noalloc", "phx_debug_unmet_barrier", "phx_context_launch_settings", "phx_tune_batch",
     "phx_scene_load", "phx_scene_destroy", "phx_scene_info", "phx_scene_mesh", "phx_scene_options",
-    "phx_scene_staging", "phx_scene_instance",
+    "phx_scene_staging", "phx_scene_instance", "phx_svl_write", "phx_svl_read_header", "phx_svl_read",
+    "phx_instance_sample_grid",
 ]
 
 
@@ -83,6 +84,17 @@ class StageGroup_(C.Structure):
     _fields_ = [("num_stages", C.c_int32), ("soft", C.c_int32), ("k_start", C.c_double), ("k_end", C.c_double),
                 ("move", C.c_double * 9), ("shift", C.c_double * 3), ("num_nodes", C.c_int32),
                 ("nodes", C.c_void_p)]
+
+
+class Grid_(C.Structure):
+    """phx_grid: a ScalarField_Grid's shape, origin and cell size."""
+    _fields_ = [("shape", C.c_int32 * 3), ("origin", C.c_double * 3), ("delta", C.c_double * 3)]
+
+
+# SVL value types (Serializer_Field.cpp's "char", "short", "int", "float", "double") and numpy's
+SVL_DTYPES = {0: np.int8, 1: np.int16, 2: np.int32, 3: np.float32, 4: np.float64}
+FIELD_DISPLACEMENT_X, FIELD_DISPLACEMENT_Y, FIELD_DISPLACEMENT_Z = 0, 1, 2
+FIELD_DISPLACEMENT_NORM, FIELD_VOLUME_RATIO, FIELD_ENERGY_DENSITY = 3, 4, 5
 
 
 class Report(C.Structure):
@@ -167,6 +179,10 @@ def lib():
         "phx_scene_options": ([vp, C.POINTER(Options)], C.c_int),
         "phx_scene_staging": ([vp, vp, i32], C.c_int),
         "phx_scene_instance": ([vp, vp, C.POINTER(vp)], C.c_int),
+        "phx_svl_write": ([C.c_char_p, C.POINTER(Grid_), i32, vp], C.c_int),
+        "phx_svl_read_header": ([C.c_char_p, C.POINTER(Grid_), C.POINTER(i32)], C.c_int),
+        "phx_svl_read": ([C.c_char_p, i32, vp, i64], C.c_int),
+        "phx_instance_sample_grid": ([vp, vp, i32, C.POINTER(Grid_), dbl, vp, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -193,6 +209,49 @@ def options(**kw) -> Options:
             raise AttributeError(f"unknown option {k}")
         setattr(o, k, v)
     return o
+
+
+def _grid(shape, origin, delta) -> Grid_:
+    g = Grid_()
+    for d in range(3):
+        g.shape[d] = int(shape[d])
+        g.origin[d] = float(origin[d])
+        g.delta[d] = float(delta[d])
+    return g
+
+
+def write_svl(path: str, values: np.ndarray, origin=(0.0, 0.0, 0.0), delta=(1.0, 1.0, 1.0)):
+    """Writes a 3-D array values[i, j, k] as an SVL grid (Serializer_Field::WriteGrid_SVL); the
+    array's dtype picks the value type (int8, int16, int32, float32 or float64)."""
+    values = np.asarray(values)
+    if values.ndim != 3:
+        raise ValueError("values must be a 3-D array indexed [i, j, k]")
+    fmt = {np.dtype(t): f for f, t in SVL_DTYPES.items()}.get(values.dtype)
+    if fmt is None:
+        raise ValueError(f"SVL holds int8, int16, int32, float32 or float64 values, not {values.dtype}")
+    flat = np.ascontiguousarray(values.ravel(order="F"))
+    _check(lib().phx_svl_write(os.fsencode(path), C.byref(_grid(values.shape, origin, delta)), fmt, _p(flat)))
+
+
+def read_svl_header(path: str):
+    """(shape, origin, delta, value type) of an SVL grid file."""
+    g = Grid_(); f = C.c_int32()
+    _check(lib().phx_svl_read_header(os.fsencode(path), C.byref(g), C.byref(f)))
+    return tuple(g.shape), tuple(g.origin), tuple(g.delta), int(f.value)
+
+
+def read_svl(path: str, dtype=None):
+    """Reads an SVL grid (Serializer_Field::ReadGrid_SVL) as values[i, j, k], origin, delta;
+    dtype (one of the five SVL types) converts the values as the reference does, None keeps the
+    file's type."""
+    shape, origin, delta, fmt = read_svl_header(path)
+    if dtype is not None:
+        fmt = {np.dtype(t): f for f, t in SVL_DTYPES.items()}.get(np.dtype(dtype))
+        if fmt is None:
+            raise ValueError(f"SVL holds int8, int16, int32, float32 or float64 values, not {dtype}")
+    flat = np.empty(int(np.prod(shape, dtype=np.int64)), dtype=SVL_DTYPES[fmt])
+    _check(lib().phx_svl_read(os.fsencode(path), fmt, _p(flat), flat.size))
+    return flat.reshape(shape, order="F"), origin, delta
 
 
 class Context:
@@ -455,6 +514,17 @@ class Instance:
         E = np.zeros(m); g = np.zeros((m, 12)); H = np.zeros((m, 12, 12))
         _check(lib().phx_element_local(self.h, _p(xx), int(precision), _p(E), _p(g), _p(H)))
         return E, g, H
+
+    def sample_grid(self, field: int, shape, origin, delta, x=None, fill: float = 0.0):
+        """A field of the solve on the cell centres of a grid over the rest shape
+        (phx_instance_sample_grid): values[i, j, k] and the owning tet of each (-1: outside)."""
+        xx = None if x is None else np.ascontiguousarray(x, dtype=np.float64)
+        count = int(np.prod(np.asarray(shape, dtype=np.int64)))
+        vals = np.empty(count, dtype=np.float64)
+        own = np.empty(count, dtype=np.int32)
+        _check(lib().phx_instance_sample_grid(self.h, _p(xx), int(field), C.byref(_grid(shape, origin, delta)),
+                                              float(fill), _p(vals), _p(own)))
+        return vals.reshape(tuple(shape), order="F"), own.reshape(tuple(shape), order="F")
 
     def solve_static(self, opts: Options, x=None):
         xx = None if x is None else np.ascontiguousarray(x, dtype=np.float64).copy()

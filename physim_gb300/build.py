@@ -17,7 +17,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libphx.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["kernels.cu", "engine.cu", "noalloc.cu", "pattern.cpp", "scene.cpp"]
+SOURCES = ["kernels.cu", "engine.cu", "noalloc.cu", "field.cu", "pattern.cpp", "scene.cpp", "field_io.cpp"]
 
 
 def nvcc() -> str:

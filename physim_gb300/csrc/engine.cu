@@ -1777,6 +1777,66 @@ int phx_element_local(phx_instance inst, const double* x, int32_t precision, dou
   return PHX_OK;
 }
 
+int phx_instance_sample_grid(phx_instance inst, const double* x, int32_t field, const phx_grid* grid, double fill,
+                             double* values, int32_t* owner) {
+  if (!inst || !grid || !values) return set_err(PHX_EINVAL, "NULL argument");
+  if (field < PHX_FIELD_DISPLACEMENT_X || field > PHX_FIELD_ENERGY_DENSITY)
+    return set_err(PHX_EINVAL, "unknown field " + std::to_string(field));
+  int64_t count = 1;
+  for (int d = 0; d < 3; ++d) {
+    if (grid->shape[d] < 1) return set_err(PHX_EINVAL, "grid: every shape entry must be >= 1");
+    if (!std::isfinite(grid->origin[d]) || !(grid->delta[d] > 0.0) || !std::isfinite(grid->delta[d]))
+      return set_err(PHX_EINVAL, "grid: origin must be finite and delta positive");
+    count *= grid->shape[d];
+    if (count > INT32_MAX) return set_err(PHX_EINVAL, "grid: more than 2^31 - 1 values");
+  }
+  TRY(require_resident(inst));
+  phx_context ctx = inst->ctx;
+  if (field == PHX_FIELD_ENERGY_DENSITY) {
+    NState s;
+    TRY(eval_eg(inst, x, 0, &s));
+  } else if (x) {
+    TRY(upload_x(inst, x, inst->dev.x));
+  }
+  int32_t* d_owner = (int32_t*)ctx->arena.alloc((size_t)count * sizeof(int32_t));
+  double* d_values = (double*)ctx->arena.alloc((size_t)count * sizeof(double));
+  auto release = [&] {
+    ctx->arena.free(d_owner);
+    ctx->arena.free(d_values);
+  };
+  if (!d_owner || !d_values) {
+    release();
+    return set_err(PHX_ENOMEM, "device arena exhausted (grid of " + std::to_string(count) + " values)");
+  }
+  GridSampleArgs a{};
+  a.n = inst->dev.n;
+  a.m = inst->dev.m;
+  a.tets = inst->dev.tets;
+  a.xrest = inst->dev.xrest;
+  a.x = inst->dev.x;
+  a.energy = inst->dev.Eloc;
+  a.field = field;
+  for (int d = 0; d < 3; ++d) {
+    a.shape[d] = grid->shape[d];
+    a.origin[d] = grid->origin[d];
+    a.delta[d] = grid->delta[d];
+  }
+  a.fill = fill;
+  a.owner = d_owner;
+  a.values = d_values;
+  cudaError_t e = launch_grid_sample(ctx->stream, a, ctx->num_sms);
+  ctx->launches += 3;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(values, d_values, (size_t)count * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess && owner)
+    e = cudaMemcpyAsync(owner, d_owner, (size_t)count * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream);
+  cudaError_t es = cudaStreamSynchronize(ctx->stream);  // nothing of the grid's may be in flight once freed
+  if (e == cudaSuccess) e = es;
+  release();
+  if (e != cudaSuccess) return set_err(PHX_ECUDA, cudaGetErrorString(e));
+  return PHX_OK;
+}
+
 int phx_solve_static(phx_instance inst, const phx_options* o, double* x, phx_report* rep) {
   if (!inst) return set_err(PHX_EINVAL, "inst is NULL");
   if (inst->in_server) return set_err(PHX_EBUSY, "instance is admitted to a server");

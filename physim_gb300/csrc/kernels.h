@@ -93,4 +93,21 @@ cudaError_t build_solve_graph(bool fp64, int grid, const BatchDev& B, const Engi
 void launch(KernelId id, int grid, cudaStream_t s, const BatchDev& B, bool fp64);
 const char* kernel_name(KernelId id);
 
+// A field of one instance sampled on the cell centres of a grid over its rest shape (field.cu).
+struct GridSampleArgs {
+  int n, m;
+  const int32_t* tets;   // [m][4]
+  const double* xrest;   // [n][4] rest positions
+  const double* x;       // [n][4] positions
+  const double* energy;  // [m] element energies (field 5), else unused
+  int field;             // PHX_FIELD_*
+  int shape[3];
+  double origin[3], delta[3];
+  double fill;
+  int32_t* owner;        // [cells] owning tet or -1
+  double* values;        // [cells]
+};
+// k_grid_init, k_grid_claim (one warp per tet), k_grid_eval (one thread per cell) on stream s.
+cudaError_t launch_grid_sample(cudaStream_t s, const GridSampleArgs& a, int num_sms);
+
 }  // namespace phx
