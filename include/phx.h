@@ -143,6 +143,8 @@ typedef struct phx_report {
   double seconds;           /* wall time of the call */
   int32_t hessian_evals;    /* element Hessian + assembly passes */
   int32_t fp64_iterations;  /* Newton iterations of the FP64 finish (0: none); included in iterations */
+  int32_t pcg_slices;       /* cluster-PCG solves that left their cluster at a time slice's end and resumed
+                               in a later launch (scheduling only: the results are the same) */
 } phx_report;
 
 /* ---- library ----------------------------------------------------------- */

@@ -101,7 +101,8 @@ class Report(C.Structure):
     _fields_ = [("result", C.c_int32), ("iterations", C.c_int32), ("bisections", C.c_int32),
                 ("reg_trials", C.c_int32), ("pcg_iterations", C.c_int64), ("refine_sweeps", C.c_int32),
                 ("status", C.c_int32), ("obj", C.c_double), ("opt", C.c_double), ("opt0", C.c_double),
-                ("seconds", C.c_double), ("hessian_evals", C.c_int32), ("fp64_iterations", C.c_int32)]
+                ("seconds", C.c_double), ("hessian_evals", C.c_int32), ("fp64_iterations", C.c_int32),
+                ("pcg_slices", C.c_int32)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}

@@ -614,6 +614,7 @@ void fill_report(const NState& s, bool step, double seconds, phx_report* r) {
   r->seconds = seconds;
   r->hessian_evals = s.hess_count;
   r->fp64_iterations = 0;
+  r->pcg_slices = s.pcg_slices;
 }
 
 // Report of a static solve that an FP64 finish continued: counts of both parts, the
@@ -627,6 +628,7 @@ void fill_report_finished(const NState& a, const NState& b, double seconds, phx_
   r->pcg_iterations += a.pcg_total;
   r->refine_sweeps += a.total_sweeps;
   r->hessian_evals += a.hess_count;
+  r->pcg_slices += a.pcg_slices;
   r->opt0 = a.opt0;
   r->fp64_iterations = b.it;
   if (a.error) r->status = PHX_ETIMEOUT;

@@ -1173,6 +1173,7 @@ __device__ __forceinline__ void st_resid(const BatchDev& B, const TileMap& M, in
         st->pcg_parity = 0;
         st->beta = 0.0;
         st->truncate = 0;
+        st->pcg_resume = 0;
         st->lin_status = LIN_RUNNING;
         st->phase = PH_PCG;
       }
@@ -1555,6 +1556,8 @@ __device__ void compact(const BatchDev& B, const EngineArgs& A) {
       W[kWaitTake + 1] = 0;
       W[kWaitLeft] = r[2];
       W[kWaitPass] = 0;
+      W[kWaitDone] = 0;
+      W[kWaitDone + 1] = 0;
       pre3[0] = 0;
     }
   }
@@ -2023,9 +2026,16 @@ static_assert(((4 * kCgMaxChunks + 15) & ~15) + ((4 * (kCgMaxCpc + 1) + 15) & ~1
               "rows of the largest cluster instance must fit in shared memory");
 
 constexpr int kLinAbort = -1;  // a reduction wait gave up: the cluster leaves together (cg_reduce)
+constexpr int kLinYield = -2;  // the solve's time slice ended: its state is saved, it resumes in a later launch
+// A solve leaves its cluster at the end of an iteration (a time slice) once it has iterated
+// kCgSliceMin times in this launch, at least one solve of the launch has ended, and at least
+// half of the launch's clusters found no solve left: the instances whose solves ended then go
+// on in the engine while this one waits for the next cluster launch, where it resumes from the
+// saved state with the same bits.
+constexpr int kCgSliceMin = 32;
 struct CgResult {  // FP32 like the solve; widened once when written to the instance state
   int iter, done, status;
-  float rr, eta, gamma, beta;
+  float rr, eta, gamma, beta, alpha;
 };
 // Dynamic shared memory of k_pcg_cg, declared at file scope so that the helpers below form
 // their pointers from it: the compiler then knows every one of them is shared and issues
@@ -2087,9 +2097,13 @@ __device__ __forceinline__ float4 cl_ld4f(uint32_t a) {
 //    returns, so no CTA touches another's shared memory after that barrier.
 constexpr long long kCgWaitCycles = 2000000000LL;
 constexpr long long kCgDrainCycles = 200000000LL;  // pushes in flight into this CTA at an abort
+// fl (thread 0's value) travels in the fourth float of the CTA's push; every CTA reads rank 0's
+// as red[0][3] once the reduction has landed, so a decision that rank 0 takes is the same in
+// every CTA.
 template <int K, int CL, int NT>
 __device__ __forceinline__ bool cg_reduce(float (&p)[K], unsigned rank, float (*red)[4], float (*ws)[4], uint32_t mbar,
-                                          unsigned& phase, int32_t* err, uint32_t abort_sm, float (&tot)[K]) {
+                                          unsigned& phase, int32_t* err, uint32_t abort_sm, float (&tot)[K],
+                                          float fl = 0.f) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < K; ++k)
@@ -2108,6 +2122,7 @@ __device__ __forceinline__ bool cg_reduce(float (&p)[K], unsigned rank, float (*
       for (int off = 16; off > 0; off >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], off);
       v[k] = __shfl_sync(0xffffffffu, v[k], 0);
     }
+    v[3] = __shfl_sync(0xffffffffu, fl, 0);
     if (lane == 0)
       asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(CL * 16) : "memory");
     if (lane < CL) {
@@ -2279,7 +2294,8 @@ template <int L, int CL, int NT>
 __device__ __forceinline__ CgResult cg_solve(const InstDev& I, const CgShared& S, unsigned rank, int c0, int row0,
                                           int row1, int64_t sb, float (*red)[4], float (*ws)[4], uint32_t mbar,
                                           unsigned& phase, int32_t* err, uint32_t abort_sm, float sh, float thr,
-                                          int maxit, bool trunc_ok, int iter0) {
+                                          int maxit, bool trunc_ok, int iter0, bool resume, const int32_t* slice,
+                                          int ncl) {
   const int nrow = row1 - row0, ms = S.mrows;
   float4* const Z = cgs<float4>(S.z);
   float4* const Rv = cgs<float4>(S.r);
@@ -2288,56 +2304,96 @@ __device__ __forceinline__ CgResult cg_solve(const InstDev& I, const CgShared& S
   float4* const Sv = cgs<float4>(S.s);
   float4* const Qv = cgs<float4>(S.q);
   const float* const Mi = cgs<const float>(S.mi);
-  CgResult out{iter0, 0, LIN_RUNNING, 0.f, 0.f, 0.f, 0.f};
-  // start: r and z = M^-1 r from the residual stage, e = 0
-  float g1[2] = {0.f, 0.f};
-  for (int t = threadIdx.x; t < nrow; t += NT) {
-    float r[3], z[3];
-    ld4(I.r32, row0 + t, r);
-    ld4(I.z32, row0 + t, z);
-    Rv[t] = make_float4(r[0], r[1], r[2], 0.f);
-    Z[t] = make_float4(z[0], z[1], z[2], 0.f);
-    Ev[t] = make_float4(0.f, 0.f, 0.f, 0.f);
-    g1[0] += r[0] * z[0] + r[1] * z[1] + r[2] * z[2];
-    g1[1] += r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
-  }
-  cl_sync();  // z of every CTA written
-  float p3[3] = {g1[0], g1[1], cg_spmv<L, NT>(I, S, c0, row0, row1, sb, sh)};
-  float t3[3];
-  if (!cg_reduce<3, CL, NT>(p3, rank, red, ws, mbar, phase, err, abort_sm, t3)) {
-    cl_sync();  // the barrier the peers reach next; they see the abort word after it
-    out.status = kLinAbort;
-    return out;
-  }
-  float gam = t3[0];
-  out.rr = t3[1];
-  if (t3[1] < thr) {
-    out.status = LIN_CONVERGED;
-    return out;
-  }
-  float eta = t3[2], beta = 0.f, alpha;
+  CgResult out{iter0, 0, LIN_RUNNING, 0.f, 0.f, 0.f, 0.f, 0.f};
+  float gam, eta, beta, alpha;
   bool last = false;
-  out.eta = eta;
-  out.gamma = gam;
-  if (!(eta > 0.f)) {
-    if (!trunc_ok && eta < 0.f) {
-      // Eigen's ConjugateGradient has no curvature test: a negative step along p, and on
-    } else if (trunc_ok && eta < 0.f && out.iter == 0) {
-      eta = -eta;  // truncated CG, first direction: one step along z with |z.Az| and stop
-      last = true;
-    } else {
-      out.status = (trunc_ok && eta < 0.f) ? LIN_TRUNCATED : LIN_BREAKDOWN;
+  if (resume) {
+    // the state the last time slice saved: this CTA's rows of r, z, e, p, s, q and the
+    // scalars of the next iteration, the exact FP32 values
+    for (int t = threadIdx.x; t < nrow; t += NT) {
+      const int v = row0 + t;
+      float r[3], z[3], e[3], p[3], s[3], q[3];
+      ld4(I.r32, v, r);
+      ld4(I.z32, v, z);
+      ld4(I.e32, v, e);
+      ld4(I.p32a, v, p);
+      ld4(I.p32b, v, s);
+      ld4(I.q32, v, q);
+      Rv[t] = make_float4(r[0], r[1], r[2], 0.f);
+      Z[t] = make_float4(z[0], z[1], z[2], 0.f);
+      Ev[t] = make_float4(e[0], e[1], e[2], 0.f);
+      Pv[t] = make_float4(p[0], p[1], p[2], 0.f);
+      Sv[t] = make_float4(s[0], s[1], s[2], 0.f);
+      Qv[t] = make_float4(q[0], q[1], q[2], 0.f);
+    }
+    const NState* st = I.st;
+    gam = (float)st->rz;
+    eta = (float)st->pq;
+    beta = (float)st->beta;
+    alpha = (float)st->alpha;
+    out.rr = (float)st->rr;
+    out.eta = eta;
+    out.gamma = gam;
+    out.beta = beta;
+    __syncthreads();  // the first iteration's vector update reads only this CTA's rows
+  } else {
+    // start: r and z = M^-1 r from the residual stage, e = 0
+    float g1[2] = {0.f, 0.f};
+    for (int t = threadIdx.x; t < nrow; t += NT) {
+      float r[3], z[3];
+      ld4(I.r32, row0 + t, r);
+      ld4(I.z32, row0 + t, z);
+      Rv[t] = make_float4(r[0], r[1], r[2], 0.f);
+      Z[t] = make_float4(z[0], z[1], z[2], 0.f);
+      Ev[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+      g1[0] += r[0] * z[0] + r[1] * z[1] + r[2] * z[2];
+      g1[1] += r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+    }
+    cl_sync();  // z of every CTA written
+    float p3[3] = {g1[0], g1[1], cg_spmv<L, NT>(I, S, c0, row0, row1, sb, sh)};
+    float t3[3];
+    if (!cg_reduce<3, CL, NT>(p3, rank, red, ws, mbar, phase, err, abort_sm, t3)) {
+      cl_sync();  // the barrier the peers reach next; they see the abort word after it
+      out.status = kLinAbort;
       return out;
     }
+    gam = t3[0];
+    out.rr = t3[1];
+    if (t3[1] < thr) {
+      out.status = LIN_CONVERGED;
+      return out;
+    }
+    eta = t3[2];
+    beta = 0.f;
+    out.eta = eta;
+    out.gamma = gam;
+    if (!(eta > 0.f)) {
+      if (!trunc_ok && eta < 0.f) {
+        // Eigen's ConjugateGradient has no curvature test: a negative step along p, and on
+      } else if (trunc_ok && eta < 0.f && out.iter == 0) {
+        eta = -eta;  // truncated CG, first direction: one step along z with |z.Az| and stop
+        last = true;
+      } else {
+        out.status = (trunc_ok && eta < 0.f) ? LIN_TRUNCATED : LIN_BREAKDOWN;
+        return out;
+      }
+    }
+    alpha = gam / eta;
   }
-  alpha = gam / eta;
   for (int it = 0;; ++it) {
     if (out.iter >= maxit) {
       out.status = LIN_MAXITER;
       break;
     }
     const float a = alpha, b = beta;
-    const bool first = it == 0;
+    const bool first = it == 0 && !resume;
+    // rank 0 decides whether this iteration ends the solve's time slice; the decision reaches
+    // every CTA with this iteration's reduction
+    float slice_fl = 0.f;
+    if (slice && rank == 0 && threadIdx.x == 0 && it + 1 >= kCgSliceMin) {
+      const int ended = *(volatile const int32_t*)slice, idle = *(volatile const int32_t*)(slice + 1);
+      if (ended > 0 && 2 * idle >= ncl) slice_fl = 1.f;
+    }
     float g[2] = {0.f, 0.f};
     for (int t = threadIdx.x; t < nrow; t += NT) {
       const float4 z = Z[t], s = Sv[t];
@@ -2380,11 +2436,12 @@ __device__ __forceinline__ CgResult cg_solve(const InstDev& I, const CgShared& S
     }
     float pg[3] = {g[0], g[1], cg_spmv<L, NT>(I, S, c0, row0, row1, sb, sh)};
     float tg[3];
-    if (!cg_reduce<3, CL, NT>(pg, rank, red, ws, mbar, phase, err, abort_sm, tg)) {
+    if (!cg_reduce<3, CL, NT>(pg, rank, red, ws, mbar, phase, err, abort_sm, tg, slice_fl)) {
       cl_sync();  // the barrier the peers reach next; they see the abort word after it
       out.status = kLinAbort;
       return out;
     }
+    const bool slice_end = red[0][3] != 0.f;  // rank 0's decision, the same in every CTA
     const float gam_new = tg[0];
     out.rr = tg[1];
     if (tg[1] < thr) {
@@ -2402,13 +2459,33 @@ __device__ __forceinline__ CgResult cg_solve(const InstDev& I, const CgShared& S
       break;
     }
     alpha = gam / eta;
+    if (slice_end) {
+      // the slice ends: the rows go to the instance's FP32 vectors (s in p32b), the scalars
+      // to its state (written by the caller); the next launch resumes with the same bits
+      for (int t = threadIdx.x; t < nrow; t += NT) {
+        const int v = row0 + t;
+        const float4 r = Rv[t], z = Z[t], e = Ev[t], p = Pv[t], sv = Sv[t], q = Qv[t];
+        st4(I.r32, v, {r.x, r.y, r.z});
+        st4(I.z32, v, {z.x, z.y, z.z});
+        st4(I.e32, v, {e.x, e.y, e.z});
+        st4(I.p32a, v, {p.x, p.y, p.z});
+        st4(I.p32b, v, {sv.x, sv.y, sv.z});
+        st4(I.q32, v, {q.x, q.y, q.z});
+      }
+      out.alpha = alpha;
+      out.status = kLinYield;
+      break;
+    }
   }
   return out;
 }
 
+// slice: [0] solves of this launch that ended, [1] clusters that found no solve left (the
+// time slices read them; null: every solve runs to its end).
 template <int CL, int NT>
 __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_pcg_cg(BatchDev B, const int32_t* list,
-                                                                               const int32_t* countp, int32_t* next) {
+                                                                               const int32_t* countp, int32_t* next,
+                                                                               int32_t* slice) {
   __shared__ __align__(16) float red[CL][4];  // partial sums pushed by every CTA of the cluster
   __shared__ float ws[NT / 32][4];
   __shared__ __align__(8) uint64_t mbar_obj;   // completes when all CL pushes of a reduction landed
@@ -2428,13 +2505,18 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_pcg_cg(Bat
   __shared__ int jslot[2];
   const int count = __ldcg(countp);
   unsigned jpar = 0;
+  const int ncl = (int)(gridDim.x / CL);
   for (;;) {
     const int j = cl_next_job<CL>(next, jslot, jpar);
-    if (j >= count) break;
+    if (j >= count) {
+      if (slice && rank == 0 && tid == 0) atomicAdd(slice + 1, 1);
+      break;
+    }
     const int i = __ldcg(list + j);
     const InstDev& I = B.inst[i];  // fields are re-read (L1) where needed: registers go to the rows
     NState* st = I.st;
     if (I.pcg_cluster != 1 || *(volatile int32_t*)&st->phase != PH_PCG) continue;  // uniform over the cluster
+    const bool resume = *(volatile int32_t*)&st->pcg_resume != 0;  // written before this launch: uniform
     const int n = I.n, nch = I.nchunks;
     const int cpc = (nch + CL - 1) / CL;
     const int c0 = min(nch, (int)rank * cpc), c1 = min(nch, c0 + cpc);
@@ -2519,14 +2601,36 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_pcg_cg(Bat
     const int iter0 = st->pcg_iter;
     CgResult out;
     if (L == 4) out = cg_solve<4, CL, NT>(I, S, rank, c0, row0, row1, sb, red, ws, mbar, phase, err, abort_sm, sh, thr, maxit,
-                                           trunc_ok, iter0);
+                                           trunc_ok, iter0, resume, slice, ncl);
     else if (L == 2) out = cg_solve<2, CL, NT>(I, S, rank, c0, row0, row1, sb, red, ws, mbar, phase, err, abort_sm, sh, thr, maxit,
-                                           trunc_ok, iter0);
+                                           trunc_ok, iter0, resume, slice, ncl);
     else out = cg_solve<1, CL, NT>(I, S, rank, c0, row0, row1, sb, red, ws, mbar, phase, err, abort_sm, sh, thr, maxit,
-                                           trunc_ok, iter0);
+                                           trunc_ok, iter0, resume, slice, ncl);
     if (out.status == kLinAbort) {  // every CTA of the cluster leaves after the same barrier
       cg_drain(mbar, phase);
       return;                       // the batch error is flagged; the host reports a timeout
+    }
+    if (out.status == kLinYield) {
+      // the rows are saved; the instance keeps waiting for the cluster PCG (phase PH_PCG)
+      if (rank == 0 && tid == 0) {
+        st->pcg_iter = out.iter;
+        st->pcg_total += out.done;
+        st->rr = out.rr;
+        st->pq = out.eta;
+        st->rz = out.gamma;
+        st->beta = out.beta;
+        st->alpha = out.alpha;
+        st->pcg_resume = 1;
+        st->pcg_slices++;
+        if (B.algo_total)
+          atomicAdd(B.algo_total + K_PCG_CLUSTER, (I.algo[K_PCG_A] + I.algo[K_PCG_B]) * out.done);
+      }
+      cl_sync();  // shared buffers and partial slots are reused by the next instance
+      if (cg_aborted(abort_sm)) {
+        cg_drain(mbar, phase);
+        return;
+      }
+      continue;
     }
     for (int t = tid; t < nrow; t += NT) {
       const float4 e = cgs<float4>(S.e)[t];
@@ -2534,6 +2638,8 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_pcg_cg(Bat
       st4(I.e32, row0 + t, ev);
     }
     if (rank == 0 && tid == 0) {
+      if (slice) atomicAdd(slice, 1);
+      st->pcg_resume = 0;
       st->pcg_iter = out.iter;
       st->pcg_total += out.done;
       st->rr = out.rr;
@@ -2617,9 +2723,11 @@ struct ClusterArgs {
   const int32_t* list;
   const int32_t* count;
   int32_t* take;
+  int32_t* slice;  // kind 1: the counters its time slices read
 };
 ClusterArgs cluster_args(int32_t* wait, int cap, int kind) {
-  return ClusterArgs{wait + kWaitLists + (kind - 1) * cap, wait + kWaitCount + (kind - 1), wait + kWaitTake + (kind - 1)};
+  return ClusterArgs{wait + kWaitLists + (kind - 1) * cap, wait + kWaitCount + (kind - 1), wait + kWaitTake + (kind - 1),
+                     wait + kWaitDone};
 }
 
 cudaError_t launch_pcg_cluster(cudaStream_t s, const BatchDev& B, int32_t* wait, int cap, int clusters, int kind) {
@@ -2628,7 +2736,7 @@ cudaError_t launch_pcg_cluster(cudaStream_t s, const BatchDev& B, int32_t* wait,
   const int32_t* list = c.list;
   const int32_t* count = c.count;
   int32_t* take = c.take;
-  if (kind == 1) k_pcg_cg<kCl, kClThreads><<<clusters * kCl, kClThreads, kCgSmem, s>>>(B, list, count, take);
+  if (kind == 1) k_pcg_cg<kCl, kClThreads><<<clusters * kCl, kClThreads, kCgSmem, s>>>(B, list, count, take, c.slice);
   else k_pcg_cluster<float, kCl, kClThreads><<<clusters * kCl, kClThreads, 0, s>>>(B, list, count, take);
   return cudaGetLastError();
 }
@@ -2774,7 +2882,8 @@ cudaError_t build_solve_graph(bool fp64, int grid, const BatchDev& B, const Engi
       const int32_t* list = c.list;
       const int32_t* countp = c.count;
       int32_t* next = c.take;
-      void* ca[] = {&b, &list, &countp, &next};
+      int32_t* slice = c.slice;
+      void* ca[] = {&b, &list, &countp, &next, &slice};  // k_pcg_cluster takes the first four
       const void* fn = k == 0 ? (const void*)k_pcg_cg<kCl, kClThreads> : (const void*)k_pcg_cluster<float, kCl, kClThreads>;
       e = add_kernel(body, &node, &prev, fn, dim3(clusters[k] * kCl), dim3(kClThreads), k == 0 ? kCgSmem : 0, ca);
       prev = node;

@@ -55,9 +55,10 @@ struct EngineArgs {
 // Layout of EngineArgs::wait: at kWaitCount the waiting counts of PCG kinds 1..3 (1, 2: one
 // cluster per instance, 3: the whole-GPU kernels k_gpcg_a/b); at kWaitTake the take counters
 // of kinds 1 and 2; at kWaitLeft the kind-3 instances still iterating; at kWaitPass the kind-3
-// loop's passes; from kWaitLists the three lists (cap each, corder's order) and the kind-3
-// PCG tile prefix (cap + 1).
-constexpr int kWaitCount = 0, kWaitTake = 3, kWaitLeft = 5, kWaitPass = 6, kWaitLists = 8;
+// loop's passes; at kWaitDone the kind-1 solves that ended in this cluster launch and at
+// kWaitDone + 1 its clusters that found no solve left (what a solve's time slice reads); from
+// kWaitLists the three lists (cap each, corder's order) and the kind-3 PCG tile prefix (cap + 1).
+constexpr int kWaitCount = 0, kWaitTake = 3, kWaitLeft = 5, kWaitPass = 6, kWaitDone = 7, kWaitLists = 10;
 inline int wait_size(int cap) { return kWaitLists + 4 * cap + 1; }
 constexpr long long kBarrierLimit = 4000000000LL;  // default wait_limit: about 2 s of SM clock
 

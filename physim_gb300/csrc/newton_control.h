@@ -356,6 +356,7 @@ PHX_HD inline void ctl_advance(NState& s, const DevOpts& o) {
         s.total_reg = 0;
         s.total_sweeps = 0;
         s.pcg_total = 0;
+        s.pcg_slices = 0;
         s.hess_count = 0;
         s.opt0 = -1.0;
         s.eta = 0.0;

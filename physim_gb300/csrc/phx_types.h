@@ -111,9 +111,11 @@ struct NState {
   double log_step;                             // ||dx_final|| of the step being logged
   double dg, dg_eval;                          // dx . g at the search's start; dx . g at the trial
   int32_t log_pending, log_count;              // per-iteration log bookkeeping
-  int32_t lsk, pad_ls;                         // trials in the batch being evaluated (PH_EVALK)
+  int32_t lsk;                                 // trials in the batch being evaluated (PH_EVALK)
+  int32_t pcg_resume;                          // 1: the cluster PCG left its solve at a time slice's end, state saved
   double ls_a[8], ls_e[8], ls_eel[8];          // their step lengths, energies, element energies
   int32_t stage, iter_staged;                  // boundary-condition stage; 1 once this iteration stepped it
+  int32_t pcg_slices, pad_sl;                  // cluster-PCG time slices that ended before their solve
 };
 
 constexpr int kLogCap = 256;                   // Newton iterations kept in the per-instance log

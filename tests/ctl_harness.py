@@ -26,9 +26,10 @@ class NState(C.Structure):
             "obj", "opt", "opt0", "obj_new", "alpha_trial", "factor", "scale", "dx_norm", "b_dot_dx", "E_el",
             "E_eval", "gg_eval", "normA2", "shift", "regT", "bb", "rr64", "rz", "rr", "pq", "alpha", "beta",
             "thr_inner", "thr_final", "tol_eff", "lin_tol", "eta", "opt_prev", "log_step", "dg", "dg_eval")] + \
-        [("log_pending", C.c_int32), ("log_count", C.c_int32), ("lsk", C.c_int32), ("pad_ls", C.c_int32),
+        [("log_pending", C.c_int32), ("log_count", C.c_int32), ("lsk", C.c_int32), ("pcg_resume", C.c_int32),
          ("ls_a", C.c_double * 8), ("ls_e", C.c_double * 8), ("ls_eel", C.c_double * 8),
-         ("stage", C.c_int32), ("iter_staged", C.c_int32)]
+         ("stage", C.c_int32), ("iter_staged", C.c_int32),
+         ("pcg_slices", C.c_int32), ("pad_sl", C.c_int32)]
 
 
 class DevOpts(C.Structure):

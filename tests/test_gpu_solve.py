@@ -142,6 +142,33 @@ def test_batch_equals_alone_bitwise(gpu_ctx):
         assert ra["obj"] == rb["obj"]
 
 
+def test_cluster_time_slices_keep_the_bits(gpu_ctx):
+    """Long cluster-PCG solves that leave their cluster at the end of a time slice (another
+    solve of the launch has ended and half the clusters found nothing left) and resume in a
+    later launch give the bits of the same instances solved alone, where no slice ends."""
+    idx = [38, 52, 399, 96]  # 196 nodes (short solves), then three with PCG solves of ~400 iterations
+    meshes = [M.batch_instance(3, i) for i in idx]
+    o = px.options(precision=px.PREC_FP32_REFINE, tol_rel=1e-6, tol_max_error=0.0, tol_min_impr=0.0,
+                   tol_min_step=0.0)
+    saved = gpu_ctx.launch_settings()
+    try:
+        gpu_ctx.launch_settings(wait_share=1)  # every waiting solve in one cluster launch
+        alone = []
+        for m in meshes:
+            inst = px.Instance(gpu_ctx, m)
+            alone.append(inst.solve_static(o, m.X0.ravel()))
+        insts = [px.Instance(gpu_ctx, m) for m in meshes]
+        reps, xs = gpu_ctx.batch_solve(insts, o, [m.X0.ravel().copy() for m in meshes])
+    finally:
+        gpu_ctx.launch_settings(**saved)
+    assert all(ra["pcg_slices"] == 0 for _, ra in alone)
+    assert sum(r["pcg_slices"] for r in reps) > 0
+    for (xa, ra), xb, rb in zip(alone, xs, reps):
+        assert np.array_equal(xa, xb)
+        assert ra["iterations"] == rb["iterations"] and ra["pcg_iterations"] == rb["pcg_iterations"]
+        assert ra["obj"] == rb["obj"] and ra["result_name"] == rb["result_name"]
+
+
 def test_batch_against_oracle(gpu_ctx):
     meshes = [M.batch_instance(3, i) for i in range(10, 14)]
     insts = [px.Instance(gpu_ctx, m) for m in meshes]
