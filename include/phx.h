@@ -188,10 +188,14 @@ typedef struct phx_launch_settings {
   int32_t wait_share;
   int32_t rounds;
   int32_t pcg_grid;
+  int32_t slice_share;  /* a cluster-PCG solve ends its time slice (and resumes in the next cluster
+                           launch) once clusters/slice_share of the launch's clusters found no solve
+                           left and another solve of the launch ended; 0: no time slices */
+  int32_t slice_min;    /* PCG iterations a solve runs in a launch before its slice may end */
 } phx_launch_settings;
 /* Reads the context's default settings into *get (if not NULL), then sets them from *set (if
  * not NULL; values checked: graph 0/1, wait_rounds 1..64, wait_share 1..64, rounds 1..1024,
- * pcg_grid 0/1).  The serving calls use the context's defaults. */
+ * pcg_grid 0/1, slice_share 0..64, slice_min 1..1000000).  The serving calls use the context's defaults. */
 int phx_context_launch_settings(phx_context ctx, phx_launch_settings* get, const phx_launch_settings* set);
 /* Tunes the settings for a batch: times phx_batch_solve-style solves of the instances from
  * their current positions under the default settings and candidates around them (one

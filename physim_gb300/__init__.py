@@ -58,7 +58,7 @@ class Mesh_(C.Structure):
 class LaunchSettings_(C.Structure):
     """phx_launch_settings: scheduling of a context's batch solves (changes no result)."""
     _fields_ = [("graph", C.c_int32), ("wait_rounds", C.c_int32), ("wait_share", C.c_int32), ("rounds", C.c_int32),
-                ("pcg_grid", C.c_int32)]
+                ("pcg_grid", C.c_int32), ("slice_share", C.c_int32), ("slice_min", C.c_int32)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}

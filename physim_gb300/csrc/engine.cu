@@ -174,7 +174,7 @@ struct phx_context_s {
   int gmax[3] = {-1, -1, -1};   // clusters of kinds 1, 2 resident at once (-1: not queried yet)
   int ggrid = 0;                // CTAs of the whole-GPU PCG kernels
   // scheduling of batch solves (defaults, and tuned settings per batch mix)
-  phx_launch_settings launch{1, kWaitRounds, kWaitShare, kRoundsPerLaunch, 0};
+  phx_launch_settings launch{1, kWaitRounds, kWaitShare, kRoundsPerLaunch, 0, kSliceShare, kSliceMin};
   std::map<std::string, phx_launch_settings> tuned;
   // pinned landing area of batch downloads (states and positions of a batch, one synchronisation)
   char* down = nullptr;
@@ -684,6 +684,8 @@ EngineArgs engine_args(phx_context ctx, const phx_launch_settings& S, int pcg_ch
   A.pcg_chunk = pcg_chunk;
   A.wait_rounds = S.wait_rounds;
   A.wait_share = S.wait_share;
+  A.slice_share = S.slice_share;
+  A.slice_min = S.slice_min;
   A.wait_limit = ctx->wait_limit;
   A.unmet_tag = ctx->unmet_tag;
   A.cfg = ctx->d_cfg;
@@ -794,7 +796,8 @@ int run_step(phx_context ctx, const BatchDev& B0, int num, bool fp64, int pcg_ch
     for (int kind = 1; kind <= 2; ++kind) {
       const int nw = ctx->h_flags[3 + kind];
       if (nw == 0) continue;
-      CU(launch_pcg_cluster(ctx->stream, B, ctx->d_wait, ctx->cap, cluster_count(ctx, kind, nw), kind));
+      CU(launch_pcg_cluster(ctx->stream, B, ctx->d_wait, ctx->cap, cluster_count(ctx, kind, nw), kind, S.slice_share,
+                            S.slice_min));
       ctx->launches++;
     }
     if (ctx->h_flags[6] > 0) TRY(run_gpcg(ctx, B, S, pcg_chunk));
@@ -1941,7 +1944,8 @@ int phx_context_launch_settings(phx_context ctx, phx_launch_settings* get, const
   if (set) {
     if ((set->graph != 0 && set->graph != 1) || set->wait_rounds < 1 || set->wait_rounds > 64 ||
         set->wait_share < 1 || set->wait_share > 64 || set->rounds < 1 || set->rounds > 1024 ||
-        (set->pcg_grid != 0 && set->pcg_grid != 1))
+        (set->pcg_grid != 0 && set->pcg_grid != 1) || set->slice_share < 0 || set->slice_share > 64 ||
+        set->slice_min < 1 || set->slice_min > 1000000)
       return set_err(PHX_EINVAL, "launch settings out of range");
     ctx->launch = *set;
   }
@@ -2035,6 +2039,19 @@ int phx_tune_batch(phx_context ctx, int32_t count, phx_instance* insts, const ph
       c.rounds = v;
       TRY(consider(c));
     }
+    for (int v : {0, 4, 8}) {  // cluster-PCG time slices: off, or once a quarter / an eighth of the clusters idle
+      phx_launch_settings c = best;
+      if (v == c.slice_share) continue;
+      c.slice_share = v;
+      TRY(consider(c));
+    }
+    if (best.slice_share > 0)
+      for (int v : {16, 64, 128}) {
+        phx_launch_settings c = best;
+        if (v == c.slice_min) continue;
+        c.slice_min = v;
+        TRY(consider(c));
+      }
     return PHX_OK;
   };
   const int rc = search();

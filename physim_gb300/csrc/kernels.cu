@@ -2028,11 +2028,10 @@ static_assert(((4 * kCgMaxChunks + 15) & ~15) + ((4 * (kCgMaxCpc + 1) + 15) & ~1
 constexpr int kLinAbort = -1;  // a reduction wait gave up: the cluster leaves together (cg_reduce)
 constexpr int kLinYield = -2;  // the solve's time slice ended: its state is saved, it resumes in a later launch
 // A solve leaves its cluster at the end of an iteration (a time slice) once it has iterated
-// kCgSliceMin times in this launch, at least one solve of the launch has ended, and at least
-// half of the launch's clusters found no solve left: the instances whose solves ended then go
-// on in the engine while this one waits for the next cluster launch, where it resumes from the
-// saved state with the same bits.
-constexpr int kCgSliceMin = 32;
+// slice_min times in this launch, at least one solve of the launch has ended, and enough of the
+// launch's clusters found no solve left (slice_share x idle >= clusters): the instances whose
+// solves ended then go on in the engine while this one waits for the next cluster launch,
+// where it resumes from the saved state with the same bits.
 struct CgResult {  // FP32 like the solve; widened once when written to the instance state
   int iter, done, status;
   float rr, eta, gamma, beta, alpha;
@@ -2295,7 +2294,7 @@ __device__ __forceinline__ CgResult cg_solve(const InstDev& I, const CgShared& S
                                           int row1, int64_t sb, float (*red)[4], float (*ws)[4], uint32_t mbar,
                                           unsigned& phase, int32_t* err, uint32_t abort_sm, float sh, float thr,
                                           int maxit, bool trunc_ok, int iter0, bool resume, const int32_t* slice,
-                                          int ncl) {
+                                          int ncl, int slice_share, int slice_min) {
   const int nrow = row1 - row0, ms = S.mrows;
   float4* const Z = cgs<float4>(S.z);
   float4* const Rv = cgs<float4>(S.r);
@@ -2390,9 +2389,9 @@ __device__ __forceinline__ CgResult cg_solve(const InstDev& I, const CgShared& S
     // rank 0 decides whether this iteration ends the solve's time slice; the decision reaches
     // every CTA with this iteration's reduction
     float slice_fl = 0.f;
-    if (slice && rank == 0 && threadIdx.x == 0 && it + 1 >= kCgSliceMin) {
+    if (slice && rank == 0 && threadIdx.x == 0 && it + 1 >= slice_min) {
       const int ended = *(volatile const int32_t*)slice, idle = *(volatile const int32_t*)(slice + 1);
-      if (ended > 0 && 2 * idle >= ncl) slice_fl = 1.f;
+      if (ended > 0 && slice_share * idle >= ncl) slice_fl = 1.f;
     }
     float g[2] = {0.f, 0.f};
     for (int t = threadIdx.x; t < nrow; t += NT) {
@@ -2481,11 +2480,14 @@ __device__ __forceinline__ CgResult cg_solve(const InstDev& I, const CgShared& S
 }
 
 // slice: [0] solves of this launch that ended, [1] clusters that found no solve left (the
-// time slices read them; null: every solve runs to its end).
+// time slices read them; null: every solve runs to its end).  A solve's slice ends after at
+// least slice_min iterations in this launch, once a solve ended and slice_share x the idle
+// clusters reach the launch's cluster count.
 template <int CL, int NT>
 __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_pcg_cg(BatchDev B, const int32_t* list,
                                                                                const int32_t* countp, int32_t* next,
-                                                                               int32_t* slice) {
+                                                                               int32_t* slice, int slice_share,
+                                                                               int slice_min) {
   __shared__ __align__(16) float red[CL][4];  // partial sums pushed by every CTA of the cluster
   __shared__ float ws[NT / 32][4];
   __shared__ __align__(8) uint64_t mbar_obj;   // completes when all CL pushes of a reduction landed
@@ -2601,11 +2603,11 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(NT, 1) k_pcg_cg(Bat
     const int iter0 = st->pcg_iter;
     CgResult out;
     if (L == 4) out = cg_solve<4, CL, NT>(I, S, rank, c0, row0, row1, sb, red, ws, mbar, phase, err, abort_sm, sh, thr, maxit,
-                                           trunc_ok, iter0, resume, slice, ncl);
+                                           trunc_ok, iter0, resume, slice, ncl, slice_share, slice_min);
     else if (L == 2) out = cg_solve<2, CL, NT>(I, S, rank, c0, row0, row1, sb, red, ws, mbar, phase, err, abort_sm, sh, thr, maxit,
-                                           trunc_ok, iter0, resume, slice, ncl);
+                                           trunc_ok, iter0, resume, slice, ncl, slice_share, slice_min);
     else out = cg_solve<1, CL, NT>(I, S, rank, c0, row0, row1, sb, red, ws, mbar, phase, err, abort_sm, sh, thr, maxit,
-                                           trunc_ok, iter0, resume, slice, ncl);
+                                           trunc_ok, iter0, resume, slice, ncl, slice_share, slice_min);
     if (out.status == kLinAbort) {  // every CTA of the cluster leaves after the same barrier
       cg_drain(mbar, phase);
       return;                       // the batch error is flagged; the host reports a timeout
@@ -2730,13 +2732,17 @@ ClusterArgs cluster_args(int32_t* wait, int cap, int kind) {
                      wait + kWaitDone};
 }
 
-cudaError_t launch_pcg_cluster(cudaStream_t s, const BatchDev& B, int32_t* wait, int cap, int clusters, int kind) {
+cudaError_t launch_pcg_cluster(cudaStream_t s, const BatchDev& B, int32_t* wait, int cap, int clusters, int kind,
+                               int slice_share, int slice_min) {
   if (clusters <= 0) return cudaSuccess;
   const ClusterArgs c = cluster_args(wait, cap, kind);
   const int32_t* list = c.list;
   const int32_t* count = c.count;
   int32_t* take = c.take;
-  if (kind == 1) k_pcg_cg<kCl, kClThreads><<<clusters * kCl, kClThreads, kCgSmem, s>>>(B, list, count, take, c.slice);
+  if (kind == 1)
+    k_pcg_cg<kCl, kClThreads><<<clusters * kCl, kClThreads, kCgSmem, s>>>(B, list, count, take,
+                                                                          slice_share > 0 ? c.slice : nullptr,
+                                                                          slice_share, slice_min);
   else k_pcg_cluster<float, kCl, kClThreads><<<clusters * kCl, kClThreads, 0, s>>>(B, list, count, take);
   return cudaGetLastError();
 }
@@ -2882,8 +2888,9 @@ cudaError_t build_solve_graph(bool fp64, int grid, const BatchDev& B, const Engi
       const int32_t* list = c.list;
       const int32_t* countp = c.count;
       int32_t* next = c.take;
-      int32_t* slice = c.slice;
-      void* ca[] = {&b, &list, &countp, &next, &slice};  // k_pcg_cluster takes the first four
+      int32_t* slice = A.slice_share > 0 ? c.slice : nullptr;
+      int share = A.slice_share, smin = A.slice_min;
+      void* ca[] = {&b, &list, &countp, &next, &slice, &share, &smin};  // k_pcg_cluster takes the first four
       const void* fn = k == 0 ? (const void*)k_pcg_cg<kCl, kClThreads> : (const void*)k_pcg_cluster<float, kCl, kClThreads>;
       e = add_kernel(body, &node, &prev, fn, dim3(clusters[k] * kCl), dim3(kClThreads), k == 0 ? kCgSmem : 0, ca);
       prev = node;

@@ -43,6 +43,8 @@ struct EngineArgs {
   int pcg_chunk;
   int wait_rounds;  // hand the waiting instances to the cluster PCG kernel this many rounds after the
   int wait_share;   // first one waited, or once waiting * wait_share >= active
+  int slice_share;  // cluster-PCG time slices (phx_launch_settings::slice_share, slice_min)
+  int slice_min;
   long long wait_limit;  // SM cycles a grid-barrier wait lasts before it gives up
   int unmet_tag;         // test hook: the grid barrier with this tag waits for one arrival more than
                          // the CTAs taking part, so it gives up (0: none)
@@ -70,7 +72,8 @@ cudaError_t launch_engine(bool fp64, int grid, cudaStream_t s, const BatchDev& B
 cudaError_t launch_prep(cudaStream_t s, const BatchDev& B, const EngineArgs& A, int grid, int max_chunks);
 // PCG of the instances the engine listed as waiting for PCG kind `kind` (1: rows in shared
 // memory, 2: rows in L2): `clusters` clusters take them in list order until none is left
-cudaError_t launch_pcg_cluster(cudaStream_t s, const BatchDev& B, int32_t* wait, int cap, int clusters, int kind);
+cudaError_t launch_pcg_cluster(cudaStream_t s, const BatchDev& B, int32_t* wait, int cap, int clusters, int kind,
+                               int slice_share, int slice_min);
 // Clusters of PCG kind `kind` that fit on the device at once (0 if the query fails)
 int max_active_clusters(int kind);
 // The whole-GPU PCG of the FP32 instances of kind 3 (above the cluster size): `pairs` PCG

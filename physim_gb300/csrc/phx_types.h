@@ -33,6 +33,8 @@ constexpr int kClWideBelow = 32;     // at most this many active instances: one-
 constexpr int kClusterMaxNodes = 13000;  // instances up to this size solve their PCG in one cluster
 constexpr int kWaitRounds = 4;           // engine rounds an instance may wait for the cluster kernel
 constexpr int kWaitShare = 2;            // ... or until 1/kWaitShare of the active instances wait
+constexpr int kSliceShare = 2;           // cluster-PCG time slices end once half the launch's clusters are idle ...
+constexpr int kSliceMin = 32;            // ... and the solve iterated this often in the launch
 
 // Phases of the per-instance Newton state machine (see control in kernels.cu).
 enum Phase : int32_t {

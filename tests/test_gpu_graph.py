@@ -3,7 +3,7 @@
 * A batch solved through CUDA-graph launches (k_prep, engine, cluster PCG kernels and the
   loop test in a device while-loop) gives the bits of the host-driven loop, on the served
   path (cluster PCG) and on the plain FP64 path (whole-GPU PCG).
-* Launch settings change no result: other wait and round settings give the same bits.
+* Launch settings change no result: other wait, round and time-slice settings give the same bits.
 * The tuner leaves the instances as it found them, caches its choice for the batch's mix, and
   a batch solved after tuning gives the bits of one solved before.
 """
@@ -58,13 +58,15 @@ def test_launch_settings_change_no_result(gpu_ctx, defaults):
                    tol_min_step=0.0)
     ref = _solve(gpu_ctx, meshes, o)
     for s in ({"wait_rounds": 1, "wait_share": 1, "rounds": 3}, {"wait_rounds": 16, "wait_share": 8, "rounds": 64},
-              {"graph": 0, "rounds": 1}):
+              {"graph": 0, "rounds": 1}, {"slice_share": 0}, {"wait_share": 1, "slice_share": 64, "slice_min": 1},
+              {"graph": 0, "wait_share": 1, "slice_share": 16, "slice_min": 8}):
         gpu_ctx.launch_settings(**{**defaults, **s})
         _same(ref, _solve(gpu_ctx, meshes, o))
 
 
 def test_launch_settings_are_checked(gpu_ctx, defaults):
-    for bad in ({"graph": 2}, {"wait_rounds": 0}, {"wait_share": 65}, {"rounds": 0}, {"pcg_grid": 2}):
+    for bad in ({"graph": 2}, {"wait_rounds": 0}, {"wait_share": 65}, {"rounds": 0}, {"pcg_grid": 2},
+                {"slice_share": -1}, {"slice_share": 65}, {"slice_min": 0}):
         with pytest.raises(px.PhxError) as ei:
             gpu_ctx.launch_settings(**bad)
         assert ei.value.code == px.PHX_EINVAL
@@ -82,7 +84,7 @@ def test_tuner_leaves_instances_and_results_unchanged(gpu_ctx, defaults):
         i.set_positions(x)
     t = gpu_ctx.tune_batch(insts, o)
     assert t["trials"] >= 3 and t["best_seconds"] <= t["default_seconds"]
-    assert set(t["chosen"]) == {"graph", "wait_rounds", "wait_share", "rounds", "pcg_grid"}
+    assert set(t["chosen"]) == {"graph", "wait_rounds", "wait_share", "rounds", "pcg_grid", "slice_share", "slice_min"}
     for i, x in zip(insts, start):
         assert np.array_equal(i.positions(), x)
     # the tuned settings serve this mix now; results are those of the default settings
