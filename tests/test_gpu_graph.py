@@ -53,7 +53,7 @@ def test_graph_loop_equals_host_loop(gpu_ctx, defaults, prec):
 
 
 def test_launch_settings_change_no_result(gpu_ctx, defaults):
-    meshes = [M.batch_instance(3, i) for i in range(40, 46)]
+    meshes = [M.batch_instance(3, i) for i in range(40, 60)]  # more solves than clusters: time slices
     o = px.options(precision=px.PREC_FP32_REFINE, tol_rel=1e-6, tol_max_error=0.0, tol_min_impr=0.0,
                    tol_min_step=0.0)
     ref = _solve(gpu_ctx, meshes, o)

@@ -146,7 +146,9 @@ def test_cluster_time_slices_keep_the_bits(gpu_ctx):
     """Long cluster-PCG solves that leave their cluster at the end of a time slice (another
     solve of the launch has ended and half the clusters found nothing left) and resume in a
     later launch give the bits of the same instances solved alone, where no slice ends."""
-    idx = [38, 52, 399, 96]  # 196 nodes (short solves), then three with PCG solves of ~400 iterations
+    # six with PCG solves of 300-400 iterations, five small ones, nine others: 20 solves wait
+    # for the 15 clusters of the first launch
+    idx = [52, 399, 96, 217, 276, 86, 16, 38, 63, 71, 83] + list(range(100, 109))
     meshes = [M.batch_instance(3, i) for i in idx]
     o = px.options(precision=px.PREC_FP32_REFINE, tol_rel=1e-6, tol_max_error=0.0, tol_min_impr=0.0,
                    tol_min_step=0.0)
