@@ -167,7 +167,7 @@ struct phx_context_s {
   // engine writes for the cluster kernels
   int32_t* d_corder = nullptr;  // [cap]
   int32_t* d_wait = nullptr;    // [wait_size(cap)]
-  int32_t* d_cfg = nullptr;     // [4]: [0] PCG tile width (k_prep), [1] graph loop passes,
+  int32_t* d_cfg = nullptr;     // [4]: [0] unused, [1] graph loop passes,
                                 // [2] whole-GPU PCG iterations run by the graph
   int ccount = 0;               // instances of the batch whose PCG runs outside the engine
   int ckind_count[4] = {0, 0, 0, 0};  // ... of each PCG kind (1, 2: clusters, 3: whole-GPU kernels)
@@ -420,7 +420,6 @@ int set_batch(phx_context ctx, const std::vector<phx_instance>& list, BatchDev& 
   CU(cudaMemcpyAsync(ctx->d_flags, hdr, sizeof(hdr), cudaMemcpyHostToDevice, ctx->stream));
   B.phase_live = ctx->d_phc;
   B.algo_total = ctx->profiling ? ctx->d_algo : nullptr;
-  B.cpt = 4;
   B.cluster_mode = 0;
   const int sms = std::max(1, ctx->num_sms);
   G.tet = std::min(pt[num], sms * 8);
@@ -696,13 +695,12 @@ EngineArgs engine_args(phx_context ctx, const phx_launch_settings& S, int pcg_ch
 }
 
 // One cooperative launch of the engine: up to `rounds` Newton rounds over the batch.
-int run_engine(phx_context ctx, const BatchDev& B, int num, bool fp64, const phx_launch_settings& S, int pcg_chunk,
-               int max_chunks) {
+int run_engine(phx_context ctx, const BatchDev& B, int num, bool fp64, const phx_launch_settings& S, int pcg_chunk) {
   TRY(ensure_engine(ctx));
   int grid;
   TRY(engine_grid_of(ctx, fp64, &grid));
   const EngineArgs A = engine_args(ctx, S, pcg_chunk);
-  CU(launch_prep(ctx->stream, B, A, grid, max_chunks));
+  CU(launch_prep(ctx->stream, B, A, grid));
   cudaEvent_t a = nullptr, b = nullptr;
   if (ctx->profiling) TRY(profile_events(ctx, &a, &b));
   CU(launch_engine(fp64, grid, ctx->stream, B, A));
@@ -779,14 +777,13 @@ int run_gpcg(phx_context ctx, const BatchDev& B, const phx_launch_settings& S, i
 // faster than the grid-wide PCG both while many instances are active and in the tail);
 // the rest iterate on the whole GPU, with one-chunk tiles while few small instances
 // remain so that a lone instance spreads over more SMs.
-int run_step(phx_context ctx, const BatchDev& B0, int num, bool fp64, int pcg_chunk, int ccount, int active,
-             int max_chunks, const phx_launch_settings& S) {
+int run_step(phx_context ctx, const BatchDev& B0, int num, bool fp64, int pcg_chunk, int ccount,
+             const phx_launch_settings& S) {
   BatchDev B = B0;
-  (void)active;
   B.cluster_mode = ccount > 0 ? 1 : 0;
-  // (the engine takes its PCG tile width from k_prep: one-chunk tiles only while few, small
-  // instances remain, as a large one would pay for thousands of per-tile reductions)
-  TRY(run_engine(ctx, B, num, fp64, S, pcg_chunk, max_chunks));
+  // (each instance's PCG tile width is its own: one-chunk tiles for small instances, which
+  // then spread over many CTAs, four-chunk tiles for large ones)
+  TRY(run_engine(ctx, B, num, fp64, S, pcg_chunk));
   if (ctx->h_flags[2]) return set_err(PHX_ETIMEOUT, "cluster PCG reduction wait timed out");
   if (B.cluster_mode && ctx->h_flags[0] > 0 && ctx->h_flags[1] > 0) {
     cudaEvent_t a = nullptr, b = nullptr;
@@ -814,7 +811,7 @@ int run_step(phx_context ctx, const BatchDev& B0, int num, bool fp64, int pcg_ch
 // the host checks the outcome (and the time limit) between launches.
 constexpr int kGraphPasses = 256;
 
-int run_graph(phx_context ctx, const BatchDev& B0, int num, bool fp64, int pcg_chunk, int max_chunks,
+int run_graph(phx_context ctx, const BatchDev& B0, int num, bool fp64, int pcg_chunk,
               const phx_launch_settings& S, clk::time_point t0) {
   TRY(ensure_engine(ctx));
   int grid;
@@ -831,14 +828,14 @@ int run_graph(phx_context ctx, const BatchDev& B0, int num, bool fp64, int pcg_c
   std::string key;
   auto put = [&](const void* p, size_t n) { key.append(static_cast<const char*>(p), n); };
   put(&fp64, sizeof(fp64)); put(&grid, sizeof(grid)); put(&B, sizeof(B)); put(&A, sizeof(A));
-  put(&max_chunks, sizeof(max_chunks)); put(clusters, sizeof(clusters)); put(&gpcg, sizeof(gpcg));
+  put(clusters, sizeof(clusters)); put(&gpcg, sizeof(gpcg));
   if (!ctx->gexec || key != ctx->gkey) {
     if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
     if (ctx->graph) cudaGraphDestroy(ctx->graph);
     ctx->gexec = nullptr;
     ctx->graph = nullptr;
     ctx->gkey.clear();
-    CU(build_solve_graph(fp64, grid, B, A, max_chunks, clusters, gpcg, ctx->d_cfg + 1, kGraphPasses, &ctx->graph,
+    CU(build_solve_graph(fp64, grid, B, A, clusters, gpcg, ctx->d_cfg + 1, kGraphPasses, &ctx->graph,
                          &ctx->gexec));
     ctx->gkey = key;
   }
@@ -902,12 +899,11 @@ int run_to_completion(phx_context ctx, const std::vector<phx_instance>& list, bo
   TRY(set_cluster_list(ctx, list, &ccount));
   const int num = (int)list.size();
   const auto t0 = clk::now();
-  int active = num, max_chunks = 0;
-  for (auto* in : list) max_chunks = std::max(max_chunks, in->dev.nchunks);
+  int active = num;
   // per-launch timing events need the host between launches: profiling runs the host loop
-  if (S.graph && !ctx->profiling) return run_graph(ctx, B, num, fp64, pcg_chunk, max_chunks, S, t0);
+  if (S.graph && !ctx->profiling) return run_graph(ctx, B, num, fp64, pcg_chunk, S, t0);
   for (int64_t r = 0;; ++r) {
-    TRY(run_step(ctx, B, num, fp64, pcg_chunk, ccount, active, max_chunks, S));
+    TRY(run_step(ctx, B, num, fp64, pcg_chunk, ccount, S));
     active = ctx->h_flags[0];
     if (active == 0) return PHX_OK;
     if (std::chrono::duration<double>(clk::now() - t0).count() > kSolveTimeLimit)
@@ -2524,10 +2520,7 @@ int phx_server_progress(phx_server s, int32_t* active, int32_t* queued) {
       s->ctx->batch_owner = s;
       s->dirty = false;
     }
-    int max_chunks = 0;
-    for (auto& r : s->active) max_chunks = std::max(max_chunks, r.inst->dev.nchunks);
-    TRY(run_step(s->ctx, s->B, (int)s->active.size(), s->fp64, s->opts.pcg_chunk, s->ccount, (int)s->active.size(),
-                 max_chunks, s->ctx->launch));
+    TRY(run_step(s->ctx, s->B, (int)s->active.size(), s->fp64, s->opts.pcg_chunk, s->ccount, s->ctx->launch));
   }
   if (active) *active = (int32_t)s->active.size();
   if (queued) *queued = (int32_t)s->queue.size();

@@ -40,8 +40,15 @@ namespace phx {
 // small helpers
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ int tiles_of(int count) { return (count + kTile - 1) / kTile; }
-// PCG tiles: B.cpt SELL chunks (32 rows each) per tile
-__device__ __forceinline__ int pcg_tiles(const BatchDev& B, const InstDev& I) { return (I.nchunks + B.cpt - 1) / B.cpt; }
+// PCG tiles of an instance: one SELL chunk (32 rows) per tile up to kOneChunkTiles chunks, so
+// that a small instance iterating alone spreads over many CTAs; four chunks (128 rows, one per
+// thread) above.  The width is the instance's own, so its per-tile partial sums, and with them
+// its bits, do not depend on the batch it runs in.
+__device__ __forceinline__ int pcg_cpt(const InstDev& I) { return I.nchunks <= kOneChunkTiles ? 1 : 4; }
+__device__ __forceinline__ int pcg_tiles(const BatchDev&, const InstDev& I) {
+  const int cpt = pcg_cpt(I);
+  return (I.nchunks + cpt - 1) / cpt;
+}
 // true when this instance's PCG is left to the cluster kernel in this launch
 __device__ __forceinline__ bool cluster_owned(const BatchDev& B, const InstDev& I) {
   return B.cluster_mode && I.pcg_cluster;
@@ -1220,20 +1227,24 @@ __device__ __forceinline__ void st_pcg_a(const BatchDev& B, const TileMap& M, in
       Real* pnew = par ? PcgBufs<Real>::pa(I) : PcgBufs<Real>::pb(I);
       const Real* z = PcgBufs<Real>::z(I);
       const Real beta = (Real)st->beta, sh = (Real)st->shift;
-      const int sub = threadIdx.x & 3, row = threadIdx.x >> 2;  // 32 rows x 4 lanes per pass
-      const int ch0 = lt * B.cpt, ch1 = min(ch0 + B.cpt, I.nchunks);
-      for (int ch = ch0; ch < ch1; ++ch) {
+      auto getx = [&](int col, Real (&xc)[3]) {
+        Real zc[3], pc[3];
+        ld4(z, col, zc);
+        ld4(pold, col, pc);
+        for (int a = 0; a < 3; ++a) xc[a] = zc[a] + beta * pc[a];
+      };
+      // one-chunk tiles: 32 rows x 4 lanes; four-chunk tiles: one row per thread, so that a
+      // warp's load of a block plane is one 128-byte line of the slot-row (the wide form
+      // spreads it over four lines, and the whole-GPU SpMV is bound by L2 requests)
+      const bool wide = pcg_cpt(I) == 1;
+      const int sub = wide ? (threadIdx.x & 3) : 0, row = wide ? (threadIdx.x >> 2) : threadIdx.x;
+      const int ch0 = wide ? lt : 4 * lt, ch1 = wide ? ch0 + 1 : min(ch0 + 4, I.nchunks);
+      for (int ch = ch0; ch < ch1; ch += wide ? 1 : 4) {
         const int v = ch * 32 + row;
         const bool valid = v < I.n;
         Real acc[3];
-        sell_row_quad<Real, Real>(I, PcgBufs<Real>::H(I), v, sub, valid,
-                                  [&](int col, Real (&xc)[3]) {
-                                    Real zc[3], pc[3];
-                                    ld4(z, col, zc);
-                                    ld4(pold, col, pc);
-                                    for (int a = 0; a < 3; ++a) xc[a] = zc[a] + beta * pc[a];
-                                  },
-                                  acc);
+        if (wide) sell_row_quad<Real, Real>(I, PcgBufs<Real>::H(I), v, sub, valid, getx, acc);
+        else sell_row_lanes<1, Real, Real>(I, PcgBufs<Real>::H(I), v, 0, valid, getx, acc);
         if (valid && sub == 0) {
           Real zv[3], pv[3];
           ld4(z, v, zv);
@@ -1287,9 +1298,10 @@ __device__ __forceinline__ void st_pcg_b(const BatchDev& B, const TileMap& M, in
     std::conditional_t<kGrid, const InstDev&, const InstDev> I = B.inst[i];  // the engine keeps a copy in registers
     NState* st = I.st;
     if (st->phase != PH_PCG || !pcg_here<Real, kGrid>(B, I)) continue;
-    const int v = lt * B.cpt * 32 + threadIdx.x;  // one row per thread over the tile's chunks
+    const int cpt = pcg_cpt(I);
+    const int v = lt * cpt * 32 + threadIdx.x;  // one row per thread over the tile's chunks
     Real p[2] = {(Real)0, (Real)0};  // per-tile inner products in the PCG's own precision
-    if ((int)threadIdx.x < B.cpt * 32 && v < I.n) {
+    if ((int)threadIdx.x < cpt * 32 && v < I.n) {
       const Real alpha = (Real)st->alpha;
       const Real* pc = st->pcg_parity ? PcgBufs<Real>::pa(I) : PcgBufs<Real>::pb(I);
       Real pv[3], qv[3], ev[3], rv[3], z[3];
@@ -1598,7 +1610,6 @@ __global__ void __launch_bounds__(kTile, (sizeof(Real) == 4 ? 3 : 2)) k_engine(B
   __shared__ double sm[32 * 5];
   __shared__ int flag;
   const int cta = blockIdx.x;
-  if (A.cfg) B.cpt = __ldcg(A.cfg);  // written by k_prep before the launch, the same for every CTA
   int* ids = A.act + 4;
   int* pt = ids + A.cap;
   int* pn = pt + A.cap + 1;
@@ -2693,16 +2704,12 @@ int engine_grid(bool fp64, int num_sms) {
   return nb * num_sms;
 }
 
-// Before an engine launch (one thread): both grid barriers cleared, the round's CTA count, and
-// the PCG tile width for the launch from the active count the previous launch left in
-// flags[0] (set_batch puts the batch size there first).
-__global__ void k_prep(BatchDev B, EngineArgs A, int grid, int max_chunks) {
+// Before an engine launch (one thread): both grid barriers cleared and the round's CTA count.
+__global__ void k_prep(BatchDev B, EngineArgs A, int grid) {
   if (threadIdx.x != 0) return;
   for (int k = 0; k < 2; ++k) A.bar[k] = GridBar{0u, 0u, 0, 0};
   A.act[0] = 0;
   A.act[1] = grid;
-  const int active = B.flags[0];
-  *A.cfg = (active <= kClWideBelow && max_chunks <= 2048) ? 1 : 4;
 }
 
 // End of one pass of the graph's solve loop (one thread): go on while instances are active and
@@ -2714,8 +2721,8 @@ __global__ void k_loop_end(BatchDev B, EngineArgs A, cudaGraphConditionalHandle 
   cudaGraphSetConditional(h, (!failed && B.flags[0] > 0 && pass < loop_cap) ? 1u : 0u);
 }
 
-cudaError_t launch_prep(cudaStream_t s, const BatchDev& B, const EngineArgs& A, int grid, int max_chunks) {
-  k_prep<<<1, 32, 0, s>>>(B, A, grid, max_chunks);
+cudaError_t launch_prep(cudaStream_t s, const BatchDev& B, const EngineArgs& A, int grid) {
+  k_prep<<<1, 32, 0, s>>>(B, A, grid);
   return cudaGetLastError();
 }
 
@@ -2765,14 +2772,12 @@ __device__ __forceinline__ TileMap gpcg_map(const EngineArgs& A) {
 __global__ void __launch_bounds__(kTile, kGpcgBlocks) k_gpcg_a(BatchDev B, EngineArgs A) {
   __shared__ double sm[32 * 5];
   __shared__ int flag;
-  B.cpt = __ldcg(A.cfg);
   st_pcg_a<float, true>(B, gpcg_map(A), blockIdx.x, gridDim.x, sm, flag, A.wait + kWaitLeft);
 }
 
 __global__ void __launch_bounds__(kTile, kGpcgBlocks) k_gpcg_b(BatchDev B, EngineArgs A) {
   __shared__ double sm[32 * 5];
   __shared__ int flag;
-  B.cpt = __ldcg(A.cfg);
   st_pcg_b<float, true>(B, gpcg_map(A), blockIdx.x, gridDim.x, sm, flag, A.wait + kWaitLeft);
 }
 
@@ -2840,7 +2845,7 @@ cudaError_t add_kernel(cudaGraph_t g, cudaGraphNode_t* node, cudaGraphNode_t* de
 }
 }  // namespace
 
-cudaError_t build_solve_graph(bool fp64, int grid, const BatchDev& B, const EngineArgs& A, int max_chunks,
+cudaError_t build_solve_graph(bool fp64, int grid, const BatchDev& B, const EngineArgs& A,
                               const int clusters[2], int gpcg, int32_t* loops, int loop_cap, cudaGraph_t* graph,
                               cudaGraphExec_t* exec) {
   *graph = nullptr;
@@ -2862,12 +2867,12 @@ cudaError_t build_solve_graph(bool fp64, int grid, const BatchDev& B, const Engi
   // kernel arguments are copied when the nodes are added
   BatchDev b = B;
   EngineArgs a = A;
-  int gr = grid, mc = max_chunks, cap = loop_cap;
+  int gr = grid, cap = loop_cap;
   int32_t* lp = loops;
   cudaGraphNode_t prev = nullptr, node = nullptr;
   if (e == cudaSuccess) {
     cudaGraph_t body = cp.conditional.phGraph_out[0];
-    void* pa[] = {&b, &a, &gr, &mc};
+    void* pa[] = {&b, &a, &gr};
     e = add_kernel(body, &node, nullptr, (const void*)k_prep, dim3(1), dim3(32), 0, pa);
     prev = node;
     if (e == cudaSuccess) {

@@ -48,7 +48,7 @@ struct EngineArgs {
   long long wait_limit;  // SM cycles a grid-barrier wait lasts before it gives up
   int unmet_tag;         // test hook: the grid barrier with this tag waits for one arrival more than
                          // the CTAs taking part, so it gives up (0: none)
-  int32_t* cfg;          // [1] PCG tile width in chunks for this launch (set by k_prep, read only here)
+  int32_t* cfg;          // [4]: [1] graph loop passes, [2] iterations of the graph's kind-3 PCG loops
   const int32_t* corder; // [ccount] batch positions of the cluster-PCG instances, largest first
   int ccount;
   int32_t* wait;         // [wait_size(cap)]: instances waiting for the cluster and grid PCG kernels
@@ -67,9 +67,8 @@ constexpr long long kBarrierLimit = 4000000000LL;  // default wait_limit: about 
 cudaError_t setup_kernel_attributes();
 int engine_grid(bool fp64, int num_sms);
 cudaError_t launch_engine(bool fp64, int grid, cudaStream_t s, const BatchDev& B, const EngineArgs& A);
-// Before each engine launch: barrier state cleared, the round's CTA count, the PCG tile width
-// from the active count the last launch left (one-chunk tiles while few, small instances remain)
-cudaError_t launch_prep(cudaStream_t s, const BatchDev& B, const EngineArgs& A, int grid, int max_chunks);
+// Before each engine launch: barrier state cleared and the round's CTA count
+cudaError_t launch_prep(cudaStream_t s, const BatchDev& B, const EngineArgs& A, int grid);
 // PCG of the instances the engine listed as waiting for PCG kind `kind` (1: rows in shared
 // memory, 2: rows in L2): `clusters` clusters take them in list order until none is left
 cudaError_t launch_pcg_cluster(cudaStream_t s, const BatchDev& B, int32_t* wait, int cap, int clusters, int kind,
@@ -89,7 +88,7 @@ cudaError_t launch_gpcg(cudaStream_t s, const BatchDev& B, const EngineArgs& A, 
 // up, or loop_cap passes) and counts the passes in loops[0].
 // gpcg > 0 adds the kind-3 loop (k_gpcg_begin, then while instances iterate: k_gpcg_a,
 // k_gpcg_b, k_gpcg_loop) with gpcg CTAs per kernel.
-cudaError_t build_solve_graph(bool fp64, int grid, const BatchDev& B, const EngineArgs& A, int max_chunks,
+cudaError_t build_solve_graph(bool fp64, int grid, const BatchDev& B, const EngineArgs& A,
                               const int clusters[2], int gpcg, int32_t* loops, int loop_cap, cudaGraph_t* graph,
                               cudaGraphExec_t* exec);
 // One stage as its own kernel, for the evaluation entry points: K_ELEM_EG, K_GATHER,

@@ -29,7 +29,7 @@ constexpr int kChunk = 32;       // SELL chunk height (one warp)
 constexpr int kPartials = 8;     // doubles reduced per tile (at most)
 constexpr int kCl = 8;           // CTAs per cluster of the cluster PCG
 constexpr int kClThreads = 512;  // threads per CTA of the cluster PCG
-constexpr int kClWideBelow = 32;     // at most this many active instances: one-chunk PCG tiles in the engine
+constexpr int kOneChunkTiles = 608;  // instances up to this many SELL chunks take one-chunk PCG tiles (else four)
 constexpr int kClusterMaxNodes = 13000;  // instances up to this size solve their PCG in one cluster
 constexpr int kWaitRounds = 4;           // engine rounds an instance may wait for the cluster kernel
 constexpr int kWaitShare = 2;            // ... or until 1/kWaitShare of the active instances wait
@@ -191,7 +191,6 @@ struct BatchDev {
   double* algo_total;         // [16] algorithmic bytes summed per kernel kind, or null
   int32_t* phase_live;        // [32] active instances per phase bucket: [0..15] kept current by
                               // advance(), [16..31] the copy taken at the last grid barrier, or null
-  int32_t cpt;                // SELL chunks per PCG tile in the engine (set per launch)
   int32_t cluster_mode;       // 1: instances with pcg_cluster leave their PCG to k_pcg_cluster
 };
 

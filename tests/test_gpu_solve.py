@@ -142,6 +142,22 @@ def test_batch_equals_alone_bitwise(gpu_ctx):
         assert ra["obj"] == rb["obj"]
 
 
+def test_engine_pcg_batch_equals_alone_bitwise(gpu_ctx):
+    """Instances whose PCG runs in the engine (the FP64 path) get the same bits alone and in a
+    batch of 40: their PCG tile width, and with it the order of the per-tile partial sums, is
+    the instance's own, whatever the number of active instances."""
+    meshes = [M.batch_instance(3, i) for i in range(200, 240)]
+    o = px.options(precision=px.PREC_FP64, tol_rel=1e-6, tol_max_error=0.0, tol_min_impr=0.0, tol_min_step=0.0)
+    insts = [px.Instance(gpu_ctx, m) for m in meshes]
+    reps, xs = gpu_ctx.batch_solve(insts, o, [m.X0.ravel().copy() for m in meshes])
+    for k in (0, 17, 39):
+        inst = px.Instance(gpu_ctx, meshes[k])
+        xa, ra = inst.solve_static(o, meshes[k].X0.ravel())
+        assert np.array_equal(xa, xs[k])
+        assert ra["iterations"] == reps[k]["iterations"] and ra["pcg_iterations"] == reps[k]["pcg_iterations"]
+        assert ra["obj"] == reps[k]["obj"]
+
+
 def test_cluster_time_slices_keep_the_bits(gpu_ctx):
     """Long cluster-PCG solves that leave their cluster at the end of a time slice (another
     solve of the launch has ended and half the clusters found nothing left) and resume in a
