@@ -2759,9 +2759,9 @@ cudaError_t launch_pcg_cluster(cudaStream_t s, const BatchDev& B, int32_t* wait,
 // ---------------------------------------------------------------------------
 // The engine's two PCG stages as kernels of their own, so that they run at the occupancy of
 // a small kernel (the engine holds 12 warps per SM) and the kernel boundary is the grid-wide
-// synchronisation.  Tiles, partial sums and decisions are the engine's (same tile width from
-// k_prep, per-tile partials summed in tile order), so an instance gets the bits it gets when
-// the engine iterates its PCG.
+// synchronisation.  Tiles, partial sums and decisions are the engine's (the instance's own
+// tile width, per-tile partials summed in tile order), so an instance gets the bits it gets
+// when the engine iterates its PCG.
 constexpr int kGpcgBlocks = 6;  // resident CTAs per SM the whole-GPU PCG kernels are built for (24 warps)
 
 __device__ __forceinline__ TileMap gpcg_map(const EngineArgs& A) {
