@@ -441,6 +441,30 @@ def run_batch(args, world, rank, dist):
     ctx.mark(3)
     served_sample_ms = ctx.elapsed_ms(2, 3)
     plain_value = len(pick) / plain_s
+    # the plain FP64 path batched through the same engine (its PCG in the engine's stages: the
+    # cluster PCG is FP32 only), on the same sample and on the whole batch: what the FP32 +
+    # refinement path buys at equal batching
+    for i in pick:
+        insts[i].reset()
+    ctx.mark(2)
+    plain_b_sample = ctx.batch_solve([insts[i] for i in pick], plain)[0]
+    ctx.mark(3)
+    plain_b_sample_ms = ctx.elapsed_ms(2, 3)
+    plain_batched = {"sample": {"value": round(len(pick) / (plain_b_sample_ms / 1e3), 3), "unit": "solves/s",
+                                "instances": len(pick),
+                                "non_success": sum(r["result_name"] != "SUCCESS" for r in plain_b_sample)}}
+    if not args.no_plain_batch:
+        for it in insts:
+            it.reset()
+        ctx.mark(2)
+        plain_b_all = ctx.batch_solve(insts, plain)[0]
+        ctx.mark(3)
+        plain_b_all_ms = ctx.elapsed_ms(2, 3)
+        plain_batched["all"] = {"value": round(count / (plain_b_all_ms / 1e3), 3), "unit": "solves/s",
+                                "instances": count, "ms": round(plain_b_all_ms, 1),
+                                "non_success": sum(r["result_name"] != "SUCCESS" for r in plain_b_all),
+                                "served_over_plain_batched": round(value / (count / (plain_b_all_ms / 1e3)), 2)}
+    plain_batched["served_over_plain_batched_sample"] = round(plain_b_sample_ms / served_sample_ms, 2)
 
     out = {
         "metric": "static solves/s @1e-6 rel residual: served batched FP32+refine (value) vs plain FP64 GPU drop-in",
@@ -459,6 +483,7 @@ def run_batch(args, world, rank, dist):
                       "served_same_sample": round(len(pick) / (served_sample_ms / 1e3), 3),
                       "ratio_served_over_plain": round((len(pick) / (served_sample_ms / 1e3)) / plain_value, 2),
                       "results": sorted(set(r["result_name"] for r in plain_reps))},
+        "plain_gpu_batched": plain_batched,
         "elements_per_s": round(sum(r["hessian_evals"] * m.m for r, m in zip(reps, meshes)) * args.steps /
                                 (eh["ms"] / 1e3), 1) if eh["ms"] > 0 else None,
         "elem_hess": {"launches": eh["launches"], "ms": round(eh["ms"], 3)},
@@ -985,6 +1010,8 @@ def main():
                     help="PCG iterations per Newton step of the plain FP64 path (the served path's budget is "
                          "served_sweeps x served_pcg_max = 4 x 3000)")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-plain-batch", action="store_true",
+                    help="skip the plain FP64 solve of the whole batch through the batched engine (about 11 s)")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0, help="serving admission budget (device bytes)")
     ap.add_argument("--serve-arena-gb", type=float, default=160.0, help="device arena of the serving context")
     ap.add_argument("--count", type=int, default=512)
