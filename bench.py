@@ -519,7 +519,7 @@ def run_batch(args, world, rank, dist):
         both_failed = 0
         for j, i in enumerate(cpu_pick[:done]):
             x0 = meshes[i].X0.ravel()
-            xg = insts[i].positions()
+            xg = final_x[i]  # the served result (the instances were solved again in FP64 since)
             xr, rr = sols[j]
             if rr["result_name"] != "SUCCESS" or reps[i]["result_name"] != "SUCCESS":
                 both_failed += rr["result_name"] != "SUCCESS" and reps[i]["result_name"] != "SUCCESS"
